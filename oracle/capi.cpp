@@ -1,0 +1,260 @@
+// capi.cpp -- flat C entry points of the oracle for the Python test harness
+// (ctypes).  TEST INFRASTRUCTURE ONLY: never linked into the product.
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <set>
+
+#include "oracle.hpp"
+
+using namespace orc;
+
+namespace {
+struct MatSpec {
+  const char* name;
+  double density, I;
+  int n;
+  const double *Z, *A, *Iel, *frac;
+};
+BaseMaterial to_material(const char* name, double density, double I, int n, const double* Z,
+                         const double* A, const double* Iel, const double* frac) {
+  std::vector<Element> els;
+  std::vector<double> fr;
+  for (int i = 0; i < n; ++i) {
+    els.push_back({"e", Z[i], A[i], Iel[i]});
+    fr.push_back(frac[i]);
+  }
+  return make_material(name, density, I, els, fr);
+}
+std::vector<double>* column(MaterialTable& t, int c) {
+  switch (c) {
+    case 0: return &t.E;
+    case 1: return &t.logE;
+    case 2: return &t.csda_S;
+    case 3: return &t.csda_R;
+    case 4: return &t.csda_T;
+    case 5: return &t.mixed_S;
+    case 6: return &t.mixed_R;
+    case 7: return &t.strag;
+    case 8: return &t.ion;
+    case 9: return &t.brems;
+    case 10: return &t.pair;
+    case 11: return &t.photo;
+    case 12: return &t.xs;
+    case 13: return &t.lb1;
+    case 14: return &t.lbe;
+    case 15: return &t.elastic_cutoff;
+    case 16: return &t.magrot;
+    case 17: return &t.mu0;
+    case 18: return &t.fspin;
+  }
+  return nullptr;
+}
+}  // namespace
+
+extern "C" {
+
+// Physics handle: empty, then materials are appended in order.
+void* orc_physics_new(double mass, double ctau, double cutoff, double elastic_ratio) {
+  Physics* p = new Physics;
+  p->mass = mass;
+  p->ctau = ctau;
+  p->cutoff = cutoff;
+  p->elastic_ratio = elastic_ratio;
+  return p;
+}
+void orc_physics_free(void* h) { delete static_cast<Physics*>(h); }
+
+// Empirical table (src/Physics.jl:280) on a log grid of n nodes.
+int orc_add_material_empirical(void* h, const char* name, double density, double I, int n_el,
+                               const double* Z, const double* A, const double* Iel,
+                               const double* frac, int n_energies, double Kmin, double Kmax,
+                               int coulomb) {
+  Physics* p = static_cast<Physics*>(h);
+  std::vector<double> E(n_energies);
+  for (int i = 0; i < n_energies; ++i)
+    E[i] = Kmin * std::pow(Kmax / Kmin, double(i) / double(n_energies - 1));
+  p->t.push_back(build_table_empirical(to_material(name, density, I, n_el, Z, A, Iel, frac),
+                                       p->mass, E, p->cutoff, p->elastic_ratio, coulomb != 0));
+  return int(p->t.size()) - 1;
+}
+
+// dE/dx-file table (src/Physics.jl:146).
+int orc_add_material_dedx(void* h, const char* path, const char* name, double density, double I,
+                          int n_el, const double* Z, const double* A, const double* Iel,
+                          const double* frac, int coulomb) {
+  Physics* p = static_cast<Physics*>(h);
+  DedxData d = load_dedx(path);
+  p->t.push_back(build_table_from_dedx(d, to_material(name, density, I, n_el, Z, A, Iel, frac),
+                                       p->mass, p->cutoff, p->elastic_ratio, coulomb != 0));
+  return int(p->t.size()) - 1;
+}
+
+// Caller-supplied columns (tests overwrite tables with analytic values).
+int orc_add_material_columns(void* h, const char* name, double density, double ZoA, int n,
+                             const double* const* cols /* 19 columns, see column() */) {
+  Physics* p = static_cast<Physics*>(h);
+  MaterialTable t;
+  t.name = name;
+  t.density = density;
+  t.ZoA = ZoA;
+  for (int c = 0; c < 19; ++c) column(t, c)->assign(cols[c], cols[c] + n);
+  p->t.push_back(t);
+  return int(p->t.size()) - 1;
+}
+
+int orc_table_size(void* h, int mat) { return int(static_cast<Physics*>(h)->t[mat].E.size()); }
+int orc_table_column(void* h, int mat, int col, double* out) {
+  auto* v = column(static_cast<Physics*>(h)->t[mat], col);
+  if (!v) return -1;
+  std::copy(v->begin(), v->end(), out);
+  return int(v->size());
+}
+
+double orc_dcs(int proc, double Z, double A, double I, double m, double K, double q) {
+  switch (proc) {
+    case BREMS: return dcs_bremsstrahlung_ssr(Z, A, m, K, q);
+    case PAIR: return dcs_pair_production_ssr(Z, A, m, K, q);
+    case PHOTO: return dcs_photonuclear_drss(Z, A, m, K, q);
+    default: return electronic_dcs(Z, I, m, K, q);
+  }
+}
+double orc_dcs_integral(int proc, double Z, double A, double I, double mass, double K,
+                        double xlo, double xhi, int mode, int npoints) {
+  return compute_dcs_integral(proc, Z, A, I, mass, K, xlo, xhi, mode, npoints);
+}
+double orc_dilog(double x) { return math_dilog(x); }
+double orc_flux_gccly(double c, double K, double q) { return flux_gccly(c, K, q); }
+double orc_electronic_stopping(const char* name, double density, double I, int n_el,
+                               const double* Z, const double* A, const double* Iel,
+                               const double* frac, double mass, double K) {
+  return electronic_stopping_power(to_material(name, density, I, n_el, Z, A, Iel, frac), mass, K);
+}
+
+// Interpolated property lookups (src/Physics.jl:783-905).
+double orc_lookup(void* h, int mat, int col, double K) {
+  MaterialTable& t = static_cast<Physics*>(h)->t[mat];
+  return interp_plain(K, t.E, t.logE, *column(t, col));
+}
+double orc_csda_energy(void* h, int mat, double X) {
+  MaterialTable& t = static_cast<Physics*>(h)->t[mat];
+  return csda_energy<double>(t, X);
+}
+
+// One deterministic CSDA history (compute_flux_single with rng = nothing) and
+// its density derivative (dual numbers through the discrete program).
+void orc_flux_single_csda(void* h, int rock, int air, double thickness, double rho,
+                          double elevation, double energy, double charge, double threshold,
+                          double primary_altitude, double* flux, double* dflux, long* steps) {
+  Physics* p = static_cast<Physics*>(h);
+  TwoLayer g{thickness, primary_altitude, rock, air};
+  Dual r = flux_single_csda<Dual>(*p, g, Dual(rho, 1.0), elevation, energy, charge, threshold,
+                                  steps);
+  *flux = r.v;
+  *dflux = r.d;
+}
+
+// Batch of histories (run_backward_mc CSDA path with recorded samples):
+// per-sample contribution w_i*f_i and its density derivative.
+void orc_backward_mc_csda(void* h, int rock, int air, double thickness, double rho,
+                          double elevation, double threshold, double primary_altitude, long n,
+                          const double* E, const double* q, const double* w, double* contrib,
+                          double* dcontrib, int nthreads) {
+  Physics* p = static_cast<Physics*>(h);
+  TwoLayer g{thickness, primary_altitude, rock, air};
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
+  for (long i = 0; i < n; ++i) {
+    Dual r = flux_single_csda<Dual>(*p, g, Dual(rho, 1.0), elevation, E[i], q[i], threshold,
+                                    nullptr);
+    contrib[i] = w[i] * r.v;
+    dcontrib[i] = w[i] * r.d;
+  }
+}
+
+void orc_flux_csda_direct(void* h, int rock, int air, double rho, double thickness,
+                          double elevation, double energy, double charge, double H,
+                          double* flux, double* dflux) {
+  Physics* p = static_cast<Physics*>(h);
+  Dual r = flux_csda_direct<Dual>(*p, rock, air, Dual(rho, 1.0), thickness, elevation, energy,
+                                  charge, H);
+  *flux = r.v;
+  *dflux = r.d;
+}
+
+// Ray trace of one ray: returns segment count (<= cap), cells, lengths, z_exit.
+int orc_trace_ray(const int* dims, const double* geom /* x0 y0 z0 dx dy dz */,
+                  const double* ray /* ox oy oz ux uy uz cos */, int cap, int* cells,
+                  double* lens, double* z_exit) {
+  Grid g{dims[0], dims[1], dims[2], geom[0], geom[1], geom[2], geom[3], geom[4], geom[5]};
+  Ray r{ray[0], ray[1], ray[2], ray[3], ray[4], ray[5], ray[6]};
+  RayTrace tr = trace_ray(g, r);
+  int n = std::min<int>(cap, int(tr.seg.size()));
+  for (int i = 0; i < n; ++i) {
+    cells[i] = tr.seg[i].cell;
+    lens[i] = tr.seg[i].len;
+  }
+  *z_exit = tr.z_exit;
+  return int(tr.seg.size());
+}
+
+// Tomography forward for many rays: flux_r = (1/N) sum_n 2 w_n f(E_n, q_n).
+void orc_tomo_forward(void* h, int rock, int air, const int* dims, const double* geom,
+                      const double* rho, double rho_side, double H, long n_rays,
+                      const double* rays /* 7 per ray */, int n_nodes, const double* nE,
+                      const double* nq, const double* nw, double* flux, int nthreads) {
+  Physics* p = static_cast<Physics*>(h);
+  Grid g{dims[0], dims[1], dims[2], geom[0], geom[1], geom[2], geom[3], geom[4], geom[5]};
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads)
+  for (long r = 0; r < n_rays; ++r) {
+    const double* q = rays + 7 * r;
+    Ray ray{q[0], q[1], q[2], q[3], q[4], q[5], q[6]};
+    RayTrace tr = trace_ray(g, ray);
+    double s = 0;
+    for (int k = 0; k < n_nodes; ++k)
+      s += 2.0 * nw[k] *
+           tomo_flux_node<double>(*p, rock, air, g, tr, q[6], rho, rho_side, -1, nE[k], nq[k], H);
+    flux[r] = s / n_nodes;
+  }
+}
+
+// One ray's flux and its density derivative for every cell it touches
+// (forward-mode: one dual pass per touched cell, plus the side density).
+// Returns the number of touched cells (written up to cap), in first-touch order.
+int orc_tomo_ray_grad(void* h, int rock, int air, const int* dims, const double* geom,
+                      const double* rho, double rho_side, double H, const double* q, int n_nodes,
+                      const double* nE, const double* nq, const double* nw, double* flux,
+                      int cap, int* cells, double* grads, double* dside) {
+  Physics* p = static_cast<Physics*>(h);
+  Grid g{dims[0], dims[1], dims[2], geom[0], geom[1], geom[2], geom[3], geom[4], geom[5]};
+  Ray ray{q[0], q[1], q[2], q[3], q[4], q[5], q[6]};
+  RayTrace tr = trace_ray(g, ray);
+  std::vector<int> uniq;
+  std::set<int> seen;
+  for (auto& s : tr.seg)
+    if (seen.insert(s.cell).second) uniq.push_back(s.cell);
+  double f = 0;
+  for (int k = 0; k < n_nodes; ++k)
+    f += 2.0 * nw[k] *
+         tomo_flux_node<double>(*p, rock, air, g, tr, q[6], rho, rho_side, -1, nE[k], nq[k], H);
+  *flux = f / n_nodes;
+  int m = int(uniq.size());
+  for (int u = 0; u <= m; ++u) {
+    int seed = u < m ? uniq[u] : -2;
+    double d = 0;
+    for (int k = 0; k < n_nodes; ++k)
+      d += 2.0 * nw[k] *
+           tomo_flux_node<Dual>(*p, rock, air, g, tr, q[6], rho, rho_side, seed, nE[k], nq[k], H).d;
+    d /= n_nodes;
+    if (u < m) {
+      if (u < cap) {
+        cells[u] = seed;
+        grads[u] = d;
+      }
+    } else {
+      *dside = d;
+    }
+  }
+  return m;
+}
+
+}  // extern "C"

@@ -1,0 +1,244 @@
+"""ctypes binding of the FP64 oracle (oracle/_build/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py.  The product (diffpumas.jl_gb300) never imports it.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+_D = C.c_double
+_I = C.c_int
+_L = C.c_long
+_P = C.c_void_p
+_DP = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_IP = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+MUON_MASS = 0.10565839
+MUON_C_TAU = 658.654
+
+# Column ids of a material table (oracle/capi.cpp column()).
+COLUMNS = ["E", "logE", "csda_S", "csda_R", "csda_T", "mixed_S", "mixed_R", "strag",
+           "ion", "brems", "pair", "photo", "xs", "lb1", "lbe", "elastic_cutoff",
+           "magrot", "mu0", "fspin"]
+BREMS, PAIR, PHOTO, IONI = 0, 1, 2, 3
+
+
+def build():
+    import subprocess
+    subprocess.check_call(["make", "-s", "-C", HERE])
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        L.orc_physics_new.restype = _P
+        L.orc_physics_new.argtypes = [_D, _D, _D, _D]
+        L.orc_physics_free.argtypes = [_P]
+        L.orc_add_material_empirical.restype = _I
+        L.orc_add_material_empirical.argtypes = [_P, C.c_char_p, _D, _D, _I, _DP, _DP, _DP, _DP,
+                                                 _I, _D, _D, _I]
+        L.orc_add_material_dedx.restype = _I
+        L.orc_add_material_dedx.argtypes = [_P, C.c_char_p, C.c_char_p, _D, _D, _I, _DP, _DP,
+                                            _DP, _DP, _I]
+        L.orc_add_material_columns.restype = _I
+        L.orc_add_material_columns.argtypes = [_P, C.c_char_p, _D, _D, _I, C.POINTER(C.POINTER(_D))]
+        L.orc_table_size.restype = _I
+        L.orc_table_size.argtypes = [_P, _I]
+        L.orc_table_column.restype = _I
+        L.orc_table_column.argtypes = [_P, _I, _I, _DP]
+        L.orc_dcs.restype = _D
+        L.orc_dcs.argtypes = [_I, _D, _D, _D, _D, _D, _D]
+        L.orc_dcs_integral.restype = _D
+        L.orc_dcs_integral.argtypes = [_I, _D, _D, _D, _D, _D, _D, _D, _I, _I]
+        L.orc_dilog.restype = _D
+        L.orc_dilog.argtypes = [_D]
+        L.orc_flux_gccly.restype = _D
+        L.orc_flux_gccly.argtypes = [_D, _D, _D]
+        L.orc_electronic_stopping.restype = _D
+        L.orc_electronic_stopping.argtypes = [C.c_char_p, _D, _D, _I, _DP, _DP, _DP, _DP, _D, _D]
+        L.orc_lookup.restype = _D
+        L.orc_lookup.argtypes = [_P, _I, _I, _D]
+        L.orc_csda_energy.restype = _D
+        L.orc_csda_energy.argtypes = [_P, _I, _D]
+        L.orc_flux_single_csda.argtypes = [_P, _I, _I, _D, _D, _D, _D, _D, _D, _D,
+                                           C.POINTER(_D), C.POINTER(_D), C.POINTER(_L)]
+        L.orc_backward_mc_csda.argtypes = [_P, _I, _I, _D, _D, _D, _D, _D, _L, _DP, _DP, _DP,
+                                           _DP, _DP, _I]
+        L.orc_flux_csda_direct.argtypes = [_P, _I, _I, _D, _D, _D, _D, _D, _D,
+                                           C.POINTER(_D), C.POINTER(_D)]
+        L.orc_trace_ray.restype = _I
+        L.orc_trace_ray.argtypes = [_IP, _DP, _DP, _I, _IP, _DP, C.POINTER(_D)]
+        L.orc_tomo_forward.argtypes = [_P, _I, _I, _IP, _DP, _DP, _D, _D, _L, _DP, _I, _DP, _DP,
+                                       _DP, _DP, _I]
+        L.orc_tomo_ray_grad.restype = _I
+        L.orc_tomo_ray_grad.argtypes = [_P, _I, _I, _IP, _DP, _DP, _D, _D, _DP, _I, _DP, _DP,
+                                        _DP, C.POINTER(_D), _I, _IP, _DP, C.POINTER(_D)]
+        _lib = L
+    return _lib
+
+
+def _arr(x):
+    return np.ascontiguousarray(x, dtype=np.float64)
+
+
+class Material:
+    """Elemental recipe (src/Materials.jl BaseMaterial)."""
+
+    def __init__(self, name, density, I, elements):
+        self.name, self.density, self.I = name, float(density), float(I)
+        self.Z = _arr([e[0] for e in elements])
+        self.A = _arr([e[1] for e in elements])
+        self.Iel = _arr([e[2] for e in elements])
+        self.frac = _arr([e[3] for e in elements])
+
+
+# src/Materials.jl:35-127 built-in recipes
+_EL = {"H": (1.0, 1.00794, 19.2e-9), "C": (6.0, 12.0107, 78.0e-9), "N": (7.0, 14.0067, 82.0e-9),
+       "O": (8.0, 15.9994, 95.0e-9), "Na": (11.0, 22.9898, 149.0e-9),
+       "Mg": (12.0, 24.305, 156.0e-9), "Al": (13.0, 26.9815, 166.0e-9),
+       "Si": (14.0, 28.0855, 173.0e-9), "K": (19.0, 39.0983, 190.0e-9),
+       "Ca": (20.0, 40.078, 191.0e-9), "Fe": (26.0, 55.845, 286.0e-9),
+       "Ar": (18.0, 39.948, 188.0e-9)}
+
+
+def _mk(name, density, I, comp):
+    return Material(name, density, I, [(*_EL[s], f) for s, f in comp])
+
+
+STANDARD_ROCK = _mk("StandardRock", 2650.0, 136.4e-9,
+                    [("O", 0.466), ("Si", 0.277), ("Al", 0.081), ("Fe", 0.050), ("Ca", 0.036),
+                     ("Na", 0.028), ("Mg", 0.021), ("K", 0.026)])
+AIR = _mk("Air", 1.205, 85.7e-9, [("N", 0.755), ("O", 0.232), ("Ar", 0.013)])
+WATER = _mk("Water", 1000.0, 75.0e-9, [("H", 0.1119), ("O", 0.8881)])
+
+
+class Physics:
+    def __init__(self, mass=MUON_MASS, ctau=MUON_C_TAU, cutoff=0.05, elastic_ratio=0.05):
+        self.h = lib().orc_physics_new(mass, ctau, cutoff, elastic_ratio)
+        self.names = []
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_physics_free(self.h)
+            self.h = None
+
+    def add_empirical(self, m, n=200, Kmin=1e-3, Kmax=1e9, coulomb=False):
+        self.names.append(m.name)
+        return lib().orc_add_material_empirical(self.h, m.name.encode(), m.density, m.I,
+                                                len(m.Z), m.Z, m.A, m.Iel, m.frac, n, Kmin, Kmax,
+                                                int(coulomb))
+
+    def add_dedx(self, path, m, coulomb=False):
+        self.names.append(m.name)
+        return lib().orc_add_material_dedx(self.h, path.encode(), m.name.encode(), m.density,
+                                           m.I, len(m.Z), m.Z, m.A, m.Iel, m.frac, int(coulomb))
+
+    def add_columns(self, name, density, ZoA, cols):
+        """cols: dict column-name -> array (missing columns are zero)."""
+        n = len(cols["E"])
+        arrs = [_arr(cols.get(c, np.zeros(n))) for c in COLUMNS]
+        if "logE" not in cols:
+            arrs[1] = np.log(arrs[0])
+        ptrs = (C.POINTER(_D) * 19)(*[a.ctypes.data_as(C.POINTER(_D)) for a in arrs])
+        self._keep = getattr(self, "_keep", []) + [arrs]
+        self.names.append(name)
+        return lib().orc_add_material_columns(self.h, name.encode(), density, ZoA, n, ptrs)
+
+    def column(self, mat, name):
+        n = lib().orc_table_size(self.h, mat)
+        out = np.zeros(n)
+        lib().orc_table_column(self.h, mat, COLUMNS.index(name), out)
+        return out
+
+    def table(self, mat):
+        return {c: self.column(mat, c) for c in COLUMNS}
+
+    def lookup(self, mat, col, K):
+        return lib().orc_lookup(self.h, mat, COLUMNS.index(col), K)
+
+
+def default_physics(materials=(STANDARD_ROCK, AIR), n=200, Kmin=1e-3, Kmax=1e9, coulomb=False):
+    """create_physics(MUON) with the empirical tables (src/Physics.jl:534)."""
+    p = Physics()
+    for m in materials:
+        p.add_empirical(m, n, Kmin, Kmax, coulomb)
+    return p
+
+
+def dcs_integral(proc, Z, A, I, mass, K, xlo, xhi, mode, npoints=180):
+    return lib().orc_dcs_integral(proc, Z, A, I, mass, K, xlo, xhi, mode, npoints)
+
+
+def dcs(proc, Z, A, I, m, K, q):
+    return lib().orc_dcs(proc, Z, A, I, m, K, q)
+
+
+def flux_gccly(c, K, q):
+    return lib().orc_flux_gccly(c, K, q)
+
+
+def flux_single_csda(p, rock, air, thickness, rho, elevation, energy, charge,
+                     threshold=1e9, primary_altitude=3e4):
+    f, d, s = _D(), _D(), _L()
+    lib().orc_flux_single_csda(p.h, rock, air, thickness, rho, elevation, energy, charge,
+                               threshold, primary_altitude, C.byref(f), C.byref(d), C.byref(s))
+    return f.value, d.value, s.value
+
+
+def backward_mc_csda(p, rock, air, thickness, rho, elevation, E, q, w, threshold=1e9,
+                     primary_altitude=3e4, threads=0):
+    E, q, w = _arr(E), _arr(q), _arr(w)
+    c, d = np.zeros(len(E)), np.zeros(len(E))
+    threads = threads or os.cpu_count()
+    lib().orc_backward_mc_csda(p.h, rock, air, thickness, rho, elevation, threshold,
+                               primary_altitude, len(E), E, q, w, c, d, threads)
+    return c, d
+
+
+def flux_csda_direct(p, rock, air, rho, thickness, elevation, energy, charge, H=3e4):
+    f, d = _D(), _D()
+    lib().orc_flux_csda_direct(p.h, rock, air, rho, thickness, elevation, energy, charge, H,
+                               C.byref(f), C.byref(d))
+    return f.value, d.value
+
+
+def trace_ray(dims, geom, ray, cap=4096):
+    cells = np.zeros(cap, np.int32)
+    lens = np.zeros(cap)
+    z = _D()
+    n = lib().orc_trace_ray(np.asarray(dims, np.int32), _arr(geom), _arr(ray), cap, cells, lens,
+                            C.byref(z))
+    return cells[:n].copy(), lens[:n].copy(), z.value
+
+
+def tomo_forward(p, rock, air, dims, geom, rho, rho_side, rays, nodes, H=3e4, threads=0):
+    rays = _arr(rays).reshape(-1, 7)
+    out = np.zeros(len(rays))
+    E, q, w = (_arr(x) for x in nodes)
+    threads = threads or os.cpu_count()
+    lib().orc_tomo_forward(p.h, rock, air, np.asarray(dims, np.int32), _arr(geom),
+                           _arr(rho).ravel(), rho_side, H, len(rays), rays.ravel(), len(E), E, q,
+                           w, out, threads)
+    return out
+
+
+def tomo_ray_grad(p, rock, air, dims, geom, rho, rho_side, ray, nodes, H=3e4, cap=4096):
+    E, q, w = (_arr(x) for x in nodes)
+    cells = np.zeros(cap, np.int32)
+    grads = np.zeros(cap)
+    f, ds = _D(), _D()
+    n = lib().orc_tomo_ray_grad(p.h, rock, air, np.asarray(dims, np.int32), _arr(geom),
+                                _arr(rho).ravel(), rho_side, H, _arr(ray), len(E), E, q, w,
+                                C.byref(f), cap, cells, grads, C.byref(ds))
+    return f.value, cells[:n].copy(), grads[:n].copy(), ds.value
