@@ -1,0 +1,367 @@
+"""Benchmark of the DiffPumas.jl hot path on GB300 through libdpgpu.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c3|c1] [--impl gpu|reference]
+
+Workloads (seeded synthetic inputs, generated by dpgpu.workloads):
+  c3  batched tomography forward + adjoint: 64x64x32 voxel grid at 10 m,
+      smooth random density field with 3 cavities, 4 detectors x 1024 rays,
+      32 CSDA energy nodes on [1, 1e6] GeV.  One step = per-ray flux and the
+      density vector-Jacobian product J^T r over all rays.  Unit: rays/s.
+  c1  backward MC, CSDA mode, StandardRock 2650 kg/m^3, 100 m, 45 deg,
+      energies log-uniform 1-100 GeV, +-1 charges, 10^4 histories, with the
+      density gradient.  One step = one run_backward_mc estimate.  Unit:
+      samples/s.
+
+The --impl reference arm times the CPU implementation of the same path (the
+FP64 oracle restating the reference's Julia code, which cannot run here) on
+all host cores.  Multi-GPU: the path has no exchange step, N ranks run
+independent replicas (weak scaling).
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "diffpumas.jl_gb300"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "MC samples/s & tomography rays/s (+dflux/drho) vs plain GPU at <=1e-4 rel err"
+L2_BYTES = 129 * 2 ** 20
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d["hbm_gbs"], "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except Exception:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, x):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ workloads
+def setup_c3(dp, torch, dev):
+    from dpgpu.workloads import tomography_config
+    grid, rho, rays, nodes = tomography_config()
+    phys = dp.create_physics()
+    model = dp.TomoModel(phys, grid, nodes, side_density=2500.0)
+    cot = np.random.default_rng(1).uniform(0.5, 1.5, len(rays))
+    _, rp, _, _ = model.jacobian(rho, rays)
+    nseg = int(rp[-1])
+    T = lambda a: torch.tensor(np.ascontiguousarray(a).ravel(), dtype=torch.float64, device=dev)
+    d = {"rho": T(rho), "rays": T(rays), "E": T(nodes[0]), "q": T(nodes[1]), "w": T(nodes[2]),
+         "cot": T(cot), "flux": torch.zeros(len(rays), dtype=torch.float64, device=dev),
+         "grad": torch.zeros(grid.ncell, dtype=torch.float64, device=dev)}
+    tp = dp.DpTomoParams(model.params.rock_material, model.params.air_material, -1, 2500.0, 3e4,
+                         len(nodes[0]), d["E"].data_ptr(), d["q"].data_ptr(), d["w"].data_ptr())
+    g = grid.to_c()
+    lib = dp.load()
+
+    def step_dev():
+        dp.check(lib.dp_tomo_vjp_dev(phys.ctx.h, phys.h, C.byref(g), C.byref(tp), d["rho"].data_ptr(),
+                                     len(rays), d["rays"].data_ptr(), d["cot"].data_ptr(),
+                                     d["flux"].data_ptr(), d["grad"].data_ptr()), phys.ctx.h)
+
+    h_flux = np.zeros(len(rays))
+    h_grad = np.zeros(grid.ncell)
+    rho_h, rays_h, cot_h = (np.ascontiguousarray(a, np.float64).ravel() for a in (rho, rays, cot))
+
+    def step_e2e():
+        model.params.side_cell = -1
+        dp.check(lib.dp_tomo_vjp(phys.ctx.h, phys.h, C.byref(g), C.byref(model.params),
+                                 rho_h.ctypes.data_as(C.c_void_p), len(rays),
+                                 rays_h.ctypes.data_as(C.c_void_p), cot_h.ctypes.data_as(C.c_void_p),
+                                 h_flux.ctypes.data_as(C.c_void_p), h_grad.ctypes.data_as(C.c_void_p)),
+                 phys.ctx.h)
+
+    def plain_dev():
+        dp.check(lib.dp_tomo_forward_plain_dev(phys.ctx.h, phys.h, C.byref(g), C.byref(tp),
+                                               d["rho"].data_ptr(), len(rays), d["rays"].data_ptr(),
+                                               d["flux"].data_ptr()), phys.ctx.h)
+
+    n_rays = len(rays)
+    # algorithmic bytes of the adjoint kernel per launch: ray record (56 B),
+    # flux (8 B) and row pointer (8 B) per ray; per traversed segment the
+    # density gather (8 B) and the Jacobian entry written (col 4 + val 8 +
+    # row 4 = 16 B).
+    alg = n_rays * (56 + 8 + 8) + nseg * (8 + 16)
+    info = {"units": n_rays, "unit": "rays/s", "kernel": "tomo_adjoint", "alg_bytes": alg,
+            "config": {"workload": "c3: tomography forward + adjoint, 64x64x32 @ 10 m, 4x1024 rays, "
+                                   "32 energy nodes [1,1e6] GeV, J^T r per step",
+                       "grid": [64, 64, 32], "rays": n_rays, "energy_nodes": 32,
+                       "segments": nseg, "precision": "fp64"},
+            "h2d": 8 * (rho_h.size + rays_h.size + cot_h.size + 3 * len(nodes[0])),
+            "d2h": 8 * (n_rays + grid.ncell)}
+    return step_dev, step_e2e, plain_dev, info, phys
+
+
+def setup_c1(dp, torch, dev):
+    phys = dp.create_physics()
+    n = 10000
+    kw = dict(rock_thickness=100.0, rock_density=2650.0, elevation=45.0, energy_min=1.0,
+              energy_max=100.0, n_samples=n, compute_gradient=True, seed=42, straggling=False,
+              scattering=False)
+    p = dp._mc_params(phys, 100.0, 2650.0, 45.0, 1.0, 100.0, n, True, 42, False, False, 100.0,
+                      None, 3e4)
+    out = dp.DpMcResult()
+    lib = dp.load()
+
+    def step():
+        dp.check(lib.dp_backward_mc(phys.ctx.h, phys.h, C.byref(p), C.byref(out)), phys.ctx.h)
+
+    info = {"units": n, "unit": "samples/s", "kernel": "csda_mc", "alg_bytes": n * (24 + 16),
+            "config": {"workload": "c1: backward MC CSDA, StandardRock 100 m @ 45 deg, 2650 kg/m3, "
+                                   "E 1-100 GeV, 1e4 histories, with d flux/d rho",
+                       "n_samples": n, "precision": "fp64"},
+            "h2d": 0, "d2h": 8 * 7}
+    return step, step, None, info, phys
+
+
+# ------------------------------------------------------------------ arms
+def run_gpu(args):
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    import dpgpu as dp
+    dp._default = dp.Context(local)
+    setup = {"c3": setup_c3, "c1": setup_c1}[args.workload]
+    step_dev, step_e2e, plain_dev, info, phys = setup(dp, torch, dev)
+    lib = dp.load()
+    ctx = phys.ctx.h
+    stream = torch.cuda.ExternalStream(lib.dp_get_stream(ctx), device=dev)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+
+    for _ in range(args.warmup):
+        step_dev()
+    torch.cuda.synchronize()
+    lib.dp_set_timing(ctx, 1)
+    launches0 = lib.dp_launch_count(ctx)
+    times = []
+    barrier(world)
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        t_wall = time.perf_counter()
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()  # L2 flush between timed steps (outside the events)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            step_dev()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall
+    barrier(world)
+    launches = lib.dp_launch_count(ctx) - launches0
+    kms = C.c_double()
+    lib.dp_kernel_time(ctx, info["kernel"].encode(), C.byref(kms))
+    lib.dp_set_timing(ctx, 0)
+    ms = max_over_ranks(world, sum(times) / len(times))
+    value = world * info["units"] / (ms * 1e-3)
+
+    # end to end through the host-pointer C ABI (copies inside the timed region)
+    for _ in range(max(1, args.warmup // 2)):
+        step_e2e()
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_e2e()
+    torch.cuda.synchronize()
+    e2e_ms = max_over_ranks(world, (time.perf_counter() - t0) * 1e3 / args.steps)
+
+    # plain FP64 one-launch-per-ray form (speed-up denominator)
+    plain = None
+    if plain_dev is not None:
+        plain_dev()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        reps = 2
+        for _ in range(reps):
+            plain_dev()
+        torch.cuda.synchronize()
+        plain_ms = (time.perf_counter() - t0) * 1e3 / reps
+        plain = {"value": info["units"] / (plain_ms * 1e-3), "unit": info["unit"],
+                 "ms_per_step": plain_ms, "what": "plain FP64 one-launch-per-ray, forward only"}
+
+    peak, peak_kind = peaks()
+    kernel_ms = kms.value / args.steps
+    achieved = info["alg_bytes"] / (kernel_ms * 1e-3) / 1e9 if kernel_ms > 0 else None
+    line = {"metric": METRIC, "value": value, "unit": info["unit"], "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "config": dict(info["config"], l2="flushed between steps",
+                                                          parallelism=f"replicas x{world}"),
+            "e2e": {"value": world * info["units"] / (e2e_ms * 1e-3), "unit": info["unit"],
+                    "h2d_bytes_per_step": info["h2d"], "d2h_bytes_per_step": info["d2h"]},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak if achieved else None, "traffic": None,
+                         "kernel": info["kernel"], "kernel_ms": kernel_ms,
+                         "peak_source": peak_kind},
+            "gpu_launches": int(launches),
+            "plain_gpu": plain,
+            "speedup_vs_plain": (value / plain["value"]) if plain else None,
+            "clocks": clk.summary(), "wall_s": t_wall}
+    if rank == 0:
+        if not args.no_cpu:
+            line["cpu_baseline"] = cpu_baseline(args.workload, budget_s=args.cpu_seconds)
+        print(json.dumps(line))
+
+
+def cpu_baseline(workload, budget_s=15.0, threads=None):
+    """The FP64 oracle on a bounded sample of the same workload, all host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    threads = threads or os.cpu_count()
+    if workload == "c3":
+        from dpgpu.workloads import tomography_config
+        grid, rho, rays, nodes = tomography_config()
+        p = O.default_physics((O.STANDARD_ROCK, O.AIR))
+        dims = np.array([grid.nx, grid.ny, grid.nz], np.int32)
+        geom = np.array([*grid.origin, *grid.pitch])
+        n, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < budget_s and n < len(rays):
+            chunk = rays[n:n + 256]
+            O.tomo_forward(p, 0, 1, dims, geom, rho, 2500.0, chunk, nodes, threads=threads)
+            n += len(chunk)
+        dt = time.perf_counter() - t0
+        return {"value": n / dt, "unit": "rays/s", "cores": threads, "kind": "port",
+                "sample": f"{n} rays of the c3 workload, forward flux only (FP64 oracle, OpenMP)"}
+    p = O.default_physics((O.STANDARD_ROCK, O.AIR))
+    rng = np.random.default_rng(0)
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < budget_s:
+        E = np.exp(rng.uniform(0, np.log(100.0), 2048))
+        q = np.where(rng.uniform(size=2048) > 0.5, 1.0, -1.0)
+        O.backward_mc_csda(p, 0, 1, 100.0, 2650.0, 45.0, E, q, 2 * E * np.log(100.0), threads=threads)
+        n += 2048
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": "samples/s", "cores": threads, "kind": "port",
+            "sample": f"{n} histories of the c1 workload with the dual-number gradient (FP64 oracle, OpenMP)"}
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    units = {"c3": "rays/s", "c1": "samples/s"}[args.workload]
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(args.workload, budget_s=args.cpu_seconds / 4)
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(args.workload, budget_s=args.cpu_seconds)["value"])
+    cb = cpu_baseline(args.workload, budget_s=1.0)
+    v = statistics.mean(vals)
+    cb["value"] = v
+    line = {"metric": METRIC, "impl": "reference", "value": v, "unit": units, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": args.workload,
+                       "note": "reference is Julia (no toolchain on this box): FP64 oracle port of "
+                               "its code path on all host cores"},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": units, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--workload", default="c3", choices=["c3", "c1"])
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,255 @@
+// api.cu -- context, error handling and physics-table handles of libdpgpu.
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "internal.h"
+
+namespace dp {
+int fail(dp_ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+int cuda_fail(dp_ctx* ctx, cudaError_t e, const char* where) {
+  return fail(ctx, DP_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+void* scratch(dp_ctx* ctx, size_t bytes, int slot) {
+  void*& p = slot ? ctx->scratch2 : ctx->scratch;
+  size_t& have = slot ? ctx->scratch2_bytes : ctx->scratch_bytes;
+  if (bytes <= have && p) return p;
+  if (p) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(p);
+  }
+  p = nullptr;
+  have = 0;
+  size_t want = bytes + bytes / 4 + 256;
+  if (cudaMalloc(&p, want) != cudaSuccess) return nullptr;
+  have = want;
+  return p;
+}
+void timed_begin(dp_ctx* ctx) {
+  ++ctx->launches;
+  if (ctx->timing) cudaEventRecord(ctx->ev0, ctx->stream);
+}
+void timed_end(dp_ctx* ctx, const char* name) {
+  if (!ctx->timing) return;
+  cudaEventRecord(ctx->ev1, ctx->stream);
+  cudaEventSynchronize(ctx->ev1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  for (auto& kv : ctx->ktime)
+    if (kv.first == name) {
+      kv.second += ms;
+      return;
+    }
+  ctx->ktime.emplace_back(name, double(ms));
+}
+}  // namespace dp
+
+using dp::fail;
+
+extern "C" {
+
+int dp_version(void) { return DPGPU_VERSION; }
+
+int dp_init(int device, dp_ctx** out) {
+  if (!out) return DP_ERR_ARG;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return DP_ERR_CUDA;
+  if (device < 0 || device >= n) return DP_ERR_ARG;
+  dp_ctx* c = new (std::nothrow) dp_ctx;
+  if (!c) return DP_ERR_ALLOC;
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
+      cudaMalloc(&c->d_flag, sizeof(int)) != cudaSuccess ||
+      cudaMemset(c->d_flag, 0, sizeof(int)) != cudaSuccess) {
+    delete c;
+    return DP_ERR_CUDA;
+  }
+  c->stream = c->own_stream;
+  *out = c;
+  return DP_OK;
+}
+
+int dp_destroy(dp_ctx* c) {
+  if (!c) return DP_ERR_ARG;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  if (c->scratch) cudaFree(c->scratch);
+  if (c->scratch2) cudaFree(c->scratch2);
+  if (c->d_flag) cudaFree(c->d_flag);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
+  return DP_OK;
+}
+
+int dp_set_stream(dp_ctx* c, void* stream) {
+  if (!c) return DP_ERR_ARG;
+  cudaStreamSynchronize(c->stream);
+  c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+  return DP_OK;
+}
+
+void* dp_get_stream(const dp_ctx* c) { return c ? static_cast<void*>(c->stream) : nullptr; }
+
+int dp_set_timing(dp_ctx* c, int enable) {
+  if (!c) return DP_ERR_ARG;
+  c->timing = enable ? 1 : 0;
+  c->ktime.clear();
+  return DP_OK;
+}
+
+int dp_kernel_time(const dp_ctx* c, const char* name, double* ms) {
+  if (!c || !name || !ms) return DP_ERR_ARG;
+  *ms = 0.0;
+  for (const auto& kv : c->ktime)
+    if (kv.first == name) *ms = kv.second;
+  return DP_OK;
+}
+
+long long dp_launch_count(const dp_ctx* c) { return c ? c->launches : -1; }
+
+const char* dp_last_error(const dp_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+static int finish_upload(dp_ctx* ctx, dp_physics* p, dp_physics** out) {
+  // Uniform log grid detection (enables O(1) interval lookup).
+  const double* lE = &p->host[size_t(DP_COL_LOGE) * p->n];
+  double d = (lE[p->n - 1] - lE[0]) / double(p->n - 1);
+  bool uni = p->n > 2;
+  for (int i = 0; i < p->n && uni; ++i)
+    if (std::fabs(lE[i] - (lE[0] + d * i)) > 1e-9 * std::fabs(d)) uni = false;
+  // All materials must share the energy grid.
+  for (int m = 1; m < p->n_mat; ++m)
+    if (std::memcmp(&p->host[(size_t(m) * DP_NCOL + DP_COL_E) * p->n], &p->host[0],
+                    sizeof(double) * p->n) != 0) {
+      delete p;
+      return fail(ctx, DP_ERR_ARG, "all materials must share one energy grid");
+    }
+  p->ld = dp::padded(p->n);
+  std::vector<double> pad(size_t(p->n_mat) * DP_NCOL * p->ld, 0.0);
+  for (int m = 0; m < p->n_mat; ++m)
+    for (int c = 0; c < DP_NCOL; ++c)
+      std::memcpy(&pad[(size_t(m) * DP_NCOL + c) * p->ld], &p->host[(size_t(m) * DP_NCOL + c) * p->n],
+                  sizeof(double) * p->n);
+  if (cudaSetDevice(ctx->device) != cudaSuccess ||
+      cudaMalloc(&p->dev, pad.size() * sizeof(double)) != cudaSuccess) {
+    delete p;
+    return fail(ctx, DP_ERR_CUDA, "table allocation failed");
+  }
+  if (cudaMemcpy(p->dev, pad.data(), pad.size() * sizeof(double), cudaMemcpyHostToDevice) !=
+      cudaSuccess) {
+    cudaFree(p->dev);
+    delete p;
+    return fail(ctx, DP_ERR_CUDA, "table upload failed");
+  }
+  p->view.base = p->dev;
+  p->view.n = p->n;
+  p->view.ld = p->ld;
+  p->view.n_mat = p->n_mat;
+  p->view.uniform = uni ? 1 : 0;
+  p->view.lE0 = lE[0];
+  p->view.inv_dlE = 1.0 / d;
+  p->ctx = ctx;
+  *out = p;
+  return DP_OK;
+}
+
+static bool to_host_material(const dp_material& m, dp::HostMaterial& h) {
+  if (m.n_elements <= 0 || !m.elements) return false;
+  h.name = m.name ? m.name : "";
+  h.density = m.density;
+  h.I = m.I;
+  double tot = 0.0;
+  for (int i = 0; i < m.n_elements; ++i) tot += m.elements[i].fraction;
+  if (!(tot > 0.0)) return false;
+  double zoa = 0.0;
+  h.elements.clear();
+  for (int i = 0; i < m.n_elements; ++i) {
+    const dp_element& e = m.elements[i];
+    double f = e.fraction / tot;
+    h.elements.push_back({e.Z, e.A, e.I, f});
+    zoa += e.Z / e.A * f;
+  }
+  h.ZoA = m.ZoA > 0.0 ? m.ZoA : zoa;
+  return true;
+}
+
+int dp_physics_upload(dp_ctx* ctx, const dp_settings* st, int n_mat, int n, const double* cols,
+                      const dp_material* recipes, dp_physics** out) {
+  if (!ctx || !st || !cols || !out || n_mat <= 0 || n < 2) return fail(ctx, DP_ERR_ARG, "bad arguments");
+  dp_physics* p = new dp_physics;
+  p->settings = *st;
+  p->n_mat = n_mat;
+  p->n = n;
+  p->host.assign(cols, cols + size_t(n_mat) * DP_NCOL * n);
+  if (recipes) {
+    p->recipes.resize(n_mat);
+    for (int m = 0; m < n_mat; ++m)
+      if (!to_host_material(recipes[m], p->recipes[m])) {
+        delete p;
+        return fail(ctx, DP_ERR_ARG, "invalid material recipe");
+      }
+    p->has_recipes = true;
+  }
+  return finish_upload(ctx, p, out);
+}
+
+int dp_physics_create(dp_ctx* ctx, const dp_settings* st, int n_mat, const dp_material* mats,
+                      int n, double Kmin, double Kmax, dp_physics** out) {
+  if (!ctx || !st || !mats || !out || n_mat <= 0 || n < 2 || !(Kmin > 0.0) || !(Kmax > Kmin))
+    return fail(ctx, DP_ERR_ARG, "bad arguments");
+  dp_physics* p = new dp_physics;
+  p->settings = *st;
+  p->n_mat = n_mat;
+  p->n = n;
+  p->host.assign(size_t(n_mat) * DP_NCOL * n, 0.0);
+  p->recipes.resize(n_mat);
+  for (int m = 0; m < n_mat; ++m) {
+    if (!to_host_material(mats[m], p->recipes[m])) {
+      delete p;
+      return fail(ctx, DP_ERR_ARG, "invalid material recipe");
+    }
+    dp::build_empirical_table(p->recipes[m], *st, n, Kmin, Kmax,
+                              &p->host[size_t(m) * DP_NCOL * n]);
+  }
+  p->has_recipes = true;
+  return finish_upload(ctx, p, out);
+}
+
+int dp_physics_free(dp_physics* p) {
+  if (!p) return DP_ERR_ARG;
+  if (p->dev) {
+    cudaSetDevice(p->ctx->device);
+    cudaFree(p->dev);
+  }
+  delete p;
+  return DP_OK;
+}
+
+int dp_physics_info(const dp_physics* p, int* n_mat, int* n) {
+  if (!p) return DP_ERR_ARG;
+  if (n_mat) *n_mat = p->n_mat;
+  if (n) *n = p->n;
+  return DP_OK;
+}
+
+int dp_physics_column(const dp_physics* p, int mat, int col, double* out) {
+  if (!p || !out || mat < 0 || mat >= p->n_mat || col < 0 || col >= DP_NCOL) return DP_ERR_ARG;
+  std::memcpy(out, &p->host[(size_t(mat) * DP_NCOL + col) * p->n], sizeof(double) * p->n);
+  return DP_OK;
+}
+
+int dp_physics_material_index(const dp_physics* p, const char* name) {
+  if (!p || !name || !p->has_recipes) return -1;
+  for (int m = 0; m < p->n_mat; ++m)
+    if (p->recipes[m].name == name) return m;
+  return -1;
+}
+
+}  // extern "C"

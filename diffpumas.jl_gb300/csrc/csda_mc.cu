@@ -1,0 +1,369 @@
+// csda_mc.cu -- backward Monte Carlo in CSDA mode (run_backward_mc with
+// straggling = scattering = false) and its density derivative.
+//
+// One thread per history.  The history follows the adaptive two-layer step
+// sequence of src/Geometry.jl:534-672 (transport_backward_step :424-457,
+// step limit :461-476) and the acceptance of :694-757.  The derivative with
+// respect to the rock density is propagated in tangent (forward) mode through
+// the same discrete program: for a single scalar density this is the cheapest
+// exact adjoint and equals what Zygote computes on the reference
+// (compute_flux_gradient, :1007-1028), step-size dependence on rho included.
+//
+// Tables used by a history (energy grid and the rock/air CSDA range and
+// stopping power) are staged once per CTA into shared memory with
+// cp.async.bulk.  Per-history results go to global memory and are reduced in a
+// fixed order (compensated), so estimates are bitwise reproducible.
+#include <cmath>
+#include <vector>
+
+#include "internal.h"
+
+namespace dp {
+
+struct CsdaParams {
+  TabView tab;
+  int rock, air;
+  double thickness, rho, H, dir_z, uz, threshold, low, air_limit, mass, ctau;
+  double cos_final, cs, cs129;
+  int use_philox;
+  uint64_t seed;
+  double emin, emax;
+  long n;
+  const double *E, *q, *w;
+  double *contrib, *dcontrib, *sample_out;
+  int32_t* steps;
+  int* err_flag;
+};
+
+// Shared-memory table slots (all materials share the energy grid).
+enum { S_E = 0, S_LOGE, S_RS, S_RR, S_AS, S_AR, S_NCOL };
+
+__device__ __forceinline__ Dd range_of(const TabView& tv, const double* sE, const double* slE,
+                                       const double* R, Dd E, Dd lE) {
+  return interp_logE(tv, sE, slE, R, E, lE, nullptr);
+}
+
+__global__ void __launch_bounds__(128) csda_mc_kernel(CsdaParams P) {
+  extern __shared__ __align__(16) double smem[];
+  __shared__ uint64_t mbar;
+  const int ld = P.tab.ld, n = P.tab.n;
+  const double* src[S_NCOL] = {P.tab.col(0, DP_COL_E),          P.tab.col(0, DP_COL_LOGE),
+                               P.tab.col(P.rock, DP_COL_CSDA_S), P.tab.col(P.rock, DP_COL_CSDA_R),
+                               P.tab.col(P.air, DP_COL_CSDA_S),  P.tab.col(P.air, DP_COL_CSDA_R)};
+  if (!stage_columns(smem, src, S_NCOL, uint32_t(ld * sizeof(double)), &mbar)) {
+    if (threadIdx.x == 0) atomicExch(P.err_flag, 1);
+    return;
+  }
+  const double* sE = smem + S_E * ld;
+  const double* slE = smem + S_LOGE * ld;
+  const double* rS = smem + S_RS * ld;
+  const double* rR = smem + S_RR * ld;
+  const double* aS = smem + S_AS * ld;
+  const double* aR = smem + S_AR * ld;
+  const double eps = kEps64;
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < P.n;
+       i += long(gridDim.x) * blockDim.x) {
+    double E0, q, w;
+    if (P.use_philox) {
+      mc_sample(P.seed, uint64_t(i), P.emin, P.emax, &E0, &q, &w);
+      if (P.sample_out) {
+        P.sample_out[3 * i] = E0;
+        P.sample_out[3 * i + 1] = q;
+        P.sample_out[3 * i + 2] = w;
+      }
+    } else {
+      E0 = P.E[i];
+      q = P.q[i];
+      w = P.w[i];
+    }
+    Dd E = dd(E0), wt = dd(1.0), z = dd(0.0);
+    const Dd rho = dd(P.rho, 1.0);
+    int hint_r = 0, hint_a = 0;
+    int32_t nsteps = 0;
+    // S(E) at the start of a step equals S(kf) of the previous step in the
+    // same material (same argument, same table): reuse it.
+    int s_mat = -1;
+    Dd s_cache = dd(0.0);
+    // Hard cap on the total step count of one history (the reference loops
+    // until a boundary; a typical history takes 10^2-10^3 steps).
+    const int32_t kMaxSteps = 2000000;
+    for (int outer = 0; outer < 1000 && nsteps < kMaxSteps; ++outer) {
+      if (!(E.v < P.threshold - eps)) break;
+      if (z.v < 0.0 || z.v >= P.H - eps) break;
+      if (wt.v <= 0.0 || !isfinite(wt.v)) break;
+      double limit = E.v < P.low - eps ? fmin(P.low, P.threshold) : P.threshold;
+      for (int inner = 0; inner < 50000 && nsteps < kMaxSteps; ++inner) {
+        if (z.v < 0.0 || z.v >= P.H - eps) break;
+        if (E.v >= limit - eps) break;
+        if (wt.v <= 0.0 || !isfinite(wt.v)) break;
+        const bool in_air = z.v >= P.thickness;
+        const double *S = in_air ? aS : rS, *R = in_air ? aR : rR;
+        int* hint = in_air ? &hint_a : &hint_r;
+        const int mat = in_air ? 1 : 0;
+        Dd dens, tob;
+        if (!in_air) {
+          dens = rho;
+          if (P.uz > eps) tob = (dd(P.thickness) - z) / P.uz;
+          else if (P.uz < -eps) tob = (dd(0.0) - z) / P.uz;
+          else tob = dd(1000.0);
+        } else {
+          dens = 1.205 * dexp(z / -12e3);
+          if (P.uz > eps) tob = (dd(P.H) - z) / P.uz;
+          else if (P.uz < -eps) tob = (dd(P.thickness) - z) / P.uz;
+          else tob = dd(1000.0);
+        }
+        Dd lE = dlog(E);
+        Dd X = range_of(P.tab, sE, slE, R, E, lE);
+        Dd lim = 0.01 * X / dmax(dens, dd(1e-6));
+        if (in_air) lim = dmin(lim, dd(P.air_limit));
+        Dd step = dmin(tob + dd(1e-7), lim);
+        if (step.v < kStepMin) step = dd(kStepMin);
+        else if (step.v > 1000.0) step = dd(1000.0);
+        // transport_backward_step (src/Geometry.jl:424-457)
+        Dd kf = inverse_range(R, sE, slE, n, X + step * dens, hint);
+        Dd gi = dd(1.0) + E / P.mass, gc = dd(1.0) + kf / P.mass, ga = (gi + gc) / 2.0;
+        Dd ba = dsqrt(dmax(dd(1.0) - dd(1.0) / (ga * ga), dd(1e-12)));
+        Dd dt = step / (ba * ga);
+        z = z - step * dd(P.dir_z);
+        Dd Si = (s_mat == mat) ? s_cache : interp_logE(P.tab, sE, slE, S, E, lE, nullptr);
+        Dd Sf = interp_logE(P.tab, sE, slE, S, kf, dlog(kf), nullptr);
+        wt = wt * (Sf / Si) * dexp(dt / -P.ctau);
+        E = kf;
+        s_mat = mat;
+        s_cache = Sf;
+        ++nsteps;
+      }
+    }
+    double f = 0.0, df = 0.0;
+    if (z.v >= P.H - 1.0 && E.v < P.threshold && P.cos_final > 0.0) {
+      double dlogf;
+      double F = gccly_flux(P.cs, P.cs129, E.v, q, &dlogf);
+      f = wt.v * F;
+      df = wt.d * F + wt.v * F * dlogf * E.d;
+    }
+    P.contrib[i] = w * f;
+    if (P.dcontrib) P.dcontrib[i] = w * df;
+    if (P.steps) P.steps[i] = nsteps;
+  }
+}
+
+// Compensated (TwoSum) accumulation in a fixed order: every thread owns a
+// fixed strided subset, blocks reduce in a fixed tree, a single block then
+// reduces the block partials.
+struct KSum {
+  double s, c;
+};
+__device__ __forceinline__ void kadd(KSum& a, double x) {
+  double t = a.s + x;
+  double bp = t - a.s;
+  a.c += (a.s - (t - bp)) + (x - bp);
+  a.s = t;
+}
+__device__ __forceinline__ void kmerge(KSum& a, const KSum& b) {
+  kadd(a, b.s);
+  a.c += b.c;
+}
+
+constexpr int kRedThreads = 256;
+__global__ void __launch_bounds__(kRedThreads) reduce3_kernel(const double* a, const double* b, long n,
+                                                              KSum* part) {
+  __shared__ KSum sh[3][kRedThreads];
+  KSum s0{0, 0}, s1{0, 0}, s2{0, 0};
+  for (long i = blockIdx.x * long(kRedThreads) + threadIdx.x; i < n; i += long(gridDim.x) * kRedThreads) {
+    double x = a[i];
+    kadd(s0, x);
+    kadd(s1, x * x);
+    if (b) kadd(s2, b[i]);
+  }
+  sh[0][threadIdx.x] = s0;
+  sh[1][threadIdx.x] = s1;
+  sh[2][threadIdx.x] = s2;
+  __syncthreads();
+  for (int h = kRedThreads / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h)
+      for (int k = 0; k < 3; ++k) kmerge(sh[k][threadIdx.x], sh[k][threadIdx.x + h]);
+    __syncthreads();
+  }
+  if (threadIdx.x < 3) part[blockIdx.x * 3 + threadIdx.x] = sh[threadIdx.x][0];
+}
+__global__ void __launch_bounds__(kRedThreads) reduce_parts_kernel(const KSum* part, int nb, double* out) {
+  __shared__ KSum sh[3][kRedThreads];
+  KSum s[3] = {{0, 0}, {0, 0}, {0, 0}};
+  for (int b = threadIdx.x; b < nb; b += kRedThreads)
+    for (int k = 0; k < 3; ++k) kmerge(s[k], part[b * 3 + k]);
+  for (int k = 0; k < 3; ++k) sh[k][threadIdx.x] = s[k];
+  __syncthreads();
+  for (int h = kRedThreads / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h)
+      for (int k = 0; k < 3; ++k) kmerge(sh[k][threadIdx.x], sh[k][threadIdx.x + h]);
+    __syncthreads();
+  }
+  if (threadIdx.x < 3) out[threadIdx.x] = sh[threadIdx.x][0].s + sh[threadIdx.x][0].c;
+}
+
+static int setup(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params* p, CsdaParams& P) {
+  if (!ctx || !ph || !p) return fail(ctx, DP_ERR_ARG, "null argument");
+  if (p->straggling || p->scattering)
+    return fail(ctx, DP_ERR_ARG, "only CSDA transport (straggling = scattering = 0) is available");
+  int rock = p->rock_material, air = p->air_material;
+  if (rock < 0) {
+    rock = dp_physics_material_index(ph, "StandardRock");
+    if (rock < 0) rock = 0;
+  }
+  if (air < 0) {
+    air = dp_physics_material_index(ph, "Air");
+    if (air < 0) air = ph->n_mat - 1;
+  }
+  if (rock >= ph->n_mat || air >= ph->n_mat) return fail(ctx, DP_ERR_ARG, "material index out of range");
+  double tmax = ph->host[(size_t(0) * DP_NCOL + DP_COL_E) * ph->n + ph->n - 1];
+  double thr = p->source_energy_max > 0.0 ? p->source_energy_max : std::fmin(1e9, tmax);
+  if (!(thr > 0.0 && thr <= tmax))
+    return fail(ctx, DP_ERR_ARG, "source_energy_max must be positive and within the physics energy grid");
+  P = CsdaParams{};
+  P.tab = ph->view;
+  P.rock = rock;
+  P.air = air;
+  P.thickness = p->rock_thickness;
+  P.rho = p->rock_density;
+  P.H = p->primary_altitude > 0.0 ? p->primary_altitude : 3e4;
+  double theta = (90.0 - p->elevation) * kPi / 180.0;
+  double c = std::cos(theta);
+  P.dir_z = -c;
+  P.uz = c;
+  P.threshold = thr;
+  P.low = p->energy_threshold_low > 0.0 ? p->energy_threshold_low : 100.0;
+  P.air_limit = 0.05 * 12e3 / std::fmax(std::fabs(c), 0.05);
+  P.mass = ph->settings.mass;
+  P.ctau = ph->settings.ctau;
+  P.cos_final = std::fmin(std::fmax(c, 0.0), 1.0);
+  P.cs = cos_theta_star(P.cos_final);
+  P.cs129 = std::pow(P.cs, 1.29);
+  P.err_flag = ctx->d_flag;
+  return DP_OK;
+}
+
+static int launch(dp_ctx* ctx, CsdaParams& P) {
+  size_t smem = size_t(S_NCOL) * P.tab.ld * sizeof(double);
+  int threads = 128;
+  long blocks = (P.n + threads - 1) / threads;
+  if (blocks > 152L * 16) blocks = 152L * 16;
+  if (blocks < 1) blocks = 1;
+  timed_begin(ctx);
+  csda_mc_kernel<<<int(blocks), threads, smem, ctx->stream>>>(P);
+  DP_CHECK_CUDA(ctx, cudaGetLastError());
+  timed_end(ctx, "csda_mc");
+  return DP_OK;
+}
+
+static int check_flag(dp_ctx* ctx) {
+  int flag = 0;
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  DP_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (flag) {
+    cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream);
+    return fail(ctx, DP_ERR_STATE, "a table-staging wait exceeded its limit");
+  }
+  return DP_OK;
+}
+
+}  // namespace dp
+
+using namespace dp;
+
+extern "C" {
+
+int dp_csda_flux_samples_dev(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params* p, long n,
+                             const double* E, const double* q, const double* w, double* contrib,
+                             double* dcontrib, int32_t* steps) {
+  CsdaParams P;
+  int rc = setup(ctx, ph, p, P);
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && (!E || !q || !w || !contrib))) return fail(ctx, DP_ERR_ARG, "bad sample arrays");
+  if (n == 0) return DP_OK;
+  DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  P.n = n;
+  P.E = E;
+  P.q = q;
+  P.w = w;
+  P.contrib = contrib;
+  P.dcontrib = dcontrib;
+  P.steps = steps;
+  rc = launch(ctx, P);
+  if (rc) return rc;
+  return check_flag(ctx);
+}
+
+int dp_csda_flux_samples(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params* p, long n,
+                         const double* E, const double* q, const double* w, double* contrib,
+                         double* dcontrib, int32_t* steps) {
+  if (!ctx) return DP_ERR_ARG;
+  if (n <= 0) return n == 0 ? DP_OK : fail(ctx, DP_ERR_ARG, "negative n");
+  DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  size_t nb = size_t(n) * sizeof(double);
+  char* s = static_cast<char*>(scratch(ctx, 6 * nb + size_t(n) * 4));
+  if (!s) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
+  double *dE = (double*)s, *dq = dE + n, *dw = dq + n, *dc = dw + n, *dd_ = dc + n;
+  int32_t* ds = (int32_t*)(dd_ + n);
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dE, E, nb, cudaMemcpyHostToDevice, ctx->stream));
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dq, q, nb, cudaMemcpyHostToDevice, ctx->stream));
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dw, w, nb, cudaMemcpyHostToDevice, ctx->stream));
+  int rc = dp_csda_flux_samples_dev(ctx, ph, p, n, dE, dq, dw, dc, dcontrib ? dd_ : nullptr,
+                                    steps ? ds : nullptr);
+  if (rc) return rc;
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(contrib, dc, nb, cudaMemcpyDeviceToHost, ctx->stream));
+  if (dcontrib) DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dcontrib, dd_, nb, cudaMemcpyDeviceToHost, ctx->stream));
+  if (steps) DP_CHECK_CUDA(ctx, cudaMemcpyAsync(steps, ds, size_t(n) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  DP_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return DP_OK;
+}
+
+int dp_mc_samples(dp_ctx* ctx, const dp_mc_params* p, long n, double* E, double* q, double* w) {
+  if (!ctx || !p || n < 0 || !E || !q || !w) return fail(ctx, DP_ERR_ARG, "bad arguments");
+  double emax = p->energy_max > p->energy_min ? p->energy_max : p->energy_min;
+  for (long i = 0; i < n; ++i) mc_sample(p->seed, uint64_t(i), p->energy_min, emax, E + i, q + i, w + i);
+  return DP_OK;
+}
+
+int dp_backward_mc(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params* p, dp_mc_result* out) {
+  CsdaParams P;
+  int rc = setup(ctx, ph, p, P);
+  if (rc) return rc;
+  if (!out || p->n_samples <= 0) return fail(ctx, DP_ERR_ARG, "n_samples must be positive");
+  DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  long n = p->n_samples;
+  const int nb = 152 * 2;
+  char* s = static_cast<char*>(scratch(ctx, size_t(n) * 2 * sizeof(double) + nb * 3 * sizeof(KSum) + 64));
+  if (!s) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
+  double* dc = (double*)s;
+  double* dd_ = dc + n;
+  KSum* part = (KSum*)(dd_ + n);
+  double* sums = (double*)(part + nb * 3);
+  P.n = n;
+  P.use_philox = 1;
+  P.seed = p->seed;
+  P.emin = p->energy_min;
+  P.emax = p->energy_max > p->energy_min ? p->energy_max : p->energy_min;
+  P.contrib = dc;
+  P.dcontrib = dd_;
+  rc = launch(ctx, P);
+  if (rc) return rc;
+  reduce3_kernel<<<nb, kRedThreads, 0, ctx->stream>>>(dc, dd_, n, part);
+  reduce_parts_kernel<<<1, kRedThreads, 0, ctx->stream>>>(part, nb, sums);
+  ctx->launches += 2;
+  DP_CHECK_CUDA(ctx, cudaGetLastError());
+  double h[3];
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  rc = check_flag(ctx);
+  if (rc) return rc;
+  double flux = h[0] / n, var = h[1] / n - flux * flux;
+  out->flux = flux;
+  out->sigma = p->rock_thickness > 0.0 ? std::sqrt(std::fmax(var, 0.0) / n) : 0.0;
+  out->gradient = p->compute_gradient ? h[2] / n : 0.0;
+  out->gradient_flux = p->compute_gradient ? flux : 0.0;
+  out->source_energy_max = P.threshold;
+  out->n_samples = n;
+  out->n_status_nonzero = 0;
+  return DP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,69 @@
+// internal.h -- host-side definitions shared by the libdpgpu translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+struct dp_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;      // stream every launch of this context uses
+  cudaStream_t own_stream = nullptr;  // created by dp_init
+  // Launch accounting and optional per-kernel timing (CUDA events on `stream`).
+  long long launches = 0;
+  int timing = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::vector<std::pair<std::string, double>> ktime;
+  std::string err;
+  // Grow-only device scratch, reused across calls on this context.
+  void* scratch = nullptr;
+  size_t scratch_bytes = 0;
+  void* scratch2 = nullptr;
+  size_t scratch2_bytes = 0;
+  int* d_flag = nullptr;  // device error flag (bounded waits that gave up)
+};
+
+namespace dp {
+struct HostElement {
+  double Z, A, I, fraction;
+};
+struct HostMaterial {
+  std::string name;
+  double density = 0, I = 0, ZoA = 0;
+  std::vector<HostElement> elements;
+};
+void build_empirical_table(const HostMaterial& m, const dp_settings& st, int n, double Kmin,
+                           double Kmax, double* cols);
+double host_dcs_moment(int proc, double Z, double A, double I, double mass, double K, double xlo,
+                       double xhi, int mode);
+// Brackets one named kernel launch with events when timing is enabled; the
+// elapsed time is added to ctx->ktime[name] by timed_end (which waits for
+// the second event).
+void timed_begin(dp_ctx* ctx);
+void timed_end(dp_ctx* ctx, const char* name);
+// Sets ctx->err and returns code.
+int fail(dp_ctx* ctx, int code, const std::string& msg);
+int cuda_fail(dp_ctx* ctx, cudaError_t e, const char* where);
+// Ensures scratch slot `slot` (0 or 1) holds at least `bytes`; returns
+// nullptr on failure.  Slot contents do not survive a grow.
+void* scratch(dp_ctx* ctx, size_t bytes, int slot = 0);
+}  // namespace dp
+
+struct dp_physics {
+  dp_ctx* ctx = nullptr;
+  dp_settings settings{};
+  int n_mat = 0, n = 0, ld = 0;
+  std::vector<double> host;           // n_mat x DP_NCOL x n
+  std::vector<dp::HostMaterial> recipes;
+  bool has_recipes = false;
+  double* dev = nullptr;              // n_mat x DP_NCOL x ld
+  dp::TabView view{};
+};
+
+#define DP_CHECK_CUDA(ctx, call)                                  \
+  do {                                                            \
+    cudaError_t e_ = (call);                                      \
+    if (e_ != cudaSuccess) return dp::cuda_fail((ctx), e_, #call); \
+  } while (0)

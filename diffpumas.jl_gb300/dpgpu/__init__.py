@@ -1,0 +1,377 @@
+"""dpgpu -- Python host mirror of the DiffPumas.jl hot-path API on libdpgpu.
+
+Names and keyword arguments follow the reference (src/DiffPumas.jl exports):
+create_physics, get_material_index, run_backward_mc, compute_flux_differentiable,
+compute_flux_gradient, csda_energy_quadrature, and the voxel-density
+tomography forward / Jacobian / vector-Jacobian product.  Every computation
+runs in libdpgpu's CUDA kernels; there is no CPU fallback.
+"""
+import ctypes as C
+import math
+import threading
+from collections import namedtuple
+
+import numpy as np
+
+from . import _lib
+from ._lib import (COLUMNS, DpElement, DpGrid, DpMaterial, DpMcParams, DpMcResult, DpRay,
+                   DpSettings, DpTomoParams, check, load)
+
+MUON_MASS = 0.10565839
+MUON_C_TAU = 658.654
+PRIMARY_ALTITUDE = 3e4
+DEFAULT_CUTOFF = 5e-2
+DEFAULT_ELASTIC_RATIO = 5e-2
+
+
+# ----------------------------------------------------------------- context
+class Context:
+    """One CUDA stream on one device (dp_ctx)."""
+
+    def __init__(self, device=0):
+        lib = load()
+        h = C.c_void_p()
+        rc = lib.dp_init(device, C.byref(h))
+        if rc != 0:
+            raise _lib.DpError(rc, f"dp_init failed on device {device}")
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().dp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default = None
+_lock = threading.Lock()
+
+
+def default_context():
+    global _default
+    with _lock:
+        if _default is None:
+            _default = Context(0)
+        return _default
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+# ----------------------------------------------------------------- materials
+class Material:
+    """Elemental recipe (src/Materials.jl BaseMaterial): elements as
+    (Z, A, I[GeV], mass fraction)."""
+
+    def __init__(self, name, density, I, elements, ZoA=0.0):
+        self.name, self.density, self.I, self.ZoA = name, float(density), float(I), float(ZoA)
+        self.elements = [tuple(map(float, e)) for e in elements]
+
+    def to_c(self):
+        arr = (DpElement * len(self.elements))(*[DpElement(*e) for e in self.elements])
+        m = DpMaterial(self.name.encode(), self.density, self.I, self.ZoA, len(self.elements),
+                       C.cast(arr, C.POINTER(DpElement)))
+        return m, arr
+
+
+# src/Materials.jl:35-127
+_EL = {"H": (1.0, 1.00794, 19.2e-9), "C": (6.0, 12.0107, 78.0e-9), "N": (7.0, 14.0067, 82.0e-9),
+       "O": (8.0, 15.9994, 95.0e-9), "Na": (11.0, 22.9898, 149.0e-9),
+       "Mg": (12.0, 24.305, 156.0e-9), "Al": (13.0, 26.9815, 166.0e-9),
+       "Si": (14.0, 28.0855, 173.0e-9), "K": (19.0, 39.0983, 190.0e-9),
+       "Ca": (20.0, 40.078, 191.0e-9), "Fe": (26.0, 55.845, 286.0e-9),
+       "Ar": (18.0, 39.948, 188.0e-9)}
+
+
+def _recipe(name, density, I, comp):
+    return Material(name, density, I, [(*_EL[s], f) for s, f in comp])
+
+
+STANDARD_ROCK = _recipe("StandardRock", 2650.0, 136.4e-9,
+                        [("O", 0.466), ("Si", 0.277), ("Al", 0.081), ("Fe", 0.050),
+                         ("Ca", 0.036), ("Na", 0.028), ("Mg", 0.021), ("K", 0.026)])
+AIR = _recipe("Air", 1.205, 85.7e-9, [("N", 0.755), ("O", 0.232), ("Ar", 0.013)])
+WATER = _recipe("Water", 1000.0, 75.0e-9, [("H", 0.1119), ("O", 0.8881)])
+
+
+# ----------------------------------------------------------------- physics
+class Physics:
+    """Device-resident physics tables (dp_physics)."""
+
+    def __init__(self, handle, ctx, names, settings):
+        self.h, self.ctx, self.names, self.settings = handle, ctx, list(names), settings
+        n_mat, n = C.c_int(), C.c_int()
+        load().dp_physics_info(self.h, C.byref(n_mat), C.byref(n))
+        self.n_materials, self.n_energies = n_mat.value, n.value
+        self.mass = settings.mass
+        self.ctau = settings.ctau
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                load().dp_physics_free(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    @property
+    def materials(self):
+        return {n: i for i, n in enumerate(self.names)}
+
+    def column(self, mat, col):
+        out = np.zeros(self.n_energies)
+        check(load().dp_physics_column(self.h, int(mat), COLUMNS.index(col), _ptr(out)),
+              self.ctx.h)
+        return out
+
+    def table(self, mat):
+        return {c: self.column(mat, c) for c in COLUMNS}
+
+
+def _settings(mass=MUON_MASS, ctau=MUON_C_TAU, cutoff=DEFAULT_CUTOFF,
+              elastic_ratio=DEFAULT_ELASTIC_RATIO):
+    return DpSettings(mass, ctau, cutoff, elastic_ratio)
+
+
+def create_physics(particle="MUON", *, n_energies=200, K_min=1e-3, K_max=1e9,
+                   materials=(STANDARD_ROCK, AIR), cutoff=DEFAULT_CUTOFF,
+                   elastic_ratio=DEFAULT_ELASTIC_RATIO, ctx=None):
+    """create_physics (src/Physics.jl:534-599) with the empirical tables built
+    on the host by libdpgpu, then uploaded to the device."""
+    if particle != "MUON":
+        raise ValueError("only MUON physics is provided")
+    ctx = ctx or default_context()
+    st = _settings(cutoff=cutoff, elastic_ratio=elastic_ratio)
+    cs = [m.to_c() for m in materials]
+    arr = (DpMaterial * len(cs))(*[c[0] for c in cs])
+    h = C.c_void_p()
+    check(load().dp_physics_create(ctx.h, C.byref(st), len(cs), C.cast(arr, C.c_void_p),
+                                   n_energies, K_min, K_max, C.byref(h)), ctx.h)
+    return Physics(h, ctx, [m.name for m in materials], st)
+
+
+def upload_physics(tables, names, materials=None, *, mass=MUON_MASS, ctau=MUON_C_TAU,
+                   cutoff=DEFAULT_CUTOFF, elastic_ratio=DEFAULT_ELASTIC_RATIO, ctx=None):
+    """Uploads caller-built tables: `tables` is a list (one per material) of
+    dicts column-name -> array on one shared energy grid."""
+    ctx = ctx or default_context()
+    n = len(tables[0]["E"])
+    cols = np.zeros((len(tables), len(COLUMNS), n))
+    for m, t in enumerate(tables):
+        for c, name in enumerate(COLUMNS):
+            if name in t:
+                cols[m, c] = t[name]
+        if "logE" not in t:
+            cols[m, 1] = np.log(cols[m, 0])
+    st = DpSettings(mass, ctau, cutoff, elastic_ratio)
+    rec = None
+    keep = []
+    if materials is not None:
+        cs = [m.to_c() for m in materials]
+        keep.append(cs)
+        rec = (DpMaterial * len(cs))(*[c[0] for c in cs])
+    h = C.c_void_p()
+    cols = np.ascontiguousarray(cols)
+    check(load().dp_physics_upload(ctx.h, C.byref(st), len(tables), n, _ptr(cols),
+                                   C.cast(rec, C.c_void_p) if rec is not None else None,
+                                   C.byref(h)), ctx.h)
+    return Physics(h, ctx, names, st)
+
+
+def get_material_index(physics, name):
+    """1-based like the reference (src/Physics.jl:609); -1 when absent."""
+    i = physics.materials.get(name)
+    return -1 if i is None else i + 1
+
+
+# ----------------------------------------------------------------- backward MC
+MCResult = namedtuple("MCResult", "flux sigma gradient gradient_flux gradient_method "
+                                  "source_energy_max")
+
+
+def _mc_params(physics, rock_thickness, rock_density, elevation, energy_min, energy_max,
+               n_samples, compute_gradient, seed, straggling, scattering,
+               energy_threshold_low, source_energy_max, primary_altitude):
+    rock = physics.materials.get("StandardRock", 0)
+    air = physics.materials.get("Air", physics.n_materials - 1)
+    return DpMcParams(float(rock_thickness), float(rock_density), float(elevation),
+                      float(energy_min), float(energy_max if energy_max is not None else energy_min),
+                      int(n_samples), int(seed) & 0xFFFFFFFFFFFFFFFF, int(bool(straggling)),
+                      int(bool(scattering)), int(bool(compute_gradient)),
+                      float(energy_threshold_low),
+                      float(source_energy_max) if source_energy_max is not None else 0.0,
+                      float(primary_altitude), rock, air)
+
+
+def run_backward_mc(physics, *, rock_thickness=100.0, rock_density=2650.0, elevation=45.0,
+                    energy_min=1.0, energy_max=None, n_samples=10000, compute_gradient=False,
+                    seed=42, straggling=True, scattering=True, energy_threshold_low=100.0,
+                    source_energy_max=None, primary_altitude=PRIMARY_ALTITUDE):
+    """run_backward_mc (src/Geometry.jl:1286-1338).  Samples are drawn from a
+    Philox stream keyed by (seed, sample id)."""
+    p = _mc_params(physics, rock_thickness, rock_density, elevation, energy_min, energy_max,
+                   n_samples, compute_gradient, seed, straggling, scattering,
+                   energy_threshold_low, source_energy_max, primary_altitude)
+    out = DpMcResult()
+    check(load().dp_backward_mc(physics.ctx.h, physics.h, C.byref(p), C.byref(out)),
+          physics.ctx.h)
+    g = (out.gradient, out.gradient_flux, "deterministic_csda_sample_average") \
+        if compute_gradient else (None, None, None)
+    return MCResult(out.flux, out.sigma, g[0], g[1], g[2], out.source_energy_max)
+
+
+def mc_samples(physics, *, energy_min=1.0, energy_max=None, n_samples=10000, seed=42):
+    """The (energy, charge, weight) triples run_backward_mc draws."""
+    p = _mc_params(physics, 0, 0, 0, energy_min, energy_max, n_samples, False, seed, False,
+                   False, 100.0, None, PRIMARY_ALTITUDE)
+    E, q, w = (np.zeros(n_samples) for _ in range(3))
+    check(load().dp_mc_samples(physics.ctx.h, C.byref(p), n_samples, _ptr(E), _ptr(q), _ptr(w)),
+          physics.ctx.h)
+    return E, q, w
+
+
+def csda_flux_samples(physics, energy, charge, weight, *, rock_thickness, rock_density,
+                      elevation, source_energy_max=None, primary_altitude=PRIMARY_ALTITUDE,
+                      energy_threshold_low=100.0, steps=False):
+    """Per-history w*flux and w*d flux/d rho of the deterministic CSDA surrogate."""
+    E, q, w = _f64(energy), _f64(charge), _f64(weight)
+    n = len(E)
+    c, d = np.zeros(n), np.zeros(n)
+    st = np.zeros(n, np.int32) if steps else None
+    p = _mc_params(physics, rock_thickness, rock_density, elevation, 1.0, None, n, True, 0,
+                   False, False, energy_threshold_low, source_energy_max, primary_altitude)
+    check(load().dp_csda_flux_samples(physics.ctx.h, physics.h, C.byref(p), n, _ptr(E), _ptr(q),
+                                      _ptr(w), _ptr(c), _ptr(d),
+                                      _ptr(st) if st is not None else None), physics.ctx.h)
+    return (c, d, st) if steps else (c, d)
+
+
+def compute_flux_differentiable(physics, rock_density, rock_thickness, elevation, energy_final,
+                                charge, *, source_energy_max=None):
+    """compute_flux_differentiable (src/Geometry.jl:958-986), CSDA."""
+    c, _ = csda_flux_samples(physics, [energy_final], [charge], [1.0],
+                             rock_thickness=rock_thickness, rock_density=rock_density,
+                             elevation=elevation, source_energy_max=source_energy_max)
+    return float(c[0])
+
+
+def compute_flux_gradient(physics, rock_density, rock_thickness, elevation, energy_final, charge,
+                          *, source_energy_max=None):
+    """compute_flux_gradient (src/Geometry.jl:1007-1028): (flux, d flux/d rho)."""
+    c, d = csda_flux_samples(physics, [energy_final], [charge], [1.0],
+                             rock_thickness=rock_thickness, rock_density=rock_density,
+                             elevation=elevation, source_energy_max=source_energy_max)
+    return float(c[0]), float(d[0])
+
+
+# ----------------------------------------------------------------- tomography
+def csda_energy_quadrature(n, energy_min, energy_max):
+    """Log-midpoint nodes with charge 0 and half weights (src/Tomography.jl:263-274)."""
+    if n <= 0:
+        raise ValueError("CSDA quadrature requires at least one energy node")
+    if not (math.isfinite(energy_min) and math.isfinite(energy_max) and 0 < energy_min < energy_max):
+        raise ValueError("CSDA quadrature requires finite 0 < energy_min < energy_max")
+    lo = math.log(energy_min)
+    span = math.log(energy_max) - lo
+    E = np.array([math.exp(lo + span * (i - 0.5) / n) for i in range(1, n + 1)])
+    return E, np.zeros(n), 0.5 * E * span
+
+
+class VoxelGrid:
+    """Regular density grid; cell c = i + nx*(j + ny*k) (x fastest)."""
+
+    def __init__(self, nx, ny, nz, origin, pitch):
+        self.nx, self.ny, self.nz = int(nx), int(ny), int(nz)
+        self.origin = tuple(map(float, origin))
+        self.pitch = tuple(map(float, pitch)) if np.ndim(pitch) else (float(pitch),) * 3
+
+    @property
+    def ncell(self):
+        return self.nx * self.ny * self.nz
+
+    def to_c(self):
+        return DpGrid(self.nx, self.ny, self.nz, *self.origin, *self.pitch)
+
+
+def make_rays(origins, zenith_deg, azimuth_deg):
+    """Rays from detector points: direction (sin t sin p, sin t cos p, cos t)
+    (the direction convention of examples/diff_flux_cube.jl:326-333)."""
+    o = np.asarray(origins, np.float64).reshape(-1, 3)
+    th, ph = np.deg2rad(np.asarray(zenith_deg, np.float64)), np.deg2rad(np.asarray(azimuth_deg, np.float64))
+    r = np.zeros((len(o), 7))
+    r[:, :3] = o
+    st = np.sin(th)
+    r[:, 3] = st * np.sin(ph)
+    r[:, 4] = st * np.cos(ph)
+    r[:, 5] = np.cos(th)
+    r[:, 6] = np.cos(th)
+    return r
+
+
+class TomoModel:
+    """Voxel-density CSDA forward model with its adjoint on one grid."""
+
+    def __init__(self, physics, grid, nodes, *, rock="StandardRock", air="Air", side_cell=-1,
+                 side_density=2650.0, primary_altitude=PRIMARY_ALTITUDE):
+        self.physics, self.grid = physics, grid
+        self.nE, self.nq, self.nw = (_f64(x) for x in nodes)
+        self.params = DpTomoParams(physics.materials[rock], physics.materials[air],
+                                   int(side_cell), float(side_density), float(primary_altitude),
+                                   len(self.nE), _ptr(self.nE).value, _ptr(self.nq).value,
+                                   _ptr(self.nw).value)
+        self._g = grid.to_c()
+
+    def _args(self, rho, rays):
+        rho = _f64(rho).ravel()
+        if rho.size != self.grid.ncell:
+            raise ValueError("density array does not match the grid")
+        rays = _f64(rays).reshape(-1, 7)
+        return rho, rays
+
+    def forward(self, rho, rays):
+        rho, rays = self._args(rho, rays)
+        out = np.zeros(len(rays))
+        check(load().dp_tomo_forward(self.physics.ctx.h, self.physics.h, C.byref(self._g),
+                                     C.byref(self.params), _ptr(rho), len(rays), _ptr(rays),
+                                     _ptr(out)), self.physics.ctx.h)
+        return out
+
+    def jacobian(self, rho, rays):
+        """(flux, row_ptr, col, val): one entry per traversed segment (col -1:
+        the side-exit remainder when its density is a fixed value)."""
+        rho, rays = self._args(rho, rays)
+        n = len(rays)
+        flux = np.zeros(n)
+        rp = np.zeros(n + 1, np.int64)
+        cap = n * (self.grid.nx + self.grid.ny + self.grid.nz + 66)
+        col = np.zeros(cap, np.int32)
+        val = np.zeros(cap)
+        nnz = C.c_int64()
+        check(load().dp_tomo_jacobian(self.physics.ctx.h, self.physics.h, C.byref(self._g),
+                                      C.byref(self.params), _ptr(rho), n, _ptr(rays), _ptr(flux),
+                                      _ptr(rp), _ptr(col), _ptr(val), cap, C.byref(nnz)),
+              self.physics.ctx.h)
+        k = nnz.value
+        return flux, rp, col[:k].copy(), val[:k].copy()
+
+    def vjp(self, rho, rays, cot):
+        """(flux, J^T cot) with a deterministic reduction."""
+        rho, rays = self._args(rho, rays)
+        cot = _f64(cot)
+        flux = np.zeros(len(rays))
+        grad = np.zeros(self.grid.ncell)
+        check(load().dp_tomo_vjp(self.physics.ctx.h, self.physics.h, C.byref(self._g),
+                                 C.byref(self.params), _ptr(rho), len(rays), _ptr(rays),
+                                 _ptr(cot), _ptr(flux), _ptr(grad)), self.physics.ctx.h)
+        return flux, grad

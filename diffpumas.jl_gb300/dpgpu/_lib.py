@@ -1,0 +1,141 @@
+"""ctypes binding of libdpgpu.so (the C ABI declared in include/dpgpu.h).
+
+The shared library is built in-tree by diffpumas.jl_gb300/build.py.  There is
+no fallback: if the library is missing or no CUDA device is visible, the calls
+raise.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.normpath(os.path.join(HERE, "..", "_build", "libdpgpu.so"))
+
+DP_OK, DP_ERR_ARG, DP_ERR_CUDA, DP_ERR_DOMAIN, DP_ERR_ALLOC, DP_ERR_STATE = 0, -1, -2, -3, -4, -5
+
+COLUMNS = ["E", "logE", "csda_S", "csda_R", "csda_T", "mixed_S", "mixed_R", "strag", "ion",
+           "brems", "pair", "photo", "xs", "lb1", "lbe", "ecut", "magrot", "mu0", "fspin"]
+NCOL = len(COLUMNS)
+
+
+class DpElement(C.Structure):
+    _fields_ = [("Z", C.c_double), ("A", C.c_double), ("I", C.c_double),
+                ("fraction", C.c_double)]
+
+
+class DpMaterial(C.Structure):
+    _fields_ = [("name", C.c_char_p), ("density", C.c_double), ("I", C.c_double),
+                ("ZoA", C.c_double), ("n_elements", C.c_int),
+                ("elements", C.POINTER(DpElement))]
+
+
+class DpSettings(C.Structure):
+    _fields_ = [("mass", C.c_double), ("ctau", C.c_double), ("cutoff", C.c_double),
+                ("elastic_ratio", C.c_double)]
+
+
+class DpMcParams(C.Structure):
+    _fields_ = [("rock_thickness", C.c_double), ("rock_density", C.c_double),
+                ("elevation", C.c_double), ("energy_min", C.c_double),
+                ("energy_max", C.c_double), ("n_samples", C.c_long), ("seed", C.c_uint64),
+                ("straggling", C.c_int), ("scattering", C.c_int),
+                ("compute_gradient", C.c_int), ("energy_threshold_low", C.c_double),
+                ("source_energy_max", C.c_double), ("primary_altitude", C.c_double),
+                ("rock_material", C.c_int), ("air_material", C.c_int)]
+
+
+class DpMcResult(C.Structure):
+    _fields_ = [("flux", C.c_double), ("sigma", C.c_double), ("gradient", C.c_double),
+                ("gradient_flux", C.c_double), ("source_energy_max", C.c_double),
+                ("n_samples", C.c_long), ("n_status_nonzero", C.c_long)]
+
+
+class DpGrid(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("x0", C.c_double),
+                ("y0", C.c_double), ("z0", C.c_double), ("dx", C.c_double),
+                ("dy", C.c_double), ("dz", C.c_double)]
+
+
+class DpRay(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("ox", "oy", "oz", "ux", "uy", "uz", "cos_theta")]
+
+
+class DpTomoParams(C.Structure):
+    _fields_ = [("rock_material", C.c_int), ("air_material", C.c_int), ("side_cell", C.c_int),
+                ("side_density", C.c_double), ("primary_altitude", C.c_double),
+                ("n_nodes", C.c_int), ("node_energy", C.c_void_p),
+                ("node_charge", C.c_void_p), ("node_weight", C.c_void_p)]
+
+
+_P = C.c_void_p
+_D = C.c_double
+_I = C.c_int
+_L = C.c_long
+_VP = C.c_void_p
+
+# name -> (restype, argtypes); pointers to arrays are passed as c_void_p.
+PROTOTYPES = {
+    "dp_version": (_I, []),
+    "dp_init": (_I, [_I, C.POINTER(_P)]),
+    "dp_destroy": (_I, [_P]),
+    "dp_last_error": (C.c_char_p, [_P]),
+    "dp_set_stream": (_I, [_P, _VP]),
+    "dp_get_stream": (_VP, [_P]),
+    "dp_set_timing": (_I, [_P, _I]),
+    "dp_kernel_time": (_I, [_P, C.c_char_p, C.POINTER(_D)]),
+    "dp_launch_count": (C.c_longlong, [_P]),
+    "dp_physics_upload": (_I, [_P, C.POINTER(DpSettings), _I, _I, _VP, _VP, C.POINTER(_P)]),
+    "dp_physics_create": (_I, [_P, C.POINTER(DpSettings), _I, _VP, _I, _D, _D, C.POINTER(_P)]),
+    "dp_physics_free": (_I, [_P]),
+    "dp_physics_info": (_I, [_P, C.POINTER(_I), C.POINTER(_I)]),
+    "dp_physics_column": (_I, [_P, _I, _I, _VP]),
+    "dp_physics_material_index": (_I, [_P, C.c_char_p]),
+    "dp_backward_mc": (_I, [_P, _P, C.POINTER(DpMcParams), C.POINTER(DpMcResult)]),
+    "dp_csda_flux_samples": (_I, [_P, _P, C.POINTER(DpMcParams), _L, _VP, _VP, _VP, _VP, _VP,
+                                  _VP]),
+    "dp_csda_flux_samples_dev": (_I, [_P, _P, C.POINTER(DpMcParams), _L, _VP, _VP, _VP, _VP,
+                                      _VP, _VP]),
+    "dp_mc_samples": (_I, [_P, C.POINTER(DpMcParams), _L, _VP, _VP, _VP]),
+    "dp_tomo_forward": (_I, [_P, _P, C.POINTER(DpGrid), C.POINTER(DpTomoParams), _VP, _L, _VP,
+                             _VP]),
+    "dp_tomo_jacobian": (_I, [_P, _P, C.POINTER(DpGrid), C.POINTER(DpTomoParams), _VP, _L, _VP,
+                              _VP, _VP, _VP, _VP, C.c_int64, C.POINTER(C.c_int64)]),
+    "dp_tomo_vjp": (_I, [_P, _P, C.POINTER(DpGrid), C.POINTER(DpTomoParams), _VP, _L, _VP, _VP,
+                         _VP, _VP]),
+    "dp_tomo_vjp_dev": (_I, [_P, _P, C.POINTER(DpGrid), C.POINTER(DpTomoParams), _VP, _L, _VP,
+                             _VP, _VP, _VP]),
+    "dp_tomo_forward_plain_dev": (_I, [_P, _P, C.POINTER(DpGrid), C.POINTER(DpTomoParams), _VP,
+                                       _L, _VP, _VP]),
+}
+
+_lib = None
+
+
+def load():
+    """Loads libdpgpu.so and declares every prototype; raises if missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libdpgpu.so not built ({LIB_PATH}); run "
+                               "python diffpumas.jl_gb300/build.py")
+        lib = C.CDLL(LIB_PATH)
+        for name, (res, args) in PROTOTYPES.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+    return _lib
+
+
+class DpError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"libdpgpu error {code}: {msg}")
+        self.code = code
+
+
+def check(rc, ctx=None):
+    if rc != DP_OK:
+        msg = load().dp_last_error(ctx).decode() if ctx else ""
+        if rc == DP_ERR_ARG:
+            raise ValueError(msg or "invalid argument")
+        raise DpError(rc, msg)
+    return rc

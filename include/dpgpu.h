@@ -1,0 +1,256 @@
+/* dpgpu.h -- C ABI of libdpgpu.so, the GB300 (sm_103a) implementation of the
+ * DiffPumas.jl data-parallel hot path: backward Monte Carlo muon transport
+ * (run_backward_mc) and the voxel-density tomography forward model with its
+ * density adjoint.
+ *
+ * Plain C types only.  Every entry point returns 0 on success, a negative
+ * DP_ERR_* code on misuse or CUDA failure (dp_last_error() gives the text),
+ * never aborts.  One CUDA stream per context; calls on one context must be
+ * serialised by the caller; contexts may be used from different threads.
+ * Device memory is owned by the handles.  Host arrays are borrowed for the
+ * duration of a call.  "_dev" variants take device pointers that must stay
+ * valid until the call returns (the call synchronises its stream).
+ *
+ * Reference citations are paths inside the DiffPumas.jl project.
+ */
+#ifndef DPGPU_H
+#define DPGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DPGPU_VERSION 1
+
+/* Return codes */
+#define DP_OK 0
+#define DP_ERR_ARG (-1)     /* ArgumentError in the reference */
+#define DP_ERR_CUDA (-2)
+#define DP_ERR_DOMAIN (-3)  /* DomainError in the reference (table domain) */
+#define DP_ERR_ALLOC (-4)
+#define DP_ERR_STATE (-5)   /* loop/iteration cap reached: status words tell which */
+
+/* Per-history status bits (MC kernels write one int32 per history when asked).
+ * They map to the reference throw sites and loop caps:
+ *   DP_ST_STEP_CAP   50000 inner steps (src/Geometry.jl:593)
+ *   DP_ST_OUTER_CAP  outer mode loop cap (no reference counterpart; 10^6)
+ *   DP_ST_EVENT_CAP  100000 hard events (src/MixedTransport.jl:157)
+ *   DP_ST_DOMAIN_HI  energy above the prepared tables (src/MixedTransport.jl:45,155,196) */
+#define DP_ST_OK 0
+#define DP_ST_STEP_CAP 1
+#define DP_ST_OUTER_CAP 2
+#define DP_ST_EVENT_CAP 4
+#define DP_ST_DOMAIN_HI 8
+#define DP_ST_DOMAIN_LO 16
+
+typedef struct dp_ctx dp_ctx;
+typedef struct dp_physics dp_physics;
+
+/* ------------------------------------------------------------------ context */
+int dp_version(void);
+/* Creates a context on CUDA device `device` with its own stream. */
+int dp_init(int device, dp_ctx** out);
+int dp_destroy(dp_ctx* ctx);
+/* Text of the last error raised on this context ("" if none). */
+const char* dp_last_error(const dp_ctx* ctx);
+/* Makes the context launch on the caller's cudaStream_t (e.g. a CUDA.jl or
+ * torch stream); NULL restores the context's own stream. */
+int dp_set_stream(dp_ctx* ctx, void* cuda_stream);
+void* dp_get_stream(const dp_ctx* ctx);
+/* Per-kernel timing with CUDA events on the context stream (off by default;
+ * enabling it serialises each timed launch).  Names: "csda_mc", "tomo_forward",
+ * "tomo_adjoint", "tomo_transpose". */
+int dp_set_timing(dp_ctx* ctx, int enable);
+int dp_kernel_time(const dp_ctx* ctx, const char* kernel, double* ms_total);
+/* Number of kernels this context has launched. */
+long long dp_launch_count(const dp_ctx* ctx);
+
+/* ------------------------------------------------------------------ physics tables
+ * Column layout of one material table (src/Physics.jl:64-102 MaterialTable).
+ * Every column holds n_energies doubles on the material's kinetic-energy grid. */
+enum dp_column {
+  DP_COL_E = 0,          /* kinetic energy, GeV */
+  DP_COL_LOGE,           /* log(E) */
+  DP_COL_CSDA_S,         /* CSDA stopping power, GeV/(kg/m^2) */
+  DP_COL_CSDA_R,         /* CSDA range, kg/m^2 */
+  DP_COL_CSDA_T,         /* CSDA proper-time integral, kg/m^2 */
+  DP_COL_MIXED_S,        /* restricted (soft) stopping power */
+  DP_COL_MIXED_R,        /* restricted range */
+  DP_COL_STRAG,          /* straggling variance, GeV^2/(kg/m^2) */
+  DP_COL_ION,            /* ionisation stopping power */
+  DP_COL_BREMS,
+  DP_COL_PAIR,
+  DP_COL_PHOTO,
+  DP_COL_XS,             /* hard-event cross section, m^2/kg */
+  DP_COL_LB1,            /* first transport path, kg/m^2 */
+  DP_COL_LBE,            /* elastic path x p^2 */
+  DP_COL_ECUT,           /* elastic cutoff angle */
+  DP_COL_MAGROT,         /* magnetic rotation */
+  DP_COL_MU0,            /* Coulomb screening parameter */
+  DP_COL_FSPIN,          /* spin factor */
+  DP_NCOL
+};
+
+typedef struct {
+  double Z, A, I;        /* atomic number, mass number (g/mol), mean excitation (GeV) */
+  double fraction;       /* mass fraction */
+} dp_element;
+
+typedef struct {
+  const char* name;
+  double density;        /* reference density, kg/m^3 */
+  double I;              /* mean excitation energy, GeV */
+  double ZoA;            /* <Z/A> (0: computed from the elements) */
+  int n_elements;
+  const dp_element* elements;
+} dp_material;
+
+typedef struct {
+  double mass;           /* GeV/c^2 (muon 0.10565839) */
+  double ctau;           /* m (muon 658.654) */
+  double cutoff;         /* relative soft/hard cutoff (0.05) */
+  double elastic_ratio;  /* (0.05) */
+} dp_settings;
+
+/* Uploads caller-built tables (the Julia create_physics output) to the device.
+ * columns: n_materials x DP_NCOL x n_energies doubles, row-major in that order.
+ * All materials share one energy grid.  recipes may be NULL (then hard-event
+ * sampling, which needs the elemental recipes, is unavailable).
+ * Replaces the table handover of src/Physics.jl:534-599 (create_physics). */
+int dp_physics_upload(dp_ctx* ctx, const dp_settings* settings, int n_materials,
+                      int n_energies, const double* columns, const dp_material* recipes,
+                      dp_physics** out);
+
+/* Builds tables on the host exactly as create_physics(MUON) does without PUMAS
+ * dE/dx files (empirical DCS integration, src/Physics.jl:280-408, 534-599),
+ * on a log grid of n_energies nodes in [K_min, K_max], then uploads them. */
+int dp_physics_create(dp_ctx* ctx, const dp_settings* settings, int n_materials,
+                      const dp_material* materials, int n_energies, double K_min, double K_max,
+                      dp_physics** out);
+int dp_physics_free(dp_physics* phys);
+int dp_physics_info(const dp_physics* phys, int* n_materials, int* n_energies);
+/* Copies column `col` of material `mat` (host copy of the device tables). */
+int dp_physics_column(const dp_physics* phys, int mat, int col, double* out);
+/* Index of the material with this name, or -1 (src/Physics.jl:609 get_material_index). */
+int dp_physics_material_index(const dp_physics* phys, const char* name);
+
+/* ------------------------------------------------------------------ backward MC
+ * run_backward_mc (src/Geometry.jl:1286-1338) on a two-layer rock + air column. */
+typedef struct {
+  double rock_thickness;     /* m */
+  double rock_density;       /* kg/m^3 */
+  double elevation;          /* degrees */
+  double energy_min;         /* GeV */
+  double energy_max;         /* GeV (<= energy_min: single energy) */
+  long n_samples;
+  uint64_t seed;             /* Philox key; stream keyed by (seed, sample id) */
+  int straggling;            /* 0: CSDA */
+  int scattering;
+  int compute_gradient;
+  double energy_threshold_low; /* GeV (100) */
+  double source_energy_max;  /* GeV, <= 0: min(1e9, table max) */
+  double primary_altitude;   /* m (3e4) */
+  int rock_material;         /* -1: "StandardRock" or 0 */
+  int air_material;          /* -1: "Air" or the last table */
+} dp_mc_params;
+
+typedef struct {
+  double flux, sigma;        /* estimate and standard error */
+  double gradient;           /* d(CSDA sample-average flux)/d(rock_density) */
+  double gradient_flux;      /* the CSDA surrogate's flux */
+  double source_energy_max;
+  long n_samples;
+  long n_status_nonzero;     /* histories that hit a cap (see DP_ST_*) */
+} dp_mc_result;
+
+/* Whole estimator: device sampling, transport, deterministic reduction.
+ * CSDA mode only in this version (straggling = 0, scattering = 0). */
+int dp_backward_mc(dp_ctx* ctx, const dp_physics* phys, const dp_mc_params* p,
+                   dp_mc_result* out);
+
+/* Deterministic CSDA flux of explicit histories (compute_flux_differentiable,
+ * src/Geometry.jl:958-986, and its Zygote gradient :1007-1028): contrib[i] =
+ * w[i]*flux_i and dcontrib[i] = w[i]*d flux_i/d rho.  Host pointers. */
+int dp_csda_flux_samples(dp_ctx* ctx, const dp_physics* phys, const dp_mc_params* p,
+                         long n, const double* energy, const double* charge,
+                         const double* weight, double* contrib, double* dcontrib,
+                         int32_t* steps);
+/* Same with device pointers (inputs resident in HBM). */
+int dp_csda_flux_samples_dev(dp_ctx* ctx, const dp_physics* phys, const dp_mc_params* p,
+                             long n, const double* energy, const double* charge,
+                             const double* weight, double* contrib, double* dcontrib,
+                             int32_t* steps);
+/* Philox samples exactly as dp_backward_mc draws them (log-uniform energy,
+ * +-1 charge, weight 2*E*log(Emax/Emin)), for parity checks.  Host pointers. */
+int dp_mc_samples(dp_ctx* ctx, const dp_mc_params* p, long n, double* energy,
+                  double* charge, double* weight);
+
+/* ------------------------------------------------------------------ tomography
+ * Voxel-density CSDA forward model (examples/diff_flux_cube.jl:304-557):
+ * ray march through a regular grid, per-segment range inversion, decay,
+ * side-exit rock remainder, closed-form air, GCCLY flux, integrated over
+ * energy nodes: flux_r = (1/N) sum_n 2 w_n f(E_n, q_n). */
+typedef struct {
+  int nx, ny, nz;
+  double x0, y0, z0;         /* lower corner; z0 is the detector level */
+  double dx, dy, dz;         /* pitch, m */
+} dp_grid;
+
+typedef struct {
+  double ox, oy, oz;         /* start point */
+  double ux, uy, uz;         /* unit direction, upward (uz > 0) */
+  double cos_theta;          /* cosine of the zenith angle */
+} dp_ray;
+
+typedef struct {
+  int rock_material, air_material;
+  int side_cell;             /* side-exit remainder density: rho[side_cell], or
+                                side_density when side_cell < 0 */
+  double side_density;
+  double primary_altitude;   /* m */
+  int n_nodes;
+  const double* node_energy; /* host pointers, n_nodes each */
+  const double* node_charge;
+  const double* node_weight;
+} dp_tomo_params;
+
+/* Per-ray flux.  rho: nx*ny*nz doubles (x fastest).  Host pointers. */
+int dp_tomo_forward(dp_ctx* ctx, const dp_physics* phys, const dp_grid* grid,
+                    const dp_tomo_params* tp, const double* rho, long n_rays,
+                    const dp_ray* rays, double* flux);
+/* Per-ray flux and the sparse Jacobian d flux_r / d rho_c in CSR form:
+ * row_ptr[n_rays+1]; col/val hold one entry per traversed segment (a cell
+ * crossed twice appears twice), in traversal order.  nnz_cap bounds col/val;
+ * *nnz receives the count (DP_ERR_ARG if it exceeds nnz_cap).  Host pointers.
+ * Replaces assemble_forward_and_jacobian (src/Tomography.jl:773-820) and the
+ * Zygote gradient of compute_flux_gradient_cube (examples/diff_flux_cube.jl:489). */
+int dp_tomo_jacobian(dp_ctx* ctx, const dp_physics* phys, const dp_grid* grid,
+                     const dp_tomo_params* tp, const double* rho, long n_rays,
+                     const dp_ray* rays, double* flux, int64_t* row_ptr, int32_t* col,
+                     double* val, int64_t nnz_cap, int64_t* nnz);
+/* Vector-Jacobian product: grad_rho[c] = sum_r cot[r] d flux_r / d rho_c,
+ * with a deterministic segmented reduction (no floating-point atomics):
+ * the result is bitwise reproducible.  Also returns the per-ray flux.
+ * Host pointers. */
+int dp_tomo_vjp(dp_ctx* ctx, const dp_physics* phys, const dp_grid* grid,
+                const dp_tomo_params* tp, const double* rho, long n_rays,
+                const dp_ray* rays, const double* cot, double* flux, double* grad_rho);
+/* Device-pointer form of dp_tomo_vjp (cot may be NULL: flux only). */
+int dp_tomo_vjp_dev(dp_ctx* ctx, const dp_physics* phys, const dp_grid* grid,
+                    const dp_tomo_params* tp, const double* rho, long n_rays,
+                    const dp_ray* rays, const double* cot, double* flux, double* grad_rho);
+
+/* ------------------------------------------------------------------ plain baseline
+ * Plain FP64 GPU form used as the speed-up denominator: one kernel launch per
+ * ray, one thread per energy node, tables read from global memory with binary
+ * search, no staging, no batching.  Device pointers; flux only. */
+int dp_tomo_forward_plain_dev(dp_ctx* ctx, const dp_physics* phys, const dp_grid* grid,
+                              const dp_tomo_params* tp, const double* rho, long n_rays,
+                              const dp_ray* rays, double* flux);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DPGPU_H */
