@@ -300,13 +300,16 @@ def cpu_baseline(workload, budget_s=15.0, threads=None):
         dims = np.array([grid.nx, grid.ny, grid.nz], np.int32)
         geom = np.array([*grid.origin, *grid.pitch])
         n, t0 = 0, time.perf_counter()
-        while time.perf_counter() - t0 < budget_s and n < len(rays):
-            chunk = rays[n:n + 256]
-            O.tomo_forward(p, 0, 1, dims, geom, rho, 2500.0, chunk, nodes, threads=threads)
+        while time.perf_counter() - t0 < budget_s:
+            i = n % len(rays)
+            chunk = rays[i:i + 512]
+            O.tomo_vjp(p, 0, 1, dims, geom, rho, 2500.0, chunk, nodes, np.ones(len(chunk)),
+                       threads=threads)
             n += len(chunk)
         dt = time.perf_counter() - t0
         return {"value": n / dt, "unit": "rays/s", "cores": threads, "kind": "port",
-                "sample": f"{n} rays of the c3 workload, forward flux only (FP64 oracle, OpenMP)"}
+                "sample": f"{n} rays of the c3 workload (cycled), forward flux + reverse-sweep "
+                          "J^T r (FP64 oracle, OpenMP)"}
     p = O.default_physics((O.STANDARD_ROCK, O.AIR))
     rng = np.random.default_rng(0)
     n, t0 = 0, time.perf_counter()

@@ -22,7 +22,8 @@ def gaussian_random_field(shape, pitch, corr_length, mean, sd, rng):
     # convolution with a Gaussian kernel of sd corr_length/sqrt(2) gives a
     # Gaussian covariance of sd corr_length
     s = corr_length / np.sqrt(2.0)
-    field = np.fft.irfftn(np.fft.rfftn(white) * np.exp(-0.5 * k2 * s * s), s=shape)
+    spec = np.fft.rfftn(white, axes=(0, 1, 2)) * np.exp(-0.5 * k2 * s * s)
+    field = np.fft.irfftn(spec, s=shape, axes=(0, 1, 2))
     field = (field - field.mean()) / field.std()
     return mean + sd * field
 
@@ -36,8 +37,9 @@ def density_field(nx, ny, nz, pitch, origin, *, seed, mean=2500.0, sd=150.0, cor
     ys = origin[1] + (np.arange(ny) + 0.5) * pitch
     zs = origin[2] + (np.arange(nz) + 0.5) * pitch
     Z, Y, X = np.meshgrid(zs, ys, xs, indexing="ij")
+    rmax_fit = 0.45 * min(nx, ny, nz) * pitch
     for _ in range(n_cavities):
-        r = rng.uniform(*radius)
+        r = min(rng.uniform(*radius), rmax_fit)
         c = [rng.uniform(origin[0] + r, origin[0] + nx * pitch - r),
              rng.uniform(origin[1] + r, origin[1] + ny * pitch - r),
              rng.uniform(origin[2] + r, origin[2] + nz * pitch - r)]

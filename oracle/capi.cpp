@@ -4,6 +4,9 @@
 #include <cstring>
 #include <map>
 #include <set>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #include "oracle.hpp"
 
@@ -214,6 +217,50 @@ void orc_tomo_forward(void* h, int rock, int air, const int* dims, const double*
       s += 2.0 * nw[k] *
            tomo_flux_node<double>(*p, rock, air, g, tr, q[6], rho, rho_side, -1, nE[k], nq[k], H);
     flux[r] = s / n_nodes;
+  }
+}
+
+// Forward + reverse-mode adjoint for many rays: flux[r] and
+// grad[c] = sum_r cot[r] d flux_r / d rho_c (side-exit remainder at the fixed
+// rho_side is not a cell).  Per-thread accumulators, summed in thread order.
+void orc_tomo_vjp(void* h, int rock, int air, const int* dims, const double* geom,
+                  const double* rho, double rho_side, double H, long n_rays, const double* rays,
+                  int n_nodes, const double* nE, const double* nq, const double* nw,
+                  const double* cot, double* flux, double* grad, int nthreads) {
+  Physics* p = static_cast<Physics*>(h);
+  Grid g{dims[0], dims[1], dims[2], geom[0], geom[1], geom[2], geom[3], geom[4], geom[5]};
+  long ncell = long(g.nx) * g.ny * g.nz;
+  std::vector<std::vector<double>> acc(nthreads > 0 ? nthreads : 1);
+#pragma omp parallel num_threads(nthreads)
+  {
+    int tid = 0;
+#ifdef _OPENMP
+    tid = omp_get_thread_num();
+#endif
+    std::vector<double>& a = acc[tid];
+    a.assign(ncell, 0.0);
+    std::vector<double> dseg, tot;
+#pragma omp for schedule(dynamic, 4)
+    for (long r = 0; r < n_rays; ++r) {
+      const double* q = rays + 7 * r;
+      Ray ray{q[0], q[1], q[2], q[3], q[4], q[5], q[6]};
+      RayTrace tr = trace_ray(g, ray);
+      double f = 0;
+      tot.assign(tr.seg.size() + 1, 0.0);
+      for (int k = 0; k < n_nodes; ++k) {
+        double c = 2.0 * nw[k] / n_nodes;
+        f += c * tomo_node_adjoint(*p, rock, air, g, tr, q[6], rho, rho_side, nE[k], nq[k], H, dseg);
+        for (size_t s = 0; s < dseg.size() && s < tr.seg.size(); ++s) tot[s] += c * dseg[s];
+      }
+      flux[r] = f;
+      for (size_t s = 0; s < tr.seg.size(); ++s) a[tr.seg[s].cell] += cot[r] * tot[s];
+    }
+  }
+  for (long c = 0; c < ncell; ++c) {
+    double s = 0;
+    for (auto& a : acc)
+      if (!a.empty()) s += a[c];
+    grad[c] = s;
   }
 }
 

@@ -264,6 +264,9 @@ struct RayTrace {
 RayTrace trace_ray(const Grid& g, const Ray& r);
 // Density of cell c (or the side-exit remainder when c < 0) with a tangent of
 // one on the seeded cell (seed == -2 seeds the side-exit density).
+double tomo_node_adjoint(const Physics& p, int rock, int air, const Grid& g, const RayTrace& tr,
+                         double cos_theta, const double* rho, double rho_side, double energy,
+                         double charge, double H, std::vector<double>& dseg);
 template <class T>
 T tomo_flux_node(const Physics& p, int rock, int air, const Grid& g,
                  const RayTrace& tr, double cos_theta, const double* rho,

@@ -81,6 +81,8 @@ def lib():
         L.orc_trace_ray.argtypes = [_IP, _DP, _DP, _I, _IP, _DP, C.POINTER(_D)]
         L.orc_tomo_forward.argtypes = [_P, _I, _I, _IP, _DP, _DP, _D, _D, _L, _DP, _I, _DP, _DP,
                                        _DP, _DP, _I]
+        L.orc_tomo_vjp.argtypes = [_P, _I, _I, _IP, _DP, _DP, _D, _D, _L, _DP, _I, _DP, _DP, _DP,
+                                   _DP, _DP, _DP, _I]
         L.orc_tomo_ray_grad.restype = _I
         L.orc_tomo_ray_grad.argtypes = [_P, _I, _I, _IP, _DP, _DP, _D, _D, _DP, _I, _DP, _DP,
                                         _DP, C.POINTER(_D), _I, _IP, _DP, C.POINTER(_D)]
@@ -231,6 +233,19 @@ def tomo_forward(p, rock, air, dims, geom, rho, rho_side, rays, nodes, H=3e4, th
                            _arr(rho).ravel(), rho_side, H, len(rays), rays.ravel(), len(E), E, q,
                            w, out, threads)
     return out
+
+
+def tomo_vjp(p, rock, air, dims, geom, rho, rho_side, rays, nodes, cot, H=3e4, threads=0):
+    """Forward flux and J^T cot by the oracle's reverse sweep (all threads)."""
+    rays = _arr(rays).reshape(-1, 7)
+    flux = np.zeros(len(rays))
+    rho = _arr(rho).ravel()
+    grad = np.zeros(rho.size)
+    E, q, w = (_arr(x) for x in nodes)
+    threads = threads or os.cpu_count()
+    lib().orc_tomo_vjp(p.h, rock, air, np.asarray(dims, np.int32), _arr(geom), rho, rho_side, H,
+                       len(rays), rays.ravel(), len(E), E, q, w, _arr(cot), flux, grad, threads)
+    return flux, grad
 
 
 def tomo_ray_grad(p, rock, air, dims, geom, rho, rho_side, ray, nodes, H=3e4, cap=4096):

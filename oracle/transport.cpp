@@ -320,4 +320,66 @@ double tomo_flux_node<double>(const Physics& p, int rock, int air, const Grid& g
 template Dual tomo_flux_node<Dual>(const Physics&, int, int, const Grid&, const RayTrace&,
                                    double, const double*, double, int, double, double, double);
 
+// Reverse-mode derivative of tomo_flux_node with respect to every segment
+// density (the side-exit remainder last), by a backward sweep over the stored
+// forward energies -- the CPU counterpart of the GPU adjoint, used to time the
+// CPU baseline of forward + adjoint.  Returns the flux; dseg gets one entry per
+// segment (+1 if there is a side-exit remainder).
+double tomo_node_adjoint(const Physics& p, int rock, int air, const Grid& g, const RayTrace& tr,
+                         double cos_theta, const double* rho, double rho_side, double energy,
+                         double charge, double H, std::vector<double>& dseg) {
+  const MaterialTable &trk = p.t[rock], &ta = p.t[air];
+  double zmax = g.z0 + g.nz * g.dz;
+  double cs = std::max(std::fabs(cos_theta), 0.01);
+  size_t ns = tr.seg.size();
+  bool side = tr.z_exit < zmax - EPS64;
+  size_t nt = ns + (side ? 1 : 0);
+  std::vector<double> L(nt), D(nt), E(nt + 1);
+  for (size_t s = 0; s < ns; ++s) {
+    L[s] = tr.seg[s].len;
+    D[s] = rho[tr.seg[s].cell];
+  }
+  if (side) {
+    L[ns] = (zmax - tr.z_exit) / cs;
+    D[ns] = rho_side;
+  }
+  dseg.assign(nt, 0.0);
+  // forward, with the derivative of each step's map E -> E' recorded
+  E[0] = energy;
+  double w = 1.0;
+  for (size_t s = 0; s < nt; ++s) {
+    double Ea = csda_energy(trk, csda_range(trk, E[s]) + L[s] * D[s]);
+    if (Ea >= 1e12 || !std::isfinite(Ea)) return 0.0;
+    w *= csda_stopping(trk, Ea) / csda_stopping(trk, E[s]);
+    w *= decay_from_path<double>(p, L[s], (E[s] + Ea) / 2.0);
+    E[s + 1] = Ea;
+  }
+  double EN = E[nt];
+  double Ga = air_grammage<double>(zmax, H, cos_theta);
+  Dual ENd(EN, 1.0);
+  Dual Ef = csda_energy(ta, csda_range(ta, ENd) + Dual(Ga));
+  if (Ef.v >= 1e12 || !std::isfinite(Ef.v)) return 0.0;
+  // d log(air factor * flux)/d EN through duals seeded on EN, plus the rock
+  // stopping power of the last segment
+  Dual La = Dual((H - zmax) / cs);
+  Dual logA = log(csda_stopping(ta, Ef)) - log(csda_stopping(ta, ENd)) +
+              log(decay_from_path<Dual>(p, La, (ENd + Ef) / Dual(2.0))) +
+              log(gccly<Dual>(cos_theta, Ef, charge));
+  double flux = w * std::exp(logA.v);
+  double lam = logA.d + csda_stopping(trk, Dual(EN, 1.0)).d / csda_stopping(trk, EN);
+  for (size_t s = nt; s-- > 0;) {
+    // E_{s+1} = K(R(E_s) + L D): derivatives by duals at the stored point
+    Dual Es(E[s], 1.0);
+    Dual Y = csda_range(trk, Es) + Dual(L[s] * D[s]);
+    Dual Ey = csda_energy(trk, Dual(Y.v, 1.0));    // dE'/dY
+    Dual Ee = csda_energy(trk, Y);                  // dE'/dE_s
+    Dual Da = log(decay_from_path<Dual>(p, Dual(L[s]), (Dual(E[s]) + Dual(E[s + 1], 1.0)) / Dual(2.0)));
+    Dual Db = log(decay_from_path<Dual>(p, Dual(L[s]), (Es + Dual(E[s + 1])) / Dual(2.0)));
+    lam += Da.d;
+    dseg[s] = flux * lam * Ey.d * L[s];
+    lam = lam * Ee.d + Db.d;
+  }
+  return flux;
+}
+
 }  // namespace orc
