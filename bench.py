@@ -118,34 +118,29 @@ def max_over_ranks(world, x):
 
 
 # ------------------------------------------------------------------ workloads
-def setup_c3(dp, torch, dev):
+def setup_c3(dp, torch, dev, precision="mixed"):
     from dpgpu.workloads import tomography_config
     grid, rho, rays, nodes = tomography_config()
     phys = dp.create_physics()
-    model = dp.TomoModel(phys, grid, nodes, side_density=2500.0)
+    model = dp.TomoModel(phys, grid, nodes, side_density=2500.0, precision=precision)
     cot = np.random.default_rng(1).uniform(0.5, 1.5, len(rays))
-    _, rp, _, _ = model.jacobian(rho, rays)
-    nseg = int(rp[-1])
+    paths = dp.TomoPaths(phys, grid, rays, nodes, side_density=2500.0)
+    nseg = paths.nnz
     T = lambda a: torch.tensor(np.ascontiguousarray(a).ravel(), dtype=torch.float64, device=dev)
-    d = {"rho": T(rho), "rays": T(rays), "E": T(nodes[0]), "q": T(nodes[1]), "w": T(nodes[2]),
-         "cot": T(cot), "flux": torch.zeros(len(rays), dtype=torch.float64, device=dev),
+    d = {"rho": T(rho), "cot": T(cot),
+         "flux": torch.zeros(len(rays), dtype=torch.float64, device=dev),
          "grad": torch.zeros(grid.ncell, dtype=torch.float64, device=dev)}
-    tp = dp.DpTomoParams(model.params.rock_material, model.params.air_material, -1, 2500.0, 3e4,
-                         len(nodes[0]), d["E"].data_ptr(), d["q"].data_ptr(), d["w"].data_ptr())
-    g = grid.to_c()
     lib = dp.load()
 
     def step_dev():
-        dp.check(lib.dp_tomo_vjp_dev(phys.ctx.h, phys.h, C.byref(g), C.byref(tp), d["rho"].data_ptr(),
-                                     len(rays), d["rays"].data_ptr(), d["cot"].data_ptr(),
-                                     d["flux"].data_ptr(), d["grad"].data_ptr()), phys.ctx.h)
+        paths.eval(d["rho"], d["cot"], precision=precision, flux=d["flux"], grad=d["grad"])
 
     h_flux = np.zeros(len(rays))
     h_grad = np.zeros(grid.ncell)
     rho_h, rays_h, cot_h = (np.ascontiguousarray(a, np.float64).ravel() for a in (rho, rays, cot))
+    g = grid.to_c()
 
     def step_e2e():
-        model.params.side_cell = -1
         dp.check(lib.dp_tomo_vjp(phys.ctx.h, phys.h, C.byref(g), C.byref(model.params),
                                  rho_h.ctypes.data_as(C.c_void_p), len(rays),
                                  rays_h.ctypes.data_as(C.c_void_p), cot_h.ctypes.data_as(C.c_void_p),
@@ -153,21 +148,24 @@ def setup_c3(dp, torch, dev):
                  phys.ctx.h)
 
     def plain_dev():
-        dp.check(lib.dp_tomo_forward_plain_dev(phys.ctx.h, phys.h, C.byref(g), C.byref(tp),
-                                               d["rho"].data_ptr(), len(rays), d["rays"].data_ptr(),
+        dp.check(lib.dp_tomo_forward_plain_dev(phys.ctx.h, phys.h, C.byref(g),
+                                               C.byref(paths.params), d["rho"].data_ptr(),
+                                               len(rays), paths.rays.data_ptr(),
                                                d["flux"].data_ptr()), phys.ctx.h)
 
     n_rays = len(rays)
-    # algorithmic bytes of the adjoint kernel per launch: ray record (56 B),
-    # flux (8 B) and row pointer (8 B) per ray; per traversed segment the
-    # density gather (8 B) and the Jacobian entry written (col 4 + val 8 +
-    # row 4 = 16 B).
-    alg = n_rays * (56 + 8 + 8) + nseg * (8 + 16)
+    # algorithmic bytes of the adjoint kernel per launch: per ray the row
+    # pointers (16 B), cos theta (8 B) and the flux written (8 B); per
+    # traversed segment the cell id (4 B), length (8 B), density gather (8 B)
+    # and the Jacobian value written (4 B in mixed precision, 8 B in FP64).
+    jb = 4 if precision == "mixed" else 8
+    alg = n_rays * (16 + 8 + 8) + nseg * (4 + 8 + 8 + jb)
     info = {"units": n_rays, "unit": "rays/s", "kernel": "tomo_adjoint", "alg_bytes": alg,
             "config": {"workload": "c3: tomography forward + adjoint, 64x64x32 @ 10 m, 4x1024 rays, "
-                                   "32 energy nodes [1,1e6] GeV, J^T r per step",
+                                   "32 energy nodes [1,1e6] GeV, flux + J^T r per step",
                        "grid": [64, 64, 32], "rays": n_rays, "energy_nodes": 32,
-                       "segments": nseg, "precision": "fp64"},
+                       "segments": nseg, "precision": precision,
+                       "paths": "traced once (resident); e2e traces on every call"},
             "h2d": 8 * (rho_h.size + rays_h.size + cot_h.size + 3 * len(nodes[0])),
             "d2h": 8 * (n_rays + grid.ncell)}
     return step_dev, step_e2e, plain_dev, info, phys
@@ -269,7 +267,8 @@ def run_gpu(args):
     achieved = info["alg_bytes"] / (kernel_ms * 1e-3) / 1e9 if kernel_ms > 0 else None
     line = {"metric": METRIC, "value": value, "unit": info["unit"], "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64" if info["config"].get("precision") == "mixed" else "f64",
             "data": "synthetic (seeded)", "config": dict(info["config"], l2="flushed between steps",
                                                           parallelism=f"replicas x{world}"),
             "e2e": {"value": world * info["units"] / (e2e_ms * 1e-3), "unit": info["unit"],

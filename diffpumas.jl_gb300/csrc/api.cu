@@ -148,6 +148,38 @@ static int finish_upload(dp_ctx* ctx, dp_physics* p, dp_physics** out) {
     delete p;
     return fail(ctx, DP_ERR_CUDA, "table upload failed");
   }
+  // single-precision derived columns
+  p->ld32 = dp::padded32(p->n);
+  std::vector<float> t32(size_t(p->n_mat) * dp::kNC32 * p->ld32, 0.0f);
+  for (int m = 0; m < p->n_mat; ++m) {
+    const double* E = &p->host[(size_t(m) * DP_NCOL + DP_COL_E) * p->n];
+    const double* L = &p->host[(size_t(m) * DP_NCOL + DP_COL_LOGE) * p->n];
+    const double* R = &p->host[(size_t(m) * DP_NCOL + DP_COL_CSDA_R) * p->n];
+    const double* S = &p->host[(size_t(m) * DP_NCOL + DP_COL_CSDA_S) * p->n];
+    auto C = [&](int c) { return &t32[(size_t(m) * dp::kNC32 + c) * p->ld32]; };
+    for (int i = 0; i < p->n; ++i) {
+      float rh = float(R[i]);
+      C(dp::C32_RH)[i] = rh;
+      C(dp::C32_RL)[i] = float(R[i] - double(rh));
+      C(dp::C32_S)[i] = float(S[i]);
+      C(dp::C32_E)[i] = float(E[i]);
+      C(dp::C32_LE)[i] = float(L[i]);
+      if (i + 1 < p->n) {
+        double dl = L[i + 1] - L[i];
+        C(dp::C32_SLOPE)[i] = float(dl / (R[i + 1] - R[i]));
+        C(dp::C32_DSDLE)[i] = float((S[i + 1] - S[i]) / dl);
+        C(dp::C32_DLE)[i] = float(dl);
+      }
+    }
+  }
+  if (cudaMalloc(&p->dev32, t32.size() * sizeof(float)) != cudaSuccess ||
+      cudaMemcpy(p->dev32, t32.data(), t32.size() * sizeof(float), cudaMemcpyHostToDevice) !=
+          cudaSuccess) {
+    cudaFree(p->dev);
+    if (p->dev32) cudaFree(p->dev32);
+    delete p;
+    return fail(ctx, DP_ERR_CUDA, "table upload failed");
+  }
   p->view.base = p->dev;
   p->view.n = p->n;
   p->view.ld = p->ld;
@@ -227,6 +259,7 @@ int dp_physics_free(dp_physics* p) {
   if (p->dev) {
     cudaSetDevice(p->ctx->device);
     cudaFree(p->dev);
+    cudaFree(p->dev32);
   }
   delete p;
   return DP_OK;

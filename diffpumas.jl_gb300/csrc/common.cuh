@@ -42,6 +42,18 @@ struct TabView {
   DP_HD const double* col(int mat, int c) const { return base + ((size_t)mat * DP_NCOL + c) * ld; }
 };
 
+// Single-precision derived table columns (one row per energy node i; the
+// per-interval columns hold the value of interval [i, i+1]):
+//   RH, RL   range as a float pair (RH + RL = R to ~2^-48)
+//   S        stopping power
+//   E        kinetic energy
+//   LE       log E
+//   SLOPE    (logE[i+1]-logE[i]) / (R[i+1]-R[i])     (d log E / d R)
+//   DSDLE    (S[i+1]-S[i]) / (logE[i+1]-logE[i])     (d S / d log E)
+//   DLE      logE[i+1]-logE[i]
+enum Col32 { C32_RH = 0, C32_RL, C32_S, C32_E, C32_LE, C32_SLOPE, C32_DSDLE, C32_DLE, kNC32 };
+DP_HD int padded32(int n) { return (n + 3) & ~3; }
+
 // ------------------------------------------------------------- dual numbers
 // Value and tangent with respect to one scalar input (forward-mode AD).
 struct Dd {

@@ -60,6 +60,29 @@ struct dp_physics {
   bool has_recipes = false;
   double* dev = nullptr;              // n_mat x DP_NCOL x ld
   dp::TabView view{};
+  // Single-precision derived columns for the mixed-precision kernels:
+  // n_mat x dp::kNC32 x ld32 floats (see dp::Col32).
+  float* dev32 = nullptr;
+  int ld32 = 0;
+};
+
+// Ray paths through a voxel grid, traced once (geometry does not depend on
+// the densities): CSR segment lists plus the CSC permutation used by the
+// deterministic J^T r gather.
+struct dp_paths {
+  dp_ctx* ctx = nullptr;
+  dp_grid grid{};
+  int side_cell = -1;
+  long n_rays = 0;
+  int64_t nnz = 0;      // segments, side-exit remainders included
+  int max_seg = 0;      // longest segment list
+  dp_ray* rays = nullptr;
+  int64_t* row_ptr = nullptr;   // n_rays + 1
+  int32_t* cell = nullptr;      // nnz (-1: side remainder at a fixed density)
+  double* len = nullptr;        // nnz
+  int32_t* row_of = nullptr;    // nnz
+  int64_t* cptr = nullptr;      // ncell + 1
+  int32_t* perm = nullptr;      // entries sorted by (cell, entry index)
 };
 
 #define DP_CHECK_CUDA(ctx, call)                                  \

@@ -1,22 +1,32 @@
 // tomo.cu -- voxel-density tomography forward model and its density adjoint.
 //
-// Forward (examples/diff_flux_cube.jl:304-470): the ray is marched through
-// the grid exactly as trace_cube_path does it (position-based boundary march,
-// candidates x, y, z with strict improvement, 1e-10 tolerance, 1 cm nudge),
-// so the segment list is identical to the reference's; the march uses
-// correctly rounded FP64 operations without contraction.  Per energy node,
-// each segment inverts the CSDA range (X = R(E), E' = R^-1(X + rho L)),
-// multiplies the weight by S(E')/S(E) and the decay factor, the side-exit
-// remainder and the closed-form air column follow, then the GCCLY flux.
+// Paths.  The geometry does not depend on the densities, so rays are traced
+// once into a device-resident CSR list of segments (cell, length) together with
+// the CSC permutation that the J^T r gather uses (the reference likewise traces
+// once: examples/diff_flux_cube.jl:489-557, examples/lvd_tomography.jl:835-861).
+// The march replicates trace_cube_path (examples/diff_flux_cube.jl:194-366):
+// position-based boundary stepping, candidates x, y, z with strict
+// improvement, 1e-10 tolerance, 1 cm nudge, 1000-step cap; it runs in
+// correctly rounded FP64 without contraction, so the segment lists equal the
+// reference's.  A side-exit remainder (exit below the top face) becomes one
+// more segment of length (zmax - z_exit)/max(|cos theta|, 0.01) whose density
+// is rho[side_cell] or a fixed side density (diff_flux_cube.jl:417-444).
 //
-// Adjoint: one warp per ray, one lane per energy node.  A reverse sweep over
-// the segment list recomputes the per-segment energies and carries
+// Evaluation.  One warp per ray, one lane per energy node.  Per segment:
+// X = R(E), E' = R^-1(X + rho L), weight *= S(E')/S(E) * exp(-L/(beta gamma
+// c tau)); then the closed-form air column and the GCCLY flux; the per-ray
+// flux is (1/N) sum_n 2 w_n f_n (compute_flux_from_segments, :374-470).
+//  * FP64 kernel: the reference's per-segment operations (parity mode).
+//  * Mixed kernel: per-segment work in FP32 -- the range is carried as a float
+//    pair (the inversion stays accurate near E_min), energies come from the
+//    node energy times exp of a small log offset, stopping powers and decay
+//    exponents in FP32; the node flux integral is accumulated in FP64.
+// Adjoint: a reverse sweep over the segment list carries
 // lambda_k = d log(flux)/d E_k; d flux/d rho_k = flux lambda_k dE_k/dY_k L_k.
-// Lanes are reduced per segment with a fixed shuffle tree, giving one Jacobian
-// entry per traversed segment (CSR).  J^T r is formed by a deterministic
-// segmented reduction: entries are bucketed by cell (integer counts), each
-// bucket is ordered by entry index, then summed in that order -- no
-// floating-point atomics, bitwise reproducible.
+// Lanes are reduced per segment by a fixed shuffle tree: one Jacobian entry per
+// segment.  J^T r = per-cell sums over the precomputed CSC permutation, each
+// bucket ordered by entry index -- no floating-point atomics, bitwise
+// reproducible.
 #include <math_constants.h>
 
 #include <algorithm>
@@ -32,6 +42,12 @@ struct GridDev {
   double x0, y0, z0, dx, dy, dz, xmax, ymax, zmax;
 };
 
+static GridDev grid_dev(const dp_grid& g) {
+  return GridDev{g.nx, g.ny, g.nz, g.x0, g.y0, g.z0, g.dx, g.dy, g.dz,
+                 g.x0 + g.nx * g.dx, g.y0 + g.ny * g.dy, g.z0 + g.nz * g.dz};
+}
+
+// examples/diff_flux_cube.jl:132-148 (get_cell_indices)
 __device__ __forceinline__ bool cell_of(const GridDev& g, double x, double y, double z, int& i,
                                         int& j, int& k) {
   if (x < g.x0 || x > g.xmax || y < g.y0 || y > g.ymax || z < g.z0 || z > g.zmax) return false;
@@ -79,9 +95,8 @@ __device__ __forceinline__ double to_boundary(const GridDev& g, double x, double
   return tmin;
 }
 
-// examples/diff_flux_cube.jl:304-366 (trace_cube_path).  Calls emit(cell, L)
-// per segment; returns the number of segments, or -1 past `cap`; *z_exit gets
-// the last segment end height.
+// examples/diff_flux_cube.jl:304-366 (trace_cube_path).  Calls emit(s, cell,
+// L) per segment; returns the segment count, or -1 past `cap`.
 template <class Emit>
 __device__ __forceinline__ int trace(const GridDev& g, const dp_ray& r, int cap, double* z_exit,
                                      Emit emit) {
@@ -111,228 +126,50 @@ __device__ __forceinline__ int trace(const GridDev& g, const dp_ray& r, int cap,
   return ns;
 }
 
-struct TomoDev {
-  TabView tab;
-  GridDev g;
-  int rock, air, side_cell, n_nodes, seg_cap;
-  double side_density, H, mass, ctau, air_dexp;  // exp(-zmax/h) - exp(-H/h)
-  const double *nE, *nq, *nw;  // device node arrays
-  const double* rho;
-  const dp_ray* rays;
-  long n_rays;
-  double* flux;
-  const int64_t* row_ptr;  // MODE 1
-  int32_t* col;
-  double* val;
-  int32_t* row_of;
-  int* err_flag;
-};
-
-// Per-segment decay exponent derivative: d log D / d Eavg for
-// D = exp(-L / (beta gamma ctau)), beta = sqrt(max(1 - 1/gamma^2, 1e-12)).
-__device__ __forceinline__ double decay_log(double L, double Eavg, double mass, double ctau,
-                                            double* dlog) {
-  double g = 1.0 + Eavg / mass, b2 = 1.0 - 1.0 / (g * g);
-  bool clamp = !(b2 > 1e-12);
-  double b = sqrt(clamp ? 1e-12 : b2), bg = b * g;
-  if (dlog) *dlog = L / (ctau * bg * bg) * (clamp ? b : 1.0 / b) / mass;
-  return -L / (bg * ctau);
-}
-
-// log-derivative helpers on the staged tables
-__device__ __forceinline__ double dlogS(const TabView& t, const double* E, const double* lE,
-                                        const double* S, double e, double* Sval) {
-  Dd s = interp_logE(t, E, lE, S, dd(e, 1.0 / e), dd(log(e), 1.0 / e), nullptr);
-  *Sval = s.v;
-  return s.d / s.v;
-}
-__device__ __forceinline__ double range_slope(const TabView& t, const double* E, const double* lE,
-                                              const double* R, double e) {
-  // dR/dE (zero outside the table, rrule convention)
-  return interp_logE(t, E, lE, R, dd(e, 1.0), dd(log(e), 1.0 / e), nullptr).d;
-}
-__device__ __forceinline__ double inv_slope(const double* R, const double* E, const double* lE,
-                                            int n, double Y) {
-  return inverse_range(R, E, lE, n, dd(Y, 1.0), nullptr).d;
-}
-
-enum { T_E = 0, T_LOGE, T_RS, T_RR, T_AS, T_AR, T_NCOL };
-
-template <int MODE>
-__global__ void __launch_bounds__(128) tomo_kernel(TomoDev P) {
-  extern __shared__ __align__(16) double smem[];
-  __shared__ uint64_t mbar;
-  const int ld = P.tab.ld, n = P.tab.n;
-  const double* src[T_NCOL] = {P.tab.col(0, DP_COL_E),          P.tab.col(0, DP_COL_LOGE),
-                               P.tab.col(P.rock, DP_COL_CSDA_S), P.tab.col(P.rock, DP_COL_CSDA_R),
-                               P.tab.col(P.air, DP_COL_CSDA_S),  P.tab.col(P.air, DP_COL_CSDA_R)};
-  if (!stage_columns(smem, src, T_NCOL, uint32_t(ld * sizeof(double)), &mbar)) {
-    if (threadIdx.x == 0) atomicExch(P.err_flag, 1);
-    return;
-  }
-  const double *tE = smem + T_E * ld, *tlE = smem + T_LOGE * ld;
-  const double *rS = smem + T_RS * ld, *rR = smem + T_RR * ld;
-  const double *aS = smem + T_AS * ld, *aR = smem + T_AR * ld;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int cap = P.seg_cap;
-  // per-warp segment buffers after the tables: length, density, Jacobian
-  // accumulator (doubles), then cell ids (ints)
-  double* wbase = smem + T_NCOL * ld + size_t(warp) * cap * 3;
-  double* sL = wbase;
-  double* sD = wbase + cap;
-  double* sJ = wbase + 2 * cap;
-  int* cells = reinterpret_cast<int*>(smem + T_NCOL * ld + size_t(4) * cap * 3) + size_t(warp) * cap;
-  const double Emax = tE[n - 1];
-  for (long r = blockIdx.x * 4L + warp; r < P.n_rays; r += gridDim.x * 4L) {
-    dp_ray ray = P.rays[r];
-    double z_exit;
-    int ns = trace(P.g, ray, cap - 1, &z_exit, [&](int s, int cell, double L) {
-      if (lane == 0) {
-        cells[s] = cell;
-        sL[s] = L;
-        sD[s] = P.rho[cell];
-      }
-    });
-    if (ns < 0) {
-      if (lane == 0) atomicExch(P.err_flag, 2);
-      continue;
-    }
-    // side-exit remainder as one more rock segment (diff_flux_cube.jl:417-444)
-    const double cs_safe = fmax(fabs(ray.cos_theta), 0.01);
-    bool side = z_exit < P.g.zmax - kEps64;
-    if (side && lane == 0) {
-      cells[ns] = P.side_cell;
-      sL[ns] = (P.g.zmax - z_exit) / cs_safe;
-      sD[ns] = P.side_cell >= 0 ? P.rho[P.side_cell] : P.side_density;
-    }
-    const int nseg = ns + (side ? 1 : 0);
-    if (MODE == 1)
-      for (int s = lane; s < nseg; s += 32) sJ[s] = 0.0;
-    __syncwarp();
-    const double Lair = (P.H - P.g.zmax) / cs_safe;
-    const double Gair = fmax((1.205 * 12e3 / cs_safe) * P.air_dexp, 0.0);
-    const double cs = cos_theta_star(ray.cos_theta), cs129 = pow(cs, 1.29);
-    double fsum = 0.0;
-    for (int base = 0; base < P.n_nodes; base += 32) {
-      const int nd = base + lane;
-      const bool active = nd < P.n_nodes;
-      double E = active ? P.nE[nd] : 1.0;
-      double w = 1.0;
-      bool ok = active;
-      int kc = -1;
-      double Eprev_c = 0.0;
-      int hint = 0;
-      for (int s = 0; s < nseg && ok; ++s) {
-        double X = interp_logE(P.tab, tE, tlE, rR, dd(E), dd(log(E)), nullptr).v;
-        double Ek = inverse_range(rR, tE, tlE, n, dd(X + sL[s] * sD[s]), &hint).v;
-        if (!(Ek < 1e12) || !isfinite(Ek)) {
-          ok = false;
-          break;
-        }
-        if (kc < 0 && Ek >= Emax) {
-          kc = s;
-          Eprev_c = E;
-        }
-        double Si = interp_logE(P.tab, tE, tlE, rS, dd(E), dd(log(E)), nullptr).v;
-        double Sf = interp_logE(P.tab, tE, tlE, rS, dd(Ek), dd(log(Ek)), nullptr).v;
-        w = w * (Sf / Si);
-        w = w * exp(decay_log(sL[s], (E + Ek) / 2.0, P.mass, P.ctau, nullptr));
-        E = Ek;
-      }
-      double f = 0.0, EN = E, Ef = 0.0;
-      if (ok) {
-        double Xa = interp_logE(P.tab, tE, tlE, aR, dd(E), dd(log(E)), nullptr).v;
-        Ef = inverse_range(aR, tE, tlE, n, dd(Xa + Gair), nullptr).v;
-        if (Ef < 1e12 && isfinite(Ef)) {
-          double Sa0 = interp_logE(P.tab, tE, tlE, aS, dd(E), dd(log(E)), nullptr).v;
-          double Sa1 = interp_logE(P.tab, tE, tlE, aS, dd(Ef), dd(log(Ef)), nullptr).v;
-          w = w * (Sa1 / Sa0);
-          w = w * exp(decay_log(Lair, (E + Ef) / 2.0, P.mass, P.ctau, nullptr));
-          f = w * gccly_flux(cs, cs129, Ef, active ? P.nq[nd] : 0.0, nullptr);
-        } else {
-          ok = false;
-        }
-      }
-      const double coef = active && ok ? 2.0 * P.nw[nd] / P.n_nodes : 0.0;
-      fsum += coef * f;
-      if (MODE == 1) {
-        // ---- reverse sweep
-        double lam = 0.0;
-        if (coef != 0.0 && f != 0.0) {
-          double Sv;
-          double aA;
-          decay_log(Lair, (EN + Ef) / 2.0, P.mass, P.ctau, &aA);
-          double dlogF;
-          gccly_flux(cs, cs129, Ef, P.nq[nd], &dlogF);
-          double dEf = inv_slope(aR, tE, tlE, n,
-                                 interp_logE(P.tab, tE, tlE, aR, dd(EN), dd(log(EN)), nullptr).v +
-                                     Gair) *
-                       range_slope(P.tab, tE, tlE, aR, EN);
-          lam = dlogS(P.tab, tE, tlE, rS, EN, &Sv) - dlogS(P.tab, tE, tlE, aS, EN, &Sv) + 0.5 * aA +
-                dEf * (dlogS(P.tab, tE, tlE, aS, Ef, &Sv) + 0.5 * aA + dlogF);
-        }
-        double Ek = EN;
-        int hint_r = n - 2;
-        for (int s = nseg - 1; s >= 0; --s) {
-          double v = 0.0, Ekm1 = 0.0, a = 0.0;
-          if (coef != 0.0 && f != 0.0) {
-            const double L = sL[s], Y = interp_logE(P.tab, tE, tlE, rR, dd(Ek), dd(log(Ek)), nullptr).v;
-            if (kc >= 0 && s > kc) Ekm1 = Emax;
-            else if (s == kc) Ekm1 = Eprev_c;
-            else {
-              // walk down from the previous interval (energies decrease)
-              Ekm1 = inverse_range(rR, tE, tlE, n, dd(Y - L * sD[s]), nullptr).v;
-            }
-            (void)hint_r;
-            double Ycur = interp_logE(P.tab, tE, tlE, rR, dd(Ekm1), dd(log(Ekm1)), nullptr).v + L * sD[s];
-            double Kp = (Ek >= Emax) ? 0.0 : inv_slope(rR, tE, tlE, n, Ycur);
-            decay_log(L, (Ekm1 + Ek) / 2.0, P.mass, P.ctau, &a);
-            lam += 0.5 * a;  // decay of this segment through E_k
-            v = coef * f * lam * Kp * L;
-            // propagate to E_{k-1}
-            double Rp = range_slope(P.tab, tE, tlE, rR, Ekm1);
-            lam = lam * Kp * Rp + 0.5 * a;
-          }
-          // deterministic lane reduction
-          for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-          if (lane == 0) sJ[s] += v;
-          Ek = Ekm1;
-        }
-      }
-    }
-    for (int o = 16; o > 0; o >>= 1) fsum += __shfl_xor_sync(0xffffffffu, fsum, o);
-    if (lane == 0) P.flux[r] = fsum;
-    if (MODE == 1) {
-      __syncwarp();
-      const int64_t off = P.row_ptr[r];
-      const int nent = int(P.row_ptr[r + 1] - off);
-      for (int s = lane; s < nseg && s < nent; s += 32) {
-        P.col[off + s] = cells[s];
-        P.val[off + s] = sJ[s];
-        if (P.row_of) P.row_of[off + s] = int32_t(r);
-      }
-    }
-    __syncwarp();
-  }
-}
-
-// Segment count per ray (+1 for a side exit), one thread per ray.
-__global__ void tomo_count_kernel(GridDev g, const dp_ray* rays, long n_rays, int cap,
-                                  int64_t* counts, int* err_flag) {
+// ============================================================ path building
+// One thread per ray: segments into a fixed-capacity slot, count per ray.
+__global__ void trace_kernel(GridDev g, const dp_ray* rays, long n_rays, int cap, int side_cell,
+                             int32_t* slot_cell, double* slot_len, int64_t* counts,
+                             int* err_flag) {
   long r = blockIdx.x * long(blockDim.x) + threadIdx.x;
   if (r >= n_rays) return;
-  double z_exit;
   dp_ray ray = rays[r];
-  int ns = trace(g, ray, cap - 1, &z_exit, [](int, int, double) {});
+  int32_t* sc = slot_cell + size_t(r) * cap;
+  double* sl = slot_len + size_t(r) * cap;
+  double z_exit;
+  int ns = trace(g, ray, cap - 1, &z_exit, [&](int s, int cell, double L) {
+    sc[s] = cell;
+    sl[s] = L;
+  });
   if (ns < 0) {
     atomicExch(err_flag, 2);
-    ns = 0;
+    counts[r] = 0;
+    return;
   }
-  counts[r] = ns + (z_exit < g.zmax - kEps64 ? 1 : 0);
+  if (z_exit < g.zmax - kEps64) {
+    sc[ns] = side_cell;
+    sl[ns] = (g.zmax - z_exit) / fmax(fabs(ray.cos_theta), 0.01);
+    ++ns;
+  }
+  counts[r] = ns;
+}
+
+__global__ void compact_kernel(const int64_t* row_ptr, long n_rays, int cap,
+                               const int32_t* slot_cell, const double* slot_len, int32_t* cell,
+                               double* len, int32_t* row_of) {
+  long idx = blockIdx.x * long(blockDim.x) + threadIdx.x;
+  long r = idx / cap;
+  int s = int(idx - r * cap);
+  if (r >= n_rays) return;
+  int64_t b = row_ptr[r];
+  if (s >= row_ptr[r + 1] - b) return;
+  cell[b + s] = slot_cell[idx];
+  len[b + s] = slot_len[idx];
+  row_of[b + s] = int32_t(r);
 }
 
 // Exclusive scan of int64 (two levels; the second level walks any number of
-// block totals serially in one block).
+// block totals serially in one block).  out[n] receives the total.
 constexpr int kScan = 1024;
 __global__ void __launch_bounds__(kScan) scan_blocks(const int64_t* in, int64_t* out, long n,
                                                      int64_t* totals) {
@@ -379,14 +216,9 @@ __global__ void scan_add(int64_t* out, long n, const int64_t* totals, const int6
   if (i == n - 1) out[n] = *grand;
 }
 
-// J^T r: bucket entries by cell.
-__global__ void hist_kernel(const int32_t* col, long nnz, int32_t* count) {
+__global__ void hist_kernel(const int32_t* col, long nnz, int64_t* count) {
   long e = blockIdx.x * long(blockDim.x) + threadIdx.x;
-  if (e < nnz && col[e] >= 0) atomicAdd(&count[col[e]], 1);
-}
-__global__ void i32_to_i64(const int32_t* a, int64_t* b, long n) {
-  long i = blockIdx.x * long(blockDim.x) + threadIdx.x;
-  if (i < n) b[i] = a[i];
+  if (e < nnz && col[e] >= 0) atomicAdd(reinterpret_cast<unsigned long long*>(&count[col[e]]), 1ull);
 }
 __global__ void place_kernel(const int32_t* col, long nnz, const int64_t* cptr, int32_t* cursor,
                              int32_t* perm) {
@@ -395,9 +227,8 @@ __global__ void place_kernel(const int32_t* col, long nnz, const int64_t* cptr, 
   int c = col[e];
   perm[cptr[c] + atomicAdd(&cursor[c], 1)] = int32_t(e);
 }
-// One thread per cell: order its bucket by entry index, then sum in order.
-__global__ void gather_kernel(const int64_t* cptr, int32_t* perm, const double* val,
-                              const int32_t* row_of, const double* cot, long ncell, double* grad) {
+// One thread per cell: order its bucket by entry index (insertion sort).
+__global__ void sort_buckets_kernel(const int64_t* cptr, long ncell, int32_t* perm) {
   long c = blockIdx.x * long(blockDim.x) + threadIdx.x;
   if (c >= ncell) return;
   int64_t b = cptr[c], e = cptr[c + 1];
@@ -410,15 +241,382 @@ __global__ void gather_kernel(const int64_t* cptr, int32_t* perm, const double* 
     }
     perm[j + 1] = x;
   }
+}
+
+// ============================================================ evaluation
+struct EvalP {
+  TabView tab;
+  const float* tab32;
+  int ld32;
+  int rock, air, n_nodes, seg_cap;
+  double H, mass, ctau, air_dexp, zmax, side_density;
+  const double *nE, *nq, *nw;
+  const double* rho;
+  const dp_ray* rays;
+  long n_rays;
+  const int64_t* row_ptr;
+  const int32_t* cell;
+  const double* len;
+  double* flux;
+  double* jval64;
+  float* jval32;
+  int* err_flag;
+};
+
+__device__ __forceinline__ double seg_density(const EvalP& P, int c) {
+  return c >= 0 ? P.rho[c] : P.side_density;
+}
+
+// d log D / d Eavg, D = exp(-L/(beta gamma ctau)), beta = sqrt(max(1-1/g^2, 1e-12))
+__device__ __forceinline__ double decay_log(double L, double Eavg, double mass, double ctau,
+                                            double* dlog) {
+  double g = 1.0 + Eavg / mass, b2 = 1.0 - 1.0 / (g * g);
+  bool clamp = !(b2 > 1e-12);
+  double b = sqrt(clamp ? 1e-12 : b2), bg = b * g;
+  if (dlog) *dlog = L / (ctau * bg * bg) * (clamp ? b : 1.0 / b) / mass;
+  return -L / (bg * ctau);
+}
+__device__ __forceinline__ double dlogS(const TabView& t, const double* E, const double* lE,
+                                        const double* S, double e) {
+  Dd s = interp_logE(t, E, lE, S, dd(e, 1.0 / e), dd(log(e), 1.0 / e), nullptr);
+  return s.d / s.v;
+}
+__device__ __forceinline__ double range_slope(const TabView& t, const double* E, const double* lE,
+                                              const double* R, double e) {
+  return interp_logE(t, E, lE, R, dd(e, 1.0), dd(log(e), 1.0 / e), nullptr).d;
+}
+__device__ __forceinline__ double inv_slope(const double* R, const double* E, const double* lE,
+                                            int n, double Y) {
+  return inverse_range(R, E, lE, n, dd(Y, 1.0), nullptr).d;
+}
+
+enum { T_E = 0, T_LOGE, T_RS, T_RR, T_AS, T_AR, T_NCOL };
+constexpr int kWarps = 8;
+
+// ---------------------------------------------------------------- FP64 kernel
+template <bool ADJ>
+__global__ void __launch_bounds__(kWarps * 32) eval64_kernel(EvalP P) {
+  extern __shared__ __align__(16) double smem[];
+  __shared__ uint64_t mbar;
+  const int ld = P.tab.ld, n = P.tab.n;
+  const double* src[T_NCOL] = {P.tab.col(0, DP_COL_E),          P.tab.col(0, DP_COL_LOGE),
+                               P.tab.col(P.rock, DP_COL_CSDA_S), P.tab.col(P.rock, DP_COL_CSDA_R),
+                               P.tab.col(P.air, DP_COL_CSDA_S),  P.tab.col(P.air, DP_COL_CSDA_R)};
+  if (!stage_columns(smem, src, T_NCOL, uint32_t(ld * sizeof(double)), &mbar)) {
+    if (threadIdx.x == 0) atomicExch(P.err_flag, 1);
+    return;
+  }
+  const double *tE = smem + T_E * ld, *tlE = smem + T_LOGE * ld;
+  const double *rS = smem + T_RS * ld, *rR = smem + T_RR * ld;
+  const double *aS = smem + T_AS * ld, *aR = smem + T_AR * ld;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, cap = P.seg_cap;
+  double* sL = smem + T_NCOL * ld + size_t(warp) * cap * 3;
+  double* sD = sL + cap;
+  double* sJ = sD + cap;
+  const double Emax = tE[n - 1];
+  for (long r = blockIdx.x * long(kWarps) + warp; r < P.n_rays; r += long(gridDim.x) * kWarps) {
+    const int64_t off = P.row_ptr[r];
+    const int nseg = int(P.row_ptr[r + 1] - off);
+    for (int s = lane; s < nseg; s += 32) {
+      sL[s] = P.len[off + s];
+      sD[s] = seg_density(P, P.cell[off + s]);
+      sJ[s] = 0.0;
+    }
+    __syncwarp();
+    const double cosz = P.rays[r].cos_theta;
+    const double cs_safe = fmax(fabs(cosz), 0.01);
+    const double Lair = (P.H - P.zmax) / cs_safe;
+    const double Gair = fmax((1.205 * 12e3 / cs_safe) * P.air_dexp, 0.0);
+    const double cs = cos_theta_star(cosz), cs129 = pow(cs, 1.29);
+    double fsum = 0.0;
+    for (int base = 0; base < P.n_nodes; base += 32) {
+      const int nd = base + lane;
+      const bool active = nd < P.n_nodes;
+      double E = active ? P.nE[nd] : 1.0, w = 1.0;
+      bool ok = active;
+      int kc = -1, hint = 0;
+      double Eprev_c = 0.0;
+      for (int s = 0; s < nseg && ok; ++s) {
+        double X = interp_logE(P.tab, tE, tlE, rR, dd(E), dd(log(E)), nullptr).v;
+        double Ek = inverse_range(rR, tE, tlE, n, dd(X + sL[s] * sD[s]), &hint).v;
+        if (!(Ek < 1e12)) {
+          ok = false;
+          break;
+        }
+        if (kc < 0 && Ek >= Emax) {
+          kc = s;
+          Eprev_c = E;
+        }
+        double Si = interp_logE(P.tab, tE, tlE, rS, dd(E), dd(log(E)), nullptr).v;
+        double Sf = interp_logE(P.tab, tE, tlE, rS, dd(Ek), dd(log(Ek)), nullptr).v;
+        w = w * (Sf / Si);
+        w = w * exp(decay_log(sL[s], (E + Ek) / 2.0, P.mass, P.ctau, nullptr));
+        E = Ek;
+      }
+      double f = 0.0, EN = E, Ef = 0.0;
+      if (ok) {
+        double Xa = interp_logE(P.tab, tE, tlE, aR, dd(E), dd(log(E)), nullptr).v;
+        Ef = inverse_range(aR, tE, tlE, n, dd(Xa + Gair), nullptr).v;
+        double Sa0 = interp_logE(P.tab, tE, tlE, aS, dd(E), dd(log(E)), nullptr).v;
+        double Sa1 = interp_logE(P.tab, tE, tlE, aS, dd(Ef), dd(log(Ef)), nullptr).v;
+        w = w * (Sa1 / Sa0);
+        w = w * exp(decay_log(Lair, (E + Ef) / 2.0, P.mass, P.ctau, nullptr));
+        f = w * gccly_flux(cs, cs129, Ef, P.nq[nd], nullptr);
+      }
+      const double coef = ok ? 2.0 * P.nw[nd] / P.n_nodes : 0.0;
+      fsum += coef * f;
+      if (ADJ) {
+        const bool live = coef != 0.0 && f != 0.0;
+        double lam = 0.0;
+        if (live) {
+          double aA, dlogF;
+          decay_log(Lair, (EN + Ef) / 2.0, P.mass, P.ctau, &aA);
+          gccly_flux(cs, cs129, Ef, P.nq[nd], &dlogF);
+          double dEf = inv_slope(aR, tE, tlE, n,
+                                 interp_logE(P.tab, tE, tlE, aR, dd(EN), dd(log(EN)), nullptr).v + Gair) *
+                       range_slope(P.tab, tE, tlE, aR, EN);
+          lam = dlogS(P.tab, tE, tlE, rS, EN) - dlogS(P.tab, tE, tlE, aS, EN) + 0.5 * aA +
+                dEf * (dlogS(P.tab, tE, tlE, aS, Ef) + 0.5 * aA + dlogF);
+        }
+        double Ek = EN;
+        for (int s = nseg - 1; s >= 0; --s) {
+          double v = 0.0, Ekm1 = 0.0;
+          if (live) {
+            const double L = sL[s];
+            if (kc >= 0 && s > kc) {
+              Ekm1 = Emax;
+            } else if (s == kc) {
+              Ekm1 = Eprev_c;
+            } else {
+              double Y = interp_logE(P.tab, tE, tlE, rR, dd(Ek), dd(log(Ek)), nullptr).v;
+              Ekm1 = s == 0 ? P.nE[nd] : inverse_range(rR, tE, tlE, n, dd(Y - L * sD[s]), nullptr).v;
+            }
+            double Ycur = interp_logE(P.tab, tE, tlE, rR, dd(Ekm1), dd(log(Ekm1)), nullptr).v + L * sD[s];
+            double Kp = (Ek >= Emax) ? 0.0 : inv_slope(rR, tE, tlE, n, Ycur);
+            double a;
+            decay_log(L, (Ekm1 + Ek) / 2.0, P.mass, P.ctau, &a);
+            lam += 0.5 * a;
+            v = coef * f * lam * Kp * L;
+            lam = lam * Kp * range_slope(P.tab, tE, tlE, rR, Ekm1) + 0.5 * a;
+          }
+          for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+          if (lane == 0) sJ[s] += v;
+          Ek = Ekm1;
+        }
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) fsum += __shfl_xor_sync(0xffffffffu, fsum, o);
+    if (lane == 0) P.flux[r] = fsum;
+    __syncwarp();
+    if (ADJ)
+      for (int s = lane; s < nseg; s += 32) P.jval64[off + s] = sJ[s];
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------- mixed kernel
+// Float-pair accumulation (TwoSum): (h, l) += x
+__device__ __forceinline__ void ff_add(float& h, float& l, float x) {
+  float s = h + x;
+  float bb = s - h;
+  float e = (h - (s - bb)) + (x - bb);
+  h = s;
+  l += e;
+}
+
+// Interval i with RH[i] <= Y < RH[i+1], moving from the current i.
+__device__ __forceinline__ int walk(const float* RH, int n, float yh, int i) {
+  while (i < n - 2 && !(yh < RH[i + 1])) ++i;
+  while (i > 0 && yh < RH[i]) --i;
+  return i;
+}
+
+template <bool ADJ>
+__global__ void __launch_bounds__(kWarps * 32) eval32_kernel(EvalP P) {
+  extern __shared__ __align__(16) float fsm[];
+  __shared__ uint64_t mbar;
+  const int ld = P.ld32, n = P.tab.n;
+  const float* base = P.tab32;
+  const double* src[2 * kNC32];
+  for (int c = 0; c < kNC32; ++c) {
+    src[c] = reinterpret_cast<const double*>(base + (size_t(P.rock) * kNC32 + c) * ld);
+    src[kNC32 + c] = reinterpret_cast<const double*>(base + (size_t(P.air) * kNC32 + c) * ld);
+  }
+  if (!stage_columns(reinterpret_cast<double*>(fsm), src, 2 * kNC32, uint32_t(ld * sizeof(float)),
+                     &mbar)) {
+    if (threadIdx.x == 0) atomicExch(P.err_flag, 1);
+    return;
+  }
+  const float* rk = fsm;                       // rock columns
+  const float* ak = fsm + size_t(kNC32) * ld;  // air columns
+  const float *RH = rk + C32_RH * ld, *RL = rk + C32_RL * ld, *SR = rk + C32_S * ld;
+  const float *EE = rk + C32_E * ld, *SLO = rk + C32_SLOPE * ld, *DS = rk + C32_DSDLE * ld;
+  const float *DLE = rk + C32_DLE * ld;
+  const float *aRH = ak + C32_RH * ld, *aRL = ak + C32_RL * ld, *aS = ak + C32_S * ld;
+  const float *aSLO = ak + C32_SLOPE * ld, *aDS = ak + C32_DSDLE * ld;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, cap = P.seg_cap;
+  float* sG = fsm + size_t(2 * kNC32) * ld + size_t(warp) * cap * 3;  // grammage rho L
+  float* sL = sG + cap;                                              // length L
+  float* sJ = sL + cap;                                              // Jacobian accumulator
+  const float inv_m = float(1.0 / P.mass), inv_ctau = float(1.0 / P.ctau);
+  const float m_ctau = float(P.mass * P.ctau);
+  const float Emax = EE[n - 1];
+  for (long r = blockIdx.x * long(kWarps) + warp; r < P.n_rays; r += long(gridDim.x) * kWarps) {
+    const int64_t off = P.row_ptr[r];
+    const int nseg = int(P.row_ptr[r + 1] - off);
+    for (int s = lane; s < nseg; s += 32) {
+      double L = P.len[off + s];
+      sG[s] = float(L * seg_density(P, P.cell[off + s]));
+      sL[s] = float(L);
+      sJ[s] = 0.0f;
+    }
+    __syncwarp();
+    const double cosz = P.rays[r].cos_theta;
+    const double cs_safe = fmax(fabs(cosz), 0.01);
+    const float Lair = float((P.H - P.zmax) / cs_safe);
+    const double Gair = fmax((1.205 * 12e3 / cs_safe) * P.air_dexp, 0.0);
+    const float Gh = float(Gair), Gl = float(Gair - double(Gh));
+    const float cs = float(cos_theta_star(cosz));
+    const float cs129 = powf(cs, 1.29f);
+    double fsum = 0.0;
+    for (int b0 = 0; b0 < P.n_nodes; b0 += 32) {
+      const int nd = b0 + lane;
+      const bool active = nd < P.n_nodes;
+      // node start: R(E0) and S(E0) from the FP64 tables (once per node)
+      const double E0d = active ? P.nE[nd] : 1.0;
+      const Dd lE0 = dd(log(E0d));
+      const double X0 = interp_logE(P.tab, P.tab.col(0, DP_COL_E), P.tab.col(0, DP_COL_LOGE),
+                                    P.tab.col(P.rock, DP_COL_CSDA_R), dd(E0d), lE0, nullptr).v;
+      const float S0 = float(interp_logE(P.tab, P.tab.col(0, DP_COL_E), P.tab.col(0, DP_COL_LOGE),
+                                         P.tab.col(P.rock, DP_COL_CSDA_S), dd(E0d), lE0, nullptr).v);
+      const float E0 = float(E0d);
+      float yh = float(X0), yl = float(X0 - double(yh));
+      int i0 = walk(RH, n, yh, P.tab.uniform ? uniform_interval(P.tab.col(0, DP_COL_LOGE), n, lE0.v,
+                                                                  P.tab.lE0, P.tab.inv_dlE)
+                                              : 0);
+      int i = i0;
+      float Eprev = E0, E = E0, u = 0.0f, dsum = 0.0f;
+      bool clamped = false;
+      for (int s = 0; s < nseg; ++s) {
+        ff_add(yh, yl, sG[s]);
+        i = walk(RH, n, yh, i);
+        clamped = !(yh < RH[n - 1]);
+        u = clamped ? DLE[n - 2] : fminf(((yh - RH[i]) + (yl - RL[i])) * SLO[i], DLE[i]);
+        if (clamped) i = n - 2;
+        E = clamped ? Emax : EE[i] * __expf(u);
+        float x = 0.5f * (Eprev + E) * inv_m;
+        dsum -= sL[s] * rsqrtf(x * (x + 2.0f));
+        Eprev = E;
+      }
+      const float EN = E, uN = u;
+      const int iN = i;
+      const bool clampN = clamped;
+      const float SN = SR[iN] + uN * DS[iN];
+      // air column: R_air(E_N) on the same energy interval, + closed-form grammage
+      float ah = aRH[iN], al = aRL[iN];
+      ff_add(ah, al, uN / aSLO[iN]);
+      ff_add(ah, al, Gh);
+      al += Gl;
+      int j = walk(aRH, n, ah, iN);
+      const bool clampF = !(ah < aRH[n - 1]);
+      const float ua = clampF ? DLE[n - 2] : fminf(((ah - aRH[j]) + (al - aRL[j])) * aSLO[j], DLE[j]);
+      if (clampF) j = n - 2;
+      const float Ef = clampF ? Emax : EE[j] * __expf(ua);
+      const float SaN = aS[iN] + uN * aDS[iN], SaF = aS[j] + ua * aDS[j];
+      const float xa = 0.5f * (EN + Ef) * inv_m;
+      const float ibga = rsqrtf(xa * (xa + 2.0f));
+      const float w = (SN / S0) * (SaF / SaN) * __expf((dsum - Lair * ibga) * inv_ctau);
+      float dlogF = 0.0f;
+      const float F = float(gccly_flux(double(cs), double(cs129), double(Ef),
+                                       active ? P.nq[nd] : 0.0, ADJ ? nullptr : nullptr));
+      const float f = active ? w * F : 0.0f;
+      const double coef = active ? 2.0 * P.nw[nd] / P.n_nodes : 0.0;
+      fsum += coef * double(f);
+      if (ADJ) {
+        // d log F / dE in single precision
+        {
+          float Emu = Ef + float(kMuonMass);
+          float a = 3.64f / (Emu * cs129);
+          float ec = 1.1f * Emu * cs;
+          float rpi = 1.0f + ec / 115.0f, rK = 1.0f + ec / 850.0f;
+          float h = 1.0f / rpi + 0.054f / rK;
+          float dh = -(1.1f * cs / 115.0f) / (rpi * rpi) - 0.054f * (1.1f * cs / 850.0f) / (rK * rK);
+          dlogF = 2.7f * a / (Emu * (1.0f + a)) - 2.7f / Emu + dh / h;
+        }
+        const float cf = float(coef) * f;
+        float lam = 0.0f;
+        if (cf != 0.0f) {
+          const float aA = Lair * (xa + 1.0f) * ibga * ibga * ibga / m_ctau;
+          const float dEf = (clampF || clampN) ? 0.0f : (Ef * aSLO[j]) / (EN * aSLO[iN]);
+          const float dSr = clampN ? 0.0f : DS[iN] / (SN * EN);
+          const float dSaN = clampN ? 0.0f : aDS[iN] / (SaN * EN);
+          const float dSaF = clampF ? 0.0f : aDS[j] / (SaF * Ef);
+          lam = dSr - dSaN + 0.5f * aA + dEf * (dSaF + 0.5f * aA + dlogF);
+        }
+        float Ek = EN;
+        int ik = iN;
+        bool ck = clampN;
+        for (int s = nseg - 1; s >= 0; --s) {
+          // previous point E_{k-1}
+          ff_add(yh, yl, -sG[s]);
+          float Ekm1;
+          int im;
+          if (s == 0) {
+            Ekm1 = E0;
+            im = i0;
+          } else {
+            im = walk(RH, n, yh, ik);
+            float um = fminf(fmaxf(((yh - RH[im]) + (yl - RL[im])) * SLO[im], 0.0f), DLE[im]);
+            Ekm1 = EE[im] * __expf(um);
+            if (!(yh < RH[n - 1])) {
+              Ekm1 = Emax;
+              im = n - 2;
+            }
+          }
+          const bool cm = !(Ekm1 < Emax);
+          const float Kp = ck ? 0.0f : Ek * SLO[ik];
+          const float x = 0.5f * (Ekm1 + Ek) * inv_m;
+          const float ib = rsqrtf(x * (x + 2.0f));
+          const float a = sL[s] * (x + 1.0f) * ib * ib * ib / m_ctau;
+          lam += 0.5f * a;
+          float v = cf * lam * Kp * sL[s];
+          const float Rp = cm ? 0.0f : 1.0f / (Ekm1 * SLO[im]);
+          lam = lam * Kp * Rp + 0.5f * a;
+          for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+          if (lane == 0) sJ[s] += v;
+          Ek = Ekm1;
+          ik = im;
+          ck = cm;
+        }
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) fsum += __shfl_xor_sync(0xffffffffu, fsum, o);
+    if (lane == 0) P.flux[r] = fsum;
+    __syncwarp();
+    if (ADJ)
+      for (int s = lane; s < nseg; s += 32) P.jval32[off + s] = sJ[s];
+    __syncwarp();
+  }
+}
+
+// J^T r over the precomputed CSC permutation (fixed order per cell).
+template <class V>
+__global__ void gather_kernel(const int64_t* cptr, const int32_t* perm, const V* val,
+                              const int32_t* row_of, const double* cot, long ncell, double* grad) {
+  long c = blockIdx.x * long(blockDim.x) + threadIdx.x;
+  if (c >= ncell) return;
   double s = 0.0;
-  for (int64_t i = b; i < e; ++i) s += val[perm[i]] * cot[row_of[perm[i]]];
+  for (int64_t p = cptr[c], e = cptr[c + 1]; p < e; ++p) {
+    int32_t k = perm[p];
+    s += double(val[k]) * cot[row_of[k]];
+  }
   grad[c] = s;
 }
 
 // ---------------------------------------------------------------- plain form
 // Plain FP64 form: one launch per ray, one thread per node, global tables,
-// bisection lookups, no staging.
-__global__ void plain_ray_kernel(TomoDev P, long r) {
+// bisection lookups, no staging, the ray traced by every thread.
+__global__ void plain_ray_kernel(EvalP P, GridDev g, int side_cell, long r, double* part) {
   int nd = threadIdx.x;
   if (nd >= P.n_nodes) return;
   const TabView& t = P.tab;
@@ -444,10 +642,10 @@ __global__ void plain_ray_kernel(TomoDev P, long r) {
     w *= exp(decay_log(L, (E + Ek) / 2.0, P.mass, P.ctau, nullptr));
     E = Ek;
   };
-  trace(P.g, ray, 1 << 30, &z_exit, [&](int, int cell, double L) { seg(P.rho[cell], L); });
+  trace(g, ray, 1 << 30, &z_exit, [&](int, int cell, double L) { seg(P.rho[cell], L); });
   double cs_safe = fmax(fabs(ray.cos_theta), 0.01);
-  if (z_exit < P.g.zmax - kEps64)
-    seg(P.side_cell >= 0 ? P.rho[P.side_cell] : P.side_density, (P.g.zmax - z_exit) / cs_safe);
+  if (z_exit < g.zmax - kEps64)
+    seg(side_cell >= 0 ? P.rho[side_cell] : P.side_density, (g.zmax - z_exit) / cs_safe);
   double f = 0.0;
   if (ok) {
     double Xa = interp_logE(tb, E_, lE, aR, dd(E), dd(log(E)), nullptr).v;
@@ -455,12 +653,11 @@ __global__ void plain_ray_kernel(TomoDev P, long r) {
     double Ef = inverse_range(aR, E_, lE, t.n, dd(Xa + Gair), nullptr).v;
     w *= interp_logE(tb, E_, lE, aS, dd(Ef), dd(log(Ef)), nullptr).v /
          interp_logE(tb, E_, lE, aS, dd(E), dd(log(E)), nullptr).v;
-    w *= exp(decay_log((P.H - P.g.zmax) / cs_safe, (E + Ef) / 2.0, P.mass, P.ctau, nullptr));
+    w *= exp(decay_log((P.H - g.zmax) / cs_safe, (E + Ef) / 2.0, P.mass, P.ctau, nullptr));
     double cs = cos_theta_star(ray.cos_theta);
     f = w * gccly_flux(cs, pow(cs, 1.29), Ef, P.nq[nd], nullptr);
   }
-  // per-node result; the host-side sum is part of the plain form
-  P.val[r * P.n_nodes + nd] = 2.0 * P.nw[nd] * f / P.n_nodes;
+  part[r * P.n_nodes + nd] = 2.0 * P.nw[nd] * f / P.n_nodes;
 }
 __global__ void plain_sum_kernel(const double* v, long n_rays, int n_nodes, double* flux) {
   long r = blockIdx.x * long(blockDim.x) + threadIdx.x;
@@ -470,50 +667,7 @@ __global__ void plain_sum_kernel(const double* v, long n_rays, int n_nodes, doub
   flux[r] = s;
 }
 
-// ---------------------------------------------------------------- host side
-struct Scratch {
-  char* p;
-  size_t off = 0;
-  template <class T>
-  T* take(size_t n) {
-    off = (off + 255) & ~size_t(255);
-    T* r = reinterpret_cast<T*>(p + off);
-    off += n * sizeof(T);
-    return r;
-  }
-};
-
-static int make_params(dp_ctx* ctx, const dp_physics* ph, const dp_grid* gr, const dp_tomo_params* tp,
-                       TomoDev& P) {
-  if (!ctx || !ph || !gr || !tp) return fail(ctx, DP_ERR_ARG, "null argument");
-  if (gr->nx <= 0 || gr->ny <= 0 || gr->nz <= 0 || !(gr->dx > 0) || !(gr->dy > 0) || !(gr->dz > 0))
-    return fail(ctx, DP_ERR_ARG, "invalid grid");
-  if (tp->n_nodes <= 0 || !tp->node_energy || !tp->node_charge || !tp->node_weight)
-    return fail(ctx, DP_ERR_ARG, "energy nodes required");
-  if (tp->rock_material < 0 || tp->rock_material >= ph->n_mat || tp->air_material < 0 ||
-      tp->air_material >= ph->n_mat)
-    return fail(ctx, DP_ERR_ARG, "material index out of range");
-  long ncell = long(gr->nx) * gr->ny * gr->nz;
-  if (tp->side_cell >= ncell) return fail(ctx, DP_ERR_ARG, "side_cell out of range");
-  P = TomoDev{};
-  P.tab = ph->view;
-  P.g = GridDev{gr->nx, gr->ny, gr->nz, gr->x0, gr->y0, gr->z0, gr->dx, gr->dy, gr->dz,
-                gr->x0 + gr->nx * gr->dx, gr->y0 + gr->ny * gr->dy, gr->z0 + gr->nz * gr->dz};
-  P.rock = tp->rock_material;
-  P.air = tp->air_material;
-  P.side_cell = tp->side_cell;
-  P.side_density = tp->side_density;
-  P.H = tp->primary_altitude > 0 ? tp->primary_altitude : 3e4;
-  P.mass = ph->settings.mass;
-  P.ctau = ph->settings.ctau;
-  P.n_nodes = tp->n_nodes;
-  // the reference march stops after 1000 steps; one segment per crossed plane
-  P.seg_cap = std::min(1001, gr->nx + gr->ny + gr->nz + 64) + 1;
-  P.air_dexp = std::exp(-P.g.zmax / 12e3) - std::exp(-P.H / 12e3);
-  P.err_flag = ctx->d_flag;
-  return DP_OK;
-}
-
+// ============================================================ host side
 static int check(dp_ctx* ctx) {
   int flag = 0;
   DP_CHECK_CUDA(ctx, cudaMemcpyAsync(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -521,281 +675,427 @@ static int check(dp_ctx* ctx) {
   if (flag) {
     cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream);
     cudaStreamSynchronize(ctx->stream);
-    return fail(ctx, DP_ERR_STATE, flag == 2 ? "ray segment buffer overflow" : "table-staging wait exceeded its limit");
+    return fail(ctx, DP_ERR_STATE,
+                flag == 2 ? "ray segment buffer overflow" : "table-staging wait exceeded its limit");
   }
   return DP_OK;
 }
 
-static size_t tomo_smem(const TomoDev& P) {
-  return size_t(T_NCOL) * P.tab.ld * sizeof(double) + size_t(4) * P.seg_cap * (3 * sizeof(double) + sizeof(int));
+static void launch_scan(dp_ctx* ctx, const int64_t* in, int64_t* out, long n, int64_t* totals) {
+  long nb = (n + kScan - 1) / kScan;
+  if (nb < 1) nb = 1;
+  scan_blocks<<<int(nb), kScan, 0, ctx->stream>>>(in, out, n, totals);
+  scan_totals<<<1, kScan, 0, ctx->stream>>>(totals, nb, totals + nb + 1);
+  scan_add<<<int(nb), kScan, 0, ctx->stream>>>(out, n, totals, totals + nb + 1);
+  ctx->launches += 3;
 }
 
-// Device-pointer core.  cot == nullptr: forward only.  Jacobian outputs when
-// row_ptr/col/val are given (device).  grad: J^T cot.
-static int tomo_core(dp_ctx* ctx, TomoDev& P, long n_rays, const dp_ray* rays, const double* rho,
-                     const double* nE, const double* nq, const double* nw, double* flux,
-                     const double* cot, double* grad, int64_t* row_ptr_out, int32_t* col_out,
-                     double* val_out, int64_t nnz_cap, int64_t* nnz_out) {
-  P.rays = rays;
-  P.n_rays = n_rays;
+template <class T>
+static T* dalloc(std::vector<void*>& keep, size_t n) {
+  void* p = nullptr;
+  if (cudaMalloc(&p, (n ? n : 1) * sizeof(T)) != cudaSuccess) return nullptr;
+  keep.push_back(p);
+  return static_cast<T*>(p);
+}
+
+static void free_paths_arrays(dp_paths* p) {
+  for (void* x : {(void*)p->rays, (void*)p->row_ptr, (void*)p->cell, (void*)p->len,
+                  (void*)p->row_of, (void*)p->cptr, (void*)p->perm})
+    if (x) cudaFree(x);
+}
+
+// Builds the paths handle from device rays.
+static int build_paths(dp_ctx* ctx, const dp_grid& gr, const dp_ray* d_rays_in, long n_rays,
+                       int side_cell, bool copy_rays, dp_paths** out) {
+  long ncell = long(gr.nx) * gr.ny * gr.nz;
+  dp_paths* P = new dp_paths;
+  P->ctx = ctx;
+  P->grid = gr;
+  P->side_cell = side_cell;
+  P->n_rays = n_rays;
+  std::vector<void*> tmp;
+  auto bail = [&](int code, const char* msg) {
+    for (void* x : tmp) cudaFree(x);
+    free_paths_arrays(P);
+    delete P;
+    return fail(ctx, code, msg);
+  };
+  if (copy_rays) {
+    if (cudaMalloc(&P->rays, sizeof(dp_ray) * (n_rays ? n_rays : 1)) != cudaSuccess)
+      return bail(DP_ERR_ALLOC, "device allocation failed");
+    if (cudaMemcpyAsync(P->rays, d_rays_in, sizeof(dp_ray) * n_rays, cudaMemcpyDeviceToDevice,
+                        ctx->stream) != cudaSuccess)
+      return bail(DP_ERR_CUDA, "ray copy failed");
+  }
+  const dp_ray* rays = copy_rays ? P->rays : d_rays_in;
+  const int cap = std::min(1001, gr.nx + gr.ny + gr.nz + 64) + 1;
+  long nbr = (n_rays + kScan) / kScan + 1;
+  int32_t* slot_cell = dalloc<int32_t>(tmp, size_t(n_rays) * cap);
+  double* slot_len = dalloc<double>(tmp, size_t(n_rays) * cap);
+  int64_t* counts = dalloc<int64_t>(tmp, n_rays + 1);
+  int64_t* totals = dalloc<int64_t>(tmp, nbr + 2);
+  if (cudaMalloc(&P->row_ptr, sizeof(int64_t) * (n_rays + 1)) != cudaSuccess || !slot_cell ||
+      !slot_len || !counts || !totals)
+    return bail(DP_ERR_ALLOC, "device allocation failed");
+  GridDev g = grid_dev(gr);
+  timed_begin(ctx);
+  trace_kernel<<<int((n_rays + 127) / 128), 128, 0, ctx->stream>>>(g, rays, n_rays, cap, side_cell,
+                                                                     slot_cell, slot_len, counts,
+                                                                     ctx->d_flag);
+  timed_end(ctx, "tomo_trace");
+  launch_scan(ctx, counts, P->row_ptr, n_rays, totals);
+  int64_t nnz = 0;
+  if (cudaMemcpyAsync(&nnz, P->row_ptr + n_rays, 8, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess)
+    return bail(DP_ERR_CUDA, "copy failed");
+  int rc = check(ctx);
+  if (rc) {
+    std::string m = ctx->err;
+    return bail(rc, m.c_str());
+  }
+  // longest list
+  std::vector<int64_t> hc(n_rays);
+  cudaMemcpy(hc.data(), counts, 8 * n_rays, cudaMemcpyDeviceToHost);
+  int mx = 0;
+  for (long r = 0; r < n_rays; ++r) mx = std::max<int>(mx, int(hc[r]));
+  P->nnz = nnz;
+  P->max_seg = mx;
+  if (cudaMalloc(&P->cell, sizeof(int32_t) * (nnz + 1)) != cudaSuccess ||
+      cudaMalloc(&P->len, sizeof(double) * (nnz + 1)) != cudaSuccess ||
+      cudaMalloc(&P->row_of, sizeof(int32_t) * (nnz + 1)) != cudaSuccess ||
+      cudaMalloc(&P->cptr, sizeof(int64_t) * (ncell + 1)) != cudaSuccess ||
+      cudaMalloc(&P->perm, sizeof(int32_t) * (nnz + 1)) != cudaSuccess)
+    return bail(DP_ERR_ALLOC, "device allocation failed");
+  long tot = n_rays * long(cap);
+  compact_kernel<<<int((tot + 255) / 256), 256, 0, ctx->stream>>>(P->row_ptr, n_rays, cap, slot_cell,
+                                                                   slot_len, P->cell, P->len, P->row_of);
+  ++ctx->launches;
+  // CSC permutation (entries of the side remainder at a fixed density excluded)
+  long nbc = (ncell + kScan) / kScan + 1;
+  int64_t* ccount = dalloc<int64_t>(tmp, ncell + 1);
+  int32_t* cursor = dalloc<int32_t>(tmp, ncell + 1);
+  int64_t* ctot = dalloc<int64_t>(tmp, nbc + 2);
+  if (!ccount || !cursor || !ctot) return bail(DP_ERR_ALLOC, "device allocation failed");
+  cudaMemsetAsync(ccount, 0, 8 * (ncell + 1), ctx->stream);
+  cudaMemsetAsync(cursor, 0, 4 * (ncell + 1), ctx->stream);
+  if (nnz > 0) hist_kernel<<<int((nnz + 255) / 256), 256, 0, ctx->stream>>>(P->cell, nnz, ccount);
+  launch_scan(ctx, ccount, P->cptr, ncell, ctot);
+  if (nnz > 0) place_kernel<<<int((nnz + 255) / 256), 256, 0, ctx->stream>>>(P->cell, nnz, P->cptr, cursor, P->perm);
+  sort_buckets_kernel<<<int((ncell + 255) / 256), 256, 0, ctx->stream>>>(P->cptr, ncell, P->perm);
+  ctx->launches += 3;
+  if (cudaGetLastError() != cudaSuccess) return bail(DP_ERR_CUDA, "path build launch failed");
+  rc = check(ctx);
+  for (void* x : tmp) cudaFree(x);
+  tmp.clear();
+  if (rc) {
+    free_paths_arrays(P);
+    delete P;
+    return rc;
+  }
+  *out = P;
+  return DP_OK;
+}
+
+static int make_eval(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, const dp_tomo_params* tp,
+                     EvalP& P) {
+  if (!ctx || !ph || !pa || !tp) return fail(ctx, DP_ERR_ARG, "null argument");
+  if (tp->n_nodes <= 0 || !tp->node_energy || !tp->node_charge || !tp->node_weight)
+    return fail(ctx, DP_ERR_ARG, "energy nodes required");
+  if (tp->rock_material < 0 || tp->rock_material >= ph->n_mat || tp->air_material < 0 ||
+      tp->air_material >= ph->n_mat)
+    return fail(ctx, DP_ERR_ARG, "material index out of range");
+  P = EvalP{};
+  P.tab = ph->view;
+  P.tab32 = ph->dev32;
+  P.ld32 = ph->ld32;
+  P.rock = tp->rock_material;
+  P.air = tp->air_material;
+  P.n_nodes = tp->n_nodes;
+  P.seg_cap = std::max(pa->max_seg, 1);
+  P.H = tp->primary_altitude > 0 ? tp->primary_altitude : 3e4;
+  P.mass = ph->settings.mass;
+  P.ctau = ph->settings.ctau;
+  P.zmax = pa->grid.z0 + pa->grid.nz * pa->grid.dz;
+  P.air_dexp = std::exp(-P.zmax / 12e3) - std::exp(-P.H / 12e3);
+  P.side_density = tp->side_density;
+  P.rays = pa->rays;
+  P.n_rays = pa->n_rays;
+  P.row_ptr = pa->row_ptr;
+  P.cell = pa->cell;
+  P.len = pa->len;
+  P.err_flag = ctx->d_flag;
+  return DP_OK;
+}
+
+// Core evaluation on device pointers.  precision: 0 = FP64, 1 = mixed.
+static int eval_core(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, const dp_tomo_params* tp,
+                     const double* rho, const double* nE, const double* nq, const double* nw,
+                     const double* cot, double* flux, double* grad, double* jac, int precision) {
+  EvalP P;
+  int rc = make_eval(ctx, ph, pa, tp, P);
+  if (rc) return rc;
+  if (pa->n_rays == 0) return DP_OK;
   P.rho = rho;
   P.nE = nE;
   P.nq = nq;
   P.nw = nw;
   P.flux = flux;
-  size_t smem = tomo_smem(P);
+  const bool adj = (cot && grad) || jac;
+  long ncell = long(pa->grid.nx) * pa->grid.ny * pa->grid.nz;
+  void* jbuf = nullptr;
+  if (adj) {
+    size_t b = size_t(pa->nnz + 1) * (precision ? 4 : 8);
+    jbuf = jac && !precision ? (void*)jac : scratch(ctx, b, 1);
+    if (!jbuf) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
+  }
+  long blocks = std::min<long>((pa->n_rays + kWarps - 1) / kWarps, 152L * 16);
+  size_t smem;
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(tomo_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(tomo_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(eval64_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    cudaFuncSetAttribute(eval64_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    cudaFuncSetAttribute(eval32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    cudaFuncSetAttribute(eval32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     attr = true;
   }
-  long blocks = (n_rays + 3) / 4;
-  if (blocks > 152L * 8) blocks = 152L * 8;
-  const bool need_j = cot || row_ptr_out;
-  if (!need_j) {
-    timed_begin(ctx);
-    tomo_kernel<0><<<int(blocks), 128, smem, ctx->stream>>>(P);
-    DP_CHECK_CUDA(ctx, cudaGetLastError());
-    timed_end(ctx, "tomo_forward");
-    return check(ctx);
-  }
-  long ncell = long(P.g.nx) * P.g.ny * P.g.nz;
-  long nbr = (n_rays + 1 + kScan - 1) / kScan;
-  // slot 0: per-ray arrays; slot 1: per-entry and per-cell arrays
-  size_t est = size_t(n_rays + 2) * 8 * 2 + size_t(nbr + 2) * 8 + 4096;
-  Scratch s0{static_cast<char*>(scratch(ctx, est, 0))};
-  if (!s0.p) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
-  int64_t* counts = s0.take<int64_t>(n_rays + 1);
-  int64_t* rptr = row_ptr_out ? row_ptr_out : s0.take<int64_t>(n_rays + 1);
-  int64_t* totals = s0.take<int64_t>(nbr + 2);
-  int64_t* grand = totals + nbr + 1;
-  tomo_count_kernel<<<int((n_rays + 127) / 128), 128, 0, ctx->stream>>>(P.g, rays, n_rays, P.seg_cap,
-                                                                          counts, ctx->d_flag);
-  scan_blocks<<<int(nbr), kScan, 0, ctx->stream>>>(counts, rptr, n_rays, totals);
-  scan_totals<<<1, kScan, 0, ctx->stream>>>(totals, nbr, grand);
-  scan_add<<<int(nbr), kScan, 0, ctx->stream>>>(rptr, n_rays, totals, grand);
-  DP_CHECK_CUDA(ctx, cudaGetLastError());
-  ctx->launches += 4;
-  int64_t nnz = 0;
-  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(&nnz, rptr + n_rays, 8, cudaMemcpyDeviceToHost, ctx->stream));
-  int rc = check(ctx);
-  if (rc) return rc;
-  if (nnz_out) *nnz_out = nnz;
-  if (row_ptr_out && nnz > nnz_cap) return fail(ctx, DP_ERR_ARG, "nnz_cap too small");
-  long nbc = (ncell + 1 + kScan - 1) / kScan;
-  size_t need = size_t(nnz + 1) * (4 + 8 + 4 + 4) + size_t(ncell + 1) * (8 + 8 + 4 + 4) +
-                size_t(nbc + 2) * 8 + 16 * 256;
-  Scratch s1{static_cast<char*>(scratch(ctx, need, 1))};
-  if (!s1.p) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
-  int32_t* col = col_out ? col_out : s1.take<int32_t>(nnz + 1);
-  double* val = val_out ? val_out : s1.take<double>(nnz + 1);
-  int32_t* row_of = cot ? s1.take<int32_t>(nnz + 1) : nullptr;
-  Scratch& s0c = s1;
-  P.row_ptr = rptr;
-  P.col = col;
-  P.val = val;
-  P.row_of = row_of;
   timed_begin(ctx);
-  tomo_kernel<1><<<int(blocks), 128, smem, ctx->stream>>>(P);
+  if (precision == 0) {
+    smem = size_t(T_NCOL) * P.tab.ld * 8 + size_t(kWarps) * P.seg_cap * 3 * 8;
+    if (smem > 220 * 1024) return fail(ctx, DP_ERR_ARG, "ray too long for the FP64 kernel");
+    P.jval64 = static_cast<double*>(jbuf);
+    if (adj) eval64_kernel<true><<<int(blocks), kWarps * 32, smem, ctx->stream>>>(P);
+    else eval64_kernel<false><<<int(blocks), kWarps * 32, smem, ctx->stream>>>(P);
+  } else {
+    smem = size_t(2 * kNC32) * P.ld32 * 4 + size_t(kWarps) * P.seg_cap * 3 * 4;
+    if (smem > 220 * 1024) return fail(ctx, DP_ERR_ARG, "ray too long for the mixed kernel");
+    P.jval32 = static_cast<float*>(jbuf);
+    if (adj) eval32_kernel<true><<<int(blocks), kWarps * 32, smem, ctx->stream>>>(P);
+    else eval32_kernel<false><<<int(blocks), kWarps * 32, smem, ctx->stream>>>(P);
+  }
   DP_CHECK_CUDA(ctx, cudaGetLastError());
-  timed_end(ctx, "tomo_adjoint");
-  if (cot && grad) {
-    int32_t* ccount = s0c.take<int32_t>(ncell + 1);
-    int32_t* cursor = s0c.take<int32_t>(ncell + 1);
-    int64_t* ccount64 = s0c.take<int64_t>(ncell + 1);
-    int64_t* cptr = s0c.take<int64_t>(ncell + 1);
-    int64_t* ctot = s0c.take<int64_t>(nbc + 2);
-    int32_t* perm = s0c.take<int32_t>(nnz + 1);
-    DP_CHECK_CUDA(ctx, cudaMemsetAsync(ccount, 0, size_t(ncell + 1) * 4, ctx->stream));
-    DP_CHECK_CUDA(ctx, cudaMemsetAsync(cursor, 0, size_t(ncell + 1) * 4, ctx->stream));
-    int tb = 256;
+  timed_end(ctx, adj ? "tomo_adjoint" : "tomo_forward");
+  if (adj && cot && grad) {
     timed_begin(ctx);
-    ctx->launches += nnz > 0 ? 6 : 4;
-    if (nnz > 0) hist_kernel<<<int((nnz + tb - 1) / tb), tb, 0, ctx->stream>>>(col, nnz, ccount);
-    i32_to_i64<<<int((ncell + tb - 1) / tb), tb, 0, ctx->stream>>>(ccount, ccount64, ncell);
-    scan_blocks<<<int(nbc), kScan, 0, ctx->stream>>>(ccount64, cptr, ncell, ctot);
-    scan_totals<<<1, kScan, 0, ctx->stream>>>(ctot, nbc, ctot + nbc + 1);
-    scan_add<<<int(nbc), kScan, 0, ctx->stream>>>(cptr, ncell, ctot, ctot + nbc + 1);
-    if (nnz > 0) place_kernel<<<int((nnz + tb - 1) / tb), tb, 0, ctx->stream>>>(col, nnz, cptr, cursor, perm);
-    gather_kernel<<<int((ncell + tb - 1) / tb), tb, 0, ctx->stream>>>(cptr, perm, val, row_of, cot, ncell, grad);
+    if (precision == 0)
+      gather_kernel<double><<<int((ncell + 255) / 256), 256, 0, ctx->stream>>>(
+          pa->cptr, pa->perm, static_cast<const double*>(jbuf), pa->row_of, cot, ncell, grad);
+    else
+      gather_kernel<float><<<int((ncell + 255) / 256), 256, 0, ctx->stream>>>(
+          pa->cptr, pa->perm, static_cast<const float*>(jbuf), pa->row_of, cot, ncell, grad);
     DP_CHECK_CUDA(ctx, cudaGetLastError());
     timed_end(ctx, "tomo_transpose");
   }
+  if (jac && precision) {
+    // widen the single-precision Jacobian into the caller's buffer
+    std::vector<float> h(pa->nnz);
+    std::vector<double> d(pa->nnz);
+    DP_CHECK_CUDA(ctx, cudaMemcpyAsync(h.data(), jbuf, 4 * pa->nnz, cudaMemcpyDeviceToHost, ctx->stream));
+    DP_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int64_t k = 0; k < pa->nnz; ++k) d[k] = h[k];
+    DP_CHECK_CUDA(ctx, cudaMemcpyAsync(jac, d.data(), 8 * pa->nnz, cudaMemcpyHostToDevice, ctx->stream));
+  }
   return check(ctx);
 }
-
-struct HostTomo {
-  dp_ray* rays;
-  double *rho, *nE, *nq, *nw, *flux, *cot, *grad;
-};
 
 }  // namespace dp
 
 using namespace dp;
 
-static int upload_common(dp_ctx* ctx, const dp_physics* ph, const dp_grid* gr, const dp_tomo_params* tp,
-                         const double* rho, long n_rays, const dp_ray* rays, TomoDev& P,
-                         std::vector<void*>& allocs, HostTomo& d) {
-  int rc = make_params(ctx, ph, gr, tp, P);
-  if (rc) return rc;
-  if (n_rays < 0 || (n_rays > 0 && (!rays || !rho))) return fail(ctx, DP_ERR_ARG, "bad ray/density arrays");
-  DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+namespace {
+// Device copies of host inputs, freed on scope exit.
+struct DevBufs {
+  std::vector<void*> keep;
+  ~DevBufs() {
+    for (void* p : keep) cudaFree(p);
+  }
+  template <class T>
+  T* up(dp_ctx* ctx, const T* h, size_t n) {
+    T* d = dalloc<T>(keep, n);
+    if (d && n) cudaMemcpyAsync(d, h, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream);
+    return d;
+  }
+  template <class T>
+  T* make(size_t n) {
+    return dalloc<T>(keep, n);
+  }
+};
+
+int host_eval(dp_ctx* ctx, const dp_physics* ph, const dp_grid* gr, const dp_tomo_params* tp,
+              const double* rho, long n_rays, const dp_ray* rays, const double* cot, double* flux,
+              double* grad, int64_t* row_ptr, int32_t* col, double* val, int64_t nnz_cap,
+              int64_t* nnz, int precision) {
+  if (!ctx || !ph || !gr || !tp) return fail(ctx, DP_ERR_ARG, "null argument");
+  if (gr->nx <= 0 || gr->ny <= 0 || gr->nz <= 0 || !(gr->dx > 0) || !(gr->dy > 0) || !(gr->dz > 0))
+    return fail(ctx, DP_ERR_ARG, "invalid grid");
   long ncell = long(gr->nx) * gr->ny * gr->nz;
-  auto al = [&](size_t b) -> void* {
-    void* p = nullptr;
-    if (cudaMalloc(&p, b ? b : 8) != cudaSuccess) return nullptr;
-    allocs.push_back(p);
-    return p;
-  };
-  d.rays = (dp_ray*)al(sizeof(dp_ray) * n_rays);
-  d.rho = (double*)al(8 * ncell);
-  d.nE = (double*)al(8 * tp->n_nodes);
-  d.nq = (double*)al(8 * tp->n_nodes);
-  d.nw = (double*)al(8 * tp->n_nodes);
-  d.flux = (double*)al(8 * n_rays);
-  for (void* p : allocs)
-    if (!p) return fail(ctx, DP_ERR_ALLOC, "device allocation failed");
-  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(d.rays, rays, sizeof(dp_ray) * n_rays, cudaMemcpyHostToDevice, ctx->stream));
-  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(d.rho, rho, 8 * ncell, cudaMemcpyHostToDevice, ctx->stream));
-  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(d.nE, tp->node_energy, 8 * tp->n_nodes, cudaMemcpyHostToDevice, ctx->stream));
-  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(d.nq, tp->node_charge, 8 * tp->n_nodes, cudaMemcpyHostToDevice, ctx->stream));
-  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(d.nw, tp->node_weight, 8 * tp->n_nodes, cudaMemcpyHostToDevice, ctx->stream));
+  if (tp->side_cell >= ncell) return fail(ctx, DP_ERR_ARG, "side_cell out of range");
+  if (n_rays < 0 || (n_rays > 0 && (!rays || !rho || !flux))) return fail(ctx, DP_ERR_ARG, "bad arrays");
+  if (n_rays == 0) return DP_OK;
+  DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  DevBufs b;
+  dp_ray* drays = b.up(ctx, rays, n_rays);
+  double* drho = b.up(ctx, rho, ncell);
+  double* dE = b.up(ctx, tp->node_energy, tp->n_nodes);
+  double* dq = b.up(ctx, tp->node_charge, tp->n_nodes);
+  double* dw = b.up(ctx, tp->node_weight, tp->n_nodes);
+  double* dflux = b.make<double>(n_rays);
+  double* dcot = cot ? b.up(ctx, cot, n_rays) : nullptr;
+  double* dgrad = grad ? b.make<double>(ncell) : nullptr;
+  if (!drays || !drho || !dE || !dq || !dw || !dflux || (cot && !dcot) || (grad && !dgrad))
+    return fail(ctx, DP_ERR_ALLOC, "device allocation failed");
+  dp_paths* pa = nullptr;
+  int rc = build_paths(ctx, *gr, drays, n_rays, tp->side_cell, false, &pa);
+  if (rc) return rc;
+  pa->rays = drays;  // borrowed; cleared before free
+  double* djac = nullptr;
+  if (row_ptr) {
+    if (pa->nnz > nnz_cap) {
+      *nnz = pa->nnz;
+      pa->rays = nullptr;
+      dp_tomo_paths_free(pa);
+      return fail(ctx, DP_ERR_ARG, "nnz_cap too small");
+    }
+    djac = b.make<double>(pa->nnz + 1);
+  }
+  rc = eval_core(ctx, ph, pa, tp, drho, dE, dq, dw, dcot, dflux, dgrad, djac, precision);
+  if (!rc) {
+    cudaMemcpy(flux, dflux, 8 * n_rays, cudaMemcpyDeviceToHost);
+    if (grad) cudaMemcpy(grad, dgrad, 8 * ncell, cudaMemcpyDeviceToHost);
+    if (row_ptr) {
+      *nnz = pa->nnz;
+      cudaMemcpy(row_ptr, pa->row_ptr, 8 * (n_rays + 1), cudaMemcpyDeviceToHost);
+      if (col) cudaMemcpy(col, pa->cell, 4 * pa->nnz, cudaMemcpyDeviceToHost);
+      if (val) cudaMemcpy(val, djac, 8 * pa->nnz, cudaMemcpyDeviceToHost);
+    }
+  }
+  pa->rays = nullptr;
+  dp_tomo_paths_free(pa);
+  return rc;
+}
+}  // namespace
+
+extern "C" {
+
+int dp_tomo_paths_create(dp_ctx* ctx, const dp_grid* gr, long n_rays, const dp_ray* rays,
+                         int side_cell, dp_paths** out) {
+  if (!ctx || !gr || !out || n_rays < 0 || (n_rays > 0 && !rays)) return fail(ctx, DP_ERR_ARG, "bad arguments");
+  if (gr->nx <= 0 || gr->ny <= 0 || gr->nz <= 0 || !(gr->dx > 0) || !(gr->dy > 0) || !(gr->dz > 0))
+    return fail(ctx, DP_ERR_ARG, "invalid grid");
+  if (side_cell >= long(gr->nx) * gr->ny * gr->nz) return fail(ctx, DP_ERR_ARG, "side_cell out of range");
+  DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  DevBufs b;
+  dp_ray* d = b.up(ctx, rays, n_rays);
+  if (!d) return fail(ctx, DP_ERR_ALLOC, "device allocation failed");
+  return build_paths(ctx, *gr, d, n_rays, side_cell, true, out);
+}
+
+int dp_tomo_paths_create_dev(dp_ctx* ctx, const dp_grid* gr, long n_rays, const dp_ray* rays,
+                             int side_cell, dp_paths** out) {
+  if (!ctx || !gr || !out || n_rays < 0 || (n_rays > 0 && !rays)) return fail(ctx, DP_ERR_ARG, "bad arguments");
+  DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  return build_paths(ctx, *gr, rays, n_rays, side_cell, true, out);
+}
+
+int dp_tomo_paths_free(dp_paths* p) {
+  if (!p) return DP_ERR_ARG;
+  cudaSetDevice(p->ctx->device);
+  free_paths_arrays(p);
+  delete p;
   return DP_OK;
 }
 
-static void free_all(std::vector<void*>& a) {
-  for (void* p : a) cudaFree(p);
-  a.clear();
+int dp_tomo_paths_info(const dp_paths* p, long* n_rays, int64_t* nnz, int* max_segments) {
+  if (!p) return DP_ERR_ARG;
+  if (n_rays) *n_rays = p->n_rays;
+  if (nnz) *nnz = p->nnz;
+  if (max_segments) *max_segments = p->max_seg;
+  return DP_OK;
 }
 
-// Air grammage depends only on the grid top and the ray's cos theta; it is
-// evaluated per ray inside the kernel from this closed form.  The kernel gets
-// the value for cos_theta of each ray through this helper applied on device.
-extern "C" {
+int dp_tomo_paths_csr(const dp_paths* p, int64_t* row_ptr, int32_t* col, double* len) {
+  if (!p) return DP_ERR_ARG;
+  cudaSetDevice(p->ctx->device);
+  if (row_ptr) cudaMemcpy(row_ptr, p->row_ptr, 8 * (p->n_rays + 1), cudaMemcpyDeviceToHost);
+  if (col) cudaMemcpy(col, p->cell, 4 * p->nnz, cudaMemcpyDeviceToHost);
+  if (len) cudaMemcpy(len, p->len, 8 * p->nnz, cudaMemcpyDeviceToHost);
+  return DP_OK;
+}
 
-int dp_tomo_vjp_dev(dp_ctx* ctx, const dp_physics* ph, const dp_grid* gr, const dp_tomo_params* tp,
-                    const double* rho, long n_rays, const dp_ray* rays, const double* cot,
-                    double* flux, double* grad) {
-  TomoDev P;
-  int rc = make_params(ctx, ph, gr, tp, P);
-  if (rc) return rc;
-  if (n_rays <= 0) return n_rays == 0 ? DP_OK : fail(ctx, DP_ERR_ARG, "negative n_rays");
+int dp_tomo_eval_dev(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, const dp_tomo_params* tp,
+                     const double* rho, const double* cot, double* flux, double* grad, double* jac,
+                     int precision) {
+  if (!ctx || !pa || !tp || !rho || !flux) return fail(ctx, DP_ERR_ARG, "null argument");
+  if ((cot == nullptr) != (grad == nullptr)) return fail(ctx, DP_ERR_ARG, "cot and grad go together");
+  if (precision != 0 && precision != 1) return fail(ctx, DP_ERR_ARG, "precision must be 0 or 1");
   DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
-  // Node arrays given as device pointers in tp for this entry point.
-  return tomo_core(ctx, P, n_rays, rays, rho, tp->node_energy, tp->node_charge, tp->node_weight, flux,
-                   cot, grad, nullptr, nullptr, nullptr, 0, nullptr);
+  return eval_core(ctx, ph, pa, tp, rho, tp->node_energy, tp->node_charge, tp->node_weight, cot, flux,
+                   grad, jac, precision);
 }
 
 int dp_tomo_forward(dp_ctx* ctx, const dp_physics* ph, const dp_grid* gr, const dp_tomo_params* tp,
                     const double* rho, long n_rays, const dp_ray* rays, double* flux) {
-  if (!flux && n_rays > 0) return fail(ctx, DP_ERR_ARG, "flux output required");
-  TomoDev P;
-  std::vector<void*> al;
-  HostTomo d{};
-  int rc = upload_common(ctx, ph, gr, tp, rho, n_rays, rays, P, al, d);
-  if (rc || n_rays == 0) {
-    free_all(al);
-    return rc;
-  }
-  rc = tomo_core(ctx, P, n_rays, d.rays, d.rho, d.nE, d.nq, d.nw, d.flux, nullptr, nullptr, nullptr,
-                 nullptr, nullptr, 0, nullptr);
-  if (!rc && cudaMemcpy(flux, d.flux, 8 * n_rays, cudaMemcpyDeviceToHost) != cudaSuccess)
-    rc = fail(ctx, DP_ERR_CUDA, "flux download failed");
-  free_all(al);
-  return rc;
+  return host_eval(ctx, ph, gr, tp, rho, n_rays, rays, nullptr, flux, nullptr, nullptr, nullptr,
+                   nullptr, 0, nullptr, tp ? tp->precision : 0);
 }
 
 int dp_tomo_jacobian(dp_ctx* ctx, const dp_physics* ph, const dp_grid* gr, const dp_tomo_params* tp,
                      const double* rho, long n_rays, const dp_ray* rays, double* flux, int64_t* row_ptr,
                      int32_t* col, double* val, int64_t nnz_cap, int64_t* nnz) {
-  if (!flux || !row_ptr || !nnz || n_rays <= 0) return fail(ctx, DP_ERR_ARG, "bad output arrays");
-  TomoDev P;
-  std::vector<void*> al;
-  HostTomo d{};
-  int rc = upload_common(ctx, ph, gr, tp, rho, n_rays, rays, P, al, d);
-  if (rc) {
-    free_all(al);
-    return rc;
-  }
-  int64_t* drp = nullptr;
-  int32_t* dcol = nullptr;
-  double* dval = nullptr;
-  size_t cap = size_t(nnz_cap > 0 ? nnz_cap : 1);
-  if (cudaMalloc(&drp, 8 * (n_rays + 1)) != cudaSuccess || cudaMalloc(&dcol, 4 * cap) != cudaSuccess ||
-      cudaMalloc(&dval, 8 * cap) != cudaSuccess) {
-    cudaFree(drp);
-    cudaFree(dcol);
-    cudaFree(dval);
-    free_all(al);
-    return fail(ctx, DP_ERR_ALLOC, "device allocation failed");
-  }
-  al.push_back(drp);
-  al.push_back(dcol);
-  al.push_back(dval);
-  rc = tomo_core(ctx, P, n_rays, d.rays, d.rho, d.nE, d.nq, d.nw, d.flux, nullptr, nullptr, drp, dcol,
-                 dval, nnz_cap, nnz);
-  if (!rc) {
-    cudaMemcpy(flux, d.flux, 8 * n_rays, cudaMemcpyDeviceToHost);
-    cudaMemcpy(row_ptr, drp, 8 * (n_rays + 1), cudaMemcpyDeviceToHost);
-    if (col) cudaMemcpy(col, dcol, 4 * size_t(*nnz), cudaMemcpyDeviceToHost);
-    if (val) cudaMemcpy(val, dval, 8 * size_t(*nnz), cudaMemcpyDeviceToHost);
-  }
-  free_all(al);
-  return rc;
+  if (!row_ptr || !nnz) return fail(ctx, DP_ERR_ARG, "row_ptr and nnz required");
+  return host_eval(ctx, ph, gr, tp, rho, n_rays, rays, nullptr, flux, nullptr, row_ptr, col, val,
+                   nnz_cap, nnz, tp ? tp->precision : 0);
 }
 
 int dp_tomo_vjp(dp_ctx* ctx, const dp_physics* ph, const dp_grid* gr, const dp_tomo_params* tp,
                 const double* rho, long n_rays, const dp_ray* rays, const double* cot, double* flux,
                 double* grad) {
-  if (!flux || !cot || !grad || n_rays <= 0) return fail(ctx, DP_ERR_ARG, "bad output arrays");
-  TomoDev P;
-  std::vector<void*> al;
-  HostTomo d{};
-  int rc = upload_common(ctx, ph, gr, tp, rho, n_rays, rays, P, al, d);
-  long ncell = long(gr->nx) * gr->ny * gr->nz;
-  double *dcot = nullptr, *dgrad = nullptr;
-  if (!rc) {
-    if (cudaMalloc(&dcot, 8 * n_rays) != cudaSuccess || cudaMalloc(&dgrad, 8 * ncell) != cudaSuccess)
-      rc = fail(ctx, DP_ERR_ALLOC, "device allocation failed");
-    al.push_back(dcot);
-    al.push_back(dgrad);
-  }
-  if (!rc && cudaMemcpy(dcot, cot, 8 * n_rays, cudaMemcpyHostToDevice) != cudaSuccess)
-    rc = fail(ctx, DP_ERR_CUDA, "cotangent upload failed");
-  if (!rc)
-    rc = tomo_core(ctx, P, n_rays, d.rays, d.rho, d.nE, d.nq, d.nw, d.flux, dcot, dgrad, nullptr,
-                   nullptr, nullptr, 0, nullptr);
-  if (!rc) {
-    cudaMemcpy(flux, d.flux, 8 * n_rays, cudaMemcpyDeviceToHost);
-    cudaMemcpy(grad, dgrad, 8 * ncell, cudaMemcpyDeviceToHost);
-  }
-  free_all(al);
-  return rc;
+  if (!cot || !grad) return fail(ctx, DP_ERR_ARG, "cot and grad required");
+  return host_eval(ctx, ph, gr, tp, rho, n_rays, rays, cot, flux, grad, nullptr, nullptr, nullptr, 0,
+                   nullptr, tp ? tp->precision : 0);
 }
 
 int dp_tomo_forward_plain_dev(dp_ctx* ctx, const dp_physics* ph, const dp_grid* gr,
                               const dp_tomo_params* tp, const double* rho, long n_rays,
                               const dp_ray* rays, double* flux) {
-  TomoDev P;
-  int rc = make_params(ctx, ph, gr, tp, P);
-  if (rc) return rc;
-  if (tp->n_nodes > 1024) return fail(ctx, DP_ERR_ARG, "plain form supports up to 1024 nodes");
+  if (!ctx || !ph || !gr || !tp || n_rays < 0) return fail(ctx, DP_ERR_ARG, "null argument");
+  if (tp->n_nodes <= 0 || tp->n_nodes > 1024) return fail(ctx, DP_ERR_ARG, "1..1024 nodes");
   DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
-  double* part = static_cast<double*>(scratch(ctx, size_t(n_rays) * tp->n_nodes * 8));
+  double* part = static_cast<double*>(scratch(ctx, size_t(n_rays) * tp->n_nodes * 8, 0));
   if (!part) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
-  P.rays = rays;
-  P.n_rays = n_rays;
+  EvalP P{};
+  P.tab = ph->view;
+  P.rock = tp->rock_material;
+  P.air = tp->air_material;
+  P.n_nodes = tp->n_nodes;
+  P.H = tp->primary_altitude > 0 ? tp->primary_altitude : 3e4;
+  P.mass = ph->settings.mass;
+  P.ctau = ph->settings.ctau;
+  GridDev g = grid_dev(*gr);
+  P.zmax = g.zmax;
+  P.air_dexp = std::exp(-P.zmax / 12e3) - std::exp(-P.H / 12e3);
+  P.side_density = tp->side_density;
   P.rho = rho;
+  P.rays = rays;
   P.nE = tp->node_energy;
   P.nq = tp->node_charge;
   P.nw = tp->node_weight;
-  P.val = part;
-  for (long r = 0; r < n_rays; ++r) plain_ray_kernel<<<1, tp->n_nodes, 0, ctx->stream>>>(P, r);
+  for (long r = 0; r < n_rays; ++r)
+    plain_ray_kernel<<<1, tp->n_nodes, 0, ctx->stream>>>(P, g, tp->side_cell, r, part);
   plain_sum_kernel<<<int((n_rays + 127) / 128), 128, 0, ctx->stream>>>(part, n_rays, tp->n_nodes, flux);
   ctx->launches += n_rays + 1;
   DP_CHECK_CUDA(ctx, cudaGetLastError());
   return check(ctx);
+}
+
+// Deprecated single-shot device form kept for callers of the first ABI version.
+int dp_tomo_vjp_dev(dp_ctx* ctx, const dp_physics* ph, const dp_grid* gr, const dp_tomo_params* tp,
+                    const double* rho, long n_rays, const dp_ray* rays, const double* cot,
+                    double* flux, double* grad) {
+  dp_paths* pa = nullptr;
+  int rc = dp_tomo_paths_create_dev(ctx, gr, n_rays, rays, tp ? tp->side_cell : -1, &pa);
+  if (rc) return rc;
+  rc = dp_tomo_eval_dev(ctx, ph, pa, tp, rho, cot, flux, grad, nullptr, tp->precision);
+  dp_tomo_paths_free(pa);
+  return rc;
 }
 
 }  // extern "C"

@@ -288,6 +288,9 @@ def csda_energy_quadrature(n, energy_min, energy_max):
     return E, np.zeros(n), 0.5 * E * span
 
 
+PRECISION = {"fp64": 0, "mixed": 1}
+
+
 class VoxelGrid:
     """Regular density grid; cell c = i + nx*(j + ny*k) (x fastest)."""
 
@@ -323,13 +326,13 @@ class TomoModel:
     """Voxel-density CSDA forward model with its adjoint on one grid."""
 
     def __init__(self, physics, grid, nodes, *, rock="StandardRock", air="Air", side_cell=-1,
-                 side_density=2650.0, primary_altitude=PRIMARY_ALTITUDE):
+                 side_density=2650.0, primary_altitude=PRIMARY_ALTITUDE, precision="fp64"):
         self.physics, self.grid = physics, grid
         self.nE, self.nq, self.nw = (_f64(x) for x in nodes)
         self.params = DpTomoParams(physics.materials[rock], physics.materials[air],
                                    int(side_cell), float(side_density), float(primary_altitude),
                                    len(self.nE), _ptr(self.nE).value, _ptr(self.nq).value,
-                                   _ptr(self.nw).value)
+                                   _ptr(self.nw).value, PRECISION[precision])
         self._g = grid.to_c()
 
     def _args(self, rho, rays):
@@ -375,3 +378,61 @@ class TomoModel:
                                  C.byref(self.params), _ptr(rho), len(rays), _ptr(rays),
                                  _ptr(cot), _ptr(flux), _ptr(grad)), self.physics.ctx.h)
         return flux, grad
+
+
+class TomoPaths:
+    """Rays traced once into device-resident segment lists (dp_paths); every
+    evaluation then works on device tensors (torch CUDA tensors, float64).
+    This is the resident form used by iterative solvers and benchmarks."""
+
+    def __init__(self, physics, grid, rays, nodes, *, rock="StandardRock", air="Air",
+                 side_cell=-1, side_density=2650.0, primary_altitude=PRIMARY_ALTITUDE):
+        import torch
+        self.physics, self.grid = physics, grid
+        dev = torch.device("cuda", physics.ctx.device)
+        self.dev = dev
+        rays = _f64(rays).reshape(-1, 7)
+        self.n_rays = len(rays)
+        self.rays = torch.tensor(rays.ravel(), dtype=torch.float64, device=dev)
+        self.nodes = [torch.tensor(_f64(x), dtype=torch.float64, device=dev) for x in nodes]
+        self.params = DpTomoParams(physics.materials[rock], physics.materials[air],
+                                   int(side_cell), float(side_density), float(primary_altitude),
+                                   len(nodes[0]), *(t.data_ptr() for t in self.nodes), 0)
+        self._g = grid.to_c()
+        h = C.c_void_p()
+        torch.cuda.synchronize(dev)
+        check(load().dp_tomo_paths_create_dev(physics.ctx.h, C.byref(self._g), self.n_rays,
+                                              self.rays.data_ptr(), int(side_cell), C.byref(h)),
+              physics.ctx.h)
+        self.h = h
+        n, nnz, mx = C.c_long(), C.c_int64(), C.c_int()
+        load().dp_tomo_paths_info(self.h, C.byref(n), C.byref(nnz), C.byref(mx))
+        self.nnz, self.max_segments = nnz.value, mx.value
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                load().dp_tomo_paths_free(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    def csr(self):
+        rp = np.zeros(self.n_rays + 1, np.int64)
+        col = np.zeros(max(self.nnz, 1), np.int32)
+        ln = np.zeros(max(self.nnz, 1))
+        load().dp_tomo_paths_csr(self.h, _ptr(rp), _ptr(col), _ptr(ln))
+        return rp, col[:self.nnz], ln[:self.nnz]
+
+    def eval(self, rho, cot=None, *, precision="mixed", flux=None, grad=None, jac=None):
+        """rho (and cot) are float64 CUDA tensors; returns (flux, grad|None, jac|None)."""
+        import torch
+        if flux is None:
+            flux = torch.empty(self.n_rays, dtype=torch.float64, device=self.dev)
+        if cot is not None and grad is None:
+            grad = torch.empty(self.grid.ncell, dtype=torch.float64, device=self.dev)
+        p = lambda t: t.data_ptr() if t is not None else None
+        check(load().dp_tomo_eval_dev(self.physics.ctx.h, self.physics.h, self.h,
+                                      C.byref(self.params), p(rho), p(cot), p(flux), p(grad),
+                                      p(jac), PRECISION[precision]), self.physics.ctx.h)
+        return flux, grad, jac

@@ -63,7 +63,8 @@ class DpTomoParams(C.Structure):
     _fields_ = [("rock_material", C.c_int), ("air_material", C.c_int), ("side_cell", C.c_int),
                 ("side_density", C.c_double), ("primary_altitude", C.c_double),
                 ("n_nodes", C.c_int), ("node_energy", C.c_void_p),
-                ("node_charge", C.c_void_p), ("node_weight", C.c_void_p)]
+                ("node_charge", C.c_void_p), ("node_weight", C.c_void_p),
+                ("precision", C.c_int)]
 
 
 _P = C.c_void_p
@@ -103,6 +104,12 @@ PROTOTYPES = {
                          _VP, _VP]),
     "dp_tomo_vjp_dev": (_I, [_P, _P, C.POINTER(DpGrid), C.POINTER(DpTomoParams), _VP, _L, _VP,
                              _VP, _VP, _VP]),
+    "dp_tomo_paths_create": (_I, [_P, C.POINTER(DpGrid), _L, _VP, _I, C.POINTER(_P)]),
+    "dp_tomo_paths_create_dev": (_I, [_P, C.POINTER(DpGrid), _L, _VP, _I, C.POINTER(_P)]),
+    "dp_tomo_paths_free": (_I, [_P]),
+    "dp_tomo_paths_info": (_I, [_P, C.POINTER(_L), C.POINTER(C.c_int64), C.POINTER(_I)]),
+    "dp_tomo_paths_csr": (_I, [_P, _VP, _VP, _VP]),
+    "dp_tomo_eval_dev": (_I, [_P, _P, _P, C.POINTER(DpTomoParams), _VP, _VP, _VP, _VP, _VP, _I]),
     "dp_tomo_forward_plain_dev": (_I, [_P, _P, C.POINTER(DpGrid), C.POINTER(DpTomoParams), _VP,
                                        _L, _VP, _VP]),
 }

@@ -214,6 +214,8 @@ typedef struct {
   const double* node_energy; /* host pointers, n_nodes each */
   const double* node_charge;
   const double* node_weight;
+  int precision;             /* DP_PREC_FP64 (0) or DP_PREC_MIXED (1) for the
+                                host-pointer entry points */
 } dp_tomo_params;
 
 /* Per-ray flux.  rho: nx*ny*nz doubles (x fastest).  Host pointers. */
@@ -237,10 +239,35 @@ int dp_tomo_jacobian(dp_ctx* ctx, const dp_physics* phys, const dp_grid* grid,
 int dp_tomo_vjp(dp_ctx* ctx, const dp_physics* phys, const dp_grid* grid,
                 const dp_tomo_params* tp, const double* rho, long n_rays,
                 const dp_ray* rays, const double* cot, double* flux, double* grad_rho);
-/* Device-pointer form of dp_tomo_vjp (cot may be NULL: flux only). */
+/* Device-pointer form of dp_tomo_vjp (traces the rays on every call; the node
+ * arrays of tp are device pointers here). */
 int dp_tomo_vjp_dev(dp_ctx* ctx, const dp_physics* phys, const dp_grid* grid,
                     const dp_tomo_params* tp, const double* rho, long n_rays,
                     const dp_ray* rays, const double* cot, double* flux, double* grad_rho);
+
+/* Ray paths: the rays are traced once (geometry does not depend on rho) into a
+ * device-resident CSR segment list with the CSC permutation of J^T r, the
+ * analogue of precompute_paths (examples/lvd_tomography.jl:835-861).  The
+ * side-exit remainder density is rho[side_cell], or the side_density of the
+ * evaluation when side_cell < 0 (then its Jacobian entry has col -1). */
+typedef struct dp_paths dp_paths;
+int dp_tomo_paths_create(dp_ctx* ctx, const dp_grid* grid, long n_rays, const dp_ray* rays,
+                         int side_cell, dp_paths** out);                 /* host rays */
+int dp_tomo_paths_create_dev(dp_ctx* ctx, const dp_grid* grid, long n_rays,
+                             const dp_ray* rays, int side_cell, dp_paths** out);  /* device rays */
+int dp_tomo_paths_free(dp_paths* paths);
+int dp_tomo_paths_info(const dp_paths* paths, long* n_rays, int64_t* nnz, int* max_segments);
+/* Host copies of the segment lists (any pointer may be NULL). */
+int dp_tomo_paths_csr(const dp_paths* paths, int64_t* row_ptr, int32_t* col, double* len);
+
+#define DP_PREC_FP64 0   /* the reference's operations in FP64 (parity mode) */
+#define DP_PREC_MIXED 1  /* per-segment work in FP32, FP64 range carry and flux integral */
+/* One evaluation on device pointers (node arrays of tp are device pointers):
+ * flux[n_rays]; if cot/grad are given, grad[ncell] = J^T cot (deterministic);
+ * if jac is given, the Jacobian values in the CSR order of the paths. */
+int dp_tomo_eval_dev(dp_ctx* ctx, const dp_physics* phys, const dp_paths* paths,
+                     const dp_tomo_params* tp, const double* rho, const double* cot,
+                     double* flux, double* grad_rho, double* jac, int precision);
 
 /* ------------------------------------------------------------------ plain baseline
  * Plain FP64 GPU form used as the speed-up denominator: one kernel launch per

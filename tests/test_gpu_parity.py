@@ -192,15 +192,18 @@ def test_vjp_is_deterministic_and_matches_jacobian(dp, phys, small_tomo):
     np.testing.assert_allclose(g1, ref, rtol=1e-12, atol=1e-14 * np.abs(ref).max())
 
 
-def test_adjoint_vs_central_fd_c3(dp, phys):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_adjoint_vs_central_fd_c3(dp, phys, precision):
     """Batched forward + adjoint config: d(sum_r c_r flux_r)/d rho_i against
-    central differences (h = 1e-3 rho) on 64 random voxels touched by rays."""
+    central differences (h = 1e-3 rho, FP64 forward) on 64 random voxels
+    touched by rays; agreement within 1e-4 for both precisions."""
     from dpgpu.workloads import tomography_config
     grid, rho, rays, nodes = tomography_config(seed=5)
     model = dp.TomoModel(phys, grid, nodes, side_density=2500.0)
     rng = np.random.default_rng(9)
     cot = rng.uniform(0.5, 1.5, len(rays))
-    flux, g = model.vjp(rho, rays, cot)
+    flux, g = dp.TomoModel(phys, grid, nodes, side_density=2500.0,
+                           precision=precision).vjp(rho, rays, cot)
     assert np.all(flux > 0)
     cand = np.flatnonzero(np.abs(g) > 1e-3 * np.abs(g).max())
     pick = rng.choice(cand, 64, replace=False)
@@ -215,6 +218,50 @@ def test_adjoint_vs_central_fd_c3(dp, phys):
         assert g[c] == pytest.approx((fp - fm) / (2 * h), rel=1e-4, abs=1e-7 * np.abs(g).max())
 
 
+def test_mixed_precision_against_fp64_oracle(dp, phys, oracle, orc_default):
+    """Mixed precision (FP32 per-segment transport): per-ray flux within
+    1e-4 relative error of the FP64 oracle; J^T r within 1e-4 (norm-wise) of
+    the FP64 adjoint."""
+    from dpgpu.workloads import tomography_config
+    grid, rho, rays, nodes = tomography_config(seed=21, rays_per_detector=256)
+    dims = np.array([grid.nx, grid.ny, grid.nz], np.int32)
+    geom = np.array([*grid.origin, *grid.pitch])
+    of = oracle.tomo_forward(orc_default, 0, 1, dims, geom, rho, 2500.0, rays, nodes)
+    m32 = dp.TomoModel(phys, grid, nodes, side_density=2500.0, precision="mixed")
+    m64 = dp.TomoModel(phys, grid, nodes, side_density=2500.0, precision="fp64")
+    f32 = m32.forward(rho, rays)
+    assert np.max(np.abs(f32 / of - 1)) < 1e-4
+    cot = np.random.default_rng(2).uniform(0.5, 1.5, len(rays))
+    _, g32 = m32.vjp(rho, rays, cot)
+    f64, g64 = m64.vjp(rho, rays, cot)
+    np.testing.assert_allclose(f64, of, rtol=1e-9)
+    assert np.linalg.norm(g32 - g64) / np.linalg.norm(g64) < 1e-4
+    big = np.abs(g64) > 1e-3 * np.abs(g64).max()
+    assert np.max(np.abs(g32[big] / g64[big] - 1)) < 1e-3
+    # the oracle's independent reverse sweep
+    _, go = oracle.tomo_vjp(orc_default, 0, 1, dims, geom, rho, 2500.0, rays, nodes, cot)
+    np.testing.assert_allclose(g64, go, rtol=1e-7, atol=1e-10 * np.abs(go).max())
+
+
+def test_resident_paths_match_host_api(dp, phys, small_tomo):
+    import torch
+    grid, rho, rays, nodes = small_tomo
+    m = dp.TomoModel(phys, grid, nodes, side_density=2500.0)
+    cot = np.random.default_rng(4).standard_normal(len(rays))
+    f_ref, g_ref = m.vjp(rho, rays, cot)
+    paths = dp.TomoPaths(phys, grid, rays, nodes, side_density=2500.0)
+    dev = paths.dev
+    trho = torch.tensor(rho.ravel(), dtype=torch.float64, device=dev)
+    tcot = torch.tensor(cot, dtype=torch.float64, device=dev)
+    f, g, _ = paths.eval(trho, tcot, precision="fp64")
+    assert np.array_equal(f.cpu().numpy(), f_ref) and np.array_equal(g.cpu().numpy(), g_ref)
+    f2, g2, _ = paths.eval(trho, tcot, precision="mixed")
+    f3, g3, _ = paths.eval(trho, tcot, precision="mixed")
+    assert torch.equal(f2, f3) and torch.equal(g2, g3)
+    rp, col, ln = paths.csr()
+    assert rp[-1] == paths.nnz and len(col) == paths.nnz
+
+
 def test_plain_form_matches_batched(dp, phys, small_tomo):
     import ctypes as C
     import torch
@@ -227,7 +274,7 @@ def test_plain_form_matches_batched(dp, phys, small_tomo):
                       ("q", nodes[1]), ("w", nodes[2]))}
     out = torch.zeros(len(rays), dtype=torch.float64, device=dev)
     tp = dp.DpTomoParams(0, 1, -1, 2500.0, 3e4, len(nodes[0]), t["E"].data_ptr(),
-                         t["q"].data_ptr(), t["w"].data_ptr())
+                         t["q"].data_ptr(), t["w"].data_ptr(), 0)
     g = grid.to_c()
     torch.cuda.synchronize()
     dp.check(dp.load().dp_tomo_forward_plain_dev(phys.ctx.h, phys.h, C.byref(g), C.byref(tp),
