@@ -14,8 +14,9 @@ int cuda_fail(dp_ctx* ctx, cudaError_t e, const char* where) {
   return fail(ctx, DP_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
 void* scratch(dp_ctx* ctx, size_t bytes, int slot) {
-  void*& p = slot ? ctx->scratch2 : ctx->scratch;
-  size_t& have = slot ? ctx->scratch2_bytes : ctx->scratch_bytes;
+  if (slot < 0 || slot > 3) return nullptr;
+  void*& p = ctx->slot[slot];
+  size_t& have = ctx->slot_bytes[slot];
   if (bytes <= have && p) return p;
   if (p) {
     cudaStreamSynchronize(ctx->stream);
@@ -28,22 +29,47 @@ void* scratch(dp_ctx* ctx, size_t bytes, int slot) {
   have = want;
   return p;
 }
+static cudaEvent_t take_event(dp_ctx* ctx) {
+  cudaEvent_t e = nullptr;
+  if (!ctx->spare.empty()) {
+    e = ctx->spare.back();
+    ctx->spare.pop_back();
+  } else {
+    cudaEventCreate(&e);
+  }
+  return e;
+}
+// Resolves recorded event pairs into ctx->ktime (synchronises on them).
+static void resolve_timing(dp_ctx* ctx) {
+  for (auto& p : ctx->pending) {
+    cudaEventSynchronize(p.b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p.a, p.b);
+    bool found = false;
+    for (auto& kv : ctx->ktime)
+      if (kv.first == p.name) {
+        kv.second += ms;
+        found = true;
+      }
+    if (!found) ctx->ktime.emplace_back(p.name, double(ms));
+    ctx->spare.push_back(p.a);
+    ctx->spare.push_back(p.b);
+  }
+  ctx->pending.clear();
+}
 void timed_begin(dp_ctx* ctx) {
   ++ctx->launches;
-  if (ctx->timing) cudaEventRecord(ctx->ev0, ctx->stream);
+  if (!ctx->timing) return;
+  if (ctx->pending.size() >= 4096) resolve_timing(ctx);
+  ctx->ev0 = take_event(ctx);
+  cudaEventRecord(ctx->ev0, ctx->stream);
 }
 void timed_end(dp_ctx* ctx, const char* name) {
-  if (!ctx->timing) return;
-  cudaEventRecord(ctx->ev1, ctx->stream);
-  cudaEventSynchronize(ctx->ev1);
-  float ms = 0.f;
-  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-  for (auto& kv : ctx->ktime)
-    if (kv.first == name) {
-      kv.second += ms;
-      return;
-    }
-  ctx->ktime.emplace_back(name, double(ms));
+  if (!ctx->timing || !ctx->ev0) return;
+  cudaEvent_t b = take_event(ctx);
+  cudaEventRecord(b, ctx->stream);
+  ctx->pending.push_back({name, ctx->ev0, b});
+  ctx->ev0 = nullptr;
 }
 }  // namespace dp
 
@@ -79,11 +105,16 @@ int dp_destroy(dp_ctx* c) {
   if (!c) return DP_ERR_ARG;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
-  if (c->scratch) cudaFree(c->scratch);
-  if (c->scratch2) cudaFree(c->scratch2);
+  for (void* s : c->slot)
+    if (s) cudaFree(s);
   if (c->d_flag) cudaFree(c->d_flag);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  for (auto& p : c->pending) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  for (cudaEvent_t e : c->spare) cudaEventDestroy(e);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
   return DP_OK;
@@ -100,13 +131,15 @@ void* dp_get_stream(const dp_ctx* c) { return c ? static_cast<void*>(c->stream) 
 
 int dp_set_timing(dp_ctx* c, int enable) {
   if (!c) return DP_ERR_ARG;
+  dp::resolve_timing(c);
   c->timing = enable ? 1 : 0;
   c->ktime.clear();
   return DP_OK;
 }
 
-int dp_kernel_time(const dp_ctx* c, const char* name, double* ms) {
+int dp_kernel_time(dp_ctx* c, const char* name, double* ms) {
   if (!c || !name || !ms) return DP_ERR_ARG;
+  dp::resolve_timing(c);
   *ms = 0.0;
   for (const auto& kv : c->ktime)
     if (kv.first == name) *ms = kv.second;
@@ -114,6 +147,27 @@ int dp_kernel_time(const dp_ctx* c, const char* name, double* ms) {
 }
 
 long long dp_launch_count(const dp_ctx* c) { return c ? c->launches : -1; }
+
+int dp_set_blocking(dp_ctx* c, int blocking) {
+  if (!c) return DP_ERR_ARG;
+  c->blocking = blocking ? 1 : 0;
+  return DP_OK;
+}
+
+int dp_sync(dp_ctx* c) {
+  if (!c) return DP_ERR_ARG;
+  int flag = 0;
+  if (cudaMemcpyAsync(&flag, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+      cudaStreamSynchronize(c->stream) != cudaSuccess)
+    return dp::fail(c, DP_ERR_CUDA, "stream synchronisation failed");
+  if (flag) {
+    cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream);
+    cudaStreamSynchronize(c->stream);
+    return dp::fail(c, DP_ERR_STATE, flag == 2 ? "ray segment buffer overflow"
+                                               : "a kernel wait exceeded its limit");
+  }
+  return DP_OK;
+}
 
 const char* dp_last_error(const dp_ctx* c) { return c ? c->err.c_str() : "null context"; }
 

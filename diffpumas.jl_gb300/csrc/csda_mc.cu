@@ -256,6 +256,7 @@ static int launch(dp_ctx* ctx, CsdaParams& P) {
 }
 
 static int check_flag(dp_ctx* ctx) {
+  if (!ctx->blocking) return DP_OK;  // deferred to dp_sync
   int flag = 0;
   DP_CHECK_CUDA(ctx, cudaMemcpyAsync(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   DP_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -353,6 +354,7 @@ int dp_backward_mc(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params* p, dp_
   DP_CHECK_CUDA(ctx, cudaGetLastError());
   double h[3];
   DP_CHECK_CUDA(ctx, cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  DP_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   rc = check_flag(ctx);
   if (rc) return rc;
   double flux = h[0] / n, var = h[1] / n - flux * flux;

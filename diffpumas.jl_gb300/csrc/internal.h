@@ -14,14 +14,21 @@ struct dp_ctx {
   // Launch accounting and optional per-kernel timing (CUDA events on `stream`).
   long long launches = 0;
   int timing = 0;
+  // 1: every device-pointer call synchronises and checks the kernels' error
+  // flag before returning; 0: calls return after enqueueing, dp_sync checks.
+  int blocking = 1;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  struct Pending {
+    std::string name;
+    cudaEvent_t a, b;
+  };
+  std::vector<Pending> pending;        // recorded, not yet resolved (no host sync)
+  std::vector<cudaEvent_t> spare;      // recycled events
   std::vector<std::pair<std::string, double>> ktime;
   std::string err;
-  // Grow-only device scratch, reused across calls on this context.
-  void* scratch = nullptr;
-  size_t scratch_bytes = 0;
-  void* scratch2 = nullptr;
-  size_t scratch2_bytes = 0;
+  // Grow-only device scratch slots, reused across calls on this context.
+  void* slot[4] = {nullptr, nullptr, nullptr, nullptr};
+  size_t slot_bytes[4] = {0, 0, 0, 0};
   int* d_flag = nullptr;  // device error flag (bounded waits that gave up)
 };
 
@@ -46,9 +53,24 @@ void timed_end(dp_ctx* ctx, const char* name);
 // Sets ctx->err and returns code.
 int fail(dp_ctx* ctx, int code, const std::string& msg);
 int cuda_fail(dp_ctx* ctx, cudaError_t e, const char* where);
-// Ensures scratch slot `slot` (0 or 1) holds at least `bytes`; returns
-// nullptr on failure.  Slot contents do not survive a grow.
+// Ensures scratch slot `slot` (0..3) holds at least `bytes`; returns nullptr
+// on failure.  Slot contents do not survive a grow.  Slot use: 0 per-call
+// temporaries of the MC and plain kernels, 1 Jacobian values of an
+// evaluation, 2 device copies of host inputs, 3 one-shot ray paths.
 void* scratch(dp_ctx* ctx, size_t bytes, int slot = 0);
+// Bump allocator over one scratch slot (256-byte aligned pieces).
+struct Arena {
+  char* base = nullptr;
+  size_t off = 0, cap = 0;
+  template <class T>
+  T* take(size_t n) {
+    size_t a = (off + 255) & ~size_t(255);
+    size_t b = a + (n ? n : 1) * sizeof(T);
+    if (!base || b > cap) return nullptr;
+    off = b;
+    return reinterpret_cast<T*>(base + a);
+  }
+};
 }  // namespace dp
 
 struct dp_physics {
@@ -83,6 +105,9 @@ struct dp_paths {
   int32_t* row_of = nullptr;    // nnz
   int64_t* cptr = nullptr;      // ncell + 1
   int32_t* perm = nullptr;      // entries sorted by (cell, entry index)
+  float4* geom = nullptr;       // per ray: cos_theta_star, its 1.29 power,
+                                // max(|cos theta|, 0.01), cos theta
+  bool owned = true;            // arrays allocated with cudaMalloc (else arena)
 };
 
 #define DP_CHECK_CUDA(ctx, call)                                  \

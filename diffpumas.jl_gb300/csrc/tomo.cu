@@ -130,10 +130,15 @@ __device__ __forceinline__ int trace(const GridDev& g, const dp_ray& r, int cap,
 // One thread per ray: segments into a fixed-capacity slot, count per ray.
 __global__ void trace_kernel(GridDev g, const dp_ray* rays, long n_rays, int cap, int side_cell,
                              int32_t* slot_cell, double* slot_len, int64_t* counts,
-                             int* err_flag) {
+                             float4* geom, int* err_flag) {
   long r = blockIdx.x * long(blockDim.x) + threadIdx.x;
   if (r >= n_rays) return;
   dp_ray ray = rays[r];
+  {
+    double cs = cos_theta_star(ray.cos_theta);
+    geom[r] = make_float4(float(cs), float(pow(cs, 1.29)), float(fmax(fabs(ray.cos_theta), 0.01)),
+                          float(ray.cos_theta));
+  }
   int32_t* sc = slot_cell + size_t(r) * cap;
   double* sl = slot_len + size_t(r) * cap;
   double z_exit;
@@ -244,9 +249,18 @@ __global__ void sort_buckets_kernel(const int64_t* cptr, long ncell, int32_t* pe
 }
 
 // ============================================================ evaluation
+// Per energy node start of the mixed kernel, shared by all rays: the range
+// R(E0) as a float pair, S(E0), E0 and the node's interval on the grid.
+struct NodeInit {
+  float yh, yl, S0, E0;
+  int i0, pad0, pad1, pad2;
+};
+
 struct EvalP {
   TabView tab;
   const float* tab32;
+  const float4* geom;
+  const NodeInit* node0;
   int ld32;
   int rock, air, n_nodes, seg_cap;
   double H, mass, ctau, air_dexp, zmax, side_density;
@@ -415,6 +429,43 @@ __global__ void __launch_bounds__(kWarps * 32) eval64_kernel(EvalP P) {
 }
 
 // ---------------------------------------------------------------- mixed kernel
+// Node starts from the FP64 tables (one thread per node, once per evaluation).
+__global__ void node_prep_kernel(EvalP P, NodeInit* out, const float* RH32) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= P.n_nodes) return;
+  const double E0 = P.nE[k];
+  const Dd lE = dd(log(E0));
+  const double *E = P.tab.col(0, DP_COL_E), *LE = P.tab.col(0, DP_COL_LOGE);
+  const double X0 = interp_logE(P.tab, E, LE, P.tab.col(P.rock, DP_COL_CSDA_R), dd(E0), lE, nullptr).v;
+  const double S0 = interp_logE(P.tab, E, LE, P.tab.col(P.rock, DP_COL_CSDA_S), dd(E0), lE, nullptr).v;
+  NodeInit o;
+  o.yh = float(X0);
+  o.yl = float(X0 - double(o.yh));
+  o.S0 = float(S0);
+  o.E0 = float(E0);
+  int n = P.tab.n, i = 0;
+  while (i < n - 2 && !(o.yh < RH32[i + 1])) ++i;
+  o.i0 = i;
+  o.pad0 = o.pad1 = o.pad2 = 0;
+  out[k] = o;
+}
+
+// flux_gccly in single precision; *dlog = d log(flux)/dK.
+__device__ __forceinline__ float gccly32(float cs, float cs129, float K, float q, float* dlog) {
+  float Emu = K + float(kMuonMass);
+  float a = 3.64f / (Emu * cs129);
+  float ec = 1.1f * Emu * cs;
+  float rpi = 1.0f + ec / 115.0f, rK = 1.0f + ec / 850.0f;
+  float h = 1.0f / rpi + 0.054f / rK;
+  float cf = q < 0.0f ? float(1.0 / 2.2766) : (q > 0.0f ? float(1.2766 / 2.2766) : 1.0f);
+  float f = powf(1.0f + a, -2.7f) * (1.4e3f * powf(Emu, -2.7f) * h * cf);
+  if (dlog) {
+    float dh = -(1.1f * cs / 115.0f) / (rpi * rpi) - 0.054f * (1.1f * cs / 850.0f) / (rK * rK);
+    *dlog = 2.7f * a / (Emu * (1.0f + a)) - 2.7f / Emu + dh / h;
+  }
+  return f;
+}
+
 // Float-pair accumulation (TwoSum): (h, l) += x
 __device__ __forceinline__ void ff_add(float& h, float& l, float x) {
   float s = h + x;
@@ -471,29 +522,20 @@ __global__ void __launch_bounds__(kWarps * 32) eval32_kernel(EvalP P) {
       sJ[s] = 0.0f;
     }
     __syncwarp();
-    const double cosz = P.rays[r].cos_theta;
-    const double cs_safe = fmax(fabs(cosz), 0.01);
+    const float4 gm = P.geom[r];
+    const float cs = gm.x, cs129 = gm.y;
+    const double cs_safe = double(gm.z);
     const float Lair = float((P.H - P.zmax) / cs_safe);
     const double Gair = fmax((1.205 * 12e3 / cs_safe) * P.air_dexp, 0.0);
     const float Gh = float(Gair), Gl = float(Gair - double(Gh));
-    const float cs = float(cos_theta_star(cosz));
-    const float cs129 = powf(cs, 1.29f);
     double fsum = 0.0;
     for (int b0 = 0; b0 < P.n_nodes; b0 += 32) {
       const int nd = b0 + lane;
       const bool active = nd < P.n_nodes;
-      // node start: R(E0) and S(E0) from the FP64 tables (once per node)
-      const double E0d = active ? P.nE[nd] : 1.0;
-      const Dd lE0 = dd(log(E0d));
-      const double X0 = interp_logE(P.tab, P.tab.col(0, DP_COL_E), P.tab.col(0, DP_COL_LOGE),
-                                    P.tab.col(P.rock, DP_COL_CSDA_R), dd(E0d), lE0, nullptr).v;
-      const float S0 = float(interp_logE(P.tab, P.tab.col(0, DP_COL_E), P.tab.col(0, DP_COL_LOGE),
-                                         P.tab.col(P.rock, DP_COL_CSDA_S), dd(E0d), lE0, nullptr).v);
-      const float E0 = float(E0d);
-      float yh = float(X0), yl = float(X0 - double(yh));
-      int i0 = walk(RH, n, yh, P.tab.uniform ? uniform_interval(P.tab.col(0, DP_COL_LOGE), n, lE0.v,
-                                                                  P.tab.lE0, P.tab.inv_dlE)
-                                              : 0);
+      const NodeInit ni = P.node0[active ? nd : 0];
+      const float S0 = ni.S0, E0 = ni.E0;
+      float yh = ni.yh, yl = ni.yl;
+      const int i0 = ni.i0;
       int i = i0;
       float Eprev = E0, E = E0, u = 0.0f, dsum = 0.0f;
       bool clamped = false;
@@ -527,22 +569,11 @@ __global__ void __launch_bounds__(kWarps * 32) eval32_kernel(EvalP P) {
       const float ibga = rsqrtf(xa * (xa + 2.0f));
       const float w = (SN / S0) * (SaF / SaN) * __expf((dsum - Lair * ibga) * inv_ctau);
       float dlogF = 0.0f;
-      const float F = float(gccly_flux(double(cs), double(cs129), double(Ef),
-                                       active ? P.nq[nd] : 0.0, ADJ ? nullptr : nullptr));
+      const float F = gccly32(cs, cs129, Ef, active ? float(P.nq[nd]) : 0.0f, ADJ ? &dlogF : nullptr);
       const float f = active ? w * F : 0.0f;
       const double coef = active ? 2.0 * P.nw[nd] / P.n_nodes : 0.0;
       fsum += coef * double(f);
       if (ADJ) {
-        // d log F / dE in single precision
-        {
-          float Emu = Ef + float(kMuonMass);
-          float a = 3.64f / (Emu * cs129);
-          float ec = 1.1f * Emu * cs;
-          float rpi = 1.0f + ec / 115.0f, rK = 1.0f + ec / 850.0f;
-          float h = 1.0f / rpi + 0.054f / rK;
-          float dh = -(1.1f * cs / 115.0f) / (rpi * rpi) - 0.054f * (1.1f * cs / 850.0f) / (rK * rK);
-          dlogF = 2.7f * a / (Emu * (1.0f + a)) - 2.7f / Emu + dh / h;
-        }
         const float cf = float(coef) * f;
         float lam = 0.0f;
         if (cf != 0.0f) {
@@ -669,6 +700,7 @@ __global__ void plain_sum_kernel(const double* v, long n_rays, int n_nodes, doub
 
 // ============================================================ host side
 static int check(dp_ctx* ctx) {
+  if (!ctx->blocking) return DP_OK;  // deferred to dp_sync
   int flag = 0;
   DP_CHECK_CUDA(ctx, cudaMemcpyAsync(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   DP_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -699,55 +731,74 @@ static T* dalloc(std::vector<void*>& keep, size_t n) {
 }
 
 static void free_paths_arrays(dp_paths* p) {
+  if (!p->owned) return;
   for (void* x : {(void*)p->rays, (void*)p->row_ptr, (void*)p->cell, (void*)p->len,
-                  (void*)p->row_of, (void*)p->cptr, (void*)p->perm})
+                  (void*)p->row_of, (void*)p->cptr, (void*)p->perm, (void*)p->geom})
     if (x) cudaFree(x);
 }
 
-// Builds the paths handle from device rays.
+// Builds the paths handle from device rays.  Temporaries live in scratch slot
+// 3.  With `arena` the handle's arrays are carved from that arena too (a
+// one-shot handle, not owned); otherwise they are cudaMalloc'ed (owned).
 static int build_paths(dp_ctx* ctx, const dp_grid& gr, const dp_ray* d_rays_in, long n_rays,
-                       int side_cell, bool copy_rays, dp_paths** out) {
+                       int side_cell, bool copy_rays, dp_paths** out, Arena* arena = nullptr) {
   long ncell = long(gr.nx) * gr.ny * gr.nz;
+  const int cap = std::min(1001, gr.nx + gr.ny + gr.nz + 64) + 1;
+  long nbr = (n_rays + kScan) / kScan + 1;
+  long nbc = (ncell + kScan) / kScan + 1;
   dp_paths* P = new dp_paths;
   P->ctx = ctx;
   P->grid = gr;
   P->side_cell = side_cell;
   P->n_rays = n_rays;
-  std::vector<void*> tmp;
+  P->owned = arena == nullptr;
+  // temporaries: slot arrays, counts, scan totals, cell histogram, cursors
+  size_t tbytes = size_t(n_rays) * cap * 12 + size_t(n_rays + nbr + 4) * 8 +
+                  size_t(ncell + 1) * 12 + size_t(nbc + 2) * 8 + 16 * 256;
+  Arena tmp;
+  if (!arena) {
+    tmp.base = static_cast<char*>(scratch(ctx, tbytes, 3));
+    tmp.cap = ctx->slot_bytes[3];
+  }
+  Arena& T = arena ? *arena : tmp;
   auto bail = [&](int code, const char* msg) {
-    for (void* x : tmp) cudaFree(x);
     free_paths_arrays(P);
     delete P;
     return fail(ctx, code, msg);
   };
+  auto perm_alloc = [&](size_t bytes) -> void* {
+    if (arena) return arena->take<char>(bytes);
+    void* p = nullptr;
+    return cudaMalloc(&p, bytes ? bytes : 1) == cudaSuccess ? p : nullptr;
+  };
   if (copy_rays) {
-    if (cudaMalloc(&P->rays, sizeof(dp_ray) * (n_rays ? n_rays : 1)) != cudaSuccess)
-      return bail(DP_ERR_ALLOC, "device allocation failed");
+    P->rays = static_cast<dp_ray*>(perm_alloc(sizeof(dp_ray) * n_rays));
+    if (!P->rays) return bail(DP_ERR_ALLOC, "device allocation failed");
     if (cudaMemcpyAsync(P->rays, d_rays_in, sizeof(dp_ray) * n_rays, cudaMemcpyDeviceToDevice,
                         ctx->stream) != cudaSuccess)
       return bail(DP_ERR_CUDA, "ray copy failed");
   }
   const dp_ray* rays = copy_rays ? P->rays : d_rays_in;
-  const int cap = std::min(1001, gr.nx + gr.ny + gr.nz + 64) + 1;
-  long nbr = (n_rays + kScan) / kScan + 1;
-  int32_t* slot_cell = dalloc<int32_t>(tmp, size_t(n_rays) * cap);
-  double* slot_len = dalloc<double>(tmp, size_t(n_rays) * cap);
-  int64_t* counts = dalloc<int64_t>(tmp, n_rays + 1);
-  int64_t* totals = dalloc<int64_t>(tmp, nbr + 2);
-  if (cudaMalloc(&P->row_ptr, sizeof(int64_t) * (n_rays + 1)) != cudaSuccess || !slot_cell ||
-      !slot_len || !counts || !totals)
+  P->row_ptr = static_cast<int64_t*>(perm_alloc(sizeof(int64_t) * (n_rays + 1)));
+  P->geom = static_cast<float4*>(perm_alloc(sizeof(float4) * n_rays));
+  int32_t* slot_cell = T.take<int32_t>(size_t(n_rays) * cap);
+  double* slot_len = T.take<double>(size_t(n_rays) * cap);
+  int64_t* counts = T.take<int64_t>(n_rays + 1);
+  int64_t* totals = T.take<int64_t>(nbr + 2);
+  if (!P->row_ptr || !P->geom || !slot_cell || !slot_len || !counts || !totals)
     return bail(DP_ERR_ALLOC, "device allocation failed");
   GridDev g = grid_dev(gr);
   timed_begin(ctx);
   trace_kernel<<<int((n_rays + 127) / 128), 128, 0, ctx->stream>>>(g, rays, n_rays, cap, side_cell,
                                                                      slot_cell, slot_len, counts,
-                                                                     ctx->d_flag);
+                                                                     P->geom, ctx->d_flag);
   timed_end(ctx, "tomo_trace");
   launch_scan(ctx, counts, P->row_ptr, n_rays, totals);
   int64_t nnz = 0;
-  if (cudaMemcpyAsync(&nnz, P->row_ptr + n_rays, 8, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess)
+  if (cudaMemcpyAsync(&nnz, P->row_ptr + n_rays, 8, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+      cudaStreamSynchronize(ctx->stream) != cudaSuccess)
     return bail(DP_ERR_CUDA, "copy failed");
-  int rc = check(ctx);
+  int rc = dp_sync(ctx);
   if (rc) {
     std::string m = ctx->err;
     return bail(rc, m.c_str());
@@ -759,21 +810,21 @@ static int build_paths(dp_ctx* ctx, const dp_grid& gr, const dp_ray* d_rays_in, 
   for (long r = 0; r < n_rays; ++r) mx = std::max<int>(mx, int(hc[r]));
   P->nnz = nnz;
   P->max_seg = mx;
-  if (cudaMalloc(&P->cell, sizeof(int32_t) * (nnz + 1)) != cudaSuccess ||
-      cudaMalloc(&P->len, sizeof(double) * (nnz + 1)) != cudaSuccess ||
-      cudaMalloc(&P->row_of, sizeof(int32_t) * (nnz + 1)) != cudaSuccess ||
-      cudaMalloc(&P->cptr, sizeof(int64_t) * (ncell + 1)) != cudaSuccess ||
-      cudaMalloc(&P->perm, sizeof(int32_t) * (nnz + 1)) != cudaSuccess)
+  P->cell = static_cast<int32_t*>(perm_alloc(sizeof(int32_t) * (nnz + 1)));
+  P->len = static_cast<double*>(perm_alloc(sizeof(double) * (nnz + 1)));
+  P->row_of = static_cast<int32_t*>(perm_alloc(sizeof(int32_t) * (nnz + 1)));
+  P->cptr = static_cast<int64_t*>(perm_alloc(sizeof(int64_t) * (ncell + 1)));
+  P->perm = static_cast<int32_t*>(perm_alloc(sizeof(int32_t) * (nnz + 1)));
+  if (!P->cell || !P->len || !P->row_of || !P->cptr || !P->perm)
     return bail(DP_ERR_ALLOC, "device allocation failed");
   long tot = n_rays * long(cap);
   compact_kernel<<<int((tot + 255) / 256), 256, 0, ctx->stream>>>(P->row_ptr, n_rays, cap, slot_cell,
                                                                    slot_len, P->cell, P->len, P->row_of);
   ++ctx->launches;
   // CSC permutation (entries of the side remainder at a fixed density excluded)
-  long nbc = (ncell + kScan) / kScan + 1;
-  int64_t* ccount = dalloc<int64_t>(tmp, ncell + 1);
-  int32_t* cursor = dalloc<int32_t>(tmp, ncell + 1);
-  int64_t* ctot = dalloc<int64_t>(tmp, nbc + 2);
+  int64_t* ccount = T.take<int64_t>(ncell + 1);
+  int32_t* cursor = T.take<int32_t>(ncell + 1);
+  int64_t* ctot = T.take<int64_t>(nbc + 2);
   if (!ccount || !cursor || !ctot) return bail(DP_ERR_ALLOC, "device allocation failed");
   cudaMemsetAsync(ccount, 0, 8 * (ncell + 1), ctx->stream);
   cudaMemsetAsync(cursor, 0, 4 * (ncell + 1), ctx->stream);
@@ -784,8 +835,6 @@ static int build_paths(dp_ctx* ctx, const dp_grid& gr, const dp_ray* d_rays_in, 
   ctx->launches += 3;
   if (cudaGetLastError() != cudaSuccess) return bail(DP_ERR_CUDA, "path build launch failed");
   rc = check(ctx);
-  for (void* x : tmp) cudaFree(x);
-  tmp.clear();
   if (rc) {
     free_paths_arrays(P);
     delete P;
@@ -818,6 +867,7 @@ static int make_eval(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, cons
   P.air_dexp = std::exp(-P.zmax / 12e3) - std::exp(-P.H / 12e3);
   P.side_density = tp->side_density;
   P.rays = pa->rays;
+  P.geom = pa->geom;
   P.n_rays = pa->n_rays;
   P.row_ptr = pa->row_ptr;
   P.cell = pa->cell;
@@ -841,11 +891,24 @@ static int eval_core(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, cons
   P.flux = flux;
   const bool adj = (cot && grad) || jac;
   long ncell = long(pa->grid.nx) * pa->grid.ny * pa->grid.nz;
+  // slot 1: node starts, then the Jacobian values
+  size_t need = size_t(P.n_nodes) * sizeof(NodeInit) + size_t(pa->nnz + 1) * 8 + 1024;
+  Arena A;
+  A.base = static_cast<char*>(scratch(ctx, need, 1));
+  A.cap = ctx->slot_bytes[1];
+  if (!A.base) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
   void* jbuf = nullptr;
   if (adj) {
-    size_t b = size_t(pa->nnz + 1) * (precision ? 4 : 8);
-    jbuf = jac && !precision ? (void*)jac : scratch(ctx, b, 1);
+    jbuf = jac && !precision ? (void*)jac : A.take<char>(size_t(pa->nnz + 1) * (precision ? 4 : 8));
     if (!jbuf) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
+  }
+  if (precision) {
+    NodeInit* ni = A.take<NodeInit>(P.n_nodes);
+    if (!ni) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
+    node_prep_kernel<<<(P.n_nodes + 63) / 64, 64, 0, ctx->stream>>>(
+        P, ni, ph->dev32 + size_t(P.rock) * kNC32 * ph->ld32 + C32_RH * ph->ld32);
+    ++ctx->launches;
+    P.node0 = ni;
   }
   long blocks = std::min<long>((pa->n_rays + kWarps - 1) / kWarps, 152L * 16);
   size_t smem;
@@ -901,23 +964,35 @@ static int eval_core(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, cons
 using namespace dp;
 
 namespace {
-// Device copies of host inputs, freed on scope exit.
-struct DevBufs {
-  std::vector<void*> keep;
-  ~DevBufs() {
-    for (void* p : keep) cudaFree(p);
-  }
-  template <class T>
-  T* up(dp_ctx* ctx, const T* h, size_t n) {
-    T* d = dalloc<T>(keep, n);
-    if (d && n) cudaMemcpyAsync(d, h, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream);
-    return d;
-  }
-  template <class T>
-  T* make(size_t n) {
-    return dalloc<T>(keep, n);
-  }
+// Device copies of host inputs carved from scratch slot 2 (reused across calls).
+struct Inputs {
+  double *rho = nullptr, *nE = nullptr, *nq = nullptr, *nw = nullptr, *flux = nullptr,
+         *cot = nullptr, *grad = nullptr;
+  dp_ray* rays = nullptr;
 };
+int upload_inputs(dp_ctx* ctx, const dp_tomo_params* tp, long ncell, long n_rays,
+                  const dp_ray* rays, const double* rho, const double* cot, bool grad, Inputs& d) {
+  size_t need = sizeof(dp_ray) * n_rays + 8 * (ncell * 2 + n_rays * 2 + 3 * tp->n_nodes) + 16 * 256;
+  Arena A;
+  A.base = static_cast<char*>(scratch(ctx, need, 2));
+  A.cap = ctx->slot_bytes[2];
+  if (!A.base) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
+  d.rho = A.take<double>(ncell);
+  d.nE = A.take<double>(tp->n_nodes);
+  d.nq = A.take<double>(tp->n_nodes);
+  d.nw = A.take<double>(tp->n_nodes);
+  d.flux = A.take<double>(n_rays);
+  if (rays) d.rays = A.take<dp_ray>(n_rays);
+  if (cot) d.cot = A.take<double>(n_rays);
+  if (grad) d.grad = A.take<double>(ncell);
+  auto up = [&](void* dst, const void* src, size_t b) {
+    return cudaMemcpyAsync(dst, src, b, cudaMemcpyHostToDevice, ctx->stream) == cudaSuccess;
+  };
+  bool ok = up(d.rho, rho, 8 * ncell) && up(d.nE, tp->node_energy, 8 * tp->n_nodes) &&
+            up(d.nq, tp->node_charge, 8 * tp->n_nodes) && up(d.nw, tp->node_weight, 8 * tp->n_nodes) &&
+            (!rays || up(d.rays, rays, sizeof(dp_ray) * n_rays)) && (!cot || up(d.cot, cot, 8 * n_rays));
+  return ok ? DP_OK : fail(ctx, DP_ERR_CUDA, "input upload failed");
+}
 
 int host_eval(dp_ctx* ctx, const dp_physics* ph, const dp_grid* gr, const dp_tomo_params* tp,
               const double* rho, long n_rays, const dp_ray* rays, const double* cot, double* flux,
@@ -928,47 +1003,53 @@ int host_eval(dp_ctx* ctx, const dp_physics* ph, const dp_grid* gr, const dp_tom
     return fail(ctx, DP_ERR_ARG, "invalid grid");
   long ncell = long(gr->nx) * gr->ny * gr->nz;
   if (tp->side_cell >= ncell) return fail(ctx, DP_ERR_ARG, "side_cell out of range");
+  if (tp->n_nodes <= 0 || !tp->node_energy || !tp->node_charge || !tp->node_weight)
+    return fail(ctx, DP_ERR_ARG, "energy nodes required");
   if (n_rays < 0 || (n_rays > 0 && (!rays || !rho || !flux))) return fail(ctx, DP_ERR_ARG, "bad arrays");
   if (n_rays == 0) return DP_OK;
   DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
-  DevBufs b;
-  dp_ray* drays = b.up(ctx, rays, n_rays);
-  double* drho = b.up(ctx, rho, ncell);
-  double* dE = b.up(ctx, tp->node_energy, tp->n_nodes);
-  double* dq = b.up(ctx, tp->node_charge, tp->n_nodes);
-  double* dw = b.up(ctx, tp->node_weight, tp->n_nodes);
-  double* dflux = b.make<double>(n_rays);
-  double* dcot = cot ? b.up(ctx, cot, n_rays) : nullptr;
-  double* dgrad = grad ? b.make<double>(ncell) : nullptr;
-  if (!drays || !drho || !dE || !dq || !dw || !dflux || (cot && !dcot) || (grad && !dgrad))
-    return fail(ctx, DP_ERR_ALLOC, "device allocation failed");
-  dp_paths* pa = nullptr;
-  int rc = build_paths(ctx, *gr, drays, n_rays, tp->side_cell, false, &pa);
+  Inputs d;
+  int rc = upload_inputs(ctx, tp, ncell, n_rays, rays, rho, cot, grad != nullptr, d);
   if (rc) return rc;
-  pa->rays = drays;  // borrowed; cleared before free
+  // one-shot paths (and the FP64 Jacobian) in scratch slot 3
+  const size_t cap = size_t(std::min(1001, gr->nx + gr->ny + gr->nz + 64) + 1);
+  size_t bound = size_t(n_rays) * cap;  // segments cannot exceed this
+  size_t need = size_t(n_rays) * cap * 12 + bound * (4 + 8 + 4 + 4 + 8) + size_t(ncell + 1) * 20 +
+                size_t(n_rays + 2) * (8 + 16 + 8) + size_t(ncell / kScan + n_rays / kScan + 8) * 16 +
+                64 * 256;
+  Arena A;
+  A.base = static_cast<char*>(scratch(ctx, need, 3));
+  A.cap = ctx->slot_bytes[3];
+  if (!A.base) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
+  dp_paths* pa = nullptr;
+  rc = build_paths(ctx, *gr, d.rays, n_rays, tp->side_cell, false, &pa, &A);
+  if (rc) return rc;
+  pa->rays = d.rays;
   double* djac = nullptr;
   if (row_ptr) {
+    *nnz = pa->nnz;
     if (pa->nnz > nnz_cap) {
-      *nnz = pa->nnz;
-      pa->rays = nullptr;
-      dp_tomo_paths_free(pa);
+      delete pa;
       return fail(ctx, DP_ERR_ARG, "nnz_cap too small");
     }
-    djac = b.make<double>(pa->nnz + 1);
-  }
-  rc = eval_core(ctx, ph, pa, tp, drho, dE, dq, dw, dcot, dflux, dgrad, djac, precision);
-  if (!rc) {
-    cudaMemcpy(flux, dflux, 8 * n_rays, cudaMemcpyDeviceToHost);
-    if (grad) cudaMemcpy(grad, dgrad, 8 * ncell, cudaMemcpyDeviceToHost);
-    if (row_ptr) {
-      *nnz = pa->nnz;
-      cudaMemcpy(row_ptr, pa->row_ptr, 8 * (n_rays + 1), cudaMemcpyDeviceToHost);
-      if (col) cudaMemcpy(col, pa->cell, 4 * pa->nnz, cudaMemcpyDeviceToHost);
-      if (val) cudaMemcpy(val, djac, 8 * pa->nnz, cudaMemcpyDeviceToHost);
+    djac = A.take<double>(pa->nnz + 1);
+    if (!djac) {
+      delete pa;
+      return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
     }
   }
-  pa->rays = nullptr;
-  dp_tomo_paths_free(pa);
+  rc = eval_core(ctx, ph, pa, tp, d.rho, d.nE, d.nq, d.nw, d.cot, d.flux, d.grad, djac, precision);
+  if (!rc) {
+    cudaMemcpyAsync(flux, d.flux, 8 * n_rays, cudaMemcpyDeviceToHost, ctx->stream);
+    if (grad) cudaMemcpyAsync(grad, d.grad, 8 * ncell, cudaMemcpyDeviceToHost, ctx->stream);
+    if (row_ptr) {
+      cudaMemcpyAsync(row_ptr, pa->row_ptr, 8 * (n_rays + 1), cudaMemcpyDeviceToHost, ctx->stream);
+      if (col) cudaMemcpyAsync(col, pa->cell, 4 * pa->nnz, cudaMemcpyDeviceToHost, ctx->stream);
+      if (val) cudaMemcpyAsync(val, djac, 8 * pa->nnz, cudaMemcpyDeviceToHost, ctx->stream);
+    }
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) rc = fail(ctx, DP_ERR_CUDA, "download failed");
+  }
+  delete pa;  // arena-backed arrays: nothing to free
   return rc;
 }
 }  // namespace
@@ -982,10 +1063,42 @@ int dp_tomo_paths_create(dp_ctx* ctx, const dp_grid* gr, long n_rays, const dp_r
     return fail(ctx, DP_ERR_ARG, "invalid grid");
   if (side_cell >= long(gr->nx) * gr->ny * gr->nz) return fail(ctx, DP_ERR_ARG, "side_cell out of range");
   DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
-  DevBufs b;
-  dp_ray* d = b.up(ctx, rays, n_rays);
-  if (!d) return fail(ctx, DP_ERR_ALLOC, "device allocation failed");
-  return build_paths(ctx, *gr, d, n_rays, side_cell, true, out);
+  dp_ray* d = nullptr;
+  if (cudaMalloc(&d, sizeof(dp_ray) * (n_rays ? n_rays : 1)) != cudaSuccess)
+    return fail(ctx, DP_ERR_ALLOC, "device allocation failed");
+  cudaMemcpyAsync(d, rays, sizeof(dp_ray) * n_rays, cudaMemcpyHostToDevice, ctx->stream);
+  int rc = build_paths(ctx, *gr, d, n_rays, side_cell, false, out);
+  if (rc) {
+    cudaFree(d);
+    return rc;
+  }
+  (*out)->rays = d;  // owned by the handle
+  return DP_OK;
+}
+
+int dp_tomo_eval(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, const dp_tomo_params* tp,
+                 const double* rho, const double* cot, double* flux, double* grad, double* jac) {
+  if (!ctx || !ph || !pa || !tp || !rho || !flux) return fail(ctx, DP_ERR_ARG, "null argument");
+  if ((cot == nullptr) != (grad == nullptr)) return fail(ctx, DP_ERR_ARG, "cot and grad go together");
+  if (tp->n_nodes <= 0 || !tp->node_energy || !tp->node_charge || !tp->node_weight)
+    return fail(ctx, DP_ERR_ARG, "energy nodes required");
+  DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  long ncell = long(pa->grid.nx) * pa->grid.ny * pa->grid.nz;
+  Inputs d;
+  int rc = upload_inputs(ctx, tp, ncell, pa->n_rays, nullptr, rho, cot, grad != nullptr, d);
+  if (rc) return rc;
+  double* djac = nullptr;
+  if (jac) {
+    djac = static_cast<double*>(scratch(ctx, size_t(pa->nnz + 1) * 8, 3));
+    if (!djac) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
+  }
+  rc = eval_core(ctx, ph, pa, tp, d.rho, d.nE, d.nq, d.nw, d.cot, d.flux, d.grad, djac, tp->precision);
+  if (rc) return rc;
+  cudaMemcpyAsync(flux, d.flux, 8 * pa->n_rays, cudaMemcpyDeviceToHost, ctx->stream);
+  if (grad) cudaMemcpyAsync(grad, d.grad, 8 * ncell, cudaMemcpyDeviceToHost, ctx->stream);
+  if (jac) cudaMemcpyAsync(jac, djac, 8 * pa->nnz, cudaMemcpyDeviceToHost, ctx->stream);
+  DP_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return DP_OK;
 }
 
 int dp_tomo_paths_create_dev(dp_ctx* ctx, const dp_grid* gr, long n_rays, const dp_ray* rays,

@@ -424,6 +424,24 @@ class TomoPaths:
         load().dp_tomo_paths_csr(self.h, _ptr(rp), _ptr(col), _ptr(ln))
         return rp, col[:self.nnz], ln[:self.nnz]
 
+    def eval_host(self, rho, cot=None, *, precision="mixed", nodes=None):
+        """Host arrays in and out through dp_tomo_eval (copies inside the call)."""
+        rho = _f64(rho).ravel()
+        nE, nq, nw = (_f64(x) for x in (nodes or [t.cpu().numpy() for t in self.nodes]))
+        self._host_nodes = (nE, nq, nw)
+        p = DpTomoParams(self.params.rock_material, self.params.air_material,
+                         self.params.side_cell, self.params.side_density,
+                         self.params.primary_altitude, len(nE), _ptr(nE).value, _ptr(nq).value,
+                         _ptr(nw).value, PRECISION[precision])
+        flux = np.zeros(self.n_rays)
+        grad = np.zeros(self.grid.ncell) if cot is not None else None
+        cot = _f64(cot) if cot is not None else None
+        check(load().dp_tomo_eval(self.physics.ctx.h, self.physics.h, self.h, C.byref(p),
+                                  _ptr(rho), _ptr(cot) if cot is not None else None, _ptr(flux),
+                                  _ptr(grad) if grad is not None else None, None),
+              self.physics.ctx.h)
+        return flux, grad
+
     def eval(self, rho, cot=None, *, precision="mixed", flux=None, grad=None, jac=None):
         """rho (and cot) are float64 CUDA tensors; returns (flux, grad|None, jac|None)."""
         import torch

@@ -84,6 +84,8 @@ PROTOTYPES = {
     "dp_set_timing": (_I, [_P, _I]),
     "dp_kernel_time": (_I, [_P, C.c_char_p, C.POINTER(_D)]),
     "dp_launch_count": (C.c_longlong, [_P]),
+    "dp_set_blocking": (_I, [_P, _I]),
+    "dp_sync": (_I, [_P]),
     "dp_physics_upload": (_I, [_P, C.POINTER(DpSettings), _I, _I, _VP, _VP, C.POINTER(_P)]),
     "dp_physics_create": (_I, [_P, C.POINTER(DpSettings), _I, _VP, _I, _D, _D, C.POINTER(_P)]),
     "dp_physics_free": (_I, [_P]),
@@ -110,6 +112,7 @@ PROTOTYPES = {
     "dp_tomo_paths_info": (_I, [_P, C.POINTER(_L), C.POINTER(C.c_int64), C.POINTER(_I)]),
     "dp_tomo_paths_csr": (_I, [_P, _VP, _VP, _VP]),
     "dp_tomo_eval_dev": (_I, [_P, _P, _P, C.POINTER(DpTomoParams), _VP, _VP, _VP, _VP, _VP, _I]),
+    "dp_tomo_eval": (_I, [_P, _P, _P, C.POINTER(DpTomoParams), _VP, _VP, _VP, _VP, _VP]),
     "dp_tomo_forward_plain_dev": (_I, [_P, _P, C.POINTER(DpGrid), C.POINTER(DpTomoParams), _VP,
                                        _L, _VP, _VP]),
 }

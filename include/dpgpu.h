@@ -59,13 +59,21 @@ const char* dp_last_error(const dp_ctx* ctx);
  * torch stream); NULL restores the context's own stream. */
 int dp_set_stream(dp_ctx* ctx, void* cuda_stream);
 void* dp_get_stream(const dp_ctx* ctx);
-/* Per-kernel timing with CUDA events on the context stream (off by default;
- * enabling it serialises each timed launch).  Names: "csda_mc", "tomo_forward",
- * "tomo_adjoint", "tomo_transpose". */
+/* Per-kernel timing with CUDA events recorded on the context stream around
+ * each main kernel (off by default; recording adds no host synchronisation,
+ * dp_kernel_time resolves the events).  Names: "csda_mc", "tomo_trace",
+ * "tomo_forward", "tomo_adjoint", "tomo_transpose". */
 int dp_set_timing(dp_ctx* ctx, int enable);
-int dp_kernel_time(const dp_ctx* ctx, const char* kernel, double* ms_total);
+int dp_kernel_time(dp_ctx* ctx, const char* kernel, double* ms_total);
 /* Number of kernels this context has launched. */
 long long dp_launch_count(const dp_ctx* ctx);
+/* blocking = 1 (default): device-pointer calls synchronise and report kernel
+ * errors before returning.  blocking = 0: they return once enqueued (no host
+ * synchronisation, e.g. for CUDA-graph capture or back-to-back solver
+ * iterations); dp_sync then waits and reports.  Host-pointer calls always
+ * synchronise. */
+int dp_set_blocking(dp_ctx* ctx, int blocking);
+int dp_sync(dp_ctx* ctx);
 
 /* ------------------------------------------------------------------ physics tables
  * Column layout of one material table (src/Physics.jl:64-102 MaterialTable).
@@ -268,6 +276,12 @@ int dp_tomo_paths_csr(const dp_paths* paths, int64_t* row_ptr, int32_t* col, dou
 int dp_tomo_eval_dev(dp_ctx* ctx, const dp_physics* phys, const dp_paths* paths,
                      const dp_tomo_params* tp, const double* rho, const double* cot,
                      double* flux, double* grad_rho, double* jac, int precision);
+/* The same with host pointers (tp->precision selects the arithmetic); the
+ * inputs are copied in and the outputs out inside the call.  This is the
+ * reference-facing call of an iterative solver: trace once, evaluate often. */
+int dp_tomo_eval(dp_ctx* ctx, const dp_physics* phys, const dp_paths* paths,
+                 const dp_tomo_params* tp, const double* rho, const double* cot, double* flux,
+                 double* grad_rho, double* jac);
 
 /* ------------------------------------------------------------------ plain baseline
  * Plain FP64 GPU form used as the speed-up denominator: one kernel launch per

@@ -260,6 +260,8 @@ def test_resident_paths_match_host_api(dp, phys, small_tomo):
     assert torch.equal(f2, f3) and torch.equal(g2, g3)
     rp, col, ln = paths.csr()
     assert rp[-1] == paths.nnz and len(col) == paths.nnz
+    fh, gh = paths.eval_host(rho, cot, precision="mixed", nodes=nodes)
+    assert np.array_equal(fh, f2.cpu().numpy()) and np.array_equal(gh, g2.cpu().numpy())
 
 
 def test_plain_form_matches_batched(dp, phys, small_tomo):
