@@ -211,13 +211,19 @@ def run_gpu(args):
     for _ in range(args.warmup):
         step_dev()
     torch.cuda.synchronize()
-    lib.dp_set_timing(ctx, 1)
-    lib.dp_set_blocking(ctx, 0)  # enqueue steps back to back; errors checked by dp_sync
-    launches0 = lib.dp_launch_count(ctx)
-    events = []
     barrier(world)
     torch.cuda.synchronize()
     with Clocks(local) as clk:
+        # keep the GPU busy with untimed steps for 0.5 s so that the 100 ms
+        # clock samples cover the load, then the timed steps
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 0.5:
+            step_dev()
+            torch.cuda.synchronize()
+        lib.dp_set_timing(ctx, 1)
+        lib.dp_set_blocking(ctx, 0)  # enqueue steps back to back; errors checked by dp_sync
+        launches0 = lib.dp_launch_count(ctx)
+        events = []
         t_wall = time.perf_counter()
         for _ in range(args.steps):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -254,7 +260,7 @@ def run_gpu(args):
 
     # plain FP64 one-launch-per-ray form (speed-up denominator)
     plain = None
-    if plain_dev is not None:
+    if plain_dev is not None and not args.no_plain:
         plain_dev()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -360,6 +366,7 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain one-launch-per-ray form")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -107,6 +107,8 @@ struct dp_paths {
   int32_t* perm = nullptr;      // entries sorted by (cell, entry index)
   float4* geom = nullptr;       // per ray: cos_theta_star, its 1.29 power,
                                 // max(|cos theta|, 0.01), cos theta
+  int32_t* order = nullptr;     // rays by decreasing segment count (schedule)
+  int32_t* prow = nullptr;      // row_of[perm[p]] (gather reads it in order)
   bool owned = true;            // arrays allocated with cudaMalloc (else arena)
 };
 

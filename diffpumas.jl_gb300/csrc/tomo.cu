@@ -232,11 +232,19 @@ __global__ void place_kernel(const int32_t* col, long nnz, const int64_t* cptr, 
   int c = col[e];
   perm[cptr[c] + atomicAdd(&cursor[c], 1)] = int32_t(e);
 }
-// One thread per cell: order its bucket by entry index (insertion sort).
-__global__ void sort_buckets_kernel(const int64_t* cptr, long ncell, int32_t* perm) {
+// Buckets are ordered by entry index.  Small buckets (<= kSmallBucket): one
+// thread, insertion sort.  Large ones (cells next to a detector collect one
+// entry per ray of that detector) are listed and sorted by a block each.
+constexpr int kSmallBucket = 32;
+__global__ void sort_small_buckets_kernel(const int64_t* cptr, long ncell, int32_t* perm,
+                                          int32_t* big, int32_t* n_big) {
   long c = blockIdx.x * long(blockDim.x) + threadIdx.x;
   if (c >= ncell) return;
   int64_t b = cptr[c], e = cptr[c + 1];
+  if (e - b > kSmallBucket) {
+    big[atomicAdd(n_big, 1)] = int32_t(c);
+    return;
+  }
   for (int64_t i = b + 1; i < e; ++i) {
     int32_t x = perm[i];
     int64_t j = i - 1;
@@ -246,6 +254,60 @@ __global__ void sort_buckets_kernel(const int64_t* cptr, long ncell, int32_t* pe
     }
     perm[j + 1] = x;
   }
+}
+// One block per large bucket: bitonic sort in shared memory (padded with
+// INT_MAX to a power of two); buckets beyond the shared capacity are sorted
+// by repeated odd-even merges of shared-memory-sized runs in global memory.
+constexpr int kSortCap = 32768;  // entries (128 KB of dynamic shared memory)
+__global__ void __launch_bounds__(1024) sort_big_buckets_kernel(const int64_t* cptr, int32_t* perm,
+                                                                const int32_t* big,
+                                                                const int32_t* n_big) {
+  extern __shared__ int32_t sh[];
+  for (int bi = blockIdx.x; bi < *n_big; bi += gridDim.x) {
+    const int c = big[bi];
+    const int64_t b = cptr[c];
+    const int m = int(cptr[c + 1] - b);
+    if (m <= kSortCap) {
+      int p2 = 1;
+      while (p2 < m) p2 <<= 1;
+      for (int i = threadIdx.x; i < p2; i += blockDim.x) sh[i] = i < m ? perm[b + i] : 0x7fffffff;
+      __syncthreads();
+      for (int k = 2; k <= p2; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+          for (int i = threadIdx.x; i < p2; i += blockDim.x) {
+            int l = i ^ j;
+            if (l > i) {
+              bool up = (i & k) == 0;
+              int32_t a = sh[i], d = sh[l];
+              if ((a > d) == up) {
+                sh[i] = d;
+                sh[l] = a;
+              }
+            }
+          }
+          __syncthreads();
+        }
+      for (int i = threadIdx.x; i < m; i += blockDim.x) perm[b + i] = sh[i];
+      __syncthreads();
+    } else {
+      // odd-even transposition over the bucket (rare: more than kSortCap
+      // entries in one cell); bounded by m passes
+      for (int pass = 0; pass < m; ++pass) {
+        for (int i = 2 * threadIdx.x + (pass & 1); i + 1 < m; i += 2 * blockDim.x) {
+          int32_t a = perm[b + i], d = perm[b + i + 1];
+          if (a > d) {
+            perm[b + i] = d;
+            perm[b + i + 1] = a;
+          }
+        }
+        __syncthreads();
+      }
+    }
+  }
+}
+__global__ void permute_rows_kernel(const int32_t* perm, const int32_t* row_of, long n, int32_t* prow) {
+  long p = blockIdx.x * long(blockDim.x) + threadIdx.x;
+  if (p < n) prow[p] = row_of[perm[p]];
 }
 
 // ============================================================ evaluation
@@ -261,6 +323,7 @@ struct EvalP {
   const float* tab32;
   const float4* geom;
   const NodeInit* node0;
+  const int32_t* order;
   int ld32;
   int rock, air, n_nodes, seg_cap;
   double H, mass, ctau, air_dexp, zmax, side_density;
@@ -305,7 +368,7 @@ __device__ __forceinline__ double inv_slope(const double* R, const double* E, co
 }
 
 enum { T_E = 0, T_LOGE, T_RS, T_RR, T_AS, T_AR, T_NCOL };
-constexpr int kWarps = 8;
+constexpr int kWarps = 4;
 
 // ---------------------------------------------------------------- FP64 kernel
 template <bool ADJ>
@@ -328,7 +391,8 @@ __global__ void __launch_bounds__(kWarps * 32) eval64_kernel(EvalP P) {
   double* sD = sL + cap;
   double* sJ = sD + cap;
   const double Emax = tE[n - 1];
-  for (long r = blockIdx.x * long(kWarps) + warp; r < P.n_rays; r += long(gridDim.x) * kWarps) {
+  for (long q = blockIdx.x * long(kWarps) + warp; q < P.n_rays; q += long(gridDim.x) * kWarps) {
+    const long r = P.order[q];
     const int64_t off = P.row_ptr[r];
     const int nseg = int(P.row_ptr[r + 1] - off);
     for (int s = lane; s < nseg; s += 32) {
@@ -444,7 +508,14 @@ __global__ void node_prep_kernel(EvalP P, NodeInit* out, const float* RH32) {
   o.S0 = float(S0);
   o.E0 = float(E0);
   int n = P.tab.n, i = 0;
-  while (i < n - 2 && !(o.yh < RH32[i + 1])) ++i;
+  {  // bisection on the single-precision range column
+    int lo = 0, hi = n - 1;
+    while (lo < hi - 1) {
+      int mid = (lo + hi) >> 1;
+      if (o.yh < RH32[mid]) hi = mid; else lo = mid;
+    }
+    i = lo;
+  }
   o.i0 = i;
   o.pad0 = o.pad1 = o.pad2 = 0;
   out[k] = o;
@@ -483,7 +554,7 @@ __device__ __forceinline__ int walk(const float* RH, int n, float yh, int i) {
 }
 
 template <bool ADJ>
-__global__ void __launch_bounds__(kWarps * 32) eval32_kernel(EvalP P) {
+__global__ void __launch_bounds__(kWarps * 32, 8) eval32_kernel(EvalP P) {
   extern __shared__ __align__(16) float fsm[];
   __shared__ uint64_t mbar;
   const int ld = P.ld32, n = P.tab.n;
@@ -512,7 +583,8 @@ __global__ void __launch_bounds__(kWarps * 32) eval32_kernel(EvalP P) {
   const float inv_m = float(1.0 / P.mass), inv_ctau = float(1.0 / P.ctau);
   const float m_ctau = float(P.mass * P.ctau);
   const float Emax = EE[n - 1];
-  for (long r = blockIdx.x * long(kWarps) + warp; r < P.n_rays; r += long(gridDim.x) * kWarps) {
+  for (long q = blockIdx.x * long(kWarps) + warp; q < P.n_rays; q += long(gridDim.x) * kWarps) {
+    const long r = P.order[q];
     const int64_t off = P.row_ptr[r];
     const int nseg = int(P.row_ptr[r + 1] - off);
     for (int s = lane; s < nseg; s += 32) {
@@ -630,18 +702,20 @@ __global__ void __launch_bounds__(kWarps * 32) eval32_kernel(EvalP P) {
   }
 }
 
-// J^T r over the precomputed CSC permutation (fixed order per cell).
+// J^T r over the precomputed CSC permutation: one warp per cell; lane l sums
+// entries l, l+32, ... of the bucket in order, then a fixed shuffle tree --
+// the same arithmetic order on every call.
 template <class V>
 __global__ void gather_kernel(const int64_t* cptr, const int32_t* perm, const V* val,
-                              const int32_t* row_of, const double* cot, long ncell, double* grad) {
-  long c = blockIdx.x * long(blockDim.x) + threadIdx.x;
+                              const int32_t* prow, const double* cot, long ncell, double* grad) {
+  long c = (blockIdx.x * long(blockDim.x) + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
   if (c >= ncell) return;
   double s = 0.0;
-  for (int64_t p = cptr[c], e = cptr[c + 1]; p < e; ++p) {
-    int32_t k = perm[p];
-    s += double(val[k]) * cot[row_of[k]];
-  }
-  grad[c] = s;
+  for (int64_t p = cptr[c] + lane, e = cptr[c + 1]; p < e; p += 32)
+    s += double(val[perm[p]]) * cot[prow[p]];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) grad[c] = s;
 }
 
 // ---------------------------------------------------------------- plain form
@@ -733,7 +807,8 @@ static T* dalloc(std::vector<void*>& keep, size_t n) {
 static void free_paths_arrays(dp_paths* p) {
   if (!p->owned) return;
   for (void* x : {(void*)p->rays, (void*)p->row_ptr, (void*)p->cell, (void*)p->len,
-                  (void*)p->row_of, (void*)p->cptr, (void*)p->perm, (void*)p->geom})
+                  (void*)p->row_of, (void*)p->cptr, (void*)p->perm, (void*)p->geom,
+                  (void*)p->order, (void*)p->prow})
     if (x) cudaFree(x);
 }
 
@@ -754,7 +829,7 @@ static int build_paths(dp_ctx* ctx, const dp_grid& gr, const dp_ray* d_rays_in, 
   P->owned = arena == nullptr;
   // temporaries: slot arrays, counts, scan totals, cell histogram, cursors
   size_t tbytes = size_t(n_rays) * cap * 12 + size_t(n_rays + nbr + 4) * 8 +
-                  size_t(ncell + 1) * 12 + size_t(nbc + 2) * 8 + 16 * 256;
+                  size_t(ncell + 1) * 16 + size_t(nbc + 2) * 8 + 24 * 256;
   Arena tmp;
   if (!arena) {
     tmp.base = static_cast<char*>(scratch(ctx, tbytes, 3));
@@ -789,7 +864,8 @@ static int build_paths(dp_ctx* ctx, const dp_grid& gr, const dp_ray* d_rays_in, 
     return bail(DP_ERR_ALLOC, "device allocation failed");
   GridDev g = grid_dev(gr);
   timed_begin(ctx);
-  trace_kernel<<<int((n_rays + 127) / 128), 128, 0, ctx->stream>>>(g, rays, n_rays, cap, side_cell,
+  // 32 rays per block: the serial FP64 march spreads over all SMs
+  trace_kernel<<<int((n_rays + 31) / 32), 32, 0, ctx->stream>>>(g, rays, n_rays, cap, side_cell,
                                                                      slot_cell, slot_len, counts,
                                                                      P->geom, ctx->d_flag);
   timed_end(ctx, "tomo_trace");
@@ -831,8 +907,28 @@ static int build_paths(dp_ctx* ctx, const dp_grid& gr, const dp_ray* d_rays_in, 
   if (nnz > 0) hist_kernel<<<int((nnz + 255) / 256), 256, 0, ctx->stream>>>(P->cell, nnz, ccount);
   launch_scan(ctx, ccount, P->cptr, ncell, ctot);
   if (nnz > 0) place_kernel<<<int((nnz + 255) / 256), 256, 0, ctx->stream>>>(P->cell, nnz, P->cptr, cursor, P->perm);
-  sort_buckets_kernel<<<int((ncell + 255) / 256), 256, 0, ctx->stream>>>(P->cptr, ncell, P->perm);
-  ctx->launches += 3;
+  int32_t* big = T.take<int32_t>(ncell + 1);
+  int32_t* n_big = T.take<int32_t>(1);
+  P->prow = static_cast<int32_t*>(perm_alloc(sizeof(int32_t) * (nnz + 1)));
+  P->order = static_cast<int32_t*>(perm_alloc(sizeof(int32_t) * (n_rays + 1)));
+  if (!big || !n_big || !P->prow || !P->order) return bail(DP_ERR_ALLOC, "device allocation failed");
+  cudaMemsetAsync(n_big, 0, 4, ctx->stream);
+  sort_small_buckets_kernel<<<int((ncell + 255) / 256), 256, 0, ctx->stream>>>(P->cptr, ncell, P->perm,
+                                                                               big, n_big);
+  cudaFuncSetAttribute(sort_big_buckets_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       kSortCap * 4);
+  sort_big_buckets_kernel<<<152, 1024, kSortCap * 4, ctx->stream>>>(P->cptr, P->perm, big, n_big);
+  if (nnz > 0) permute_rows_kernel<<<int((nnz + 255) / 256), 256, 0, ctx->stream>>>(P->perm, P->row_of, nnz, P->prow);
+  ctx->launches += 5;
+  // schedule: longest ray first (stable), so that the tail of the launch is short
+  {
+    std::vector<int32_t> ord(n_rays);
+    for (long r = 0; r < n_rays; ++r) ord[r] = int32_t(r);
+    std::stable_sort(ord.begin(), ord.end(), [&](int32_t a, int32_t b) { return hc[a] > hc[b]; });
+    if (cudaMemcpyAsync(P->order, ord.data(), 4 * n_rays, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+      return bail(DP_ERR_CUDA, "schedule upload failed");
+  }
   if (cudaGetLastError() != cudaSuccess) return bail(DP_ERR_CUDA, "path build launch failed");
   rc = check(ctx);
   if (rc) {
@@ -868,6 +964,7 @@ static int make_eval(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, cons
   P.side_density = tp->side_density;
   P.rays = pa->rays;
   P.geom = pa->geom;
+  P.order = pa->order;
   P.n_rays = pa->n_rays;
   P.row_ptr = pa->row_ptr;
   P.cell = pa->cell;
@@ -939,11 +1036,11 @@ static int eval_core(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, cons
   if (adj && cot && grad) {
     timed_begin(ctx);
     if (precision == 0)
-      gather_kernel<double><<<int((ncell + 255) / 256), 256, 0, ctx->stream>>>(
-          pa->cptr, pa->perm, static_cast<const double*>(jbuf), pa->row_of, cot, ncell, grad);
+      gather_kernel<double><<<int((ncell * 32 + 255) / 256), 256, 0, ctx->stream>>>(
+          pa->cptr, pa->perm, static_cast<const double*>(jbuf), pa->prow, cot, ncell, grad);
     else
-      gather_kernel<float><<<int((ncell + 255) / 256), 256, 0, ctx->stream>>>(
-          pa->cptr, pa->perm, static_cast<const float*>(jbuf), pa->row_of, cot, ncell, grad);
+      gather_kernel<float><<<int((ncell * 32 + 255) / 256), 256, 0, ctx->stream>>>(
+          pa->cptr, pa->perm, static_cast<const float*>(jbuf), pa->prow, cot, ncell, grad);
     DP_CHECK_CUDA(ctx, cudaGetLastError());
     timed_end(ctx, "tomo_transpose");
   }
@@ -1014,8 +1111,8 @@ int host_eval(dp_ctx* ctx, const dp_physics* ph, const dp_grid* gr, const dp_tom
   // one-shot paths (and the FP64 Jacobian) in scratch slot 3
   const size_t cap = size_t(std::min(1001, gr->nx + gr->ny + gr->nz + 64) + 1);
   size_t bound = size_t(n_rays) * cap;  // segments cannot exceed this
-  size_t need = size_t(n_rays) * cap * 12 + bound * (4 + 8 + 4 + 4 + 8) + size_t(ncell + 1) * 20 +
-                size_t(n_rays + 2) * (8 + 16 + 8) + size_t(ncell / kScan + n_rays / kScan + 8) * 16 +
+  size_t need = size_t(n_rays) * cap * 12 + bound * (4 + 8 + 4 + 4 + 4 + 8) + size_t(ncell + 1) * 28 +
+                size_t(n_rays + 2) * (8 + 16 + 8 + 4) + size_t(ncell / kScan + n_rays / kScan + 8) * 16 +
                 64 * 256;
   Arena A;
   A.base = static_cast<char*>(scratch(ctx, need, 3));
