@@ -106,9 +106,11 @@ struct dp_paths {
   int64_t* cptr = nullptr;      // ncell + 1
   int32_t* perm = nullptr;      // entries sorted by (cell, entry index)
   float4* geom = nullptr;       // per ray: cos_theta_star, its 1.29 power,
-                                // max(|cos theta|, 0.01), cos theta
+                                // 1/max(|cos theta|, 0.01), cos theta
   int32_t* order = nullptr;     // rays by decreasing segment count (schedule)
   int32_t* prow = nullptr;      // row_of[perm[p]] (gather reads it in order)
+  int32_t* big = nullptr;       // cells whose bucket holds more than 32 entries
+  int n_big = 0;
   bool owned = true;            // arrays allocated with cudaMalloc (else arena)
 };
 

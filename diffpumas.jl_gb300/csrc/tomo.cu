@@ -136,8 +136,8 @@ __global__ void trace_kernel(GridDev g, const dp_ray* rays, long n_rays, int cap
   dp_ray ray = rays[r];
   {
     double cs = cos_theta_star(ray.cos_theta);
-    geom[r] = make_float4(float(cs), float(pow(cs, 1.29)), float(fmax(fabs(ray.cos_theta), 0.01)),
-                          float(ray.cos_theta));
+    geom[r] = make_float4(float(cs), float(pow(cs, 1.29)),
+                          float(1.0 / fmax(fabs(ray.cos_theta), 0.01)), float(ray.cos_theta));
   }
   int32_t* sc = slot_cell + size_t(r) * cap;
   double* sl = slot_len + size_t(r) * cap;
@@ -305,9 +305,13 @@ __global__ void __launch_bounds__(1024) sort_big_buckets_kernel(const int64_t* c
     }
   }
 }
-__global__ void permute_rows_kernel(const int32_t* perm, const int32_t* row_of, long n, int32_t* prow) {
+// prow[p] = row of the p-th bucketed entry.  Only the first cptr[ncell]
+// positions of perm are filled (side-exit entries at a fixed density have no
+// cell and are not bucketed).
+__global__ void permute_rows_kernel(const int32_t* perm, const int32_t* row_of,
+                                    const int64_t* n_bucketed, int32_t* prow) {
   long p = blockIdx.x * long(blockDim.x) + threadIdx.x;
-  if (p < n) prow[p] = row_of[perm[p]];
+  if (p < *n_bucketed) prow[p] = row_of[perm[p]];
 }
 
 // ============================================================ evaluation
@@ -315,7 +319,8 @@ __global__ void permute_rows_kernel(const int32_t* perm, const int32_t* row_of, 
 // R(E0) as a float pair, S(E0), E0 and the node's interval on the grid.
 struct NodeInit {
   float yh, yl, S0, E0;
-  int i0, pad0, pad1, pad2;
+  int i0;
+  float coef, q, pad;
 };
 
 struct EvalP {
@@ -493,10 +498,8 @@ __global__ void __launch_bounds__(kWarps * 32) eval64_kernel(EvalP P) {
 }
 
 // ---------------------------------------------------------------- mixed kernel
-// Node starts from the FP64 tables (one thread per node, once per evaluation).
-__global__ void node_prep_kernel(EvalP P, NodeInit* out, const float* RH32) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= P.n_nodes) return;
+// Node start from the FP64 tables (each block computes all nodes once).
+__device__ __forceinline__ void node_init(const EvalP& P, int k, const float* RH32, NodeInit* out) {
   const double E0 = P.nE[k];
   const Dd lE = dd(log(E0));
   const double *E = P.tab.col(0, DP_COL_E), *LE = P.tab.col(0, DP_COL_LOGE);
@@ -517,7 +520,9 @@ __global__ void node_prep_kernel(EvalP P, NodeInit* out, const float* RH32) {
     i = lo;
   }
   o.i0 = i;
-  o.pad0 = o.pad1 = o.pad2 = 0;
+  o.coef = float(2.0 * P.nw[k] / P.n_nodes);
+  o.q = float(P.nq[k]);
+  o.pad = 0.0f;
   out[k] = o;
 }
 
@@ -580,7 +585,11 @@ __global__ void __launch_bounds__(kWarps * 32, 8) eval32_kernel(EvalP P) {
   float* sG = fsm + size_t(2 * kNC32) * ld + size_t(warp) * cap * 3;  // grammage rho L
   float* sL = sG + cap;                                              // length L
   float* sJ = sL + cap;                                              // Jacobian accumulator
+  NodeInit* snode = reinterpret_cast<NodeInit*>(fsm + size_t(2 * kNC32) * ld + size_t(kWarps) * cap * 3);
+  for (int k = threadIdx.x; k < P.n_nodes; k += blockDim.x) node_init(P, k, RH, snode);
+  __syncthreads();
   const float inv_m = float(1.0 / P.mass), inv_ctau = float(1.0 / P.ctau);
+  const float Lair_c = float(P.H - P.zmax), Gair_c = float(1.205 * 12e3 * P.air_dexp);
   const float m_ctau = float(P.mass * P.ctau);
   const float Emax = EE[n - 1];
   for (long q = blockIdx.x * long(kWarps) + warp; q < P.n_rays; q += long(gridDim.x) * kWarps) {
@@ -588,23 +597,21 @@ __global__ void __launch_bounds__(kWarps * 32, 8) eval32_kernel(EvalP P) {
     const int64_t off = P.row_ptr[r];
     const int nseg = int(P.row_ptr[r + 1] - off);
     for (int s = lane; s < nseg; s += 32) {
-      double L = P.len[off + s];
-      sG[s] = float(L * seg_density(P, P.cell[off + s]));
-      sL[s] = float(L);
+      const float L = float(P.len[off + s]);
+      sG[s] = L * float(seg_density(P, P.cell[off + s]));
+      sL[s] = L;
       sJ[s] = 0.0f;
     }
     __syncwarp();
     const float4 gm = P.geom[r];
-    const float cs = gm.x, cs129 = gm.y;
-    const double cs_safe = double(gm.z);
-    const float Lair = float((P.H - P.zmax) / cs_safe);
-    const double Gair = fmax((1.205 * 12e3 / cs_safe) * P.air_dexp, 0.0);
-    const float Gh = float(Gair), Gl = float(Gair - double(Gh));
+    const float cs = gm.x, cs129 = gm.y, inv_cs = gm.z;
+    const float Lair = Lair_c * inv_cs;
+    const float Gh = fmaxf(Gair_c * inv_cs, 0.0f), Gl = 0.0f;
     double fsum = 0.0;
     for (int b0 = 0; b0 < P.n_nodes; b0 += 32) {
       const int nd = b0 + lane;
       const bool active = nd < P.n_nodes;
-      const NodeInit ni = P.node0[active ? nd : 0];
+      const NodeInit ni = snode[active ? nd : 0];
       const float S0 = ni.S0, E0 = ni.E0;
       float yh = ni.yh, yl = ni.yl;
       const int i0 = ni.i0;
@@ -641,12 +648,12 @@ __global__ void __launch_bounds__(kWarps * 32, 8) eval32_kernel(EvalP P) {
       const float ibga = rsqrtf(xa * (xa + 2.0f));
       const float w = (SN / S0) * (SaF / SaN) * __expf((dsum - Lair * ibga) * inv_ctau);
       float dlogF = 0.0f;
-      const float F = gccly32(cs, cs129, Ef, active ? float(P.nq[nd]) : 0.0f, ADJ ? &dlogF : nullptr);
+      const float F = gccly32(cs, cs129, Ef, ni.q, ADJ ? &dlogF : nullptr);
       const float f = active ? w * F : 0.0f;
-      const double coef = active ? 2.0 * P.nw[nd] / P.n_nodes : 0.0;
-      fsum += coef * double(f);
+      const float coef = active ? ni.coef : 0.0f;
+      fsum += double(coef) * double(f);  // node integral accumulated in FP64
       if (ADJ) {
-        const float cf = float(coef) * f;
+        const float cf = coef * f;
         float lam = 0.0f;
         if (cf != 0.0f) {
           const float aA = Lair * (xa + 1.0f) * ibga * ibga * ibga / m_ctau;
@@ -706,16 +713,31 @@ __global__ void __launch_bounds__(kWarps * 32, 8) eval32_kernel(EvalP P) {
 // entries l, l+32, ... of the bucket in order, then a fixed shuffle tree --
 // the same arithmetic order on every call.
 template <class V>
-__global__ void gather_kernel(const int64_t* cptr, const int32_t* perm, const V* val,
-                              const int32_t* prow, const double* cot, long ncell, double* grad) {
-  long c = (blockIdx.x * long(blockDim.x) + threadIdx.x) >> 5;
+__global__ void gather_big_kernel(const int64_t* cptr, const int32_t* perm, const V* val,
+                                  const int32_t* prow, const double* cot, const int32_t* big,
+                                  int n_big, double* grad) {
+  long w = (blockIdx.x * long(blockDim.x) + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
-  if (c >= ncell) return;
+  if (w >= n_big) return;
+  int c = big[w];
   double s = 0.0;
   for (int64_t p = cptr[c] + lane, e = cptr[c + 1]; p < e; p += 32)
     s += double(val[perm[p]]) * cot[prow[p]];
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if (lane == 0) grad[c] = s;
+}
+// Cells with at most kSmallBucket entries: one thread, entries in order.
+template <class V>
+__global__ void gather_small_kernel(const int64_t* cptr, const int32_t* perm, const V* val,
+                                    const int32_t* prow, const double* cot, long ncell,
+                                    double* grad) {
+  long c = blockIdx.x * long(blockDim.x) + threadIdx.x;
+  if (c >= ncell) return;
+  int64_t b = cptr[c], e = cptr[c + 1];
+  if (e - b > kSmallBucket) return;  // gather_big_kernel
+  double s = 0.0;
+  for (int64_t p = b; p < e; ++p) s += double(val[perm[p]]) * cot[prow[p]];
+  grad[c] = s;
 }
 
 // ---------------------------------------------------------------- plain form
@@ -808,7 +830,7 @@ static void free_paths_arrays(dp_paths* p) {
   if (!p->owned) return;
   for (void* x : {(void*)p->rays, (void*)p->row_ptr, (void*)p->cell, (void*)p->len,
                   (void*)p->row_of, (void*)p->cptr, (void*)p->perm, (void*)p->geom,
-                  (void*)p->order, (void*)p->prow})
+                  (void*)p->order, (void*)p->prow, (void*)p->big})
     if (x) cudaFree(x);
 }
 
@@ -918,7 +940,9 @@ static int build_paths(dp_ctx* ctx, const dp_grid& gr, const dp_ray* d_rays_in, 
   cudaFuncSetAttribute(sort_big_buckets_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        kSortCap * 4);
   sort_big_buckets_kernel<<<152, 1024, kSortCap * 4, ctx->stream>>>(P->cptr, P->perm, big, n_big);
-  if (nnz > 0) permute_rows_kernel<<<int((nnz + 255) / 256), 256, 0, ctx->stream>>>(P->perm, P->row_of, nnz, P->prow);
+  if (nnz > 0)
+    permute_rows_kernel<<<int((nnz + 255) / 256), 256, 0, ctx->stream>>>(P->perm, P->row_of,
+                                                                          P->cptr + ncell, P->prow);
   ctx->launches += 5;
   // schedule: longest ray first (stable), so that the tail of the launch is short
   {
@@ -926,8 +950,15 @@ static int build_paths(dp_ctx* ctx, const dp_grid& gr, const dp_ray* d_rays_in, 
     for (long r = 0; r < n_rays; ++r) ord[r] = int32_t(r);
     std::stable_sort(ord.begin(), ord.end(), [&](int32_t a, int32_t b) { return hc[a] > hc[b]; });
     if (cudaMemcpyAsync(P->order, ord.data(), 4 * n_rays, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
+        cudaMemcpyAsync(&P->n_big, n_big, 4, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
         cudaStreamSynchronize(ctx->stream) != cudaSuccess)
       return bail(DP_ERR_CUDA, "schedule upload failed");
+    // the large-bucket list survives the build (the temporaries do not)
+    int32_t* keep = static_cast<int32_t*>(perm_alloc(sizeof(int32_t) * (P->n_big + 1)));
+    if (!keep) return bail(DP_ERR_ALLOC, "device allocation failed");
+    if (P->n_big > 0)
+      cudaMemcpyAsync(keep, big, 4 * size_t(P->n_big), cudaMemcpyDeviceToDevice, ctx->stream);
+    P->big = keep;
   }
   if (cudaGetLastError() != cudaSuccess) return bail(DP_ERR_CUDA, "path build launch failed");
   rc = check(ctx);
@@ -999,14 +1030,6 @@ static int eval_core(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, cons
     jbuf = jac && !precision ? (void*)jac : A.take<char>(size_t(pa->nnz + 1) * (precision ? 4 : 8));
     if (!jbuf) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
   }
-  if (precision) {
-    NodeInit* ni = A.take<NodeInit>(P.n_nodes);
-    if (!ni) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
-    node_prep_kernel<<<(P.n_nodes + 63) / 64, 64, 0, ctx->stream>>>(
-        P, ni, ph->dev32 + size_t(P.rock) * kNC32 * ph->ld32 + C32_RH * ph->ld32);
-    ++ctx->launches;
-    P.node0 = ni;
-  }
   long blocks = std::min<long>((pa->n_rays + kWarps - 1) / kWarps, 152L * 16);
   size_t smem;
   static bool attr = false;
@@ -1025,7 +1048,8 @@ static int eval_core(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, cons
     if (adj) eval64_kernel<true><<<int(blocks), kWarps * 32, smem, ctx->stream>>>(P);
     else eval64_kernel<false><<<int(blocks), kWarps * 32, smem, ctx->stream>>>(P);
   } else {
-    smem = size_t(2 * kNC32) * P.ld32 * 4 + size_t(kWarps) * P.seg_cap * 3 * 4;
+    smem = size_t(2 * kNC32) * P.ld32 * 4 + size_t(kWarps) * P.seg_cap * 3 * 4 +
+           size_t(P.n_nodes) * sizeof(NodeInit);
     if (smem > 220 * 1024) return fail(ctx, DP_ERR_ARG, "ray too long for the mixed kernel");
     P.jval32 = static_cast<float*>(jbuf);
     if (adj) eval32_kernel<true><<<int(blocks), kWarps * 32, smem, ctx->stream>>>(P);
@@ -1035,12 +1059,23 @@ static int eval_core(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, cons
   timed_end(ctx, adj ? "tomo_adjoint" : "tomo_forward");
   if (adj && cot && grad) {
     timed_begin(ctx);
-    if (precision == 0)
-      gather_kernel<double><<<int((ncell * 32 + 255) / 256), 256, 0, ctx->stream>>>(
-          pa->cptr, pa->perm, static_cast<const double*>(jbuf), pa->prow, cot, ncell, grad);
-    else
-      gather_kernel<float><<<int((ncell * 32 + 255) / 256), 256, 0, ctx->stream>>>(
-          pa->cptr, pa->perm, static_cast<const float*>(jbuf), pa->prow, cot, ncell, grad);
+    const int nbw = int((long(pa->n_big) * 32 + 255) / 256);
+    if (precision == 0) {
+      const double* v = static_cast<const double*>(jbuf);
+      gather_small_kernel<double><<<int((ncell + 255) / 256), 256, 0, ctx->stream>>>(
+          pa->cptr, pa->perm, v, pa->prow, cot, ncell, grad);
+      if (pa->n_big > 0)
+        gather_big_kernel<double><<<nbw, 256, 0, ctx->stream>>>(pa->cptr, pa->perm, v, pa->prow, cot,
+                                                                 pa->big, pa->n_big, grad);
+    } else {
+      const float* v = static_cast<const float*>(jbuf);
+      gather_small_kernel<float><<<int((ncell + 255) / 256), 256, 0, ctx->stream>>>(
+          pa->cptr, pa->perm, v, pa->prow, cot, ncell, grad);
+      if (pa->n_big > 0)
+        gather_big_kernel<float><<<nbw, 256, 0, ctx->stream>>>(pa->cptr, pa->perm, v, pa->prow, cot,
+                                                                pa->big, pa->n_big, grad);
+    }
+    ctx->launches += pa->n_big > 0 ? 1 : 0;
     DP_CHECK_CUDA(ctx, cudaGetLastError());
     timed_end(ctx, "tomo_transpose");
   }
