@@ -160,7 +160,11 @@ def setup_c3(dp, torch, dev, precision="mixed"):
     # and the Jacobian value written (4 B in mixed precision, 8 B in FP64).
     jb = 4 if precision == "mixed" else 8
     alg = n_rays * (16 + 8 + 8) + nseg * (4 + 8 + 8 + jb)
+    # DRAM read+write bytes of one tomo_adjoint launch on this workload, from the
+    # ncu capture summarised in profiles/tomo_adjoint_c3_mixed.md
+    traffic = 3494400 if precision == "mixed" else None
     info = {"units": n_rays, "unit": "rays/s", "kernel": "tomo_adjoint", "alg_bytes": alg,
+            "traffic": traffic,
             "config": {"workload": "c3: tomography forward + adjoint, 64x64x32 @ 10 m, 4x1024 rays, "
                                    "32 energy nodes [1,1e6] GeV, flux + J^T r per step",
                        "grid": [64, 64, 32], "rays": n_rays, "energy_nodes": 32,
@@ -284,7 +288,8 @@ def run_gpu(args):
             "e2e": {"value": world * info["units"] / (e2e_ms * 1e-3), "unit": info["unit"],
                     "h2d_bytes_per_step": info["h2d"], "d2h_bytes_per_step": info["d2h"]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak if achieved else None, "traffic": None,
+                         "frac": achieved / peak if achieved else None,
+                         "traffic": info.get("traffic"),
                          "kernel": info["kernel"], "kernel_ms": kernel_ms,
                          "peak_source": peak_kind},
             "gpu_launches": int(launches),
