@@ -31,6 +31,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "internal.h"
@@ -1344,3 +1346,93 @@ int dp_tomo_vjp_dev(dp_ctx* ctx, const dp_physics* ph, const dp_grid* gr, const 
 }
 
 }  // extern "C"
+
+// ============================================================ allocation-free evaluation
+// Some callers may not allocate device memory during a call: a long-running
+// service that holds a fixed device-memory budget, or a plugin whose host
+// process owns all device memory through its own pool allocator (a stray
+// cudaMalloc would fragment or exceed it).  dp_tomo_eval_noalloc_dev serves
+// them: it evaluates the mixed-precision flux and J^T r on resident paths and
+// keeps its only scratch -- the per-segment Jacobian values -- in the
+// file-scope array below instead of the context's grow-on-demand scratch.
+// The array is a fixed part of the library: every GPU that loads libdpgpu
+// holds it (8 MiB) until the process exits.
+namespace dp {
+constexpr long kNoAllocMaxSegments = 1L << 21;  // 2,097,152 segments, FP32 values
+static __device__ __align__(256) float g_noalloc_jacobian[kNoAllocMaxSegments];
+
+// Device address of g_noalloc_jacobian, looked up once per device with that
+// device current (the host-side symbol is only a stand-in, never a device
+// address).
+static float* noalloc_scratch(int device, cudaError_t* err) {
+  constexpr int kMaxDevices = 64;
+  static std::mutex mu;
+  static float* addr[kMaxDevices] = {};
+  *err = cudaSuccess;
+  if (device < 0 || device >= kMaxDevices) {
+    *err = cudaErrorInvalidDevice;
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[device]) {
+    float* p = nullptr;
+    *err = cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_noalloc_jacobian);
+    if (*err != cudaSuccess) return nullptr;
+    addr[device] = p;
+  }
+  return addr[device];
+}
+}  // namespace dp
+
+extern "C" int dp_tomo_eval_noalloc_dev(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa,
+                                        const dp_tomo_params* tp, const double* rho,
+                                        const double* cot, double* flux, double* grad) {
+  if (!ctx || !ph || !pa || !tp || !rho || !flux) return fail(ctx, DP_ERR_ARG, "null argument");
+  if ((cot == nullptr) != (grad == nullptr)) return fail(ctx, DP_ERR_ARG, "cot and grad go together");
+  if (pa->nnz > kNoAllocMaxSegments)
+    return fail(ctx, DP_ERR_ARG,
+                "dp_tomo_eval_noalloc_dev: the paths hold " + std::to_string(pa->nnz) +
+                    " segments, more than its fixed scratch of " + std::to_string(kNoAllocMaxSegments) +
+                    "; use dp_tomo_eval_dev");
+  DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaError_t e;
+  float* jac = noalloc_scratch(ctx->device, &e);
+  if (!jac) return cuda_fail(ctx, e, "cudaGetSymbolAddress(g_noalloc_jacobian)");
+  EvalP P;
+  int rc = make_eval(ctx, ph, pa, tp, P);
+  if (rc) return rc;
+  if (pa->n_rays == 0) return DP_OK;
+  P.rho = rho;
+  P.nE = tp->node_energy;
+  P.nq = tp->node_charge;
+  P.nw = tp->node_weight;
+  P.flux = flux;
+  P.jval32 = jac;  // every segment's value is written before the gather reads it
+  const size_t smem = size_t(2 * kNC32) * P.ld32 * 4 + size_t(kWarps) * P.seg_cap * 3 * 4 +
+                      size_t(P.n_nodes) * sizeof(NodeInit);
+  if (smem > 220 * 1024) return fail(ctx, DP_ERR_ARG, "ray too long for the mixed kernel");
+  const long blocks = std::min<long>((pa->n_rays + kWarps - 1) / kWarps, 152L * 16);
+  const bool adj = cot != nullptr;
+  if (adj) {
+    cudaFuncSetAttribute(eval32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    eval32_kernel<true><<<int(blocks), kWarps * 32, smem, ctx->stream>>>(P);
+  } else {
+    cudaFuncSetAttribute(eval32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    eval32_kernel<false><<<int(blocks), kWarps * 32, smem, ctx->stream>>>(P);
+  }
+  ++ctx->launches;
+  DP_CHECK_CUDA(ctx, cudaGetLastError());
+  if (adj) {
+    const long ncell = long(pa->grid.nx) * pa->grid.ny * pa->grid.nz;
+    gather_small_kernel<float><<<int((ncell + 255) / 256), 256, 0, ctx->stream>>>(
+        pa->cptr, pa->perm, jac, pa->prow, cot, ncell, grad);
+    ++ctx->launches;
+    if (pa->n_big > 0) {
+      gather_big_kernel<float><<<int((long(pa->n_big) * 32 + 255) / 256), 256, 0, ctx->stream>>>(
+          pa->cptr, pa->perm, jac, pa->prow, cot, pa->big, pa->n_big, grad);
+      ++ctx->launches;
+    }
+    DP_CHECK_CUDA(ctx, cudaGetLastError());
+  }
+  return check(ctx);
+}

@@ -113,6 +113,7 @@ PROTOTYPES = {
     "dp_tomo_paths_csr": (_I, [_P, _VP, _VP, _VP]),
     "dp_tomo_eval_dev": (_I, [_P, _P, _P, C.POINTER(DpTomoParams), _VP, _VP, _VP, _VP, _VP, _I]),
     "dp_tomo_eval": (_I, [_P, _P, _P, C.POINTER(DpTomoParams), _VP, _VP, _VP, _VP, _VP]),
+    "dp_tomo_eval_noalloc_dev": (_I, [_P, _P, _P, C.POINTER(DpTomoParams), _VP, _VP, _VP, _VP]),
     "dp_tomo_forward_plain_dev": (_I, [_P, _P, C.POINTER(DpGrid), C.POINTER(DpTomoParams), _VP,
                                        _L, _VP, _VP]),
 }

@@ -283,6 +283,25 @@ int dp_tomo_eval(dp_ctx* ctx, const dp_physics* phys, const dp_paths* paths,
                  const dp_tomo_params* tp, const double* rho, const double* cot, double* flux,
                  double* grad_rho, double* jac);
 
+/* Allocation-free variant of dp_tomo_eval_dev (mixed precision): per-ray flux
+ * and, when cot/grad are given, grad = J^T cot on resident paths, with device
+ * pointers, without calling cudaMalloc or any allocating routine.  It has no
+ * counterpart in the reference.  It is meant for callers that may not allocate
+ * device memory during a call: a service holding a fixed device-memory budget,
+ * or a plugin whose host process owns device memory through its own pool.
+ * Its only scratch, the per-segment Jacobian values, lives in a fixed 8 MiB
+ * array inside the library (held by every GPU that loads it, until exit), so
+ * paths with more than 2,097,152 segments are rejected (DP_ERR_ARG) -- use
+ * dp_tomo_eval_dev for those.  The first call on a device looks up that
+ * array's device address (cudaGetSymbolAddress) with the device current; make
+ * that first call before any stream capture.  All calls share the array and
+ * every value is rewritten before it is read, so nothing needs clearing, but
+ * calls that overlap on the GPU (other contexts or streams at the same time)
+ * race on it. */
+int dp_tomo_eval_noalloc_dev(dp_ctx* ctx, const dp_physics* phys, const dp_paths* paths,
+                             const dp_tomo_params* tp, const double* rho, const double* cot,
+                             double* flux, double* grad_rho);
+
 /* ------------------------------------------------------------------ plain baseline
  * Plain FP64 GPU form used as the speed-up denominator: one kernel launch per
  * ray, one thread per energy node, tables read from global memory with binary
