@@ -66,30 +66,31 @@ def revision_physics(oracle):
            (18.0, 39.9481, 188e-9, 0.012827), (6.0, 12.0108, 78e-9, 0.000124)]
     p = oracle.Physics()
     d = os.path.join(GOLDEN, "dedx_muon")
-    p.add_dedx(os.path.join(d, "standard_rock.txt"), oracle.Material("StandardRock", 2650.0, _bragg(rk), rk))
-    p.add_dedx(os.path.join(d, "air.txt"), oracle.Material("Air", 1.205, _bragg(air), air))
-    p.add_dedx(os.path.join(d, "water.txt"), oracle.Material("Water", 1000.0, 79.7e-9, wat))
+    p.add_dedx(os.path.join(d, "standard_rock.txt"),
+               oracle.Material("StandardRock", 2650.0, _bragg(rk), rk), coulomb=True)
+    p.add_dedx(os.path.join(d, "air.txt"), oracle.Material("Air", 1.205, _bragg(air), air),
+               coulomb=True)
+    p.add_dedx(os.path.join(d, "water.txt"), oracle.Material("Water", 1000.0, 79.7e-9, wat),
+               coulomb=True)
     return p
 
 
 def test_revision_tables_vs_reference_outputs(oracle):
     """docs/revision_evidence/corrected_transport/physics-julia.csv: the
-    reference's own property values at 10..1e5 GeV for rock and air.  The
-    Coulomb transport path is not restated (scattering tables), every other
-    property must agree to 1e-12."""
+    reference's own property values at 10..1e5 GeV for rock and air: CSDA and
+    restricted stopping power and range, proper time, straggling, hard cross
+    section and the Coulomb first transport path; all 80 agree to 1e-12."""
     p = revision_physics(oracle)
     colmap = {"stopping_power_0": "csda_S", "stopping_power_1": "mixed_S", "range_0": "csda_R",
               "range_1": "mixed_R", "proper_time_0": "csda_T", "energy_straggling": "strag",
-              "cross_section": "xs"}
+              "cross_section": "xs", "transport_path_1": "lb1"}
     mats = {"StandardRock": 0, "Air": 1}
     n = 0
     for m, E, prop, v in _rows(os.path.join(GOLDEN, "physics-julia.csv")):
-        if prop not in colmap:
-            continue
         got = p.lookup(mats[m], colmap[prop], float(E))
         assert got == pytest.approx(float(v), rel=1e-12), (m, E, prop)
         n += 1
-    assert n == 70
+    assert n == 80
 
 
 def test_electronic_stopping_vs_pumas_table(oracle):
