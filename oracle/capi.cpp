@@ -8,6 +8,7 @@
 #include <omp.h>
 #endif
 
+#include "mc.hpp"
 #include "oracle.hpp"
 
 using namespace orc;
@@ -262,6 +263,141 @@ void orc_tomo_vjp(void* h, int rock, int air, const int* dims, const double* geo
       if (!a.empty()) s += a[c];
     grad[c] = s;
   }
+}
+
+// Stochastic backward MC histories (straggled / mixed / CSDA dual-mode loop).
+// rock: n_rock materials with mass fractions; air: material index.  Per
+// history i: geometry (thickness, density, elevation, primary altitude) from
+// the arrays (index i, or index 0 when the stride flag is 0), final energy
+// E[i], charge q[i]; the random stream is (seed, id0 + i).  Outputs the flux
+// contribution w[i]*flux, the status bits, the step count and the final energy.
+void orc_mc_histories(void* h, int n_rock, const int* rock_mats, const double* rock_fracs, int air,
+                      long n, const double* thick, const double* dens, const double* elev,
+                      const double* H, int geo_per_history, const double* E, const double* q,
+                      const double* w, uint64_t seed, uint64_t id0, int straggling, int scattering,
+                      double threshold_low, double source_max, double* contrib, int* status,
+                      long* steps, double* Efinal, int nthreads) {
+  Physics* p = static_cast<Physics*>(h);
+  Mixture rm;
+  for (int j = 0; j < n_rock; ++j) {
+    rm.mats.push_back(rock_mats[j]);
+    rm.fracs.push_back(rock_fracs[j]);
+  }
+  Mixture am;
+  am.mats.push_back(air);
+  am.fracs.push_back(1.0);
+  McMedia md;
+  md.rock = make_medium(*p, rm);
+  md.air = make_medium(*p, am);
+  md.krock = prepare_mixed_kernel(*p, rm);
+  md.kair = prepare_mixed_kernel(*p, am);
+  McOptions o;
+  o.straggling = straggling != 0;
+  o.scattering = scattering != 0;
+  o.energy_threshold_low = threshold_low;
+  o.source_energy_max = source_max;
+#pragma omp parallel for schedule(dynamic, 8) num_threads(nthreads)
+  for (long i = 0; i < n; ++i) {
+    long gi = geo_per_history ? i : 0;
+    McGeometry geo{thick[gi], dens[gi], elev[gi], H[gi]};
+    Rng g;
+    g.seed = seed;
+    g.id = id0 + uint64_t(i);
+    McState fs;
+    double f = stochastic_history(*p, md, geo, E[i], q[i], g, o, &fs);
+    contrib[i] = w[i] * f;
+    if (status) status[i] = fs.status;
+    if (steps) steps[i] = fs.steps;
+    if (Efinal) Efinal[i] = fs.E;
+  }
+}
+
+// MixedKernel columns for tests: returns the node count; cols receives
+// E, stop, sigma, range, hazard, proper (6 x n, when cap allows) and onset.
+int orc_mixed_kernel(void* h, int n_mats, const int* mats, const double* fracs, int cap,
+                     double* cols, double* onset) {
+  Physics* p = static_cast<Physics*>(h);
+  Mixture mx;
+  for (int j = 0; j < n_mats; ++j) {
+    mx.mats.push_back(mats[j]);
+    mx.fracs.push_back(fracs[j]);
+  }
+  MixedKernel k = prepare_mixed_kernel(*p, mx);
+  int n = int(k.E.size());
+  if (n <= cap) {
+    const std::vector<double>* c[6] = {&k.E, &k.stop, &k.sigma, &k.range, &k.hazard, &k.proper};
+    for (int j = 0; j < 6; ++j) std::copy(c[j]->begin(), c[j]->end(), cols + size_t(j) * n);
+  }
+  *onset = k.onset;
+  return n;
+}
+
+}  // extern "C"
+
+namespace {
+// A MixedKernel from explicit columns (E, stop, sigma, range, hazard, proper;
+// n nodes each) and n_el elements of 4 values (Z, A, I, fraction): the
+// reference tests build kernels this way (test/test_mixed_kernel.jl).
+MixedKernel explicit_kernel(double mass, double ctau, double cutoff, int n, const double* cols,
+                            int n_el, const double* el, double onset) {
+  MixedKernel c;
+  c.mass = mass;
+  c.ctau = ctau;
+  c.cutoff = cutoff;
+  c.onset = onset;
+  std::vector<double>* dst[6] = {&c.E, &c.stop, &c.sigma, &c.range, &c.hazard, &c.proper};
+  for (int j = 0; j < 6; ++j) dst[j]->assign(cols + size_t(j) * n, cols + size_t(j + 1) * n);
+  for (int e = 0; e < n_el; ++e) c.el.push_back({el[4 * e], el[4 * e + 1], el[4 * e + 2], el[4 * e + 3]});
+  return c;
+}
+Rng make_rng(uint64_t seed, uint64_t id, int n_script, const double* script) {
+  Rng g;
+  g.seed = seed;
+  g.id = id;
+  if (n_script >= 0) {
+    g.script = script;
+    g.n_script = n_script;
+  }
+  return g;
+}
+}  // namespace
+
+extern "C" {
+
+// One transport_mixed_step on an explicit kernel.  state: E, w, t, x, y, z,
+// ux, uy, uz, dist, X (11 values, in and out).  n_script < 0: Philox stream
+// (seed, id); else the scripted values.  Returns the status bits; *consumed
+// = scripted values used (-1 on overrun).
+int orc_mixed_step(double mass, double ctau, double cutoff, int n, const double* cols, int n_el,
+                   const double* el, double onset, double* state, double density,
+                   double distance, double energy_limit, uint64_t seed, uint64_t id, int n_script,
+                   const double* script, int* consumed) {
+  MixedKernel c = explicit_kernel(mass, ctau, cutoff, n, cols, n_el, el, onset);
+  Rng g = make_rng(seed, id, n_script, script);
+  McState s;
+  double* f[11] = {&s.E, &s.w, &s.t, &s.x, &s.y, &s.z, &s.ux, &s.uy, &s.uz, &s.dist, &s.X};
+  for (int j = 0; j < 11; ++j) *f[j] = state[j];
+  transport_mixed_step(c, s, density, distance, g, energy_limit);
+  for (int j = 0; j < 11; ++j) state[j] = *f[j];
+  if (consumed) *consumed = g.overrun ? -1 : g.pos;
+  return s.status;
+}
+
+// reverse_del_event on an explicit kernel: out = (energy, weight, process,
+// element).  Returns the status bits.
+int orc_reverse_del(double mass, double ctau, double cutoff, int n, const double* cols, int n_el,
+                    const double* el, double onset, double k, int details, uint64_t seed,
+                    uint64_t id, int n_script, const double* script, double* out, int* consumed) {
+  MixedKernel c = explicit_kernel(mass, ctau, cutoff, n, cols, n_el, el, onset);
+  Rng g = make_rng(seed, id, n_script, script);
+  int status = 0;
+  DelResult r = reverse_del_event(c, k, g, details != 0, &status);
+  out[0] = r.energy;
+  out[1] = r.weight;
+  out[2] = r.process;
+  out[3] = r.element;
+  if (consumed) *consumed = g.overrun ? -1 : g.pos;
+  return status;
 }
 
 // One ray's flux and its density derivative for every cell it touches

@@ -4,6 +4,7 @@ TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
 CPU-baseline leg of bench.py.  The product (diffpumas.jl_gb300) never imports it.
 """
 import ctypes as C
+import math
 import os
 
 import numpy as np
@@ -86,6 +87,19 @@ def lib():
         L.orc_tomo_ray_grad.restype = _I
         L.orc_tomo_ray_grad.argtypes = [_P, _I, _I, _IP, _DP, _DP, _D, _D, _DP, _I, _DP, _DP,
                                         _DP, C.POINTER(_D), _I, _IP, _DP, C.POINTER(_D)]
+        _U64 = C.c_uint64
+        L.orc_mc_histories.argtypes = [_P, _I, _IP, _DP, _I, _L, _DP, _DP, _DP, _DP, _I, _DP, _DP,
+                                       _DP, _U64, _U64, _I, _I, _D, _D, _DP, _IP,
+                                       np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS"),
+                                       _DP, _I]
+        L.orc_mixed_kernel.restype = _I
+        L.orc_mixed_kernel.argtypes = [_P, _I, _IP, _DP, _I, _DP, C.POINTER(_D)]
+        L.orc_mixed_step.restype = _I
+        L.orc_mixed_step.argtypes = [_D, _D, _D, _I, _DP, _I, _DP, _D, _DP, _D, _D, _D, _U64,
+                                     _U64, _I, _DP, C.POINTER(_I)]
+        L.orc_reverse_del.restype = _I
+        L.orc_reverse_del.argtypes = [_D, _D, _D, _I, _DP, _I, _DP, _D, _D, _I, _U64, _U64, _I,
+                                      _DP, _DP, C.POINTER(_I)]
         _lib = L
     return _lib
 
@@ -257,3 +271,95 @@ def tomo_ray_grad(p, rock, air, dims, geom, rho, rho_side, ray, nodes, H=3e4, ca
                                 _arr(rho).ravel(), rho_side, H, _arr(ray), len(E), E, q, w,
                                 C.byref(f), cap, cells, grads, C.byref(ds))
     return f.value, cells[:n].copy(), grads[:n].copy(), ds.value
+
+
+# ------------------------------------------------------------ stochastic MC
+# History status bits (oracle/mc.hpp)
+ST_STEP_CAP, ST_EVENT_CAP, ST_DOMAIN_HI, ST_DOMAIN_LO, ST_ZERO_RATE, ST_BAD_WEIGHT = (
+    1, 4, 8, 16, 32, 64)
+
+
+class Kernel:
+    """Explicit MIXED transport kernel (src/MixedTransport.jl MixedKernel):
+    columns E, stop, sigma, range, hazard, proper; elements (Z, A, I, fraction)."""
+
+    def __init__(self, E, stop, sigma, range_, hazard, proper, elements=(), onset=math.inf,
+                 mass=MUON_MASS, ctau=MUON_C_TAU, cutoff=0.05):
+        self.cols = _arr(np.concatenate([_arr(c) for c in (E, stop, sigma, range_, hazard,
+                                                            proper)]))
+        self.n = len(E)
+        self.el = _arr(np.array(elements, dtype=np.float64).reshape(-1, 4)).ravel()
+        self.n_el = len(elements)
+        self.onset, self.mass, self.ctau, self.cutoff = onset, mass, ctau, cutoff
+
+
+STATE_FIELDS = ("E", "w", "t", "x", "y", "z", "ux", "uy", "uz", "dist", "X")
+
+
+def _state(**kw):
+    d = dict(E=0.0, w=1.0, t=0.0, x=0.0, y=0.0, z=0.0, ux=0.0, uy=0.0, uz=-1.0, dist=0.0, X=0.0)
+    d.update(kw)
+    return _arr([d[f] for f in STATE_FIELDS])
+
+
+def mixed_step(kern, state, density, distance, energy_limit=-1.0, seed=0, id=0, script=None):
+    """transport_mixed_step: returns (dict state, status, consumed script values)."""
+    st = _state(**state) if isinstance(state, dict) else _arr(state).copy()
+    sc = _arr(script if script is not None else [0.0])
+    used = _I()
+    status = lib().orc_mixed_step(kern.mass, kern.ctau, kern.cutoff, kern.n, kern.cols, kern.n_el,
+                                  kern.el if kern.n_el else _arr([0.0]), kern.onset, st,
+                                  density, distance, energy_limit, seed, id,
+                                  -1 if script is None else len(script), sc, C.byref(used))
+    return dict(zip(STATE_FIELDS, st)), status, used.value
+
+
+def reverse_del(kern, k, details=False, seed=0, id=0, script=None):
+    """reverse_del_event: returns (energy, weight, process, element, status, consumed)."""
+    out = np.zeros(4)
+    sc = _arr(script if script is not None else [0.0])
+    used = _I()
+    status = lib().orc_reverse_del(kern.mass, kern.ctau, kern.cutoff, kern.n, kern.cols,
+                                   kern.n_el, kern.el if kern.n_el else _arr([0.0]), kern.onset, k,
+                                   int(details), seed, id,
+                                   -1 if script is None else len(script), sc, out, C.byref(used))
+    return out[0], out[1], int(out[2]), int(out[3]), status, used.value
+
+
+def mixed_kernel(p, mats, fracs=None):
+    """prepare_mixed_kernel (src/MixedTransport.jl:51-97) of a material or mixture."""
+    mats = np.asarray(mats, np.int32)
+    fracs = _arr(fracs if fracs is not None else np.ones(len(mats)))
+    onset = _D()
+    n = lib().orc_mixed_kernel(p.h, len(mats), mats, fracs, 0, np.zeros(1), C.byref(onset))
+    cols = np.zeros(6 * n)
+    lib().orc_mixed_kernel(p.h, len(mats), mats, fracs, n, cols, C.byref(onset))
+    c = cols.reshape(6, n)
+    return dict(E=c[0], stop=c[1], sigma=c[2], range=c[3], hazard=c[4], proper=c[5],
+                onset=onset.value)
+
+
+def mc_histories(p, rock, air, thickness, density, elevation, H, E, q, w, seed, id0=0,
+                 straggling=True, scattering=True, threshold_low=100.0, source_max=1e9,
+                 rock_fracs=None, threads=0):
+    """Stochastic backward histories (the dual-mode loop of src/Geometry.jl:534-757).
+
+    rock: a material index or a list of indices (mixture with rock_fracs);
+    geometry arguments are scalars or per-history arrays.  Returns
+    (contribution w*f, status, steps, final energy) per history."""
+    rock = np.atleast_1d(np.asarray(rock, np.int32))
+    fr = _arr(rock_fracs if rock_fracs is not None else np.ones(len(rock)))
+    E, q, w = _arr(E), _arr(q), _arr(w)
+    n = len(E)
+    geo = [_arr(np.atleast_1d(v)) for v in (thickness, density, elevation, H)]
+    per = int(any(len(g) > 1 for g in geo))
+    if per:
+        geo = [_arr(np.broadcast_to(g, (n,))) for g in geo]
+    contrib, Ef = np.zeros(n), np.zeros(n)
+    status = np.zeros(n, np.int32)
+    steps = np.zeros(n, np.int64)
+    threads = threads or os.cpu_count()
+    lib().orc_mc_histories(p.h, len(rock), rock, fr, air, n, geo[0], geo[1], geo[2], geo[3], per,
+                           E, q, w, seed, id0, int(straggling), int(scattering), threshold_low,
+                           source_max, contrib, status, steps, Ef, threads)
+    return contrib, status, steps, Ef

@@ -11,6 +11,10 @@ Files (paths inside the reference project):
       the reference's own tabulated properties of the revision physics
   examples/data/revision_physics/pumas-materials/dedx/muon/{standard_rock,water,air}.txt
       the PUMAS dE/dx inputs that physics-julia.csv was built from
+  docs/revision_evidence/corrected_transport/full102_comparison.csv
+      stochastic backward-MC flux (straggling + scattering, 10^4 histories per
+      point) of the reference and of the official PUMAS C library on the flat
+      rock column: 17 thicknesses x 6 zenith angles
 """
 import os
 import shutil
@@ -22,6 +26,7 @@ FILES = {
     "examples/data/revision_physics/pumas-materials/dedx/muon/standard_rock.txt": "dedx_muon/standard_rock.txt",
     "examples/data/revision_physics/pumas-materials/dedx/muon/water.txt": "dedx_muon/water.txt",
     "examples/data/revision_physics/pumas-materials/dedx/muon/air.txt": "dedx_muon/air.txt",
+    "docs/revision_evidence/corrected_transport/full102_comparison.csv": "full102_comparison.csv",
 }
 
 
