@@ -16,7 +16,7 @@ LIB = os.path.join(OUT, "libdpgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr", "--extended-lambda"]
-UNITS = ["api.cu", "physics_build.cu", "csda_mc.cu", "tomo.cu"]
+UNITS = ["api.cu", "physics_build.cu", "csda_mc.cu", "tomo.cu", "mc.cu"]
 
 
 def nvcc():

@@ -215,6 +215,22 @@ DP_HD double gccly_flux(double cs, double cs129, double K, double q, double* dlo
   return f;
 }
 
+// ------------------------------------------------------------- tallies
+// Compensated (TwoSum) accumulator for the deterministic FP64 tallies.
+struct KSum {
+  double s, c;
+};
+DP_HD void kadd(KSum& a, double x) {
+  double t = a.s + x;
+  double bp = t - a.s;
+  a.c += (a.s - (t - bp)) + (x - bp);
+  a.s = t;
+}
+DP_HD void kmerge(KSum& a, const KSum& b) {
+  kadd(a, b.s);
+  a.c += b.c;
+}
+
 // ------------------------------------------------------------- staging (TMA)
 #ifdef __CUDACC__
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {

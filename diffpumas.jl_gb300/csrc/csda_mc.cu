@@ -150,19 +150,6 @@ __global__ void __launch_bounds__(128) csda_mc_kernel(CsdaParams P) {
 // Compensated (TwoSum) accumulation in a fixed order: every thread owns a
 // fixed strided subset, blocks reduce in a fixed tree, a single block then
 // reduces the block partials.
-struct KSum {
-  double s, c;
-};
-__device__ __forceinline__ void kadd(KSum& a, double x) {
-  double t = a.s + x;
-  double bp = t - a.s;
-  a.c += (a.s - (t - bp)) + (x - bp);
-  a.s = t;
-}
-__device__ __forceinline__ void kmerge(KSum& a, const KSum& b) {
-  kadd(a, b.s);
-  a.c += b.c;
-}
 
 constexpr int kRedThreads = 256;
 __global__ void __launch_bounds__(kRedThreads) reduce3_kernel(const double* a, const double* b, long n,
@@ -203,8 +190,6 @@ __global__ void __launch_bounds__(kRedThreads) reduce_parts_kernel(const KSum* p
 
 static int setup(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params* p, CsdaParams& P) {
   if (!ctx || !ph || !p) return fail(ctx, DP_ERR_ARG, "null argument");
-  if (p->straggling || p->scattering)
-    return fail(ctx, DP_ERR_ARG, "only CSDA transport (straggling = scattering = 0) is available");
   int rock = p->rock_material, air = p->air_material;
   if (rock < 0) {
     rock = dp_physics_material_index(ph, "StandardRock");
@@ -332,6 +317,23 @@ int dp_backward_mc(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params* p, dp_
   if (!out || p->n_samples <= 0) return fail(ctx, DP_ERR_ARG, "n_samples must be positive");
   DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
   long n = p->n_samples;
+  // stochastic transport first (its scratch is released before the CSDA pass)
+  const bool stochastic = p->straggling || p->scattering;
+  dp_los_result st{};
+  int st_rc = DP_OK;
+  if (stochastic) {
+    st_rc = mc_backward_stochastic(ctx, ph, p, P.rock, P.air, P.threshold, &st);
+    if (st_rc && st_rc != DP_ERR_DOMAIN && st_rc != DP_ERR_STATE) return st_rc;
+    if (!p->compute_gradient) {
+      *out = dp_mc_result{};
+      out->flux = st.flux;
+      out->sigma = st.sigma;
+      out->source_energy_max = P.threshold;
+      out->n_samples = n;
+      out->n_status_nonzero = st.n_status_nonzero;
+      return st_rc;
+    }
+  }
   const int nb = 152 * 2;
   char* s = static_cast<char*>(scratch(ctx, size_t(n) * 2 * sizeof(double) + nb * 3 * sizeof(KSum) + 64));
   if (!s) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
@@ -365,6 +367,12 @@ int dp_backward_mc(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params* p, dp_
   out->source_energy_max = P.threshold;
   out->n_samples = n;
   out->n_status_nonzero = 0;
+  if (stochastic) {
+    out->flux = st.flux;
+    out->sigma = st.sigma;
+    out->n_status_nonzero = st.n_status_nonzero;
+    return st_rc;
+  }
   return DP_OK;
 }
 

@@ -58,6 +58,12 @@ int cuda_fail(dp_ctx* ctx, cudaError_t e, const char* where);
 // temporaries of the MC and plain kernels, 1 Jacobian values of an
 // evaluation, 2 device copies of host inputs, 3 one-shot ray paths.
 void* scratch(dp_ctx* ctx, size_t bytes, int slot = 0);
+// Stochastic run_backward_mc on single-material rock and air media (one line
+// of sight, FP64 or mixed precision per p->precision); fills flux, sigma and
+// the flagged-history count of *res.  Returns DP_ERR_DOMAIN / DP_ERR_STATE
+// (with the results filled) where the reference would throw.
+int mc_backward_stochastic(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params* p, int rock,
+                           int air, double threshold, dp_los_result* res);
 // Bump allocator over one scratch slot (256-byte aligned pieces).
 struct Arena {
   char* base = nullptr;

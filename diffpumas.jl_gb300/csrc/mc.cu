@@ -1,0 +1,942 @@
+// mc.cu -- stochastic backward Monte Carlo of libdpgpu: medium preparation on
+// the host (mixture properties and the MIXED transport kernel), the
+// persistent history kernel in FP64 and mixed precision, the deterministic
+// per-line-of-sight tallies and the C ABI.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <vector>
+
+#include "internal.h"
+#include "mc_device.cuh"
+
+namespace {
+// Nuclear RMS radii (fm) by atomic number (src/Straggling.jl:726-729 table).
+#include "physics_data.inc"
+}  // namespace
+
+namespace cg = cooperative_groups;
+using namespace dp;
+using namespace dp::mc;
+
+// A prepared medium: host columns plus device blobs cached per partner medium.
+struct dp_mixture {
+  const dp_physics* phys = nullptr;
+  uint64_t uid = 0;
+  int nm = 0;
+  std::vector<int> mats;
+  std::vector<double> fracs;
+  int n = 0;                  // physics grid nodes
+  std::vector<double> cols;   // (MC_LB1 + 2*nm) columns of n: see MedCol
+  int nk = 0;                 // MIXED kernel nodes
+  std::vector<double> kcols;  // K_NCOL columns of nk
+  double onset = 0, ZoA = 0;
+  std::vector<double> el;     // nel x kElStride
+  int nel = 0;
+  struct Blob {
+    uint64_t partner;
+    int precision;
+    unsigned char* dev;
+    Layout lay;
+  };
+  std::vector<Blob> blobs;    // this medium as rock, `partner` as air
+};
+
+namespace {
+
+std::atomic<uint64_t> g_uid{1};
+
+// interpolate_table_fast (src/Physics.jl:660-687) on the host.
+double h_interp(double x, const double* xs, const double* lxs, const double* ys, int n) {
+  if (x <= xs[0]) return ys[0];
+  if (x >= xs[n - 1]) return ys[n - 1];
+  double lx = std::log(x);
+  int lo = 0, hi = n - 1;
+  while (lo < hi - 1) {
+    int mid = (lo + hi) >> 1;
+    if (lx < lxs[mid]) hi = mid; else lo = mid;
+  }
+  double t = (lx - lxs[lo]) / (lxs[lo + 1] - lxs[lo]);
+  return ys[lo] + t * (ys[lo + 1] - ys[lo]);
+}
+
+const double* hcol(const dp_physics* ph, int mat, int c) {
+  return ph->host.data() + (size_t(mat) * DP_NCOL + c) * ph->n;
+}
+
+double rms_radius(double Z) {
+  long iz = std::lround(Z);
+  int i = int(std::min(std::max(iz, 1L), 120L));
+  return DPDATA_NUCLEAR_RMS_RADII_FM[i - 1] * 1e-15;
+}
+
+int prepare(dp_ctx* ctx, const dp_physics* ph, int nm, const int* mats, const double* fr,
+            dp_mixture* m) {
+  if (!ph->has_recipes) return fail(ctx, DP_ERR_ARG, "elemental recipes required");
+  if (nm < 1 || nm > kMaxMix) return fail(ctx, DP_ERR_ARG, "a mixture holds 1 to 4 materials");
+  double tot = 0.0;
+  for (int j = 0; j < nm; ++j) {
+    if (mats[j] < 0 || mats[j] >= ph->n_mat) return fail(ctx, DP_ERR_ARG, "invalid mixture material");
+    if (!(std::isfinite(fr[j]) && fr[j] >= 0.0)) return fail(ctx, DP_ERR_ARG, "invalid mixture fractions");
+    tot += fr[j];
+  }
+  if (!(tot > 0.0)) return fail(ctx, DP_ERR_ARG, "invalid mixture fractions");
+  const int n = ph->n;
+  const double* E = hcol(ph, mats[0], DP_COL_E);
+  const double* lE = hcol(ph, mats[0], DP_COL_LOGE);
+  for (int j = 1; j < nm; ++j)
+    if (std::memcmp(E, hcol(ph, mats[j], DP_COL_E), sizeof(double) * n) != 0)
+      return fail(ctx, DP_ERR_ARG, "mixture materials must share the energy grid");
+  m->phys = ph;
+  m->uid = g_uid.fetch_add(1);
+  m->nm = nm;
+  m->mats.assign(mats, mats + nm);
+  m->fracs.resize(nm);
+  // MaterialMixture normalises its fractions (src/Types.jl:363-368)
+  for (int j = 0; j < nm; ++j) m->fracs[j] = fr[j] / tot;
+  m->n = n;
+  const int ncol = MC_LB1 + 2 * nm;
+  m->cols.assign(size_t(ncol) * n, 0.0);
+  auto C = [&](int c) { return m->cols.data() + size_t(c) * n; };
+  std::copy(E, E + n, C(MC_E));
+  std::copy(lE, lE + n, C(MC_LE));
+  const int src[7] = {DP_COL_CSDA_S, DP_COL_CSDA_R, DP_COL_MIXED_S, DP_COL_MIXED_R,
+                      DP_COL_STRAG, DP_COL_MU0, DP_COL_FSPIN};
+  const int dst[7] = {MC_CS, MC_CR, MC_MS, MC_MR, MC_STRAG, MC_MU0, MC_FSPIN};
+  if (nm == 1) {
+    for (int k = 0; k < 7; ++k) std::copy(hcol(ph, mats[0], src[k]), hcol(ph, mats[0], src[k]) + n, C(dst[k]));
+    m->ZoA = ph->recipes[mats[0]].ZoA;
+  } else {
+    // src/Physics.jl:1152-1323: fraction-weighted node values on the shared
+    // grid; ranges integrated from the mixture stopping power
+    // (_build_mixture_table, src/Physics.jl:1058-1105)
+    for (int k = 0; k < 7; ++k) {
+      if (dst[k] == MC_CR || dst[k] == MC_MR) continue;
+      double* o = C(dst[k]);
+      for (int j = 0; j < nm; ++j) {
+        const double* y = hcol(ph, mats[j], src[k]);
+        for (int i = 0; i < n; ++i) o[i] += m->fracs[j] * y[i];
+      }
+    }
+    const double* gE = hcol(ph, 0, DP_COL_E);
+    auto stop = [&](bool mixed, double K) {
+      double v = 0.0;
+      for (int j = 0; j < nm; ++j)
+        v += m->fracs[j] * h_interp(K, hcol(ph, mats[j], DP_COL_E), hcol(ph, mats[j], DP_COL_LOGE),
+                                    hcol(ph, mats[j], mixed ? DP_COL_MIXED_S : DP_COL_CSDA_S), n);
+      return v;
+    };
+    double* cR = C(MC_CR);
+    double* mR = C(MC_MR);
+    double cp = stop(false, gE[0]), mp = stop(true, gE[0]);
+    cR[0] = gE[0] / cp;
+    mR[0] = gE[0] / mp;
+    for (int i = 1; i < n; ++i) {
+      double K = gE[i], Kp = gE[i - 1], dK = K - Kp;
+      double c = stop(false, K), mm = stop(true, K);
+      cR[i] = cR[i - 1] + dK / ((c + cp) / 2);
+      mR[i] = mR[i - 1] + dK / ((mm + mp) / 2);
+      cp = c;
+      mp = mm;
+    }
+    m->ZoA = 0.0;
+    for (int j = 0; j < nm; ++j) m->ZoA += m->fracs[j] * ph->recipes[mats[j]].ZoA;
+  }
+  for (int j = 0; j < nm; ++j) {
+    std::copy(hcol(ph, mats[j], DP_COL_LB1), hcol(ph, mats[j], DP_COL_LB1) + n, C(MC_LB1 + j));
+    std::copy(hcol(ph, mats[j], DP_COL_LBE), hcol(ph, mats[j], DP_COL_LBE) + n, C(MC_LB1 + nm + j));
+  }
+
+  // prepare_mixed_kernel (src/MixedTransport.jl:57-97)
+  const dp_settings& st = ph->settings;
+  double lo = -1e300, hi = 1e300;
+  for (int j = 0; j < nm; ++j) {
+    lo = std::max(lo, hcol(ph, mats[j], DP_COL_E)[0]);
+    hi = std::min(hi, hcol(ph, mats[j], DP_COL_E)[n - 1]);
+  }
+  std::vector<double> grid;
+  for (int j = 0; j < nm; ++j)
+    for (int i = 0; i < n; ++i) {
+      double e = hcol(ph, mats[j], DP_COL_E)[i];
+      if (lo <= e && e <= hi) grid.push_back(e);
+    }
+  std::sort(grid.begin(), grid.end());
+  grid.erase(std::unique(grid.begin(), grid.end()), grid.end());
+  const int refinement = 8;
+  std::vector<double> kE;
+  for (size_t j = 0; j + 1 < grid.size(); ++j) {
+    double a = std::log(grid[j]), b = std::log(grid[j + 1]);
+    for (int k = 0; k < refinement; ++k)
+      kE.push_back(std::exp(a + double(k) * (b - a) / double(refinement)));
+  }
+  kE.push_back(hi);
+  kE[0] = lo;
+  const int nk = int(kE.size());
+  auto prop = [&](int col, double k) {
+    double v = 0.0;
+    for (int j = 0; j < nm; ++j)
+      v += m->fracs[j] * h_interp(k, hcol(ph, mats[j], DP_COL_E), hcol(ph, mats[j], DP_COL_LOGE),
+                                  hcol(ph, mats[j], col), n);
+    return v;
+  };
+  m->nk = nk;
+  m->kcols.assign(size_t(K_NCOL) * nk, 0.0);
+  double* K0 = m->kcols.data();
+  double *kS = K0 + size_t(K_S) * nk, *kSig = K0 + size_t(K_SIG) * nk,
+         *kR = K0 + size_t(K_R) * nk, *kH = K0 + size_t(K_H) * nk, *kT = K0 + size_t(K_T) * nk;
+  std::copy(kE.begin(), kE.end(), K0);
+  for (int i = 0; i < nk; ++i) {
+    kS[i] = prop(DP_COL_MIXED_S, kE[i]);
+    kSig[i] = prop(DP_COL_XS, kE[i]);
+  }
+  m->onset = std::numeric_limits<double>::infinity();
+  for (double g : grid) {
+    double r = prop(DP_COL_XS, g);
+    if (r > 0) {
+      m->onset = g;
+      for (int i = 0; i < nk; ++i)
+        if (kE[i] < g) kSig[i] = r;
+      break;
+    }
+  }
+  for (int j = 1; j < nk; ++j) {
+    double a = kE[j - 1], b = kE[j], d = b - a;
+    kR[j] = kR[j - 1] + d / 2 * (1 / kS[j - 1] + 1 / kS[j]);
+    kH[j] = kH[j - 1] + d / 2 * (kSig[j - 1] / kS[j - 1] + kSig[j] / kS[j]);
+    kT[j] = kT[j - 1] + d / 2 * st.mass *
+                            (1 / (std::sqrt(a * (a + 2 * st.mass)) * kS[j - 1]) +
+                             1 / (std::sqrt(b * (b + 2 * st.mass)) * kS[j]));
+  }
+  m->el.clear();
+  for (int j = 0; j < nm; ++j)
+    for (const HostElement& e : ph->recipes[mats[j]].elements) {
+      const double v[kElStride] = {e.Z, e.A, e.I, m->fracs[j] * e.fraction, rms_radius(e.Z)};
+      m->el.insert(m->el.end(), v, v + kElStride);
+    }
+  m->nel = int(m->el.size() / kElStride);
+  if (m->nel > kMaxEl) return fail(ctx, DP_ERR_ARG, "a medium holds at most 32 elements");
+  return DP_OK;
+}
+
+int pad_elems(int n, size_t esize) {
+  int per = int(16 / esize);
+  return (n + per - 1) / per * per;
+}
+
+Layout make_layout(const dp_mixture* a, const dp_mixture* b, size_t esize) {
+  Layout L{};
+  L.n = a->n;
+  L.nk = a->nk;
+  L.slots = std::max(a->nm, b->nm);
+  L.ld = pad_elems(L.n, esize);
+  L.ldk = pad_elems(L.nk, esize);
+  L.o_phys = uint32_t(kMaxEl * kElStride * sizeof(double));
+  L.o_ker = L.o_phys + uint32_t(size_t(MC_LB1 + 2 * L.slots) * L.ld * esize);
+  L.med_bytes = L.o_ker + uint32_t(size_t(K_NCOL) * L.ldk * esize);
+  const dp_physics* ph = a->phys;
+  L.uniform = ph->view.uniform;
+  L.lE0 = ph->view.lE0;
+  L.inv_dlE = ph->view.inv_dlE;
+  return L;
+}
+
+template <class R>
+void pack(const dp_mixture* m, const Layout& L, unsigned char* out) {
+  std::memset(out, 0, L.med_bytes);
+  std::memcpy(out, m->el.data(), m->el.size() * sizeof(double));
+  R* P = reinterpret_cast<R*>(out + L.o_phys);
+  auto put = [&](R* dst, const double* src, int n) {
+    for (int i = 0; i < n; ++i) dst[i] = R(src[i]);
+  };
+  for (int c = 0; c < MC_LB1; ++c) put(P + size_t(c) * L.ld, m->cols.data() + size_t(c) * m->n, m->n);
+  for (int j = 0; j < m->nm; ++j) {
+    put(P + size_t(MC_LB1 + j) * L.ld, m->cols.data() + size_t(MC_LB1 + j) * m->n, m->n);
+    put(P + size_t(MC_LB1 + L.slots + j) * L.ld, m->cols.data() + size_t(MC_LB1 + m->nm + j) * m->n,
+        m->n);
+  }
+  R* K = reinterpret_cast<R*>(out + L.o_ker);
+  for (int c = 0; c < K_NCOL; ++c) put(K + size_t(c) * L.ldk, m->kcols.data() + size_t(c) * m->nk, m->nk);
+}
+
+MedInfo make_info(const dp_mixture* m) {
+  MedInfo I{};
+  I.nm = m->nm;
+  I.nel = m->nel;
+  for (int j = 0; j < kMaxMix; ++j) I.frac[j] = j < m->nm ? m->fracs[j] : 0.0;
+  I.ZoA = m->ZoA;
+  I.onset = m->onset;
+  return I;
+}
+
+// Device blob of the (rock, air) pair in one precision, built once per pair.
+int get_blob(dp_ctx* ctx, dp_mixture* rock, const dp_mixture* air, int precision,
+             const unsigned char** dev, Layout* lay) {
+  for (auto& b : rock->blobs)
+    if (b.partner == air->uid && b.precision == precision) {
+      *dev = b.dev;
+      *lay = b.lay;
+      return DP_OK;
+    }
+  if (rock->n != air->n || rock->nk != air->nk || rock->phys != air->phys)
+    return fail(ctx, DP_ERR_ARG, "rock and air media must come from one physics");
+  size_t es = precision == DP_PREC_MIXED ? sizeof(float) : sizeof(double);
+  Layout L = make_layout(rock, air, es);
+  std::vector<unsigned char> h(size_t(2) * L.med_bytes);
+  if (es == sizeof(float)) {
+    pack<float>(rock, L, h.data());
+    pack<float>(air, L, h.data() + L.med_bytes);
+  } else {
+    pack<double>(rock, L, h.data());
+    pack<double>(air, L, h.data() + L.med_bytes);
+  }
+  unsigned char* d = nullptr;
+  DP_CHECK_CUDA(ctx, cudaMalloc(&d, h.size()));
+  DP_CHECK_CUDA(ctx, cudaMemcpy(d, h.data(), h.size(), cudaMemcpyHostToDevice));
+  rock->blobs.push_back({air->uid, precision, d, L});
+  *dev = d;
+  *lay = L;
+  return DP_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ kernel
+namespace dp {
+namespace mc {
+
+struct McParams {
+  const unsigned char* blob;  // rock medium, then air medium
+  Layout lay;
+  MedInfo info[2];
+  Consts C;
+  uint64_t seed;
+  int staged;
+  int source;  // 0 explicit histories, 1 lines of sight
+  long n;
+  uint64_t id0;
+  const double *E, *q, *w, *thick, *dens, *elev, *H;
+  int geo_stride;
+  const dp_los* los;
+  const int64_t* los_off;  // n_los + 1 running sample offsets
+  long n_los;
+  double* contrib;
+  int32_t* status;
+  int32_t* steps;
+  double* efinal;
+  unsigned long long* counter;
+  int* err_flag;
+};
+
+constexpr int kMcThreads = 256;
+
+// Copies `bytes` (16-byte multiple) from global to shared memory with
+// cp.async.bulk completing on one mbarrier; all threads call it.  Returns
+// false if the bounded wait gave up.
+__device__ bool stage_blob(unsigned char* dst, const unsigned char* src, uint32_t bytes,
+                           uint64_t* mbar) {
+  uint32_t bar = smem_u32(mbar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(1) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+    const uint32_t chunk = 32768;
+    for (uint32_t off = 0; off < bytes; off += chunk) {
+      uint32_t b = bytes - off < chunk ? bytes - off : chunk;
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+              smem_u32(dst + off)),
+          "l"(src + off), "r"(b), "r"(bar)
+          : "memory");
+    }
+  }
+  uint32_t done = 0;
+  for (int it = 0; it < (1 << 22) && !done; ++it) {
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(0)
+        : "memory");
+  }
+  return __syncthreads_and(done != 0) != 0;
+}
+
+// Next history index for the calling thread (warp-aggregated atomic).
+__device__ __forceinline__ long next_history(unsigned long long* counter) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  unsigned long long base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(counter, (unsigned long long)g.size());
+  base = g.shfl(base, 0);
+  return long(base + g.thread_rank());
+}
+
+template <class R>
+__device__ __forceinline__ void start_history(const McParams& P, long i, Hist<R>& h, Stream& g) {
+  double E0, q, ws, thick, rho, elev, H;
+  uint64_t id;
+  if (P.source == 0) {
+    E0 = P.E[i];
+    q = P.q[i];
+    ws = P.w[i];
+    long gi = P.geo_stride ? i : 0;
+    thick = P.thick[gi];
+    rho = P.dens[gi];
+    elev = P.elev[gi];
+    H = P.H[gi];
+    id = P.id0 + uint64_t(i);
+  } else {
+    long lo = 0, hi = P.n_los;  // los_off[lo] <= i < los_off[lo + 1]
+    while (hi - lo > 1) {
+      long mid = (lo + hi) >> 1;
+      if (P.los_off[mid] <= i) lo = mid; else hi = mid;
+    }
+    const dp_los& L = P.los[lo];
+    id = uint64_t(i);
+    double emax = L.energy_max > L.energy_min ? L.energy_max : L.energy_min;
+    mc_sample(P.seed, id, L.energy_min, emax, &E0, &q, &ws);
+    U4 b1 = philox(U4{uint32_t(id), uint32_t(id >> 32), 1u, 0u}, uint32_t(P.seed), uint32_t(P.seed >> 32));
+    U4 b2 = philox(U4{uint32_t(id), uint32_t(id >> 32), 2u, 0u}, uint32_t(P.seed), uint32_t(P.seed >> 32));
+    thick = L.thickness_max > L.thickness
+                ? L.thickness + (L.thickness_max - L.thickness) * u01(b1.x, b1.y)
+                : L.thickness;
+    rho = L.density_max > L.density ? L.density + (L.density_max - L.density) * u01(b1.z, b1.w)
+                                    : L.density;
+    elev = L.elevation_max > L.elevation
+               ? L.elevation + (L.elevation_max - L.elevation) * u01(b2.x, b2.y)
+               : L.elevation;
+    H = L.air_height > 0.0 ? thick + L.air_height
+                           : (L.primary_altitude > 0.0 ? L.primary_altitude : 3e4);
+  }
+  double theta = (90.0 - elev) * kPi / 180.0;
+  h.s.x = h.s.y = h.s.z = 0.0;
+  h.s.ux = R(-sin(theta));
+  h.s.uy = R(0);
+  h.s.uz = R(-cos(theta));
+  h.s.E = R(E0);
+  h.s.w = R(1);
+  h.s.status = 0;
+  h.limit = 0.0;
+  h.thick = thick;
+  h.rho = rho;
+  h.H = H;
+  h.q = q;
+  h.ws = ws;
+  h.steps = h.inner = h.outer = 0;
+  h.need_mode = true;
+  h.strag = h.mixed = h.scat = false;
+  g.init(P.seed, id);
+}
+
+template <class R>
+__device__ __forceinline__ void end_history(const McParams& P, long i, const Hist<R>& h) {
+  P.contrib[i] = h.ws * history_flux(P.C, h);
+  if (P.status) P.status[i] = h.s.status;
+  if (P.steps) P.steps[i] = h.steps;
+  if (P.efinal) {
+    double* f = P.efinal + 4 * i;
+    f[0] = double(h.s.E);
+    f[1] = h.s.z;
+    f[2] = double(h.s.uz);
+    f[3] = double(h.s.w);
+  }
+}
+
+template <class R>
+__global__ void __launch_bounds__(kMcThreads) mc_kernel(const __grid_constant__ McParams P) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const unsigned char* base = P.blob;
+  if (P.staged) {
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
+    unsigned char* dst = smem + 16;
+    if (!stage_blob(dst, P.blob, 2 * P.lay.med_bytes, bar)) {
+      // give the copy in flight a second bounded wait before leaving
+      uint32_t done = 0;
+      for (int it = 0; it < (1 << 22) && !done; ++it)
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(0)
+            : "memory");
+      if (threadIdx.x == 0) atomicExch(P.err_flag, 1);
+      return;
+    }
+    base = dst;
+  }
+  const Med<R> rock = make_med<R>(base, P.lay, P.info[0]);
+  const Med<R> air = make_med<R>(base + P.lay.med_bytes, P.lay, P.info[1]);
+  Hist<R> h;
+  Stream g;
+  long i = next_history(P.counter);
+  bool live = i < P.n;
+  if (live) start_history(P, i, h, g);
+  while (live) {
+    if (advance(rock, air, P.C, h, g)) {
+      end_history(P, i, h);
+      i = next_history(P.counter);
+      live = i < P.n;
+      if (live) start_history(P, i, h, g);
+    }
+  }
+}
+
+// Per line of sight: compensated sums of the contributions and of their
+// squares in a fixed order (one warp per line of sight), then flux, sigma
+// (src/Geometry.jl:883-893) and the count of flagged histories.
+__global__ void __launch_bounds__(256) los_tally_kernel(const double* contrib, const int32_t* status,
+                                                        const int64_t* off, const dp_los* los,
+                                                        long n_los, dp_los_result* out,
+                                                        int* status_or) {
+  long l = (long(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (l >= n_los) return;
+  long a = off[l], b = off[l + 1];
+  KSum s{0, 0}, s2{0, 0};
+  long bad = 0;
+  int bits = 0;
+  for (long i = a + lane; i < b; i += 32) {
+    double x = contrib[i];
+    kadd(s, x);
+    kadd(s2, x * x);
+    int st = status[i];
+    bad += st != 0;
+    bits |= st;
+  }
+  bits = __reduce_or_sync(0xffffffffu, unsigned(bits));
+  for (int d = 16; d > 0; d >>= 1) {
+    KSum o{__shfl_down_sync(0xffffffffu, s.s, d), __shfl_down_sync(0xffffffffu, s.c, d)};
+    KSum o2{__shfl_down_sync(0xffffffffu, s2.s, d), __shfl_down_sync(0xffffffffu, s2.c, d)};
+    long ob = __shfl_down_sync(0xffffffffu, bad, d);
+    kmerge(s, o);
+    kmerge(s2, o2);
+    bad += ob;
+  }
+  if (lane == 0) {
+    long n = b - a;
+    double sum = s.s + s.c, sum2 = s2.s + s2.c;
+    dp_los_result r{};
+    r.n_samples = n;
+    r.n_status_nonzero = bad;
+    if (n > 0) {
+      double f = sum / double(n), var = sum2 / double(n) - f * f;
+      r.flux = f;
+      r.sigma = los[l].thickness > 0.0 ? sqrt(fmax(var, 0.0) / double(n)) : 0.0;
+    }
+    out[l] = r;
+    if (bits) atomicOr(status_or, bits);
+  }
+}
+
+// Running sample offsets of the lines of sight (single block, sequential
+// chunks; n_los is at most a few 10^5).
+__global__ void __launch_bounds__(1024) los_offsets_kernel(const dp_los* los, long n_los,
+                                                           int64_t* off, long expect, int* err) {
+  __shared__ int64_t part[1024];
+  long per = (n_los + 1023) / 1024;
+  long a = threadIdx.x * per, b = a + per < n_los ? a + per : n_los;
+  int64_t s = 0;
+  for (long l = a; l < b; ++l) s += los[l].n_samples > 0 ? los[l].n_samples : 0;
+  part[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int64_t run = 0;
+    for (int t = 0; t < 1024; ++t) {
+      int64_t v = part[t];
+      part[t] = run;
+      run += v;
+    }
+    off[n_los] = run;
+    if (run != expect) atomicExch(err, 2);
+  }
+  __syncthreads();
+  int64_t run = part[threadIdx.x];
+  for (long l = a; l < b; ++l) {
+    off[l] = run;
+    run += los[l].n_samples > 0 ? los[l].n_samples : 0;
+  }
+}
+
+}  // namespace mc
+}  // namespace dp
+
+namespace {
+
+int check_cfg(dp_ctx* ctx, const dp_physics* ph, const dp_mc_config* cfg, Consts* C) {
+  if (!cfg) return fail(ctx, DP_ERR_ARG, "null config");
+  if (cfg->precision != DP_PREC_FP64 && cfg->precision != DP_PREC_MIXED)
+    return fail(ctx, DP_ERR_ARG, "precision must be DP_PREC_FP64 or DP_PREC_MIXED");
+  double tmax = ph->host[(size_t(0) * DP_NCOL + DP_COL_E) * ph->n + ph->n - 1];
+  double thr = cfg->source_energy_max > 0.0 ? cfg->source_energy_max : std::fmin(1e9, tmax);
+  if (!(thr > 0.0 && thr <= tmax))
+    return fail(ctx, DP_ERR_ARG, "source_energy_max must be positive and within the physics energy grid");
+  double low = cfg->energy_threshold_low > 0.0 ? cfg->energy_threshold_low : 100.0;
+  if (cfg->precision == DP_PREC_MIXED) {
+    // thresholds exactly representable in the FP32 transport
+    thr = double(float(thr));
+    if (thr > tmax) thr = double(std::nextafter(float(tmax), 0.0f));
+    low = double(float(low));
+  }
+  C->mass = ph->settings.mass;
+  C->ctau = ph->settings.ctau;
+  C->cutoff = ph->settings.cutoff;
+  C->elastic_ratio = ph->settings.elastic_ratio;
+  C->thr = thr;
+  C->thr_low = low;
+  C->straggling = cfg->straggling != 0;
+  C->scattering = cfg->scattering != 0;
+  return DP_OK;
+}
+
+template <class R>
+int launch_mc(dp_ctx* ctx, McParams& P) {
+  const int threads = kMcThreads;
+  size_t smem = 16 + size_t(2) * P.lay.med_bytes;
+  int dev_smem = 0;
+  DP_CHECK_CUDA(ctx, cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+  P.staged = smem <= size_t(dev_smem) ? 1 : 0;
+  if (!P.staged) smem = 0;
+  DP_CHECK_CUDA(ctx, cudaFuncSetAttribute(mc_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          int(smem)));
+  int per_sm = 0, n_sm = 0;
+  DP_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_kernel<R>, threads, smem));
+  DP_CHECK_CUDA(ctx, cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, ctx->device));
+  if (per_sm < 1) return fail(ctx, DP_ERR_CUDA, "MC kernel does not fit on a multiprocessor");
+  long blocks = long(per_sm) * n_sm;
+  long need = (P.n + threads - 1) / threads;
+  if (blocks > need) blocks = need;
+  if (blocks < 1) blocks = 1;
+  DP_CHECK_CUDA(ctx, cudaMemsetAsync(P.counter, 0, sizeof(unsigned long long), ctx->stream));
+  timed_begin(ctx);
+  mc_kernel<R><<<int(blocks), threads, smem, ctx->stream>>>(P);
+  DP_CHECK_CUDA(ctx, cudaGetLastError());
+  timed_end(ctx, sizeof(R) == 4 ? "mc_mixed" : "mc_fp64");
+  return DP_OK;
+}
+
+int run(dp_ctx* ctx, McParams& P, int precision) {
+  return precision == DP_PREC_MIXED ? launch_mc<float>(ctx, P) : launch_mc<double>(ctx, P);
+}
+
+int read_flag(dp_ctx* ctx) {
+  int flag = 0;
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  DP_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (flag) {
+    cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream);
+    return fail(ctx, DP_ERR_STATE,
+                flag == 2 ? "total_samples differs from the sum of n_samples"
+                          : "a table-staging wait exceeded its limit");
+  }
+  return DP_OK;
+}
+
+int status_code(dp_ctx* ctx, int bits) {
+  if (bits & (DP_ST_DOMAIN_HI | DP_ST_DOMAIN_LO | DP_ST_ZERO_RATE | DP_ST_BAD_WEIGHT))
+    return fail(ctx, DP_ERR_DOMAIN, "a history left the prepared tables or met an invalid hard event");
+  if (bits & (DP_ST_STEP_CAP | DP_ST_EVENT_CAP | DP_ST_TABLE_WAIT))
+    return fail(ctx, DP_ERR_STATE, "a history reached a loop cap");
+  return DP_OK;
+}
+
+McParams base_params(dp_ctx* ctx, const unsigned char* blob, const Layout& lay, const dp_mixture* rock,
+                     const dp_mixture* air, const Consts& C, uint64_t seed) {
+  McParams P{};
+  P.blob = blob;
+  P.lay = lay;
+  P.info[0] = make_info(rock);
+  P.info[1] = make_info(air);
+  P.C = C;
+  P.seed = seed;
+  P.err_flag = ctx->d_flag;
+  return P;
+}
+
+}  // namespace
+
+int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_mixture* air,
+                  const dp_mc_config* cfg, long n_los, const dp_los* d_los, long total,
+                  dp_los_result* d_out, double** contrib_out, int** status_or);
+
+namespace {
+// Status bits of a finished run: the call's error code where the reference
+// would have thrown (host synchronises).
+int status_result(dp_ctx* ctx, const int* d_bits) {
+  int bits = 0;
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(&bits, d_bits, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  int rc = read_flag(ctx);
+  if (rc) return rc;
+  return status_code(ctx, bits);
+}
+}  // namespace
+
+extern "C" {
+
+int dp_mixture_prepare(dp_ctx* ctx, const dp_physics* ph, int n, const int* mats,
+                       const double* fracs, dp_mixture** out) {
+  if (!ctx || !ph || !mats || !fracs || !out) return fail(ctx, DP_ERR_ARG, "null argument");
+  dp_mixture* m = new dp_mixture;
+  int rc = prepare(ctx, ph, n, mats, fracs, m);
+  if (rc) {
+    delete m;
+    return rc;
+  }
+  *out = m;
+  return DP_OK;
+}
+
+int dp_mixture_free(dp_mixture* m) {
+  if (!m) return DP_OK;
+  for (auto& b : m->blobs) cudaFree(b.dev);
+  delete m;
+  return DP_OK;
+}
+
+int dp_mixture_kernel(const dp_mixture* m, int col, double* out, int cap, int* n, double* onset) {
+  if (!m || col < 0 || col >= K_NCOL) return DP_ERR_ARG;
+  if (n) *n = m->nk;
+  if (onset) *onset = m->onset;
+  if (out && cap > 0)
+    std::copy(m->kcols.begin() + size_t(col) * m->nk,
+              m->kcols.begin() + size_t(col) * m->nk + std::min(cap, m->nk), out);
+  return DP_OK;
+}
+
+int dp_mc_histories(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock_c,
+                    const dp_mixture* air, const dp_mc_config* cfg, long n, const double* E,
+                    const double* q, const double* w, const double* thick, const double* dens,
+                    const double* elev, const double* H, int geo_stride, uint64_t id0,
+                    double* contrib, int32_t* status, int32_t* steps, double* efinal) {
+  if (!ctx || !ph || !rock_c || !air) return fail(ctx, DP_ERR_ARG, "null argument");
+  dp_mixture* rock = const_cast<dp_mixture*>(rock_c);
+  Consts C;
+  int rc = check_cfg(ctx, ph, cfg, &C);
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && (!E || !q || !w || !thick || !dens || !elev || !H || !contrib)))
+    return fail(ctx, DP_ERR_ARG, "bad history arrays");
+  if (n == 0) return DP_OK;
+  for (long i = 0; i < (geo_stride ? n : 1); ++i)
+    if (!(dens[i] > 0.0) || !(thick[i] >= 0.0) || !(H[i] > 0.0))
+      return fail(ctx, DP_ERR_ARG, "positive density and altitude, nonnegative thickness required");
+  DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  const unsigned char* blob;
+  Layout lay;
+  rc = get_blob(ctx, rock, air, cfg->precision, &blob, &lay);
+  if (rc) return rc;
+  long ng = geo_stride ? n : 1;
+  size_t nb = size_t(n) * sizeof(double), gb = size_t(ng) * sizeof(double);
+  Arena A;
+  A.base = static_cast<char*>(scratch(ctx, 8 * nb + 4 * gb + size_t(n) * 8 + 4096, 0));
+  A.cap = ctx->slot_bytes[0];
+  double* dE = A.take<double>(n);
+  double* dq = A.take<double>(n);
+  double* dw = A.take<double>(n);
+  double* dc = A.take<double>(n);
+  double* dEf = A.take<double>(4 * n);
+  double* dt = A.take<double>(ng);
+  double* dd = A.take<double>(ng);
+  double* de = A.take<double>(ng);
+  double* dH = A.take<double>(ng);
+  int32_t* ds = A.take<int32_t>(n);
+  int32_t* dn = A.take<int32_t>(n);
+  unsigned long long* ctr = A.take<unsigned long long>(1);
+  if (!ctr) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
+  cudaStream_t s = ctx->stream;
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dE, E, nb, cudaMemcpyHostToDevice, s));
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dq, q, nb, cudaMemcpyHostToDevice, s));
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dw, w, nb, cudaMemcpyHostToDevice, s));
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dt, thick, gb, cudaMemcpyHostToDevice, s));
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dd, dens, gb, cudaMemcpyHostToDevice, s));
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(de, elev, gb, cudaMemcpyHostToDevice, s));
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dH, H, gb, cudaMemcpyHostToDevice, s));
+  McParams P = base_params(ctx, blob, lay, rock, air, C, cfg->seed);
+  P.source = 0;
+  P.n = n;
+  P.id0 = id0;
+  P.E = dE;
+  P.q = dq;
+  P.w = dw;
+  P.thick = dt;
+  P.dens = dd;
+  P.elev = de;
+  P.H = dH;
+  P.geo_stride = geo_stride ? 1 : 0;
+  P.contrib = dc;
+  P.status = ds;
+  P.steps = dn;
+  P.efinal = dEf;
+  P.counter = ctr;
+  rc = run(ctx, P, cfg->precision);
+  if (rc) return rc;
+  std::vector<int32_t> st_h;
+  if (!status) {
+    st_h.resize(n);
+    status = st_h.data();
+  }
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(contrib, dc, nb, cudaMemcpyDeviceToHost, s));
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(status, ds, size_t(n) * 4, cudaMemcpyDeviceToHost, s));
+  if (steps) DP_CHECK_CUDA(ctx, cudaMemcpyAsync(steps, dn, size_t(n) * 4, cudaMemcpyDeviceToHost, s));
+  if (efinal) DP_CHECK_CUDA(ctx, cudaMemcpyAsync(efinal, dEf, 4 * nb, cudaMemcpyDeviceToHost, s));
+  DP_CHECK_CUDA(ctx, cudaStreamSynchronize(s));
+  rc = read_flag(ctx);
+  if (rc) return rc;
+  int bits = 0;
+  for (long i = 0; i < n; ++i) bits |= status[i];
+  return status_code(ctx, bits);
+}
+
+int dp_mc_los_dev(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock_c,
+                  const dp_mixture* air, const dp_mc_config* cfg, long n_los, const dp_los* los,
+                  long total, int compute_gradient, dp_los_result* out) {
+  if (!ctx || !ph || !rock_c || !air || !los || !out || n_los <= 0 || total < 0)
+    return fail(ctx, DP_ERR_ARG, "bad arguments");
+  if (compute_gradient)
+    return fail(ctx, DP_ERR_ARG, "the per-line-of-sight CSDA gradient is not available in this call");
+  double* contrib = nullptr;
+  int* bits = nullptr;
+  int rc = dp_mc_run_los(ctx, ph, const_cast<dp_mixture*>(rock_c), air, cfg, n_los, los, total, out,
+                         &contrib, &bits);
+  if (rc) return rc;
+  if (ctx->blocking) return status_result(ctx, bits);
+  return DP_OK;
+}
+
+int dp_mc_los(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock, const dp_mixture* air,
+              const dp_mc_config* cfg, long n_los, const dp_los* los, int compute_gradient,
+              dp_los_result* out) {
+  if (!ctx || !los || !out || n_los <= 0) return fail(ctx, DP_ERR_ARG, "bad arguments");
+  long total = 0;
+  for (long l = 0; l < n_los; ++l) {
+    const dp_los& L = los[l];
+    if (L.n_samples < 0) return fail(ctx, DP_ERR_ARG, "negative n_samples");
+    if (!(L.energy_min > 0.0)) return fail(ctx, DP_ERR_ARG, "energy_min must be positive");
+    // transport_mixed_step needs a positive density (src/MixedTransport.jl:146)
+    if (!(L.density > 0.0) || !(L.thickness >= 0.0))
+      return fail(ctx, DP_ERR_ARG, "positive density and nonnegative thickness required");
+    total += L.n_samples;
+  }
+  DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  Arena A;
+  size_t lb = size_t(n_los) * sizeof(dp_los), ob = size_t(n_los) * sizeof(dp_los_result);
+  A.base = static_cast<char*>(scratch(ctx, lb + ob + 1024, 2));
+  A.cap = ctx->slot_bytes[2];
+  dp_los* dl = A.take<dp_los>(n_los);
+  dp_los_result* dr = A.take<dp_los_result>(n_los);
+  if (!dr) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dl, los, lb, cudaMemcpyHostToDevice, ctx->stream));
+  if (compute_gradient)
+    return fail(ctx, DP_ERR_ARG, "the per-line-of-sight CSDA gradient is not available in this call");
+  double* contrib = nullptr;
+  int* bits = nullptr;
+  int rc = dp_mc_run_los(ctx, ph, const_cast<dp_mixture*>(rock), air, cfg, n_los, dl, total, dr,
+                         &contrib, &bits);
+  if (rc) return rc;
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(out, dr, ob, cudaMemcpyDeviceToHost, ctx->stream));
+  return status_result(ctx, bits);
+}
+
+}  // extern "C"
+
+// Enqueues one batched run over n_los lines of sight (device records) and
+// the per-line-of-sight tallies; *contrib_out receives the per-history
+// contributions (scratch slot 0, valid until the next call on ctx).
+int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_mixture* air,
+                  const dp_mc_config* cfg, long n_los, const dp_los* d_los, long total,
+                  dp_los_result* d_out, double** contrib_out, int** status_or) {
+  Consts C;
+  int rc = check_cfg(ctx, ph, cfg, &C);
+  if (rc) return rc;
+  DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  const unsigned char* blob;
+  Layout lay;
+  rc = get_blob(ctx, rock, air, cfg->precision, &blob, &lay);
+  if (rc) return rc;
+  long nt = total > 0 ? total : 1;
+  Arena A;
+  A.base = static_cast<char*>(scratch(ctx, size_t(nt) * 12 + size_t(n_los + 1) * 8 + 4096, 0));
+  A.cap = ctx->slot_bytes[0];
+  double* dc = A.take<double>(nt);
+  int32_t* ds = A.take<int32_t>(nt);
+  int64_t* off = A.take<int64_t>(n_los + 1);
+  unsigned long long* ctr = A.take<unsigned long long>(1);
+  int* bits = A.take<int>(1);
+  if (!bits) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
+  DP_CHECK_CUDA(ctx, cudaMemsetAsync(bits, 0, sizeof(int), ctx->stream));
+  los_offsets_kernel<<<1, 1024, 0, ctx->stream>>>(d_los, n_los, off, total, ctx->d_flag);
+  ++ctx->launches;
+  DP_CHECK_CUDA(ctx, cudaGetLastError());
+  if (total > 0) {
+    McParams P = base_params(ctx, blob, lay, rock, air, C, cfg->seed);
+    P.source = 1;
+    P.n = total;
+    P.los = d_los;
+    P.los_off = off;
+    P.n_los = n_los;
+    P.contrib = dc;
+    P.status = ds;
+    P.counter = ctr;
+    rc = run(ctx, P, cfg->precision);
+    if (rc) return rc;
+  }
+  long warps_per_block = 8;
+  long blocks = (n_los + warps_per_block - 1) / warps_per_block;
+  timed_begin(ctx);
+  los_tally_kernel<<<int(blocks), 256, 0, ctx->stream>>>(dc, ds, off, d_los, n_los, d_out, bits);
+  DP_CHECK_CUDA(ctx, cudaGetLastError());
+  timed_end(ctx, "mc_tally");
+  if (contrib_out) *contrib_out = dc;
+  if (status_or) *status_or = bits;
+  return DP_OK;
+}
+
+namespace dp {
+int mc_backward_stochastic(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params* p, int rock,
+                           int air, double threshold, dp_los_result* res) {
+  dp_mixture rm, am;
+  const double one = 1.0;
+  int rc = prepare(ctx, ph, 1, &rock, &one, &rm);
+  if (!rc) rc = prepare(ctx, ph, 1, &air, &one, &am);
+  if (rc) return rc;
+  dp_mc_config cfg{};
+  cfg.straggling = p->straggling;
+  cfg.scattering = p->scattering;
+  cfg.energy_threshold_low = p->energy_threshold_low;
+  cfg.source_energy_max = threshold;
+  cfg.seed = p->seed;
+  cfg.precision = p->precision;
+  dp_los L{};
+  L.thickness = p->rock_thickness;
+  L.density = p->rock_density;
+  L.elevation = p->elevation;
+  L.primary_altitude = p->primary_altitude > 0.0 ? p->primary_altitude : 3e4;
+  L.energy_min = p->energy_min;
+  L.energy_max = p->energy_max > p->energy_min ? p->energy_max : p->energy_min;
+  L.n_samples = p->n_samples;
+  Arena A;
+  A.base = static_cast<char*>(scratch(ctx, sizeof(dp_los) + sizeof(dp_los_result) + 1024, 2));
+  A.cap = ctx->slot_bytes[2];
+  dp_los* dl = A.take<dp_los>(1);
+  dp_los_result* dr = A.take<dp_los_result>(1);
+  if (!dr) rc = fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
+  int* bits = nullptr;
+  if (!rc) {
+    cudaError_t e = cudaMemcpyAsync(dl, &L, sizeof(L), cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) rc = cuda_fail(ctx, e, "cudaMemcpyAsync");
+  }
+  if (!rc) rc = dp_mc_run_los(ctx, ph, &rm, &am, &cfg, 1, dl, p->n_samples, dr, nullptr, &bits);
+  if (!rc) {
+    cudaError_t e = cudaMemcpyAsync(res, dr, sizeof(*res), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e != cudaSuccess) rc = cuda_fail(ctx, e, "cudaMemcpyAsync");
+  }
+  if (!rc) rc = status_result(ctx, bits);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& b : rm.blobs) cudaFree(b.dev);
+  return rc;
+}
+}  // namespace dp

@@ -1,0 +1,919 @@
+// mc_device.cuh -- device side of the stochastic backward Monte Carlo: one
+// thread per history, templated on the transport arithmetic R (double: the
+// reference's FP64 operations; float: the mixed-precision form, where
+// positions, event kinematics, DCS and the flux stay FP64).
+//
+// Restates src/Geometry.jl:148-357 (straggled step), :424-457 (CSDA step),
+// :461-476 (step limit), :534-672 (dual-mode loop), :694-757 (acceptance),
+// src/MixedTransport.jl:43-200 (MIXED kernel lookups, adjoint hard events,
+// mixed step) and src/Straggling.jl (fluctuations, EHS, angles, rotations).
+// Random numbers: Philox4x32-10 keyed by the seed with counter (history id,
+// block); block 0 holds the energy/charge draws, blocks 1-2 the drawn
+// geometry, transport draws start at block 3.
+#pragma once
+#include <math_constants.h>
+
+#include "common.cuh"
+#include "dcs.cuh"
+
+namespace dp {
+namespace mc {
+
+constexpr int kMaxMix = 4;   // materials in one mixture medium
+constexpr int kMaxEl = 32;   // elements in one medium
+constexpr int kElStride = 5; // Z, A, I, fraction, nuclear RMS radius (m)
+constexpr double kEhsPathMax = 1e9;
+constexpr uint32_t kTransportBlock = 3;
+
+enum : int {
+  ST_STEP_CAP = DP_ST_STEP_CAP,
+  ST_OUTER_CAP = DP_ST_OUTER_CAP,
+  ST_EVENT_CAP = DP_ST_EVENT_CAP,
+  ST_DOMAIN_HI = DP_ST_DOMAIN_HI,
+  ST_DOMAIN_LO = DP_ST_DOMAIN_LO,
+  ST_ZERO_RATE = DP_ST_ZERO_RATE,
+  ST_BAD_WEIGHT = DP_ST_BAD_WEIGHT,
+  ST_TABLE = DP_ST_TABLE_WAIT,
+  ST_FATAL = ST_STEP_CAP | ST_EVENT_CAP | ST_DOMAIN_HI | ST_DOMAIN_LO | ST_ZERO_RATE |
+             ST_BAD_WEIGHT | ST_TABLE,
+};
+
+// Packed medium (one blob per medium and precision, the same layout for
+// every medium of a launch): kMaxEl elements of kElStride doubles, then the
+// physics-grid columns (stride ld), then the MIXED kernel columns (stride ldk).
+// Physics-grid columns: MC_E ... MC_FSPIN, then `slots` transport-path columns
+// (one per mixture material) and `slots` elastic-path columns.
+enum MedCol { MC_E = 0, MC_LE, MC_CS, MC_CR, MC_MS, MC_MR, MC_STRAG, MC_MU0, MC_FSPIN, MC_LB1 };
+// MIXED kernel columns (src/MixedTransport.jl:15-29).
+enum KerCol { K_E = 0, K_S, K_SIG, K_R, K_H, K_T, K_NCOL };
+
+struct Layout {
+  uint32_t med_bytes;  // bytes of one medium (16-byte multiple)
+  uint32_t o_phys;     // byte offset of the physics columns
+  uint32_t o_ker;      // byte offset of the kernel columns
+  int ld, ldk;         // column strides (elements)
+  int n, nk, slots, uniform;
+  double lE0, inv_dlE;
+};
+struct MedInfo {
+  int nm, nel;
+  double frac[kMaxMix];
+  double ZoA, onset;
+};
+
+template <class R>
+struct Med {
+  const R* p;
+  const R* kp;
+  const double* el;
+  int ld, ldk, n, nk, nm, nel, slots, uniform;
+  R frac[kMaxMix];
+  R ZoA, onset, lE0, inv_dlE;
+  __device__ __forceinline__ const R* col(int k) const { return p + k * ld; }
+  __device__ __forceinline__ const R* kcol(int j) const { return kp + j * ldk; }
+  __device__ __forceinline__ int lbe(int j) const { return MC_LB1 + slots + j; }
+};
+
+template <class R>
+__device__ __forceinline__ Med<R> make_med(const unsigned char* base, const Layout& L,
+                                           const MedInfo& I) {
+  Med<R> m;
+  m.p = reinterpret_cast<const R*>(base + L.o_phys);
+  m.kp = reinterpret_cast<const R*>(base + L.o_ker);
+  m.el = reinterpret_cast<const double*>(base);
+  m.ld = L.ld;
+  m.ldk = L.ldk;
+  m.n = L.n;
+  m.nk = L.nk;
+  m.slots = L.slots;
+  m.uniform = L.uniform;
+  m.lE0 = R(L.lE0);
+  m.inv_dlE = R(L.inv_dlE);
+  m.nm = I.nm;
+  m.nel = I.nel;
+#pragma unroll
+  for (int j = 0; j < kMaxMix; ++j) m.frac[j] = R(I.frac[j]);
+  m.ZoA = R(I.ZoA);
+  m.onset = R(I.onset);
+  return m;
+}
+
+// Run constants shared by every history of a launch.
+struct Consts {
+  double mass, ctau, cutoff, elastic_ratio;
+  double thr_low, thr;  // mode switch and source ceiling (GeV)
+  int straggling, scattering;
+};
+
+// ------------------------------------------------------------ random stream
+struct Stream {
+  uint32_t k0, k1, c0, c1, block, w0, w1, w2, w3;
+  int used;
+  __device__ __forceinline__ void init(uint64_t seed, uint64_t id) {
+    k0 = uint32_t(seed);
+    k1 = uint32_t(seed >> 32);
+    c0 = uint32_t(id);
+    c1 = uint32_t(id >> 32);
+    block = kTransportBlock;
+    used = 2;
+  }
+  __device__ __forceinline__ void next(uint32_t& a, uint32_t& b) {
+    if (used >= 2) {
+      U4 r = philox(U4{c0, c1, block, 0u}, k0, k1);
+      ++block;
+      w0 = r.x;
+      w1 = r.y;
+      w2 = r.z;
+      w3 = r.w;
+      used = 0;
+    }
+    a = used == 0 ? w0 : w2;
+    b = used == 0 ? w1 : w3;
+    ++used;
+  }
+};
+template <class R> __device__ __forceinline__ R uni(Stream& g);
+template <> __device__ __forceinline__ double uni<double>(Stream& g) {
+  uint32_t a, b;
+  g.next(a, b);
+  return u01(a, b);
+}
+// The leading 24 bits of the same draw (it differs from the double by < 2^-24).
+template <> __device__ __forceinline__ float uni<float>(Stream& g) {
+  uint32_t a, b;
+  g.next(a, b);
+  return float(a >> 8) * 0x1p-24f;
+}
+__device__ __forceinline__ double uni_d(Stream& g) {
+  uint32_t a, b;
+  g.next(a, b);
+  return u01(a, b);
+}
+template <class R> __device__ __forceinline__ R expo(Stream& g) { return -log1p(-uni<R>(g)); }
+
+template <class R> __device__ __forceinline__ R ulp_up(R x);
+template <> __device__ __forceinline__ double ulp_up<double>(double x) {
+  return nextafter(x, CUDART_INF) - x;
+}
+template <> __device__ __forceinline__ float ulp_up<float>(float x) {
+  return nextafterf(x, CUDART_INF_F) - x;
+}
+
+// ------------------------------------------------------------ physics grid
+template <class R>
+__device__ __forceinline__ int bisect_r(const R* xs, int n, R x) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi - 1) {
+    int mid = (lo + hi) >> 1;
+    if (x < xs[mid]) hi = mid; else lo = mid;
+  }
+  return lo;
+}
+
+// Interval of x on the physics grid (src/Physics.jl:660-687): clamped ends,
+// else linear in log E.  One location serves every column at that energy.
+template <class R>
+struct Loc {
+  int i, edge;
+  R t;
+};
+template <class R>
+__device__ __forceinline__ Loc<R> locate(const Med<R>& m, R x) {
+  Loc<R> L{0, 0, R(0)};
+  const R* E = m.col(MC_E);
+  if (x <= E[0]) {
+    L.edge = -1;
+    return L;
+  }
+  if (x >= E[m.n - 1]) {
+    L.edge = 1;
+    return L;
+  }
+  const R* lE = m.col(MC_LE);
+  R lx = log(x);
+  int i;
+  if (m.uniform) {
+    R f = floor((lx - m.lE0) * m.inv_dlE);
+    i = !(f >= R(0)) ? 0 : (f > R(m.n - 2) ? m.n - 2 : int(f));
+    while (i > 0 && lx < lE[i]) --i;
+    while (i < m.n - 2 && !(lx < lE[i + 1])) ++i;
+  } else {
+    i = bisect_r(lE, m.n, lx);
+  }
+  L.i = i;
+  L.t = (lx - lE[i]) / (lE[i + 1] - lE[i]);
+  return L;
+}
+template <class R>
+__device__ __forceinline__ R at(const Med<R>& m, const Loc<R>& L, int col) {
+  const R* y = m.col(col);
+  if (L.edge < 0) return y[0];
+  if (L.edge > 0) return y[m.n - 1];
+  return y[L.i] + L.t * (y[L.i + 1] - y[L.i]);
+}
+// Inverse of a range column (src/Physics.jl:833-867).
+template <class R>
+__device__ __forceinline__ R inv_range(const Med<R>& m, int col, R X) {
+  const R* Rc = m.col(col);
+  int n = m.n;
+  if (X <= Rc[0]) return m.col(MC_E)[0];
+  if (X >= Rc[n - 1]) return m.col(MC_E)[n - 1];
+  int i = bisect_r(Rc, n, X);
+  const R* lE = m.col(MC_LE);
+  R t = (X - Rc[i]) / (Rc[i + 1] - Rc[i]);
+  return exp(lE[i] + t * (lE[i + 1] - lE[i]));
+}
+
+// property_transport_path of a material or a mixture (harmonic, src/Physics.jl:912, :1220).
+template <class R>
+__device__ __forceinline__ R transport_path(const Med<R>& m, const Loc<R>& L) {
+  if (m.nm == 1) return at(m, L, MC_LB1);
+  R inv = R(0);
+  for (int j = 0; j < m.nm; ++j) {
+    R lp = at(m, L, MC_LB1 + j);
+    if (lp > R(0)) inv += m.frac[j] / lp;
+  }
+  return inv > R(0) ? R(1) / inv : R(1e9);
+}
+// compute_ehs_mean_free_path (src/Straggling.jl:330-360, :1025-1038).
+template <class R>
+__device__ __forceinline__ R ehs_single(const Med<R>& m, int j, R K, const Loc<R>& L, R mass,
+                                        R elastic_ratio) {
+  if (K < R(1e-3)) return R(kEhsPathMax);
+  R Lb = at(m, L, m.lbe(j));
+  R p2 = K * (K + R(2) * mass);
+  if (Lb > R(0) && Lb < R(kEhsPathMax) * p2) return Lb / p2;
+  R tp = at(m, L, MC_LB1 + j);
+  if (tp > R(0)) return fmin(tp / elastic_ratio, R(kEhsPathMax));
+  return R(kEhsPathMax);
+}
+template <class R>
+__device__ __forceinline__ R ehs_path(const Med<R>& m, R K, R mass, R elastic_ratio) {
+  Loc<R> L = locate(m, K);
+  if (m.nm == 1) return ehs_single(m, 0, K, L, mass, elastic_ratio);
+  R inv = R(0);
+  for (int j = 0; j < m.nm; ++j) {
+    R lp = ehs_single(m, j, K, L, mass, elastic_ratio);
+    if (lp > R(0) && lp < R(kEhsPathMax)) inv += m.frac[j] / lp;
+  }
+  return inv > R(0) ? R(1) / inv : R(kEhsPathMax);
+}
+
+// ------------------------------------------------------------ MIXED kernel
+// searchsortedlast lookup (src/MixedTransport.jl:43-49); values outside the
+// table set the domain bits (the reference throws DomainError there).
+template <class R>
+struct KLoc {
+  int i, edge;
+  R f;
+};
+template <class R>
+__device__ __forceinline__ KLoc<R> klocate(const R* xs, int n, R x, int* status) {
+  KLoc<R> L{0, 0, R(0)};
+  if (x < xs[0]) {
+    *status |= ST_DOMAIN_LO;
+    L.edge = -1;
+    return L;
+  }
+  if (x > xs[n - 1]) {
+    *status |= ST_DOMAIN_HI;
+    L.edge = 1;
+    return L;
+  }
+  int lo = 0, hi = n;  // first index with xs[idx] > x
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (xs[mid] <= x) lo = mid + 1; else hi = mid;
+  }
+  int i = (lo < 1 ? 1 : (lo > n - 1 ? n - 1 : lo)) - 1;
+  R d = xs[i + 1] - xs[i];
+  L.i = i;
+  L.f = d == R(0) ? R(0) : (x - xs[i]) / d;
+  return L;
+}
+template <class R>
+__device__ __forceinline__ R kat(const R* ys, int n, const KLoc<R>& L) {
+  if (L.edge < 0) return ys[0];
+  if (L.edge > 0) return ys[n - 1];
+  return ys[L.i] + L.f * (ys[L.i + 1] - ys[L.i]);
+}
+template <class R>
+__device__ __forceinline__ R klookup(const Med<R>& m, int xcol, int ycol, R x, int* status) {
+  return kat(m.kcol(ycol), m.nk, klocate(m.kcol(xcol), m.nk, x, status));
+}
+
+// Sum over elements and processes of f * dsigma/dq (src/MixedTransport.jl:99-106).
+// pick < 0: total; else the component index whose running sum first exceeds
+// u (returned in *which, total in the return value is then meaningless).
+__device__ __noinline__ double del_total(const double* el, int nel, double mass, double anc,
+                                         double q) {
+  double total = 0.0;
+  for (int e = 0; e < nel; ++e) {
+    const double* x = el + kElStride * e;
+    double f = x[3] * kAvogadro / (x[1] * 0.001) * anc;
+    total += f * dcs_brems(x[0], x[1], mass, anc, q);
+    total += f * dcs_pair(x[0], x[1], mass, anc, q);
+    total += f * dcs_photo(x[0], x[1], mass, anc, q);
+    total += f * dcs_ionisation(x[0], x[2], mass, anc, q);
+  }
+  return total;
+}
+__device__ __noinline__ int del_pick(const double* el, int nel, double mass, double anc, double q,
+                                     double u) {
+  int last = 4 * nel - 1;
+  for (int i = 0; i <= last; ++i) {
+    const double* x = el + kElStride * (i / 4);
+    double f = x[3] * kAvogadro / (x[1] * 0.001) * anc;
+    int p = i % 4;
+    double v = p == 0 ? dcs_brems(x[0], x[1], mass, anc, q)
+               : p == 1 ? dcs_pair(x[0], x[1], mass, anc, q)
+               : p == 2 ? dcs_photo(x[0], x[1], mass, anc, q)
+                        : dcs_ionisation(x[0], x[2], mass, anc, q);
+    u -= f * v;
+    if (u <= 0.0) return i;
+  }
+  return last;
+}
+
+struct DelOut {
+  double energy, weight;
+  int process, element;  // process 0: null CEL event
+};
+// reverse_del_event (src/MixedTransport.jl:111-142).
+template <class R>
+__device__ __noinline__ DelOut reverse_del(const Med<R>& m, const Consts& C, double k, Stream& g,
+                                           bool details, int* status) {
+  DelOut r{k, 1.0, 0, -1};
+  double sigma = double(klookup(m, K_E, K_SIG, R(k), status));
+  if (!(sigma > 0.0)) {
+    *status |= ST_ZERO_RATE;
+    return r;
+  }
+  double onset = double(m.onset), cut = C.cutoff;
+  double pcel = k >= onset ? 0.0 : -log(cut) / (-log(cut) + log(onset / (onset - k)));
+  if (pcel > 0.0 && uni_d(g) < pcel) {
+    r.weight = 1.0 / pcel;
+    return r;
+  }
+  const double me = kElectronMass, M = C.mass;
+  double xmax = k < 0.5 * (M - me) * (M - me) / me
+                    ? fmin(1.0, 2.0 * me * (k + 2.0 * M) / ((M + me) * (M + me)))
+                    : 1.0;
+  double xmin = k >= onset * (1.0 - cut) ? cut : 1.0 - k / onset;
+  if (!(xmax > xmin)) return r;
+  double invnorm = 1.0 / xmin - 1.0 / xmax;
+  double nu = 1.0 / (1.0 / xmin - uni_d(g) * invnorm);
+  double rr = 1.0 - nu, anc = k / rr, pdf = 1.0 / (invnorm * nu * nu);
+  double total = del_total(m.el, m.nel, M, anc, anc - k);
+  r.energy = anc;
+  r.weight = total / (pdf * rr * sigma * (1.0 - pcel));
+  if (details) {
+    if (total <= 0.0) return r;
+    double u = uni_d(g) * total;
+    int i = del_pick(m.el, m.nel, M, anc, anc - k, u);
+    r.process = i % 4 + 1;
+    r.element = i / 4;
+  }
+  return r;
+}
+
+// Mutable part of a history.
+template <class R>
+struct State {
+  double x, y, z;
+  R ux, uy, uz, E, w;
+  int status;
+};
+
+// transport_mixed_step (src/MixedTransport.jl:144-200).  The grammage
+// bookkeeping (requested, remaining, travelled) is FP64 in both precisions:
+// in FP32 the reference's round-off floor eps(max(1, grammage)) would exceed
+// the grammage of the 1e-7 m boundary-crossing steps.
+template <class R>
+__device__ void mixed_step(const Med<R>& m, const Consts& C, State<R>& s, double density,
+                           double distance, Stream& g, R energy_limit) {
+  const int nk = m.nk;
+  const R* kE = m.kcol(K_E);
+  R k = s.E;
+  const R Emax = kE[nk - 1];
+  double remaining = distance * density, travelled = 0.0;
+  R weight = s.w;
+  R ceiling = energy_limit > R(0) ? fmin(energy_limit, Emax) : Emax;
+  if (s.E > Emax) {
+    s.status |= ST_DOMAIN_HI;
+    return;
+  }
+  const R mass = R(C.mass), ctau = R(C.ctau), rdens = R(density);
+  bool exhausted = true;
+  const double dXreq = fmax(1.0, distance * density);
+  const double tol = ulp_up(dXreq);
+  for (int event = 0; event < 100000; ++event) {
+    if (remaining <= tol || k >= ceiling) {
+      exhausted = false;
+      break;
+    }
+    KLoc<R> Lk = klocate(kE, nk, k, &s.status);
+    R ri = kat(m.kcol(K_R), nk, Lk), hi = kat(m.kcol(K_H), nk, Lk);
+    R rtc = fmax(R(0), klookup(m, K_E, K_R, ceiling, &s.status) - ri);
+    double eg = fmin(remaining, double(rtc));
+    R endpoint = eg == double(rtc) ? ceiling
+                                   : fmax(k, klookup(m, K_R, K_E, R(double(ri) + eg), &s.status));
+    R eventh = hi + expo<R>(g);
+    bool occurs = eventh < klookup(m, K_E, K_H, endpoint, &s.status);
+    R pre = occurs ? fmax(k, klookup(m, K_H, K_E, eventh, &s.status)) : endpoint;
+    KLoc<R> Lp = klocate(kE, nk, pre, &s.status);
+    double dxd = occurs ? double(fmax(R(0), kat(m.kcol(K_R), nk, Lp) - ri)) : eg;
+    R dx = R(dxd);
+    R dt;
+    if (dx <= R(8) * ulp_up(fabs(ri)) || pre - k <= R(8) * ulp_up(fabs(k)))
+      dt = R(dxd / density) * mass / R(2) *
+           (R(1) / sqrt(k * (k + R(2) * mass)) + R(1) / sqrt(pre * (pre + R(2) * mass)));
+    else
+      dt = (kat(m.kcol(K_T), nk, Lp) - kat(m.kcol(K_T), nk, Lk)) / rdens;
+    weight *= kat(m.kcol(K_S), nk, Lp) / kat(m.kcol(K_S), nk, Lk) * exp(-dt / ctau);
+    travelled += dxd;
+    remaining = fmax(0.0, remaining - dxd);
+    k = pre;
+    if (occurs) {
+      DelOut d = reverse_del(m, C, double(k), g, false, &s.status);
+      k = R(d.energy);
+      weight = R(double(weight) * d.weight);
+      if (!(isfinite(weight) && weight >= R(0))) s.status |= ST_BAD_WEIGHT;
+      if (weight == R(0)) {
+        exhausted = false;
+        break;
+      }
+    } else {
+      exhausted = false;
+      break;
+    }
+  }
+  if (exhausted) s.status |= ST_EVENT_CAP;
+  if (weight > R(0) && k >= Emax && remaining > tol && (energy_limit < R(0) || k < energy_limit))
+    s.status |= ST_DOMAIN_HI;
+  double d = travelled / density;
+  s.E = k;
+  s.w = weight;
+  s.x -= d * double(s.ux);
+  s.y -= d * double(s.uy);
+  s.z -= d * double(s.uz);
+}
+
+// ------------------------------------------------------------ straggling
+template <class R>
+__device__ __forceinline__ R box_muller(Stream& g) {
+  R r = sqrt(R(-2) * log(uni<R>(g)));
+  R phi = R(2) * R(kPi) * uni<R>(g);
+  return r * sin(phi);
+}
+template <class R>
+__device__ __forceinline__ R truncated_randn(Stream& g) {
+  R u = box_muller<R>(g);
+  for (int it = 0; it < 1000 && fabs(u) > R(3); ++it) u = box_muller<R>(g);
+  return u * R(0.9848416472);
+}
+
+// fluctuate_energy_loss, backward (src/Straggling.jl:103-173, :1046-1105).
+template <class R>
+__device__ R fluctuate(const Med<R>& m, R ki, const Loc<R>& Li, R dX, R Xtot, Stream& g,
+                       R* ratio_out) {
+  R k1 = inv_range(m, MC_MR, Xtot + dX);
+  R dk0 = fabs(ki - k1), ratio = R(1);
+  if (k1 > R(0) && dk0 > R(0)) {
+    Loc<R> L1 = locate(m, k1);
+    R O0 = at(m, Li, MC_STRAG), O1 = at(m, L1, MC_STRAG);
+    R dk12 = R(0.5) * dX * (O0 + O1);
+    if (dX / Xtot > R(0.05)) {
+      R de1 = at(m, L1, MC_MS), de0 = at(m, Li, MC_MS);
+      dk12 *= R(1) - dX / dk0 * (de1 - de0);
+    }
+    R dk1 = sqrt(fmax(dk12, R(0)));
+    if (dk0 >= R(3) * dk1 && dk1 > R(0)) {
+      k1 += truncated_randn<R>(g) * dk1;
+    } else if (dk0 >= R(1.7320508) * dk1 && dk1 > R(0)) {
+      k1 += R(1.7320508) * (R(1) - R(2) * uni<R>(g)) * dk1;
+    } else if (dk1 > R(0)) {
+      R dk32 = R(3) * dk12, dk02 = dk0 * dk0;
+      R a = R(1) - (dk32 - dk02) / (dk32 + R(3) * dk02);
+      if (uni<R>(g) <= a) {
+        R b = R(0.5) * (dk32 + R(3) * dk02) / dk0;
+        k1 = ki + b * uni<R>(g);
+        if (k1 < R(0)) k1 = R(0);
+      } else {
+        k1 = ki;
+      }
+    }
+    ratio = fabs(ki - k1) / dk0;
+  }
+  if (ratio == R(0)) ratio = R(1);
+  *ratio_out = ratio;
+  return fmax(k1, R(0));
+}
+
+// sample_ehs_event, backward (src/Straggling.jl:373-434, :1284-1334).
+template <class R>
+__device__ bool ehs_event(const Med<R>& m, R ki, R kf, R dX, R Xtot, R ratio, Stream& g, R mass,
+                          R eratio, R* X_ehs, R* k_ehs) {
+  R kmin = fmin(ki, kf), kmax = fmax(ki, kf);
+  if (kmin < R(0.001)) {
+    R t = kmin;
+    kmin = kmax;
+    kmax = t;
+  }
+  R lb = ehs_path(m, kmin, mass, eratio);
+  if (lb <= R(0) || lb >= R(kEhsPathMax)) return false;
+  R zeta = uni<R>(g);
+  if (zeta <= R(0) || zeta >= R(1)) return false;
+  R X = -log(zeta) * lb;
+  if (X >= dX) return false;
+  R kh = inv_range(m, MC_MR, Xtot + X);
+  R k = ki + ratio * fabs(ki - kh);
+  if (k <= R(0)) return false;
+  R lbk = ehs_path(m, k, mass, eratio);
+  if (lbk <= R(0) || lbk >= R(kEhsPathMax)) return false;
+  R r = lbk / lb;
+  if (r <= R(0) || uni<R>(g) > R(1) / r) return false;
+  *X_ehs = X;
+  *k_ehs = k;
+  return true;
+}
+
+// sample_scattering_angle (src/Straggling.jl:446-517, :1344-1405), FP64.
+template <class R>
+__device__ __noinline__ double scattering_angle(const Med<R>& m, double mass, double K,
+                                                Stream& g) {
+  Loc<R> L = locate(m, R(K));
+  double p2 = K * (K + 2.0 * mass);
+  double mu0 = fmax(double(at(m, L, MC_MU0)), 1e-12);
+  double zoa = double(m.ZoA);
+  double At = zoa > 0.0 ? 1.0 / zoa : 22.0, Mt = At * kNeutronMass;
+  double s = mass * mass + Mt * Mt + 2.0 * (K + mass) * Mt;
+  double K0 = (s - (mass + Mt) * (mass + Mt)) / (2.0 * sqrt(s));
+  double Ecm = K0 + mass, pcm = sqrt(fmax(K0 * (K0 + 2.0 * mass), 0.0));
+  double El = K + mass, pl = sqrt(fmax(p2, 0.0));
+  double gCM = (pl > 0.0 && pcm > 0.0) ? (El * Ecm + pl * pcm) / (mass * sqrt(s)) : 1.0;
+  double tau = (pl > 0.0 && pcm > 0.0) ? (El * pcm - Ecm * pl) / (pl * pcm) : 0.0;
+  double A = mu0 / 4.0, fs = double(at(m, L, MC_FSPIN));
+  double Apm = A + mu0, Ap1 = A + 1.0, omm = 1.0 - mu0, mu1 = mu0;
+  for (int it = 0; it < 100; ++it) {
+    double zeta = uni_d(g);
+    double tmp = Ap1 - zeta * omm;
+    if (tmp <= 0.0) continue;
+    double tr = fmin(fmax(Apm * Ap1 / tmp - A, mu0), 1.0);
+    if (uni_d(g) <= 1.0 - fs * tr) {
+      mu1 = tr;
+      break;
+    }
+  }
+  double mu;
+  if (mu1 > 1e-6) {
+    double a = gCM * (tau + 1.0 - 2.0 * mu1);
+    double ct = a / sqrt(4.0 * mu1 * (1.0 - mu1) + a * a);
+    mu = 0.5 * (1.0 - ct);
+  } else {
+    double d = gCM * (1.0 + tau);
+    mu = mu1 / (d * d);
+  }
+  return fmin(fmax(mu, 0.0), 1.0);
+}
+
+// sample_soft_scattering (src/Straggling.jl:539-590, :1204-1253).
+template <class R>
+__device__ R soft_scattering(const Med<R>& m, const Loc<R>& L0, R k1, R step, R density,
+                             Stream& g) {
+  if (step <= R(0) || density <= R(0)) return R(0);
+  R lb0 = transport_path(m, L0);
+  R inv0 = lb0 > R(0) ? density / lb0 : R(0), inv1;
+  if (k1 > R(0)) {
+    R lb1 = transport_path(m, locate(m, k1));
+    inv1 = lb1 > R(0) ? density / lb1 : R(0);
+  } else {
+    inv1 = inv0;
+  }
+  if (inv0 <= R(0) && inv1 <= R(0)) return R(0);
+  R ilb1 = R(0.25) * step * (inv0 + inv1);
+  if (ilb1 < R(1e-12)) return R(0);
+  if (ilb1 > R(1)) ilb1 = R(1);
+  for (int it = 0; it < 1000; ++it) {
+    R u = uni<R>(g);
+    if (!(u > R(0))) continue;
+    R mu = -ilb1 * log(u);
+    if (mu <= R(1)) return fmax(mu, R(0));
+  }
+  return ilb1;
+}
+
+// rotate_direction (src/Straggling.jl:645-710).
+template <class R>
+__device__ void rotate(State<R>& s, R mu, Stream& g) {
+  R ct = R(1) - R(2) * mu, st2 = R(4) * mu * (R(1) - mu);
+  if (st2 <= R(0)) return;
+  R st = sqrt(st2), d0 = s.ux, d1 = s.uy, d2 = s.uz;
+  R ax = fabs(d0), ay = fabs(d1), az = fabs(d2);
+  R u0x = R(0), u0y = R(0), u0z = R(0);
+  if (ax > ay) {
+    if (ax > az) {
+      R nrm = R(1) / sqrt(d0 * d0 + d2 * d2);
+      u0x = -d2 * nrm;
+      u0z = d0 * nrm;
+    } else {
+      R nrm = R(1) / sqrt(d1 * d1 + d2 * d2);
+      u0y = d2 * nrm;
+      u0z = -d1 * nrm;
+    }
+  } else {
+    if (ay > az) {
+      R nrm = R(1) / sqrt(d0 * d0 + d1 * d1);
+      u0x = d1 * nrm;
+      u0y = -d0 * nrm;
+    } else {
+      R nrm = R(1) / sqrt(d1 * d1 + d2 * d2);
+      u0y = d2 * nrm;
+      u0z = -d1 * nrm;
+    }
+  }
+  R u1x = u0y * d2 - u0z * d1, u1y = u0z * d0 - u0x * d2, u1z = u0x * d1 - u0y * d0;
+  R cp, sp;
+  sincospi(R(1) - R(2) * uni<R>(g), &sp, &cp);
+  R nx = ct * d0 + st * (cp * u0x + sp * u1x);
+  R ny = ct * d1 + st * (cp * u0y + sp * u1y);
+  R nz = ct * d2 + st * (cp * u0z + sp * u1z);
+  R nrm = sqrt(nx * nx + ny * ny + nz * nz);
+  if (nrm > R(0)) {
+    nx /= nrm;
+    ny /= nrm;
+    nz /= nrm;
+  }
+  s.ux = nx;
+  s.uy = ny;
+  s.uz = nz;
+}
+
+// DEL polar angles, FP64 (src/Straggling.jl:746-914).
+__device__ __noinline__ double polar_brems(double m, double ki, double kf, double RN, Stream& g) {
+  double E = ki + m, nu = ki - kf;
+  if (nu <= 0.0 || E <= m) return 0.0;
+  double y = nu / E, tmp = 0.5 * m * nu / (E * (E - nu)), mu0 = tmp * tmp;
+  double c1 = (2.0 * (1.0 - y) + y * y) * mu0, c2 = 4.0 * (1.0 - y) * mu0 * mu0;
+  double t2 = m * RN / kHbarC, muni = t2 * t2 / 6.0;
+  if (sqrt(mu0) - mu0 < 0.0) return 0.0;
+  double q0 = muni, r0 = mu0, qr0 = q0 * r0, den0 = r0 + qr0;
+  if (den0 <= 0.0 || (1.0 + qr0) <= 0.0) return 0.0;
+  double x0 = (1.0 + 2.0 * qr0) * log((1.0 + qr0) / den0) - (1.0 - r0) * (1.0 + 2.0 * q0) / (1.0 + q0);
+  if (x0 <= 0.0) return 0.0;
+  for (int it = 0; it < 100; ++it) {
+    double r0r = uni_d(g), r1 = uni_d(g);
+    double mu = r0r * mu0 / (mu0 + 1.0 - r0r);
+    double mus = mu0 + mu, mu2 = mus * mus, d1 = 1.0 / mu2, d2 = d1 * d1;
+    double score = r1 * c1 * d1, pdf = c1 * d1 - mu * c2 * d2;
+    if (score > pdf) continue;
+    double l2 = mu2 / (mu0 * mu0), q = muni * l2, r = mu0 * l2, qr = q * r;
+    if (qr > 1e5) continue;
+    double den = r + qr;
+    if (den <= 0.0 || (1.0 + qr) <= 0.0) continue;
+    double x = (1.0 + 2.0 * qr) * log((1.0 + qr) / den) - (1.0 - r) * (1.0 + 2.0 * q) / (1.0 + q);
+    pdf *= x / x0;
+    if (score <= pdf) return mu;
+  }
+  return 0.0;
+}
+__device__ __noinline__ double polar_photo(double ml, double ki, double kf, Stream& g) {
+  double M = 0.5 * (kProtonMass + kNeutronMass), q = ki - kf, E = ki + ml, ml2 = ml * ml;
+  double Q2min = ml2 * (q * q - 0.5 * ml2) / (E * (E - q));
+  double Q2max = 2.0 * M * (q - kPionMass) - kPionMass * kPionMass;
+  if (Q2max < Q2min || Q2min < 0.0) return 0.0;
+  double rQ2 = log(Q2max) - log(Q2min);
+  double Q2 = Q2min * exp(rQ2 * uni_d(g));
+  double p = sqrt(ki * (ki + 2.0 * ml)), E1 = E - q, er = ml / E1;
+  double p1 = E1 * sqrt(fmax((1.0 + er) * (1.0 - er), 0.0)), p2 = p * p1;
+  if (p2 <= 0.0) return 0.0;
+  double tv = p2 + ml2 - E * E1;
+  if (fabs(tv) <= 3.0 * kEps64 * p2) tv = 0.0;
+  double mu = 0.5 * tv / p2 + 0.25 / p2 * Q2;
+  return fmin(fmax(mu, 0.0), 1.0);
+}
+__device__ __forceinline__ double polar_ioni(double m, double ki, double kf) {
+  double nu = ki - kf, p2 = ki * (ki + 2.0 * m), E = ki + m;
+  double den = sqrt(p2 * (p2 + nu * nu - 2.0 * nu * E));
+  if (den <= 0.0) return 0.0;
+  double c = (p2 - nu * (E + kElectronMass)) / den;
+  return 0.5 * (1.0 - c);
+}
+
+// transport_backward_step_full, mode :straggled (src/Geometry.jl:148-357).
+template <class R>
+__device__ void straggled_step(const Med<R>& m, const Consts& C, State<R>& s, const Loc<R>& Li,
+                               R density, double step, Stream& g, bool scattering, R energy_limit) {
+  const R mass = R(C.mass), eratio = R(C.elastic_ratio);
+  R ki = s.E, dX = R(step) * density;
+  bool shortened = false;  // the step ended before its requested length
+  R Xi = at(m, Li, MC_MR);
+  R kf = ki, ratio = R(1);
+  if (ki > R(0.001)) {
+    kf = fluctuate(m, ki, Li, dX, Xi, g, &ratio);
+    kf = fmax(kf, ki);
+  } else {
+    kf = inv_range(m, MC_MR, Xi + dX);
+  }
+  if (energy_limit > R(0) && kf >= energy_limit) {
+    R dk = fabs(ki - kf);
+    if (dk > R(0)) {
+      dX = dX * (fabs(energy_limit - ki) / dk);
+      kf = energy_limit;
+      shortened = true;
+    }
+  }
+  bool del = false, ehs = false;
+  R X_del = R(CUDART_INF), k_del = R(0), X_ehs = R(CUDART_INF), k_ehs = R(0);
+  R rate = fmax(klookup(m, K_E, K_SIG, ki, &s.status), klookup(m, K_E, K_SIG, kf, &s.status));
+  if (rate > R(0)) {
+    R cand = expo<R>(g) / rate;
+    if (cand < dX) {
+      R kh = inv_range(m, MC_MR, Xi + cand);
+      R pre = ki + ratio * fabs(kh - ki);
+      if (pre > R(0) && uni<R>(g) <= klookup(m, K_E, K_SIG, pre, &s.status) / rate) {
+        del = true;
+        X_del = cand;
+        k_del = pre;
+      }
+    }
+  }
+  if (scattering) {
+    R X, k;
+    if (ehs_event(m, ki, kf, dX, Xi, ratio, g, mass, eratio, &X, &k) && k > R(0)) {
+      ehs = true;
+      X_ehs = X;
+      k_ehs = k;
+    }
+  }
+  if (del && ehs) {
+    if (X_del <= X_ehs) ehs = false;
+    else del = false;
+  }
+  double dw = 1.0;
+  R ckf = kf;
+  int proc = 0, elem = -1;
+  if (del) {
+    ckf = k_del;
+    DelOut d = reverse_del(m, C, double(k_del), g, true, &s.status);
+    kf = R(d.energy);
+    dw = d.weight;
+    proc = d.process;
+    elem = d.element;
+    dX = X_del;
+    shortened = true;
+  }
+  if (ehs) {
+    kf = k_ehs;
+    ckf = k_ehs;
+    dX = X_ehs;
+    shortened = true;
+  }
+  R astep = dX / density;
+  R ox = s.ux, oy = s.uy, oz = s.uz;  // the position moves along the incoming direction
+  if (scattering) {
+    if (del && proc > 0) {
+      const double* e = m.el + kElStride * elem;
+      double mu = proc == 1 || proc == 2 ? polar_brems(C.mass, double(kf), double(ckf), e[4], g)
+                  : proc == 3            ? polar_photo(C.mass, double(kf), double(ckf), g)
+                                         : polar_ioni(C.mass, double(kf), double(ckf));
+      if (mu > 0.0) rotate(s, R(mu), g);
+    }
+    if (ehs) {
+      double mu = scattering_angle(m, C.mass, double(k_ehs), g);
+      if (mu > 0.0) rotate(s, R(mu), g);
+    }
+    R mu = soft_scattering(m, Li, ckf, astep, density, g);
+    if (mu > R(0)) rotate(s, mu, g);
+  }
+  R pt = astep * mass / R(2) *
+         (R(1) / sqrt(ki * (ki + R(2) * mass)) + R(1) / sqrt(ckf * (ckf + R(2) * mass)));
+  // FP64: the reference's dX/density; FP32: the requested FP64 step unless
+  // an event or the energy limit shortened it
+  double da = double(astep);
+  if (sizeof(R) == 4) da = shortened ? double(dX) / double(density) : step;
+  s.x -= da * double(ox);
+  s.y -= da * double(oy);
+  s.z -= da * double(oz);
+  R wf = at(m, locate(m, ckf), MC_MS) / at(m, Li, MC_MS);
+  s.w = R(double(s.w * wf * exp(-pt / R(C.ctau))) * dw);
+  s.E = kf;
+}
+
+// Deterministic CSDA step on a medium (src/Geometry.jl:424-457).
+template <class R>
+__device__ __forceinline__ void csda_step(const Med<R>& m, const Consts& C, State<R>& s,
+                                          const Loc<R>& Li, R density, double step_d) {
+  const R mass = R(C.mass), step = R(step_d);
+  R ki = s.E, dX = step * density;
+  R kf = inv_range(m, MC_CR, at(m, Li, MC_CR) + dX);
+  R gm = (R(1) + ki / mass + R(1) + kf / mass) / R(2);
+  R b = sqrt(fmax(R(1) - R(1) / (gm * gm), R(1e-12)));
+  R dt = step / (b * gm);
+  double ds = step_d;
+  s.x -= ds * double(s.ux);
+  s.y -= ds * double(s.uy);
+  s.z -= ds * double(s.uz);
+  s.w = s.w * (at(m, locate(m, kf), MC_CS) / at(m, Li, MC_CS)) * exp(-dt / R(C.ctau));
+  s.E = kf;
+}
+
+// One history in flight: the state plus its position in the dual-mode loop
+// of src/Geometry.jl:534-672, flattened so that a thread can refill itself
+// with a new history as soon as the current one ends.
+template <class R>
+struct Hist {
+  State<R> s;
+  double limit;  // energy limit of the current mode (exactly representable in R)
+  double thick, rho, H, q, ws;
+  int steps, inner, outer;
+  bool need_mode, strag, mixed, scat;
+};
+
+// Advances a history by one transport step.  Returns true when it has ended.
+template <class R>
+__device__ __forceinline__ bool advance(const Med<R>& rock, const Med<R>& air, const Consts& C,
+                                        Hist<R>& h, Stream& g) {
+  const double eps = kEps64;
+  State<R>& s = h.s;
+  for (int guard = 0; guard < 4; ++guard) {
+    if (h.need_mode) {
+      if (!(double(s.E) < C.thr - eps)) return true;
+      if (h.outer >= 1000) {
+        s.status |= ST_OUTER_CAP;
+        return true;
+      }
+      if (s.z < 0.0 || s.z >= h.H - eps) return true;
+      if (!(s.w > R(0)) || !isfinite(s.w)) return true;
+      if (double(s.E) < C.thr_low - eps) {
+        h.strag = C.straggling != 0;
+        h.mixed = false;
+        h.scat = C.scattering != 0;
+        h.limit = fmin(C.thr_low, C.thr);
+      } else {
+        h.strag = false;
+        h.mixed = C.straggling != 0;
+        h.scat = false;
+        h.limit = C.thr;
+      }
+      h.inner = 0;
+      ++h.outer;
+      h.need_mode = false;
+    }
+    if (h.inner >= 50000 || s.z < 0.0 || s.z >= h.H - eps || double(s.E) >= h.limit - eps ||
+        !(s.w > R(0)) || !isfinite(s.w)) {
+      h.need_mode = true;
+      continue;
+    }
+    // medium, boundary distance and step (src/Geometry.jl:603-650, :461-476)
+    double uz = -double(s.uz);
+    bool in_air = s.z >= h.thick;
+    const Med<R>& m = in_air ? air : rock;
+    double dens, tob;
+    if (!in_air) {
+      dens = h.rho;
+      tob = uz > eps ? (h.thick - s.z) / uz : uz < -eps ? (0.0 - s.z) / uz : 1000.0;
+    } else {
+      dens = 1.205 * exp(-s.z / 12e3);
+      tob = uz > eps ? (h.H - s.z) / uz : uz < -eps ? (h.thick - s.z) / uz : 1000.0;
+    }
+    const R rd = R(dens);
+    Loc<R> Li = locate(m, s.E);
+    R Xi = at(m, Li, MC_CR);
+    R lim = R(0.01) * Xi / fmax(rd, R(1e-6));
+    if (h.scat) {
+      R lb1 = transport_path(m, Li);
+      if (lb1 > R(0) && rd > R(0)) lim = fmin(lim, R(0.01) * lb1 / rd);
+    }
+    if (in_air) lim = fmin(lim, R(0.05 * 12e3) / fmax(R(fabs(uz)), R(0.05)));
+    double step = fmin(tob + 1e-7, double(lim));
+    step = fmin(fmax(step, kStepMin), 1000.0);
+    if (h.strag) straggled_step(m, C, s, Li, rd, step, g, h.scat, R(h.limit));
+    else if (h.mixed) mixed_step(m, C, s, dens, step, g, R(h.limit));
+    else csda_step(m, C, s, Li, rd, step);
+    ++h.inner;
+    if (++h.steps > 2000000) s.status |= ST_STEP_CAP;
+    return (s.status & ST_FATAL) != 0;
+  }
+  // The mode checks alternate without a step only if the thresholds were not
+  // representable in R (the host rounds them); end the history flagged.
+  s.status |= ST_OUTER_CAP;
+  return true;
+}
+
+// Contribution of an ended history (src/Geometry.jl:729-757), FP64.
+template <class R>
+__device__ __forceinline__ double history_flux(const Consts& C, const Hist<R>& h) {
+  const State<R>& s = h.s;
+  if (s.status & ST_FATAL) return 0.0;
+  if (s.z >= h.H - 1.0 && double(s.E) < C.thr) {
+    double c = fmin(fmax(-double(s.uz), 0.0), 1.0);
+    if (c <= 0.0) return 0.0;
+    double cs = cos_theta_star(c);
+    return double(s.w) * gccly_flux(cs, pow(cs, 1.29), double(s.E), h.q, nullptr);
+  }
+  return 0.0;
+}
+
+}  // namespace mc
+}  // namespace dp

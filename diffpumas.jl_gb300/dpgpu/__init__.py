@@ -14,9 +14,10 @@ from collections import namedtuple
 import numpy as np
 
 from . import _lib
-from ._lib import (COLUMNS, DpElement, DpGrid, DpMaterial, DpMcParams, DpMcResult, DpRay,
-                   DpSettings, DpTomoParams, check, load)
+from ._lib import (COLUMNS, DpElement, DpGrid, DpLos, DpLosResult, DpMaterial, DpMcConfig,
+                   DpMcParams, DpMcResult, DpRay, DpSettings, DpTomoParams, check, load)
 
+PRECISION = {"fp64": 0, "mixed": 1}
 MUON_MASS = 0.10565839
 MUON_C_TAU = 658.654
 PRIMARY_ALTITUDE = 3e4
@@ -202,7 +203,7 @@ MCResult = namedtuple("MCResult", "flux sigma gradient gradient_flux gradient_me
 
 def _mc_params(physics, rock_thickness, rock_density, elevation, energy_min, energy_max,
                n_samples, compute_gradient, seed, straggling, scattering,
-               energy_threshold_low, source_energy_max, primary_altitude):
+               energy_threshold_low, source_energy_max, primary_altitude, precision="fp64"):
     rock = physics.materials.get("StandardRock", 0)
     air = physics.materials.get("Air", physics.n_materials - 1)
     return DpMcParams(float(rock_thickness), float(rock_density), float(elevation),
@@ -211,18 +212,20 @@ def _mc_params(physics, rock_thickness, rock_density, elevation, energy_min, ene
                       int(bool(scattering)), int(bool(compute_gradient)),
                       float(energy_threshold_low),
                       float(source_energy_max) if source_energy_max is not None else 0.0,
-                      float(primary_altitude), rock, air)
+                      float(primary_altitude), rock, air, PRECISION[precision])
 
 
 def run_backward_mc(physics, *, rock_thickness=100.0, rock_density=2650.0, elevation=45.0,
                     energy_min=1.0, energy_max=None, n_samples=10000, compute_gradient=False,
                     seed=42, straggling=True, scattering=True, energy_threshold_low=100.0,
-                    source_energy_max=None, primary_altitude=PRIMARY_ALTITUDE):
+                    source_energy_max=None, primary_altitude=PRIMARY_ALTITUDE,
+                    precision="fp64"):
     """run_backward_mc (src/Geometry.jl:1286-1338).  Samples are drawn from a
-    Philox stream keyed by (seed, sample id)."""
+    Philox stream keyed by (seed, sample id); straggling/scattering select the
+    stochastic dual-mode transport, else deterministic CSDA."""
     p = _mc_params(physics, rock_thickness, rock_density, elevation, energy_min, energy_max,
                    n_samples, compute_gradient, seed, straggling, scattering,
-                   energy_threshold_low, source_energy_max, primary_altitude)
+                   energy_threshold_low, source_energy_max, primary_altitude, precision)
     out = DpMcResult()
     check(load().dp_backward_mc(physics.ctx.h, physics.h, C.byref(p), C.byref(out)),
           physics.ctx.h)
@@ -275,6 +278,117 @@ def compute_flux_gradient(physics, rock_density, rock_thickness, elevation, ener
     return float(c[0]), float(d[0])
 
 
+# ----------------------------------------------------------------- stochastic MC
+class MaterialMixture:
+    """A prepared propagation medium: one material or a runtime mixture with
+    mass fractions (src/Types.jl:357-376), together with its MIXED transport
+    kernel (prepare_mixed_kernel, src/MixedTransport.jl:51-97).  materials
+    are 1-based indices like the reference's."""
+
+    def __init__(self, physics, materials, fractions=None):
+        mats = np.ascontiguousarray(np.atleast_1d(materials).astype(np.int32) - 1)
+        fr = _f64(np.ones(len(mats)) if fractions is None else np.atleast_1d(fractions))
+        self.physics = physics
+        self.h = C.c_void_p()
+        check(load().dp_mixture_prepare(physics.ctx.h, physics.h, len(mats), _ptr(mats), _ptr(fr),
+                                        C.byref(self.h)), physics.ctx.h)
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                load().dp_mixture_free(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    def kernel(self):
+        """The MIXED kernel columns: energies, stopping, sigma, range, hazard,
+        proper, and the onset energy."""
+        n, onset = C.c_int(), C.c_double()
+        load().dp_mixture_kernel(self.h, 0, None, 0, C.byref(n), C.byref(onset))
+        out = {}
+        for j, name in enumerate(("energies", "stopping", "sigma", "range", "hazard", "proper")):
+            a = np.zeros(n.value)
+            load().dp_mixture_kernel(self.h, j, _ptr(a), n.value, None, None)
+            out[name] = a
+        out["onset"] = onset.value
+        return out
+
+
+def prepare_mixed_kernel(physics, material):
+    """prepare_mixed_kernel (src/MixedTransport.jl:51-97) of a 1-based material
+    index or a MaterialMixture; returns the kernel columns."""
+    m = material if isinstance(material, MaterialMixture) else MaterialMixture(physics, material)
+    return m.kernel()
+
+
+def _mc_config(seed, straggling, scattering, energy_threshold_low, source_energy_max, precision):
+    return DpMcConfig(int(bool(straggling)), int(bool(scattering)), float(energy_threshold_low),
+                      float(source_energy_max) if source_energy_max is not None else 0.0,
+                      int(seed) & 0xFFFFFFFFFFFFFFFF, PRECISION[precision])
+
+
+def mc_histories(physics, rock, air, energy, charge, weight, *, thickness, density, elevation,
+                 primary_altitude=PRIMARY_ALTITUDE, seed=42, id0=0, straggling=True,
+                 scattering=True, energy_threshold_low=100.0, source_energy_max=None,
+                 precision="fp64"):
+    """Explicit stochastic histories (compute_flux_single with an rng,
+    src/Geometry.jl:694-757): per-history w*flux, status bits, step counts and
+    final states (n x 4: energy, altitude, u_z, transport weight).  Geometry
+    arguments are scalars or per-history arrays."""
+    E, q, w = _f64(energy), _f64(charge), _f64(weight)
+    n = len(E)
+    geo = [np.atleast_1d(_f64(v)) for v in (thickness, density, elevation, primary_altitude)]
+    stride = int(any(len(g) > 1 for g in geo))
+    if stride:
+        geo = [_f64(np.broadcast_to(g, (n,))) for g in geo]
+    c, Ef = np.zeros(n), np.zeros((n, 4))
+    st, ns = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    cfg = _mc_config(seed, straggling, scattering, energy_threshold_low, source_energy_max,
+                     precision)
+    check(load().dp_mc_histories(physics.ctx.h, physics.h, rock.h, air.h, C.byref(cfg), n, _ptr(E),
+                                 _ptr(q), _ptr(w), _ptr(geo[0]), _ptr(geo[1]), _ptr(geo[2]),
+                                 _ptr(geo[3]), stride, int(id0), _ptr(c), _ptr(st), _ptr(ns),
+                                 _ptr(Ef)), physics.ctx.h)
+    return c, st, ns, Ef
+
+
+LOS_FIELDS = ("thickness", "thickness_max", "density", "density_max", "elevation",
+              "elevation_max", "primary_altitude", "air_height", "energy_min", "energy_max",
+              "n_samples")
+
+
+def make_los(n_samples, *, thickness, density, elevation, energy_min, energy_max=None,
+             thickness_max=0.0, density_max=0.0, elevation_max=0.0,
+             primary_altitude=PRIMARY_ALTITUDE, air_height=0.0):
+    """Array of dp_los records (arguments are scalars or arrays of one length)."""
+    vals = dict(thickness=thickness, thickness_max=thickness_max, density=density,
+                density_max=density_max, elevation=elevation, elevation_max=elevation_max,
+                primary_altitude=primary_altitude, air_height=air_height, energy_min=energy_min,
+                energy_max=energy_min if energy_max is None else energy_max, n_samples=n_samples)
+    n = max(len(np.atleast_1d(v)) for v in vals.values())
+    arr = (DpLos * n)()
+    cols = {k: np.broadcast_to(np.atleast_1d(v), (n,)) for k, v in vals.items()}
+    for i in range(n):
+        for k in LOS_FIELDS:
+            setattr(arr[i], k, int(cols[k][i]) if k == "n_samples" else float(cols[k][i]))
+    return arr
+
+
+def backward_mc_batch(physics, los, *, rock, air, seed=42, straggling=True, scattering=True,
+                      energy_threshold_low=100.0, source_energy_max=None, precision="mixed"):
+    """Batched stochastic backward MC over lines of sight (one persistent
+    launch): per line of sight (flux, sigma, n_samples, n_status_nonzero)."""
+    n = len(los)
+    out = (DpLosResult * n)()
+    cfg = _mc_config(seed, straggling, scattering, energy_threshold_low, source_energy_max,
+                     precision)
+    check(load().dp_mc_los(physics.ctx.h, physics.h, rock.h, air.h, C.byref(cfg), n,
+                           C.cast(los, C.c_void_p), 0, C.cast(out, C.c_void_p)), physics.ctx.h)
+    return {k: np.array([getattr(r, k) for r in out]) for k in
+            ("flux", "sigma", "n_samples", "n_status_nonzero")}
+
+
 # ----------------------------------------------------------------- tomography
 def csda_energy_quadrature(n, energy_min, energy_max):
     """Log-midpoint nodes with charge 0 and half weights (src/Tomography.jl:263-274)."""
@@ -288,7 +402,6 @@ def csda_energy_quadrature(n, energy_min, energy_max):
     return E, np.zeros(n), 0.5 * E * span
 
 
-PRECISION = {"fp64": 0, "mixed": 1}
 
 
 class VoxelGrid:

@@ -40,13 +40,31 @@ class DpMcParams(C.Structure):
                 ("straggling", C.c_int), ("scattering", C.c_int),
                 ("compute_gradient", C.c_int), ("energy_threshold_low", C.c_double),
                 ("source_energy_max", C.c_double), ("primary_altitude", C.c_double),
-                ("rock_material", C.c_int), ("air_material", C.c_int)]
+                ("rock_material", C.c_int), ("air_material", C.c_int), ("precision", C.c_int)]
 
 
 class DpMcResult(C.Structure):
     _fields_ = [("flux", C.c_double), ("sigma", C.c_double), ("gradient", C.c_double),
                 ("gradient_flux", C.c_double), ("source_energy_max", C.c_double),
                 ("n_samples", C.c_long), ("n_status_nonzero", C.c_long)]
+
+
+class DpMcConfig(C.Structure):
+    _fields_ = [("straggling", C.c_int), ("scattering", C.c_int),
+                ("energy_threshold_low", C.c_double), ("source_energy_max", C.c_double),
+                ("seed", C.c_uint64), ("precision", C.c_int)]
+
+
+class DpLos(C.Structure):
+    _fields_ = [(k, C.c_double) for k in (
+        "thickness", "thickness_max", "density", "density_max", "elevation", "elevation_max",
+        "primary_altitude", "air_height", "energy_min", "energy_max")] + [("n_samples", C.c_long)]
+
+
+class DpLosResult(C.Structure):
+    _fields_ = [("flux", C.c_double), ("sigma", C.c_double), ("gradient", C.c_double),
+                ("gradient_flux", C.c_double), ("n_samples", C.c_long),
+                ("n_status_nonzero", C.c_long)]
 
 
 class DpGrid(C.Structure):
@@ -98,6 +116,13 @@ PROTOTYPES = {
     "dp_csda_flux_samples_dev": (_I, [_P, _P, C.POINTER(DpMcParams), _L, _VP, _VP, _VP, _VP,
                                       _VP, _VP]),
     "dp_mc_samples": (_I, [_P, C.POINTER(DpMcParams), _L, _VP, _VP, _VP]),
+    "dp_mixture_prepare": (_I, [_P, _P, _I, _VP, _VP, C.POINTER(_P)]),
+    "dp_mixture_free": (_I, [_P]),
+    "dp_mixture_kernel": (_I, [_P, _I, _VP, _I, C.POINTER(_I), C.POINTER(_D)]),
+    "dp_mc_histories": (_I, [_P, _P, _P, _P, C.POINTER(DpMcConfig), _L, _VP, _VP, _VP, _VP, _VP,
+                             _VP, _VP, _I, C.c_uint64, _VP, _VP, _VP, _VP]),
+    "dp_mc_los": (_I, [_P, _P, _P, _P, C.POINTER(DpMcConfig), _L, _VP, _I, _VP]),
+    "dp_mc_los_dev": (_I, [_P, _P, _P, _P, C.POINTER(DpMcConfig), _L, _VP, _L, _I, _VP]),
     "dp_tomo_forward": (_I, [_P, _P, C.POINTER(DpGrid), C.POINTER(DpTomoParams), _VP, _L, _VP,
                              _VP]),
     "dp_tomo_jacobian": (_I, [_P, _P, C.POINTER(DpGrid), C.POINTER(DpTomoParams), _VP, _L, _VP,

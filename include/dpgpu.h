@@ -34,16 +34,27 @@ extern "C" {
 
 /* Per-history status bits (MC kernels write one int32 per history when asked).
  * They map to the reference throw sites and loop caps:
- *   DP_ST_STEP_CAP   50000 inner steps (src/Geometry.jl:593)
- *   DP_ST_OUTER_CAP  outer mode loop cap (no reference counterpart; 10^6)
- *   DP_ST_EVENT_CAP  100000 hard events (src/MixedTransport.jl:157)
- *   DP_ST_DOMAIN_HI  energy above the prepared tables (src/MixedTransport.jl:45,155,196) */
+ *   DP_ST_STEP_CAP    2,000,000 transport steps (no reference counterpart: the
+ *                     reference loop is unbounded; src/Geometry.jl:553)
+ *   DP_ST_OUTER_CAP   1000 mode-loop passes (src/Geometry.jl:553 is unbounded)
+ *   DP_ST_EVENT_CAP   100000 hard events (src/MixedTransport.jl:157,193)
+ *   DP_ST_DOMAIN_HI   energy above the prepared tables (src/MixedTransport.jl:45,155,196)
+ *   DP_ST_DOMAIN_LO   energy below the prepared tables (src/MixedTransport.jl:44)
+ *   DP_ST_ZERO_RATE   non-positive hard-event rate (src/MixedTransport.jl:113)
+ *   DP_ST_BAD_WEIGHT  invalid adjoint hard-event weight (src/MixedTransport.jl:186)
+ *   DP_ST_TABLE_WAIT  a table-staging wait gave up (no reference counterpart)
+ * A history with any bit but DP_ST_OUTER_CAP contributes zero flux; the call
+ * then returns DP_ERR_DOMAIN (domain, rate, weight bits) or DP_ERR_STATE
+ * (caps), where the reference would throw. */
 #define DP_ST_OK 0
 #define DP_ST_STEP_CAP 1
 #define DP_ST_OUTER_CAP 2
 #define DP_ST_EVENT_CAP 4
 #define DP_ST_DOMAIN_HI 8
 #define DP_ST_DOMAIN_LO 16
+#define DP_ST_ZERO_RATE 32
+#define DP_ST_BAD_WEIGHT 64
+#define DP_ST_TABLE_WAIT 128
 
 typedef struct dp_ctx dp_ctx;
 typedef struct dp_physics dp_physics;
@@ -162,6 +173,8 @@ typedef struct {
   double primary_altitude;   /* m (3e4) */
   int rock_material;         /* -1: "StandardRock" or 0 */
   int air_material;          /* -1: "Air" or the last table */
+  int precision;             /* stochastic transport: DP_PREC_FP64 (0) or
+                                DP_PREC_MIXED (1); the CSDA path is FP64 */
 } dp_mc_params;
 
 typedef struct {
@@ -174,7 +187,11 @@ typedef struct {
 } dp_mc_result;
 
 /* Whole estimator: device sampling, transport, deterministic reduction.
- * CSDA mode only in this version (straggling = 0, scattering = 0). */
+ * straggling = scattering = 0: deterministic CSDA transport; otherwise the
+ * stochastic dual-mode transport (straggled with scattering below
+ * energy_threshold_low, mixed above, src/Geometry.jl:534-672) of the rock
+ * and air materials.  compute_gradient adds the CSDA sample-average gradient
+ * over the same samples (src/Geometry.jl:933-945). */
 int dp_backward_mc(dp_ctx* ctx, const dp_physics* phys, const dp_mc_params* p,
                    dp_mc_result* out);
 
@@ -194,6 +211,89 @@ int dp_csda_flux_samples_dev(dp_ctx* ctx, const dp_physics* phys, const dp_mc_pa
  * +-1 charge, weight 2*E*log(Emax/Emin)), for parity checks.  Host pointers. */
 int dp_mc_samples(dp_ctx* ctx, const dp_mc_params* p, long n, double* energy,
                   double* charge, double* weight);
+
+/* ------------------------------------------------------------------ stochastic MC
+ * Propagation medium: one material or a runtime mixture with mass fractions
+ * (MaterialMixture, src/Types.jl:357-376; mixture properties of
+ * src/Physics.jl:1058-1323), with its MIXED transport kernel
+ * (prepare_mixed_kernel, src/MixedTransport.jl:51-97: 8-fold refined log grid,
+ * restricted stopping power, hard-event rate regularised below its onset,
+ * cumulative range, hazard and proper-time integrals, elemental recipe).
+ * The materials must share the physics energy grid and carry recipes. */
+typedef struct dp_mixture dp_mixture;
+int dp_mixture_prepare(dp_ctx* ctx, const dp_physics* phys, int n_materials,
+                       const int* materials, const double* fractions, dp_mixture** out);
+int dp_mixture_free(dp_mixture* mix);
+/* Host copy of MIXED kernel column col (0 energy, 1 stopping power, 2 hard
+ * rate, 3 range, 4 hazard, 5 proper time) into out (up to cap values); *n
+ * receives the node count and *onset the hard-event onset energy. */
+int dp_mixture_kernel(const dp_mixture* mix, int col, double* out, int cap, int* n,
+                      double* onset);
+
+/* Options of a stochastic run (run_backward_mc kwargs, src/Geometry.jl:1286). */
+typedef struct {
+  int straggling;              /* 1: straggled below / mixed above the threshold */
+  int scattering;              /* 1: EHS, DEL angles and soft scattering below it */
+  double energy_threshold_low; /* GeV (100) */
+  double source_energy_max;    /* GeV; <= 0: min(1e9, table maximum) */
+  uint64_t seed;               /* Philox key: stream (seed, history id) */
+  int precision;               /* DP_PREC_FP64: the reference's FP64 operations;
+                                  DP_PREC_MIXED: FP32 transport, FP64 positions,
+                                  event kinematics, flux and tallies */
+} dp_mc_config;
+
+/* Explicit histories, the parity form of compute_flux_single with an rng
+ * (src/Geometry.jl:694-757) on a rock (mixture) layer under air: history i has
+ * final energy E[i], charge q[i], sampling weight w[i] and geometry
+ * thickness/density/elevation/primary_altitude[i] (index 0 for every history
+ * when geo_stride is 0); its random stream is (seed, id0 + i).  Outputs
+ * contrib[i] = w[i]*flux_i and optionally status[i], steps[i] and the final
+ * state (4 values per history: energy, altitude, direction cosine u_z,
+ * transport weight).  Host pointers. */
+int dp_mc_histories(dp_ctx* ctx, const dp_physics* phys, const dp_mixture* rock,
+                    const dp_mixture* air, const dp_mc_config* cfg, long n, const double* E,
+                    const double* q, const double* w, const double* thickness,
+                    const double* density, const double* elevation,
+                    const double* primary_altitude, int geo_stride, uint64_t id0,
+                    double* contrib, int32_t* status, int32_t* steps, double* final_state);
+
+/* One line of sight of a batched run: n_samples histories with log-uniform
+ * final energies and +-1 charges drawn as run_backward_mc draws them
+ * (src/Geometry.jl:863-875).  Geometry: rock thickness, bulk density and
+ * elevation; when a *_max field exceeds its base value, each history draws
+ * the value uniformly in [base, max] instead (Philox blocks 1-2).  Primary
+ * altitude: thickness + air_height when air_height > 0, else
+ * primary_altitude (<= 0: 3e4 m). */
+typedef struct {
+  double thickness, thickness_max;
+  double density, density_max;
+  double elevation, elevation_max;
+  double primary_altitude, air_height;
+  double energy_min, energy_max;
+  long n_samples;
+} dp_los;
+
+typedef struct {
+  double flux, sigma;          /* estimate and standard error (src/Geometry.jl:883-893) */
+  double gradient;             /* d(CSDA sample-average flux)/d(density), when asked */
+  double gradient_flux;        /* that CSDA surrogate flux */
+  long n_samples;
+  long n_status_nonzero;       /* histories with a status bit */
+} dp_los_result;
+
+/* Batched stochastic backward MC over many lines of sight in one persistent
+ * launch (histories of all lines of sight share the device; the history id
+ * is the running sample index over the batch).  compute_gradient adds the
+ * deterministic CSDA sample-average gradient per line of sight
+ * (src/Geometry.jl:933-945); it needs fixed (undrawn) geometry.  Host pointers. */
+int dp_mc_los(dp_ctx* ctx, const dp_physics* phys, const dp_mixture* rock, const dp_mixture* air,
+              const dp_mc_config* cfg, long n_los, const dp_los* los, int compute_gradient,
+              dp_los_result* out);
+/* Same with los and out in device memory; total_samples must equal the sum
+ * of n_samples. */
+int dp_mc_los_dev(dp_ctx* ctx, const dp_physics* phys, const dp_mixture* rock,
+                  const dp_mixture* air, const dp_mc_config* cfg, long n_los, const dp_los* los,
+                  long total_samples, int compute_gradient, dp_los_result* out);
 
 /* ------------------------------------------------------------------ tomography
  * Voxel-density CSDA forward model (examples/diff_flux_cube.jl:304-557):

@@ -279,9 +279,11 @@ void orc_mc_histories(void* h, int n_rock, const int* rock_mats, const double* r
                       long* steps, double* Efinal, int nthreads) {
   Physics* p = static_cast<Physics*>(h);
   Mixture rm;
-  for (int j = 0; j < n_rock; ++j) {
+  double tot = 0;
+  for (int j = 0; j < n_rock; ++j) tot += rock_fracs[j];
+  for (int j = 0; j < n_rock; ++j) {  // MaterialMixture normalises (src/Types.jl:363-368)
     rm.mats.push_back(rock_mats[j]);
-    rm.fracs.push_back(rock_fracs[j]);
+    rm.fracs.push_back(rock_fracs[j] / tot);
   }
   Mixture am;
   am.mats.push_back(air);
@@ -318,9 +320,11 @@ int orc_mixed_kernel(void* h, int n_mats, const int* mats, const double* fracs, 
                      double* cols, double* onset) {
   Physics* p = static_cast<Physics*>(h);
   Mixture mx;
+  double tot = 0;
+  for (int j = 0; j < n_mats; ++j) tot += fracs[j];
   for (int j = 0; j < n_mats; ++j) {
     mx.mats.push_back(mats[j]);
-    mx.fracs.push_back(fracs[j]);
+    mx.fracs.push_back(fracs[j] / tot);
   }
   MixedKernel k = prepare_mixed_kernel(*p, mx);
   int n = int(k.E.size());

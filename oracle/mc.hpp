@@ -19,10 +19,11 @@ enum : int {
 void philox4x32(uint32_t c[4], uint32_t k0, uint32_t k1);
 
 // Sequential uniforms of history `id`: Philox4x32-10 keyed by the seed, counter
-// (id, block); two 32-bit words per double.  Blocks 0 and 1 hold the history's
-// energy/charge and geometry draws; transport starts at block 2.
+// (id, block); two 32-bit words per double.  Block 0 holds the history's
+// energy/charge draws, blocks 1-2 its drawn geometry; transport starts at
+// block 3.
 struct Rng {
-  uint64_t seed = 0, id = 0, block = 2;
+  uint64_t seed = 0, id = 0, block = 3;
   uint32_t w[4] = {0, 0, 0, 0};
   int used = 2;
   // Optional scripted stream (tests): uniform() and expo() both pop the next

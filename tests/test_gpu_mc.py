@@ -1,0 +1,223 @@
+"""Stochastic backward MC on the GPU (straggled / mixed dual-mode transport)
+against the oracle, through the C ABI.
+
+Both sides transport over identical tables (the oracle's, Coulomb columns
+included, uploaded with the elemental recipes) and draw from the same
+counter-based Philox streams, so histories can be compared one by one.  In
+FP64 the kernel evaluates the reference's operations; transcendental
+functions (CUDA vs the host libm) differ in the last bit, so a history
+agrees to ~1e-12 unless that difference flips a sampling decision, which
+the tests allow for a small fraction of histories.  The mixed-precision
+kernel is compared statistically (paired differences) and per history
+with a looser bar.
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def dp():
+    import dpgpu
+    return dpgpu
+
+
+@pytest.fixture(scope="module")
+def orc_phys(oracle):
+    return oracle.default_physics((oracle.STANDARD_ROCK, oracle.AIR, oracle.WATER), coulomb=True)
+
+
+@pytest.fixture(scope="module")
+def phys(dp, orc_phys):
+    tabs = [orc_phys.table(i) for i in range(3)]
+    return dp.upload_physics(tabs, ["StandardRock", "Air", "Water"],
+                             materials=(dp.STANDARD_ROCK, dp.AIR, dp.WATER))
+
+
+@pytest.fixture(scope="module")
+def media(dp, phys):
+    rock = dp.MaterialMixture(phys, 1)
+    air = dp.MaterialMixture(phys, 2)
+    mix = dp.MaterialMixture(phys, [1, 3, 2], [0.70, 0.25, 0.05])
+    return rock, air, mix
+
+
+def _agree(a, b, rtol):
+    return np.abs(a - b) <= rtol * np.maximum(np.abs(a), np.abs(b)) + 1e-300
+
+
+# ------------------------------------------------------------------ kernel prep
+@pytest.mark.parametrize("which", ["rock", "mixture"])
+def test_mixed_kernel_matches_oracle(dp, media, oracle, orc_phys, which):
+    """prepare_mixed_kernel (src/MixedTransport.jl:51-97) in the library
+    against the oracle, single material and the rock/water/air mixture."""
+    m = media[0] if which == "rock" else media[2]
+    k = m.kernel()
+    ref = oracle.mixed_kernel(orc_phys, [0]) if which == "rock" else \
+        oracle.mixed_kernel(orc_phys, [0, 2, 1], [0.70, 0.25, 0.05])
+    assert k["onset"] == ref["onset"]
+    for a, b in (("energies", "E"), ("stopping", "stop"), ("sigma", "sigma"), ("range", "range"),
+                 ("hazard", "hazard"), ("proper", "proper")):
+        np.testing.assert_allclose(k[a], ref[b], rtol=1e-13, atol=0, err_msg=a)
+
+
+# ------------------------------------------------------------------ histories
+def _histories(n, seed, per_history_geometry=True):
+    rng = np.random.default_rng(seed)
+    E = np.exp(rng.uniform(np.log(1.0), np.log(1e4), n))
+    q = np.where(rng.random(n) > 0.5, 1.0, -1.0)
+    w = 2 * E * np.log(1e4)
+    if per_history_geometry:
+        t = rng.uniform(20.0, 500.0, n)
+        geo = dict(thickness=t, density=rng.uniform(2000.0, 2800.0, n),
+                   elevation=rng.uniform(30.0, 90.0, n), primary_altitude=t + 1000.0)
+    else:
+        geo = dict(thickness=120.0, density=2650.0, elevation=60.0, primary_altitude=1120.0)
+    return E, q, w, geo
+
+
+def _oracle_histories(oracle, orc_phys, E, q, w, geo, seed, rock=(0,), fracs=None, **kw):
+    return oracle.mc_histories(orc_phys, list(rock), 1, geo["thickness"], geo["density"],
+                               geo["elevation"], geo["primary_altitude"], E, q, w, seed=seed,
+                               rock_fracs=fracs, **kw)
+
+
+@pytest.mark.parametrize("case", ["straggled_scattering", "mixed_only", "mixture"])
+def test_fp64_histories_match_oracle(dp, phys, media, oracle, orc_phys, case):
+    """One history at a time: contribution, status, step count, final energy."""
+    n, seed = 3000, 11
+    E, q, w, geo = _histories(n, seed)
+    rock, air, mix = media
+    kw = dict(straggling=True, scattering=case != "mixed_only",
+              threshold_low=100.0 if case != "mixed_only" else 1.0)
+    if case == "mixture":
+        oc, ost, osteps, oE = _oracle_histories(oracle, orc_phys, E, q, w, geo, seed, rock=(0, 2, 1),
+                                                fracs=[0.70, 0.25, 0.05], **kw)
+        med = mix
+    else:
+        oc, ost, osteps, oE = _oracle_histories(oracle, orc_phys, E, q, w, geo, seed, **kw)
+        med = rock
+    c, st, steps, Ef = dp.mc_histories(phys, med, air, E, q, w, seed=seed,
+                                       straggling=kw["straggling"], scattering=kw["scattering"],
+                                       energy_threshold_low=kw["threshold_low"], precision="fp64",
+                                       **geo)
+    assert np.all(st == 0) and np.all(ost == 0)
+    same = _agree(c, oc, 1e-9) & (steps == osteps) & _agree(Ef[:, 0], oE, 1e-9)
+    assert same.mean() >= 0.99, same.mean()
+    assert (c > 0).sum() > n // 10  # a good share of histories reach the sky
+    # estimator over all histories: paired difference within 3 sigma
+    d = c - oc
+    assert abs(d.mean()) <= 3 * d.std() / math.sqrt(n) + 1e-14 * abs(oc.mean())
+
+
+def test_mixed_precision_histories_track_fp64(dp, phys, media, oracle, orc_phys):
+    """FP32 transport with FP64 positions, kinematics and tally: the paired
+    flux difference against the FP64 oracle is within 3 sigma of its own
+    spread and below 1e-3 of the flux; most histories agree to 1e-3."""
+    n, seed = 20000, 5
+    E, q, w, geo = _histories(n, seed)
+    rock, air, mix = media
+    oc, ost, _, _ = _oracle_histories(oracle, orc_phys, E, q, w, geo, seed, rock=(0, 2, 1),
+                                      fracs=[0.70, 0.25, 0.05], straggling=True, scattering=True)
+    c, st, _, _ = dp.mc_histories(phys, mix, air, E, q, w, seed=seed, precision="mixed", **geo)
+    assert np.all(st == 0)
+    d = c - oc
+    f = oc.mean()
+    assert abs(d.mean()) <= 3 * d.std() / math.sqrt(n) + 1e-12 * abs(f)
+    assert abs(c.mean() - f) <= 1e-3 * abs(f) + 3 * d.std() / math.sqrt(n)
+    assert _agree(c, oc, 1e-3).mean() >= 0.9
+
+
+# ------------------------------------------------------------------ batched LOS
+def test_line_of_sight_batch_matches_oracle(dp, phys, media, oracle, orc_phys):
+    """dp_mc_los: histories of all lines of sight in one launch; history id
+    = running sample index; per-LOS flux and sigma from the compensated
+    tally equal the oracle's over the same samples."""
+    rock, air, _ = media
+    depth = np.array([60.0, 150.0, 400.0])
+    rho = np.array([2450.0, 2650.0, 2750.0])
+    ns = np.array([300, 1000, 700])
+    los = dp.make_los(ns, thickness=depth, density=rho, elevation=90.0, energy_min=1.0,
+                      energy_max=1e4, primary_altitude=depth + 1000.0)
+    out = dp.backward_mc_batch(phys, los, rock=rock, air=air, seed=3, precision="fp64",
+                               scattering=False)
+    E, q, w = dp.mc_samples(phys, energy_min=1.0, energy_max=1e4, n_samples=int(ns.sum()), seed=3)
+    off = np.concatenate([[0], np.cumsum(ns)])
+    for l in range(3):
+        sl = slice(off[l], off[l + 1])
+        oc, ost, _, _ = oracle.mc_histories(orc_phys, [0], 1, depth[l], rho[l], 90.0,
+                                            depth[l] + 1000.0, E[sl], q[sl], w[sl], seed=3,
+                                            id0=int(off[l]), straggling=True, scattering=False)
+        f = oc.mean()
+        s = math.sqrt(max((oc ** 2).mean() - f * f, 0.0) / ns[l])
+        assert out["n_samples"][l] == ns[l] and out["n_status_nonzero"][l] == 0
+        assert abs(out["flux"][l] - f) <= max(0.5 * s, 1e-9 * abs(f))
+        assert out["sigma"][l] == pytest.approx(s, rel=0.05)
+
+
+def _philox_u01(ids, block, seed):
+    """Philox4x32-10 (seed, (id, block)) -> two 53-bit uniforms per id."""
+    M0, M1, W0, W1 = 0xD2511F53, 0xCD9E8D57, 0x9E3779B9, 0xBB67AE85
+    c0 = ids.astype(np.uint64) & 0xFFFFFFFF
+    c1 = ids.astype(np.uint64) >> 32
+    c2 = np.full_like(c0, block)
+    c3 = np.zeros_like(c0)
+    k0, k1 = seed & 0xFFFFFFFF, seed >> 32
+    for _ in range(10):
+        p0, p1 = np.uint64(M0) * c0, np.uint64(M1) * c2
+        c0, c1, c2, c3 = ((p1 >> 32) ^ c1 ^ np.uint64(k0)) & 0xFFFFFFFF, p1 & 0xFFFFFFFF, \
+            ((p0 >> 32) ^ c3 ^ np.uint64(k1)) & 0xFFFFFFFF, p0 & 0xFFFFFFFF
+        k0, k1 = (k0 + W0) & 0xFFFFFFFF, (k1 + W1) & 0xFFFFFFFF
+    f = lambda a, b: ((a >> 5).astype(np.float64) * 67108864.0 + (b >> 6).astype(np.float64)) \
+        / 9007199254740992.0
+    return f(c0, c1), f(c2, c3)
+
+
+def test_drawn_geometry_batch_matches_oracle(dp, phys, media, oracle, orc_phys):
+    """Per-history geometry drawn on the device (thickness U[20,500],
+    density U[2000,2800] from Philox block 1, elevation U[30,90] from block 2,
+    primary altitude thickness + 1000 m), the rock/water/air mixture."""
+    rock, air, mix = media
+    n, seed = 2000, 21
+    los = dp.make_los(n, thickness=20.0, thickness_max=500.0, density=2000.0, density_max=2800.0,
+                      elevation=30.0, elevation_max=90.0, air_height=1000.0, energy_min=1.0,
+                      energy_max=1e4)
+    out = dp.backward_mc_batch(phys, los, rock=mix, air=air, seed=seed, precision="fp64")
+    ids = np.arange(n, dtype=np.uint64)
+    u1, u2 = _philox_u01(ids, 1, seed)
+    u3, _ = _philox_u01(ids, 2, seed)
+    t = 20.0 + 480.0 * u1
+    geo = dict(thickness=t, density=2000.0 + 800.0 * u2, elevation=30.0 + 60.0 * u3,
+               primary_altitude=t + 1000.0)
+    E, q, w = dp.mc_samples(phys, energy_min=1.0, energy_max=1e4, n_samples=n, seed=seed)
+    oc, ost, _, _ = _oracle_histories(oracle, orc_phys, E, q, w, geo, seed, rock=(0, 2, 1),
+                                      fracs=[0.70, 0.25, 0.05], straggling=True, scattering=True)
+    f = oc.mean()
+    s = math.sqrt(max((oc ** 2).mean() - f * f, 0.0) / n)
+    assert out["n_status_nonzero"][0] == 0
+    assert abs(out["flux"][0] - f) <= max(0.5 * s, 1e-9 * abs(f))
+
+
+def test_run_backward_mc_stochastic(dp, phys, oracle, orc_phys):
+    """run_backward_mc with straggling and scattering (the reference's
+    defaults): flux and sigma of the stochastic transport, gradient of the
+    CSDA surrogate over the same samples."""
+    n = 3000
+    kw = dict(rock_thickness=100.0, rock_density=2650.0, elevation=45.0, energy_min=1.0,
+              energy_max=1e3, n_samples=n, seed=8)
+    r = dp.run_backward_mc(phys, compute_gradient=True, **kw)
+    E, q, w = dp.mc_samples(phys, energy_min=1.0, energy_max=1e3, n_samples=n, seed=8)
+    oc, ost, _, _ = oracle.mc_histories(orc_phys, [0], 1, 100.0, 2650.0, 45.0, 3e4, E, q, w,
+                                        seed=8, straggling=True, scattering=True)
+    f = oc.mean()
+    s = math.sqrt(max((oc ** 2).mean() - f * f, 0.0) / n)
+    assert abs(r.flux - f) <= max(0.5 * s, 1e-9 * f)
+    assert r.sigma == pytest.approx(s, rel=0.05)
+    cc, cd = oracle.backward_mc_csda(orc_phys, 0, 1, 100.0, 2650.0, 45.0, E, q, w)
+    assert r.gradient_flux == pytest.approx(cc.mean(), rel=1e-10)
+    assert r.gradient == pytest.approx(cd.mean(), rel=1e-8)
+    m = dp.run_backward_mc(phys, precision="mixed", **kw)
+    assert abs(m.flux - r.flux) <= 3 * r.sigma
