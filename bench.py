@@ -1,8 +1,13 @@
 """Benchmark of the DiffPumas.jl hot path on GB300 through libdpgpu.
 
-python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c3|c1] [--impl gpu|reference]
+python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c2|c3|c1] [--impl gpu|reference]
 
-Workloads (seeded synthetic inputs, generated by dpgpu.workloads):
+Workloads (seeded synthetic inputs):
+  c2  (default) straggled backward MC with DEL/EHS hard events and Coulomb
+      scattering through a runtime rock/water/air mixture (0.70/0.25/0.05)
+      under 1 km of air; per-history thickness, density and elevation drawn
+      on the device; 10^6 histories per step, FP32 transport with FP64
+      positions, kinematics and compensated tally.  Unit: samples/s.
   c3  batched tomography forward + adjoint: 64x64x32 voxel grid at 10 m,
       smooth random density field with 3 cavities, 4 detectors x 1024 rays,
       32 CSDA energy nodes on [1, 1e6] GeV.  One step = per-ray flux and the
@@ -175,6 +180,62 @@ def setup_c3(dp, torch, dev, precision="mixed"):
     return step_dev, step_e2e, plain_dev, info, phys
 
 
+def _device_bytes(torch, dev, obj):
+    raw = bytes(C.string_at(C.addressof(obj), C.sizeof(obj)))
+    return torch.tensor(list(raw), dtype=torch.uint8, device=dev)
+
+
+C2_MIX = ([1, 3, 2], [0.70, 0.25, 0.05])  # rock, water, air (1-based material indices)
+
+
+def c2_los(dp, n):
+    return dp.make_los(n, thickness=20.0, thickness_max=500.0, density=2000.0, density_max=2800.0,
+                       elevation=30.0, elevation_max=90.0, air_height=1000.0, energy_min=1.0,
+                       energy_max=1e4)
+
+
+def setup_c2(dp, torch, dev, precision="mixed"):
+    """Straggled backward MC with DEL/EHS events and Coulomb scattering below
+    100 GeV, mixed above, through rock (runtime mixture rock/water/air
+    0.70/0.25/0.05) under 1 km of air; per history thickness U[20,500] m,
+    density U[2000,2800] kg/m^3, elevation U[30,90] deg drawn on the device;
+    final energies log-uniform 1 GeV - 10 TeV, +-1 charges; 10^6 histories."""
+    phys = dp.create_physics(materials=(dp.STANDARD_ROCK, dp.AIR, dp.WATER))
+    mix = dp.MaterialMixture(phys, *C2_MIX)
+    air = dp.MaterialMixture(phys, 2)
+    n = 1_000_000
+    los = c2_los(dp, n)
+    lib = dp.load()
+    ctx = phys.ctx.h
+    cfgs = {p: dp._mc_config(2026, True, True, 100.0, None, p) for p in ("mixed", "fp64")}
+    d_los = _device_bytes(torch, dev, los)
+    d_out = torch.zeros(C.sizeof(dp.DpLosResult), dtype=torch.uint8, device=dev)
+
+    def run_dev(p):
+        dp.check(lib.dp_mc_los_dev(ctx, phys.h, mix.h, air.h, C.byref(cfgs[p]), 1, d_los.data_ptr(),
+                                   n, 0, d_out.data_ptr()), ctx)
+
+    def step_e2e():
+        r = dp.backward_mc_batch(phys, los, rock=mix, air=air, seed=2026, precision=precision)
+        assert r["n_status_nonzero"][0] == 0
+
+    kernel = "mc_mixed_lo+mc_mixed_hi" if precision == "mixed" else "mc_fp64_lo+mc_fp64_hi"
+    info = {"units": n, "unit": "samples/s", "kernel": kernel,
+            # per history: contribution (8 B) and status (4 B) written by the
+            # transport kernel and read back by the tally
+            "alg_bytes": n * 24, "traffic": None,
+            "config": {"workload": "c2: straggled MC with DEL/EHS + Coulomb scattering, rock mixture "
+                                   "rock/water/air 0.70/0.25/0.05 (per-history thickness U[20,500] m, "
+                                   "density U[2000,2800], elevation U[30,90] deg) under 1 km air, "
+                                   "E 1 GeV-10 TeV, 1e6 histories",
+                       "n_samples": n, "precision": precision, "tables": "create_physics(MUON), "
+                       "rock+air+water, 200 nodes, with Coulomb columns"},
+            "h2d": C.sizeof(dp.DpLos), "d2h": C.sizeof(dp.DpLosResult),
+            "plain_what": "FP64 transport (the reference's operations), same launch",
+            "plain_reps": 1, "plain_warm": False}
+    return (lambda: run_dev(precision)), step_e2e, (lambda: run_dev("fp64")), info, phys
+
+
 def setup_c1(dp, torch, dev):
     phys = dp.create_physics()
     n = 10000
@@ -205,7 +266,7 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
     import dpgpu as dp
     dp._default = dp.Context(local)
-    setup = {"c3": setup_c3, "c1": setup_c1}[args.workload]
+    setup = {"c2": setup_c2, "c3": setup_c3, "c1": setup_c1}[args.workload]
     step_dev, step_e2e, plain_dev, info, phys = setup(dp, torch, dev)
     lib = dp.load()
     ctx = phys.ctx.h
@@ -245,8 +306,11 @@ def run_gpu(args):
     times = [a.elapsed_time(b) for a, b in events]
     barrier(world)
     launches = lib.dp_launch_count(ctx) - launches0
-    kms = C.c_double()
-    lib.dp_kernel_time(ctx, info["kernel"].encode(), C.byref(kms))
+    kms = C.c_double(0.0)
+    for name in info["kernel"].split("+"):  # summed over the kernels of the timed step
+        k = C.c_double()
+        lib.dp_kernel_time(ctx, name.encode(), C.byref(k))
+        kms.value += k.value
     lib.dp_set_timing(ctx, 0)
     ms = max_over_ranks(world, sum(times) / len(times))
     value = world * info["units"] / (ms * 1e-3)
@@ -265,16 +329,18 @@ def run_gpu(args):
     # plain FP64 one-launch-per-ray form (speed-up denominator)
     plain = None
     if plain_dev is not None and not args.no_plain:
-        plain_dev()
+        if info.get("plain_warm", True):
+            plain_dev()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        reps = 2
+        reps = info.get("plain_reps", 2)
         for _ in range(reps):
             plain_dev()
         torch.cuda.synchronize()
         plain_ms = (time.perf_counter() - t0) * 1e3 / reps
         plain = {"value": info["units"] / (plain_ms * 1e-3), "unit": info["unit"],
-                 "ms_per_step": plain_ms, "what": "plain FP64 one-launch-per-ray, forward only"}
+                 "ms_per_step": plain_ms,
+                 "what": info.get("plain_what", "plain FP64 one-launch-per-ray, forward only")}
 
     peak, peak_kind = peaks()
     kernel_ms = kms.value / args.steps
@@ -324,6 +390,22 @@ def cpu_baseline(workload, budget_s=15.0, threads=None):
         return {"value": n / dt, "unit": "rays/s", "cores": threads, "kind": "port",
                 "sample": f"{n} rays of the c3 workload (cycled), forward flux + reverse-sweep "
                           "J^T r (FP64 oracle, OpenMP)"}
+    if workload == "c2":
+        p = O.default_physics((O.STANDARD_ROCK, O.AIR, O.WATER), coulomb=True)
+        rng = np.random.default_rng(0)
+        n, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < budget_s:
+            m = 4096
+            E = np.exp(rng.uniform(0, np.log(1e4), m))
+            q = np.where(rng.uniform(size=m) > 0.5, 1.0, -1.0)
+            t = rng.uniform(20.0, 500.0, m)
+            O.mc_histories(p, [0, 2, 1], 1, t, rng.uniform(2000.0, 2800.0, m),
+                           rng.uniform(30.0, 90.0, m), t + 1000.0, E, q, 2 * E * np.log(1e4),
+                           seed=7, id0=n, rock_fracs=[0.70, 0.25, 0.05], threads=threads)
+            n += m
+        dt = time.perf_counter() - t0
+        return {"value": n / dt, "unit": "samples/s", "cores": threads, "kind": "port",
+                "sample": f"{n} histories of the c2 workload (FP64 oracle, OpenMP over histories)"}
     p = O.default_physics((O.STANDARD_ROCK, O.AIR))
     rng = np.random.default_rng(0)
     n, t0 = 0, time.perf_counter()
@@ -342,7 +424,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    units = {"c3": "rays/s", "c1": "samples/s"}[args.workload]
+    units = {"c2": "samples/s", "c3": "rays/s", "c1": "samples/s"}[args.workload]
     vals = []
     for _ in range(args.warmup):
         cpu_baseline(args.workload, budget_s=args.cpu_seconds / 4)
@@ -367,7 +449,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--workload", default="c3", choices=["c3", "c1"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c1"])
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")

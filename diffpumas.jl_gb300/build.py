@@ -14,9 +14,14 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libdpgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code: no FMA contraction, so the host table builders give the same
+# bits on x86 and Arm (the device code keeps nvcc's default contraction)
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-         "--expt-relaxed-constexpr", "--extended-lambda"]
+         "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr", "--extended-lambda"]
 UNITS = ["api.cu", "physics_build.cu", "csda_mc.cu", "tomo.cu", "mc.cu"]
+# per-unit flags: the stochastic transport's FP32 kernel uses the hardware
+# (MUFU) transcendentals; FP64 arithmetic is not affected by these flags
+UNIT_FLAGS = {"mc.cu": ["--use_fast_math"]}
 
 
 def nvcc():
@@ -47,7 +52,7 @@ def build(force=False, verbose=False, extra=()):
 
     def run(job):
         src, obj = job
-        cmd = [*cmdline, "-c", src, "-o", obj]
+        cmd = [*cmdline, *UNIT_FLAGS.get(os.path.basename(src), []), "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {os.path.basename(src)}:\n{r.stderr}")

@@ -18,6 +18,7 @@ constexpr double kElectronMass = 0.510998910e-3;
 constexpr double kElectronRadius = 2.817940285e-15;
 constexpr double kAlpha = 7.2973525693e-3;
 constexpr double kHbarC = 1.973269804e-16;
+constexpr double kBohrRadius = 0.529177210903e-10;
 constexpr double kProtonMass = 0.938272;
 constexpr double kNeutronMass = 0.939565;
 constexpr double kPionMass = 0.13957018;

@@ -327,11 +327,11 @@ struct McParams {
   int32_t* status;
   int32_t* steps;
   double* efinal;
-  unsigned long long* counter;
+  unsigned long long* counter;  // [0] phase-0 histories taken, [1] phase-1, [2] queued
   int* err_flag;
+  int coop_nel, coop_stride;  // cooperative DCS buffers: elements, floats per warp
+  void* queue;                // Handoff<R> x n: histories crossing the mode switch
 };
-
-constexpr int kMcThreads = 256;
 
 // Copies `bytes` (16-byte multiple) from global to shared memory with
 // cp.async.bulk completing on one mbarrier; all threads call it.  Returns
@@ -432,6 +432,7 @@ __device__ __forceinline__ void start_history(const McParams& P, long i, Hist<R>
   h.steps = h.inner = h.outer = 0;
   h.need_mode = true;
   h.strag = h.mixed = h.scat = false;
+  h.x.kind = CONT_NONE;
   g.init(P.seed, id);
 }
 
@@ -449,14 +450,28 @@ __device__ __forceinline__ void end_history(const McParams& P, long i, const His
   }
 }
 
-template <class R>
-__global__ void __launch_bounds__(kMcThreads) mc_kernel(const __grid_constant__ McParams P) {
+// Launch shape per precision: the FP32 transport runs 16 warps per SM
+// sharing one staged copy of the tables and evaluates hard-event DCS sums
+// cooperatively per warp; the FP64 transport (one thread per sum) runs 8.
+template <class R> struct KCfg;
+template <> struct KCfg<float> {
+  static constexpr int threads = 512;
+  static constexpr bool coop = true;
+};
+template <> struct KCfg<double> {
+  static constexpr int threads = 256;
+  static constexpr bool coop = false;
+};
+
+template <class R, int PHASE>
+__global__ void __launch_bounds__(KCfg<R>::threads, 1) mc_kernel(const __grid_constant__ McParams P) {
   extern __shared__ __align__(16) unsigned char smem[];
   const unsigned char* base = P.blob;
+  const uint32_t tables = P.staged ? 2 * P.lay.med_bytes : 0;
   if (P.staged) {
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
     unsigned char* dst = smem + 16;
-    if (!stage_blob(dst, P.blob, 2 * P.lay.med_bytes, bar)) {
+    if (!stage_blob(dst, P.blob, tables, bar)) {
       // give the copy in flight a second bounded wait before leaving
       uint32_t done = 0;
       for (int it = 0; it < (1 << 22) && !done; ++it)
@@ -472,18 +487,80 @@ __global__ void __launch_bounds__(kMcThreads) mc_kernel(const __grid_constant__ 
   }
   const Med<R> rock = make_med<R>(base, P.lay, P.info[0]);
   const Med<R> air = make_med<R>(base + P.lay.med_bytes, P.lay, P.info[1]);
+  Handoff<R>* queue = static_cast<Handoff<R>*>(P.queue);
+  const long n = PHASE == 0 ? P.n : long(*(volatile unsigned long long*)(P.counter + 2));
   Hist<R> h;
   Stream g;
-  long i = next_history(P.counter);
-  bool live = i < P.n;
-  if (live) start_history(P, i, h, g);
-  while (live) {
-    if (advance(rock, air, P.C, h, g)) {
-      end_history(P, i, h);
-      i = next_history(P.counter);
-      live = i < P.n;
-      if (live) start_history(P, i, h, g);
+  auto take = [&](long* idx) -> bool {
+    long j = next_history(P.counter + PHASE);
+    if (j >= n) return false;
+    if (PHASE == 0) {
+      *idx = j;
+      start_history(P, j, h, g);
+    } else {
+      *idx = load_handoff(queue[j], P.seed, h, g);
     }
+    return true;
+  };
+  // after a step: end the history, hand it to phase 1, or keep going
+  auto settle = [&](int r, long* idx) -> bool {
+    if (r == ADV_HANDOFF) {
+      unsigned long long slot = atomicAdd(P.counter + 2, 1ull);
+      save_handoff(h, g, *idx, queue + slot);
+      return take(idx);
+    }
+    if (r == ADV_DONE) {
+      end_history(P, *idx, h);
+      return take(idx);
+    }
+    return true;
+  };
+  long i = 0;
+  bool live = take(&i);
+  if constexpr (KCfg<R>::coop) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float* item = reinterpret_cast<float*>(smem + 16 + tables) + size_t(warp) * P.coop_stride;
+    float* comp = item + kItemsPerElement * P.coop_nel;
+    for (;;) {
+      // serve the hard events the warp's suspended steps wait for, one at a time
+      unsigned want = __ballot_sync(0xffffffffu, live && h.x.kind != CONT_NONE);
+      while (want) {
+        const int L = __ffs(want) - 1;
+        want &= want - 1;
+        const int med = __shfl_sync(0xffffffffu, h.x.medium, L);
+        const double anc = __shfl_sync(0xffffffffu, h.x.anc, L);
+        const double q = __shfl_sync(0xffffffffu, h.x.q, L);
+        const Med<R>& m = med ? air : rock;
+        const double total = coop_total(m.el, m.nel, P.C.mass, anc, q, item, comp);
+        if (lane == L) {
+          h.x.total = total;
+          h.x.pick = -1;
+          if (h.x.details && total > 0.0) {
+            // process and element pick in the reference's order (src/MixedTransport.jl:131-140)
+            double u = uni_d(g) * total;
+            const int last = 4 * m.nel - 1;
+            int pick = last;
+            for (int c = 0; c <= last; ++c) {
+              u -= double(comp[c]);
+              if (u <= 0.0) {
+                pick = c;
+                break;
+              }
+            }
+            h.x.pick = pick;
+          }
+        }
+        __syncwarp();
+      }
+      if (live) {
+        const int r = h.x.kind != CONT_NONE ? resume<R, PHASE>(rock, air, P.C, h, g)
+                                            : advance<R, true, PHASE>(rock, air, P.C, h, g);
+        live = settle(r, &i);
+      }
+      if (!__any_sync(0xffffffffu, live)) break;
+    }
+  } else {
+    while (live) live = settle(advance<R, false, PHASE>(rock, air, P.C, h, g), &i);
   }
 }
 
@@ -594,30 +671,45 @@ int check_cfg(dp_ctx* ctx, const dp_physics* ph, const dp_mc_config* cfg, Consts
   return DP_OK;
 }
 
-template <class R>
-int launch_mc(dp_ctx* ctx, McParams& P) {
-  const int threads = kMcThreads;
-  size_t smem = 16 + size_t(2) * P.lay.med_bytes;
-  int dev_smem = 0;
-  DP_CHECK_CUDA(ctx, cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
-  P.staged = smem <= size_t(dev_smem) ? 1 : 0;
-  if (!P.staged) smem = 0;
-  DP_CHECK_CUDA(ctx, cudaFuncSetAttribute(mc_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          int(smem)));
+template <class R, int PHASE>
+int launch_phase(dp_ctx* ctx, McParams& P, size_t smem, long max_blocks) {
+  const int threads = KCfg<R>::threads;
+  DP_CHECK_CUDA(ctx, cudaFuncSetAttribute(mc_kernel<R, PHASE>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   int per_sm = 0, n_sm = 0;
-  DP_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_kernel<R>, threads, smem));
+  DP_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_kernel<R, PHASE>,
+                                                                   threads, smem));
   DP_CHECK_CUDA(ctx, cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, ctx->device));
   if (per_sm < 1) return fail(ctx, DP_ERR_CUDA, "MC kernel does not fit on a multiprocessor");
-  long blocks = long(per_sm) * n_sm;
-  long need = (P.n + threads - 1) / threads;
-  if (blocks > need) blocks = need;
+  long blocks = std::min(long(per_sm) * n_sm, max_blocks);
   if (blocks < 1) blocks = 1;
-  DP_CHECK_CUDA(ctx, cudaMemsetAsync(P.counter, 0, sizeof(unsigned long long), ctx->stream));
   timed_begin(ctx);
-  mc_kernel<R><<<int(blocks), threads, smem, ctx->stream>>>(P);
+  mc_kernel<R, PHASE><<<int(blocks), threads, smem, ctx->stream>>>(P);
   DP_CHECK_CUDA(ctx, cudaGetLastError());
-  timed_end(ctx, sizeof(R) == 4 ? "mc_mixed" : "mc_fp64");
+  timed_end(ctx, sizeof(R) == 4 ? (PHASE ? "mc_mixed_hi" : "mc_mixed_lo")
+                                : (PHASE ? "mc_fp64_hi" : "mc_fp64_lo"));
   return DP_OK;
+}
+
+// Both transport phases; P.queue must hold P.n handoff records and
+// P.counter three zeroed words (set here).
+template <class R>
+int launch_mc(dp_ctx* ctx, McParams& P) {
+  const int threads = KCfg<R>::threads;
+  P.coop_nel = std::max(P.info[0].nel, P.info[1].nel);
+  P.coop_stride = KCfg<R>::coop ? ((kItemsPerElement + 4) * P.coop_nel + 3) / 4 * 4 : 0;
+  size_t coop_bytes = size_t(threads / 32) * P.coop_stride * sizeof(float);
+  size_t tables = size_t(2) * P.lay.med_bytes;
+  int dev_smem = 0;
+  DP_CHECK_CUDA(ctx, cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+  P.staged = 16 + tables + coop_bytes <= size_t(dev_smem) ? 1 : 0;
+  size_t smem = 16 + (P.staged ? tables : 0) + coop_bytes;
+  if (smem > size_t(dev_smem)) return fail(ctx, DP_ERR_ARG, "media too large for the MC kernel");
+  long need = (P.n + threads - 1) / threads;
+  DP_CHECK_CUDA(ctx, cudaMemsetAsync(P.counter, 0, 3 * sizeof(unsigned long long), ctx->stream));
+  int rc = launch_phase<R, 0>(ctx, P, smem, need);
+  if (rc) return rc;
+  return launch_phase<R, 1>(ctx, P, smem, need);
 }
 
 int run(dp_ctx* ctx, McParams& P, int precision) {
@@ -732,7 +824,7 @@ int dp_mc_histories(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock_c,
   long ng = geo_stride ? n : 1;
   size_t nb = size_t(n) * sizeof(double), gb = size_t(ng) * sizeof(double);
   Arena A;
-  A.base = static_cast<char*>(scratch(ctx, 8 * nb + 4 * gb + size_t(n) * 8 + 4096, 0));
+  A.base = static_cast<char*>(scratch(ctx, 8 * nb + 4 * gb + size_t(n) * (8 + sizeof(Handoff<double>)) + 4096, 0));
   A.cap = ctx->slot_bytes[0];
   double* dE = A.take<double>(n);
   double* dq = A.take<double>(n);
@@ -745,8 +837,9 @@ int dp_mc_histories(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock_c,
   double* dH = A.take<double>(ng);
   int32_t* ds = A.take<int32_t>(n);
   int32_t* dn = A.take<int32_t>(n);
-  unsigned long long* ctr = A.take<unsigned long long>(1);
-  if (!ctr) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
+  unsigned long long* ctr = A.take<unsigned long long>(3);
+  Handoff<double>* queue = A.take<Handoff<double>>(n);
+  if (!queue) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
   cudaStream_t s = ctx->stream;
   DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dE, E, nb, cudaMemcpyHostToDevice, s));
   DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dq, q, nb, cudaMemcpyHostToDevice, s));
@@ -772,6 +865,7 @@ int dp_mc_histories(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock_c,
   P.steps = dn;
   P.efinal = dEf;
   P.counter = ctr;
+  P.queue = queue;
   rc = run(ctx, P, cfg->precision);
   if (rc) return rc;
   std::vector<int32_t> st_h;
@@ -859,12 +953,14 @@ int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_
   if (rc) return rc;
   long nt = total > 0 ? total : 1;
   Arena A;
-  A.base = static_cast<char*>(scratch(ctx, size_t(nt) * 12 + size_t(n_los + 1) * 8 + 4096, 0));
+  A.base = static_cast<char*>(scratch(
+      ctx, size_t(nt) * (12 + sizeof(Handoff<double>)) + size_t(n_los + 1) * 8 + 4096, 0));
   A.cap = ctx->slot_bytes[0];
   double* dc = A.take<double>(nt);
   int32_t* ds = A.take<int32_t>(nt);
   int64_t* off = A.take<int64_t>(n_los + 1);
-  unsigned long long* ctr = A.take<unsigned long long>(1);
+  unsigned long long* ctr = A.take<unsigned long long>(3);
+  Handoff<double>* queue = A.take<Handoff<double>>(nt);
   int* bits = A.take<int>(1);
   if (!bits) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
   DP_CHECK_CUDA(ctx, cudaMemsetAsync(bits, 0, sizeof(int), ctx->stream));
@@ -881,6 +977,7 @@ int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_
     P.contrib = dc;
     P.status = ds;
     P.counter = ctr;
+    P.queue = queue;
     rc = run(ctx, P, cfg->precision);
     if (rc) return rc;
   }

@@ -117,21 +117,28 @@ struct Stream {
     block = kTransportBlock;
     used = 2;
   }
-  __device__ __forceinline__ void next(uint32_t& a, uint32_t& b) {
-    if (used >= 2) {
-      U4 r = philox(U4{c0, c1, block, 0u}, k0, k1);
-      ++block;
-      w0 = r.x;
-      w1 = r.y;
-      w2 = r.z;
-      w3 = r.w;
-      used = 0;
-    }
-    a = used == 0 ? w0 : w2;
-    b = used == 0 ? w1 : w3;
-    ++used;
-  }
+  __device__ __forceinline__ void next(uint32_t& a, uint32_t& b);
 };
+// One Philox block for the stream (kept out of line: every draw site would
+// otherwise carry the ten unrolled rounds).
+__device__ __noinline__ U4 philox_block(uint32_t c0, uint32_t c1, uint32_t block, uint32_t k0,
+                                        uint32_t k1) {
+  return philox(U4{c0, c1, block, 0u}, k0, k1);
+}
+__device__ __forceinline__ void Stream::next(uint32_t& a, uint32_t& b) {
+  if (used >= 2) {
+    U4 r = philox_block(c0, c1, block, k0, k1);
+    ++block;
+    w0 = r.x;
+    w1 = r.y;
+    w2 = r.z;
+    w3 = r.w;
+    used = 0;
+  }
+  a = used == 0 ? w0 : w2;
+  b = used == 0 ? w1 : w3;
+  ++used;
+}
 template <class R> __device__ __forceinline__ R uni(Stream& g);
 template <> __device__ __forceinline__ double uni<double>(Stream& g) {
   uint32_t a, b;
@@ -302,9 +309,8 @@ __device__ __forceinline__ R klookup(const Med<R>& m, int xcol, int ycol, R x, i
   return kat(m.kcol(ycol), m.nk, klocate(m.kcol(xcol), m.nk, x, status));
 }
 
-// Sum over elements and processes of f * dsigma/dq (src/MixedTransport.jl:99-106).
-// pick < 0: total; else the component index whose running sum first exceeds
-// u (returned in *which, total in the return value is then meaningless).
+// Sum over elements and processes of f * dsigma/dq (src/MixedTransport.jl:99-106)
+// by one thread in FP64 (the FP64 transport), in the reference's order.
 __device__ __noinline__ double del_total(const double* el, int nel, double mass, double anc,
                                          double q) {
   double total = 0.0;
@@ -318,6 +324,8 @@ __device__ __noinline__ double del_total(const double* el, int nel, double mass,
   }
   return total;
 }
+// Index of the component whose running sum first exceeds u (the process and
+// element pick of src/MixedTransport.jl:131-140).
 __device__ __noinline__ int del_pick(const double* el, int nel, double mass, double anc, double q,
                                      double u) {
   int last = 4 * nel - 1;
@@ -335,46 +343,125 @@ __device__ __noinline__ int del_pick(const double* el, int nel, double mass, dou
   return last;
 }
 
+// Terms of one hard-event DCS sum spread over a warp: per element one
+// bremsstrahlung, 12 pair-asymmetry and 9 photonuclear quadrature points and
+// one ionisation term.
+constexpr int kItemsPerElement = 23;
+
+// Warp-cooperative FP32 form of del_total: every lane evaluates a share of the
+// terms (per-mass scale N_A/(A 1e-3) against FP32 underflow), the components
+// are summed in a fixed order into comp[] (kept for the pick) and the total
+// is reduced in a fixed tree; all 32 lanes call it with the same arguments.
+__device__ __noinline__ double coop_total(const double* el, int nel, double mass, double anc,
+                                          double q, float* item, float* comp) {
+  const int lane = threadIdx.x & 31;
+  const float fm = float(mass), fk = float(anc), fq = float(q);
+  const int n_items = kItemsPerElement * nel;
+  for (int it = lane; it < n_items; it += 32) {
+    const int e = it / kItemsPerElement, j = it - e * kItemsPerElement;
+    const double* x = el + kElStride * e;
+    const float Z = float(x[0]), A = float(x[1]), sc = float(kAvogadro / (x[1] * 0.001));
+    float v = 0.f;
+    if (j == 0) {
+      v = dcs_brems<float>(Z, A, fm, fk, fq, sc);
+    } else if (j <= 12) {
+      float tmin;
+      if (pair_range<float>(Z, A, fm, fk, fq, &tmin))
+        v = -pair_point<float>(Z, A, fm, fk, fq, tmin, j - 1, sc);
+    } else if (j <= 21) {
+      float lmin, dx;
+      if (photo_range<float>(Z, A, fm, fk, fq, &lmin, &dx))
+        v = photo_point<float>(Z, A, fm, fk, fq, lmin, dx, j - 13, sc);
+    } else {
+      v = dcs_ionisation<float>(Z, float(x[2]), fm, fk, fq, sc);
+    }
+    item[it] = isfinite(v) ? v : 0.f;
+  }
+  __syncwarp();
+  float mine = 0.f;
+  for (int c = lane; c < 4 * nel; c += 32) {
+    const int e = c >> 2, p = c & 3, base = e * kItemsPerElement;
+    float v;
+    if (p == 0) {
+      v = item[base];
+    } else if (p == 1) {
+      v = 0.f;
+      for (int i = 0; i < 12; ++i) v += item[base + 1 + i];
+      v = fmaxf(v, 0.f);
+    } else if (p == 2) {
+      v = 0.f;
+      for (int i = 0; i < 9; ++i) v += item[base + 13 + i];
+      v = fmaxf(v, 0.f);
+    } else {
+      v = item[base + 22];
+    }
+    v *= float(el[kElStride * e + 3] * anc);  // fraction x ancestor energy
+    comp[c] = v;
+    mine += v;
+  }
+  for (int d = 16; d > 0; d >>= 1) mine += __shfl_down_sync(0xffffffffu, mine, d);
+  mine = __shfl_sync(0xffffffffu, mine, 0);
+  __syncwarp();
+  return double(mine);
+}
+
 struct DelOut {
   double energy, weight;
   int process, element;  // process 0: null CEL event
 };
-// reverse_del_event (src/MixedTransport.jl:111-142).
+
+// reverse_del_event (src/MixedTransport.jl:111-142) up to the DCS sum.  Returns
+// true when the event needs that sum; *anc and *denom (pdf r sigma (1 - p_cel))
+// then describe it.  Otherwise *out is the result.
 template <class R>
-__device__ __noinline__ DelOut reverse_del(const Med<R>& m, const Consts& C, double k, Stream& g,
-                                           bool details, int* status) {
-  DelOut r{k, 1.0, 0, -1};
+__device__ __noinline__ bool del_begin(const Med<R>& m, const Consts& C, double k, Stream& g, int* status,
+                          DelOut* out, double* anc_out, double* denom) {
+  *out = DelOut{k, 1.0, 0, -1};
   double sigma = double(klookup(m, K_E, K_SIG, R(k), status));
   if (!(sigma > 0.0)) {
     *status |= ST_ZERO_RATE;
-    return r;
+    return false;
   }
   double onset = double(m.onset), cut = C.cutoff;
   double pcel = k >= onset ? 0.0 : -log(cut) / (-log(cut) + log(onset / (onset - k)));
   if (pcel > 0.0 && uni_d(g) < pcel) {
-    r.weight = 1.0 / pcel;
-    return r;
+    out->weight = 1.0 / pcel;
+    return false;
   }
   const double me = kElectronMass, M = C.mass;
   double xmax = k < 0.5 * (M - me) * (M - me) / me
                     ? fmin(1.0, 2.0 * me * (k + 2.0 * M) / ((M + me) * (M + me)))
                     : 1.0;
   double xmin = k >= onset * (1.0 - cut) ? cut : 1.0 - k / onset;
-  if (!(xmax > xmin)) return r;
+  if (!(xmax > xmin)) return false;
   double invnorm = 1.0 / xmin - 1.0 / xmax;
   double nu = 1.0 / (1.0 / xmin - uni_d(g) * invnorm);
   double rr = 1.0 - nu, anc = k / rr, pdf = 1.0 / (invnorm * nu * nu);
-  double total = del_total(m.el, m.nel, M, anc, anc - k);
-  r.energy = anc;
-  r.weight = total / (pdf * rr * sigma * (1.0 - pcel));
-  if (details) {
-    if (total <= 0.0) return r;
-    double u = uni_d(g) * total;
-    int i = del_pick(m.el, m.nel, M, anc, anc - k, u);
-    r.process = i % 4 + 1;
-    r.element = i / 4;
+  *anc_out = anc;
+  *denom = pdf * rr * sigma * (1.0 - pcel);
+  return true;
+}
+// The rest of reverse_del_event once the DCS sum (and, with details, the
+// picked component) is known.
+__device__ __forceinline__ DelOut del_end(double anc, double denom, double total, int pick) {
+  DelOut r{anc, total / denom, 0, -1};
+  if (pick >= 0) {
+    r.process = pick % 4 + 1;
+    r.element = pick / 4;
   }
   return r;
+}
+// reverse_del_event in one thread, FP64 (src/MixedTransport.jl:111-142).
+template <class R>
+__device__ __noinline__ DelOut reverse_del(const Med<R>& m, const Consts& C, double k, Stream& g,
+                                           bool details, int* status) {
+  DelOut r;
+  double anc, denom;
+  if (!del_begin(m, C, k, g, status, &r, &anc, &denom)) return r;
+  double total = del_total(m.el, m.nel, C.mass, anc, anc - k);
+  int pick = -1;
+  if (details && total > 0.0) pick = del_pick(m.el, m.nel, C.mass, anc, anc - k, uni_d(g) * total);
+  return del_end(anc, denom, total, pick);
 }
 
 // Mutable part of a history.
@@ -385,38 +472,66 @@ struct State {
   int status;
 };
 
-// transport_mixed_step (src/MixedTransport.jl:144-200).  The grammage
-// bookkeeping (requested, remaining, travelled) is FP64 in both precisions:
-// in FP32 the reference's round-off floor eps(max(1, grammage)) would exceed
-// the grammage of the 1e-7 m boundary-crossing steps.
+// A step suspended on a hard-event DCS sum (cooperative evaluation): what it
+// needs to resume.  Mixed step: a = remaining, b = travelled, c = density,
+// d = round-off floor, r0 = energy, r1 = weight, r2 = ceiling, event.
+// Straggled step: a = requested length, r0 = initial energy, r1 = event
+// energy, r2 = event grammage, r3 = density, flag = scattering.
 template <class R>
-__device__ void mixed_step(const Med<R>& m, const Consts& C, State<R>& s, double density,
-                           double distance, Stream& g, R energy_limit) {
+struct Cont {
+  double a, b, c, d;
+  R r0, r1, r2, r3;
+  int event, kind, medium, flag;
+  double anc, q, denom;  // the pending event: ancestor, energy transfer, weight denominator
+  int details;
+  double total;          // answer: DCS sum and picked component
+  int pick;
+};
+enum : int { CONT_NONE = 0, CONT_MIXED = 1, CONT_STRAG = 2 };
+
+// transport_mixed_step (src/MixedTransport.jl:144-200), resumable.  The
+// grammage bookkeeping (requested, remaining, travelled) is FP64 in both
+// precisions: in FP32 the reference's round-off floor eps(max(1, grammage))
+// would exceed the grammage of the 1e-7 m boundary-crossing steps.
+template <class R>
+__device__ void mixed_end(State<R>& s, const Cont<R>& x, R Emax, R energy_limit, bool exhausted) {
+  if (exhausted) s.status |= ST_EVENT_CAP;
+  if (x.r1 > R(0) && x.r0 >= Emax && x.a > x.d && (energy_limit < R(0) || x.r0 < energy_limit))
+    s.status |= ST_DOMAIN_HI;
+  double d = x.b / x.c;
+  s.E = x.r0;
+  s.w = x.r1;
+  s.x -= d * double(s.ux);
+  s.y -= d * double(s.uy);
+  s.z -= d * double(s.uz);
+}
+// Applies a hard event; true when the history's weight vanished.
+template <class R>
+__device__ __forceinline__ bool mixed_event(State<R>& s, Cont<R>& x, const DelOut& d) {
+  x.r0 = R(d.energy);
+  x.r1 = R(double(x.r1) * d.weight);
+  if (!(isfinite(x.r1) && x.r1 >= R(0))) s.status |= ST_BAD_WEIGHT;
+  return x.r1 == R(0);
+}
+// Runs the event loop from x.event; returns true when it suspended on a DCS sum.
+template <class R, bool COOP>
+__device__ __noinline__ bool mixed_run(const Med<R>& m, const Consts& C, State<R>& s, Cont<R>& x, Stream& g,
+                          R energy_limit) {
   const int nk = m.nk;
   const R* kE = m.kcol(K_E);
-  R k = s.E;
   const R Emax = kE[nk - 1];
-  double remaining = distance * density, travelled = 0.0;
-  R weight = s.w;
-  R ceiling = energy_limit > R(0) ? fmin(energy_limit, Emax) : Emax;
-  if (s.E > Emax) {
-    s.status |= ST_DOMAIN_HI;
-    return;
-  }
-  const R mass = R(C.mass), ctau = R(C.ctau), rdens = R(density);
-  bool exhausted = true;
-  const double dXreq = fmax(1.0, distance * density);
-  const double tol = ulp_up(dXreq);
-  for (int event = 0; event < 100000; ++event) {
-    if (remaining <= tol || k >= ceiling) {
-      exhausted = false;
-      break;
+  const R mass = R(C.mass), ctau = R(C.ctau), rdens = R(x.c);
+  for (; x.event < 100000; ++x.event) {
+    R k = x.r0;
+    if (x.a <= x.d || k >= x.r2) {
+      mixed_end(s, x, Emax, energy_limit, false);
+      return false;
     }
     KLoc<R> Lk = klocate(kE, nk, k, &s.status);
     R ri = kat(m.kcol(K_R), nk, Lk), hi = kat(m.kcol(K_H), nk, Lk);
-    R rtc = fmax(R(0), klookup(m, K_E, K_R, ceiling, &s.status) - ri);
-    double eg = fmin(remaining, double(rtc));
-    R endpoint = eg == double(rtc) ? ceiling
+    R rtc = fmax(R(0), klookup(m, K_E, K_R, x.r2, &s.status) - ri);
+    double eg = fmin(x.a, double(rtc));
+    R endpoint = eg == double(rtc) ? x.r2
                                    : fmax(k, klookup(m, K_R, K_E, R(double(ri) + eg), &s.status));
     R eventh = hi + expo<R>(g);
     bool occurs = eventh < klookup(m, K_E, K_H, endpoint, &s.status);
@@ -426,37 +541,55 @@ __device__ void mixed_step(const Med<R>& m, const Consts& C, State<R>& s, double
     R dx = R(dxd);
     R dt;
     if (dx <= R(8) * ulp_up(fabs(ri)) || pre - k <= R(8) * ulp_up(fabs(k)))
-      dt = R(dxd / density) * mass / R(2) *
+      dt = R(dxd / x.c) * mass / R(2) *
            (R(1) / sqrt(k * (k + R(2) * mass)) + R(1) / sqrt(pre * (pre + R(2) * mass)));
     else
       dt = (kat(m.kcol(K_T), nk, Lp) - kat(m.kcol(K_T), nk, Lk)) / rdens;
-    weight *= kat(m.kcol(K_S), nk, Lp) / kat(m.kcol(K_S), nk, Lk) * exp(-dt / ctau);
-    travelled += dxd;
-    remaining = fmax(0.0, remaining - dxd);
-    k = pre;
-    if (occurs) {
-      DelOut d = reverse_del(m, C, double(k), g, false, &s.status);
-      k = R(d.energy);
-      weight = R(double(weight) * d.weight);
-      if (!(isfinite(weight) && weight >= R(0))) s.status |= ST_BAD_WEIGHT;
-      if (weight == R(0)) {
-        exhausted = false;
-        break;
+    x.r1 *= kat(m.kcol(K_S), nk, Lp) / kat(m.kcol(K_S), nk, Lk) * exp(-dt / ctau);
+    x.b += dxd;
+    x.a = fmax(0.0, x.a - dxd);
+    x.r0 = pre;
+    if (!occurs) {
+      mixed_end(s, x, Emax, energy_limit, false);
+      return false;
+    }
+    DelOut d;
+    if (COOP) {
+      if (del_begin(m, C, double(pre), g, &s.status, &d, &x.anc, &x.denom)) {
+        x.q = x.anc - double(pre);
+        x.details = 0;
+        return true;
       }
     } else {
-      exhausted = false;
-      break;
+      d = reverse_del(m, C, double(pre), g, false, &s.status);
+    }
+    if (mixed_event(s, x, d)) {
+      mixed_end(s, x, Emax, energy_limit, false);
+      return false;
     }
   }
-  if (exhausted) s.status |= ST_EVENT_CAP;
-  if (weight > R(0) && k >= Emax && remaining > tol && (energy_limit < R(0) || k < energy_limit))
+  mixed_end(s, x, Emax, energy_limit, true);
+  return false;
+}
+// Starts a mixed step of `distance` m at `density`; true when it suspended.
+template <class R, bool COOP>
+__device__ bool mixed_step(const Med<R>& m, const Consts& C, State<R>& s, double density,
+                           double distance, Stream& g, R energy_limit, Cont<R>& x) {
+  const R Emax = m.kcol(K_E)[m.nk - 1];
+  if (s.E > Emax) {
     s.status |= ST_DOMAIN_HI;
-  double d = travelled / density;
-  s.E = k;
-  s.w = weight;
-  s.x -= d * double(s.ux);
-  s.y -= d * double(s.uy);
-  s.z -= d * double(s.uz);
+    return false;
+  }
+  x.a = distance * density;
+  x.b = 0.0;
+  x.c = density;
+  const double dXreq = fmax(1.0, distance * density);
+  x.d = ulp_up(dXreq);
+  x.r0 = s.E;
+  x.r1 = s.w;
+  x.r2 = energy_limit > R(0) ? fmin(energy_limit, Emax) : Emax;
+  x.event = 0;
+  return mixed_run<R, COOP>(m, C, s, x, g, energy_limit);
 }
 
 // ------------------------------------------------------------ straggling
@@ -475,7 +608,7 @@ __device__ __forceinline__ R truncated_randn(Stream& g) {
 
 // fluctuate_energy_loss, backward (src/Straggling.jl:103-173, :1046-1105).
 template <class R>
-__device__ R fluctuate(const Med<R>& m, R ki, const Loc<R>& Li, R dX, R Xtot, Stream& g,
+__device__ __noinline__ R fluctuate(const Med<R>& m, R ki, const Loc<R>& Li, R dX, R Xtot, Stream& g,
                        R* ratio_out) {
   R k1 = inv_range(m, MC_MR, Xtot + dX);
   R dk0 = fabs(ki - k1), ratio = R(1);
@@ -512,7 +645,7 @@ __device__ R fluctuate(const Med<R>& m, R ki, const Loc<R>& Li, R dX, R Xtot, St
 
 // sample_ehs_event, backward (src/Straggling.jl:373-434, :1284-1334).
 template <class R>
-__device__ bool ehs_event(const Med<R>& m, R ki, R kf, R dX, R Xtot, R ratio, Stream& g, R mass,
+__device__ __noinline__ bool ehs_event(const Med<R>& m, R ki, R kf, R dX, R Xtot, R ratio, Stream& g, R mass,
                           R eratio, R* X_ehs, R* k_ehs) {
   R kmin = fmin(ki, kf), kmax = fmax(ki, kf);
   if (kmin < R(0.001)) {
@@ -577,9 +710,49 @@ __device__ __noinline__ double scattering_angle(const Med<R>& m, double mass, do
   return fmin(fmax(mu, 0.0), 1.0);
 }
 
+// FP32 form of scattering_angle for the mixed-precision transport.  The CM
+// kinetic energy uses the exact identity s - (m + M)^2 = 2 K M instead of the
+// difference (which cancels in FP32 at low energy).
+__device__ __noinline__ float scattering_angle_f(const Med<float>& m, float mass, float K,
+                                                 Stream& g) {
+  Loc<float> L = locate(m, K);
+  float p2 = K * (K + 2.f * mass);
+  float mu0 = fmaxf(at(m, L, MC_MU0), 1e-12f);
+  float zoa = m.ZoA;
+  float At = zoa > 0.f ? 1.f / zoa : 22.f, Mt = At * float(kNeutronMass);
+  float s = mass * mass + Mt * Mt + 2.f * (K + mass) * Mt, rs = sqrtf(s);
+  float K0 = K * Mt / rs;
+  float Ecm = K0 + mass, pcm = sqrtf(fmaxf(K0 * (K0 + 2.f * mass), 0.f));
+  float El = K + mass, pl = sqrtf(fmaxf(p2, 0.f));
+  float gCM = (pl > 0.f && pcm > 0.f) ? (El * Ecm + pl * pcm) / (mass * rs) : 1.f;
+  float tau = (pl > 0.f && pcm > 0.f) ? (El * pcm - Ecm * pl) / (pl * pcm) : 0.f;
+  float A = mu0 * 0.25f, fs = at(m, L, MC_FSPIN);
+  float Apm = A + mu0, Ap1 = A + 1.f, omm = 1.f - mu0, mu1 = mu0;
+  for (int it = 0; it < 100; ++it) {
+    float zeta = uni<float>(g);
+    float tmp = Ap1 - zeta * omm;
+    if (tmp <= 0.f) continue;
+    float tr = fminf(fmaxf(Apm * Ap1 / tmp - A, mu0), 1.f);
+    if (uni<float>(g) <= 1.f - fs * tr) {
+      mu1 = tr;
+      break;
+    }
+  }
+  float mu;
+  if (mu1 > 1e-6f) {
+    float a = gCM * (tau + 1.f - 2.f * mu1);
+    float ct = a / sqrtf(4.f * mu1 * (1.f - mu1) + a * a);
+    mu = 0.5f * (1.f - ct);
+  } else {
+    float d = gCM * (1.f + tau);
+    mu = mu1 / (d * d);
+  }
+  return fminf(fmaxf(mu, 0.f), 1.f);
+}
+
 // sample_soft_scattering (src/Straggling.jl:539-590, :1204-1253).
 template <class R>
-__device__ R soft_scattering(const Med<R>& m, const Loc<R>& L0, R k1, R step, R density,
+__device__ __noinline__ R soft_scattering(const Med<R>& m, const Loc<R>& L0, R k1, R step, R density,
                              Stream& g) {
   if (step <= R(0) || density <= R(0)) return R(0);
   R lb0 = transport_path(m, L0);
@@ -605,7 +778,7 @@ __device__ R soft_scattering(const Med<R>& m, const Loc<R>& L0, R k1, R step, R 
 
 // rotate_direction (src/Straggling.jl:645-710).
 template <class R>
-__device__ void rotate(State<R>& s, R mu, Stream& g) {
+__device__ __noinline__ void rotate(State<R>& s, R mu, Stream& g) {
   R ct = R(1) - R(2) * mu, st2 = R(4) * mu * (R(1) - mu);
   if (st2 <= R(0)) return;
   R st = sqrt(st2), d0 = s.ux, d1 = s.uy, d2 = s.uz;
@@ -700,10 +873,54 @@ __device__ __forceinline__ double polar_ioni(double m, double ki, double kf) {
   return 0.5 * (1.0 - c);
 }
 
-// transport_backward_step_full, mode :straggled (src/Geometry.jl:148-357).
+// transport_backward_step_full, mode :straggled (src/Geometry.jl:148-357):
+// straggled_end completes a step from its energy-loss and event decisions.
 template <class R>
-__device__ void straggled_step(const Med<R>& m, const Consts& C, State<R>& s, const Loc<R>& Li,
-                               R density, double step, Stream& g, bool scattering, R energy_limit) {
+__device__ __noinline__ void straggled_end(const Med<R>& m, const Consts& C, State<R>& s, const Loc<R>& Li,
+                              R ki, R kf, R ckf, R dX, double dw, int proc, int elem, bool del,
+                              bool ehs, R k_ehs, R density, double step, bool shortened,
+                              bool scattering, Stream& g) {
+  const R mass = R(C.mass);
+  R astep = dX / density;
+  R ox = s.ux, oy = s.uy, oz = s.uz;  // the position moves along the incoming direction
+  if (scattering) {
+    if (del && proc > 0) {
+      const double* e = m.el + kElStride * elem;
+      double mu = proc == 1 || proc == 2 ? polar_brems(C.mass, double(kf), double(ckf), e[4], g)
+                  : proc == 3            ? polar_photo(C.mass, double(kf), double(ckf), g)
+                                         : polar_ioni(C.mass, double(kf), double(ckf));
+      if (mu > 0.0) rotate(s, R(mu), g);
+    }
+    if (ehs) {
+      R mu;
+      if constexpr (sizeof(R) == 4) mu = scattering_angle_f(m, mass, k_ehs, g);
+      else mu = R(scattering_angle(m, C.mass, double(k_ehs), g));
+      if (mu > R(0)) rotate(s, mu, g);
+    }
+    R mu = soft_scattering(m, Li, ckf, astep, density, g);
+    if (mu > R(0)) rotate(s, mu, g);
+  }
+  R pt = astep * mass / R(2) *
+         (R(1) / sqrt(ki * (ki + R(2) * mass)) + R(1) / sqrt(ckf * (ckf + R(2) * mass)));
+  // FP64: the reference's dX/density; FP32: the requested FP64 step unless
+  // an event or the energy limit shortened it
+  double da = double(astep);
+  if (sizeof(R) == 4) da = shortened ? double(dX) / double(density) : step;
+  s.x -= da * double(ox);
+  s.y -= da * double(oy);
+  s.z -= da * double(oz);
+  R wf = at(m, locate(m, ckf), MC_MS) / at(m, Li, MC_MS);
+  s.w = R(double(s.w * wf * exp(-pt / R(C.ctau))) * dw);
+  s.E = kf;
+}
+
+// The step up to its hard-event decision; true when it suspended on the
+// event's DCS sum (cooperative evaluation), with x holding what straggled_end
+// needs.
+template <class R, bool COOP>
+__device__ bool straggled_step(const Med<R>& m, const Consts& C, State<R>& s, const Loc<R>& Li,
+                               R density, double step, Stream& g, bool scattering, R energy_limit,
+                               Cont<R>& x) {
   const R mass = R(C.mass), eratio = R(C.elastic_ratio);
   R ki = s.E, dX = R(step) * density;
   bool shortened = false;  // the step ended before its requested length
@@ -754,8 +971,23 @@ __device__ void straggled_step(const Med<R>& m, const Consts& C, State<R>& s, co
   R ckf = kf;
   int proc = 0, elem = -1;
   if (del) {
+    DelOut d;
+    if (COOP) {
+      if (del_begin(m, C, double(k_del), g, &s.status, &d, &x.anc, &x.denom)) {
+        x.q = x.anc - double(k_del);
+        x.details = 1;
+        x.a = step;
+        x.r0 = ki;
+        x.r1 = k_del;
+        x.r2 = X_del;
+        x.r3 = density;
+        x.flag = scattering;
+        return true;
+      }
+    } else {
+      d = reverse_del(m, C, double(k_del), g, true, &s.status);
+    }
     ckf = k_del;
-    DelOut d = reverse_del(m, C, double(k_del), g, true, &s.status);
     kf = R(d.energy);
     dw = d.weight;
     proc = d.process;
@@ -769,35 +1001,9 @@ __device__ void straggled_step(const Med<R>& m, const Consts& C, State<R>& s, co
     dX = X_ehs;
     shortened = true;
   }
-  R astep = dX / density;
-  R ox = s.ux, oy = s.uy, oz = s.uz;  // the position moves along the incoming direction
-  if (scattering) {
-    if (del && proc > 0) {
-      const double* e = m.el + kElStride * elem;
-      double mu = proc == 1 || proc == 2 ? polar_brems(C.mass, double(kf), double(ckf), e[4], g)
-                  : proc == 3            ? polar_photo(C.mass, double(kf), double(ckf), g)
-                                         : polar_ioni(C.mass, double(kf), double(ckf));
-      if (mu > 0.0) rotate(s, R(mu), g);
-    }
-    if (ehs) {
-      double mu = scattering_angle(m, C.mass, double(k_ehs), g);
-      if (mu > 0.0) rotate(s, R(mu), g);
-    }
-    R mu = soft_scattering(m, Li, ckf, astep, density, g);
-    if (mu > R(0)) rotate(s, mu, g);
-  }
-  R pt = astep * mass / R(2) *
-         (R(1) / sqrt(ki * (ki + R(2) * mass)) + R(1) / sqrt(ckf * (ckf + R(2) * mass)));
-  // FP64: the reference's dX/density; FP32: the requested FP64 step unless
-  // an event or the energy limit shortened it
-  double da = double(astep);
-  if (sizeof(R) == 4) da = shortened ? double(dX) / double(density) : step;
-  s.x -= da * double(ox);
-  s.y -= da * double(oy);
-  s.z -= da * double(oz);
-  R wf = at(m, locate(m, ckf), MC_MS) / at(m, Li, MC_MS);
-  s.w = R(double(s.w * wf * exp(-pt / R(C.ctau))) * dw);
-  s.E = kf;
+  straggled_end(m, C, s, Li, ki, kf, ckf, dX, dw, proc, elem, del, ehs, k_ehs, density, step,
+                shortened, scattering, g);
+  return false;
 }
 
 // Deterministic CSDA step on a medium (src/Geometry.jl:424-457).
@@ -828,29 +1034,52 @@ struct Hist {
   double thick, rho, H, q, ws;
   int steps, inner, outer;
   bool need_mode, strag, mixed, scat;
+  Cont<R> x;     // suspended step, if x.kind != CONT_NONE
 };
 
-// Advances a history by one transport step.  Returns true when it has ended.
+enum : int { ADV_STEP = 0, ADV_DONE = 1, ADV_WAIT = 2, ADV_HANDOFF = 3 };
+
+// The transport runs in two persistent phases: PHASE 0 below the mode switch
+// (straggled or CSDA steps), PHASE 1 above it (mixed or CSDA steps).  The
+// energy never decreases in backward transport, so a history crosses the
+// switch once; phase 0 hands it over (ADV_HANDOFF) through a queue in HBM.
+// Each phase's loop then holds one step type, not all of them.
+
+// Bookkeeping after a completed step.
 template <class R>
-__device__ __forceinline__ bool advance(const Med<R>& rock, const Med<R>& air, const Consts& C,
-                                        Hist<R>& h, Stream& g) {
+__device__ __forceinline__ int step_done(Hist<R>& h) {
+  ++h.inner;
+  if (++h.steps > 2000000) h.s.status |= ST_STEP_CAP;
+  return (h.s.status & ST_FATAL) != 0 ? ADV_DONE : ADV_STEP;
+}
+
+// Advances a history by one transport step: ADV_STEP, ADV_DONE when it has
+// ended, ADV_WAIT when the step suspended on a hard-event DCS sum.
+template <class R, bool COOP, int PHASE>
+__device__ __forceinline__ int advance(const Med<R>& rock, const Med<R>& air, const Consts& C,
+                                       Hist<R>& h, Stream& g) {
   const double eps = kEps64;
   State<R>& s = h.s;
   for (int guard = 0; guard < 4; ++guard) {
     if (h.need_mode) {
-      if (!(double(s.E) < C.thr - eps)) return true;
+      if (!(double(s.E) < C.thr - eps)) return ADV_DONE;
       if (h.outer >= 1000) {
         s.status |= ST_OUTER_CAP;
-        return true;
+        return ADV_DONE;
       }
-      if (s.z < 0.0 || s.z >= h.H - eps) return true;
-      if (!(s.w > R(0)) || !isfinite(s.w)) return true;
+      if (s.z < 0.0 || s.z >= h.H - eps) return ADV_DONE;
+      if (!(s.w > R(0)) || !isfinite(s.w)) return ADV_DONE;
       if (double(s.E) < C.thr_low - eps) {
+        if (PHASE == 1) {  // not reached: the energy never decreases
+          s.status |= ST_OUTER_CAP;
+          return ADV_DONE;
+        }
         h.strag = C.straggling != 0;
         h.mixed = false;
         h.scat = C.scattering != 0;
         h.limit = fmin(C.thr_low, C.thr);
       } else {
+        if (PHASE == 0) return ADV_HANDOFF;  // need_mode stays set for phase 1
         h.strag = false;
         h.mixed = C.straggling != 0;
         h.scat = false;
@@ -888,17 +1117,133 @@ __device__ __forceinline__ bool advance(const Med<R>& rock, const Med<R>& air, c
     if (in_air) lim = fmin(lim, R(0.05 * 12e3) / fmax(R(fabs(uz)), R(0.05)));
     double step = fmin(tob + 1e-7, double(lim));
     step = fmin(fmax(step, kStepMin), 1000.0);
-    if (h.strag) straggled_step(m, C, s, Li, rd, step, g, h.scat, R(h.limit));
-    else if (h.mixed) mixed_step(m, C, s, dens, step, g, R(h.limit));
-    else csda_step(m, C, s, Li, rd, step);
-    ++h.inner;
-    if (++h.steps > 2000000) s.status |= ST_STEP_CAP;
-    return (s.status & ST_FATAL) != 0;
+    if (PHASE == 0 && h.strag) {
+      if constexpr (PHASE == 0) {
+        if (straggled_step<R, COOP>(m, C, s, Li, rd, step, g, h.scat, R(h.limit), h.x)) {
+          h.x.kind = CONT_STRAG;
+          h.x.medium = in_air;
+          return ADV_WAIT;
+        }
+      }
+    } else if (PHASE == 1 && h.mixed) {
+      if constexpr (PHASE == 1) {
+        if (mixed_step<R, COOP>(m, C, s, dens, step, g, R(h.limit), h.x)) {
+          h.x.kind = CONT_MIXED;
+          h.x.medium = in_air;
+          return ADV_WAIT;
+        }
+      }
+    } else {
+      csda_step(m, C, s, Li, rd, step);
+    }
+    return step_done(h);
   }
   // The mode checks alternate without a step only if the thresholds were not
   // representable in R (the host rounds them); end the history flagged.
   s.status |= ST_OUTER_CAP;
-  return true;
+  return ADV_DONE;
+}
+
+// Resumes a suspended step once h.x.total (and h.x.pick) hold the DCS sum.
+template <class R, int PHASE>
+__device__ int resume(const Med<R>& rock, const Med<R>& air, const Consts& C, Hist<R>& h,
+                      Stream& g) {
+  Cont<R>& x = h.x;
+  const Med<R>& m = x.medium ? air : rock;
+  x.kind = CONT_NONE;
+  DelOut d = del_end(x.anc, x.denom, x.total, x.pick);
+  if constexpr (PHASE == 1) {
+    const R Emax = m.kcol(K_E)[m.nk - 1];
+    if (mixed_event(h.s, x, d)) {
+      mixed_end(h.s, x, Emax, R(h.limit), false);
+    } else {
+      ++x.event;
+      if (mixed_run<R, true>(m, C, h.s, x, g, R(h.limit))) {
+        x.kind = CONT_MIXED;
+        return ADV_WAIT;
+      }
+    }
+  } else {
+    Loc<R> Li = locate(m, x.r0);
+    straggled_end(m, C, h.s, Li, x.r0, R(d.energy), x.r1, x.r2, d.weight, d.process, d.element,
+                  true, false, R(0), x.r3, x.a, true, x.flag != 0, g);
+  }
+  return step_done(h);
+}
+
+// A history handed from phase 0 to phase 1: its state, geometry, loop
+// counters and random stream position.
+template <class R>
+struct Handoff {
+  double x, y, z, thick, rho, H, q, ws;
+  R ux, uy, uz, E, w;
+  int status, steps, outer, used;
+  uint32_t block, w0, w1, w2, w3;
+  long index;       // history index (output slot)
+  uint64_t stream;  // stream id
+};
+template <class R>
+__device__ __forceinline__ void save_handoff(const Hist<R>& h, const Stream& g, long i,
+                                             Handoff<R>* o) {
+  Handoff<R> v;
+  v.x = h.s.x;
+  v.y = h.s.y;
+  v.z = h.s.z;
+  v.thick = h.thick;
+  v.rho = h.rho;
+  v.H = h.H;
+  v.q = h.q;
+  v.ws = h.ws;
+  v.ux = h.s.ux;
+  v.uy = h.s.uy;
+  v.uz = h.s.uz;
+  v.E = h.s.E;
+  v.w = h.s.w;
+  v.status = h.s.status;
+  v.steps = h.steps;
+  v.outer = h.outer;
+  v.used = g.used;
+  v.block = g.block;
+  v.w0 = g.w0;
+  v.w1 = g.w1;
+  v.w2 = g.w2;
+  v.w3 = g.w3;
+  v.index = i;
+  v.stream = uint64_t(g.c0) | (uint64_t(g.c1) << 32);
+  *o = v;
+}
+template <class R>
+__device__ __forceinline__ long load_handoff(const Handoff<R>& v, uint64_t seed, Hist<R>& h,
+                                             Stream& g) {
+  h.s.x = v.x;
+  h.s.y = v.y;
+  h.s.z = v.z;
+  h.thick = v.thick;
+  h.rho = v.rho;
+  h.H = v.H;
+  h.q = v.q;
+  h.ws = v.ws;
+  h.s.ux = v.ux;
+  h.s.uy = v.uy;
+  h.s.uz = v.uz;
+  h.s.E = v.E;
+  h.s.w = v.w;
+  h.s.status = v.status;
+  h.steps = v.steps;
+  h.outer = v.outer;
+  h.inner = 0;
+  h.limit = 0.0;
+  h.need_mode = true;
+  h.strag = h.mixed = h.scat = false;
+  h.x.kind = CONT_NONE;
+  g.init(seed, v.stream);
+  g.block = v.block;
+  g.used = v.used;
+  g.w0 = v.w0;
+  g.w1 = v.w1;
+  g.w2 = v.w2;
+  g.w3 = v.w3;
+  return v.index;
 }
 
 // Contribution of an ended history (src/Geometry.jl:729-757), FP64.

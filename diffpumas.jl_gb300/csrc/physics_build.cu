@@ -144,6 +144,323 @@ double dcs_moment(int proc, double Z, double A, double I, double mass, double K,
   return s * kAvogadro / (A * 1e-3);
 }
 
+// ------------------------------------------------------------ Coulomb tables
+// src/Coulomb.jl: Salvat's screened Coulomb DCS (three exponentials plus a
+// nuclear-size term), reduced to simple poles, with the KTV Born correction;
+// the first transport path adds the electronic transverse transport and the
+// radiative soft-scattering integrals below the cutoff.
+
+// Nuclear radius by the reference's C-index rule (src/Coulomb.jl:166-181):
+// hydrogen with A >= 1.5 uses the first entry, the standard-rock pseudo
+// element (Z 11, A 22) the last one.
+double nuclear_radius(double Z, double A) {
+  const int nN = 120;
+  int iN = int(Z);
+  if (iN >= nN - 1) iN = nN - 2;
+  else if (iN == 1 && A >= 1.5) iN = 0;
+  else if (iN == 11 && A == 22.0) iN = nN - 1;
+  return DPDATA_NUCLEAR_RADII_FM[iN] * 1e-15;
+}
+
+// Centre-of-mass frame of the muon-nucleus collision (src/Coulomb.jl:192-206).
+void cm_frame(double Z, double A, double mass, double K, double* K0, double* gCM, double* tau) {
+  double Ma = Z * kProtonMass + (A - Z) * kNeutronMass;
+  double s12i = 1.0 / std::sqrt((mass + Ma) * (mass + Ma) + 2.0 * Ma * K);
+  *gCM = (K + mass + Ma) * s12i;
+  double k0 = (K * Ma + mass * (mass + Ma)) * s12i - mass;
+  *K0 = k0 < 1e-9 ? 1e-9 : k0;
+  double et = K + mass + Ma, b2 = K * (K + 2.0 * mass) / (et * et), rm = mass / Ma;
+  *tau = std::sqrt(rm * rm * (1.0 - b2) + b2);
+}
+
+// Inverse of the DCS normalisation per unit mass (src/Coulomb.jl:211-217).
+double cm_normalisation(double Z, double A, double mass, double K, double K0) {
+  double p2 = K * (K + 2.0 * mass), p02 = K0 * (K0 + 2.0 * mass);
+  double d = kAlpha * Z * kHbarC * (K + mass);
+  return A * 1e-3 * p2 * p02 / (d * d * kPi * kAvogadro);
+}
+
+// Screening amplitudes and parameters; the last parameter is the nuclear
+// term (src/Coulomb.jl:224-289).
+struct Screening {
+  int n = 0;
+  double amp[4] = {0, 0, 0, 0}, par[5] = {0, 0, 0, 0, 0};
+};
+Screening screening(double Z, double A, double mass, double K, double K0) {
+  double aZE = kAlpha * Z * (K + mass), z2 = aZE * aZE / (K * (K + 2.0 * mass)), f;
+  if (z2 < 1.0) {
+    f = z2 * (1.0 / (1.0 + z2) + 0.20205690315959424 - 0.03692775514336999 * z2 +
+              0.008349277381922926 * z2 * z2);
+  } else {
+    double r2i = 1.0 / (1.0 + z2), phi = -std::atan(std::sqrt(z2));
+    f = -0.5 * std::log(r2i) + 0.5 * (1.0 - r2i) + (1.0 - std::cos(2 * phi) * r2i) / 12.0 -
+        (1.0 - std::cos(4 * phi) * r2i * r2i) / 120.0 +
+        (1.0 - std::cos(6 * phi) * r2i * r2i * r2i) / 252.0;
+  }
+  double d = 0.25 * kHbarC * kHbarC / (K0 * (K0 + 2.0 * mass)) * std::exp(2.0 * f);
+  int iZ = std::min(std::max(int(Z) - 1, 0), 102);
+  Screening s;
+  int n;
+  if (DPDATA_SALVAT_EXPONENT2[iZ] == 1.0) {
+    n = iZ == 0 ? 1 : 2;
+    s.amp[0] = iZ == 0 ? 1.0 : DPDATA_SALVAT_PREFACTOR0[iZ];
+    if (n == 2) s.amp[1] = 1.0 - s.amp[0];
+  } else {
+    n = 3;
+    s.amp[0] = DPDATA_SALVAT_PREFACTOR0[iZ];
+    s.amp[1] = DPDATA_SALVAT_PREFACTOR1[iZ];
+    s.amp[2] = 1.0 - (s.amp[0] + s.amp[1]);
+  }
+  const double* ex[3] = {DPDATA_SALVAT_EXPONENT0, DPDATA_SALVAT_EXPONENT1, DPDATA_SALVAT_EXPONENT2};
+  for (int i = 0; i < n; ++i) {
+    double a = ex[i][iZ] / kBohrRadius;
+    s.par[i] = d * a * a;
+  }
+  double RN = nuclear_radius(Z, A);
+  s.par[n] = 12.0 * d / (RN * RN);
+  s.n = n + 1;
+  return s;
+}
+
+// Partial fractions of the screened DCS times the nuclear form factor
+// (src/Coulomb.jl:292-348).
+struct Poles {
+  double a[3] = {0, 0, 0}, b[3] = {0, 0, 0}, c[4] = {0, 0, 0, 0};
+};
+Poles poles(const Screening& s) {
+  Poles P;
+  const int n = s.n - 1;
+  for (int i = 0; i < n; ++i) {
+    P.b[i] = s.amp[i] * s.amp[i];
+    for (int j = i + 1; j < n; ++j) {
+      double d = 2.0 * s.amp[i] * s.amp[j] / (s.par[j] - s.par[i]);
+      P.a[i] += d;
+      P.a[j] -= d;
+    }
+  }
+  const double N = s.par[n];
+  double Sa[4] = {0, 0, 0, 0}, Sb[4] = {0, 0, 0, 0};
+  for (int i = 0; i < n; ++i) {
+    double x = 1.0 - s.par[i] / N, r = x;
+    for (int j = 0; j < 4; ++j) {
+      Sa[j] += P.a[i] / r;
+      r *= x;
+      Sb[j] += P.b[i] / r;
+    }
+  }
+  double t = 1.0;
+  for (int i = 0; i < 4; ++i) {
+    P.c[i] = ((4 - i) * Sb[3 - i] / N - Sa[3 - i]) * t;
+    t *= N;
+  }
+  for (int i = 0; i < n; ++i) {
+    double dd = 1.0 - s.par[i] / N, d4 = dd * dd * dd * dd;
+    P.a[i] = (P.a[i] - 4.0 * P.b[i] / (N - s.par[i])) / d4;
+    P.b[i] /= d4;
+  }
+  return P;
+}
+
+// Zeroth and (twice the) first transport coefficients of the cross section
+// restricted to deflections below mu, spin factor S (src/Coulomb.jl:350-406).
+void transport_coefs(double mu, double S, const Screening& s, const Poles& P, double* c0,
+                     double* c1x2) {
+  const int n = s.n - 1;
+  double t0 = 0, t1 = 0;
+  for (int i = 0; i < n; ++i) {
+    double al = s.par[i], r = mu / (mu + al), L = std::log(1.0 + mu / al);
+    double I0 = r / al, J0 = L, I1 = L - r, J1 = -al * L, I2 = mu + al * (r - 2.0 * L);
+    double J2 = al * (al * L - mu);
+    t0 += P.a[i] * (J0 - S * J1) + P.b[i] * (I0 - S * I1);
+    t1 += P.a[i] * (J1 - S * J2) + P.b[i] * (I1 - S * I2);
+  }
+  const double N = s.par[n], r = mu / (mu + N), L = std::log(1.0 + mu / N);
+  double I0 = r / N, J0 = L, I1 = L - r, J1 = -N * L, I2 = mu + N * (r - 2.0 * L),
+         J2 = N * (N * L - mu);
+  double rn = 1.0 / (1.0 + mu / N);
+  double K0 = (1.0 - rn) * (1.0 + rn) / (2.0 * N * N);
+  double L0 = (1.0 - rn) * ((1.0 + rn) * (1.0 + rn) - rn) / (3.0 * N * N * N);
+  double K1 = I0 - N * K0, L1 = K0 - N * L0, K2 = I1 - N * K1, L2 = K1 - N * L1;
+  t0 += P.c[0] * (J0 - S * J1) + P.c[1] * (I0 - S * I1) + P.c[2] * (K0 - S * K1) +
+        P.c[3] * (L0 - S * L1);
+  t1 += P.c[0] * (J1 - S * J2) + P.c[1] * (I1 - S * I2) + P.c[2] * (K1 - S * K2) +
+        P.c[3] * (L1 - S * L2);
+  *c0 = t0;
+  *c1x2 = 2.0 * t1;
+}
+
+// Cross section of deflections above mu (src/Coulomb.jl:409-417).
+double hard_cs(double mu, double S, const Screening& s, const Poles& P) {
+  if (mu >= 1.0 || mu >= 1e6 * s.par[s.n - 1]) return 0.0;
+  double f0, f1, m0, m1;
+  transport_coefs(1.0, S, s, P, &f0, &f1);
+  transport_coefs(mu, S, s, P, &m0, &m1);
+  return m0 > f0 ? 0.0 : f0 - m0;
+}
+
+// Ridder's root bracketing (src/Coulomb.jl:428-471).
+template <class F>
+double ridder(F f, double xa, double xb, double fa, double fb, double xtol, double rtol,
+              int maxiter) {
+  if (fa * fb > 0) return 0.0;
+  if (fa == 0) return xa;
+  if (fb == 0) return xb;
+  double tol = xtol + rtol * std::min(std::fabs(xa), std::fabs(xb)), xn = 0.0;
+  for (int it = 0; it < maxiter; ++it) {
+    double dm = 0.5 * (xb - xa), xm = xa + dm, fm = f(xm);
+    double dn = (fb > fa ? 1.0 : -1.0) * dm * fm / std::sqrt(fm * fm - fa * fb);
+    double sg = dn > 0.0 ? 1.0 : -1.0, step = std::fabs(dm) - 0.5 * tol;
+    if (std::fabs(dn) < step) step = std::fabs(dn);
+    xn = xm - sg * step;
+    double fn = f(xn);
+    if (fn * fm < 0.0) {
+      xa = xn;
+      fa = fn;
+      xb = xm;
+      fb = fm;
+    } else if (fn * fa < 0.0) {
+      xb = xn;
+      fb = fn;
+    } else {
+      xa = xn;
+      fa = fn;
+    }
+    if (fn == 0.0 || std::fabs(xb - xa) < tol) return xn;
+  }
+  return xn;
+}
+
+// Electronic transverse transport cross section (src/Coulomb.jl:493-510).
+double electronic_transport(double ZoA, double I, double aS, double mass, double K, double nu) {
+  double p2 = K * (K + 2.0 * mass), E = K + mass;
+  double Wr = 2.0 * kElectronMass * p2 / (mass * mass + kElectronMass * (kElectronMass + 2.0 * E));
+  double Wmax = std::min(nu, Wr), b2 = p2 / (E * E);
+  double J = std::log(aS * Wmax / I) - b2 * Wmax / Wr + 0.25 * Wmax * Wmax / (E * E) + 1.0 / aS;
+  double g = E / mass, lQ = std::log(1.0 + 2.0 * Wr / kElectronMass);
+  double Delta = kAlpha / (2 * kPi) * (std::log(2.0 * g) - lQ / 3.0) * lQ * lQ;
+  return 2 * kPi * kElectronRadius * kElectronRadius * kElectronMass * kElectronMass * kAvogadro *
+         ZoA / (b2 * 1e-3 * p2) * (J + Delta);
+}
+
+// Gauss-Legendre rule on [0, 1] by Newton iteration on P_n.
+struct GaussLegendre {
+  double x[20], w[20];
+  explicit GaussLegendre(int n) {
+    for (int i = 0; i < n; ++i) {
+      double z = std::cos(kPi * (i + 0.75) / (n + 0.5)), pp = 0;
+      for (int it = 0; it < 100; ++it) {
+        double p1 = 1, p2 = 0;
+        for (int j = 1; j <= n; ++j) {
+          double p3 = p2;
+          p2 = p1;
+          p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
+        }
+        pp = n * (z * p1 - p2) / (z * z - 1.0);
+        double z1 = z;
+        z = z1 - p1 / pp;
+        if (std::fabs(z - z1) < 1e-16) break;
+      }
+      x[i] = 0.5 * (1.0 - z);
+      w[i] = 1.0 / ((1.0 - z * z) * pp * pp);
+    }
+  }
+};
+
+// Angular transport integral of a radiative DCS over log q (src/Coulomb.jl:564-593).
+template <class D>
+double radiative_transport(D dcs, double Z, double A, double mass, double K, double qmin,
+                           double qmax) {
+  if (qmin >= qmax || qmin <= 0.0) return 0.0;
+  static const GaussLegendre g(20);
+  double p2 = K * (K + 2.0 * mass), lo = std::log(qmin), hi = std::log(qmax), r = 0.0;
+  for (int i = 0; i < 20; ++i) {
+    double q = std::exp(lo + (hi - lo) * g.x[i]), v = dcs(Z, A, mass, K, q);
+    if (v > 0.0) r += v * (q * q / p2) * q * (g.w[i] * (hi - lo));
+  }
+  return r;
+}
+
+// Soft radiative scattering below the cutoff (src/Coulomb.jl:595-635).
+double radiative_soft(double Z, double A, double mass, double K, double cutoff) {
+  double qmaxp = K + mass * (1.0 - 0.75 * 1.6487212707 * std::pow(Z, 1.0 / 3.0));
+  double qb = std::min(cutoff * K, qmaxp);
+  double r = radiative_transport([](double z, double a, double m, double k, double q) {
+    return dcs_brems(z, a, m, k, q); }, Z, A, mass, K, 1e-3 * qb, qb);
+  r += radiative_transport([](double z, double a, double m, double k, double q) {
+    return dcs_pair(z, a, m, k, q); }, Z, A, mass, K, std::max(4.0 * kElectronMass, 1e-3 * qb), qb);
+  double qp = cutoff * K;
+  r += radiative_transport([](double z, double a, double m, double k, double q) {
+    return dcs_photo(z, a, m, k, q); }, Z, A, mass, K, std::max(0.0, 1e-3 * qp), qp);
+  return r;
+}
+
+// compute_coulomb_tables! (src/Coulomb.jl:688-826) at one energy node:
+// first transport path lb1, elastic path x p^2 lbe, screening cutoff mu0.
+void coulomb_node(const HostMaterial& m, double mass, double elastic_ratio, double cutoff,
+                  double aS, double K, double range, double* lb1, double* lbe, double* mu0_out) {
+  if (K <= 0.0) {
+    *lb1 = *lbe = *mu0_out = 0.0;
+    return;
+  }
+  const size_t ne = m.elements.size();
+  std::vector<Screening> sc(ne);
+  std::vector<Poles> po(ne);
+  std::vector<double> fs(ne), nf(ne), d2(ne);
+  double cs_m = 0, cs1_m = 0, A_min = 1e300, cs_A = 0;
+  for (size_t k = 0; k < ne; ++k) {
+    const HostElement& el = m.elements[k];
+    double K0, gCM, tau;
+    cm_frame(el.Z, el.A, mass, K, &K0, &gCM, &tau);
+    double e = K + mass;
+    fs[k] = K * (e + mass) / (e * e);
+    sc[k] = screening(el.Z, el.A, mass, K, K0);
+    po[k] = poles(sc[k]);
+    double G0, G1;
+    transport_coefs(1.0, fs[k], sc[k], po[k], &G0, &G1);
+    nf[k] = el.fraction / cm_normalisation(el.Z, el.A, mass, K, K0);
+    cs_m += nf[k] * G0;
+    double d = 1.0 / (gCM * (1.0 + tau));
+    d2[k] = d * d;
+    cs1_m += nf[k] * G1 * d2[k];
+    for (int j = 0; j < sc[k].n - 1; ++j) A_min = std::min(A_min, sc[k].par[j]);
+    cs_A += nf[k];
+  }
+  cs_A /= A_min * (A_min + 1.0);
+  const double path_max = 1e9, max_mu0 = 0.5 * (1.0 - std::cos(kPi / 180.0));
+  double cs_h = std::max(cs1_m, range > 0.0 ? 1.0 / range : 0.0) / elastic_ratio;
+  if (cs_h < 1.0 / path_max) cs_h = 1.0 / path_max;
+  double mu0, lb_h;
+  if (cs_h < cs_m) {
+    double zeta = cs_h / cs_A;
+    double mu_max = std::min(A_min * (1.0 - zeta) / (A_min + zeta), max_mu0);
+    auto obj = [&](double mu) {
+      double t = 0;
+      for (size_t k = 0; k < ne; ++k) t += nf[k] * hard_cs(mu, fs[k], sc[k], po[k]);
+      return t - cs_h;
+    };
+    mu0 = ridder(obj, 0.0, mu_max, cs_m - cs_h, obj(mu_max), 1e-6 * mu_max, 1e-6, 100);
+    if (mu0 > max_mu0) mu0 = max_mu0;
+    cs_h += obj(mu0);
+    lb_h = cs_h <= 1.0 / path_max ? path_max : 1.0 / cs_h;
+  } else {
+    mu0 = 0.0;
+    lb_h = 1.0 / cs_m;
+  }
+  *mu0_out = mu0;
+  *lbe = lb_h * K * (K + 2.0 * mass);
+  double inv = 0;
+  for (size_t k = 0; k < ne; ++k) {
+    double G0, G1;
+    transport_coefs(mu0, fs[k], sc[k], po[k], &G0, &G1);
+    inv += nf[k] * d2[k] * G1;
+  }
+  double rad = 0;
+  for (size_t k = 0; k < ne; ++k)
+    rad += radiative_soft(m.elements[k].Z, m.elements[k].A, mass, K, cutoff) * m.elements[k].fraction;
+  double tot = inv + rad + electronic_transport(m.ZoA, m.I, aS, mass, K, cutoff * K);
+  *lb1 = tot > 0.0 ? 1.0 / tot : 0.0;
+}
+
 template <class F>
 void parallel_for(int n, F f) {
   unsigned nt = std::max(1u, std::min(std::thread::hardware_concurrency(), 64u));
@@ -158,8 +475,8 @@ void parallel_for(int n, F f) {
 
 }  // namespace
 
-// src/Physics.jl:280-408.  Columns per DP_COL_*; Coulomb columns (LB1, LBE,
-// MU0, ECUT) are left zero: the scattering tables are not built here.
+// src/Physics.jl:280-408.  Columns per DP_COL_*, the Coulomb scattering
+// columns (LB1, LBE, MU0, ECUT) included.
 void build_empirical_table(const HostMaterial& m, const dp_settings& st, int n, double Kmin,
                            double Kmax, double* cols /* DP_NCOL x n */) {
   auto C = [&](int c) { return cols + size_t(c) * n; };
@@ -210,12 +527,20 @@ void build_empirical_table(const HostMaterial& m, const dp_settings& st, int n, 
     double b = std::sqrt(1.0 - 1.0 / (g * g)), bp = std::sqrt(1.0 - 1.0 / (gp * gp));
     T[i] = T[i - 1] + dK / (((S[i] + S[i - 1]) / 2) * ((b + bp) / 2) * ((g + gp) / 2));
   }
+  // Coulomb scattering tables (src/Physics.jl:386-397)
+  const double aS = m.I * 1e9 / (28.816 * std::sqrt(m.ZoA * m.density * 1e-3));
+  parallel_for(n, [&](int i) {
+    coulomb_node(m, mass, st.elastic_ratio, cut, aS, E[i], R[i], C(DP_COL_LB1) + i,
+                 C(DP_COL_LBE) + i, C(DP_COL_MU0) + i);
+  });
   for (int i = 0; i < n; ++i) {
     double K = E[i], g = 1.0 + K / mass, b = std::sqrt(1.0 - 1.0 / (g * g));
     double p = std::sqrt(K * (K + 2 * mass)), e = K + mass;
     C(DP_COL_FSPIN)[i] = K * (e + mass) / (e * e);
     C(DP_COL_MAGROT)[i] = kLarmor / (b * p);
-    C(DP_COL_ECUT)[i] = 0.0;  // mu0 = 0 -> 2 sqrt(0)
+    double mu0 = C(DP_COL_MU0)[i];
+    C(DP_COL_ECUT)[i] = mu0 < 1e-8 ? 2.0 * std::sqrt(std::max(mu0, 0.0))
+                                   : std::acos(std::max(1.0 - 2.0 * mu0, -1.0));
   }
 }
 
