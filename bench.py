@@ -181,8 +181,8 @@ def setup_c3(dp, torch, dev, precision="mixed"):
 
 
 def _device_bytes(torch, dev, obj):
-    raw = bytes(C.string_at(C.addressof(obj), C.sizeof(obj)))
-    return torch.tensor(list(raw), dtype=torch.uint8, device=dev)
+    raw = bytearray(C.string_at(C.addressof(obj), C.sizeof(obj)))
+    return torch.frombuffer(raw, dtype=torch.uint8).to(dev)
 
 
 C2_MIX = ([1, 3, 2], [0.70, 0.25, 0.05])  # rock, water, air (1-based material indices)
@@ -236,6 +236,72 @@ def setup_c2(dp, torch, dev, precision="mixed"):
     return (lambda: run_dev(precision)), step_e2e, (lambda: run_dev("fp64")), info, phys
 
 
+def c4_los(dp, seed=4, n_los=16384):
+    rng = np.random.default_rng(seed)
+    depth = np.exp(rng.uniform(np.log(50.0), np.log(2000.0), n_los))
+    rho = rng.uniform(2400.0, 2800.0, n_los)
+    ns = rng.integers(64, 1025, n_los)
+    return dp.make_los(ns, thickness=depth, density=rho, elevation=90.0, energy_min=1.0,
+                       energy_max=1e4), int(ns.sum()), (depth, rho, ns)
+
+
+def setup_c4(dp, torch, dev, precision="mixed"):
+    """Batched backward MC over 16384 vertical lines of sight (depth
+    log-uniform 50-2000 m, density U[2400,2800], 64-1024 histories each,
+    StandardRock under air to 30 km), mixed transport everywhere (threshold at
+    the 1 GeV lowest final energy, no scattering), plus the CSDA sample-average
+    gradient per line of sight; one persistent launch per phase."""
+    phys = dp.create_physics(materials=(dp.STANDARD_ROCK, dp.AIR))
+    rock = dp.MaterialMixture(phys, 1)
+    air = dp.MaterialMixture(phys, 2)
+    los, total, _ = c4_los(dp)
+    lib = dp.load()
+    ctx = phys.ctx.h
+    cfgs = {p: dp._mc_config(2027, True, False, 1.0, None, p) for p in ("mixed", "fp64")}
+    d_los = _device_bytes(torch, dev, los)
+    d_out = torch.zeros(len(los) * C.sizeof(dp.DpLosResult), dtype=torch.uint8, device=dev)
+    n_los = len(los)
+
+    def run_dev():
+        dp.check(lib.dp_mc_los_dev(ctx, phys.h, rock.h, air.h, C.byref(cfgs[precision]), n_los,
+                                   d_los.data_ptr(), total, 1, d_out.data_ptr()), ctx)
+
+    def step_e2e():
+        r = dp.backward_mc_batch(phys, los, rock=rock, air=air, seed=2027, scattering=False,
+                                 energy_threshold_low=1.0, precision=precision,
+                                 compute_gradient=True)
+        assert r["n_status_nonzero"].sum() == 0
+
+    # plain form: FP64 transport, one launch per line of sight, on the first
+    # 16 lines (their rate stands for the batch)
+    sub = (dp.DpLos * 16)(*[los[i] for i in range(16)])
+    sub_n = sum(los[i].n_samples for i in range(16))
+    d_sub = _device_bytes(torch, dev, sub)
+    one = C.sizeof(dp.DpLos)
+
+    def plain_dev():
+        for i in range(16):
+            dp.check(lib.dp_mc_los_dev(ctx, phys.h, rock.h, air.h, C.byref(cfgs["fp64"]), 1,
+                                       d_sub.data_ptr() + i * one, sub[i].n_samples, 1,
+                                       d_out.data_ptr()), ctx)
+
+    kernel = "mc_mixed_lo+mc_mixed_hi+csda_mc32" if precision == "mixed" else \
+        "mc_fp64_lo+mc_fp64_hi+csda_mc"
+    info = {"units": total, "unit": "samples/s", "kernel": kernel,
+            # per history: contribution and status written and read back,
+            # CSDA contribution and derivative written and read back
+            "alg_bytes": total * (24 + 32), "traffic": None,
+            "config": {"workload": "c4: 16384 vertical lines of sight, depth log-uniform 50-2000 m, "
+                                   "density U[2400,2800], 64-1024 histories each (uneven), mixed "
+                                   "transport everywhere, E 1 GeV-10 TeV, + CSDA d flux/d rho per "
+                                   "line of sight",
+                       "n_los": n_los, "n_samples": total, "precision": precision},
+            "h2d": n_los * C.sizeof(dp.DpLos), "d2h": n_los * C.sizeof(dp.DpLosResult),
+            "plain_what": "FP64 transport (+ FP64 CSDA gradient), one launch per line of sight, "
+                          "first 16 lines", "plain_units": sub_n, "plain_reps": 1}
+    return run_dev, step_e2e, plain_dev, info, phys
+
+
 def setup_c1(dp, torch, dev):
     phys = dp.create_physics()
     n = 10000
@@ -266,7 +332,7 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
     import dpgpu as dp
     dp._default = dp.Context(local)
-    setup = {"c2": setup_c2, "c3": setup_c3, "c1": setup_c1}[args.workload]
+    setup = {"c2": setup_c2, "c3": setup_c3, "c4": setup_c4, "c1": setup_c1}[args.workload]
     step_dev, step_e2e, plain_dev, info, phys = setup(dp, torch, dev)
     lib = dp.load()
     ctx = phys.ctx.h
@@ -307,10 +373,12 @@ def run_gpu(args):
     barrier(world)
     launches = lib.dp_launch_count(ctx) - launches0
     kms = C.c_double(0.0)
+    breakdown = {}
     for name in info["kernel"].split("+"):  # summed over the kernels of the timed step
         k = C.c_double()
         lib.dp_kernel_time(ctx, name.encode(), C.byref(k))
         kms.value += k.value
+        breakdown[name] = k.value / args.steps
     lib.dp_set_timing(ctx, 0)
     ms = max_over_ranks(world, sum(times) / len(times))
     value = world * info["units"] / (ms * 1e-3)
@@ -338,7 +406,8 @@ def run_gpu(args):
             plain_dev()
         torch.cuda.synchronize()
         plain_ms = (time.perf_counter() - t0) * 1e3 / reps
-        plain = {"value": info["units"] / (plain_ms * 1e-3), "unit": info["unit"],
+        plain = {"value": info.get("plain_units", info["units"]) / (plain_ms * 1e-3),
+                 "unit": info["unit"],
                  "ms_per_step": plain_ms,
                  "what": info.get("plain_what", "plain FP64 one-launch-per-ray, forward only")}
 
@@ -357,7 +426,7 @@ def run_gpu(args):
                          "frac": achieved / peak if achieved else None,
                          "traffic": info.get("traffic"),
                          "kernel": info["kernel"], "kernel_ms": kernel_ms,
-                         "peak_source": peak_kind},
+                         "kernel_ms_each": breakdown, "peak_source": peak_kind},
             "gpu_launches": int(launches),
             "plain_gpu": plain,
             "speedup_vs_plain": (value / plain["value"]) if plain else None,
@@ -390,6 +459,26 @@ def cpu_baseline(workload, budget_s=15.0, threads=None):
         return {"value": n / dt, "unit": "rays/s", "cores": threads, "kind": "port",
                 "sample": f"{n} rays of the c3 workload (cycled), forward flux + reverse-sweep "
                           "J^T r (FP64 oracle, OpenMP)"}
+    if workload == "c4":
+        import dpgpu as dp
+        p = O.default_physics((O.STANDARD_ROCK, O.AIR), coulomb=True)
+        _, _, (depth, rho, ns) = c4_los(dp)
+        rng = np.random.default_rng(1)
+        n, t0, l = 0, time.perf_counter(), 0
+        while time.perf_counter() - t0 < budget_s:
+            m = int(ns[l])
+            E = np.exp(rng.uniform(0, np.log(1e4), m))
+            q = np.where(rng.uniform(size=m) > 0.5, 1.0, -1.0)
+            w = 2 * E * np.log(1e4)
+            O.mc_histories(p, [0], 1, depth[l], rho[l], 90.0, 3e4, E, q, w, seed=9, id0=n,
+                           straggling=True, scattering=False, threshold_low=1.0, threads=threads)
+            O.backward_mc_csda(p, 0, 1, depth[l], rho[l], 90.0, E, q, w, threads=threads)
+            n += m
+            l += 1
+        dt = time.perf_counter() - t0
+        return {"value": n / dt, "unit": "samples/s", "cores": threads, "kind": "port",
+                "sample": f"{l} lines of sight ({n} histories) of the c4 workload: stochastic "
+                          "transport + dual-number CSDA gradient (FP64 oracle, OpenMP)"}
     if workload == "c2":
         p = O.default_physics((O.STANDARD_ROCK, O.AIR, O.WATER), coulomb=True)
         rng = np.random.default_rng(0)
@@ -424,7 +513,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    units = {"c2": "samples/s", "c3": "rays/s", "c1": "samples/s"}[args.workload]
+    units = {"c2": "samples/s", "c3": "rays/s", "c4": "samples/s", "c1": "samples/s"}[args.workload]
     vals = []
     for _ in range(args.warmup):
         cpu_baseline(args.workload, budget_s=args.cpu_seconds / 4)
@@ -449,7 +538,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c1"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c1"])
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")

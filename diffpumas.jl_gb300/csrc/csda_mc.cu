@@ -20,11 +20,32 @@
 
 namespace dp {
 
+// Geometry of one history: the two-layer column and the direction-dependent
+// constants of the acceptance flux.
+struct CsdaGeo {
+  double thickness, rho, H, dir_z, uz, air_limit, cos_final, cs, cs129;
+};
+__host__ __device__ inline CsdaGeo csda_geo(double thickness, double rho, double elevation, double H) {
+  CsdaGeo g;
+  double theta = (90.0 - elevation) * kPi / 180.0;
+  double c = cos(theta);
+  g.thickness = thickness;
+  g.rho = rho;
+  g.H = H;
+  g.dir_z = -c;
+  g.uz = c;
+  g.air_limit = 0.05 * 12e3 / fmax(fabs(c), 0.05);
+  g.cos_final = fmin(fmax(c, 0.0), 1.0);
+  g.cs = cos_theta_star(g.cos_final);
+  g.cs129 = pow(g.cs, 1.29);
+  return g;
+}
+
 struct CsdaParams {
   TabView tab;
   int rock, air;
-  double thickness, rho, H, dir_z, uz, threshold, low, air_limit, mass, ctau;
-  double cos_final, cs, cs129;
+  CsdaGeo geo;  // fixed geometry (los == nullptr)
+  double threshold, low, mass, ctau;
   int use_philox;
   uint64_t seed;
   double emin, emax;
@@ -33,6 +54,11 @@ struct CsdaParams {
   double *contrib, *dcontrib, *sample_out;
   int32_t* steps;
   int* err_flag;
+  // lines of sight: history i belongs to the record l with
+  // los_off[l] <= i < los_off[l + 1] and takes its geometry and energy range
+  const dp_los* los;
+  const int64_t* los_off;
+  long n_los;
 };
 
 // Shared-memory table slots (all materials share the energy grid).
@@ -64,7 +90,20 @@ __global__ void __launch_bounds__(128) csda_mc_kernel(CsdaParams P) {
   for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < P.n;
        i += long(gridDim.x) * blockDim.x) {
     double E0, q, w;
-    if (P.use_philox) {
+    CsdaGeo G = P.geo;
+    if (P.los) {
+      long lo = 0, hi = P.n_los;
+      while (hi - lo > 1) {
+        long mid = (lo + hi) >> 1;
+        if (P.los_off[mid] <= i) lo = mid; else hi = mid;
+      }
+      const dp_los& L = P.los[lo];
+      double H = L.air_height > 0.0 ? L.thickness + L.air_height
+                                    : (L.primary_altitude > 0.0 ? L.primary_altitude : 3e4);
+      G = csda_geo(L.thickness, L.density, L.elevation, H);
+      mc_sample(P.seed, uint64_t(i), L.energy_min,
+                L.energy_max > L.energy_min ? L.energy_max : L.energy_min, &E0, &q, &w);
+    } else if (P.use_philox) {
       mc_sample(P.seed, uint64_t(i), P.emin, P.emax, &E0, &q, &w);
       if (P.sample_out) {
         P.sample_out[3 * i] = E0;
@@ -77,7 +116,7 @@ __global__ void __launch_bounds__(128) csda_mc_kernel(CsdaParams P) {
       w = P.w[i];
     }
     Dd E = dd(E0), wt = dd(1.0), z = dd(0.0);
-    const Dd rho = dd(P.rho, 1.0);
+    const Dd rho = dd(G.rho, 1.0);
     int hint_r = 0, hint_a = 0;
     int32_t nsteps = 0;
     // S(E) at the start of a step equals S(kf) of the previous step in the
@@ -89,33 +128,33 @@ __global__ void __launch_bounds__(128) csda_mc_kernel(CsdaParams P) {
     const int32_t kMaxSteps = 2000000;
     for (int outer = 0; outer < 1000 && nsteps < kMaxSteps; ++outer) {
       if (!(E.v < P.threshold - eps)) break;
-      if (z.v < 0.0 || z.v >= P.H - eps) break;
+      if (z.v < 0.0 || z.v >= G.H - eps) break;
       if (wt.v <= 0.0 || !isfinite(wt.v)) break;
       double limit = E.v < P.low - eps ? fmin(P.low, P.threshold) : P.threshold;
       for (int inner = 0; inner < 50000 && nsteps < kMaxSteps; ++inner) {
-        if (z.v < 0.0 || z.v >= P.H - eps) break;
+        if (z.v < 0.0 || z.v >= G.H - eps) break;
         if (E.v >= limit - eps) break;
         if (wt.v <= 0.0 || !isfinite(wt.v)) break;
-        const bool in_air = z.v >= P.thickness;
+        const bool in_air = z.v >= G.thickness;
         const double *S = in_air ? aS : rS, *R = in_air ? aR : rR;
         int* hint = in_air ? &hint_a : &hint_r;
         const int mat = in_air ? 1 : 0;
         Dd dens, tob;
         if (!in_air) {
           dens = rho;
-          if (P.uz > eps) tob = (dd(P.thickness) - z) / P.uz;
-          else if (P.uz < -eps) tob = (dd(0.0) - z) / P.uz;
+          if (G.uz > eps) tob = (dd(G.thickness) - z) / G.uz;
+          else if (G.uz < -eps) tob = (dd(0.0) - z) / G.uz;
           else tob = dd(1000.0);
         } else {
           dens = 1.205 * dexp(z / -12e3);
-          if (P.uz > eps) tob = (dd(P.H) - z) / P.uz;
-          else if (P.uz < -eps) tob = (dd(P.thickness) - z) / P.uz;
+          if (G.uz > eps) tob = (dd(G.H) - z) / G.uz;
+          else if (G.uz < -eps) tob = (dd(G.thickness) - z) / G.uz;
           else tob = dd(1000.0);
         }
         Dd lE = dlog(E);
         Dd X = range_of(P.tab, sE, slE, R, E, lE);
         Dd lim = 0.01 * X / dmax(dens, dd(1e-6));
-        if (in_air) lim = dmin(lim, dd(P.air_limit));
+        if (in_air) lim = dmin(lim, dd(G.air_limit));
         Dd step = dmin(tob + dd(1e-7), lim);
         if (step.v < kStepMin) step = dd(kStepMin);
         else if (step.v > 1000.0) step = dd(1000.0);
@@ -124,7 +163,7 @@ __global__ void __launch_bounds__(128) csda_mc_kernel(CsdaParams P) {
         Dd gi = dd(1.0) + E / P.mass, gc = dd(1.0) + kf / P.mass, ga = (gi + gc) / 2.0;
         Dd ba = dsqrt(dmax(dd(1.0) - dd(1.0) / (ga * ga), dd(1e-12)));
         Dd dt = step / (ba * ga);
-        z = z - step * dd(P.dir_z);
+        z = z - step * dd(G.dir_z);
         Dd Si = (s_mat == mat) ? s_cache : interp_logE(P.tab, sE, slE, S, E, lE, nullptr);
         Dd Sf = interp_logE(P.tab, sE, slE, S, kf, dlog(kf), nullptr);
         wt = wt * (Sf / Si) * dexp(dt / -P.ctau);
@@ -135,11 +174,217 @@ __global__ void __launch_bounds__(128) csda_mc_kernel(CsdaParams P) {
       }
     }
     double f = 0.0, df = 0.0;
-    if (z.v >= P.H - 1.0 && E.v < P.threshold && P.cos_final > 0.0) {
+    if (z.v >= G.H - 1.0 && E.v < P.threshold && G.cos_final > 0.0) {
       double dlogf;
-      double F = gccly_flux(P.cs, P.cs129, E.v, q, &dlogf);
+      double F = gccly_flux(G.cs, G.cs129, E.v, q, &dlogf);
       f = wt.v * F;
       df = wt.d * F + wt.v * F * dlogf * E.d;
+    }
+    P.contrib[i] = w * f;
+    if (P.dcontrib) P.dcontrib[i] = w * df;
+    if (P.steps) P.steps[i] = nsteps;
+  }
+}
+
+// ------------------------------------------------------------ mixed precision
+// The same history loop with the transport and its density tangent in FP32
+// (the single-precision derived columns: range, stopping power, energy, log
+// energy and the per-interval slopes) and the position in FP64.  Within the
+// mixed-mode tolerance (1e-4) of the FP64 program.
+struct Df {
+  float v, d;
+};
+__device__ __forceinline__ Df operator+(Df a, Df b) { return Df{a.v + b.v, a.d + b.d}; }
+__device__ __forceinline__ Df operator-(Df a, Df b) { return Df{a.v - b.v, a.d - b.d}; }
+__device__ __forceinline__ Df operator*(Df a, Df b) { return Df{a.v * b.v, a.d * b.v + a.v * b.d}; }
+__device__ __forceinline__ Df operator*(float a, Df b) { return Df{a * b.v, a * b.d}; }
+__device__ __forceinline__ Df operator/(Df a, Df b) {
+  float q = a.v / b.v;
+  return Df{q, (a.d - q * b.d) / b.v};
+}
+__device__ __forceinline__ Df fexp(Df a) {
+  float e = expf(a.v);
+  return Df{e, e * a.d};
+}
+__device__ __forceinline__ Df fsqrt(Df a) {
+  float r = sqrtf(a.v);
+  return Df{r, a.d / (2.f * r)};
+}
+__device__ __forceinline__ Df fmin2(Df a, Df b) { return b.v < a.v ? b : a; }
+__device__ __forceinline__ Df fmax2(Df a, Df b) { return b.v > a.v ? b : a; }
+
+// Staged FP32 columns per material (rock, air).
+enum { F_R = 0, F_S, F_E, F_LE, F_SLOPE, F_DSDLE, F_DLE, F_NCOL };
+
+struct Tab32 {
+  const float *R, *S, *E, *LE, *SLOPE, *DSDLE, *DLE;
+};
+__device__ __forceinline__ int f_interval(const Tab32& t, int n, float lx, const TabView& tv) {
+  int i;
+  if (tv.uniform) {
+    float f = floorf((lx - float(tv.lE0)) * float(tv.inv_dlE));
+    i = !(f >= 0.f) ? 0 : (f > float(n - 2) ? n - 2 : int(f));
+  } else {
+    i = 0;
+  }
+  while (i > 0 && lx < t.LE[i]) --i;
+  while (i < n - 2 && !(lx < t.LE[i + 1])) ++i;
+  return i;
+}
+// y(E) linear in log E, derivative through log E (src/Physics.jl:660-739).
+__device__ __forceinline__ void f_lookup(const Tab32& t, int n, const TabView& tv, Df E, Df* X,
+                                         Df* S) {
+  if (E.v <= t.E[0]) {
+    *X = Df{t.R[0], 0.f};
+    *S = Df{t.S[0], 0.f};
+    return;
+  }
+  if (E.v >= t.E[n - 1]) {
+    *X = Df{t.R[n - 1], 0.f};
+    *S = Df{t.S[n - 1], 0.f};
+    return;
+  }
+  float lx = logf(E.v), dl = E.d / E.v;
+  int i = f_interval(t, n, lx, tv);
+  float tt = (lx - t.LE[i]) / t.DLE[i];
+  *X = Df{t.R[i] + tt * (t.R[i + 1] - t.R[i]), dl / t.SLOPE[i]};
+  *S = Df{t.S[i] + tt * (t.S[i + 1] - t.S[i]), t.DSDLE[i] * dl};
+}
+__device__ __forceinline__ Df f_stopping(const Tab32& t, int n, const TabView& tv, Df E) {
+  Df X, S;
+  f_lookup(t, n, tv, E, &X, &S);
+  return S;
+}
+// Inverse range (src/Physics.jl:833-867), differentiated through t and exp.
+__device__ __forceinline__ Df f_inverse(const Tab32& t, int n, Df X, int* hint) {
+  if (X.v <= t.R[0]) return Df{t.E[0], 0.f};
+  if (X.v >= t.R[n - 1]) return Df{t.E[n - 1], 0.f};
+  int i = *hint < 0 ? 0 : (*hint > n - 2 ? n - 2 : *hint);
+  while (i > 0 && X.v < t.R[i]) --i;
+  while (i < n - 2 && !(X.v < t.R[i + 1])) ++i;
+  *hint = i;
+  float e = expf(t.LE[i] + (X.v - t.R[i]) * t.SLOPE[i]);
+  return Df{e, e * t.SLOPE[i] * X.d};
+}
+
+__global__ void __launch_bounds__(128) csda32_kernel(CsdaParams P, const float* tab32, int ld32) {
+  extern __shared__ __align__(16) double smem[];
+  __shared__ uint64_t mbar;
+  const int n = P.tab.n;
+  const int cols[F_NCOL] = {C32_RH, C32_S, C32_E, C32_LE, C32_SLOPE, C32_DSDLE, C32_DLE};
+  // FP32 columns are staged as pairs of doubles: ld32 floats = ld32/2 doubles
+  const double* src[2 * F_NCOL];
+  for (int m = 0; m < 2; ++m)
+    for (int c = 0; c < F_NCOL; ++c)
+      src[m * F_NCOL + c] = reinterpret_cast<const double*>(
+          tab32 + (size_t(m == 0 ? P.rock : P.air) * kNC32 + cols[c]) * ld32);
+  if (!stage_columns(smem, src, 2 * F_NCOL, uint32_t(ld32 * sizeof(float)), &mbar)) {
+    if (threadIdx.x == 0) atomicExch(P.err_flag, 1);
+    return;
+  }
+  const float* sf = reinterpret_cast<const float*>(smem);
+  auto tab = [&](int m) {
+    const float* b = sf + size_t(m) * F_NCOL * ld32;
+    return Tab32{b + F_R * ld32, b + F_S * ld32, b + F_E * ld32, b + F_LE * ld32,
+                 b + F_SLOPE * ld32, b + F_DSDLE * ld32, b + F_DLE * ld32};
+  };
+
+  const double eps = kEps64;
+  const float mass = float(P.mass), ctau = float(P.ctau);
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < P.n;
+       i += long(gridDim.x) * blockDim.x) {
+    double E0, q, w;
+    CsdaGeo G = P.geo;
+    if (P.los) {
+      long lo = 0, hi = P.n_los;
+      while (hi - lo > 1) {
+        long mid = (lo + hi) >> 1;
+        if (P.los_off[mid] <= i) lo = mid; else hi = mid;
+      }
+      const dp_los& L = P.los[lo];
+      double H = L.air_height > 0.0 ? L.thickness + L.air_height
+                                    : (L.primary_altitude > 0.0 ? L.primary_altitude : 3e4);
+      G = csda_geo(L.thickness, L.density, L.elevation, H);
+      mc_sample(P.seed, uint64_t(i), L.energy_min,
+                L.energy_max > L.energy_min ? L.energy_max : L.energy_min, &E0, &q, &w);
+    } else if (P.use_philox) {
+      mc_sample(P.seed, uint64_t(i), P.emin, P.emax, &E0, &q, &w);
+    } else {
+      E0 = P.E[i];
+      q = P.q[i];
+      w = P.w[i];
+    }
+    Df E{float(E0), 0.f}, wt{1.f, 0.f};
+    double zv = 0.0;
+    float zd = 0.f;
+    const Df rho{float(G.rho), 1.f};
+    const float uz = float(G.uz), dir_z = float(G.dir_z);
+    int hint_r = 0, hint_a = 0;
+    int32_t nsteps = 0;
+    int s_mat = -1;
+    Df s_cache{0.f, 0.f};
+    const int32_t kMaxSteps = 2000000;
+    for (int outer = 0; outer < 1000 && nsteps < kMaxSteps; ++outer) {
+      if (!(double(E.v) < P.threshold - eps)) break;
+      if (zv < 0.0 || zv >= G.H - eps) break;
+      if (wt.v <= 0.f || !isfinite(wt.v)) break;
+      double limit = double(E.v) < P.low - eps ? fmin(P.low, P.threshold) : P.threshold;
+      for (int inner = 0; inner < 50000 && nsteps < kMaxSteps; ++inner) {
+        if (zv < 0.0 || zv >= G.H - eps) break;
+        if (double(E.v) >= limit - eps) break;
+        if (wt.v <= 0.f || !isfinite(wt.v)) break;
+        const bool in_air = zv >= G.thickness;
+        const int mat = in_air ? 1 : 0;
+        const Tab32 t = tab(mat);
+        Df dens;
+        double tob_v;
+        float tob_d;
+        if (!in_air) {
+          dens = rho;
+          if (G.uz > eps) { tob_v = (G.thickness - zv) / G.uz; tob_d = -zd / uz; }
+          else if (G.uz < -eps) { tob_v = (0.0 - zv) / G.uz; tob_d = -zd / uz; }
+          else { tob_v = 1000.0; tob_d = 0.f; }
+        } else {
+          float dv = float(1.205 * exp(-zv / 12e3));
+          dens = Df{dv, -dv / 12e3f * zd};
+          if (G.uz > eps) { tob_v = (G.H - zv) / G.uz; tob_d = -zd / uz; }
+          else if (G.uz < -eps) { tob_v = (G.thickness - zv) / G.uz; tob_d = -zd / uz; }
+          else { tob_v = 1000.0; tob_d = 0.f; }
+        }
+        Df X, Si;
+        f_lookup(t, n, P.tab, E, &X, &Si);
+        if (s_mat == mat) Si = s_cache;
+        Df lim = 0.01f * X / fmax2(dens, Df{1e-6f, 0.f});
+        if (in_air) lim = fmin2(lim, Df{float(G.air_limit), 0.f});
+        // step = min(tob + 1e-7, lim) clamped to [STEP_MIN, 1000]; FP64 value
+        double stepv;
+        float stepd;
+        if (tob_v + 1e-7 <= double(lim.v)) { stepv = tob_v + 1e-7; stepd = tob_d; }
+        else { stepv = double(lim.v); stepd = lim.d; }
+        if (stepv < kStepMin) { stepv = kStepMin; stepd = 0.f; }
+        else if (stepv > 1000.0) { stepv = 1000.0; stepd = 0.f; }
+        const Df step{float(stepv), stepd};
+        Df kf = f_inverse(t, n, X + step * dens, in_air ? &hint_a : &hint_r);
+        Df gi = Df{1.f, 0.f} + E / Df{mass, 0.f}, gc = Df{1.f, 0.f} + kf / Df{mass, 0.f};
+        Df ga = 0.5f * (gi + gc);
+        Df ba = fsqrt(fmax2(Df{1.f, 0.f} - Df{1.f, 0.f} / (ga * ga), Df{1e-12f, 0.f}));
+        Df dt = step / (ba * ga);
+        zv -= stepv * G.dir_z;
+        zd -= stepd * dir_z;
+        Df Sf = f_stopping(t, n, P.tab, kf);
+        wt = wt * (Sf / Si) * fexp(Df{-1.f / ctau, 0.f} * dt);
+        E = kf;
+        s_mat = mat;
+        s_cache = Sf;
+        ++nsteps;
+      }
+    }
+    double f = 0.0, df = 0.0;
+    if (zv >= G.H - 1.0 && double(E.v) < P.threshold && G.cos_final > 0.0) {
+      double dlogf;
+      double F = gccly_flux(G.cs, G.cs129, double(E.v), q, &dlogf);
+      f = double(wt.v) * F;
+      df = double(wt.d) * F + double(wt.v) * F * dlogf * double(E.d);
     }
     P.contrib[i] = w * f;
     if (P.dcontrib) P.dcontrib[i] = w * df;
@@ -208,35 +453,31 @@ static int setup(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params* p, CsdaP
   P.tab = ph->view;
   P.rock = rock;
   P.air = air;
-  P.thickness = p->rock_thickness;
-  P.rho = p->rock_density;
-  P.H = p->primary_altitude > 0.0 ? p->primary_altitude : 3e4;
-  double theta = (90.0 - p->elevation) * kPi / 180.0;
-  double c = std::cos(theta);
-  P.dir_z = -c;
-  P.uz = c;
+  P.geo = csda_geo(p->rock_thickness, p->rock_density, p->elevation,
+                   p->primary_altitude > 0.0 ? p->primary_altitude : 3e4);
   P.threshold = thr;
   P.low = p->energy_threshold_low > 0.0 ? p->energy_threshold_low : 100.0;
-  P.air_limit = 0.05 * 12e3 / std::fmax(std::fabs(c), 0.05);
   P.mass = ph->settings.mass;
   P.ctau = ph->settings.ctau;
-  P.cos_final = std::fmin(std::fmax(c, 0.0), 1.0);
-  P.cs = cos_theta_star(P.cos_final);
-  P.cs129 = std::pow(P.cs, 1.29);
   P.err_flag = ctx->d_flag;
   return DP_OK;
 }
 
-static int launch(dp_ctx* ctx, CsdaParams& P) {
-  size_t smem = size_t(S_NCOL) * P.tab.ld * sizeof(double);
+static int launch(dp_ctx* ctx, CsdaParams& P, const dp_physics* ph32 = nullptr) {
   int threads = 128;
   long blocks = (P.n + threads - 1) / threads;
   if (blocks > 152L * 16) blocks = 152L * 16;
   if (blocks < 1) blocks = 1;
   timed_begin(ctx);
-  csda_mc_kernel<<<int(blocks), threads, smem, ctx->stream>>>(P);
+  if (ph32) {
+    size_t smem = size_t(2 * F_NCOL) * ph32->ld32 * sizeof(float);
+    csda32_kernel<<<int(blocks), threads, smem, ctx->stream>>>(P, ph32->dev32, ph32->ld32);
+  } else {
+    size_t smem = size_t(S_NCOL) * P.tab.ld * sizeof(double);
+    csda_mc_kernel<<<int(blocks), threads, smem, ctx->stream>>>(P);
+  }
   DP_CHECK_CUDA(ctx, cudaGetLastError());
-  timed_end(ctx, "csda_mc");
+  timed_end(ctx, ph32 ? "csda_mc32" : "csda_mc");
   return DP_OK;
 }
 
@@ -250,6 +491,30 @@ static int check_flag(dp_ctx* ctx) {
     return fail(ctx, DP_ERR_STATE, "a table-staging wait exceeded its limit");
   }
   return DP_OK;
+}
+
+// CSDA histories of a batch of lines of sight (device records and running
+// offsets): per-history w*flux and w*dflux/drho of the line's density.
+int csda_los(dp_ctx* ctx, const dp_physics* ph, int rock, int air, double threshold, double low,
+             uint64_t seed, const dp_los* los, const int64_t* off, long n_los, long n,
+             double* contrib, double* dcontrib, int precision) {
+  CsdaParams P{};
+  P.tab = ph->view;
+  P.rock = rock;
+  P.air = air;
+  P.threshold = threshold;
+  P.low = low;
+  P.mass = ph->settings.mass;
+  P.ctau = ph->settings.ctau;
+  P.err_flag = ctx->d_flag;
+  P.seed = seed;
+  P.n = n;
+  P.los = los;
+  P.los_off = off;
+  P.n_los = n_los;
+  P.contrib = contrib;
+  P.dcontrib = dcontrib;
+  return launch(ctx, P, precision == DP_PREC_MIXED ? ph : nullptr);
 }
 
 }  // namespace dp

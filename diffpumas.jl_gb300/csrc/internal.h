@@ -64,6 +64,12 @@ void* scratch(dp_ctx* ctx, size_t bytes, int slot = 0);
 // (with the results filled) where the reference would throw.
 int mc_backward_stochastic(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params* p, int rock,
                            int air, double threshold, dp_los_result* res);
+// CSDA histories (tangent mode) of lines of sight: history i of the running
+// offsets off[] takes its record's geometry and draws (seed, i).
+// precision DP_PREC_MIXED: FP32 transport and tangent, FP64 positions.
+int csda_los(dp_ctx* ctx, const dp_physics* ph, int rock, int air, double threshold, double low,
+             uint64_t seed, const dp_los* los, const int64_t* off, long n_los, long n,
+             double* contrib, double* dcontrib, int precision);
 // Bump allocator over one scratch slot (256-byte aligned pieces).
 struct Arena {
   char* base = nullptr;

@@ -241,6 +241,9 @@ Layout make_layout(const dp_mixture* a, const dp_mixture* b, size_t esize) {
   L.uniform = ph->view.uniform;
   L.lE0 = ph->view.lE0;
   L.inv_dlE = ph->view.inv_dlE;
+  // kernel energies: 8 log-uniform nodes per interval of a uniform grid
+  L.kuniform = L.uniform && a->nk == 8 * (a->n - 1) + 1 && b->nk == a->nk ? 1 : 0;
+  L.kinv_dlE = 8.0 * ph->view.inv_dlE;
   return L;
 }
 
@@ -570,12 +573,13 @@ __global__ void __launch_bounds__(KCfg<R>::threads, 1) mc_kernel(const __grid_co
 __global__ void __launch_bounds__(256) los_tally_kernel(const double* contrib, const int32_t* status,
                                                         const int64_t* off, const dp_los* los,
                                                         long n_los, dp_los_result* out,
-                                                        int* status_or) {
+                                                        int* status_or, const double* csda,
+                                                        const double* dcsda) {
   long l = (long(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (l >= n_los) return;
   long a = off[l], b = off[l + 1];
-  KSum s{0, 0}, s2{0, 0};
+  KSum s{0, 0}, s2{0, 0}, g{0, 0}, gf{0, 0};
   long bad = 0;
   int bits = 0;
   for (long i = a + lane; i < b; i += 32) {
@@ -585,15 +589,22 @@ __global__ void __launch_bounds__(256) los_tally_kernel(const double* contrib, c
     int st = status[i];
     bad += st != 0;
     bits |= st;
+    if (csda) {
+      kadd(gf, csda[i]);
+      kadd(g, dcsda[i]);
+    }
   }
   bits = __reduce_or_sync(0xffffffffu, unsigned(bits));
+  auto down = [](KSum& v, int d) {
+    KSum o{__shfl_down_sync(0xffffffffu, v.s, d), __shfl_down_sync(0xffffffffu, v.c, d)};
+    kmerge(v, o);
+  };
   for (int d = 16; d > 0; d >>= 1) {
-    KSum o{__shfl_down_sync(0xffffffffu, s.s, d), __shfl_down_sync(0xffffffffu, s.c, d)};
-    KSum o2{__shfl_down_sync(0xffffffffu, s2.s, d), __shfl_down_sync(0xffffffffu, s2.c, d)};
-    long ob = __shfl_down_sync(0xffffffffu, bad, d);
-    kmerge(s, o);
-    kmerge(s2, o2);
-    bad += ob;
+    down(s, d);
+    down(s2, d);
+    down(g, d);
+    down(gf, d);
+    bad += __shfl_down_sync(0xffffffffu, bad, d);
   }
   if (lane == 0) {
     long n = b - a;
@@ -605,6 +616,10 @@ __global__ void __launch_bounds__(256) los_tally_kernel(const double* contrib, c
       double f = sum / double(n), var = sum2 / double(n) - f * f;
       r.flux = f;
       r.sigma = los[l].thickness > 0.0 ? sqrt(fmax(var, 0.0) / double(n)) : 0.0;
+      if (csda) {
+        r.gradient_flux = (gf.s + gf.c) / double(n);
+        r.gradient = (g.s + g.c) / double(n);
+      }
     }
     out[l] = r;
     if (bits) atomicOr(status_or, bits);
@@ -645,7 +660,8 @@ __global__ void __launch_bounds__(1024) los_offsets_kernel(const dp_los* los, lo
 
 namespace {
 
-int check_cfg(dp_ctx* ctx, const dp_physics* ph, const dp_mc_config* cfg, Consts* C) {
+int check_cfg(dp_ctx* ctx, const dp_physics* ph, const dp_mc_config* cfg, Consts* C,
+              double* thr_fp64 = nullptr) {
   if (!cfg) return fail(ctx, DP_ERR_ARG, "null config");
   if (cfg->precision != DP_PREC_FP64 && cfg->precision != DP_PREC_MIXED)
     return fail(ctx, DP_ERR_ARG, "precision must be DP_PREC_FP64 or DP_PREC_MIXED");
@@ -654,6 +670,7 @@ int check_cfg(dp_ctx* ctx, const dp_physics* ph, const dp_mc_config* cfg, Consts
   if (!(thr > 0.0 && thr <= tmax))
     return fail(ctx, DP_ERR_ARG, "source_energy_max must be positive and within the physics energy grid");
   double low = cfg->energy_threshold_low > 0.0 ? cfg->energy_threshold_low : 100.0;
+  if (thr_fp64) *thr_fp64 = thr;
   if (cfg->precision == DP_PREC_MIXED) {
     // thresholds exactly representable in the FP32 transport
     thr = double(float(thr));
@@ -754,7 +771,8 @@ McParams base_params(dp_ctx* ctx, const unsigned char* blob, const Layout& lay, 
 
 int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_mixture* air,
                   const dp_mc_config* cfg, long n_los, const dp_los* d_los, long total,
-                  dp_los_result* d_out, double** contrib_out, int** status_or);
+                  dp_los_result* d_out, double** contrib_out, int** status_or,
+                  int compute_gradient);
 
 namespace {
 // Status bits of a finished run: the call's error code where the reference
@@ -890,12 +908,10 @@ int dp_mc_los_dev(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock_c,
                   long total, int compute_gradient, dp_los_result* out) {
   if (!ctx || !ph || !rock_c || !air || !los || !out || n_los <= 0 || total < 0)
     return fail(ctx, DP_ERR_ARG, "bad arguments");
-  if (compute_gradient)
-    return fail(ctx, DP_ERR_ARG, "the per-line-of-sight CSDA gradient is not available in this call");
   double* contrib = nullptr;
   int* bits = nullptr;
   int rc = dp_mc_run_los(ctx, ph, const_cast<dp_mixture*>(rock_c), air, cfg, n_los, los, total, out,
-                         &contrib, &bits);
+                         &contrib, &bits, compute_gradient);
   if (rc) return rc;
   if (ctx->blocking) return status_result(ctx, bits);
   return DP_OK;
@@ -925,11 +941,14 @@ int dp_mc_los(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock, const d
   if (!dr) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
   DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dl, los, lb, cudaMemcpyHostToDevice, ctx->stream));
   if (compute_gradient)
-    return fail(ctx, DP_ERR_ARG, "the per-line-of-sight CSDA gradient is not available in this call");
+    for (long l = 0; l < n_los; ++l)
+      if (los[l].thickness_max > los[l].thickness || los[l].density_max > los[l].density ||
+          los[l].elevation_max > los[l].elevation)
+        return fail(ctx, DP_ERR_ARG, "the CSDA gradient needs fixed line-of-sight geometry");
   double* contrib = nullptr;
   int* bits = nullptr;
   int rc = dp_mc_run_los(ctx, ph, const_cast<dp_mixture*>(rock), air, cfg, n_los, dl, total, dr,
-                         &contrib, &bits);
+                         &contrib, &bits, compute_gradient);
   if (rc) return rc;
   DP_CHECK_CUDA(ctx, cudaMemcpyAsync(out, dr, ob, cudaMemcpyDeviceToHost, ctx->stream));
   return status_result(ctx, bits);
@@ -942,10 +961,14 @@ int dp_mc_los(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock, const d
 // contributions (scratch slot 0, valid until the next call on ctx).
 int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_mixture* air,
                   const dp_mc_config* cfg, long n_los, const dp_los* d_los, long total,
-                  dp_los_result* d_out, double** contrib_out, int** status_or) {
+                  dp_los_result* d_out, double** contrib_out, int** status_or,
+                  int compute_gradient) {
   Consts C;
-  int rc = check_cfg(ctx, ph, cfg, &C);
+  double thr64;
+  int rc = check_cfg(ctx, ph, cfg, &C, &thr64);
   if (rc) return rc;
+  if (compute_gradient && (rock->nm != 1 || air->nm != 1))
+    return fail(ctx, DP_ERR_ARG, "the CSDA gradient needs single-material rock and air");
   DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
   const unsigned char* blob;
   Layout lay;
@@ -954,13 +977,15 @@ int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_
   long nt = total > 0 ? total : 1;
   Arena A;
   A.base = static_cast<char*>(scratch(
-      ctx, size_t(nt) * (12 + sizeof(Handoff<double>)) + size_t(n_los + 1) * 8 + 4096, 0));
+      ctx, size_t(nt) * (12 + 16 + sizeof(Handoff<double>)) + size_t(n_los + 1) * 8 + 4096, 0));
   A.cap = ctx->slot_bytes[0];
   double* dc = A.take<double>(nt);
   int32_t* ds = A.take<int32_t>(nt);
   int64_t* off = A.take<int64_t>(n_los + 1);
   unsigned long long* ctr = A.take<unsigned long long>(3);
   Handoff<double>* queue = A.take<Handoff<double>>(nt);
+  double* cc = compute_gradient ? A.take<double>(nt) : nullptr;
+  double* cd = compute_gradient ? A.take<double>(nt) : nullptr;
   int* bits = A.take<int>(1);
   if (!bits) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
   DP_CHECK_CUDA(ctx, cudaMemsetAsync(bits, 0, sizeof(int), ctx->stream));
@@ -980,11 +1005,19 @@ int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_
     P.queue = queue;
     rc = run(ctx, P, cfg->precision);
     if (rc) return rc;
+    if (compute_gradient) {
+      // deterministic CSDA surrogate over the same samples (src/Geometry.jl:933-945)
+      rc = csda_los(ctx, ph, rock->mats[0], air->mats[0], thr64,
+                    cfg->energy_threshold_low > 0.0 ? cfg->energy_threshold_low : 100.0,
+                    cfg->seed, d_los, off, n_los, total, cc, cd, cfg->precision);
+      if (rc) return rc;
+    }
   }
   long warps_per_block = 8;
   long blocks = (n_los + warps_per_block - 1) / warps_per_block;
   timed_begin(ctx);
-  los_tally_kernel<<<int(blocks), 256, 0, ctx->stream>>>(dc, ds, off, d_los, n_los, d_out, bits);
+  los_tally_kernel<<<int(blocks), 256, 0, ctx->stream>>>(dc, ds, off, d_los, n_los, d_out, bits,
+                                                         total > 0 ? cc : nullptr, cd);
   DP_CHECK_CUDA(ctx, cudaGetLastError());
   timed_end(ctx, "mc_tally");
   if (contrib_out) *contrib_out = dc;
@@ -1026,7 +1059,7 @@ int mc_backward_stochastic(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params
     cudaError_t e = cudaMemcpyAsync(dl, &L, sizeof(L), cudaMemcpyHostToDevice, ctx->stream);
     if (e != cudaSuccess) rc = cuda_fail(ctx, e, "cudaMemcpyAsync");
   }
-  if (!rc) rc = dp_mc_run_los(ctx, ph, &rm, &am, &cfg, 1, dl, p->n_samples, dr, nullptr, &bits);
+  if (!rc) rc = dp_mc_run_los(ctx, ph, &rm, &am, &cfg, 1, dl, p->n_samples, dr, nullptr, &bits, 0);
   if (!rc) {
     cudaError_t e = cudaMemcpyAsync(res, dr, sizeof(*res), cudaMemcpyDeviceToHost, ctx->stream);
     if (e != cudaSuccess) rc = cuda_fail(ctx, e, "cudaMemcpyAsync");

@@ -54,6 +54,8 @@ struct Layout {
   int ld, ldk;         // column strides (elements)
   int n, nk, slots, uniform;
   double lE0, inv_dlE;
+  int kuniform;        // MIXED kernel energies: the uniform log grid refined 8-fold
+  double kinv_dlE;     // 1 / log step of the kernel energies
 };
 struct MedInfo {
   int nm, nel;
@@ -66,9 +68,9 @@ struct Med {
   const R* p;
   const R* kp;
   const double* el;
-  int ld, ldk, n, nk, nm, nel, slots, uniform;
+  int ld, ldk, n, nk, nm, nel, slots, uniform, kuniform;
   R frac[kMaxMix];
-  R ZoA, onset, lE0, inv_dlE;
+  R ZoA, onset, lE0, inv_dlE, kinv_dlE;
   __device__ __forceinline__ const R* col(int k) const { return p + k * ld; }
   __device__ __forceinline__ const R* kcol(int j) const { return kp + j * ldk; }
   __device__ __forceinline__ int lbe(int j) const { return MC_LB1 + slots + j; }
@@ -89,6 +91,8 @@ __device__ __forceinline__ Med<R> make_med(const unsigned char* base, const Layo
   m.uniform = L.uniform;
   m.lE0 = R(L.lE0);
   m.inv_dlE = R(L.inv_dlE);
+  m.kuniform = L.kuniform;
+  m.kinv_dlE = R(L.kinv_dlE);
   m.nm = I.nm;
   m.nel = I.nel;
 #pragma unroll
@@ -304,8 +308,36 @@ __device__ __forceinline__ R kat(const R* ys, int n, const KLoc<R>& L) {
   if (L.edge > 0) return ys[n - 1];
   return ys[L.i] + L.f * (ys[L.i + 1] - ys[L.i]);
 }
+// The same location on the kernel's energy axis: on a uniform log grid an
+// O(1) guess corrected to the searchsortedlast interval.
+template <class R>
+__device__ __forceinline__ KLoc<R> klocate_e(const Med<R>& m, R x, int* status) {
+  const R* xs = m.kcol(K_E);
+  const int n = m.nk;
+  if (!m.kuniform || !(x == x)) return klocate(xs, n, x, status);
+  KLoc<R> L{0, 0, R(0)};
+  if (x < xs[0]) {
+    *status |= ST_DOMAIN_LO;
+    L.edge = -1;
+    return L;
+  }
+  if (x > xs[n - 1]) {
+    *status |= ST_DOMAIN_HI;
+    L.edge = 1;
+    return L;
+  }
+  R f = floor((log(x) - m.lE0) * m.kinv_dlE);
+  int i = !(f >= R(0)) ? 0 : (f > R(n - 2) ? n - 2 : int(f));
+  while (i > 0 && x < xs[i]) --i;
+  while (i < n - 2 && !(x < xs[i + 1])) ++i;
+  R d = xs[i + 1] - xs[i];
+  L.i = i;
+  L.f = d == R(0) ? R(0) : (x - xs[i]) / d;
+  return L;
+}
 template <class R>
 __device__ __forceinline__ R klookup(const Med<R>& m, int xcol, int ycol, R x, int* status) {
+  if (xcol == K_E) return kat(m.kcol(ycol), m.nk, klocate_e(m, x, status));
   return kat(m.kcol(ycol), m.nk, klocate(m.kcol(xcol), m.nk, x, status));
 }
 
@@ -527,7 +559,7 @@ __device__ __noinline__ bool mixed_run(const Med<R>& m, const Consts& C, State<R
       mixed_end(s, x, Emax, energy_limit, false);
       return false;
     }
-    KLoc<R> Lk = klocate(kE, nk, k, &s.status);
+    KLoc<R> Lk = klocate_e(m, k, &s.status);
     R ri = kat(m.kcol(K_R), nk, Lk), hi = kat(m.kcol(K_H), nk, Lk);
     R rtc = fmax(R(0), klookup(m, K_E, K_R, x.r2, &s.status) - ri);
     double eg = fmin(x.a, double(rtc));
@@ -536,7 +568,7 @@ __device__ __noinline__ bool mixed_run(const Med<R>& m, const Consts& C, State<R
     R eventh = hi + expo<R>(g);
     bool occurs = eventh < klookup(m, K_E, K_H, endpoint, &s.status);
     R pre = occurs ? fmax(k, klookup(m, K_H, K_E, eventh, &s.status)) : endpoint;
-    KLoc<R> Lp = klocate(kE, nk, pre, &s.status);
+    KLoc<R> Lp = klocate_e(m, pre, &s.status);
     double dxd = occurs ? double(fmax(R(0), kat(m.kcol(K_R), nk, Lp) - ri)) : eg;
     R dx = R(dxd);
     R dt;

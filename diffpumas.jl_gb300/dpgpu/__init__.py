@@ -376,17 +376,22 @@ def make_los(n_samples, *, thickness, density, elevation, energy_min, energy_max
 
 
 def backward_mc_batch(physics, los, *, rock, air, seed=42, straggling=True, scattering=True,
-                      energy_threshold_low=100.0, source_energy_max=None, precision="mixed"):
+                      energy_threshold_low=100.0, source_energy_max=None, precision="mixed",
+                      compute_gradient=False):
     """Batched stochastic backward MC over lines of sight (one persistent
-    launch): per line of sight (flux, sigma, n_samples, n_status_nonzero)."""
+    launch): per line of sight flux, sigma, n_samples, n_status_nonzero and,
+    with compute_gradient, the CSDA surrogate's gradient_flux and gradient
+    (d flux / d density of the line)."""
     n = len(los)
     out = (DpLosResult * n)()
     cfg = _mc_config(seed, straggling, scattering, energy_threshold_low, source_energy_max,
                      precision)
     check(load().dp_mc_los(physics.ctx.h, physics.h, rock.h, air.h, C.byref(cfg), n,
-                           C.cast(los, C.c_void_p), 0, C.cast(out, C.c_void_p)), physics.ctx.h)
-    return {k: np.array([getattr(r, k) for r in out]) for k in
-            ("flux", "sigma", "n_samples", "n_status_nonzero")}
+                           C.cast(los, C.c_void_p), int(bool(compute_gradient)),
+                           C.cast(out, C.c_void_p)), physics.ctx.h)
+    keys = ("flux", "sigma", "n_samples", "n_status_nonzero") + \
+        (("gradient", "gradient_flux") if compute_gradient else ())
+    return {k: np.array([getattr(r, k) for r in out]) for k in keys}
 
 
 # ----------------------------------------------------------------- tomography

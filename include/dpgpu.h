@@ -284,8 +284,10 @@ typedef struct {
 /* Batched stochastic backward MC over many lines of sight in one persistent
  * launch (histories of all lines of sight share the device; the history id
  * is the running sample index over the batch).  compute_gradient adds the
- * deterministic CSDA sample-average gradient per line of sight
- * (src/Geometry.jl:933-945); it needs fixed (undrawn) geometry.  Host pointers. */
+ * deterministic CSDA sample-average flux and its derivative with respect to
+ * each line's density over the same samples (src/Geometry.jl:933-945); it
+ * needs fixed (undrawn) geometry and single-material rock and air.  Host
+ * pointers. */
 int dp_mc_los(dp_ctx* ctx, const dp_physics* phys, const dp_mixture* rock, const dp_mixture* air,
               const dp_mc_config* cfg, long n_los, const dp_los* los, int compute_gradient,
               dp_los_result* out);

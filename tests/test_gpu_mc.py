@@ -177,6 +177,33 @@ def test_line_of_sight_batch_matches_oracle(dp, phys, media, oracle, orc_phys):
         assert out["sigma"][l] == pytest.approx(s, rel=0.05)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_line_of_sight_gradient_matches_oracle(dp, phys, media, oracle, orc_phys, precision):
+    """compute_gradient over lines of sight: the CSDA sample-average flux and
+    its derivative with respect to each line's density (src/Geometry.jl:933-945)
+    over the stochastic run's own samples; mixed transport everywhere
+    (threshold at the lowest final energy, no scattering).  FP64: the
+    reference's operations; mixed: FP32 transport and tangent, FP64
+    positions, within the 1e-4 mixed-mode bar."""
+    rock, air, _ = media
+    tol_f, tol_g = (1e-9, 1e-7) if precision == "fp64" else (1e-4, 1e-4)
+    depth = np.array([50.0, 320.0, 1500.0])
+    rho = np.array([2400.0, 2600.0, 2800.0])
+    ns = np.array([64, 500, 256])
+    los = dp.make_los(ns, thickness=depth, density=rho, elevation=90.0, energy_min=1.0,
+                      energy_max=1e4)
+    out = dp.backward_mc_batch(phys, los, rock=rock, air=air, seed=5, precision=precision,
+                               scattering=False, energy_threshold_low=1.0, compute_gradient=True)
+    E, q, w = dp.mc_samples(phys, energy_min=1.0, energy_max=1e4, n_samples=int(ns.sum()), seed=5)
+    off = np.concatenate([[0], np.cumsum(ns)])
+    for l in range(3):
+        sl = slice(off[l], off[l + 1])
+        cc, cd = oracle.backward_mc_csda(orc_phys, 0, 1, depth[l], rho[l], 90.0, E[sl], q[sl], w[sl])
+        assert out["gradient_flux"][l] == pytest.approx(cc.mean(), rel=tol_f)
+        assert out["gradient"][l] == pytest.approx(cd.mean(), rel=tol_g, abs=1e-12 * abs(cc.mean()))
+        assert out["n_status_nonzero"][l] == 0 and out["flux"][l] > 0
+
+
 def _philox_u01(ids, block, seed):
     """Philox4x32-10 (seed, (id, block)) -> two 53-bit uniforms per id."""
     M0, M1, W0, W1 = 0xD2511F53, 0xCD9E8D57, 0x9E3779B9, 0xBB67AE85
