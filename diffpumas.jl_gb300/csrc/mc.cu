@@ -234,9 +234,15 @@ Layout make_layout(const dp_mixture* a, const dp_mixture* b, size_t esize) {
   L.slots = std::max(a->nm, b->nm);
   L.ld = pad_elems(L.n, esize);
   L.ldk = pad_elems(L.nk, esize);
-  L.o_phys = uint32_t(kMaxEl * kElStride * sizeof(double));
+  // elements, then the index-table origins and widths (2 doubles per column)
+  L.o_phys = uint32_t((kMaxEl * kElStride + 2 * I_NCOL) * sizeof(double));
   L.o_ker = L.o_phys + uint32_t(size_t(MC_LB1 + 2 * L.slots) * L.ld * esize);
-  L.med_bytes = L.o_ker + uint32_t(size_t(K_NCOL) * L.ldk * esize);
+  L.o_idx = L.o_ker + uint32_t(size_t(K_NCOL) * L.ldk * esize);
+  L.nbp = kIdxBinsPhys;
+  L.nbk = kIdxBinsKer;
+  uint32_t idx_bytes = uint32_t((2 * kIdxBinsPhys + 2 * kIdxBinsKer) * sizeof(int16_t));
+  L.o_elf = L.o_idx + (idx_bytes + 15) / 16 * 16;
+  L.med_bytes = L.o_elf + uint32_t(kMaxEl * kElfStride * sizeof(float));
   const dp_physics* ph = a->phys;
   L.uniform = ph->view.uniform;
   L.lE0 = ph->view.lE0;
@@ -263,6 +269,42 @@ void pack(const dp_mixture* m, const Layout& L, unsigned char* out) {
   }
   R* K = reinterpret_cast<R*>(out + L.o_ker);
   for (int c = 0; c < K_NCOL; ++c) put(K + size_t(c) * L.ldk, m->kcols.data() + size_t(c) * m->nk, m->nk);
+  // FP32 element table of the cooperative DCS sums
+  float* elf = reinterpret_cast<float*>(out + L.o_elf);
+  for (int e = 0; e < m->nel; ++e) {
+    const double* x = m->el.data() + kElStride * e;
+    float* f = elf + kElfStride * e;
+    f[0] = float(x[0]);
+    f[1] = float(x[1]);
+    f[2] = float(x[2]);
+    f[3] = float(x[3]);
+    f[4] = float(kAvogadro / (x[1] * 0.001));
+  }
+  // index tables of the inverse lookups (origins and widths in R)
+  R* prm = reinterpret_cast<R*>(reinterpret_cast<double*>(out) + kMaxEl * kElStride);
+  int16_t* idx = reinterpret_cast<int16_t*>(out + L.o_idx);
+  const double* cols[I_NCOL] = {m->cols.data() + size_t(MC_CR) * m->n,
+                                m->cols.data() + size_t(MC_MR) * m->n,
+                                m->kcols.data() + size_t(K_R) * m->nk,
+                                m->kcols.data() + size_t(K_H) * m->nk};
+  for (int c = 0; c < I_NCOL; ++c) {
+    const int n = c < I_KR ? m->n : m->nk, nb = c < I_KR ? kIdxBinsPhys : kIdxBinsKer;
+    int16_t* out_idx = idx + (c < I_KR ? c * kIdxBinsPhys : 2 * kIdxBinsPhys + (c - I_KR) * kIdxBinsKer);
+    const double* y = cols[c];
+    int j0 = 0;
+    while (j0 < n - 1 && !(y[j0] > 0.0)) ++j0;
+    double lo = y[j0] > 0.0 ? std::log(y[j0]) : 0.0;
+    double hi = y[n - 1] > 0.0 ? std::log(y[n - 1]) : lo;
+    double inv = hi > lo ? nb / (hi - lo) : 0.0;
+    prm[2 * c] = R(lo);
+    prm[2 * c + 1] = R(inv);
+    int j = 0;
+    for (int b = 0; b < nb; ++b) {
+      double edge = inv > 0.0 ? std::exp(lo + b / inv) : 0.0;
+      while (j < n - 2 && y[j + 1] <= edge) ++j;
+      out_idx[b] = int16_t(j);
+    }
+  }
 }
 
 MedInfo make_info(const dp_mixture* m) {
@@ -334,6 +376,8 @@ struct McParams {
   int* err_flag;
   int coop_nel, coop_stride;  // cooperative DCS buffers: elements, floats per warp
   void* queue;                // Handoff<R> x n: histories crossing the mode switch
+  void* start;                // StartRec<R> x n
+  void* end;                  // EndRec<R> x n
 };
 
 // Copies `bytes` (16-byte multiple) from global to shared memory with
@@ -381,75 +425,116 @@ __device__ __forceinline__ long next_history(unsigned long long* counter) {
   return long(base + g.thread_rank());
 }
 
+// Start record of history i: energy, charge and weight drawn as
+// run_backward_mc draws them (src/Geometry.jl:863-875) or given; geometry
+// given, taken from its line of sight or drawn (Philox blocks 1-2).
+template <class R>
+__global__ void __launch_bounds__(256) mc_init_kernel(const __grid_constant__ McParams P) {
+  StartRec<R>* out = static_cast<StartRec<R>*>(P.start);
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < P.n;
+       i += long(gridDim.x) * blockDim.x) {
+    double E0, q, ws, thick, rho, elev, H;
+    if (P.source == 0) {
+      E0 = P.E[i];
+      q = P.q[i];
+      ws = P.w[i];
+      long gi = P.geo_stride ? i : 0;
+      thick = P.thick[gi];
+      rho = P.dens[gi];
+      elev = P.elev[gi];
+      H = P.H[gi];
+    } else {
+      long lo = 0, hi = P.n_los;  // los_off[lo] <= i < los_off[lo + 1]
+      while (hi - lo > 1) {
+        long mid = (lo + hi) >> 1;
+        if (P.los_off[mid] <= i) lo = mid; else hi = mid;
+      }
+      const dp_los& L = P.los[lo];
+      const uint64_t id = uint64_t(i);
+      double emax = L.energy_max > L.energy_min ? L.energy_max : L.energy_min;
+      mc_sample(P.seed, id, L.energy_min, emax, &E0, &q, &ws);
+      U4 b1 = philox(U4{uint32_t(id), uint32_t(id >> 32), 1u, 0u}, uint32_t(P.seed),
+                     uint32_t(P.seed >> 32));
+      U4 b2 = philox(U4{uint32_t(id), uint32_t(id >> 32), 2u, 0u}, uint32_t(P.seed),
+                     uint32_t(P.seed >> 32));
+      thick = L.thickness_max > L.thickness
+                  ? L.thickness + (L.thickness_max - L.thickness) * u01(b1.x, b1.y)
+                  : L.thickness;
+      rho = L.density_max > L.density ? L.density + (L.density_max - L.density) * u01(b1.z, b1.w)
+                                      : L.density;
+      elev = L.elevation_max > L.elevation
+                 ? L.elevation + (L.elevation_max - L.elevation) * u01(b2.x, b2.y)
+                 : L.elevation;
+      H = L.air_height > 0.0 ? thick + L.air_height
+                             : (L.primary_altitude > 0.0 ? L.primary_altitude : 3e4);
+    }
+    double theta = (90.0 - elev) * kPi / 180.0;
+    StartRec<R> r;
+    r.thick = alt_make<R>(thick);
+    r.H = alt_make<R>(H);
+    r.q = q;
+    r.ws = ws;
+    r.E = R(E0);
+    r.rho = R(rho);
+    r.ux = R(-sin(theta));
+    r.uz = R(-cos(theta));
+    out[i] = r;
+  }
+}
+
 template <class R>
 __device__ __forceinline__ void start_history(const McParams& P, long i, Hist<R>& h, Stream& g) {
-  double E0, q, ws, thick, rho, elev, H;
-  uint64_t id;
-  if (P.source == 0) {
-    E0 = P.E[i];
-    q = P.q[i];
-    ws = P.w[i];
-    long gi = P.geo_stride ? i : 0;
-    thick = P.thick[gi];
-    rho = P.dens[gi];
-    elev = P.elev[gi];
-    H = P.H[gi];
-    id = P.id0 + uint64_t(i);
-  } else {
-    long lo = 0, hi = P.n_los;  // los_off[lo] <= i < los_off[lo + 1]
-    while (hi - lo > 1) {
-      long mid = (lo + hi) >> 1;
-      if (P.los_off[mid] <= i) lo = mid; else hi = mid;
-    }
-    const dp_los& L = P.los[lo];
-    id = uint64_t(i);
-    double emax = L.energy_max > L.energy_min ? L.energy_max : L.energy_min;
-    mc_sample(P.seed, id, L.energy_min, emax, &E0, &q, &ws);
-    U4 b1 = philox(U4{uint32_t(id), uint32_t(id >> 32), 1u, 0u}, uint32_t(P.seed), uint32_t(P.seed >> 32));
-    U4 b2 = philox(U4{uint32_t(id), uint32_t(id >> 32), 2u, 0u}, uint32_t(P.seed), uint32_t(P.seed >> 32));
-    thick = L.thickness_max > L.thickness
-                ? L.thickness + (L.thickness_max - L.thickness) * u01(b1.x, b1.y)
-                : L.thickness;
-    rho = L.density_max > L.density ? L.density + (L.density_max - L.density) * u01(b1.z, b1.w)
-                                    : L.density;
-    elev = L.elevation_max > L.elevation
-               ? L.elevation + (L.elevation_max - L.elevation) * u01(b2.x, b2.y)
-               : L.elevation;
-    H = L.air_height > 0.0 ? thick + L.air_height
-                           : (L.primary_altitude > 0.0 ? L.primary_altitude : 3e4);
-  }
-  double theta = (90.0 - elev) * kPi / 180.0;
-  h.s.x = h.s.y = h.s.z = 0.0;
-  h.s.ux = R(-sin(theta));
+  const StartRec<R> r = static_cast<const StartRec<R>*>(P.start)[i];
+  h.s.z = alt_make<R>(0.0);
+  h.s.ux = r.ux;
   h.s.uy = R(0);
-  h.s.uz = R(-cos(theta));
-  h.s.E = R(E0);
+  h.s.uz = r.uz;
+  h.s.E = r.E;
   h.s.w = R(1);
   h.s.status = 0;
-  h.limit = 0.0;
-  h.thick = thick;
-  h.rho = rho;
-  h.H = H;
-  h.q = q;
-  h.ws = ws;
+  h.limit = R(0);
+  h.thick = r.thick;
+  h.rho = r.rho;
+  h.H = r.H;
   h.steps = h.inner = h.outer = 0;
   h.need_mode = true;
   h.strag = h.mixed = h.scat = false;
   h.x.kind = CONT_NONE;
-  g.init(P.seed, id);
+  g.init(P.seed, P.source == 0 ? P.id0 + uint64_t(i) : uint64_t(i));
 }
 
 template <class R>
 __device__ __forceinline__ void end_history(const McParams& P, long i, const Hist<R>& h) {
-  P.contrib[i] = h.ws * history_flux(P.C, h);
-  if (P.status) P.status[i] = h.s.status;
-  if (P.steps) P.steps[i] = h.steps;
-  if (P.efinal) {
-    double* f = P.efinal + 4 * i;
-    f[0] = double(h.s.E);
-    f[1] = h.s.z;
-    f[2] = double(h.s.uz);
-    f[3] = double(h.s.w);
+  EndRec<R> e;
+  e.z = h.s.z;
+  e.E = h.s.E;
+  e.w = h.s.w;
+  e.uz = h.s.uz;
+  e.status = h.s.status;
+  e.steps = h.steps;
+  static_cast<EndRec<R>*>(P.end)[i] = e;
+}
+
+// Flux contribution w_i * flux_i of every ended history, FP64, one thread per
+// history (src/Geometry.jl:729-757).
+template <class R>
+__global__ void __launch_bounds__(256) mc_finish_kernel(const __grid_constant__ McParams P) {
+  const StartRec<R>* st = static_cast<const StartRec<R>*>(P.start);
+  const EndRec<R>* en = static_cast<const EndRec<R>*>(P.end);
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < P.n;
+       i += long(gridDim.x) * blockDim.x) {
+    const EndRec<R> e = en[i];
+    const StartRec<R> r = st[i];
+    P.contrib[i] = r.ws * history_flux(P.C, e, alt_value(r.H), r.q);
+    if (P.status) P.status[i] = e.status;
+    if (P.steps) P.steps[i] = e.steps;
+    if (P.efinal) {
+      double* f = P.efinal + 4 * i;
+      f[0] = double(e.E);
+      f[1] = alt_value(e.z);
+      f[2] = double(e.uz);
+      f[3] = double(e.w);
+    }
   }
 }
 
@@ -534,7 +619,7 @@ __global__ void __launch_bounds__(KCfg<R>::threads, 1) mc_kernel(const __grid_co
         const double anc = __shfl_sync(0xffffffffu, h.x.anc, L);
         const double q = __shfl_sync(0xffffffffu, h.x.q, L);
         const Med<R>& m = med ? air : rock;
-        const double total = coop_total(m.el, m.nel, P.C.mass, anc, q, item, comp);
+        const double total = coop_total(m.elf, m.nel, float(P.C.mass), anc, q, item, comp);
         if (lane == L) {
           h.x.total = total;
           h.x.pick = -1;
@@ -660,6 +745,10 @@ __global__ void __launch_bounds__(1024) los_offsets_kernel(const dp_los* los, lo
 
 namespace {
 
+// Per-history device records of a run (hand-off, start, end), sized for FP64.
+constexpr size_t kRecBytes = sizeof(Handoff<double>) + sizeof(StartRec<double>) +
+                             sizeof(EndRec<double>) + 64;
+
 int check_cfg(dp_ctx* ctx, const dp_physics* ph, const dp_mc_config* cfg, Consts* C,
               double* thr_fp64 = nullptr) {
   if (!cfg) return fail(ctx, DP_ERR_ARG, "null config");
@@ -683,6 +772,8 @@ int check_cfg(dp_ctx* ctx, const dp_physics* ph, const dp_mc_config* cfg, Consts
   C->elastic_ratio = ph->settings.elastic_ratio;
   C->thr = thr;
   C->thr_low = low;
+  C->thr_f = float(thr);
+  C->thr_low_f = float(low);
   C->straggling = cfg->straggling != 0;
   C->scattering = cfg->scattering != 0;
   return DP_OK;
@@ -723,10 +814,21 @@ int launch_mc(dp_ctx* ctx, McParams& P) {
   size_t smem = 16 + (P.staged ? tables : 0) + coop_bytes;
   if (smem > size_t(dev_smem)) return fail(ctx, DP_ERR_ARG, "media too large for the MC kernel");
   long need = (P.n + threads - 1) / threads;
+  long rec_blocks = std::min((P.n + 255) / 256, 152L * 32);
   DP_CHECK_CUDA(ctx, cudaMemsetAsync(P.counter, 0, 3 * sizeof(unsigned long long), ctx->stream));
+  timed_begin(ctx);
+  mc_init_kernel<R><<<int(rec_blocks), 256, 0, ctx->stream>>>(P);
+  DP_CHECK_CUDA(ctx, cudaGetLastError());
+  timed_end(ctx, "mc_init");
   int rc = launch_phase<R, 0>(ctx, P, smem, need);
   if (rc) return rc;
-  return launch_phase<R, 1>(ctx, P, smem, need);
+  rc = launch_phase<R, 1>(ctx, P, smem, need);
+  if (rc) return rc;
+  timed_begin(ctx);
+  mc_finish_kernel<R><<<int(rec_blocks), 256, 0, ctx->stream>>>(P);
+  DP_CHECK_CUDA(ctx, cudaGetLastError());
+  timed_end(ctx, "mc_finish");
+  return DP_OK;
 }
 
 int run(dp_ctx* ctx, McParams& P, int precision) {
@@ -842,7 +944,7 @@ int dp_mc_histories(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock_c,
   long ng = geo_stride ? n : 1;
   size_t nb = size_t(n) * sizeof(double), gb = size_t(ng) * sizeof(double);
   Arena A;
-  A.base = static_cast<char*>(scratch(ctx, 8 * nb + 4 * gb + size_t(n) * (8 + sizeof(Handoff<double>)) + 4096, 0));
+  A.base = static_cast<char*>(scratch(ctx, 8 * nb + 4 * gb + size_t(n) * (8 + kRecBytes) + 4096, 0));
   A.cap = ctx->slot_bytes[0];
   double* dE = A.take<double>(n);
   double* dq = A.take<double>(n);
@@ -857,7 +959,9 @@ int dp_mc_histories(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock_c,
   int32_t* dn = A.take<int32_t>(n);
   unsigned long long* ctr = A.take<unsigned long long>(3);
   Handoff<double>* queue = A.take<Handoff<double>>(n);
-  if (!queue) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
+  StartRec<double>* srec = A.take<StartRec<double>>(n);
+  EndRec<double>* erec = A.take<EndRec<double>>(n);
+  if (!erec) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
   cudaStream_t s = ctx->stream;
   DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dE, E, nb, cudaMemcpyHostToDevice, s));
   DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dq, q, nb, cudaMemcpyHostToDevice, s));
@@ -884,6 +988,8 @@ int dp_mc_histories(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock_c,
   P.efinal = dEf;
   P.counter = ctr;
   P.queue = queue;
+  P.start = srec;
+  P.end = erec;
   rc = run(ctx, P, cfg->precision);
   if (rc) return rc;
   std::vector<int32_t> st_h;
@@ -977,13 +1083,15 @@ int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_
   long nt = total > 0 ? total : 1;
   Arena A;
   A.base = static_cast<char*>(scratch(
-      ctx, size_t(nt) * (12 + 16 + sizeof(Handoff<double>)) + size_t(n_los + 1) * 8 + 4096, 0));
+      ctx, size_t(nt) * (12 + 16 + kRecBytes) + size_t(n_los + 1) * 8 + 4096, 0));
   A.cap = ctx->slot_bytes[0];
   double* dc = A.take<double>(nt);
   int32_t* ds = A.take<int32_t>(nt);
   int64_t* off = A.take<int64_t>(n_los + 1);
   unsigned long long* ctr = A.take<unsigned long long>(3);
   Handoff<double>* queue = A.take<Handoff<double>>(nt);
+  StartRec<double>* srec = A.take<StartRec<double>>(nt);
+  EndRec<double>* erec = A.take<EndRec<double>>(nt);
   double* cc = compute_gradient ? A.take<double>(nt) : nullptr;
   double* cd = compute_gradient ? A.take<double>(nt) : nullptr;
   int* bits = A.take<int>(1);
@@ -1003,6 +1111,8 @@ int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_
     P.status = ds;
     P.counter = ctr;
     P.queue = queue;
+    P.start = srec;
+    P.end = erec;
     rc = run(ctx, P, cfg->precision);
     if (rc) return rc;
     if (compute_gradient) {

@@ -56,7 +56,22 @@ struct Layout {
   double lE0, inv_dlE;
   int kuniform;        // MIXED kernel energies: the uniform log grid refined 8-fold
   double kinv_dlE;     // 1 / log step of the kernel energies
+  uint32_t o_idx;      // byte offset of the inverse-lookup index tables (int16)
+  int nbp, nbk;        // index bins of the physics and kernel columns
+  uint32_t o_elf;      // byte offset of the FP32 element table (kElfStride floats each)
 };
+// FP32 element table for the cooperative DCS sums: Z, A, I, fraction,
+// N_A / (A 1e-3) (per-mass scale).
+constexpr int kElfStride = 8;
+
+// Inverse lookups (energy from a range or hazard value) start from an index
+// table over log-uniform bins of the column's values instead of a bisection:
+// entry b holds the last node at or below the bin's lower edge; the search
+// then walks up (a few nodes).  Columns: 0 CSDA range, 1 restricted range
+// (physics grid), 2 kernel range, 3 kernel hazard.  Per column the bin
+// origin and inverse width (two doubles) follow the elements.
+enum IdxCol { I_CR = 0, I_MR, I_KR, I_KH, I_NCOL };
+constexpr int kIdxBinsPhys = 256, kIdxBinsKer = 1024;
 struct MedInfo {
   int nm, nel;
   double frac[kMaxMix];
@@ -68,6 +83,8 @@ struct Med {
   const R* p;
   const R* kp;
   const double* el;
+  const float* elf;
+  const int16_t* idx;
   int ld, ldk, n, nk, nm, nel, slots, uniform, kuniform;
   R frac[kMaxMix];
   R ZoA, onset, lE0, inv_dlE, kinv_dlE;
@@ -83,6 +100,8 @@ __device__ __forceinline__ Med<R> make_med(const unsigned char* base, const Layo
   m.p = reinterpret_cast<const R*>(base + L.o_phys);
   m.kp = reinterpret_cast<const R*>(base + L.o_ker);
   m.el = reinterpret_cast<const double*>(base);
+  m.elf = reinterpret_cast<const float*>(base + L.o_elf);
+  m.idx = reinterpret_cast<const int16_t*>(base + L.o_idx);
   m.ld = L.ld;
   m.ldk = L.ldk;
   m.n = L.n;
@@ -106,6 +125,7 @@ __device__ __forceinline__ Med<R> make_med(const unsigned char* base, const Layo
 struct Consts {
   double mass, ctau, cutoff, elastic_ratio;
   double thr_low, thr;  // mode switch and source ceiling (GeV)
+  float thr_low_f, thr_f;  // the same in FP32 (exact for the FP32 transport)
   int straggling, scattering;
 };
 
@@ -222,6 +242,28 @@ __device__ __forceinline__ R at(const Med<R>& m, const Loc<R>& L, int col) {
   if (L.edge > 0) return y[m.n - 1];
   return y[L.i] + L.t * (y[L.i + 1] - y[L.i]);
 }
+// Starting node of an inverse lookup of x in index column `which`.
+template <class R>
+__device__ __forceinline__ int index_guess(const Med<R>& m, int which, R x) {
+  const R* prm = reinterpret_cast<const R*>(m.el + kMaxEl * kElStride) + 2 * which;
+  const int nb = which < I_KR ? kIdxBinsPhys : kIdxBinsKer;
+  const int16_t* idx = m.idx + (which < I_KR ? which * kIdxBinsPhys
+                                             : 2 * kIdxBinsPhys + (which - I_KR) * kIdxBinsKer);
+  if (!(x > R(0))) return 0;
+  R f = (log(x) - prm[0]) * prm[1];
+  int b = !(f >= R(0)) ? 0 : (f >= R(nb) ? nb - 1 : int(f));
+  return idx[b];
+}
+// Largest i in [0, n-2] with xs[i] <= x, walking from a guess (equals the
+// bisection for x inside (xs[0], xs[n-1])).
+template <class R>
+__device__ __forceinline__ int walk_from(const R* xs, int n, R x, int i) {
+  i = i < 0 ? 0 : (i > n - 2 ? n - 2 : i);
+  while (i > 0 && x < xs[i]) --i;
+  while (i < n - 2 && !(x < xs[i + 1])) ++i;
+  return i;
+}
+
 // Inverse of a range column (src/Physics.jl:833-867).
 template <class R>
 __device__ __forceinline__ R inv_range(const Med<R>& m, int col, R X) {
@@ -229,7 +271,7 @@ __device__ __forceinline__ R inv_range(const Med<R>& m, int col, R X) {
   int n = m.n;
   if (X <= Rc[0]) return m.col(MC_E)[0];
   if (X >= Rc[n - 1]) return m.col(MC_E)[n - 1];
-  int i = bisect_r(Rc, n, X);
+  int i = walk_from(Rc, n, X, index_guess(m, col == MC_CR ? I_CR : I_MR, X));
   const R* lE = m.col(MC_LE);
   R t = (X - Rc[i]) / (Rc[i + 1] - Rc[i]);
   return exp(lE[i] + t * (lE[i + 1] - lE[i]));
@@ -335,9 +377,34 @@ __device__ __forceinline__ KLoc<R> klocate_e(const Med<R>& m, R x, int* status) 
   L.f = d == R(0) ? R(0) : (x - xs[i]) / d;
   return L;
 }
+// searchsortedlast location on the kernel's range or hazard axis from its
+// index table.
+template <class R>
+__device__ __forceinline__ KLoc<R> klocate_idx(const Med<R>& m, int xcol, R x, int* status) {
+  const R* xs = m.kcol(xcol);
+  const int n = m.nk;
+  KLoc<R> L{0, 0, R(0)};
+  if (x < xs[0]) {
+    *status |= ST_DOMAIN_LO;
+    L.edge = -1;
+    return L;
+  }
+  if (x > xs[n - 1]) {
+    *status |= ST_DOMAIN_HI;
+    L.edge = 1;
+    return L;
+  }
+  if (!(x == x)) return klocate(xs, n, x, status);
+  int i = walk_from(xs, n, x, index_guess(m, xcol == K_R ? I_KR : I_KH, x));
+  R d = xs[i + 1] - xs[i];
+  L.i = i;
+  L.f = d == R(0) ? R(0) : (x - xs[i]) / d;
+  return L;
+}
 template <class R>
 __device__ __forceinline__ R klookup(const Med<R>& m, int xcol, int ycol, R x, int* status) {
   if (xcol == K_E) return kat(m.kcol(ycol), m.nk, klocate_e(m, x, status));
+  if (xcol == K_R || xcol == K_H) return kat(m.kcol(ycol), m.nk, klocate_idx(m, xcol, x, status));
   return kat(m.kcol(ycol), m.nk, klocate(m.kcol(xcol), m.nk, x, status));
 }
 
@@ -384,15 +451,15 @@ constexpr int kItemsPerElement = 23;
 // terms (per-mass scale N_A/(A 1e-3) against FP32 underflow), the components
 // are summed in a fixed order into comp[] (kept for the pick) and the total
 // is reduced in a fixed tree; all 32 lanes call it with the same arguments.
-__device__ __noinline__ double coop_total(const double* el, int nel, double mass, double anc,
+__device__ __noinline__ double coop_total(const float* elf, int nel, float fm, double anc,
                                           double q, float* item, float* comp) {
   const int lane = threadIdx.x & 31;
-  const float fm = float(mass), fk = float(anc), fq = float(q);
+  const float fk = float(anc), fq = float(q);
   const int n_items = kItemsPerElement * nel;
   for (int it = lane; it < n_items; it += 32) {
     const int e = it / kItemsPerElement, j = it - e * kItemsPerElement;
-    const double* x = el + kElStride * e;
-    const float Z = float(x[0]), A = float(x[1]), sc = float(kAvogadro / (x[1] * 0.001));
+    const float* x = elf + kElfStride * e;
+    const float Z = x[0], A = x[1], sc = x[4];
     float v = 0.f;
     if (j == 0) {
       v = dcs_brems<float>(Z, A, fm, fk, fq, sc);
@@ -405,7 +472,7 @@ __device__ __noinline__ double coop_total(const double* el, int nel, double mass
       if (photo_range<float>(Z, A, fm, fk, fq, &lmin, &dx))
         v = photo_point<float>(Z, A, fm, fk, fq, lmin, dx, j - 13, sc);
     } else {
-      v = dcs_ionisation<float>(Z, float(x[2]), fm, fk, fq, sc);
+      v = dcs_ionisation<float>(Z, x[2], fm, fk, fq, sc);
     }
     item[it] = isfinite(v) ? v : 0.f;
   }
@@ -427,7 +494,7 @@ __device__ __noinline__ double coop_total(const double* el, int nel, double mass
     } else {
       v = item[base + 22];
     }
-    v *= float(el[kElStride * e + 3] * anc);  // fraction x ancestor energy
+    v *= elf[kElfStride * e + 3] * fk;  // fraction x ancestor energy
     comp[c] = v;
     mine += v;
   }
@@ -496,10 +563,43 @@ __device__ __noinline__ DelOut reverse_del(const Med<R>& m, const Consts& C, dou
   return del_end(anc, denom, total, pick);
 }
 
+// Altitude of a history and of the layer boundaries.  FP64 transport: a
+// double.  FP32 transport: an unevaluated pair hi + lo of floats updated by
+// compensated sums (about 48 bits), so that the step loop needs no FP64
+// instruction (FP64 issues at 1/64 of the FP32 rate on this GPU).  Only the
+// altitude enters the transport; the horizontal position is not tracked.
+struct F2 {
+  float h, l;
+};
+template <class R> struct AltT;
+template <> struct AltT<double> { using type = double; };
+template <> struct AltT<float> { using type = F2; };
+template <class R> using Alt = typename AltT<R>::type;
+
+__device__ __forceinline__ double alt_value(double z) { return z; }
+__device__ __forceinline__ double alt_value(F2 z) { return double(z.h) + double(z.l); }
+template <class R> __device__ __forceinline__ Alt<R> alt_make(double v);
+template <> __device__ __forceinline__ double alt_make<double>(double v) { return v; }
+template <> __device__ __forceinline__ F2 alt_make<float>(double v) {
+  float h = float(v);
+  return F2{h, float(v - double(h))};
+}
+// z += dz
+__device__ __forceinline__ void alt_add(double& z, double dz) { z += dz; }
+__device__ __forceinline__ void alt_add(F2& z, float dz) {
+  float s = z.h + dz, bp = s - z.h;
+  float e = (z.h - (s - bp)) + (dz - bp);
+  float l = z.l + e, h = s + l;
+  z.l = l - (h - s);
+  z.h = h;
+}
+// a - b in the transport precision
+__device__ __forceinline__ float alt_sub(F2 a, F2 b) { return (a.h - b.h) + (a.l - b.l); }
+
 // Mutable part of a history.
 template <class R>
 struct State {
-  double x, y, z;
+  Alt<R> z;
   R ux, uy, uz, E, w;
   int status;
 };
@@ -511,7 +611,7 @@ struct State {
 // energy, r2 = event grammage, r3 = density, flag = scattering.
 template <class R>
 struct Cont {
-  double a, b, c, d;
+  R a, b, c, d, dist;  // dist: requested length of a mixed step
   R r0, r1, r2, r3;
   int event, kind, medium, flag;
   double anc, q, denom;  // the pending event: ancestor, energy transfer, weight denominator
@@ -522,20 +622,22 @@ struct Cont {
 enum : int { CONT_NONE = 0, CONT_MIXED = 1, CONT_STRAG = 2 };
 
 // transport_mixed_step (src/MixedTransport.jl:144-200), resumable.  The
-// grammage bookkeeping (requested, remaining, travelled) is FP64 in both
-// precisions: in FP32 the reference's round-off floor eps(max(1, grammage))
-// would exceed the grammage of the 1e-7 m boundary-crossing steps.
+// round-off floor of the grammage bookkeeping is the reference's FP64
+// eps(max(1, grammage)) in both precisions: an FP32 ulp would exceed the
+// grammage of the 1e-7 m boundary-crossing steps.
 template <class R>
 __device__ void mixed_end(State<R>& s, const Cont<R>& x, R Emax, R energy_limit, bool exhausted) {
   if (exhausted) s.status |= ST_EVENT_CAP;
   if (x.r1 > R(0) && x.r0 >= Emax && x.a > x.d && (energy_limit < R(0) || x.r0 < energy_limit))
     s.status |= ST_DOMAIN_HI;
-  double d = x.b / x.c;
+  // FP64: travelled / density as the reference; FP32: the requested length
+  // when the segment was consumed
+  R d;
+  if (sizeof(R) == 4 && x.a <= x.d) d = x.dist;
+  else d = x.b / x.c;
   s.E = x.r0;
   s.w = x.r1;
-  s.x -= d * double(s.ux);
-  s.y -= d * double(s.uy);
-  s.z -= d * double(s.uz);
+  alt_add(s.z, -(d * s.uz));
 }
 // Applies a hard event; true when the history's weight vanished.
 template <class R>
@@ -552,7 +654,7 @@ __device__ __noinline__ bool mixed_run(const Med<R>& m, const Consts& C, State<R
   const int nk = m.nk;
   const R* kE = m.kcol(K_E);
   const R Emax = kE[nk - 1];
-  const R mass = R(C.mass), ctau = R(C.ctau), rdens = R(x.c);
+  const R mass = R(C.mass), ctau = R(C.ctau), rdens = x.c;
   for (; x.event < 100000; ++x.event) {
     R k = x.r0;
     if (x.a <= x.d || k >= x.r2) {
@@ -562,24 +664,22 @@ __device__ __noinline__ bool mixed_run(const Med<R>& m, const Consts& C, State<R
     KLoc<R> Lk = klocate_e(m, k, &s.status);
     R ri = kat(m.kcol(K_R), nk, Lk), hi = kat(m.kcol(K_H), nk, Lk);
     R rtc = fmax(R(0), klookup(m, K_E, K_R, x.r2, &s.status) - ri);
-    double eg = fmin(x.a, double(rtc));
-    R endpoint = eg == double(rtc) ? x.r2
-                                   : fmax(k, klookup(m, K_R, K_E, R(double(ri) + eg), &s.status));
+    R eg = fmin(x.a, rtc);
+    R endpoint = eg == rtc ? x.r2 : fmax(k, klookup(m, K_R, K_E, ri + eg, &s.status));
     R eventh = hi + expo<R>(g);
     bool occurs = eventh < klookup(m, K_E, K_H, endpoint, &s.status);
     R pre = occurs ? fmax(k, klookup(m, K_H, K_E, eventh, &s.status)) : endpoint;
     KLoc<R> Lp = klocate_e(m, pre, &s.status);
-    double dxd = occurs ? double(fmax(R(0), kat(m.kcol(K_R), nk, Lp) - ri)) : eg;
-    R dx = R(dxd);
+    R dx = occurs ? fmax(R(0), kat(m.kcol(K_R), nk, Lp) - ri) : eg;
     R dt;
     if (dx <= R(8) * ulp_up(fabs(ri)) || pre - k <= R(8) * ulp_up(fabs(k)))
-      dt = R(dxd / x.c) * mass / R(2) *
+      dt = dx / x.c * mass / R(2) *
            (R(1) / sqrt(k * (k + R(2) * mass)) + R(1) / sqrt(pre * (pre + R(2) * mass)));
     else
       dt = (kat(m.kcol(K_T), nk, Lp) - kat(m.kcol(K_T), nk, Lk)) / rdens;
     x.r1 *= kat(m.kcol(K_S), nk, Lp) / kat(m.kcol(K_S), nk, Lk) * exp(-dt / ctau);
-    x.b += dxd;
-    x.a = fmax(0.0, x.a - dxd);
+    x.b += dx;
+    x.a = fmax(R(0), x.a - dx);
     x.r0 = pre;
     if (!occurs) {
       mixed_end(s, x, Emax, energy_limit, false);
@@ -605,18 +705,20 @@ __device__ __noinline__ bool mixed_run(const Med<R>& m, const Consts& C, State<R
 }
 // Starts a mixed step of `distance` m at `density`; true when it suspended.
 template <class R, bool COOP>
-__device__ bool mixed_step(const Med<R>& m, const Consts& C, State<R>& s, double density,
-                           double distance, Stream& g, R energy_limit, Cont<R>& x) {
+__device__ bool mixed_step(const Med<R>& m, const Consts& C, State<R>& s, R density, R distance,
+                           Stream& g, R energy_limit, Cont<R>& x) {
   const R Emax = m.kcol(K_E)[m.nk - 1];
   if (s.E > Emax) {
     s.status |= ST_DOMAIN_HI;
     return false;
   }
   x.a = distance * density;
-  x.b = 0.0;
+  x.b = R(0);
   x.c = density;
-  const double dXreq = fmax(1.0, distance * density);
-  x.d = ulp_up(dXreq);
+  x.dist = distance;
+  const R dXreq = fmax(R(1), distance * density);
+  if (sizeof(R) == 8) x.d = ulp_up(dXreq);
+  else x.d = dXreq * R(2.220446049250313e-16);
   x.r0 = s.E;
   x.r1 = s.w;
   x.r2 = energy_limit > R(0) ? fmin(energy_limit, Emax) : Emax;
@@ -910,11 +1012,11 @@ __device__ __forceinline__ double polar_ioni(double m, double ki, double kf) {
 template <class R>
 __device__ __noinline__ void straggled_end(const Med<R>& m, const Consts& C, State<R>& s, const Loc<R>& Li,
                               R ki, R kf, R ckf, R dX, double dw, int proc, int elem, bool del,
-                              bool ehs, R k_ehs, R density, double step, bool shortened,
+                              bool ehs, R k_ehs, R density, R step, bool shortened,
                               bool scattering, Stream& g) {
   const R mass = R(C.mass);
   R astep = dX / density;
-  R ox = s.ux, oy = s.uy, oz = s.uz;  // the position moves along the incoming direction
+  R oz = s.uz;  // the position moves along the incoming direction
   if (scattering) {
     if (del && proc > 0) {
       const double* e = m.el + kElStride * elem;
@@ -936,13 +1038,12 @@ __device__ __noinline__ void straggled_end(const Med<R>& m, const Consts& C, Sta
          (R(1) / sqrt(ki * (ki + R(2) * mass)) + R(1) / sqrt(ckf * (ckf + R(2) * mass)));
   // FP64: the reference's dX/density; FP32: the requested FP64 step unless
   // an event or the energy limit shortened it
-  double da = double(astep);
-  if (sizeof(R) == 4) da = shortened ? double(dX) / double(density) : step;
-  s.x -= da * double(ox);
-  s.y -= da * double(oy);
-  s.z -= da * double(oz);
+  R da = astep;
+  if (sizeof(R) == 4) da = shortened ? dX / density : step;
+  alt_add(s.z, -(da * oz));
   R wf = at(m, locate(m, ckf), MC_MS) / at(m, Li, MC_MS);
-  s.w = R(double(s.w * wf * exp(-pt / R(C.ctau))) * dw);
+  if (sizeof(R) == 4) s.w = s.w * wf * exp(-pt / R(C.ctau)) * R(dw);
+  else s.w = R(double(s.w * wf * exp(-pt / R(C.ctau))) * dw);
   s.E = kf;
 }
 
@@ -951,10 +1052,10 @@ __device__ __noinline__ void straggled_end(const Med<R>& m, const Consts& C, Sta
 // needs.
 template <class R, bool COOP>
 __device__ bool straggled_step(const Med<R>& m, const Consts& C, State<R>& s, const Loc<R>& Li,
-                               R density, double step, Stream& g, bool scattering, R energy_limit,
+                               R density, R step, Stream& g, bool scattering, R energy_limit,
                                Cont<R>& x) {
   const R mass = R(C.mass), eratio = R(C.elastic_ratio);
-  R ki = s.E, dX = R(step) * density;
+  R ki = s.E, dX = step * density;
   bool shortened = false;  // the step ended before its requested length
   R Xi = at(m, Li, MC_MR);
   R kf = ki, ratio = R(1);
@@ -1041,17 +1142,14 @@ __device__ bool straggled_step(const Med<R>& m, const Consts& C, State<R>& s, co
 // Deterministic CSDA step on a medium (src/Geometry.jl:424-457).
 template <class R>
 __device__ __forceinline__ void csda_step(const Med<R>& m, const Consts& C, State<R>& s,
-                                          const Loc<R>& Li, R density, double step_d) {
-  const R mass = R(C.mass), step = R(step_d);
+                                          const Loc<R>& Li, R density, R step) {
+  const R mass = R(C.mass);
   R ki = s.E, dX = step * density;
   R kf = inv_range(m, MC_CR, at(m, Li, MC_CR) + dX);
   R gm = (R(1) + ki / mass + R(1) + kf / mass) / R(2);
   R b = sqrt(fmax(R(1) - R(1) / (gm * gm), R(1e-12)));
   R dt = step / (b * gm);
-  double ds = step_d;
-  s.x -= ds * double(s.ux);
-  s.y -= ds * double(s.uy);
-  s.z -= ds * double(s.uz);
+  alt_add(s.z, -(step * s.uz));
   s.w = s.w * (at(m, locate(m, kf), MC_CS) / at(m, Li, MC_CS)) * exp(-dt / R(C.ctau));
   s.E = kf;
 }
@@ -1062,8 +1160,9 @@ __device__ __forceinline__ void csda_step(const Med<R>& m, const Consts& C, Stat
 template <class R>
 struct Hist {
   State<R> s;
-  double limit;  // energy limit of the current mode (exactly representable in R)
-  double thick, rho, H, q, ws;
+  R limit;  // energy limit of the current mode (exactly representable in R)
+  Alt<R> thick, H;
+  R rho;
   int steps, inner, outer;
   bool need_mode, strag, mixed, scat;
   Cont<R> x;     // suspended step, if x.kind != CONT_NONE
@@ -1087,21 +1186,60 @@ __device__ __forceinline__ int step_done(Hist<R>& h) {
 
 // Advances a history by one transport step: ADV_STEP, ADV_DONE when it has
 // ended, ADV_WAIT when the step suspended on a hard-event DCS sum.
+// Geometry of the current step (src/Geometry.jl:553-650): whether the
+// history has left the column, the medium, the distance to the boundary
+// ahead and the local density.  FP64: the reference's operations on doubles;
+// FP32: the altitude pairs and FP32 arithmetic.
+__device__ __forceinline__ bool outside(double z, double H) {
+  return z < 0.0 || z >= H - kEps64;
+}
+__device__ __forceinline__ bool outside(F2 z, F2 H) {
+  return z.h + z.l < 0.f || alt_sub(z, H) >= 0.f;
+}
+__device__ __forceinline__ bool in_air_at(double z, double thick) { return z >= thick; }
+__device__ __forceinline__ bool in_air_at(F2 z, F2 thick) { return alt_sub(z, thick) >= 0.f; }
+__device__ __forceinline__ void boundary(double z, double thick, double H, bool in_air, double uz,
+                                         double rho, double* tob, double* dens) {
+  const double eps = kEps64;
+  if (!in_air) {
+    *dens = rho;
+    *tob = uz > eps ? (thick - z) / uz : uz < -eps ? (0.0 - z) / uz : 1000.0;
+  } else {
+    *dens = 1.205 * exp(-z / 12e3);
+    *tob = uz > eps ? (H - z) / uz : uz < -eps ? (thick - z) / uz : 1000.0;
+  }
+}
+__device__ __forceinline__ void boundary(F2 z, F2 thick, F2 H, bool in_air, float uz, float rho,
+                                         float* tob, float* dens) {
+  const float eps = float(kEps64);
+  float ahead = !in_air ? (uz > eps ? alt_sub(thick, z) : -(z.h + z.l))
+                        : (uz > eps ? alt_sub(H, z) : alt_sub(thick, z));
+  *tob = (uz > eps || uz < -eps) ? ahead / uz : 1000.f;
+  *dens = !in_air ? rho : 1.205f * expf(-(z.h + z.l) * (1.f / 12e3f));
+}
+
+// Advances a history by one transport step: ADV_STEP, ADV_DONE when it has
+// ended, ADV_WAIT when the step suspended on a hard-event DCS sum,
+// ADV_HANDOFF when phase 0 reached the mode switch.
 template <class R, bool COOP, int PHASE>
 __device__ __forceinline__ int advance(const Med<R>& rock, const Med<R>& air, const Consts& C,
                                        Hist<R>& h, Stream& g) {
   const double eps = kEps64;
   State<R>& s = h.s;
+  // FP32: thresholds are exactly representable (the host rounds them), eps
+  // below their resolution
+  const R thr = sizeof(R) == 8 ? R(C.thr) : R(C.thr_f);
+  const R thr_low = sizeof(R) == 8 ? R(C.thr_low) : R(C.thr_low_f);
   for (int guard = 0; guard < 4; ++guard) {
     if (h.need_mode) {
-      if (!(double(s.E) < C.thr - eps)) return ADV_DONE;
+      if (sizeof(R) == 8 ? !(double(s.E) < C.thr - eps) : !(s.E < thr)) return ADV_DONE;
       if (h.outer >= 1000) {
         s.status |= ST_OUTER_CAP;
         return ADV_DONE;
       }
-      if (s.z < 0.0 || s.z >= h.H - eps) return ADV_DONE;
+      if (outside(s.z, h.H)) return ADV_DONE;
       if (!(s.w > R(0)) || !isfinite(s.w)) return ADV_DONE;
-      if (double(s.E) < C.thr_low - eps) {
+      if (sizeof(R) == 8 ? double(s.E) < C.thr_low - eps : s.E < thr_low) {
         if (PHASE == 1) {  // not reached: the energy never decreases
           s.status |= ST_OUTER_CAP;
           return ADV_DONE;
@@ -1109,36 +1247,29 @@ __device__ __forceinline__ int advance(const Med<R>& rock, const Med<R>& air, co
         h.strag = C.straggling != 0;
         h.mixed = false;
         h.scat = C.scattering != 0;
-        h.limit = fmin(C.thr_low, C.thr);
+        h.limit = fmin(thr_low, thr);
       } else {
         if (PHASE == 0) return ADV_HANDOFF;  // need_mode stays set for phase 1
         h.strag = false;
         h.mixed = C.straggling != 0;
         h.scat = false;
-        h.limit = C.thr;
+        h.limit = thr;
       }
       h.inner = 0;
       ++h.outer;
       h.need_mode = false;
     }
-    if (h.inner >= 50000 || s.z < 0.0 || s.z >= h.H - eps || double(s.E) >= h.limit - eps ||
-        !(s.w > R(0)) || !isfinite(s.w)) {
+    const bool at_limit = sizeof(R) == 8 ? double(s.E) >= double(h.limit) - eps : s.E >= h.limit;
+    if (h.inner >= 50000 || outside(s.z, h.H) || at_limit || !(s.w > R(0)) || !isfinite(s.w)) {
       h.need_mode = true;
       continue;
     }
     // medium, boundary distance and step (src/Geometry.jl:603-650, :461-476)
-    double uz = -double(s.uz);
-    bool in_air = s.z >= h.thick;
+    const bool in_air = in_air_at(s.z, h.thick);
     const Med<R>& m = in_air ? air : rock;
-    double dens, tob;
-    if (!in_air) {
-      dens = h.rho;
-      tob = uz > eps ? (h.thick - s.z) / uz : uz < -eps ? (0.0 - s.z) / uz : 1000.0;
-    } else {
-      dens = 1.205 * exp(-s.z / 12e3);
-      tob = uz > eps ? (h.H - s.z) / uz : uz < -eps ? (h.thick - s.z) / uz : 1000.0;
-    }
-    const R rd = R(dens);
+    const R uz = -s.uz;
+    R tob, rd;
+    boundary(s.z, h.thick, h.H, in_air, uz, h.rho, &tob, &rd);
     Loc<R> Li = locate(m, s.E);
     R Xi = at(m, Li, MC_CR);
     R lim = R(0.01) * Xi / fmax(rd, R(1e-6));
@@ -1146,12 +1277,12 @@ __device__ __forceinline__ int advance(const Med<R>& rock, const Med<R>& air, co
       R lb1 = transport_path(m, Li);
       if (lb1 > R(0) && rd > R(0)) lim = fmin(lim, R(0.01) * lb1 / rd);
     }
-    if (in_air) lim = fmin(lim, R(0.05 * 12e3) / fmax(R(fabs(uz)), R(0.05)));
-    double step = fmin(tob + 1e-7, double(lim));
-    step = fmin(fmax(step, kStepMin), 1000.0);
+    if (in_air) lim = fmin(lim, R(0.05 * 12e3) / fmax(fabs(uz), R(0.05)));
+    R step = fmin(tob + R(1e-7), lim);
+    step = fmin(fmax(step, R(kStepMin)), R(1000));
     if (PHASE == 0 && h.strag) {
       if constexpr (PHASE == 0) {
-        if (straggled_step<R, COOP>(m, C, s, Li, rd, step, g, h.scat, R(h.limit), h.x)) {
+        if (straggled_step<R, COOP>(m, C, s, Li, rd, step, g, h.scat, h.limit, h.x)) {
           h.x.kind = CONT_STRAG;
           h.x.medium = in_air;
           return ADV_WAIT;
@@ -1159,7 +1290,7 @@ __device__ __forceinline__ int advance(const Med<R>& rock, const Med<R>& air, co
       }
     } else if (PHASE == 1 && h.mixed) {
       if constexpr (PHASE == 1) {
-        if (mixed_step<R, COOP>(m, C, s, dens, step, g, R(h.limit), h.x)) {
+        if (mixed_step<R, COOP>(m, C, s, rd, step, g, h.limit, h.x)) {
           h.x.kind = CONT_MIXED;
           h.x.medium = in_air;
           return ADV_WAIT;
@@ -1187,10 +1318,10 @@ __device__ int resume(const Med<R>& rock, const Med<R>& air, const Consts& C, Hi
   if constexpr (PHASE == 1) {
     const R Emax = m.kcol(K_E)[m.nk - 1];
     if (mixed_event(h.s, x, d)) {
-      mixed_end(h.s, x, Emax, R(h.limit), false);
+      mixed_end(h.s, x, Emax, h.limit, false);
     } else {
       ++x.event;
-      if (mixed_run<R, true>(m, C, h.s, x, g, R(h.limit))) {
+      if (mixed_run<R, true>(m, C, h.s, x, g, h.limit)) {
         x.kind = CONT_MIXED;
         return ADV_WAIT;
       }
@@ -1207,8 +1338,8 @@ __device__ int resume(const Med<R>& rock, const Med<R>& air, const Consts& C, Hi
 // counters and random stream position.
 template <class R>
 struct Handoff {
-  double x, y, z, thick, rho, H, q, ws;
-  R ux, uy, uz, E, w;
+  Alt<R> z, thick, H;
+  R rho, ux, uy, uz, E, w;
   int status, steps, outer, used;
   uint32_t block, w0, w1, w2, w3;
   long index;       // history index (output slot)
@@ -1218,14 +1349,10 @@ template <class R>
 __device__ __forceinline__ void save_handoff(const Hist<R>& h, const Stream& g, long i,
                                              Handoff<R>* o) {
   Handoff<R> v;
-  v.x = h.s.x;
-  v.y = h.s.y;
   v.z = h.s.z;
   v.thick = h.thick;
   v.rho = h.rho;
   v.H = h.H;
-  v.q = h.q;
-  v.ws = h.ws;
   v.ux = h.s.ux;
   v.uy = h.s.uy;
   v.uz = h.s.uz;
@@ -1247,14 +1374,10 @@ __device__ __forceinline__ void save_handoff(const Hist<R>& h, const Stream& g, 
 template <class R>
 __device__ __forceinline__ long load_handoff(const Handoff<R>& v, uint64_t seed, Hist<R>& h,
                                              Stream& g) {
-  h.s.x = v.x;
-  h.s.y = v.y;
   h.s.z = v.z;
   h.thick = v.thick;
   h.rho = v.rho;
   h.H = v.H;
-  h.q = v.q;
-  h.ws = v.ws;
   h.s.ux = v.ux;
   h.s.uy = v.uy;
   h.s.uz = v.uz;
@@ -1264,7 +1387,7 @@ __device__ __forceinline__ long load_handoff(const Handoff<R>& v, uint64_t seed,
   h.steps = v.steps;
   h.outer = v.outer;
   h.inner = 0;
-  h.limit = 0.0;
+  h.limit = R(0);
   h.need_mode = true;
   h.strag = h.mixed = h.scat = false;
   h.x.kind = CONT_NONE;
@@ -1278,16 +1401,33 @@ __device__ __forceinline__ long load_handoff(const Handoff<R>& v, uint64_t seed,
   return v.index;
 }
 
+// Start record of a history, written by the init kernel in one converged
+// pass (energy, charge and geometry draws, direction), read by phase 0.
+template <class R>
+struct StartRec {
+  Alt<R> thick, H;
+  double q, ws;  // charge and sampling weight (read back by the finish kernel)
+  R E, rho, ux, uz;
+};
+// End record of a history, written by the transport, turned into the flux
+// contribution by the finish kernel.
+template <class R>
+struct EndRec {
+  Alt<R> z;
+  R E, w, uz;
+  int status, steps;
+};
+
 // Contribution of an ended history (src/Geometry.jl:729-757), FP64.
 template <class R>
-__device__ __forceinline__ double history_flux(const Consts& C, const Hist<R>& h) {
-  const State<R>& s = h.s;
-  if (s.status & ST_FATAL) return 0.0;
-  if (s.z >= h.H - 1.0 && double(s.E) < C.thr) {
-    double c = fmin(fmax(-double(s.uz), 0.0), 1.0);
+__device__ __forceinline__ double history_flux(const Consts& C, const EndRec<R>& e, double H,
+                                               double q) {
+  if (e.status & ST_FATAL) return 0.0;
+  if (alt_value(e.z) >= H - 1.0 && double(e.E) < C.thr) {
+    double c = fmin(fmax(-double(e.uz), 0.0), 1.0);
     if (c <= 0.0) return 0.0;
     double cs = cos_theta_star(c);
-    return double(s.w) * gccly_flux(cs, pow(cs, 1.29), double(s.E), h.q, nullptr);
+    return double(e.w) * gccly_flux(cs, pow(cs, 1.29), double(e.E), q, nullptr);
   }
   return 0.0;
 }
