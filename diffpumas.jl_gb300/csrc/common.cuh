@@ -216,6 +216,27 @@ DP_HD double gccly_flux(double cs, double cs129, double K, double q, double* dlo
   return f;
 }
 
+// ------------------------------------------------------------- altitude pairs
+// An unevaluated pair hi + lo of floats (about 48 bits) for positions in the
+// FP32 transports: compensated updates and differences, no FP64 instruction.
+struct F2 {
+  float h, l;
+};
+DP_HD F2 f2_make(double v) {
+  float h = float(v);
+  return F2{h, float(v - double(h))};
+}
+// z += dz (TwoSum of the high parts, error folded into the low part)
+DP_HD void alt_add(F2& z, float dz) {
+  float s = z.h + dz, bp = s - z.h;
+  float e = (z.h - (s - bp)) + (dz - bp);
+  float l = z.l + e, h = s + l;
+  z.l = l - (h - s);
+  z.h = h;
+}
+// a - b as a float
+DP_HD float alt_sub(F2 a, F2 b) { return (a.h - b.h) + (a.l - b.l); }
+
 // ------------------------------------------------------------- tallies
 // Compensated (TwoSum) accumulator for the deterministic FP64 tallies.
 struct KSum {

@@ -315,62 +315,66 @@ __global__ void __launch_bounds__(128) csda32_kernel(CsdaParams P, const float* 
       w = P.w[i];
     }
     Df E{float(E0), 0.f}, wt{1.f, 0.f};
-    double zv = 0.0;
+    // altitude as an FP32 pair with its FP32 tangent; boundaries likewise
+    F2 z{0.f, 0.f};
     float zd = 0.f;
+    const F2 thick = f2_make(G.thickness), Htop = f2_make(G.H);
     const Df rho{float(G.rho), 1.f};
-    const float uz = float(G.uz), dir_z = float(G.dir_z);
+    const float uz = float(G.uz), dir_z = float(G.dir_z), air_limit = float(G.air_limit);
+    const float eps = float(kEps64);
+    const float thr = float(P.threshold), low = float(P.low);
+    auto outside = [&]() { return z.h + z.l < 0.f || alt_sub(z, Htop) >= 0.f; };
     int hint_r = 0, hint_a = 0;
     int32_t nsteps = 0;
     int s_mat = -1;
     Df s_cache{0.f, 0.f};
     const int32_t kMaxSteps = 2000000;
     for (int outer = 0; outer < 1000 && nsteps < kMaxSteps; ++outer) {
-      if (!(double(E.v) < P.threshold - eps)) break;
-      if (zv < 0.0 || zv >= G.H - eps) break;
+      if (!(E.v < thr)) break;
+      if (outside()) break;
       if (wt.v <= 0.f || !isfinite(wt.v)) break;
-      double limit = double(E.v) < P.low - eps ? fmin(P.low, P.threshold) : P.threshold;
+      const float limit = E.v < low ? fminf(low, thr) : thr;
       for (int inner = 0; inner < 50000 && nsteps < kMaxSteps; ++inner) {
-        if (zv < 0.0 || zv >= G.H - eps) break;
-        if (double(E.v) >= limit - eps) break;
+        if (outside()) break;
+        if (E.v >= limit) break;
         if (wt.v <= 0.f || !isfinite(wt.v)) break;
-        const bool in_air = zv >= G.thickness;
+        const bool in_air = alt_sub(z, thick) >= 0.f;
         const int mat = in_air ? 1 : 0;
         const Tab32 t = tab(mat);
         Df dens;
-        double tob_v;
-        float tob_d;
+        float ahead;
         if (!in_air) {
           dens = rho;
-          if (G.uz > eps) { tob_v = (G.thickness - zv) / G.uz; tob_d = -zd / uz; }
-          else if (G.uz < -eps) { tob_v = (0.0 - zv) / G.uz; tob_d = -zd / uz; }
-          else { tob_v = 1000.0; tob_d = 0.f; }
+          ahead = uz > eps ? alt_sub(thick, z) : -(z.h + z.l);
         } else {
-          float dv = float(1.205 * exp(-zv / 12e3));
+          float dv = 1.205f * expf(-(z.h + z.l) * (1.f / 12e3f));
           dens = Df{dv, -dv / 12e3f * zd};
-          if (G.uz > eps) { tob_v = (G.H - zv) / G.uz; tob_d = -zd / uz; }
-          else if (G.uz < -eps) { tob_v = (G.thickness - zv) / G.uz; tob_d = -zd / uz; }
-          else { tob_v = 1000.0; tob_d = 0.f; }
+          ahead = uz > eps ? alt_sub(Htop, z) : alt_sub(thick, z);
+        }
+        float tob_v, tob_d;
+        if (uz > eps || uz < -eps) {
+          tob_v = ahead / uz;
+          tob_d = -zd / uz;
+        } else {
+          tob_v = 1000.f;
+          tob_d = 0.f;
         }
         Df X, Si;
         f_lookup(t, n, P.tab, E, &X, &Si);
         if (s_mat == mat) Si = s_cache;
         Df lim = 0.01f * X / fmax2(dens, Df{1e-6f, 0.f});
-        if (in_air) lim = fmin2(lim, Df{float(G.air_limit), 0.f});
-        // step = min(tob + 1e-7, lim) clamped to [STEP_MIN, 1000]; FP64 value
-        double stepv;
-        float stepd;
-        if (tob_v + 1e-7 <= double(lim.v)) { stepv = tob_v + 1e-7; stepd = tob_d; }
-        else { stepv = double(lim.v); stepd = lim.d; }
-        if (stepv < kStepMin) { stepv = kStepMin; stepd = 0.f; }
-        else if (stepv > 1000.0) { stepv = 1000.0; stepd = 0.f; }
-        const Df step{float(stepv), stepd};
+        if (in_air) lim = fmin2(lim, Df{air_limit, 0.f});
+        // step = min(tob + 1e-7, lim) clamped to [STEP_MIN, 1000]
+        Df step = tob_v + 1e-7f <= lim.v ? Df{tob_v + 1e-7f, tob_d} : lim;
+        if (step.v < float(kStepMin)) step = Df{float(kStepMin), 0.f};
+        else if (step.v > 1000.f) step = Df{1000.f, 0.f};
         Df kf = f_inverse(t, n, X + step * dens, in_air ? &hint_a : &hint_r);
         Df gi = Df{1.f, 0.f} + E / Df{mass, 0.f}, gc = Df{1.f, 0.f} + kf / Df{mass, 0.f};
         Df ga = 0.5f * (gi + gc);
         Df ba = fsqrt(fmax2(Df{1.f, 0.f} - Df{1.f, 0.f} / (ga * ga), Df{1e-12f, 0.f}));
         Df dt = step / (ba * ga);
-        zv -= stepv * G.dir_z;
-        zd -= stepd * dir_z;
+        alt_add(z, -(step.v * dir_z));
+        zd -= step.d * dir_z;
         Df Sf = f_stopping(t, n, P.tab, kf);
         wt = wt * (Sf / Si) * fexp(Df{-1.f / ctau, 0.f} * dt);
         E = kf;
@@ -380,7 +384,7 @@ __global__ void __launch_bounds__(128) csda32_kernel(CsdaParams P, const float* 
       }
     }
     double f = 0.0, df = 0.0;
-    if (zv >= G.H - 1.0 && double(E.v) < P.threshold && G.cos_final > 0.0) {
+    if (alt_sub(z, Htop) >= -1.f && double(E.v) < P.threshold && G.cos_final > 0.0) {
       double dlogf;
       double F = gccly_flux(G.cs, G.cs129, double(E.v), q, &dlogf);
       f = double(wt.v) * F;

@@ -774,6 +774,9 @@ int check_cfg(dp_ctx* ctx, const dp_physics* ph, const dp_mc_config* cfg, Consts
   C->thr_low = low;
   C->thr_f = float(thr);
   C->thr_low_f = float(low);
+  C->mass_f = float(C->mass);
+  C->ctau_f = float(C->ctau);
+  C->elastic_ratio_f = float(C->elastic_ratio);
   C->straggling = cfg->straggling != 0;
   C->scattering = cfg->scattering != 0;
   return DP_OK;

@@ -126,7 +126,18 @@ struct Consts {
   double mass, ctau, cutoff, elastic_ratio;
   double thr_low, thr;  // mode switch and source ceiling (GeV)
   float thr_low_f, thr_f;  // the same in FP32 (exact for the FP32 transport)
+  float mass_f, ctau_f, elastic_ratio_f;
   int straggling, scattering;
+  // physics constants in the transport precision
+  template <class R> __device__ __forceinline__ R mass_r() const {
+    return sizeof(R) == 8 ? R(mass) : R(mass_f);
+  }
+  template <class R> __device__ __forceinline__ R ctau_r() const {
+    return sizeof(R) == 8 ? R(ctau) : R(ctau_f);
+  }
+  template <class R> __device__ __forceinline__ R eratio_r() const {
+    return sizeof(R) == 8 ? R(elastic_ratio) : R(elastic_ratio_f);
+  }
 };
 
 // ------------------------------------------------------------ random stream
@@ -568,9 +579,6 @@ __device__ __noinline__ DelOut reverse_del(const Med<R>& m, const Consts& C, dou
 // compensated sums (about 48 bits), so that the step loop needs no FP64
 // instruction (FP64 issues at 1/64 of the FP32 rate on this GPU).  Only the
 // altitude enters the transport; the horizontal position is not tracked.
-struct F2 {
-  float h, l;
-};
 template <class R> struct AltT;
 template <> struct AltT<double> { using type = double; };
 template <> struct AltT<float> { using type = F2; };
@@ -586,15 +594,6 @@ template <> __device__ __forceinline__ F2 alt_make<float>(double v) {
 }
 // z += dz
 __device__ __forceinline__ void alt_add(double& z, double dz) { z += dz; }
-__device__ __forceinline__ void alt_add(F2& z, float dz) {
-  float s = z.h + dz, bp = s - z.h;
-  float e = (z.h - (s - bp)) + (dz - bp);
-  float l = z.l + e, h = s + l;
-  z.l = l - (h - s);
-  z.h = h;
-}
-// a - b in the transport precision
-__device__ __forceinline__ float alt_sub(F2 a, F2 b) { return (a.h - b.h) + (a.l - b.l); }
 
 // Mutable part of a history.
 template <class R>
@@ -654,7 +653,7 @@ __device__ __noinline__ bool mixed_run(const Med<R>& m, const Consts& C, State<R
   const int nk = m.nk;
   const R* kE = m.kcol(K_E);
   const R Emax = kE[nk - 1];
-  const R mass = R(C.mass), ctau = R(C.ctau), rdens = x.c;
+  const R mass = C.mass_r<R>(), ctau = C.ctau_r<R>(), rdens = x.c;
   for (; x.event < 100000; ++x.event) {
     R k = x.r0;
     if (x.a <= x.d || k >= x.r2) {
@@ -1014,7 +1013,7 @@ __device__ __noinline__ void straggled_end(const Med<R>& m, const Consts& C, Sta
                               R ki, R kf, R ckf, R dX, double dw, int proc, int elem, bool del,
                               bool ehs, R k_ehs, R density, R step, bool shortened,
                               bool scattering, Stream& g) {
-  const R mass = R(C.mass);
+  const R mass = C.mass_r<R>();
   R astep = dX / density;
   R oz = s.uz;  // the position moves along the incoming direction
   if (scattering) {
@@ -1042,8 +1041,8 @@ __device__ __noinline__ void straggled_end(const Med<R>& m, const Consts& C, Sta
   if (sizeof(R) == 4) da = shortened ? dX / density : step;
   alt_add(s.z, -(da * oz));
   R wf = at(m, locate(m, ckf), MC_MS) / at(m, Li, MC_MS);
-  if (sizeof(R) == 4) s.w = s.w * wf * exp(-pt / R(C.ctau)) * R(dw);
-  else s.w = R(double(s.w * wf * exp(-pt / R(C.ctau))) * dw);
+  if (sizeof(R) == 4) s.w = s.w * wf * exp(-pt / C.ctau_r<R>()) * R(dw);
+  else s.w = R(double(s.w * wf * exp(-pt / C.ctau_r<R>())) * dw);
   s.E = kf;
 }
 
@@ -1054,7 +1053,7 @@ template <class R, bool COOP>
 __device__ bool straggled_step(const Med<R>& m, const Consts& C, State<R>& s, const Loc<R>& Li,
                                R density, R step, Stream& g, bool scattering, R energy_limit,
                                Cont<R>& x) {
-  const R mass = R(C.mass), eratio = R(C.elastic_ratio);
+  const R mass = C.mass_r<R>(), eratio = C.eratio_r<R>();
   R ki = s.E, dX = step * density;
   bool shortened = false;  // the step ended before its requested length
   R Xi = at(m, Li, MC_MR);
@@ -1143,14 +1142,14 @@ __device__ bool straggled_step(const Med<R>& m, const Consts& C, State<R>& s, co
 template <class R>
 __device__ __forceinline__ void csda_step(const Med<R>& m, const Consts& C, State<R>& s,
                                           const Loc<R>& Li, R density, R step) {
-  const R mass = R(C.mass);
+  const R mass = C.mass_r<R>();
   R ki = s.E, dX = step * density;
   R kf = inv_range(m, MC_CR, at(m, Li, MC_CR) + dX);
   R gm = (R(1) + ki / mass + R(1) + kf / mass) / R(2);
   R b = sqrt(fmax(R(1) - R(1) / (gm * gm), R(1e-12)));
   R dt = step / (b * gm);
   alt_add(s.z, -(step * s.uz));
-  s.w = s.w * (at(m, locate(m, kf), MC_CS) / at(m, Li, MC_CS)) * exp(-dt / R(C.ctau));
+  s.w = s.w * (at(m, locate(m, kf), MC_CS) / at(m, Li, MC_CS)) * exp(-dt / C.ctau_r<R>());
   s.E = kf;
 }
 
