@@ -194,7 +194,7 @@ def c2_los(dp, n):
                        energy_max=1e4)
 
 
-def setup_c2(dp, torch, dev, precision="mixed"):
+def setup_c2(dp, torch, dev, precision="mixed", scale=1.0):
     """Straggled backward MC with DEL/EHS events and Coulomb scattering below
     100 GeV, mixed above, through rock (runtime mixture rock/water/air
     0.70/0.25/0.05) under 1 km of air; per history thickness U[20,500] m,
@@ -203,7 +203,7 @@ def setup_c2(dp, torch, dev, precision="mixed"):
     phys = dp.create_physics(materials=(dp.STANDARD_ROCK, dp.AIR, dp.WATER))
     mix = dp.MaterialMixture(phys, *C2_MIX)
     air = dp.MaterialMixture(phys, 2)
-    n = 1_000_000
+    n = max(1, int(1_000_000 * scale))
     los = c2_los(dp, n)
     lib = dp.load()
     ctx = phys.ctx.h
@@ -246,7 +246,7 @@ def c4_los(dp, seed=4, n_los=16384):
                        energy_max=1e4), int(ns.sum()), (depth, rho, ns)
 
 
-def setup_c4(dp, torch, dev, precision="mixed"):
+def setup_c4(dp, torch, dev, precision="mixed", scale=1.0):
     """Batched backward MC over 16384 vertical lines of sight (depth
     log-uniform 50-2000 m, density U[2400,2800], 64-1024 histories each,
     StandardRock under air to 30 km), mixed transport everywhere (threshold at
@@ -255,7 +255,7 @@ def setup_c4(dp, torch, dev, precision="mixed"):
     phys = dp.create_physics(materials=(dp.STANDARD_ROCK, dp.AIR))
     rock = dp.MaterialMixture(phys, 1)
     air = dp.MaterialMixture(phys, 2)
-    los, total, _ = c4_los(dp)
+    los, total, _ = c4_los(dp, n_los=max(16, int(16384 * scale)))
     lib = dp.load()
     ctx = phys.ctx.h
     cfgs = {p: dp._mc_config(2027, True, False, 1.0, None, p) for p in ("mixed", "fp64")}
@@ -303,6 +303,62 @@ def setup_c4(dp, torch, dev, precision="mixed"):
     return run_dev, step_e2e, plain_dev, info, phys
 
 
+def setup_c5(dp, torch, dev, precision="mixed", scale=1.0):
+    """Gauss-Newton inversion loop on a 128x128x64 grid (truth: the c3
+    generator), 8 detectors x 8192 rays, synthetic Poisson counts at an
+    exposure of ~10^3 counts per ray (tau = 10^3 / median flux), weights
+    W = tau^2 / max(counts, 1) (inverse variance of the observed flux),
+    smoothness prior 1e-5 sum_edges (rho_i - rho_j)^2; start rho = 2650.
+    One step = 50 Gauss-Newton iterations (10 CG iterations per linear
+    solve) from the same start; SART (50 iterations, smoothing sweeps) is run
+    once after the timed region for the record."""
+    from dpgpu.workloads import tomography_config
+    grid, truth, rays, nodes = tomography_config(nx=128, ny=128, nz=64, n_detectors=8,
+                                                 rays_per_detector=max(64, int(8192 * scale)))
+    phys = dp.create_physics()
+    paths = dp.TomoPaths(phys, grid, rays, nodes, side_density=2500.0)
+    T = lambda a: torch.tensor(np.ascontiguousarray(a, np.float64).ravel(), device=dev)
+    f_true, _, _ = paths.eval(T(truth), precision="fp64")
+    f_true = f_true.cpu().numpy()
+    tau = 1e3 / np.median(f_true)
+    counts = np.random.default_rng(5).poisson(tau * f_true)
+    obs, W = T(counts / tau), T(tau * tau / np.maximum(counts, 1))
+    rho0 = T(np.full(grid.ncell, 2650.0))
+    n_iter = 50
+    state = {}
+
+    def step():
+        rho, hist = paths.solve(obs, rho0, method="gn", n_iter=n_iter, weight=W, cg_iter=10,
+                                precision=precision, prior_weight=1e-5)
+        state["rho"], state["hist"] = rho, hist
+
+    def finish():
+        rmse = lambda x: float(np.sqrt(np.mean((x - truth.ravel()) ** 2)))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rho_s, hist_s = paths.solve(obs, rho0, method="sart", n_iter=n_iter, precision=precision,
+                                    prior_weight=1.0)
+        torch.cuda.synchronize()
+        sart_ms = (time.perf_counter() - t0) * 1e3 / n_iter
+        return {"rmse_start": rmse(np.full(grid.ncell, 2650.0)),
+                "gn": {"rmse": rmse(state["rho"].cpu().numpy()),
+                       "misfit": [float(state["hist"][0]), float(state["hist"][-1])]},
+                "sart": {"rmse": rmse(rho_s.cpu().numpy()), "ms_per_iteration": sart_ms,
+                         "misfit": [float(hist_s[0]), float(hist_s[-1])]}}
+
+    def e2e():
+        step()
+        state["rho_host"] = state["rho"].cpu().numpy()
+
+    info = {"units": n_iter, "unit": "iterations/s", "kernel": "tomo_adjoint+tomo_forward+tomo_transpose",
+            "alg_bytes": 0, "traffic": None,
+            "config": {"workload": "c5: Gauss-Newton inversion, 128x128x64 @ 10 m, 8 x 8192 rays, "
+                                   "Poisson counts ~1e3/ray, 50 iterations x 10 CG, start 2650",
+                       "rays": len(rays), "segments": paths.nnz, "precision": precision},
+            "h2d": 0, "d2h": 8 * grid.ncell, "finish": finish}
+    return step, e2e, None, info, phys
+
+
 def setup_c1(dp, torch, dev):
     phys = dp.create_physics()
     n = 10000
@@ -333,8 +389,18 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
     import dpgpu as dp
     dp._default = dp.Context(local)
-    setup = {"c2": setup_c2, "c3": setup_c3, "c4": setup_c4, "c1": setup_c1}[args.workload]
-    step_dev, step_e2e, plain_dev, info, phys = setup(dp, torch, dev)
+    setup = {"c2": setup_c2, "c3": setup_c3, "c4": setup_c4, "c5": setup_c5,
+             "c1": setup_c1}[args.workload]
+    kw = {"scale": args.scale} if args.workload in ("c2", "c4", "c5") else {}
+    step_dev, step_e2e, plain_dev, info, phys = setup(dp, torch, dev, **kw)
+    if args.scale != 1.0:
+        info["config"]["scale"] = args.scale
+    if args.profile_run:
+        # capture mode for the profiler: warm-up steps and one step, nothing else
+        for _ in range(args.warmup + 1):
+            step_dev()
+        torch.cuda.synchronize()
+        return
     lib = dp.load()
     ctx = phys.ctx.h
     stream = torch.cuda.ExternalStream(lib.dp_get_stream(ctx), device=dev)
@@ -432,8 +498,10 @@ def run_gpu(args):
             "plain_gpu": plain,
             "speedup_vs_plain": (value / plain["value"]) if plain else None,
             "clocks": clk.summary(), "wall_s": t_wall}
+    if "finish" in info:
+        line["result"] = info["finish"]()
     if rank == 0:
-        if not args.no_cpu:
+        if not args.no_cpu and args.workload != "c5":
             line["cpu_baseline"] = cpu_baseline(args.workload, budget_s=args.cpu_seconds)
         print(json.dumps(line))
 
@@ -514,7 +582,8 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    units = {"c2": "samples/s", "c3": "rays/s", "c4": "samples/s", "c1": "samples/s"}[args.workload]
+    units = {"c2": "samples/s", "c3": "rays/s", "c4": "samples/s", "c5": "iterations/s",
+             "c1": "samples/s"}[args.workload]
     vals = []
     for _ in range(args.warmup):
         cpu_baseline(args.workload, budget_s=args.cpu_seconds / 4)
@@ -539,11 +608,15 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c1"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "c1"])
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain one-launch-per-ray form")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="c2/c4: fraction of the histories / lines of sight (profiling captures)")
+    ap.add_argument("--profile-run", action="store_true",
+                    help="only warm-up steps and one step (for ncu captures); prints nothing")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -70,6 +70,12 @@ int mc_backward_stochastic(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params
 int csda_los(dp_ctx* ctx, const dp_physics* ph, int rock, int air, double threshold, double low,
              uint64_t seed, const dp_los* los, const int64_t* off, long n_los, long n,
              double* contrib, double* dcontrib, int precision);
+// Tomography internals used by the inversion loops (tomo.cu): evaluation into
+// a caller-owned Jacobian buffer and J^T v on the resident paths' buckets.
+int tomo_eval_raw(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, const dp_tomo_params* tp,
+                  const double* rho, double* flux, void* jraw, int precision);
+int tomo_transpose(dp_ctx* ctx, const dp_paths* pa, const void* jbuf, int precision,
+                   const double* cot, double* grad);
 // Bump allocator over one scratch slot (256-byte aligned pieces).
 struct Arena {
   char* base = nullptr;

@@ -1,0 +1,551 @@
+// inverse.cu -- inversion loops on the device over resident ray paths, the
+// consumers of the tomography forward model and its Jacobian
+// (src/Tomography_inverse.jl):
+//
+//   SART  (:98-132)  rho <- clamp(rho + lambda D_col J^T D_row (obs - f(rho)), box)
+//                    with D_row = 1/sum_j|J_ij|, D_col = 1/sum_i|J_ij|; the
+//                    Jacobian is re-evaluated at every iterate (the reference
+//                    solves a fixed linear system A w = b).
+//   Gauss-Newton (:448-603, legacy acceptance) on 0.5 sum_i W_i (f_i - obs_i)^2:
+//                    the Levenberg-Marquardt system (J^T W J + mu diag) d = -g
+//                    is solved matrix-free by Jacobi-preconditioned conjugate
+//                    gradients (J v and J^T u on the CSR/CSC layouts) instead
+//                    of a dense normal matrix, then a backtracking line search
+//                    with the reference's acceptance f_new < f - 1e-10 |f|.
+//
+// The unknown is the voxel density (the reference's water fraction w maps
+// onto it linearly).  All reductions run in a fixed order (deterministic).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "internal.h"
+
+namespace dp {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kRedBlocks = 304;  // 2 x 152 SMs for the reduction partials
+
+// y_i = sum_j J_ij x_j over the row's cells (side-exit entries excluded);
+// one warp per row.
+template <class V>
+__global__ void spmv_kernel(const int64_t* row_ptr, const int32_t* cell, const V* val,
+                            const double* x, long n_rows, const double* wt, double* y) {
+  long r = (blockIdx.x * long(blockDim.x) + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (r >= n_rows) return;
+  double s = 0.0;
+  for (int64_t p = row_ptr[r] + lane, e = row_ptr[r + 1]; p < e; p += 32) {
+    int c = cell[p];
+    if (c >= 0) s += double(val[p]) * x[c];
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) y[r] = wt ? wt[r] * s : s;
+}
+
+// Row sums of |J| (SART's D_row; zero rows count as 1).
+template <class V>
+__global__ void rowabs_kernel(const int64_t* row_ptr, const int32_t* cell, const V* val,
+                              long n_rows, double* out) {
+  long r = (blockIdx.x * long(blockDim.x) + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (r >= n_rows) return;
+  double s = 0.0;
+  for (int64_t p = row_ptr[r] + lane, e = row_ptr[r + 1]; p < e; p += 32)
+    if (cell[p] >= 0) s += fabs(double(val[p]));
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) out[r] = s > 0.0 ? s : 1.0;
+}
+
+// Column sums over the CSC buckets: mode 0 sum_i |J_ij| (SART's D_col, zero
+// columns count as 1); mode 1 sum_i W_i J_ij^2 (the Gauss-Newton diagonal).
+// A ray can cross a cell in several segments: J_ij is the sum of its
+// segments' entries, which sit next to each other in the bucket (ordered by
+// entry index), so runs of one row are merged before squaring.
+template <class V>
+__global__ void colsum_kernel(const int64_t* cptr, const int32_t* perm, const V* val,
+                              const int32_t* prow, const double* wt, long ncell, int mode,
+                              double* out) {
+  long c = blockIdx.x * long(blockDim.x) + threadIdx.x;
+  if (c >= ncell) return;
+  double s = 0.0, run = 0.0;
+  int row = -1;
+  for (int64_t p = cptr[c], e = cptr[c + 1]; p < e; ++p) {
+    const int r = prow[p];
+    if (r != row) {
+      if (row >= 0) s += mode == 0 ? fabs(run) : (wt ? wt[row] : 1.0) * run * run;
+      row = r;
+      run = 0.0;
+    }
+    run += double(val[perm[p]]);
+  }
+  if (row >= 0) s += mode == 0 ? fabs(run) : (wt ? wt[row] : 1.0) * run * run;
+  out[c] = mode == 0 ? (s > 0.0 ? s : 1.0) : s;
+}
+
+// Fixed-order dot product: block partials, then one block.
+__global__ void __launch_bounds__(kThreads) dot_part_kernel(const double* a, const double* b,
+                                                            const double* w, long n, double* part) {
+  __shared__ double sh[kThreads];
+  double s = 0.0;
+  for (long i = blockIdx.x * long(kThreads) + threadIdx.x; i < n; i += long(gridDim.x) * kThreads) {
+    double v = a[i] * (b ? b[i] : a[i]);
+    s += w ? w[i] * v : v;
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int h = kThreads / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) sh[threadIdx.x] += sh[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+__global__ void __launch_bounds__(kThreads) dot_final_kernel(const double* part, int nb,
+                                                             double* out) {
+  __shared__ double sh[kThreads];
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nb; b += kThreads) s += part[b];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int h = kThreads / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) sh[threadIdx.x] += sh[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
+// r_i = s (f_i - obs_i); with wr: wr_i = W_i r_i as well.
+__global__ void residual_kernel(const double* f, const double* obs, const double* wt, long n,
+                                double sgn, double* r, double* wr) {
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
+       i += long(gridDim.x) * blockDim.x) {
+    double v = sgn * (f[i] - obs[i]);
+    r[i] = v;
+    if (wr) wr[i] = (wt ? wt[i] : 1.0) * v;
+  }
+}
+// u_i = a_i / b_i
+__global__ void divide_kernel(const double* a, const double* b, long n, double* u) {
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
+       i += long(gridDim.x) * blockDim.x)
+    u[i] = a[i] / b[i];
+}
+// SART update: rho = clamp(rho + lambda g / colsum, box)
+__global__ void sart_update_kernel(double* rho, const double* g, const double* colsum, long n,
+                                   double lambda, double lo, double hi) {
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
+       i += long(gridDim.x) * blockDim.x)
+    rho[i] = fmin(fmax(rho[i] + lambda * g[i] / colsum[i], lo), hi);
+}
+
+// Conjugate-gradient pieces with device-resident scalars (no host round trip
+// inside the CG loop).  s[0] = r.z, s[1] = p.Ap, s[2] = new r.z.
+__global__ void cg_init_kernel(const double* g, const double* prec, long n, double* x, double* r,
+                               double* z, double* p) {
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
+       i += long(gridDim.x) * blockDim.x) {
+    double ri = -g[i];
+    double zi = ri / prec[i];
+    x[i] = 0.0;
+    r[i] = ri;
+    z[i] = zi;
+    p[i] = zi;
+  }
+}
+// Ap += mu * diag * p (the Levenberg-Marquardt term)
+__global__ void lm_add_kernel(const double* p, const double* damp, long n, double* Ap) {
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
+       i += long(gridDim.x) * blockDim.x)
+    Ap[i] += damp[i] * p[i];
+}
+// x += a p, r -= a Ap, z = r / prec with a = s[0] / s[1]
+__global__ void cg_step_kernel(const double* s, const double* p, const double* Ap,
+                               const double* prec, long n, double* x, double* r, double* z) {
+  const double a = s[1] != 0.0 ? s[0] / s[1] : 0.0;
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
+       i += long(gridDim.x) * blockDim.x) {
+    x[i] += a * p[i];
+    double ri = r[i] - a * Ap[i];
+    r[i] = ri;
+    z[i] = ri / prec[i];
+  }
+}
+// p = z + b p with b = s[2] / s[0]; then s[0] = s[2]
+__global__ void cg_dir_kernel(double* s, const double* z, long n, double* p) {
+  const double b = s[0] != 0.0 ? s[2] / s[0] : 0.0;
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
+       i += long(gridDim.x) * blockDim.x)
+    p[i] = z[i] + b * p[i];
+}
+__global__ void cg_shift_kernel(double* s) { s[0] = s[2]; }
+// trial = clamp(rho + alpha d, box)
+__global__ void trial_kernel(const double* rho, const double* d, long n, double alpha, double lo,
+                             double hi, double* out) {
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
+       i += long(gridDim.x) * blockDim.x)
+    out[i] = fmin(fmax(rho[i] + alpha * d[i], lo), hi);
+}
+// prec = max(diag, floor) (Jacobi preconditioner) and damp = mu max(diag, floor)
+__global__ void lm_diag_kernel(const double* diag, long n, double floor_, double mu, double* prec,
+                               double* damp) {
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
+       i += long(gridDim.x) * blockDim.x) {
+    double d = fmax(diag[i], floor_);
+    damp[i] = mu * d;
+    prec[i] = (1.0 + mu) * d;
+  }
+}
+__global__ void max_part_kernel(const double* a, long n, double* part) {
+  __shared__ double sh[kThreads];
+  double s = 0.0;
+  for (long i = blockIdx.x * long(kThreads) + threadIdx.x; i < n; i += long(gridDim.x) * kThreads)
+    s = fmax(s, a[i]);
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int h = kThreads / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + h]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// Smoothness prior on the voxel grid's 6-neighbour graph (SmoothnessPrior,
+// src/Tomography_inverse.jl:17-79, 262-268): R = weight sum_edges (x_i - x_j)^2.
+struct Dims {
+  int nx, ny, nz;
+};
+__device__ __forceinline__ int degree(Dims d, long c, int* nb) {
+  const long sxy = long(d.nx) * d.ny;
+  const int i = int(c % d.nx), j = int((c / d.nx) % d.ny), k = int(c / sxy);
+  int n = 0;
+  if (i > 0) nb[n++] = int(c - 1);
+  if (i < d.nx - 1) nb[n++] = int(c + 1);
+  if (j > 0) nb[n++] = int(c - d.nx);
+  if (j < d.ny - 1) nb[n++] = int(c + d.nx);
+  if (k > 0) nb[n++] = int(c - sxy);
+  if (k < d.nz - 1) nb[n++] = int(c + sxy);
+  return n;
+}
+// out = (accumulate ? out : 0) + coef * sum_{j in N(c)} (x_c - x_j)
+__global__ void lap_kernel(const double* x, Dims d, double coef, int accumulate, double* out) {
+  const long n = long(d.nx) * d.ny * d.nz;
+  for (long c = blockIdx.x * long(blockDim.x) + threadIdx.x; c < n;
+       c += long(gridDim.x) * blockDim.x) {
+    int nb[6];
+    const int m = degree(d, c, nb);
+    double s = 0.0;
+    for (int t = 0; t < m; ++t) s += x[c] - x[nb[t]];
+    out[c] = (accumulate ? out[c] : 0.0) + coef * s;
+  }
+}
+// block partials of sum over the forward edges of (x_i - x_j)^2
+__global__ void __launch_bounds__(kThreads) prior_part_kernel(const double* x, Dims d,
+                                                              double* part) {
+  __shared__ double sh[kThreads];
+  const long n = long(d.nx) * d.ny * d.nz, sxy = long(d.nx) * d.ny;
+  double s = 0.0;
+  for (long c = blockIdx.x * long(kThreads) + threadIdx.x; c < n;
+       c += long(gridDim.x) * kThreads) {
+    const int i = int(c % d.nx), j = int((c / d.nx) % d.ny), k = int(c / sxy);
+    if (i < d.nx - 1) s += (x[c] - x[c + 1]) * (x[c] - x[c + 1]);
+    if (j < d.ny - 1) s += (x[c] - x[c + d.nx]) * (x[c] - x[c + d.nx]);
+    if (k < d.nz - 1) s += (x[c] - x[c + sxy]) * (x[c] - x[c + sxy]);
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int h = kThreads / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) sh[threadIdx.x] += sh[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+// diag += coef * degree (the prior Hessian's diagonal)
+__global__ void add_degree_kernel(Dims d, double coef, double* diag) {
+  const long n = long(d.nx) * d.ny * d.nz;
+  for (long c = blockIdx.x * long(blockDim.x) + threadIdx.x; c < n;
+       c += long(gridDim.x) * blockDim.x) {
+    int nb[6];
+    diag[c] += coef * degree(d, c, nb);
+  }
+}
+// one smoothing sweep (apply_laplacian_smoothing, :64-79), then the box
+__global__ void smooth_kernel(const double* x, Dims d, double strength, double lo, double hi,
+                              double* out) {
+  const long n = long(d.nx) * d.ny * d.nz;
+  for (long c = blockIdx.x * long(blockDim.x) + threadIdx.x; c < n;
+       c += long(gridDim.x) * blockDim.x) {
+    int nb[6];
+    const int m = degree(d, c, nb);
+    double mean = 0.0;
+    for (int t = 0; t < m; ++t) mean += x[nb[t]];
+    double v = m ? (1.0 - strength) * x[c] + strength * (mean / m) : x[c];
+    out[c] = fmin(fmax(v, lo), hi);
+  }
+}
+
+struct Solver {
+  dp_ctx* ctx;
+  const dp_physics* ph;
+  const dp_paths* pa;
+  const dp_tomo_params* tp;
+  int precision;
+  long n_rays, ncell;
+  void* jv;      // Jacobian values (FP32 or FP64)
+  double* part;  // reduction partials
+  double* s;     // device scalars
+  int grid(long n) const { return int(std::min<long>((n + kThreads - 1) / kThreads, 152L * 8)); }
+
+  int dot(const double* a, const double* b, const double* w, long n, double* out) {
+    dot_part_kernel<<<kRedBlocks, kThreads, 0, ctx->stream>>>(a, b, w, n, part);
+    dot_final_kernel<<<1, kThreads, 0, ctx->stream>>>(part, kRedBlocks, out);
+    ctx->launches += 2;
+    DP_CHECK_CUDA(ctx, cudaGetLastError());
+    return DP_OK;
+  }
+  double host_scalar(const double* d) {
+    double h = 0.0;
+    cudaMemcpyAsync(&h, d, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    return h;
+  }
+  int spmv(const double* x, const double* wt, double* y) {
+    int blocks = int((n_rays * 32 + kThreads - 1) / kThreads);
+    if (precision)
+      spmv_kernel<float><<<blocks, kThreads, 0, ctx->stream>>>(pa->row_ptr, pa->cell,
+                                                               static_cast<const float*>(jv), x,
+                                                               n_rays, wt, y);
+    else
+      spmv_kernel<double><<<blocks, kThreads, 0, ctx->stream>>>(pa->row_ptr, pa->cell,
+                                                                static_cast<const double*>(jv), x,
+                                                                n_rays, wt, y);
+    ++ctx->launches;
+    DP_CHECK_CUDA(ctx, cudaGetLastError());
+    return DP_OK;
+  }
+  int transpose(const double* u, double* out) { return tomo_transpose(ctx, pa, jv, precision, u, out); }
+  int colsum(const double* wt, int mode, double* out) {
+    int blocks = int((ncell + kThreads - 1) / kThreads);
+    if (precision)
+      colsum_kernel<float><<<blocks, kThreads, 0, ctx->stream>>>(
+          pa->cptr, pa->perm, static_cast<const float*>(jv), pa->prow, wt, ncell, mode, out);
+    else
+      colsum_kernel<double><<<blocks, kThreads, 0, ctx->stream>>>(
+          pa->cptr, pa->perm, static_cast<const double*>(jv), pa->prow, wt, ncell, mode, out);
+    ++ctx->launches;
+    DP_CHECK_CUDA(ctx, cudaGetLastError());
+    return DP_OK;
+  }
+  int rowabs(double* out) {
+    int blocks = int((n_rays * 32 + kThreads - 1) / kThreads);
+    if (precision)
+      rowabs_kernel<float><<<blocks, kThreads, 0, ctx->stream>>>(
+          pa->row_ptr, pa->cell, static_cast<const float*>(jv), n_rays, out);
+    else
+      rowabs_kernel<double><<<blocks, kThreads, 0, ctx->stream>>>(
+          pa->row_ptr, pa->cell, static_cast<const double*>(jv), n_rays, out);
+    ++ctx->launches;
+    DP_CHECK_CUDA(ctx, cudaGetLastError());
+    return DP_OK;
+  }
+  // forward (and Jacobian when jac) at rho
+  int eval(const double* rho, double* flux, bool jac) {
+    return tomo_eval_raw(ctx, ph, pa, tp, rho, flux, jac ? jv : nullptr, precision);
+  }
+  Dims dims;
+  double prior = 0.0;  // smoothness weight
+  // 0.5 sum W (f - obs)^2 + prior(rho), on the host
+  double objective(const double* f, const double* obs, const double* wt, double* r,
+                   const double* rho) {
+    residual_kernel<<<grid(n_rays), kThreads, 0, ctx->stream>>>(f, obs, wt, n_rays, 1.0, r,
+                                                               nullptr);
+    ++ctx->launches;
+    dot(r, r, wt, n_rays, s + 3);
+    if (prior > 0.0) {
+      prior_part_kernel<<<kRedBlocks, kThreads, 0, ctx->stream>>>(rho, dims, part);
+      dot_final_kernel<<<1, kThreads, 0, ctx->stream>>>(part, kRedBlocks, s + 4);
+      ctx->launches += 2;
+    }
+    double v = 0.5 * host_scalar(s + 3);
+    if (prior > 0.0) v += prior * host_scalar(s + 4);
+    return v;
+  }
+};
+
+}  // namespace
+}  // namespace dp
+
+using namespace dp;
+
+extern "C" {
+
+int dp_tomo_solve_dev(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa,
+                      const dp_tomo_params* tp, const double* obs, const double* weight,
+                      double* rho, const dp_solve_params* sp, double* history) {
+  if (!ctx || !ph || !pa || !tp || !obs || !rho || !sp)
+    return fail(ctx, DP_ERR_ARG, "null argument");
+  if (sp->n_iter < 0 || (sp->method != DP_SOLVE_SART && sp->method != DP_SOLVE_GN) ||
+      (sp->precision != DP_PREC_FP64 && sp->precision != DP_PREC_MIXED) ||
+      !(sp->box_hi > sp->box_lo))
+    return fail(ctx, DP_ERR_ARG, "invalid solver parameters");
+  DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  Solver S{};
+  S.ctx = ctx;
+  S.ph = ph;
+  S.pa = pa;
+  S.tp = tp;
+  S.precision = sp->precision;
+  S.n_rays = pa->n_rays;
+  S.ncell = long(pa->grid.nx) * pa->grid.ny * pa->grid.nz;
+  S.dims = Dims{pa->grid.nx, pa->grid.ny, pa->grid.nz};
+  S.prior = sp->prior_weight > 0.0 ? sp->prior_weight : 0.0;
+  const long nr = S.n_rays, nc = S.ncell;
+  // slot 0: Jacobian values, 5 row vectors, 10 cell vectors, partials, scalars
+  size_t need = size_t(pa->nnz + 1) * (S.precision ? 4 : 8) + size_t(nr) * 5 * 8 +
+                size_t(nc) * 10 * 8 + kRedBlocks * 8 + 64 + 16 * 256;
+  Arena A;
+  A.base = static_cast<char*>(scratch(ctx, need, 0));
+  A.cap = ctx->slot_bytes[0];
+  S.jv = A.take<char>(size_t(pa->nnz + 1) * (S.precision ? 4 : 8));
+  double *flux = A.take<double>(nr), *r = A.take<double>(nr), *u = A.take<double>(nr),
+         *rowsum = A.take<double>(nr), *tmp = A.take<double>(nr);
+  double *g = A.take<double>(nc), *col = A.take<double>(nc), *x = A.take<double>(nc),
+         *cr = A.take<double>(nc), *z = A.take<double>(nc), *p = A.take<double>(nc),
+         *Ap = A.take<double>(nc), *prec = A.take<double>(nc), *damp = A.take<double>(nc),
+         *trial = A.take<double>(nc);
+  S.part = A.take<double>(kRedBlocks);
+  S.s = A.take<double>(8);
+  if (!S.s) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
+  const int saved = ctx->blocking;
+  ctx->blocking = 0;  // kernels are enqueued; host reads only the line-search scalars
+  int rc = DP_OK;
+  if (history)
+    for (int k = 0; k <= sp->n_iter; ++k) history[k] = std::nan("");
+  auto record = [&](int k, double v) {
+    if (history) history[k] = v;
+  };
+  if (sp->method == DP_SOLVE_SART) {
+    const double lambda = sp->relaxation > 0.0 ? sp->relaxation : 0.2;
+    for (int it = 0; it < sp->n_iter && !rc; ++it) {
+      rc = S.eval(rho, flux, true);
+      if (rc) break;
+      residual_kernel<<<S.grid(nr), kThreads, 0, ctx->stream>>>(flux, obs, nullptr, nr, -1.0, r,
+                                                                 nullptr);
+      ++ctx->launches;
+      S.dot(r, r, nullptr, nr, S.s + 3);
+      record(it, std::sqrt(S.host_scalar(S.s + 3)));
+      if ((rc = S.rowabs(rowsum))) break;
+      divide_kernel<<<S.grid(nr), kThreads, 0, ctx->stream>>>(r, rowsum, nr, u);
+      ++ctx->launches;
+      if ((rc = S.transpose(u, g))) break;
+      if ((rc = S.colsum(nullptr, 0, col))) break;
+      sart_update_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(rho, g, col, nc, lambda,
+                                                                   sp->box_lo, sp->box_hi);
+      ++ctx->launches;
+      if (S.prior > 0.0) {  // smoothing sweep of the Tikhonov-style prior
+        const double strength = sp->smooth_strength > 0.0 ? sp->smooth_strength : 0.1;
+        smooth_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(rho, S.dims, strength, sp->box_lo,
+                                                                sp->box_hi, trial);
+        DP_CHECK_CUDA(ctx, cudaMemcpyAsync(rho, trial, nc * 8, cudaMemcpyDeviceToDevice,
+                                           ctx->stream));
+        ++ctx->launches;
+      }
+    }
+  } else {
+    double mu = sp->lm_damping > 0.0 ? sp->lm_damping : 1e-3;
+    const int cg_iter = sp->cg_iter > 0 ? sp->cg_iter : 10;
+    rc = S.eval(rho, flux, true);
+    double f_cur = rc ? 0.0 : S.objective(flux, obs, weight, r, rho);
+    for (int it = 0; it < sp->n_iter && !rc; ++it) {
+      {
+        S.dot(r, r, nullptr, nr, S.s + 3);
+        record(it, std::sqrt(S.host_scalar(S.s + 3)));
+      }
+      // gradient g = J^T W r and the Gauss-Newton diagonal sum_i W_i J_ij^2
+      residual_kernel<<<S.grid(nr), kThreads, 0, ctx->stream>>>(flux, obs, weight, nr, 1.0, r, u);
+      ++ctx->launches;
+      if ((rc = S.transpose(u, g))) break;
+      if ((rc = S.colsum(weight, 1, col))) break;
+      if (S.prior > 0.0) {  // prior gradient 2 w L rho and Hessian diagonal 2 w deg
+        lap_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(rho, S.dims, 2.0 * S.prior, 1, g);
+        add_degree_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(S.dims, 2.0 * S.prior, col);
+        ctx->launches += 2;
+      }
+      max_part_kernel<<<kRedBlocks, kThreads, 0, ctx->stream>>>(col, nc, S.part);
+      ++ctx->launches;
+      std::vector<double> hp(kRedBlocks);
+      DP_CHECK_CUDA(ctx, cudaMemcpyAsync(hp.data(), S.part, kRedBlocks * 8, cudaMemcpyDeviceToHost,
+                                         ctx->stream));
+      DP_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      double dmax = 0.0;
+      for (double v : hp) dmax = std::max(dmax, v);
+      if (!(dmax > 0.0)) dmax = 1.0;
+      bool accepted = false;
+      for (int attempt = 0; attempt < 6 && !accepted && !rc; ++attempt) {
+        // (J^T W J + mu D) d = -g by Jacobi-preconditioned CG from d = 0
+        lm_diag_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(col, nc, 1e-12 * dmax, mu, prec,
+                                                                damp);
+        cg_init_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(g, prec, nc, x, cr, z, p);
+        ctx->launches += 2;
+        S.dot(cr, z, nullptr, nc, S.s + 0);
+        for (int k = 0; k < cg_iter && !rc; ++k) {
+          if ((rc = S.spmv(p, weight, tmp))) break;  // W J p
+          if ((rc = S.transpose(tmp, Ap))) break;    // J^T W J p
+          lm_add_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(p, damp, nc, Ap);
+          ++ctx->launches;
+          if (S.prior > 0.0) {  // + 2 w L p
+            lap_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(p, S.dims, 2.0 * S.prior, 1, Ap);
+            ++ctx->launches;
+          }
+          S.dot(p, Ap, nullptr, nc, S.s + 1);
+          cg_step_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(S.s, p, Ap, prec, nc, x, cr, z);
+          ++ctx->launches;
+          S.dot(cr, z, nullptr, nc, S.s + 2);
+          cg_dir_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(S.s, z, nc, p);
+          cg_shift_kernel<<<1, 1, 0, ctx->stream>>>(S.s);
+          ctx->launches += 2;
+        }
+        if (rc) break;
+        // backtracking line search, legacy acceptance (src/Tomography_inverse.jl:443-448)
+        double alpha = 1.0;
+        for (int ls = 0; ls < 14 && !rc; ++ls) {
+          trial_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(rho, x, nc, alpha, sp->box_lo,
+                                                                 sp->box_hi, trial);
+          ++ctx->launches;
+          if ((rc = S.eval(trial, tmp, false))) break;
+          double f_new = S.objective(tmp, obs, weight, u, trial);
+          if (std::isfinite(f_new) && f_new < f_cur - 1e-10 * std::fabs(f_cur)) {
+            DP_CHECK_CUDA(ctx, cudaMemcpyAsync(rho, trial, nc * 8, cudaMemcpyDeviceToDevice,
+                                               ctx->stream));
+            f_cur = f_new;
+            accepted = true;
+            break;
+          }
+          alpha *= 0.5;
+        }
+        if (accepted) mu = std::max(mu / 3.0, 1e-12);
+        else mu = std::min(mu * 3.0, 1e12);
+      }
+      if (rc || !accepted) break;
+      rc = S.eval(rho, flux, true);
+      if (!rc) f_cur = S.objective(flux, obs, weight, r, rho);
+    }
+  }
+  if (!rc) {
+    // final misfit ||obs - f(rho)||
+    rc = S.eval(rho, flux, false);
+    if (!rc) {
+      residual_kernel<<<S.grid(nr), kThreads, 0, ctx->stream>>>(flux, obs, nullptr, nr, -1.0, r,
+                                                                nullptr);
+      ++ctx->launches;
+      S.dot(r, r, nullptr, nr, S.s + 3);
+      record(sp->n_iter, std::sqrt(S.host_scalar(S.s + 3)));
+    }
+  }
+  ctx->blocking = saved;
+  if (rc) return rc;
+  DP_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return dp_sync(ctx);
+}
+
+}  // extern "C"

@@ -1007,9 +1007,16 @@ static int make_eval(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, cons
 }
 
 // Core evaluation on device pointers.  precision: 0 = FP64, 1 = mixed.
+__global__ void widen_kernel(const float* in, int64_t n, double* out) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x)
+    out[i] = double(in[i]);
+}
+
 static int eval_core(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, const dp_tomo_params* tp,
                      const double* rho, const double* nE, const double* nq, const double* nw,
-                     const double* cot, double* flux, double* grad, double* jac, int precision) {
+                     const double* cot, double* flux, double* grad, double* jac, int precision,
+                     void* jraw = nullptr) {
   EvalP P;
   int rc = make_eval(ctx, ph, pa, tp, P);
   if (rc) return rc;
@@ -1019,7 +1026,7 @@ static int eval_core(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, cons
   P.nq = nq;
   P.nw = nw;
   P.flux = flux;
-  const bool adj = (cot && grad) || jac;
+  const bool adj = (cot && grad) || jac || jraw;
   long ncell = long(pa->grid.nx) * pa->grid.ny * pa->grid.nz;
   // slot 1: node starts, then the Jacobian values
   size_t need = size_t(P.n_nodes) * sizeof(NodeInit) + size_t(pa->nnz + 1) * 8 + 1024;
@@ -1029,7 +1036,9 @@ static int eval_core(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, cons
   if (!A.base) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
   void* jbuf = nullptr;
   if (adj) {
-    jbuf = jac && !precision ? (void*)jac : A.take<char>(size_t(pa->nnz + 1) * (precision ? 4 : 8));
+    jbuf = jraw ? jraw
+                : jac && !precision ? (void*)jac
+                                    : A.take<char>(size_t(pa->nnz + 1) * (precision ? 4 : 8));
     if (!jbuf) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
   }
   long blocks = std::min<long>((pa->n_rays + kWarps - 1) / kWarps, 152L * 16);
@@ -1060,6 +1069,23 @@ static int eval_core(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, cons
   DP_CHECK_CUDA(ctx, cudaGetLastError());
   timed_end(ctx, adj ? "tomo_adjoint" : "tomo_forward");
   if (adj && cot && grad) {
+    int rc2 = tomo_transpose(ctx, pa, jbuf, precision, cot, grad);
+    if (rc2) return rc2;
+  }
+  if (jac && precision) {
+    widen_kernel<<<int(std::min<long>((pa->nnz + 255) / 256, 152L * 64)), 256, 0, ctx->stream>>>(
+        static_cast<const float*>(jbuf), pa->nnz, jac);
+    ++ctx->launches;
+    DP_CHECK_CUDA(ctx, cudaGetLastError());
+  }
+  return ctx->blocking ? check(ctx) : DP_OK;
+}
+
+// J^T v over the CSC buckets (deterministic segmented sums, no float atomics).
+int tomo_transpose(dp_ctx* ctx, const dp_paths* pa, const void* jbuf, int precision,
+                   const double* cot, double* grad) {
+  long ncell = long(pa->grid.nx) * pa->grid.ny * pa->grid.nz;
+  {
     timed_begin(ctx);
     const int nbw = int((long(pa->n_big) * 32 + 255) / 256);
     if (precision == 0) {
@@ -1081,16 +1107,15 @@ static int eval_core(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, cons
     DP_CHECK_CUDA(ctx, cudaGetLastError());
     timed_end(ctx, "tomo_transpose");
   }
-  if (jac && precision) {
-    // widen the single-precision Jacobian into the caller's buffer
-    std::vector<float> h(pa->nnz);
-    std::vector<double> d(pa->nnz);
-    DP_CHECK_CUDA(ctx, cudaMemcpyAsync(h.data(), jbuf, 4 * pa->nnz, cudaMemcpyDeviceToHost, ctx->stream));
-    DP_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    for (int64_t k = 0; k < pa->nnz; ++k) d[k] = h[k];
-    DP_CHECK_CUDA(ctx, cudaMemcpyAsync(jac, d.data(), 8 * pa->nnz, cudaMemcpyHostToDevice, ctx->stream));
-  }
-  return check(ctx);
+  return DP_OK;
+}
+
+// Flux, and the Jacobian values of the resident paths into jraw (FP32 for the
+// mixed-precision kernel, FP64 otherwise); node arrays of tp on the device.
+int tomo_eval_raw(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, const dp_tomo_params* tp,
+                  const double* rho, double* flux, void* jraw, int precision) {
+  return eval_core(ctx, ph, pa, tp, rho, tp->node_energy, tp->node_charge, tp->node_weight,
+                   nullptr, flux, nullptr, nullptr, precision, jraw);
 }
 
 }  // namespace dp

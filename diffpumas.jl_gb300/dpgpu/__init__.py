@@ -572,3 +572,26 @@ class TomoPaths:
                                       C.byref(self.params), p(rho), p(cot), p(flux), p(grad),
                                       p(jac), PRECISION[precision]), self.physics.ctx.h)
         return flux, grad, jac
+
+    def solve(self, obs, rho0, *, method="gn", n_iter=12, weight=None, cg_iter=10,
+              relaxation=0.2, lm_damping=1e-3, box=(500.0, 3500.0), precision="mixed",
+              prior_weight=0.0, smooth_strength=0.1):
+        """Inversion loop on the device (src/Tomography_inverse.jl): "sart"
+        (sart_reconstruct, Jacobian re-evaluated per iterate) or "gn"
+        (gauss_newton_reconstruct with matrix-free CG).  obs, weight and rho0
+        are float64 CUDA tensors; returns (rho, misfit history)."""
+        import torch
+        from ._lib import DpSolveParams
+        rho = rho0.clone()
+        sp = DpSolveParams({"sart": 0, "gn": 1}[method], int(n_iter), int(cg_iter),
+                           PRECISION[precision], float(relaxation), float(lm_damping),
+                           float(box[0]), float(box[1]), float(prior_weight),
+                           float(smooth_strength))
+        hist = np.zeros(n_iter + 1)
+        torch.cuda.synchronize(self.dev)
+        check(load().dp_tomo_solve_dev(self.physics.ctx.h, self.physics.h, self.h,
+                                       C.byref(self.params), obs.data_ptr(),
+                                       weight.data_ptr() if weight is not None else None,
+                                       rho.data_ptr(), C.byref(sp), _ptr(hist)),
+              self.physics.ctx.h)
+        return rho, hist

@@ -67,6 +67,13 @@ class DpLosResult(C.Structure):
                 ("n_status_nonzero", C.c_long)]
 
 
+class DpSolveParams(C.Structure):
+    _fields_ = [("method", C.c_int), ("n_iter", C.c_int), ("cg_iter", C.c_int),
+                ("precision", C.c_int), ("relaxation", C.c_double), ("lm_damping", C.c_double),
+                ("box_lo", C.c_double), ("box_hi", C.c_double), ("prior_weight", C.c_double),
+                ("smooth_strength", C.c_double)]
+
+
 class DpGrid(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("x0", C.c_double),
                 ("y0", C.c_double), ("z0", C.c_double), ("dx", C.c_double),
@@ -139,6 +146,8 @@ PROTOTYPES = {
     "dp_tomo_eval_dev": (_I, [_P, _P, _P, C.POINTER(DpTomoParams), _VP, _VP, _VP, _VP, _VP, _I]),
     "dp_tomo_eval": (_I, [_P, _P, _P, C.POINTER(DpTomoParams), _VP, _VP, _VP, _VP, _VP]),
     "dp_tomo_eval_noalloc_dev": (_I, [_P, _P, _P, C.POINTER(DpTomoParams), _VP, _VP, _VP, _VP]),
+    "dp_tomo_solve_dev": (_I, [_P, _P, _P, C.POINTER(DpTomoParams), _VP, _VP, _VP,
+                               C.POINTER(DpSolveParams), _VP]),
     "dp_tomo_forward_plain_dev": (_I, [_P, _P, C.POINTER(DpGrid), C.POINTER(DpTomoParams), _VP,
                                        _L, _VP, _VP]),
 }

@@ -412,6 +412,43 @@ int dp_tomo_forward_plain_dev(dp_ctx* ctx, const dp_physics* phys, const dp_grid
                               const dp_tomo_params* tp, const double* rho, long n_rays,
                               const dp_ray* rays, double* flux);
 
+/* ------------------------------------------------------------------ inversion loops
+ * Consumers of the forward model and its Jacobian (src/Tomography_inverse.jl)
+ * on resident paths, the unknown being the voxel density:
+ *   DP_SOLVE_SART  rho <- clamp(rho + relaxation D_col J^T D_row (obs - f(rho)), box),
+ *                  D_row = 1/sum_j|J_ij|, D_col = 1/sum_i|J_ij| (sart_reconstruct,
+ *                  :98-132), with J re-evaluated at every iterate;
+ *   DP_SOLVE_GN    Gauss-Newton / Levenberg-Marquardt on 0.5 sum_i W_i (f_i - obs_i)^2
+ *                  (gauss_newton_reconstruct, :448-603, legacy acceptance), the
+ *                  damped normal equations solved matrix-free by preconditioned
+ *                  conjugate gradients on the device (no dense J^T W J).
+ * No reference entry point takes this exact form: it replaces the solver loops
+ * around make_csda_operator (:614-626) for the voxel-density model. */
+#define DP_SOLVE_SART 0
+#define DP_SOLVE_GN 1
+typedef struct {
+  int method;            /* DP_SOLVE_SART or DP_SOLVE_GN */
+  int n_iter;            /* outer iterations */
+  int cg_iter;           /* GN: conjugate-gradient iterations per solve (<= 0: 10) */
+  int precision;         /* forward model: DP_PREC_FP64 or DP_PREC_MIXED */
+  double relaxation;     /* SART relaxation (<= 0: 0.2) */
+  double lm_damping;     /* GN initial damping (<= 0: 1e-3) */
+  double box_lo, box_hi; /* density bounds, kg/m^3 */
+  double prior_weight;   /* > 0: smoothness prior weight * sum over the grid's
+                            6-neighbour edges of (rho_i - rho_j)^2 (SmoothnessPrior,
+                            src/Tomography_inverse.jl:17-79): GN objective term,
+                            SART smoothing sweep */
+  double smooth_strength; /* SART sweep strength (<= 0: 0.1) */
+} dp_solve_params;
+/* obs: n_rays observed fluxes, weight: n_rays data weights (NULL: 1), rho:
+ * the start density in, the estimate out (all device pointers; node arrays of
+ * tp on the device).  history (host, n_iter + 1 values, may be NULL): the misfit
+ * ||obs - f(rho)|| before each iteration and after the last; NaN where a
+ * Gauss-Newton loop stopped early (no accepted step). */
+int dp_tomo_solve_dev(dp_ctx* ctx, const dp_physics* phys, const dp_paths* paths,
+                      const dp_tomo_params* tp, const double* obs, const double* weight,
+                      double* rho, const dp_solve_params* sp, double* history);
+
 #ifdef __cplusplus
 }
 #endif
