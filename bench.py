@@ -219,8 +219,8 @@ def setup_c2(dp, torch, dev, precision="mixed", scale=1.0):
         r = dp.backward_mc_batch(phys, los, rock=mix, air=air, seed=2026, precision=precision)
         assert r["n_status_nonzero"][0] == 0
 
-    kernel = ("mc_init+mc_mixed_lo+mc_mixed_hi+mc_finish" if precision == "mixed"
-              else "mc_init+mc_fp64_lo+mc_fp64_hi+mc_finish")
+    kernel = ("mc_init+mc_mixed_lo+mc_mixed_hi+mc_finish+mc_tally" if precision == "mixed"
+              else "mc_init+mc_fp64_lo+mc_fp64_hi+mc_finish+mc_tally")
     info = {"units": n, "unit": "samples/s", "kernel": kernel,
             # per history: contribution (8 B) and status (4 B) written by the
             # transport kernel and read back by the tally
@@ -286,8 +286,8 @@ def setup_c4(dp, torch, dev, precision="mixed", scale=1.0):
                                        d_sub.data_ptr() + i * one, sub[i].n_samples, 1,
                                        d_out.data_ptr()), ctx)
 
-    kernel = "mc_init+mc_mixed_lo+mc_mixed_hi+mc_finish+csda_mc32" if precision == "mixed" else \
-        "mc_init+mc_fp64_lo+mc_fp64_hi+mc_finish+csda_mc"
+    kernel = "mc_init+mc_mixed_lo+mc_mixed_hi+mc_finish+csda_mc32+mc_tally" if precision == "mixed" \
+        else "mc_init+mc_fp64_lo+mc_fp64_hi+mc_finish+csda_mc+mc_tally"
     info = {"units": total, "unit": "samples/s", "kernel": kernel,
             # per history: contribution and status written and read back,
             # CSDA contribution and derivative written and read back

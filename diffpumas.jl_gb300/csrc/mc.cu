@@ -653,90 +653,141 @@ __global__ void __launch_bounds__(KCfg<R>::threads, 1) mc_kernel(const __grid_co
 }
 
 // Per line of sight: compensated sums of the contributions and of their
-// squares in a fixed order (one warp per line of sight), then flux, sigma
-// (src/Geometry.jl:883-893) and the count of flagged histories.
-__global__ void __launch_bounds__(256) los_tally_kernel(const double* contrib, const int32_t* status,
-                                                        const int64_t* off, const dp_los* los,
-                                                        long n_los, dp_los_result* out,
-                                                        int* status_or, const double* csda,
-                                                        const double* dcsda) {
+// squares in a fixed order, then flux, sigma (src/Geometry.jl:883-893) and
+// the count of flagged histories.  Two levels so that one long line of sight
+// does not serialise on one warp: fixed chunks of kTallyChunk histories of a
+// line (one warp each), then one warp per line combines its chunks in order.
+constexpr long kTallyChunk = 4096;
+struct TallyPart {
+  KSum s, s2, gf, g;
+  long bad;
+  int bits;
+};
+__device__ __forceinline__ void warp_down(KSum& v, int d) {
+  KSum o{__shfl_down_sync(0xffffffffu, v.s, d), __shfl_down_sync(0xffffffffu, v.c, d)};
+  kmerge(v, o);
+}
+__global__ void __launch_bounds__(256) los_chunk_kernel(const double* contrib, const int32_t* status,
+                                                        const int64_t* off, const int64_t* coff,
+                                                        long n_los, long max_jobs,
+                                                        const double* csda, const double* dcsda,
+                                                        TallyPart* part) {
+  long j = (long(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (j >= max_jobs || j >= coff[n_los]) return;
+  long lo = 0, hi = n_los;  // coff[lo] <= j < coff[lo + 1]
+  while (hi - lo > 1) {
+    long mid = (lo + hi) >> 1;
+    if (coff[mid] <= j) lo = mid; else hi = mid;
+  }
+  const long a = off[lo] + (j - coff[lo]) * kTallyChunk;
+  const long b = a + kTallyChunk < off[lo + 1] ? a + kTallyChunk : off[lo + 1];
+  TallyPart t{{0, 0}, {0, 0}, {0, 0}, {0, 0}, 0, 0};
+  for (long i = a + lane; i < b; i += 32) {
+    double x = contrib[i];
+    kadd(t.s, x);
+    kadd(t.s2, x * x);
+    int st = status[i];
+    t.bad += st != 0;
+    t.bits |= st;
+    if (csda) {
+      kadd(t.gf, csda[i]);
+      kadd(t.g, dcsda[i]);
+    }
+  }
+  t.bits = __reduce_or_sync(0xffffffffu, unsigned(t.bits));
+  for (int d = 16; d > 0; d >>= 1) {
+    warp_down(t.s, d);
+    warp_down(t.s2, d);
+    warp_down(t.gf, d);
+    warp_down(t.g, d);
+    t.bad += __shfl_down_sync(0xffffffffu, t.bad, d);
+  }
+  if (lane == 0) part[j] = t;
+}
+__global__ void __launch_bounds__(256) los_tally_kernel(const TallyPart* part, const int64_t* off,
+                                                        const int64_t* coff, const dp_los* los,
+                                                        long n_los, int has_csda,
+                                                        dp_los_result* out, int* status_or) {
   long l = (long(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (l >= n_los) return;
-  long a = off[l], b = off[l + 1];
-  KSum s{0, 0}, s2{0, 0}, g{0, 0}, gf{0, 0};
-  long bad = 0;
-  int bits = 0;
-  for (long i = a + lane; i < b; i += 32) {
-    double x = contrib[i];
-    kadd(s, x);
-    kadd(s2, x * x);
-    int st = status[i];
-    bad += st != 0;
-    bits |= st;
-    if (csda) {
-      kadd(gf, csda[i]);
-      kadd(g, dcsda[i]);
-    }
+  TallyPart t{{0, 0}, {0, 0}, {0, 0}, {0, 0}, 0, 0};
+  for (int64_t j = coff[l] + lane; j < coff[l + 1]; j += 32) {
+    const TallyPart& q = part[j];
+    kmerge(t.s, q.s);
+    kmerge(t.s2, q.s2);
+    kmerge(t.gf, q.gf);
+    kmerge(t.g, q.g);
+    t.bad += q.bad;
+    t.bits |= q.bits;
   }
-  bits = __reduce_or_sync(0xffffffffu, unsigned(bits));
-  auto down = [](KSum& v, int d) {
-    KSum o{__shfl_down_sync(0xffffffffu, v.s, d), __shfl_down_sync(0xffffffffu, v.c, d)};
-    kmerge(v, o);
-  };
+  t.bits = __reduce_or_sync(0xffffffffu, unsigned(t.bits));
   for (int d = 16; d > 0; d >>= 1) {
-    down(s, d);
-    down(s2, d);
-    down(g, d);
-    down(gf, d);
-    bad += __shfl_down_sync(0xffffffffu, bad, d);
+    warp_down(t.s, d);
+    warp_down(t.s2, d);
+    warp_down(t.gf, d);
+    warp_down(t.g, d);
+    t.bad += __shfl_down_sync(0xffffffffu, t.bad, d);
   }
   if (lane == 0) {
-    long n = b - a;
-    double sum = s.s + s.c, sum2 = s2.s + s2.c;
+    long n = off[l + 1] - off[l];
+    double sum = t.s.s + t.s.c, sum2 = t.s2.s + t.s2.c;
     dp_los_result r{};
     r.n_samples = n;
-    r.n_status_nonzero = bad;
+    r.n_status_nonzero = t.bad;
     if (n > 0) {
       double f = sum / double(n), var = sum2 / double(n) - f * f;
       r.flux = f;
       r.sigma = los[l].thickness > 0.0 ? sqrt(fmax(var, 0.0) / double(n)) : 0.0;
-      if (csda) {
-        r.gradient_flux = (gf.s + gf.c) / double(n);
-        r.gradient = (g.s + g.c) / double(n);
+      if (has_csda) {
+        r.gradient_flux = (t.gf.s + t.gf.c) / double(n);
+        r.gradient = (t.g.s + t.g.c) / double(n);
       }
     }
     out[l] = r;
-    if (bits) atomicOr(status_or, bits);
+    if (t.bits) atomicOr(status_or, t.bits);
   }
 }
 
 // Running sample offsets of the lines of sight (single block, sequential
 // chunks; n_los is at most a few 10^5).
+// Also the running chunk offsets of the tally (coff).
 __global__ void __launch_bounds__(1024) los_offsets_kernel(const dp_los* los, long n_los,
-                                                           int64_t* off, long expect, int* err) {
-  __shared__ int64_t part[1024];
+                                                           int64_t* off, int64_t* coff, long expect,
+                                                           int* err) {
+  __shared__ int64_t part[1024], cpart[1024];
   long per = (n_los + 1023) / 1024;
   long a = threadIdx.x * per, b = a + per < n_los ? a + per : n_los;
-  int64_t s = 0;
-  for (long l = a; l < b; ++l) s += los[l].n_samples > 0 ? los[l].n_samples : 0;
+  auto count = [&](long l) { return los[l].n_samples > 0 ? int64_t(los[l].n_samples) : int64_t(0); };
+  int64_t s = 0, cs = 0;
+  for (long l = a; l < b; ++l) {
+    s += count(l);
+    cs += (count(l) + kTallyChunk - 1) / kTallyChunk;
+  }
   part[threadIdx.x] = s;
+  cpart[threadIdx.x] = cs;
   __syncthreads();
   if (threadIdx.x == 0) {
-    int64_t run = 0;
+    int64_t run = 0, crun = 0;
     for (int t = 0; t < 1024; ++t) {
-      int64_t v = part[t];
+      int64_t v = part[t], cv = cpart[t];
       part[t] = run;
+      cpart[t] = crun;
       run += v;
+      crun += cv;
     }
     off[n_los] = run;
+    coff[n_los] = crun;
     if (run != expect) atomicExch(err, 2);
   }
   __syncthreads();
-  int64_t run = part[threadIdx.x];
+  int64_t run = part[threadIdx.x], crun = cpart[threadIdx.x];
   for (long l = a; l < b; ++l) {
     off[l] = run;
-    run += los[l].n_samples > 0 ? los[l].n_samples : 0;
+    coff[l] = crun;
+    run += count(l);
+    crun += (count(l) + kTallyChunk - 1) / kTallyChunk;
   }
 }
 
@@ -1086,11 +1137,15 @@ int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_
   long nt = total > 0 ? total : 1;
   Arena A;
   A.base = static_cast<char*>(scratch(
-      ctx, size_t(nt) * (12 + 16 + kRecBytes) + size_t(n_los + 1) * 8 + 4096, 0));
+      ctx, size_t(nt) * (12 + 16 + kRecBytes) + size_t(n_los + 1) * 16 +
+               size_t(n_los + nt / kTallyChunk + 1) * sizeof(TallyPart) + 4096, 0));
   A.cap = ctx->slot_bytes[0];
   double* dc = A.take<double>(nt);
   int32_t* ds = A.take<int32_t>(nt);
   int64_t* off = A.take<int64_t>(n_los + 1);
+  int64_t* coff = A.take<int64_t>(n_los + 1);
+  const long max_jobs = n_los + nt / kTallyChunk + 1;
+  TallyPart* tpart = A.take<TallyPart>(max_jobs);
   unsigned long long* ctr = A.take<unsigned long long>(3);
   Handoff<double>* queue = A.take<Handoff<double>>(nt);
   StartRec<double>* srec = A.take<StartRec<double>>(nt);
@@ -1100,7 +1155,7 @@ int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_
   int* bits = A.take<int>(1);
   if (!bits) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
   DP_CHECK_CUDA(ctx, cudaMemsetAsync(bits, 0, sizeof(int), ctx->stream));
-  los_offsets_kernel<<<1, 1024, 0, ctx->stream>>>(d_los, n_los, off, total, ctx->d_flag);
+  los_offsets_kernel<<<1, 1024, 0, ctx->stream>>>(d_los, n_los, off, coff, total, ctx->d_flag);
   ++ctx->launches;
   DP_CHECK_CUDA(ctx, cudaGetLastError());
   if (total > 0) {
@@ -1126,11 +1181,13 @@ int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_
       if (rc) return rc;
     }
   }
-  long warps_per_block = 8;
-  long blocks = (n_los + warps_per_block - 1) / warps_per_block;
+  const long warps_per_block = 8;
   timed_begin(ctx);
-  los_tally_kernel<<<int(blocks), 256, 0, ctx->stream>>>(dc, ds, off, d_los, n_los, d_out, bits,
-                                                         total > 0 ? cc : nullptr, cd);
+  los_chunk_kernel<<<int((max_jobs + warps_per_block - 1) / warps_per_block), 256, 0, ctx->stream>>>(
+      dc, ds, off, coff, n_los, max_jobs, total > 0 ? cc : nullptr, cd, tpart);
+  los_tally_kernel<<<int((n_los + warps_per_block - 1) / warps_per_block), 256, 0, ctx->stream>>>(
+      tpart, off, coff, d_los, n_los, total > 0 && cc ? 1 : 0, d_out, bits);
+  ++ctx->launches;
   DP_CHECK_CUDA(ctx, cudaGetLastError());
   timed_end(ctx, "mc_tally");
   if (contrib_out) *contrib_out = dc;
