@@ -224,7 +224,13 @@ def setup_c2(dp, torch, dev, precision="mixed", scale=1.0):
     info = {"units": n, "unit": "samples/s", "kernel": kernel,
             # per history: contribution (8 B) and status (4 B) written by the
             # transport kernel and read back by the tally
-            "alg_bytes": n * 24, "traffic": None,
+            "alg_bytes": n * 24,
+            # DRAM bytes of one step from an ncu capture of all six launches at
+            # 2e5 histories (89.6 MB), scaled by the histories: the start, hand-off
+            # and end records grow in proportion
+            "traffic": int(448 * n) if precision == "mixed" else None,
+            "note": "SM-issue bound, not HBM: ncu smsp__issue_active 18.0% (phase 0) and "
+                    "28.5% (phase 1), DRAM throughput < 0.1%",
             "config": {"workload": "c2: straggled MC with DEL/EHS + Coulomb scattering, rock mixture "
                                    "rock/water/air 0.70/0.25/0.05 (per-history thickness U[20,500] m, "
                                    "density U[2000,2800], elevation U[30,90] deg) under 1 km air, "
@@ -292,6 +298,7 @@ def setup_c4(dp, torch, dev, precision="mixed", scale=1.0):
             # per history: contribution and status written and read back,
             # CSDA contribution and derivative written and read back
             "alg_bytes": total * (24 + 32), "traffic": None,
+            "note": "SM-issue bound, not HBM: ncu smsp__issue_active 26.3% (mixed transport)",
             "config": {"workload": "c4: 16384 vertical lines of sight, depth log-uniform 50-2000 m, "
                                    "density U[2400,2800], 64-1024 histories each (uneven), mixed "
                                    "transport everywhere, E 1 GeV-10 TeV, + CSDA d flux/d rho per "
@@ -493,7 +500,8 @@ def run_gpu(args):
                          "frac": achieved / peak if achieved else None,
                          "traffic": info.get("traffic"),
                          "kernel": info["kernel"], "kernel_ms": kernel_ms,
-                         "kernel_ms_each": breakdown, "peak_source": peak_kind},
+                         "kernel_ms_each": breakdown, "peak_source": peak_kind,
+                         **({"note": info["note"]} if info.get("note") else {})},
             "gpu_launches": int(launches),
             "plain_gpu": plain,
             "speedup_vs_plain": (value / plain["value"]) if plain else None,
