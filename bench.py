@@ -12,6 +12,10 @@ Workloads (seeded synthetic inputs):
       smooth random density field with 3 cavities, 4 detectors x 1024 rays,
       32 CSDA energy nodes on [1, 1e6] GeV.  One step = per-ray flux and the
       density vector-Jacobian product J^T r over all rays.  Unit: rays/s.
+  dir fixed-path stochastic MC (compute_directional_flux_mc): 4096
+      directions x 1024 histories through a voxel volume of rock and
+      rock+water cells, rock to the surface and air above; energies
+      1e-3 - 1e9 GeV drawn on the device.  Unit: samples/s.
   c1  backward MC, CSDA mode, StandardRock 2650 kg/m^3, 100 m, 45 deg,
       energies log-uniform 1-100 GeV, +-1 charges, 10^4 histories, with the
       density gradient.  One step = one run_backward_mc estimate.  Unit:
@@ -366,6 +370,70 @@ def setup_c5(dp, torch, dev, precision="mixed", scale=1.0):
     return step, e2e, None, info, phys
 
 
+DIR_E = (1e-3, 1e9)  # final-energy range of the reference's directional runs (GeV)
+
+
+def dir_scene(dp, phys, n_dirs):
+    """Fixed-path workload inputs: material config, site, paths and per-cell
+    mixtures (rock or rock with 30 % water by mass)."""
+    from dpgpu.workloads import directional_config
+    raw, wf = directional_config(n_dirs)
+    cfg = dp.MaterialConfig(1, 3, 2, -1, 2710.0, 1000.0, 0.0, 0.0)
+    site = dp.SiteConfig(963.0, 30000.0)
+    mats, dens = dp.build_cell_properties_for_mc(phys, np.zeros(len(wf), bool), wf, cfg)
+    paths = [dp.DirectionalPath(z, a, [dp.CellSegment(c, l) for c, l in segs], tin, slant, rem,
+                                sz, True) for z, a, segs, tin, slant, rem, sz in raw]
+    return cfg, site, paths, mats, dens, wf
+
+
+def setup_dir(dp, torch, dev, precision="mixed", scale=1.0):
+    """Fixed-path stochastic MC (compute_directional_flux_mc) over 4096
+    directions x 1024 histories: a 640 m x 640 m x 320 m voxel volume of
+    rock and rock with 30 % water (by mass, half the cells each), rock to a
+    flat surface 600 m above the detector (slant depths 0.6-2.3 km), air to
+    30 km; final energies log-uniform 1e-3 - 1e9 GeV drawn on the device,
+    straggling on, mode switch at 100 GeV, no scattering (the settings of the
+    reference's directional timing runs)."""
+    phys = dp.create_physics(materials=(dp.STANDARD_ROCK, dp.AIR, dp.WATER))
+    n_dirs = max(16, int(4096 * scale))
+    per = 1024
+    cfg, site, paths, mats, dens, _ = dir_scene(dp, phys, n_dirs)
+    batch = dp.DirBatch(phys, cfg, site, paths, mats, dens, None, n_samples=per,
+                        energy_min=DIR_E[0], energy_max=DIR_E[1]).to_device()
+    sub = dp.DirBatch(phys, cfg, site, paths[:16], mats, dens, None, n_samples=per,
+                      energy_min=DIR_E[0], energy_max=DIR_E[1])
+    one = [dp.DirBatch(phys, cfg, site, [p], mats, dens, None, n_samples=per,
+                       energy_min=DIR_E[0], energy_max=DIR_E[1]).to_device() for p in paths[:16]]
+
+    def step_dev():
+        batch.run_dev(2028, precision=precision)
+
+    def step_e2e():
+        r = batch.run(2028, precision=precision)
+        assert r["n_status_nonzero"].sum() == 0
+
+    def plain_dev():
+        for b in one:
+            b.run_dev(2028, precision="fp64")
+
+    name = "mixed" if precision == "mixed" else "fp64"
+    info = {"units": batch.total, "unit": "samples/s",
+            "kernel": f"dir_init+dir_{name}_lo+dir_{name}_hi+dir_finish+mc_tally",
+            # per history: contribution and status written and read back
+            "alg_bytes": batch.total * 24, "traffic": None,
+            "note": "SM-issue bound (one thread per history, table lookups in shared memory)",
+            "config": {"workload": "dir: fixed-path MC (compute_directional_flux_mc), 4096 "
+                                   "directions x 1024 histories, 32x32x16 cells @ 20 m of rock / "
+                                   "rock+30% water, rock to a surface 600 m up, air to 30 km, "
+                                   "E 1e-3-1e9 GeV, straggling, switch 100 GeV",
+                       "n_dirs": n_dirs, "n_samples": batch.total, "precision": precision,
+                       "segments": int(batch.arrays["seg_ptr"][-1]), "media": len(batch.media)},
+            "h2d": batch.host_bytes(), "d2h": n_dirs * C.sizeof(dp.DpLosResult),
+            "plain_what": "FP64 transport, one launch per direction, first 16 directions",
+            "plain_units": sub.total, "plain_reps": 1}
+    return step_dev, step_e2e, plain_dev, info, phys
+
+
 def setup_c1(dp, torch, dev):
     phys = dp.create_physics()
     n = 10000
@@ -397,8 +465,8 @@ def run_gpu(args):
     import dpgpu as dp
     dp._default = dp.Context(local)
     setup = {"c2": setup_c2, "c3": setup_c3, "c4": setup_c4, "c5": setup_c5,
-             "c1": setup_c1}[args.workload]
-    kw = {"scale": args.scale} if args.workload in ("c2", "c4", "c5") else {}
+             "c1": setup_c1, "dir": setup_dir}[args.workload]
+    kw = {"scale": args.scale} if args.workload in ("c2", "c4", "c5", "dir") else {}
     step_dev, step_e2e, plain_dev, info, phys = setup(dp, torch, dev, **kw)
     if args.scale != 1.0:
         info["config"]["scale"] = args.scale
@@ -556,6 +624,8 @@ def cpu_baseline(workload, budget_s=15.0, threads=None):
         return {"value": n / dt, "unit": "samples/s", "cores": threads, "kind": "port",
                 "sample": f"{l} lines of sight ({n} histories) of the c4 workload: stochastic "
                           "transport + dual-number CSDA gradient (FP64 oracle, OpenMP)"}
+    if workload == "dir":
+        return cpu_baseline_dir(O, budget_s, threads)
     if workload == "c2":
         p = O.default_physics((O.STANDARD_ROCK, O.AIR, O.WATER), coulomb=True)
         rng = np.random.default_rng(0)
@@ -585,13 +655,45 @@ def cpu_baseline(workload, budget_s=15.0, threads=None):
             "sample": f"{n} histories of the c1 workload with the dual-number gradient (FP64 oracle, OpenMP)"}
 
 
+def cpu_baseline_dir(O, budget_s, threads):
+    """The oracle's fixed-path MC over the dir workload's directions (cycled),
+    1024 histories each with the device's Philox energy draws."""
+    from dpgpu.workloads import directional_config
+    raw, wf = directional_config(4096)
+    p = O.default_physics((O.STANDARD_ROCK, O.AIR, O.WATER), coulomb=True)
+    mix = 1.0 / (0.7 / 2710.0 + 0.3 / 1000.0)
+    media = [([0], [1.0]), ([0, 2], [0.7, 0.3]), ([1], [1.0])]  # rock, rock+water, air
+    per = 1024
+    rk = np.log(DIR_E[1] / DIR_E[0])
+    n, t0, d = 0, time.perf_counter(), 0
+    while time.perf_counter() - t0 < budget_s:
+        z, a, segs, tin, slant, rem, sz = raw[d % len(raw)]
+        cells = np.array([c - 1 for c, _ in segs])
+        wet = wf[cells] > 0
+        ct = np.cos(np.radians(z))
+        rng = np.random.default_rng(n)
+        E = DIR_E[0] * np.exp(rk * rng.random(per))
+        q = np.where(rng.random(per) > 0.5, 1.0, -1.0)
+        O.dir_histories(p, media, 0, 2710.0, 2, 963.0, [ct], [rem],
+                        [max(0.0, 30000.0 - sz) / max(ct, 1e-3)], [0, len(segs)],
+                        wet.astype(np.int32), np.where(wet, mix, 2710.0),
+                        [l for _, l in segs], [0, per], E, q, E * rk, seed=11, id0=n,
+                        threads=threads)
+        n += per
+        d += 1
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": "samples/s", "cores": threads, "kind": "port",
+            "sample": f"{d} directions x {per} histories of the dir workload (FP64 oracle, "
+                      "OpenMP over histories)"}
+
+
 def run_reference(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     units = {"c2": "samples/s", "c3": "rays/s", "c4": "samples/s", "c5": "iterations/s",
-             "c1": "samples/s"}[args.workload]
+             "c1": "samples/s", "dir": "samples/s"}[args.workload]
     vals = []
     for _ in range(args.warmup):
         cpu_baseline(args.workload, budget_s=args.cpu_seconds / 4)
@@ -616,7 +718,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "c1"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "c1", "dir"])
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")

@@ -18,10 +18,11 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # bits on x86 and Arm (the device code keeps nvcc's default contraction)
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr", "--extended-lambda"]
-UNITS = ["api.cu", "physics_build.cu", "csda_mc.cu", "tomo.cu", "mc.cu", "inverse.cu"]
+UNITS = ["api.cu", "physics_build.cu", "csda_mc.cu", "tomo.cu", "mc.cu", "dir_mc.cu",
+         "inverse.cu"]
 # per-unit flags: the stochastic transport's FP32 kernel uses the hardware
 # (MUFU) transcendentals; FP64 arithmetic is not affected by these flags
-UNIT_FLAGS = {"mc.cu": ["--use_fast_math"]}
+UNIT_FLAGS = {"mc.cu": ["--use_fast_math"], "dir_mc.cu": ["--use_fast_math"]}
 
 
 def nvcc():

@@ -2,8 +2,6 @@
 // the host (mixture properties and the MIXED transport kernel), the
 // persistent history kernel in FP64 and mixed precision, the deterministic
 // per-line-of-sight tallies and the C ABI.
-#include <cooperative_groups.h>
-
 #include <algorithm>
 #include <atomic>
 #include <cmath>
@@ -11,40 +9,16 @@
 #include <limits>
 #include <vector>
 
-#include "internal.h"
-#include "mc_device.cuh"
+#include "mc_host.h"
+#include "mc_loop.cuh"
 
 namespace {
 // Nuclear RMS radii (fm) by atomic number (src/Straggling.jl:726-729 table).
 #include "physics_data.inc"
 }  // namespace
 
-namespace cg = cooperative_groups;
 using namespace dp;
 using namespace dp::mc;
-
-// A prepared medium: host columns plus device blobs cached per partner medium.
-struct dp_mixture {
-  const dp_physics* phys = nullptr;
-  uint64_t uid = 0;
-  int nm = 0;
-  std::vector<int> mats;
-  std::vector<double> fracs;
-  int n = 0;                  // physics grid nodes
-  std::vector<double> cols;   // (MC_LB1 + 2*nm) columns of n: see MedCol
-  int nk = 0;                 // MIXED kernel nodes
-  std::vector<double> kcols;  // K_NCOL columns of nk
-  double onset = 0, ZoA = 0;
-  std::vector<double> el;     // nel x kElStride
-  int nel = 0;
-  struct Blob {
-    uint64_t partner;
-    int precision;
-    unsigned char* dev;
-    Layout lay;
-  };
-  std::vector<Blob> blobs;    // this medium as rock, `partner` as air
-};
 
 namespace {
 
@@ -227,11 +201,22 @@ int pad_elems(int n, size_t esize) {
   return (n + per - 1) / per * per;
 }
 
-Layout make_layout(const dp_mixture* a, const dp_mixture* b, size_t esize) {
+}  // namespace
+
+namespace dp {
+namespace mc {
+
+Layout make_layout(const dp_mixture* const* media, int n_media, size_t esize) {
+  const dp_mixture* a = media[0];
   Layout L{};
   L.n = a->n;
   L.nk = a->nk;
-  L.slots = std::max(a->nm, b->nm);
+  L.slots = 1;
+  bool same_nk = true;
+  for (int k = 0; k < n_media; ++k) {
+    L.slots = std::max(L.slots, media[k]->nm);
+    same_nk = same_nk && media[k]->nk == a->nk;
+  }
   L.ld = pad_elems(L.n, esize);
   L.ldk = pad_elems(L.nk, esize);
   // elements, then the index-table origins and widths (2 doubles per column)
@@ -248,13 +233,13 @@ Layout make_layout(const dp_mixture* a, const dp_mixture* b, size_t esize) {
   L.lE0 = ph->view.lE0;
   L.inv_dlE = ph->view.inv_dlE;
   // kernel energies: 8 log-uniform nodes per interval of a uniform grid
-  L.kuniform = L.uniform && a->nk == 8 * (a->n - 1) + 1 && b->nk == a->nk ? 1 : 0;
+  L.kuniform = L.uniform && a->nk == 8 * (a->n - 1) + 1 && same_nk ? 1 : 0;
   L.kinv_dlE = 8.0 * ph->view.inv_dlE;
   return L;
 }
 
 template <class R>
-void pack(const dp_mixture* m, const Layout& L, unsigned char* out) {
+static void pack(const dp_mixture* m, const Layout& L, unsigned char* out) {
   std::memset(out, 0, L.med_bytes);
   std::memcpy(out, m->el.data(), m->el.size() * sizeof(double));
   R* P = reinterpret_cast<R*>(out + L.o_phys);
@@ -307,6 +292,11 @@ void pack(const dp_mixture* m, const Layout& L, unsigned char* out) {
   }
 }
 
+void pack_medium(const dp_mixture* m, const Layout& L, size_t esize, unsigned char* out) {
+  if (esize == sizeof(float)) pack<float>(m, L, out);
+  else pack<double>(m, L, out);
+}
+
 MedInfo make_info(const dp_mixture* m) {
   MedInfo I{};
   I.nm = m->nm;
@@ -316,6 +306,11 @@ MedInfo make_info(const dp_mixture* m) {
   I.onset = m->onset;
   return I;
 }
+
+}  // namespace mc
+}  // namespace dp
+
+namespace {
 
 // Device blob of the (rock, air) pair in one precision, built once per pair.
 int get_blob(dp_ctx* ctx, dp_mixture* rock, const dp_mixture* air, int precision,
@@ -329,15 +324,11 @@ int get_blob(dp_ctx* ctx, dp_mixture* rock, const dp_mixture* air, int precision
   if (rock->n != air->n || rock->nk != air->nk || rock->phys != air->phys)
     return fail(ctx, DP_ERR_ARG, "rock and air media must come from one physics");
   size_t es = precision == DP_PREC_MIXED ? sizeof(float) : sizeof(double);
-  Layout L = make_layout(rock, air, es);
+  const dp_mixture* pair[2] = {rock, air};
+  Layout L = make_layout(pair, 2, es);
   std::vector<unsigned char> h(size_t(2) * L.med_bytes);
-  if (es == sizeof(float)) {
-    pack<float>(rock, L, h.data());
-    pack<float>(air, L, h.data() + L.med_bytes);
-  } else {
-    pack<double>(rock, L, h.data());
-    pack<double>(air, L, h.data() + L.med_bytes);
-  }
+  pack_medium(rock, L, es, h.data());
+  pack_medium(air, L, es, h.data() + L.med_bytes);
   unsigned char* d = nullptr;
   DP_CHECK_CUDA(ctx, cudaMalloc(&d, h.size()));
   DP_CHECK_CUDA(ctx, cudaMemcpy(d, h.data(), h.size(), cudaMemcpyHostToDevice));
@@ -379,51 +370,6 @@ struct McParams {
   void* start;                // StartRec<R> x n
   void* end;                  // EndRec<R> x n
 };
-
-// Copies `bytes` (16-byte multiple) from global to shared memory with
-// cp.async.bulk completing on one mbarrier; all threads call it.  Returns
-// false if the bounded wait gave up.
-__device__ bool stage_blob(unsigned char* dst, const unsigned char* src, uint32_t bytes,
-                           uint64_t* mbar) {
-  uint32_t bar = smem_u32(mbar);
-  if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(1) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-                 : "memory");
-    const uint32_t chunk = 32768;
-    for (uint32_t off = 0; off < bytes; off += chunk) {
-      uint32_t b = bytes - off < chunk ? bytes - off : chunk;
-      asm volatile(
-          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-              smem_u32(dst + off)),
-          "l"(src + off), "r"(b), "r"(bar)
-          : "memory");
-    }
-  }
-  uint32_t done = 0;
-  for (int it = 0; it < (1 << 22) && !done; ++it) {
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(bar), "r"(0)
-        : "memory");
-  }
-  return __syncthreads_and(done != 0) != 0;
-}
-
-// Next history index for the calling thread (warp-aggregated atomic).
-__device__ __forceinline__ long next_history(unsigned long long* counter) {
-  cg::coalesced_group g = cg::coalesced_threads();
-  unsigned long long base = 0;
-  if (g.thread_rank() == 0) base = atomicAdd(counter, (unsigned long long)g.size());
-  base = g.shfl(base, 0);
-  return long(base + g.thread_rank());
-}
 
 // Start record of history i: energy, charge and weight drawn as
 // run_backward_mc draws them (src/Geometry.jl:863-875) or given; geometry
@@ -538,17 +484,32 @@ __global__ void __launch_bounds__(256) mc_finish_kernel(const __grid_constant__ 
   }
 }
 
-// Launch shape per precision: the FP32 transport runs 16 warps per SM
-// sharing one staged copy of the tables and evaluates hard-event DCS sums
-// cooperatively per warp; the FP64 transport (one thread per sum) runs 8.
-template <class R> struct KCfg;
-template <> struct KCfg<float> {
-  static constexpr int threads = 512;
-  static constexpr bool coop = true;
-};
-template <> struct KCfg<double> {
-  static constexpr int threads = 256;
-  static constexpr bool coop = false;
+// Two-layer geometry of run_backward_mc (rock column under air) for the
+// shared history loop.
+template <class R>
+struct SlabGeo {
+  using Hist = mc::Hist<R>;
+  using Queue = Handoff<R>;
+  const McParams& P;
+  Med<R> rock, air;
+  __device__ long n0() const { return P.n; }
+  __device__ void start(long i, Hist& h, Stream& g) const { start_history(P, i, h, g); }
+  __device__ long load(const Queue& q, Hist& h, Stream& g) const {
+    return load_handoff(q, P.seed, h, g);
+  }
+  __device__ void save(const Hist& h, const Stream& g, long i, Queue* q) const {
+    save_handoff(h, g, i, q);
+  }
+  __device__ void end(long i, const Hist& h) const { end_history(P, i, h); }
+  __device__ const Med<R>& medium(int k) const { return k ? air : rock; }
+  template <bool COOP, int PHASE>
+  __device__ int advance(Hist& h, Stream& g) const {
+    return mc::advance<R, COOP, PHASE>(rock, air, P.C, h, g);
+  }
+  template <int PHASE>
+  __device__ int resume(Hist& h, Stream& g) const {
+    return mc::resume<R, PHASE>(rock, air, P.C, h, g);
+  }
 };
 
 template <class R, int PHASE>
@@ -557,99 +518,17 @@ __global__ void __launch_bounds__(KCfg<R>::threads, 1) mc_kernel(const __grid_co
   const unsigned char* base = P.blob;
   const uint32_t tables = P.staged ? 2 * P.lay.med_bytes : 0;
   if (P.staged) {
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
-    unsigned char* dst = smem + 16;
-    if (!stage_blob(dst, P.blob, tables, bar)) {
-      // give the copy in flight a second bounded wait before leaving
-      uint32_t done = 0;
-      for (int it = 0; it < (1 << 22) && !done; ++it)
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(smem_u32(bar)), "r"(0)
-            : "memory");
+    if (!stage_blob(smem + 16, P.blob, tables, reinterpret_cast<uint64_t*>(smem))) {
       if (threadIdx.x == 0) atomicExch(P.err_flag, 1);
       return;
     }
-    base = dst;
+    base = smem + 16;
   }
-  const Med<R> rock = make_med<R>(base, P.lay, P.info[0]);
-  const Med<R> air = make_med<R>(base + P.lay.med_bytes, P.lay, P.info[1]);
-  Handoff<R>* queue = static_cast<Handoff<R>*>(P.queue);
-  const long n = PHASE == 0 ? P.n : long(*(volatile unsigned long long*)(P.counter + 2));
-  Hist<R> h;
-  Stream g;
-  auto take = [&](long* idx) -> bool {
-    long j = next_history(P.counter + PHASE);
-    if (j >= n) return false;
-    if (PHASE == 0) {
-      *idx = j;
-      start_history(P, j, h, g);
-    } else {
-      *idx = load_handoff(queue[j], P.seed, h, g);
-    }
-    return true;
-  };
-  // after a step: end the history, hand it to phase 1, or keep going
-  auto settle = [&](int r, long* idx) -> bool {
-    if (r == ADV_HANDOFF) {
-      unsigned long long slot = atomicAdd(P.counter + 2, 1ull);
-      save_handoff(h, g, *idx, queue + slot);
-      return take(idx);
-    }
-    if (r == ADV_DONE) {
-      end_history(P, *idx, h);
-      return take(idx);
-    }
-    return true;
-  };
-  long i = 0;
-  bool live = take(&i);
-  if constexpr (KCfg<R>::coop) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float* item = reinterpret_cast<float*>(smem + 16 + tables) + size_t(warp) * P.coop_stride;
-    float* comp = item + kItemsPerElement * P.coop_nel;
-    for (;;) {
-      // serve the hard events the warp's suspended steps wait for, one at a time
-      unsigned want = __ballot_sync(0xffffffffu, live && h.x.kind != CONT_NONE);
-      while (want) {
-        const int L = __ffs(want) - 1;
-        want &= want - 1;
-        const int med = __shfl_sync(0xffffffffu, h.x.medium, L);
-        const double anc = __shfl_sync(0xffffffffu, h.x.anc, L);
-        const double q = __shfl_sync(0xffffffffu, h.x.q, L);
-        const Med<R>& m = med ? air : rock;
-        const double total = coop_total(m.elf, m.nel, float(P.C.mass), anc, q, item, comp);
-        if (lane == L) {
-          h.x.total = total;
-          h.x.pick = -1;
-          if (h.x.details && total > 0.0) {
-            // process and element pick in the reference's order (src/MixedTransport.jl:131-140)
-            double u = uni_d(g) * total;
-            const int last = 4 * m.nel - 1;
-            int pick = last;
-            for (int c = 0; c <= last; ++c) {
-              u -= double(comp[c]);
-              if (u <= 0.0) {
-                pick = c;
-                break;
-              }
-            }
-            h.x.pick = pick;
-          }
-        }
-        __syncwarp();
-      }
-      if (live) {
-        const int r = h.x.kind != CONT_NONE ? resume<R, PHASE>(rock, air, P.C, h, g)
-                                            : advance<R, true, PHASE>(rock, air, P.C, h, g);
-        live = settle(r, &i);
-      }
-      if (!__any_sync(0xffffffffu, live)) break;
-    }
-  } else {
-    while (live) live = settle(advance<R, false, PHASE>(rock, air, P.C, h, g), &i);
-  }
+  SlabGeo<R> geo{P, make_med<R>(base, P.lay, P.info[0]),
+                 make_med<R>(base + P.lay.med_bytes, P.lay, P.info[1])};
+  float* item = reinterpret_cast<float*>(smem + 16 + tables) + size_t(threadIdx.x >> 5) * P.coop_stride;
+  transport_histories<R, PHASE, KCfg<R>::coop>(geo, P.C, P.counter, static_cast<Handoff<R>*>(P.queue),
+                                               item, item + kItemsPerElement * P.coop_nel);
 }
 
 // Per line of sight: compensated sums of the contributions and of their
@@ -705,9 +584,13 @@ __global__ void __launch_bounds__(256) los_chunk_kernel(const double* contrib, c
   }
   if (lane == 0) part[j] = t;
 }
+// sigma_n1 = 0: run_backward_mc's sigma (src/Geometry.jl:883-893); 1: the
+// directional MC's, with n - 1 (src/Tomography.jl:1036-1039), NaN results
+// for directions with valid[l] == 0 (src/Tomography.jl:991-993).
 __global__ void __launch_bounds__(256) los_tally_kernel(const TallyPart* part, const int64_t* off,
                                                         const int64_t* coff, const dp_los* los,
-                                                        long n_los, int has_csda,
+                                                        const int32_t* valid, long n_los,
+                                                        int has_csda, int sigma_n1,
                                                         dp_los_result* out, int* status_or) {
   long l = (long(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
@@ -739,27 +622,32 @@ __global__ void __launch_bounds__(256) los_tally_kernel(const TallyPart* part, c
     if (n > 0) {
       double f = sum / double(n), var = sum2 / double(n) - f * f;
       r.flux = f;
-      r.sigma = los[l].thickness > 0.0 ? sqrt(fmax(var, 0.0) / double(n)) : 0.0;
+      if (sigma_n1) r.sigma = sqrt(fmax(0.0, var / double(n > 1 ? n - 1 : 1)));
+      else r.sigma = los[l].thickness > 0.0 ? sqrt(fmax(var, 0.0) / double(n)) : 0.0;
       if (has_csda) {
         r.gradient_flux = (t.gf.s + t.gf.c) / double(n);
         r.gradient = (t.g.s + t.g.c) / double(n);
       }
     }
+    if (valid && !valid[l]) r.flux = r.sigma = CUDART_NAN;
     out[l] = r;
     if (t.bits) atomicOr(status_or, t.bits);
   }
 }
 
 // Running sample offsets of the lines of sight (single block, sequential
-// chunks; n_los is at most a few 10^5).
-// Also the running chunk offsets of the tally (coff).
-__global__ void __launch_bounds__(1024) los_offsets_kernel(const dp_los* los, long n_los,
-                                                           int64_t* off, int64_t* coff, long expect,
-                                                           int* err) {
+// chunks; n_los is at most a few 10^5), or a copy of given offsets, and the
+// running chunk offsets of the tally (coff).
+__global__ void __launch_bounds__(1024) los_offsets_kernel(const dp_los* los, const int64_t* given,
+                                                           long n_los, int64_t* off, int64_t* coff,
+                                                           long expect, int* err) {
   __shared__ int64_t part[1024], cpart[1024];
   long per = (n_los + 1023) / 1024;
   long a = threadIdx.x * per, b = a + per < n_los ? a + per : n_los;
-  auto count = [&](long l) { return los[l].n_samples > 0 ? int64_t(los[l].n_samples) : int64_t(0); };
+  auto count = [&](long l) {
+    if (given) return given[l + 1] - given[l] > 0 ? given[l + 1] - given[l] : int64_t(0);
+    return los[l].n_samples > 0 ? int64_t(los[l].n_samples) : int64_t(0);
+  };
   int64_t s = 0, cs = 0;
   for (long l = a; l < b; ++l) {
     s += count(l);
@@ -800,8 +688,13 @@ namespace {
 constexpr size_t kRecBytes = sizeof(Handoff<double>) + sizeof(StartRec<double>) +
                              sizeof(EndRec<double>) + 64;
 
+}  // namespace
+
+namespace dp {
+namespace mc {
+
 int check_cfg(dp_ctx* ctx, const dp_physics* ph, const dp_mc_config* cfg, Consts* C,
-              double* thr_fp64 = nullptr) {
+              double* thr_fp64) {
   if (!cfg) return fail(ctx, DP_ERR_ARG, "null config");
   if (cfg->precision != DP_PREC_FP64 && cfg->precision != DP_PREC_MIXED)
     return fail(ctx, DP_ERR_ARG, "precision must be DP_PREC_FP64 or DP_PREC_MIXED");
@@ -832,6 +725,73 @@ int check_cfg(dp_ctx* ctx, const dp_physics* ph, const dp_mc_config* cfg, Consts
   C->scattering = cfg->scattering != 0;
   return DP_OK;
 }
+
+int read_flag(dp_ctx* ctx) {
+  int flag = 0;
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  DP_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (flag) {
+    cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream);
+    return fail(ctx, DP_ERR_STATE,
+                flag == 2 ? "total_samples differs from the sum of n_samples"
+                          : "a table-staging wait exceeded its limit");
+  }
+  return DP_OK;
+}
+
+int status_code(dp_ctx* ctx, int bits) {
+  if (bits & (DP_ST_DOMAIN_HI | DP_ST_DOMAIN_LO | DP_ST_ZERO_RATE | DP_ST_BAD_WEIGHT))
+    return fail(ctx, DP_ERR_DOMAIN, "a history left the prepared tables or met an invalid hard event");
+  if (bits & (DP_ST_STEP_CAP | DP_ST_EVENT_CAP | DP_ST_TABLE_WAIT))
+    return fail(ctx, DP_ERR_STATE, "a history reached a loop cap");
+  if (bits & DP_ST_NO_PROGRESS)
+    return fail(ctx, DP_ERR_STATE, "MC segment made no spatial progress");
+  if (bits & DP_ST_BAD_MEDIUM)
+    return fail(ctx, DP_ERR_ARG, "segment medium outside the media set");
+  return DP_OK;
+}
+
+// Status bits of a finished run: the call's error code where the reference
+// would have thrown (host synchronises).
+int status_result(dp_ctx* ctx, const int* d_bits) {
+  int bits = 0;
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(&bits, d_bits, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  int rc = read_flag(ctx);
+  if (rc) return rc;
+  return status_code(ctx, bits);
+}
+int group_offsets(dp_ctx* ctx, const dp_los* los, const int64_t* given, long n, int64_t* off,
+                  int64_t* coff, long expect) {
+  los_offsets_kernel<<<1, 1024, 0, ctx->stream>>>(los, given, n, off, coff, expect, ctx->d_flag);
+  ++ctx->launches;
+  DP_CHECK_CUDA(ctx, cudaGetLastError());
+  return DP_OK;
+}
+
+long tally_jobs(long n, long total) { return n + total / kTallyChunk + 1; }
+size_t tally_part_bytes() { return sizeof(TallyPart); }
+
+int group_tally(dp_ctx* ctx, const double* contrib, const int32_t* status, const double* csda,
+                const double* dcsda, const dp_los* los, const int32_t* valid, long n, long total,
+                int sigma_n1, const int64_t* off, const int64_t* coff, void* part,
+                dp_los_result* out, int* bits) {
+  const long max_jobs = tally_jobs(n, total), warps_per_block = 8;
+  TallyPart* tp = static_cast<TallyPart*>(part);
+  timed_begin(ctx);
+  los_chunk_kernel<<<int((max_jobs + warps_per_block - 1) / warps_per_block), 256, 0, ctx->stream>>>(
+      contrib, status, off, coff, n, max_jobs, csda, dcsda, tp);
+  los_tally_kernel<<<int((n + warps_per_block - 1) / warps_per_block), 256, 0, ctx->stream>>>(
+      tp, off, coff, los, valid, n, csda ? 1 : 0, sigma_n1, out, bits);
+  ctx->launches += 2;
+  DP_CHECK_CUDA(ctx, cudaGetLastError());
+  timed_end(ctx, "mc_tally");
+  return DP_OK;
+}
+
+}  // namespace mc
+}  // namespace dp
+
+namespace {
 
 template <class R, int PHASE>
 int launch_phase(dp_ctx* ctx, McParams& P, size_t smem, long max_blocks) {
@@ -889,27 +849,6 @@ int run(dp_ctx* ctx, McParams& P, int precision) {
   return precision == DP_PREC_MIXED ? launch_mc<float>(ctx, P) : launch_mc<double>(ctx, P);
 }
 
-int read_flag(dp_ctx* ctx) {
-  int flag = 0;
-  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  DP_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  if (flag) {
-    cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream);
-    return fail(ctx, DP_ERR_STATE,
-                flag == 2 ? "total_samples differs from the sum of n_samples"
-                          : "a table-staging wait exceeded its limit");
-  }
-  return DP_OK;
-}
-
-int status_code(dp_ctx* ctx, int bits) {
-  if (bits & (DP_ST_DOMAIN_HI | DP_ST_DOMAIN_LO | DP_ST_ZERO_RATE | DP_ST_BAD_WEIGHT))
-    return fail(ctx, DP_ERR_DOMAIN, "a history left the prepared tables or met an invalid hard event");
-  if (bits & (DP_ST_STEP_CAP | DP_ST_EVENT_CAP | DP_ST_TABLE_WAIT))
-    return fail(ctx, DP_ERR_STATE, "a history reached a loop cap");
-  return DP_OK;
-}
-
 McParams base_params(dp_ctx* ctx, const unsigned char* blob, const Layout& lay, const dp_mixture* rock,
                      const dp_mixture* air, const Consts& C, uint64_t seed) {
   McParams P{};
@@ -929,18 +868,6 @@ int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_
                   const dp_mc_config* cfg, long n_los, const dp_los* d_los, long total,
                   dp_los_result* d_out, double** contrib_out, int** status_or,
                   int compute_gradient);
-
-namespace {
-// Status bits of a finished run: the call's error code where the reference
-// would have thrown (host synchronises).
-int status_result(dp_ctx* ctx, const int* d_bits) {
-  int bits = 0;
-  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(&bits, d_bits, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  int rc = read_flag(ctx);
-  if (rc) return rc;
-  return status_code(ctx, bits);
-}
-}  // namespace
 
 extern "C" {
 
@@ -1144,8 +1071,7 @@ int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_
   int32_t* ds = A.take<int32_t>(nt);
   int64_t* off = A.take<int64_t>(n_los + 1);
   int64_t* coff = A.take<int64_t>(n_los + 1);
-  const long max_jobs = n_los + nt / kTallyChunk + 1;
-  TallyPart* tpart = A.take<TallyPart>(max_jobs);
+  TallyPart* tpart = A.take<TallyPart>(tally_jobs(n_los, nt));
   unsigned long long* ctr = A.take<unsigned long long>(3);
   Handoff<double>* queue = A.take<Handoff<double>>(nt);
   StartRec<double>* srec = A.take<StartRec<double>>(nt);
@@ -1155,9 +1081,8 @@ int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_
   int* bits = A.take<int>(1);
   if (!bits) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
   DP_CHECK_CUDA(ctx, cudaMemsetAsync(bits, 0, sizeof(int), ctx->stream));
-  los_offsets_kernel<<<1, 1024, 0, ctx->stream>>>(d_los, n_los, off, coff, total, ctx->d_flag);
-  ++ctx->launches;
-  DP_CHECK_CUDA(ctx, cudaGetLastError());
+  rc = group_offsets(ctx, d_los, nullptr, n_los, off, coff, total);
+  if (rc) return rc;
   if (total > 0) {
     McParams P = base_params(ctx, blob, lay, rock, air, C, cfg->seed);
     P.source = 1;
@@ -1181,15 +1106,9 @@ int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_
       if (rc) return rc;
     }
   }
-  const long warps_per_block = 8;
-  timed_begin(ctx);
-  los_chunk_kernel<<<int((max_jobs + warps_per_block - 1) / warps_per_block), 256, 0, ctx->stream>>>(
-      dc, ds, off, coff, n_los, max_jobs, total > 0 ? cc : nullptr, cd, tpart);
-  los_tally_kernel<<<int((n_los + warps_per_block - 1) / warps_per_block), 256, 0, ctx->stream>>>(
-      tpart, off, coff, d_los, n_los, total > 0 && cc ? 1 : 0, d_out, bits);
-  ++ctx->launches;
-  DP_CHECK_CUDA(ctx, cudaGetLastError());
-  timed_end(ctx, "mc_tally");
+  rc = group_tally(ctx, dc, ds, total > 0 ? cc : nullptr, cd, d_los, nullptr, n_los, total, 0, off,
+                   coff, tpart, d_out, bits);
+  if (rc) return rc;
   if (contrib_out) *contrib_out = dc;
   if (status_or) *status_or = bits;
   return DP_OK;

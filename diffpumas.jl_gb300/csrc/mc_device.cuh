@@ -34,8 +34,10 @@ enum : int {
   ST_ZERO_RATE = DP_ST_ZERO_RATE,
   ST_BAD_WEIGHT = DP_ST_BAD_WEIGHT,
   ST_TABLE = DP_ST_TABLE_WAIT,
+  ST_NO_PROGRESS = DP_ST_NO_PROGRESS,
+  ST_BAD_MEDIUM = DP_ST_BAD_MEDIUM,
   ST_FATAL = ST_STEP_CAP | ST_EVENT_CAP | ST_DOMAIN_HI | ST_DOMAIN_LO | ST_ZERO_RATE |
-             ST_BAD_WEIGHT | ST_TABLE,
+             ST_BAD_WEIGHT | ST_TABLE | ST_NO_PROGRESS | ST_BAD_MEDIUM,
 };
 
 // Packed medium (one blob per medium and precision, the same layout for
@@ -156,7 +158,7 @@ struct Stream {
 };
 // One Philox block for the stream (kept out of line: every draw site would
 // otherwise carry the ten unrolled rounds).
-__device__ __noinline__ U4 philox_block(uint32_t c0, uint32_t c1, uint32_t block, uint32_t k0,
+static __device__ __noinline__ U4 philox_block(uint32_t c0, uint32_t c1, uint32_t block, uint32_t k0,
                                         uint32_t k1) {
   return philox(U4{c0, c1, block, 0u}, k0, k1);
 }
@@ -181,10 +183,14 @@ template <> __device__ __forceinline__ double uni<double>(Stream& g) {
   return u01(a, b);
 }
 // The leading 24 bits of the same draw (it differs from the double by < 2^-24).
+// FP32: the midpoints of 2^24 bins, in (0, 1).  A 24-bit uniform of exactly 0
+// (probability 2^-24, against 2^-53 in FP64) would place a hard event at zero
+// grammage: a step of no length, which the fixed-path loop rejects
+// (src/Tomography.jl:916), and -log(0) in the Gaussian draws.
 template <> __device__ __forceinline__ float uni<float>(Stream& g) {
   uint32_t a, b;
   g.next(a, b);
-  return float(a >> 8) * 0x1p-24f;
+  return (float(a >> 8) + 0.5f) * 0x1p-24f;
 }
 __device__ __forceinline__ double uni_d(Stream& g) {
   uint32_t a, b;
@@ -421,7 +427,7 @@ __device__ __forceinline__ R klookup(const Med<R>& m, int xcol, int ycol, R x, i
 
 // Sum over elements and processes of f * dsigma/dq (src/MixedTransport.jl:99-106)
 // by one thread in FP64 (the FP64 transport), in the reference's order.
-__device__ __noinline__ double del_total(const double* el, int nel, double mass, double anc,
+static __device__ __noinline__ double del_total(const double* el, int nel, double mass, double anc,
                                          double q) {
   double total = 0.0;
   for (int e = 0; e < nel; ++e) {
@@ -436,7 +442,7 @@ __device__ __noinline__ double del_total(const double* el, int nel, double mass,
 }
 // Index of the component whose running sum first exceeds u (the process and
 // element pick of src/MixedTransport.jl:131-140).
-__device__ __noinline__ int del_pick(const double* el, int nel, double mass, double anc, double q,
+static __device__ __noinline__ int del_pick(const double* el, int nel, double mass, double anc, double q,
                                      double u) {
   int last = 4 * nel - 1;
   for (int i = 0; i <= last; ++i) {
@@ -462,7 +468,7 @@ constexpr int kItemsPerElement = 23;
 // terms (per-mass scale N_A/(A 1e-3) against FP32 underflow), the components
 // are summed in a fixed order into comp[] (kept for the pick) and the total
 // is reduced in a fixed tree; all 32 lanes call it with the same arguments.
-__device__ __noinline__ double coop_total(const float* elf, int nel, float fm, double anc,
+static __device__ __noinline__ double coop_total(const float* elf, int nel, float fm, double anc,
                                           double q, float* item, float* comp) {
   const int lane = threadIdx.x & 31;
   const float fk = float(anc), fq = float(q);
@@ -524,7 +530,7 @@ struct DelOut {
 // true when the event needs that sum; *anc and *denom (pdf r sigma (1 - p_cel))
 // then describe it.  Otherwise *out is the result.
 template <class R>
-__device__ __noinline__ bool del_begin(const Med<R>& m, const Consts& C, double k, Stream& g, int* status,
+static __device__ __noinline__ bool del_begin(const Med<R>& m, const Consts& C, double k, Stream& g, int* status,
                           DelOut* out, double* anc_out, double* denom) {
   *out = DelOut{k, 1.0, 0, -1};
   double sigma = double(klookup(m, K_E, K_SIG, R(k), status));
@@ -563,7 +569,7 @@ __device__ __forceinline__ DelOut del_end(double anc, double denom, double total
 }
 // reverse_del_event in one thread, FP64 (src/MixedTransport.jl:111-142).
 template <class R>
-__device__ __noinline__ DelOut reverse_del(const Med<R>& m, const Consts& C, double k, Stream& g,
+static __device__ __noinline__ DelOut reverse_del(const Med<R>& m, const Consts& C, double k, Stream& g,
                                            bool details, int* status) {
   DelOut r;
   double anc, denom;
@@ -611,6 +617,7 @@ struct State {
 template <class R>
 struct Cont {
   R a, b, c, d, dist;  // dist: requested length of a mixed step
+  R moved;             // path length of the last completed straggled or mixed step
   R r0, r1, r2, r3;
   int event, kind, medium, flag;
   double anc, q, denom;  // the pending event: ancestor, energy transfer, weight denominator
@@ -625,7 +632,7 @@ enum : int { CONT_NONE = 0, CONT_MIXED = 1, CONT_STRAG = 2 };
 // eps(max(1, grammage)) in both precisions: an FP32 ulp would exceed the
 // grammage of the 1e-7 m boundary-crossing steps.
 template <class R>
-__device__ void mixed_end(State<R>& s, const Cont<R>& x, R Emax, R energy_limit, bool exhausted) {
+__device__ void mixed_end(State<R>& s, Cont<R>& x, R Emax, R energy_limit, bool exhausted) {
   if (exhausted) s.status |= ST_EVENT_CAP;
   if (x.r1 > R(0) && x.r0 >= Emax && x.a > x.d && (energy_limit < R(0) || x.r0 < energy_limit))
     s.status |= ST_DOMAIN_HI;
@@ -637,6 +644,7 @@ __device__ void mixed_end(State<R>& s, const Cont<R>& x, R Emax, R energy_limit,
   s.E = x.r0;
   s.w = x.r1;
   alt_add(s.z, -(d * s.uz));
+  x.moved = d;
 }
 // Applies a hard event; true when the history's weight vanished.
 template <class R>
@@ -648,7 +656,7 @@ __device__ __forceinline__ bool mixed_event(State<R>& s, Cont<R>& x, const DelOu
 }
 // Runs the event loop from x.event; returns true when it suspended on a DCS sum.
 template <class R, bool COOP>
-__device__ __noinline__ bool mixed_run(const Med<R>& m, const Consts& C, State<R>& s, Cont<R>& x, Stream& g,
+static __device__ __noinline__ bool mixed_run(const Med<R>& m, const Consts& C, State<R>& s, Cont<R>& x, Stream& g,
                           R energy_limit) {
   const int nk = m.nk;
   const R* kE = m.kcol(K_E);
@@ -741,7 +749,7 @@ __device__ __forceinline__ R truncated_randn(Stream& g) {
 
 // fluctuate_energy_loss, backward (src/Straggling.jl:103-173, :1046-1105).
 template <class R>
-__device__ __noinline__ R fluctuate(const Med<R>& m, R ki, const Loc<R>& Li, R dX, R Xtot, Stream& g,
+static __device__ __noinline__ R fluctuate(const Med<R>& m, R ki, const Loc<R>& Li, R dX, R Xtot, Stream& g,
                        R* ratio_out) {
   R k1 = inv_range(m, MC_MR, Xtot + dX);
   R dk0 = fabs(ki - k1), ratio = R(1);
@@ -778,7 +786,7 @@ __device__ __noinline__ R fluctuate(const Med<R>& m, R ki, const Loc<R>& Li, R d
 
 // sample_ehs_event, backward (src/Straggling.jl:373-434, :1284-1334).
 template <class R>
-__device__ __noinline__ bool ehs_event(const Med<R>& m, R ki, R kf, R dX, R Xtot, R ratio, Stream& g, R mass,
+static __device__ __noinline__ bool ehs_event(const Med<R>& m, R ki, R kf, R dX, R Xtot, R ratio, Stream& g, R mass,
                           R eratio, R* X_ehs, R* k_ehs) {
   R kmin = fmin(ki, kf), kmax = fmax(ki, kf);
   if (kmin < R(0.001)) {
@@ -806,7 +814,7 @@ __device__ __noinline__ bool ehs_event(const Med<R>& m, R ki, R kf, R dX, R Xtot
 
 // sample_scattering_angle (src/Straggling.jl:446-517, :1344-1405), FP64.
 template <class R>
-__device__ __noinline__ double scattering_angle(const Med<R>& m, double mass, double K,
+static __device__ __noinline__ double scattering_angle(const Med<R>& m, double mass, double K,
                                                 Stream& g) {
   Loc<R> L = locate(m, R(K));
   double p2 = K * (K + 2.0 * mass);
@@ -846,7 +854,7 @@ __device__ __noinline__ double scattering_angle(const Med<R>& m, double mass, do
 // FP32 form of scattering_angle for the mixed-precision transport.  The CM
 // kinetic energy uses the exact identity s - (m + M)^2 = 2 K M instead of the
 // difference (which cancels in FP32 at low energy).
-__device__ __noinline__ float scattering_angle_f(const Med<float>& m, float mass, float K,
+static __device__ __noinline__ float scattering_angle_f(const Med<float>& m, float mass, float K,
                                                  Stream& g) {
   Loc<float> L = locate(m, K);
   float p2 = K * (K + 2.f * mass);
@@ -885,7 +893,7 @@ __device__ __noinline__ float scattering_angle_f(const Med<float>& m, float mass
 
 // sample_soft_scattering (src/Straggling.jl:539-590, :1204-1253).
 template <class R>
-__device__ __noinline__ R soft_scattering(const Med<R>& m, const Loc<R>& L0, R k1, R step, R density,
+static __device__ __noinline__ R soft_scattering(const Med<R>& m, const Loc<R>& L0, R k1, R step, R density,
                              Stream& g) {
   if (step <= R(0) || density <= R(0)) return R(0);
   R lb0 = transport_path(m, L0);
@@ -911,7 +919,7 @@ __device__ __noinline__ R soft_scattering(const Med<R>& m, const Loc<R>& L0, R k
 
 // rotate_direction (src/Straggling.jl:645-710).
 template <class R>
-__device__ __noinline__ void rotate(State<R>& s, R mu, Stream& g) {
+static __device__ __noinline__ void rotate(State<R>& s, R mu, Stream& g) {
   R ct = R(1) - R(2) * mu, st2 = R(4) * mu * (R(1) - mu);
   if (st2 <= R(0)) return;
   R st = sqrt(st2), d0 = s.ux, d1 = s.uy, d2 = s.uz;
@@ -956,7 +964,7 @@ __device__ __noinline__ void rotate(State<R>& s, R mu, Stream& g) {
 }
 
 // DEL polar angles, FP64 (src/Straggling.jl:746-914).
-__device__ __noinline__ double polar_brems(double m, double ki, double kf, double RN, Stream& g) {
+static __device__ __noinline__ double polar_brems(double m, double ki, double kf, double RN, Stream& g) {
   double E = ki + m, nu = ki - kf;
   if (nu <= 0.0 || E <= m) return 0.0;
   double y = nu / E, tmp = 0.5 * m * nu / (E * (E - nu)), mu0 = tmp * tmp;
@@ -983,7 +991,7 @@ __device__ __noinline__ double polar_brems(double m, double ki, double kf, doubl
   }
   return 0.0;
 }
-__device__ __noinline__ double polar_photo(double ml, double ki, double kf, Stream& g) {
+static __device__ __noinline__ double polar_photo(double ml, double ki, double kf, Stream& g) {
   double M = 0.5 * (kProtonMass + kNeutronMass), q = ki - kf, E = ki + ml, ml2 = ml * ml;
   double Q2min = ml2 * (q * q - 0.5 * ml2) / (E * (E - q));
   double Q2max = 2.0 * M * (q - kPionMass) - kPionMass * kPionMass;
@@ -1009,7 +1017,7 @@ __device__ __forceinline__ double polar_ioni(double m, double ki, double kf) {
 // transport_backward_step_full, mode :straggled (src/Geometry.jl:148-357):
 // straggled_end completes a step from its energy-loss and event decisions.
 template <class R>
-__device__ __noinline__ void straggled_end(const Med<R>& m, const Consts& C, State<R>& s, const Loc<R>& Li,
+static __device__ __noinline__ R straggled_end(const Med<R>& m, const Consts& C, State<R>& s, const Loc<R>& Li,
                               R ki, R kf, R ckf, R dX, double dw, int proc, int elem, bool del,
                               bool ehs, R k_ehs, R density, R step, bool shortened,
                               bool scattering, Stream& g) {
@@ -1044,6 +1052,7 @@ __device__ __noinline__ void straggled_end(const Med<R>& m, const Consts& C, Sta
   if (sizeof(R) == 4) s.w = s.w * wf * exp(-pt / C.ctau_r<R>()) * R(dw);
   else s.w = R(double(s.w * wf * exp(-pt / C.ctau_r<R>())) * dw);
   s.E = kf;
+  return da;
 }
 
 // The step up to its hard-event decision; true when it suspended on the
@@ -1133,8 +1142,8 @@ __device__ bool straggled_step(const Med<R>& m, const Consts& C, State<R>& s, co
     dX = X_ehs;
     shortened = true;
   }
-  straggled_end(m, C, s, Li, ki, kf, ckf, dX, dw, proc, elem, del, ehs, k_ehs, density, step,
-                shortened, scattering, g);
+  x.moved = straggled_end(m, C, s, Li, ki, kf, ckf, dX, dw, proc, elem, del, ehs, k_ehs, density,
+                          step, shortened, scattering, g);
   return false;
 }
 
@@ -1327,7 +1336,7 @@ __device__ int resume(const Med<R>& rock, const Med<R>& air, const Consts& C, Hi
     }
   } else {
     Loc<R> Li = locate(m, x.r0);
-    straggled_end(m, C, h.s, Li, x.r0, R(d.energy), x.r1, x.r2, d.weight, d.process, d.element,
+    x.moved = straggled_end(m, C, h.s, Li, x.r0, R(d.energy), x.r1, x.r2, d.weight, d.process, d.element,
                   true, false, R(0), x.r3, x.a, true, x.flag != 0, g);
   }
   return step_done(h);

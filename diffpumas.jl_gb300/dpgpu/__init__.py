@@ -289,6 +289,8 @@ class MaterialMixture:
         mats = np.ascontiguousarray(np.atleast_1d(materials).astype(np.int32) - 1)
         fr = _f64(np.ones(len(mats)) if fractions is None else np.atleast_1d(fractions))
         self.physics = physics
+        self.materials = [int(m) + 1 for m in mats]
+        self.fractions = [float(f) / float(fr.sum()) for f in fr] if fr.sum() > 0 else list(fr)
         self.h = C.c_void_p()
         check(load().dp_mixture_prepare(physics.ctx.h, physics.h, len(mats), _ptr(mats), _ptr(fr),
                                         C.byref(self.h)), physics.ctx.h)
@@ -392,6 +394,13 @@ def backward_mc_batch(physics, los, *, rock, air, seed=42, straggling=True, scat
     keys = ("flux", "sigma", "n_samples", "n_status_nonzero") + \
         (("gradient", "gradient_flux") if compute_gradient else ())
     return {k: np.array([getattr(r, k) for r in out]) for k in keys}
+
+
+from .directional import (CellSegment, DirBatch, DirectionalPath, DirMedia,  # noqa: E402
+                          EnergySample,
+                          MaterialConfig, SiteConfig, build_cell_properties_for_mc,
+                          compute_directional_flux_mc, directional_flux_mc_batch,
+                          mc_cell_mixture_and_density, sample_energy_set)
 
 
 # ----------------------------------------------------------------- tomography

@@ -67,6 +67,16 @@ class DpLosResult(C.Structure):
                 ("n_status_nonzero", C.c_long)]
 
 
+class DpDirBatch(C.Structure):
+    _fields_ = [("n_dirs", C.c_long), ("cos_theta", C.c_void_p), ("remaining_rock", C.c_void_p),
+                ("air_distance", C.c_void_p), ("valid", C.c_void_p), ("seg_ptr", C.c_void_p),
+                ("seg_medium", C.c_void_p), ("seg_density", C.c_void_p),
+                ("seg_length", C.c_void_p), ("sample_ptr", C.c_void_p), ("energy", C.c_void_p),
+                ("charge", C.c_void_p), ("weight", C.c_void_p), ("energy_min", C.c_double),
+                ("energy_max", C.c_double), ("rock_medium", C.c_int), ("air_medium", C.c_int),
+                ("rock_density", C.c_double), ("detector_elevation", C.c_double)]
+
+
 class DpSolveParams(C.Structure):
     _fields_ = [("method", C.c_int), ("n_iter", C.c_int), ("cg_iter", C.c_int),
                 ("precision", C.c_int), ("relaxation", C.c_double), ("lm_damping", C.c_double),
@@ -130,6 +140,11 @@ PROTOTYPES = {
                              _VP, _VP, _I, C.c_uint64, _VP, _VP, _VP, _VP]),
     "dp_mc_los": (_I, [_P, _P, _P, _P, C.POINTER(DpMcConfig), _L, _VP, _I, _VP]),
     "dp_mc_los_dev": (_I, [_P, _P, _P, _P, C.POINTER(DpMcConfig), _L, _VP, _L, _I, _VP]),
+    "dp_dir_media_create": (_I, [_P, _P, _I, C.POINTER(_P), C.POINTER(_P)]),
+    "dp_dir_media_free": (_I, [_P]),
+    "dp_dir_mc": (_I, [_P, _P, _P, C.POINTER(DpDirBatch), C.POINTER(DpMcConfig), _VP, _VP, _VP,
+                       _VP]),
+    "dp_dir_mc_dev": (_I, [_P, _P, _P, C.POINTER(DpDirBatch), _L, C.POINTER(DpMcConfig), _VP]),
     "dp_tomo_forward": (_I, [_P, _P, C.POINTER(DpGrid), C.POINTER(DpTomoParams), _VP, _L, _VP,
                              _VP]),
     "dp_tomo_jacobian": (_I, [_P, _P, C.POINTER(DpGrid), C.POINTER(DpTomoParams), _VP, _L, _VP,

@@ -1,0 +1,257 @@
+"""Fixed-path stochastic MC of src/Tomography.jl (compute_directional_flux_mc,
+:826-1041) on libdpgpu: the reference's types and helpers for one direction,
+and a batched form that runs many directions in one launch."""
+import ctypes as C
+import math
+from collections import namedtuple
+
+import numpy as np
+
+from ._lib import DpDirBatch, DpLosResult, check, load
+
+# src/Tomography.jl:179-223 (material indices are 1-based like the reference's)
+MaterialConfig = namedtuple("MaterialConfig", "rock_material water_material air_material "
+                            "porous_material rock_density water_density porous_density "
+                            "porous_top_thickness")
+SiteConfig = namedtuple("SiteConfig", "detector_elevation primary_altitude")
+EnergySample = namedtuple("EnergySample", "energy charge weight")
+CellSegment = namedtuple("CellSegment", "cell_idx distance")
+DirectionalPath = namedtuple("DirectionalPath", "zenith azimuth segments distance_in_volume "
+                             "surface_distance remaining_rock_distance surface_exit_z valid")
+
+
+def is_shallow_porous(shallow, matcfg):
+    """src/Tomography.jl:299-301."""
+    return bool(shallow) and matcfg.porous_material > 0 and matcfg.porous_top_thickness > 0.0
+
+
+def mc_cell_mixture_and_density(w, shallow, matcfg):
+    """Mixture recipe ((materials, fractions)) and density of a cell with water
+    mass fraction w (src/Tomography.jl:826-845): specific volumes add."""
+    w = float(w)
+    if is_shallow_porous(shallow, matcfg):
+        porous = rock = 0.5 * (1.0 - w)
+        recipe = ((matcfg.porous_material, matcfg.rock_material, matcfg.water_material),
+                  (porous, rock, w))
+        density = 1.0 / (porous / matcfg.porous_density + rock / matcfg.rock_density +
+                         w / matcfg.water_density)
+        return recipe, density
+    if w <= 1e-12:
+        return ((matcfg.rock_material,), (1.0,)), float(matcfg.rock_density)
+    recipe = ((matcfg.rock_material, matcfg.water_material), (1.0 - w, w))
+    return recipe, 1.0 / ((1.0 - w) / matcfg.rock_density + w / matcfg.water_density)
+
+
+def build_cell_properties_for_mc(physics, shallow_flags, water_fractions, matcfg):
+    """Per-cell prepared mixtures and densities (src/Tomography.jl:847-861);
+    cells with the same (shallow, w) share one MaterialMixture."""
+    from . import MaterialMixture
+    cache = {}
+    materials, densities = [], np.zeros(len(water_fractions))
+    for i, (s, w) in enumerate(zip(shallow_flags, water_fractions)):
+        key = (bool(s), float(w))
+        if key not in cache:
+            (mats, fr), rho = mc_cell_mixture_and_density(w, s, matcfg)
+            cache[key] = (MaterialMixture(physics, list(mats), list(fr)), rho)
+        materials.append(cache[key][0])
+        densities[i] = cache[key][1]
+    return materials, densities
+
+
+def sample_energy_set(n_samples, energy_min, energy_max, seed):
+    """Log-uniform final energies with weight k ln(E_max/E_min) and charges +-1
+    (src/Tomography.jl:236-248, src/Pumas.jl:195-207).  The draws come from
+    numpy's seeded generator, not Julia's MersenneTwister."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(int(n_samples)):
+        if energy_max <= energy_min:
+            kf, w = float(energy_min), 1.0
+        else:
+            rk = math.log(energy_max / energy_min)
+            kf = energy_min * math.exp(rk * rng.random())
+            w = kf * rk
+        out.append(EnergySample(kf, 1.0 if rng.random() > 0.5 else -1.0, w))
+    return out
+
+
+class DirMedia:
+    """A media set of fixed-path runs (dp_dir_media): the prepared media in the
+    order given (the kernel stages the leading ones in shared memory)."""
+
+    def __init__(self, physics, media):
+        self.physics, self.media = physics, list(media)
+        arr = (C.c_void_p * len(self.media))(*[m.h.value for m in self.media])
+        self.h = C.c_void_p()
+        check(load().dp_dir_media_create(physics.ctx.h, physics.h, len(self.media), arr,
+                                         C.byref(self.h)), physics.ctx.h)
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                load().dp_dir_media_free(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+class DirBatch:
+    """A batch of directions prepared for dp_dir_mc: the paths' segment
+    arrays, the media set (the rock first, the cell mixtures by use, the air
+    last; the kernel stages the leading media in shared memory) and the
+    samples (explicit EnergySample lists, or counts drawn on the device).
+    run() passes host arrays; to_device() + run_dev() keep them resident."""
+
+    def __init__(self, physics, matcfg, site, paths, cell_materials, cell_densities,
+                 energy_samples=None, *, n_samples=None, energy_min=None, energy_max=None):
+        from . import MaterialMixture
+        self.physics = physics
+        n = self.n_dirs = len(paths)
+        cos_t = np.array([math.cos(math.radians(p.zenith)) for p in paths])
+        valid = np.array([1 if (p.valid and c > 0.0) else 0 for p, c in zip(paths, cos_t)],
+                         np.int32)
+        if energy_samples is None:
+            n_smp = np.broadcast_to(np.asarray(n_samples, np.int64), (n,)).copy()
+        else:
+            n_smp = np.array([len(s) for s in energy_samples], np.int64)
+        seg_ptr = np.zeros(n + 1, np.int64)
+        cells, lens = [], []
+        for d, p in enumerate(paths):
+            segs = p.segments if valid[d] else []
+            seg_ptr[d + 1] = seg_ptr[d] + len(segs)
+            cells.extend(int(s.cell_idx) - 1 for s in segs)
+            lens.extend(float(s.distance) for s in segs)
+        cells = np.array(cells, np.int64)
+        use = {}
+        for d in range(n):
+            for c in cells[seg_ptr[d]:seg_ptr[d + 1]]:
+                m = cell_materials[c]
+                use[id(m)] = (m, use.get(id(m), (m, 0))[1] + int(n_smp[d]))
+        rock = MaterialMixture(physics, matcfg.rock_material)
+        air = MaterialMixture(physics, matcfg.air_material)
+        self.media = [rock] + [m for m, _ in sorted(use.values(), key=lambda t: -t[1])] + [air]
+        index = {id(m): k for k, m in enumerate(self.media)}
+        self.arrays = {
+            "cos_theta": cos_t,
+            "remaining_rock": np.array([p.remaining_rock_distance for p in paths], np.float64),
+            "air_distance": np.array([max(0.0, site.primary_altitude - p.surface_exit_z) /
+                                      max(c, 1e-3) for p, c in zip(paths, cos_t)]),
+            "valid": valid, "seg_ptr": seg_ptr,
+            "seg_medium": np.array([index[id(cell_materials[c])] for c in cells], np.int32),
+            "seg_density": np.array([cell_densities[c] for c in cells], np.float64),
+            "seg_length": np.array(lens, np.float64),
+            "sample_ptr": np.concatenate([[0], np.cumsum(n_smp)]).astype(np.int64)}
+        if energy_samples is not None:
+            flat = [s for ss in energy_samples for s in ss]
+            for k, j in (("energy", 0), ("charge", 1), ("weight", 2)):
+                self.arrays[k] = np.array([s[j] for s in flat], np.float64)
+        self.energy_min = float(energy_min) if energy_min is not None else 0.0
+        self.energy_max = float(energy_max) if energy_max is not None else 0.0
+        self.total = int(self.arrays["sample_ptr"][-1])
+        self.rock_density = float(matcfg.rock_density)
+        self.detector_elevation = float(site.detector_elevation)
+        self.set = DirMedia(physics, self.media)
+        self.dev = None
+
+    def _struct(self, ptr):
+        B = DpDirBatch()
+        B.n_dirs = self.n_dirs
+        for k in ("cos_theta", "remaining_rock", "air_distance", "valid", "seg_ptr", "seg_medium",
+                  "seg_density", "seg_length", "sample_ptr", "energy", "charge", "weight"):
+            setattr(B, k, ptr(k))
+        B.energy_min, B.energy_max = self.energy_min, self.energy_max
+        B.rock_medium, B.air_medium = 0, len(self.media) - 1
+        B.rock_density, B.detector_elevation = self.rock_density, self.detector_elevation
+        return B
+
+    def host_bytes(self):
+        """Bytes of the batch arrays a host call copies to the device."""
+        return sum(a.nbytes for a in self.arrays.values())
+
+    def run(self, seed=42, *, straggling=True, energy_threshold_low=100.0, precision="mixed",
+            return_histories=False):
+        from . import _mc_config, _ptr
+        B = self._struct(lambda k: self.arrays[k].ctypes.data if k in self.arrays else None)
+        out = (DpLosResult * self.n_dirs)()
+        n = max(self.total, 1)
+        contrib, status, final = np.zeros(n), np.zeros(n, np.int32), np.zeros((n, 2))
+        cfg = _mc_config(seed, straggling, False, energy_threshold_low, None, precision)
+        ctx = self.physics.ctx.h
+        h = return_histories
+        rc = load().dp_dir_mc(ctx, self.physics.h, self.set.h, C.byref(B), C.byref(cfg),
+                              C.cast(out, C.c_void_p), _ptr(contrib) if h else None,
+                              _ptr(status) if h else None, _ptr(final) if h else None)
+        res = {k: np.array([getattr(r, k) for r in out])
+               for k in ("flux", "sigma", "n_samples", "n_status_nonzero")}
+        if h:
+            res["contrib"], res["status"] = contrib[:self.total], status[:self.total]
+            res["final"] = final[:self.total]
+        try:
+            check(rc, ctx)
+        except Exception as e:
+            e.result = res  # the per-history records of a run that flagged histories
+            raise
+        return res
+
+    def to_device(self):
+        """Copies the batch arrays to torch device tensors (kept on self.dev)."""
+        import torch
+        dev = torch.device("cuda", self.physics.ctx.device)
+        self.dev = {k: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+                    for k, a in self.arrays.items()}
+        self.dev_out = torch.zeros(self.n_dirs * C.sizeof(DpLosResult), dtype=torch.uint8,
+                                   device=dev)
+        return self
+
+    def run_dev(self, seed=42, *, straggling=True, energy_threshold_low=100.0,
+                precision="mixed"):
+        """Enqueues one run on the resident arrays; results stay in dev_out."""
+        from . import _mc_config
+        B = self._struct(lambda k: self.dev[k].data_ptr() if k in self.dev else None)
+        cfg = _mc_config(seed, straggling, False, energy_threshold_low, None, precision)
+        ctx = self.physics.ctx.h
+        check(load().dp_dir_mc_dev(ctx, self.physics.h, self.set.h, C.byref(B), self.total,
+                                   C.byref(cfg), self.dev_out.data_ptr()), ctx)
+
+    def results_dev(self):
+        raw = bytearray(self.dev_out.cpu().numpy().tobytes())
+        out = (DpLosResult * self.n_dirs).from_buffer(raw)
+        return {k: np.array([getattr(r, k) for r in out])
+                for k in ("flux", "sigma", "n_samples", "n_status_nonzero")}
+
+
+def directional_flux_mc_batch(physics, matcfg, site, paths, cell_materials, cell_densities,
+                              energy_samples=None, seed=42, *, straggling=True,
+                              energy_threshold_low=100.0, scattering=False, precision="mixed",
+                              n_samples=None, energy_min=None, energy_max=None,
+                              return_histories=False):
+    """compute_directional_flux_mc over many directions in one launch.
+
+    energy_samples: one list of EnergySample per path, or None to draw
+    n_samples per path (an int or one per path) on the device from
+    [energy_min, energy_max] (sample_energy_set semantics).  Returns flux,
+    sigma (NaN for invalid paths), n_samples and n_status_nonzero per path;
+    with return_histories also the per-sample 2 w_i w flux_i and status."""
+    if scattering:
+        raise ValueError("Fixed RayPath MC supports energy-loss fluctuations only; "
+                         "use Geometry for scattered boundary retracing")
+    b = DirBatch(physics, matcfg, site, paths, cell_materials, cell_densities, energy_samples,
+                 n_samples=n_samples, energy_min=energy_min, energy_max=energy_max)
+    return b.run(seed, straggling=straggling, energy_threshold_low=energy_threshold_low,
+                 precision=precision, return_histories=return_histories)
+
+
+def compute_directional_flux_mc(physics, matcfg, site, path, cell_materials, cell_densities,
+                                energy_samples, seed, *, straggling, energy_threshold_low,
+                                scattering=False, precision="fp64"):
+    """(flux, sigma) of one direction (src/Tomography.jl:979-1041)."""
+    if scattering:
+        raise ValueError("Fixed RayPath MC supports energy-loss fluctuations only; "
+                         "use Geometry for scattered boundary retracing")
+    if not all(s.charge in (-1.0, 1.0) for s in energy_samples):
+        raise ValueError("MC requires physical charges ±1; CSDA quadrature nodes are not MC "
+                         "samples")
+    r = directional_flux_mc_batch(physics, matcfg, site, [path], cell_materials, cell_densities,
+                                  [list(energy_samples)], seed, straggling=straggling,
+                                  energy_threshold_low=energy_threshold_low, precision=precision)
+    return float(r["flux"][0]), float(r["sigma"][0])

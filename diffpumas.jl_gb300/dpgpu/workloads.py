@@ -73,3 +73,56 @@ def tomography_config(nx=64, ny=64, nz=32, pitch=10.0, n_detectors=4, rays_per_d
     rays = detector_rays(dets, rays_per_detector, 60.0, seed=seed + 1)
     nodes = csda_energy_quadrature(n_nodes, 1.0, 1e6)
     return grid, rho, rays, nodes
+
+
+def voxel_walk(nx, ny, nz, origin, pitch, start, direction):
+    """Cells (1-based, x fastest) and lengths of a ray from `start` through a
+    voxel grid (exact cell-boundary walk), and the distance to the grid exit."""
+    o = np.asarray(origin, float)
+    p = np.asarray(start, float)
+    u = np.asarray(direction, float)
+    n = np.array([nx, ny, nz])
+    # entry: the start is on or inside the grid
+    cell = np.clip(np.floor((p - o) / pitch).astype(int), 0, n - 1)
+    step = np.where(u > 0, 1, -1)
+    with np.errstate(divide="ignore"):
+        nxt = o + (cell + (u > 0)) * pitch
+        t_max = np.where(u != 0, (nxt - p) / u, np.inf)
+        t_delta = np.where(u != 0, pitch / np.abs(u), np.inf)
+    t, segs = 0.0, []
+    while True:
+        a = int(np.argmin(t_max))
+        t_next = float(t_max[a])
+        if t_next > t:
+            segs.append((int(cell[0] + nx * (cell[1] + ny * cell[2])) + 1, t_next - t))
+        t = t_next
+        cell[a] += step[a]
+        if cell[a] < 0 or cell[a] >= n[a]:
+            return segs, t
+        t_max[a] += t_delta[a]
+
+
+def directional_config(n_dirs=4096, nx=32, ny=32, nz=16, pitch=20.0, surface=600.0,
+                       zenith_max=75.0, water_fraction=0.3, seed=2026):
+    """Fixed-path MC directions in the manner of the reference's directional
+    runs: a detector at the centre of the bottom face of a 640 m x 640 m x
+    320 m voxel volume, directions uniform in zenith [0, zenith_max] and
+    azimuth, cells of pure rock or of rock with the given water mass fraction
+    (half each, seeded), rock beyond the volume up to a flat surface `surface`
+    m above the detector.  Returns (paths as (zenith, azimuth, segments,
+    in-volume distance, slant distance to the surface, remaining rock,
+    surface exit z)), per-cell water fractions."""
+    rng = np.random.default_rng(seed)
+    origin = (-nx * pitch / 2, -ny * pitch / 2, 0.0)
+    zen = np.degrees(np.arccos(rng.uniform(np.cos(np.radians(zenith_max)), 1.0, n_dirs)))
+    az = rng.uniform(0.0, 360.0, n_dirs)
+    out = []
+    for z, a in zip(zen, az):
+        th, ph = np.radians(z), np.radians(a)
+        u = (np.sin(th) * np.sin(ph), np.sin(th) * np.cos(ph), np.cos(th))
+        segs, t_exit = voxel_walk(nx, ny, nz, origin, pitch, (0.0, 0.0, 0.0), u)
+        z_exit = t_exit * u[2]
+        slant = surface / u[2]
+        out.append((float(z), float(a), segs, t_exit, slant, max(0.0, slant - t_exit), surface))
+    wf = np.where(rng.random(nx * ny * nz) < 0.5, water_fraction, 0.0)
+    return out, wf

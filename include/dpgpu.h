@@ -43,9 +43,13 @@ extern "C" {
  *   DP_ST_ZERO_RATE   non-positive hard-event rate (src/MixedTransport.jl:113)
  *   DP_ST_BAD_WEIGHT  invalid adjoint hard-event weight (src/MixedTransport.jl:186)
  *   DP_ST_TABLE_WAIT  a table-staging wait gave up (no reference counterpart)
+ *   DP_ST_NO_PROGRESS a fixed-path step made no spatial progress
+ *                     (src/Tomography.jl:916,965)
+ *   DP_ST_BAD_MEDIUM  a fixed-path segment names a medium outside the media
+ *                     set (device-array calls; host calls reject it up front)
  * A history with any bit but DP_ST_OUTER_CAP contributes zero flux; the call
  * then returns DP_ERR_DOMAIN (domain, rate, weight bits) or DP_ERR_STATE
- * (caps), where the reference would throw. */
+ * (caps, no progress), where the reference would throw. */
 #define DP_ST_OK 0
 #define DP_ST_STEP_CAP 1
 #define DP_ST_OUTER_CAP 2
@@ -55,6 +59,8 @@ extern "C" {
 #define DP_ST_ZERO_RATE 32
 #define DP_ST_BAD_WEIGHT 64
 #define DP_ST_TABLE_WAIT 128
+#define DP_ST_NO_PROGRESS 256
+#define DP_ST_BAD_MEDIUM 512
 
 typedef struct dp_ctx dp_ctx;
 typedef struct dp_physics dp_physics;
@@ -296,6 +302,59 @@ int dp_mc_los(dp_ctx* ctx, const dp_physics* phys, const dp_mixture* rock, const
 int dp_mc_los_dev(dp_ctx* ctx, const dp_physics* phys, const dp_mixture* rock,
                   const dp_mixture* air, const dp_mc_config* cfg, long n_los, const dp_los* los,
                   long total_samples, int compute_gradient, dp_los_result* out);
+
+/* ---------------------------------------------------------- fixed-path MC
+ * compute_directional_flux_mc (src/Tomography.jl:979-1041) over many
+ * directions at once.  A media set lists the distinct prepared media the
+ * paths use (cell mixtures from mc_cell_mixture_and_density,
+ * src/Tomography.jl:826-845, the rock beyond the cells and the air); the
+ * kernel copies the leading media to shared memory when they fit, so list
+ * the most used first.  Replaces the per-call kernel preparation of
+ * src/Tomography.jl:995-1003. */
+typedef struct dp_dir_media dp_dir_media;
+int dp_dir_media_create(dp_ctx* ctx, const dp_physics* phys, int n_media,
+                        const dp_mixture* const* media, dp_dir_media** out);
+int dp_dir_media_free(dp_dir_media* media);
+
+/* One batch of directions (DirectionalPath, src/Tomography.jl:214-223). */
+typedef struct {
+  long n_dirs;
+  const double* cos_theta;       /* cosd(zenith) per direction */
+  const double* remaining_rock;  /* remaining_rock_distance (m) per direction */
+  const double* air_distance;    /* metres of air: max(0, primary_altitude - surface_exit_z)
+                                    / max(cos_theta, 1e-3) (src/Tomography.jl:1020) */
+  const int32_t* valid;          /* NULL: all valid; 0: flux and sigma NaN */
+  const int64_t* seg_ptr;        /* n_dirs + 1 running segment offsets (< 2^31 segments) */
+  const int32_t* seg_medium;     /* media-set index per segment (the cell's mixture) */
+  const double* seg_density;     /* kg/m^3 per segment (the cell's density) */
+  const double* seg_length;      /* m per segment (CellSegment.distance) */
+  const int64_t* sample_ptr;     /* n_dirs + 1 running sample offsets */
+  const double* energy;          /* final energy (GeV) per sample; NULL: drawn per history */
+  const double* charge;          /* +-1 per sample */
+  const double* weight;          /* EnergySample.weight per sample */
+  double energy_min, energy_max; /* draw range when energy == NULL (sample_energy_set,
+                                    src/Tomography.jl:236-248, on Philox block 0) */
+  int rock_medium, air_medium;   /* media-set indices of the rock beyond the cells, the air */
+  double rock_density;           /* MaterialConfig.rock_density (kg/m^3) */
+  double detector_elevation;     /* SiteConfig.detector_elevation (m): air density altitude */
+} dp_dir_batch;
+
+/* Flux and sigma (n - 1 form, src/Tomography.jl:1036-1039) per direction into
+ * out[n_dirs] (gradient fields 0).  cfg: straggling, energy_threshold_low,
+ * seed, precision; scattering must be 0 (the reference's ArgumentError);
+ * source_energy_max 0 selects min(1e9, last table energy), the reference's
+ * energy limit.  History i of the batch draws from Philox stream (seed, i).
+ * contrib and status (optional, one per sample) receive 2 w_i w flux_i and
+ * the DP_ST_* bits, final_state (optional, two per sample) the final energy
+ * and transport weight. */
+int dp_dir_mc(dp_ctx* ctx, const dp_physics* phys, dp_dir_media* media, const dp_dir_batch* batch,
+              const dp_mc_config* cfg, dp_los_result* out, double* contrib, int32_t* status,
+              double* final_state);
+/* The same with every batch array and out in device memory (the struct
+ * itself on the host); total_samples = sample_ptr[n_dirs]. */
+int dp_dir_mc_dev(dp_ctx* ctx, const dp_physics* phys, dp_dir_media* media,
+                  const dp_dir_batch* batch, long total_samples, const dp_mc_config* cfg,
+                  dp_los_result* out);
 
 /* ------------------------------------------------------------------ tomography
  * Voxel-density CSDA forward model (examples/diff_flux_cube.jl:304-557):

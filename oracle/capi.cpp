@@ -314,6 +314,118 @@ void orc_mc_histories(void* h, int n_rock, const int* rock_mats, const double* r
   }
 }
 
+// Fixed-path MC histories of n_dirs directions (src/Tomography.jl:979-1041).
+// Media: n_media mixtures of up to 4 materials (med_mats/med_fracs, 4 per
+// medium, med_nm used); segments of direction d are seg_ptr[d]..seg_ptr[d+1]
+// (medium index, density, length); samples of direction d are
+// smp_ptr[d]..smp_ptr[d+1]; history i uses the Philox stream id0 + i.
+// contrib[i] = 2 w_i w flux_gccly, as the reference accumulates it.
+void orc_dir_histories(void* h, int n_media, const int* med_nm, const int* med_mats,
+                       const double* med_fracs, int rock, double rock_density, int air,
+                       double detector_elevation, long n_dirs, const double* cos_theta,
+                       const double* remaining_rock, const double* air_distance,
+                       const int64_t* seg_ptr, const int* seg_medium, const double* seg_density,
+                       const double* seg_length, const int64_t* smp_ptr, const double* E,
+                       const double* q, const double* w, uint64_t seed, uint64_t id0,
+                       int straggling, double threshold_low, double energy_limit,
+                       double* contrib, int* status, long* steps, double* Efinal, int nthreads) {
+  Physics* p = static_cast<Physics*>(h);
+  DirMedia md;
+  for (int k = 0; k < n_media; ++k) {
+    Mixture mx;
+    double tot = 0;
+    for (int j = 0; j < med_nm[k]; ++j) tot += med_fracs[4 * k + j];
+    for (int j = 0; j < med_nm[k]; ++j) {  // MaterialMixture normalises (src/Types.jl:363-368)
+      mx.mats.push_back(med_mats[4 * k + j]);
+      mx.fracs.push_back(med_fracs[4 * k + j] / tot);
+    }
+    md.med.push_back(make_medium(*p, mx));
+    md.kern.push_back(prepare_mixed_kernel(*p, mx));
+  }
+  md.rock = rock;
+  md.air = air;
+  md.rock_density = rock_density;
+  md.detector_elevation = detector_elevation;
+  McOptions o;
+  o.straggling = straggling != 0;
+  o.scattering = false;
+  o.energy_threshold_low = threshold_low;
+  o.source_energy_max = energy_limit;
+  const long n = long(smp_ptr[n_dirs]);
+#pragma omp parallel for schedule(dynamic, 8) num_threads(nthreads)
+  for (long i = 0; i < n; ++i) {
+    long d = long(std::upper_bound(smp_ptr, smp_ptr + n_dirs + 1, int64_t(i)) - smp_ptr) - 1;
+    DirPath path;
+    path.cos_theta = cos_theta[d];
+    path.medium = seg_medium + seg_ptr[d];
+    path.density = seg_density + seg_ptr[d];
+    path.length = seg_length + seg_ptr[d];
+    path.n_seg = long(seg_ptr[d + 1] - seg_ptr[d]);
+    path.remaining_rock = remaining_rock[d];
+    path.air_distance = air_distance[d];
+    Rng g;
+    g.seed = seed;
+    g.id = id0 + uint64_t(i);
+    McState fs;
+    double f = directional_history(*p, md, path, E[i], q[i], g, o, &fs);
+    contrib[i] = 2.0 * w[i] * f;
+    if (status) status[i] = fs.status;
+    if (steps) steps[i] = fs.steps;
+    if (Efinal) Efinal[i] = fs.E;
+  }
+}
+
+double orc_mc_segment_step(double remaining, double max_step) {
+  return mc_segment_step(remaining, max_step);
+}
+
+// propagate_mc_uniform_segment of one medium (src/Tomography.jl:876-920).
+// state: E, w, distance, grammage, z, u_z in and out; the transport stream is
+// (seed, id) or the scripted uniforms; returns the script values consumed.
+int orc_dir_segment(void* h, int n_mats, const int* mats, const double* fracs, double* state,
+                    double density, double distance, int straggling, double threshold_low,
+                    double energy_limit, uint64_t seed, uint64_t id, int n_script,
+                    const double* script, int* status) {
+  Physics* p = static_cast<Physics*>(h);
+  Mixture mx;
+  double tot = 0;
+  for (int j = 0; j < n_mats; ++j) tot += fracs[j];
+  for (int j = 0; j < n_mats; ++j) {
+    mx.mats.push_back(mats[j]);
+    mx.fracs.push_back(fracs[j] / tot);
+  }
+  Medium m = make_medium(*p, mx);
+  MixedKernel k = prepare_mixed_kernel(*p, mx);
+  McState s;
+  s.E = state[0];
+  s.w = state[1];
+  s.dist = state[2];
+  s.X = state[3];
+  s.z = state[4];
+  s.uz = state[5];
+  Rng g;
+  g.seed = seed;
+  g.id = id;
+  if (n_script > 0) {
+    g.script = script;
+    g.n_script = n_script;
+  }
+  McOptions o;
+  o.straggling = straggling != 0;
+  o.scattering = false;
+  o.energy_threshold_low = threshold_low;
+  o.source_energy_max = energy_limit;
+  propagate_segment(*p, m, k, s, false, density, distance, -s.uz, 0.0, g, o);
+  state[0] = s.E;
+  state[1] = s.w;
+  state[2] = s.dist;
+  state[3] = s.X;
+  state[4] = s.z;
+  state[5] = s.uz;
+  if (status) *status = s.status | (g.overrun ? (1 << 30) : 0);
+  return g.pos;
+}
+
 // MixedKernel columns for tests: returns the node count; cols receives
 // E, stop, sigma, range, hazard, proper (6 x n, when cap allows) and onset.
 int orc_mixed_kernel(void* h, int n_mats, const int* mats, const double* fracs, int cap,

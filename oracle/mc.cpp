@@ -784,4 +784,74 @@ double stochastic_history(const Physics& p, const McMedia& md, const McGeometry&
   return 0.0;
 }
 
+// propagate_mc_uniform_segment / propagate_mc_air_segment
+// (src/Tomography.jl:876-969): consume `distance` metres of one medium with
+// the segment step rule of :873-874; air takes its density at the current
+// altitude above the detector.
+double mc_segment_step(double remaining, double max_step) {
+  return std::min(remaining, std::max(1e-6, std::min(remaining + 1e-7, max_step)));
+}
+
+void propagate_segment(const Physics& p, const Medium& m, const MixedKernel& k, McState& s,
+                       bool air, double density, double distance, double cos_theta,
+                       double detector_elevation, Rng& g, const McOptions& o) {
+  const double eps = EPS64, elimit = o.source_energy_max, low = o.energy_threshold_low;
+  double remaining = distance;
+  while (remaining > 1e-8 && s.E < elimit - eps) {
+    if (s.w <= 0 || !std::isfinite(s.w)) break;
+    const double cur = s.E < low - eps ? std::min(low, elimit) : elimit;
+    const double rho = air ? 1.205 * std::exp(-(detector_elevation + s.z) / 12e3) : density;
+    double mx = 0.01 * tl(m, m.csda_R, s.E) / std::max(rho, air ? 1e-8 : 1e-6);
+    if (air) mx = std::min(mx, 0.05 * 12e3 / std::max(cos_theta, 0.05));
+    const double step = mc_segment_step(remaining, mx);
+    const double d0 = s.dist, E0 = s.E;
+    if (s.E < low - eps) {
+      if (o.straggling) straggled_step(p, m, k, s, rho, step, g, false, cur);
+      else csda_step_medium(p, m, s, rho, step);
+    } else {
+      if (o.straggling) transport_mixed_step(k, s, rho, step, g, cur);
+      else csda_step_medium(p, m, s, rho, step);
+    }
+    if (++s.steps > 2000000) s.status |= ST_STEP_CAP;
+    if (s.status & ST_FATAL) break;
+    const double actual = s.dist - d0;
+    if (s.w <= 0 || !std::isfinite(s.w)) break;
+    // a sub-ulp displacement that reached the mode boundary is progress
+    if (actual <= 0 && E0 < cur && cur < elimit && s.E >= cur) continue;
+    if (!(actual > 0)) {
+      if (s.E >= elimit) break;
+      s.status |= ST_NO_PROGRESS;  // the reference raises an error
+      break;
+    }
+    remaining = std::max(0.0, remaining - actual);
+  }
+}
+
+// compute_directional_flux_mc, one sample (src/Tomography.jl:1009-1034).
+double directional_history(const Physics& p, const DirMedia& md, const DirPath& path, double E0,
+                           double q, Rng& g, const McOptions& o, McState* final_state) {
+  McState s;
+  s.E = E0;
+  s.ux = s.uy = 0.0;
+  s.uz = -path.cos_theta;  // initial_state: direction -dir (src/Tomography.jl:863-869)
+  auto ok = [&] { return s.w > 0.0 && std::isfinite(s.w) && !(s.status & (ST_FATAL | ST_NO_PROGRESS)); };
+  for (long j = 0; j < path.n_seg; ++j) {
+    const int k = path.medium[j];
+    propagate_segment(p, md.med[k], md.kern[k], s, false, path.density[j], path.length[j],
+                      path.cos_theta, md.detector_elevation, g, o);
+    if (!ok()) break;
+  }
+  if (ok() && path.remaining_rock > 1e-8)
+    propagate_segment(p, md.med[md.rock], md.kern[md.rock], s, false, md.rock_density,
+                      path.remaining_rock, path.cos_theta, md.detector_elevation, g, o);
+  if (ok())
+    propagate_segment(p, md.med[md.air], md.kern[md.air], s, true, 0.0, path.air_distance,
+                      path.cos_theta, md.detector_elevation, g, o);
+  if (final_state) *final_state = s;
+  if (s.status & (ST_FATAL | ST_NO_PROGRESS)) return 0.0;
+  if (s.w > 0.0 && std::isfinite(s.w) && s.E < o.source_energy_max)
+    return s.w * flux_gccly(path.cos_theta, s.E, q);
+  return 0.0;
+}
+
 }  // namespace orc

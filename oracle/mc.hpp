@@ -85,4 +85,33 @@ struct McOptions {
 double stochastic_history(const Physics& p, const McMedia& md, const McGeometry& geo, double E0,
                           double q, Rng& g, const McOptions& o, McState* final_state);
 
+// Fixed-path MC of one direction (src/Tomography.jl:826-1041): the media a
+// path's segments use, the rock beyond them and the air above.
+enum : int { ST_NO_PROGRESS = 256 };  // src/Tomography.jl:916,965
+struct DirMedia {
+  std::vector<Medium> med;
+  std::vector<MixedKernel> kern;
+  int rock = 0, air = 0;
+  double rock_density = 0, detector_elevation = 0;
+};
+struct DirPath {
+  double cos_theta = 1;
+  const int* medium = nullptr;      // per segment
+  const double* density = nullptr;  // per segment
+  const double* length = nullptr;   // per segment
+  long n_seg = 0;
+  double remaining_rock = 0, air_distance = 0;
+};
+// _mc_segment_step (src/Tomography.jl:873-874).
+double mc_segment_step(double remaining, double max_step);
+// propagate_mc_uniform_segment (air = false) or propagate_mc_air_segment.
+void propagate_segment(const Physics& p, const Medium& m, const MixedKernel& k, McState& s,
+                       bool air, double density, double distance, double cos_theta,
+                       double detector_elevation, Rng& g, const McOptions& o);
+// One history of compute_directional_flux_mc; returns w * flux_gccly (the
+// caller applies 2 * sample weight).  o.source_energy_max is the energy
+// limit min(1e9, last table energy).
+double directional_history(const Physics& p, const DirMedia& md, const DirPath& path, double E0,
+                           double q, Rng& g, const McOptions& o, McState* final_state);
+
 }  // namespace orc

@@ -92,6 +92,15 @@ def lib():
                                        _DP, _U64, _U64, _I, _I, _D, _D, _DP, _IP,
                                        np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS"),
                                        _DP, _I]
+        _I64P = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+        L.orc_dir_histories.argtypes = [_P, _I, _IP, _IP, _DP, _I, _D, _I, _D, _L, _DP, _DP, _DP,
+                                        _I64P, _IP, _DP, _DP, _I64P, _DP, _DP, _DP, _U64, _U64,
+                                        _I, _D, _D, _DP, _IP, _I64P, _DP, _I]
+        L.orc_mc_segment_step.restype = _D
+        L.orc_mc_segment_step.argtypes = [_D, _D]
+        L.orc_dir_segment.restype = _I
+        L.orc_dir_segment.argtypes = [_P, _I, _IP, _DP, _DP, _D, _D, _I, _D, _D, _U64, _U64, _I,
+                                      _DP, C.POINTER(_I)]
         L.orc_mixed_kernel.restype = _I
         L.orc_mixed_kernel.argtypes = [_P, _I, _IP, _DP, _I, _DP, C.POINTER(_D)]
         L.orc_mixed_step.restype = _I
@@ -324,6 +333,59 @@ def reverse_del(kern, k, details=False, seed=0, id=0, script=None):
                                    int(details), seed, id,
                                    -1 if script is None else len(script), sc, out, C.byref(used))
     return out[0], out[1], int(out[2]), int(out[3]), status, used.value
+
+
+def dir_histories(p, media, rock, rock_density, air, detector_elevation, cos_theta,
+                  remaining_rock, air_distance, seg_ptr, seg_medium, seg_density, seg_length,
+                  smp_ptr, E, q, w, seed, id0=0, straggling=True, threshold_low=100.0,
+                  energy_limit=1e9, threads=0):
+    """Fixed-path MC histories (compute_directional_flux_mc,
+    src/Tomography.jl:826-1041).  media: list of (materials, fractions).
+    Returns (2 w_i w flux per history, status, steps, final energy)."""
+    nm = np.array([len(m[0]) for m in media], np.int32)
+    mats = np.zeros((len(media), 4), np.int32)
+    fr = np.zeros((len(media), 4))
+    for k, (ms, fs) in enumerate(media):
+        mats[k, :len(ms)] = ms
+        fr[k, :len(fs)] = fs
+    i64 = lambda a: np.ascontiguousarray(a, np.int64)
+    smp_ptr = i64(smp_ptr)
+    n = int(smp_ptr[-1])
+    contrib, Ef = np.zeros(n), np.zeros(n)
+    status = np.zeros(n, np.int32)
+    steps = np.zeros(n, np.int64)
+    lib().orc_dir_histories(p.h, len(media), nm, mats.ravel(), fr.ravel(), rock, rock_density,
+                            air, detector_elevation, len(cos_theta), _arr(cos_theta),
+                            _arr(remaining_rock), _arr(air_distance), i64(seg_ptr),
+                            np.ascontiguousarray(seg_medium, np.int32), _arr(seg_density),
+                            _arr(seg_length), smp_ptr, _arr(E), _arr(q), _arr(w), seed, id0,
+                            int(straggling), threshold_low, energy_limit, contrib, status, steps,
+                            Ef, threads or os.cpu_count())
+    return contrib, status, steps, Ef
+
+
+def mc_segment_step(remaining, max_step):
+    """_mc_segment_step (src/Tomography.jl:873-874) as the oracle applies it."""
+    return lib().orc_mc_segment_step(remaining, max_step)
+
+
+DIR_STATE = ("energy", "weight", "distance", "grammage", "z", "uz")
+
+
+def dir_segment(p, mats, state, density, distance, *, fracs=None, straggling=True,
+                threshold_low=100.0, energy_limit=1e9, seed=0, id=0, script=None):
+    """propagate_mc_uniform_segment (src/Tomography.jl:876-920) of one medium:
+    returns (final state dict, status, script values consumed)."""
+    mats = np.atleast_1d(np.asarray(mats, np.int32))
+    fr = _arr(fracs if fracs is not None else np.ones(len(mats)))
+    st = _arr([state.get(k, d) for k, d in zip(DIR_STATE, (0.0, 1.0, 0.0, 0.0, 0.0, -1.0))])
+    sc = _arr(script if script is not None else [0.0])
+    status = C.c_int()
+    used = lib().orc_dir_segment(p.h, len(mats), mats, fr, st, density, distance, int(straggling),
+                                 threshold_low, energy_limit, seed, id,
+                                 len(script) if script is not None else 0, sc,
+                                 C.byref(status))
+    return dict(zip(DIR_STATE, st)), status.value, used
 
 
 def mixed_kernel(p, mats, fracs=None):
