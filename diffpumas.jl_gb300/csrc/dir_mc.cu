@@ -331,23 +331,23 @@ struct PathGeo {
     h.limit = limit;
     if (C.straggling) {
       if constexpr (PHASE == 0) {
-        if (straggled_step<R, COOP>(m, C, s, Li, rho, step, g, false, limit, h.x)) {
+        if (straggled_step<R, COOP, true>(m, C, s, Li, rho, step, g, false, limit, h.x)) {
           h.x.kind = CONT_STRAG;
           h.x.medium = h.med;
           return ADV_WAIT;
         }
+        return step_end(h, h.x.moved);
       } else {
         if (mixed_step<R, COOP>(m, C, s, rho, step, g, limit, h.x)) {
           h.x.kind = CONT_MIXED;
           h.x.medium = h.med;
           return ADV_WAIT;
         }
+        return step_end(h, mixed_moved(h.x));
       }
-    } else {
-      csda_step(m, C, s, Li, rho, step);
-      return step_end(h, step);
     }
-    return step_end(h, h.x.moved);
+    csda_step(m, C, s, Li, rho, step);
+    return step_end(h, step);
   }
 
   template <int PHASE>
@@ -367,12 +367,14 @@ struct PathGeo {
           return ADV_WAIT;
         }
       }
+      return step_end(h, mixed_moved(x));
     } else {
       Loc<R> Li = locate(m, x.r0);
-      x.moved = straggled_end(m, P.C, h.s, Li, x.r0, R(d.energy), x.r1, x.r2, d.weight, d.process,
-                              d.element, true, false, R(0), x.r3, x.a, true, x.flag != 0, g);
+      const R moved = straggled_end(m, P.C, h.s, Li, x.r0, R(d.energy), x.r1, x.r2, d.weight,
+                                    d.process, d.element, true, false, R(0), x.r3, x.a, true,
+                                    x.flag != 0, g);
+      return step_end(h, moved);
     }
-    return step_end(h, x.moved);
   }
 };
 

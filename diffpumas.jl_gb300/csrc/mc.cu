@@ -491,7 +491,8 @@ struct SlabGeo {
   using Hist = mc::Hist<R>;
   using Queue = Handoff<R>;
   const McParams& P;
-  Med<R> rock, air;
+  const Med<R>& rock;
+  const Med<R>& air;
   __device__ long n0() const { return P.n; }
   __device__ void start(long i, Hist& h, Stream& g) const { start_history(P, i, h, g); }
   __device__ long load(const Queue& q, Hist& h, Stream& g) const {
@@ -524,8 +525,9 @@ __global__ void __launch_bounds__(KCfg<R>::threads, 1) mc_kernel(const __grid_co
     }
     base = smem + 16;
   }
-  SlabGeo<R> geo{P, make_med<R>(base, P.lay, P.info[0]),
-                 make_med<R>(base + P.lay.med_bytes, P.lay, P.info[1])};
+  const Med<R> rock = make_med<R>(base, P.lay, P.info[0]);
+  const Med<R> air = make_med<R>(base + P.lay.med_bytes, P.lay, P.info[1]);
+  SlabGeo<R> geo{P, rock, air};
   float* item = reinterpret_cast<float*>(smem + 16 + tables) + size_t(threadIdx.x >> 5) * P.coop_stride;
   transport_histories<R, PHASE, KCfg<R>::coop>(geo, P.C, P.counter, static_cast<Handoff<R>*>(P.queue),
                                                item, item + kItemsPerElement * P.coop_nel);

@@ -183,14 +183,14 @@ template <> __device__ __forceinline__ double uni<double>(Stream& g) {
   return u01(a, b);
 }
 // The leading 24 bits of the same draw (it differs from the double by < 2^-24).
-// FP32: the midpoints of 2^24 bins, in (0, 1).  A 24-bit uniform of exactly 0
+// FP32: 24 bits of the draw, in (0, 1).  A 24-bit uniform of exactly 0
 // (probability 2^-24, against 2^-53 in FP64) would place a hard event at zero
-// grammage: a step of no length, which the fixed-path loop rejects
-// (src/Tomography.jl:916), and -log(0) in the Gaussian draws.
+// grammage, a step of no length that the fixed-path loop rejects
+// (src/Tomography.jl:916): the lowest bin maps to 2^-25 instead.
 template <> __device__ __forceinline__ float uni<float>(Stream& g) {
   uint32_t a, b;
   g.next(a, b);
-  return (float(a >> 8) + 0.5f) * 0x1p-24f;
+  return fmaxf(float(a >> 8) * 0x1p-24f, 0x1p-25f);
 }
 __device__ __forceinline__ double uni_d(Stream& g) {
   uint32_t a, b;
@@ -617,7 +617,7 @@ struct State {
 template <class R>
 struct Cont {
   R a, b, c, d, dist;  // dist: requested length of a mixed step
-  R moved;             // path length of the last completed straggled or mixed step
+  R moved;             // path length of a completed straggled step (when asked)
   R r0, r1, r2, r3;
   int event, kind, medium, flag;
   double anc, q, denom;  // the pending event: ancestor, energy transfer, weight denominator
@@ -627,24 +627,26 @@ struct Cont {
 };
 enum : int { CONT_NONE = 0, CONT_MIXED = 1, CONT_STRAG = 2 };
 
+// Path length of a completed mixed step: FP64, travelled grammage / density as
+// the reference (src/MixedTransport.jl:198); FP32, the requested length when
+// the segment was consumed.
+template <class R>
+__device__ __forceinline__ R mixed_moved(const Cont<R>& x) {
+  return (sizeof(R) == 4 && x.a <= x.d) ? x.dist : x.b / x.c;
+}
+
 // transport_mixed_step (src/MixedTransport.jl:144-200), resumable.  The
 // round-off floor of the grammage bookkeeping is the reference's FP64
 // eps(max(1, grammage)) in both precisions: an FP32 ulp would exceed the
 // grammage of the 1e-7 m boundary-crossing steps.
 template <class R>
-__device__ void mixed_end(State<R>& s, Cont<R>& x, R Emax, R energy_limit, bool exhausted) {
+__device__ void mixed_end(State<R>& s, const Cont<R>& x, R Emax, R energy_limit, bool exhausted) {
   if (exhausted) s.status |= ST_EVENT_CAP;
   if (x.r1 > R(0) && x.r0 >= Emax && x.a > x.d && (energy_limit < R(0) || x.r0 < energy_limit))
     s.status |= ST_DOMAIN_HI;
-  // FP64: travelled / density as the reference; FP32: the requested length
-  // when the segment was consumed
-  R d;
-  if (sizeof(R) == 4 && x.a <= x.d) d = x.dist;
-  else d = x.b / x.c;
   s.E = x.r0;
   s.w = x.r1;
-  alt_add(s.z, -(d * s.uz));
-  x.moved = d;
+  alt_add(s.z, -(mixed_moved(x) * s.uz));
 }
 // Applies a hard event; true when the history's weight vanished.
 template <class R>
@@ -1058,7 +1060,8 @@ static __device__ __noinline__ R straggled_end(const Med<R>& m, const Consts& C,
 // The step up to its hard-event decision; true when it suspended on the
 // event's DCS sum (cooperative evaluation), with x holding what straggled_end
 // needs.
-template <class R, bool COOP>
+// With MOVED, x.moved receives the path length of a completed step.
+template <class R, bool COOP, bool MOVED = false>
 __device__ bool straggled_step(const Med<R>& m, const Consts& C, State<R>& s, const Loc<R>& Li,
                                R density, R step, Stream& g, bool scattering, R energy_limit,
                                Cont<R>& x) {
@@ -1142,8 +1145,9 @@ __device__ bool straggled_step(const Med<R>& m, const Consts& C, State<R>& s, co
     dX = X_ehs;
     shortened = true;
   }
-  x.moved = straggled_end(m, C, s, Li, ki, kf, ckf, dX, dw, proc, elem, del, ehs, k_ehs, density,
-                          step, shortened, scattering, g);
+  const R moved = straggled_end(m, C, s, Li, ki, kf, ckf, dX, dw, proc, elem, del, ehs, k_ehs,
+                                density, step, shortened, scattering, g);
+  if (MOVED) x.moved = moved;
   return false;
 }
 
@@ -1336,7 +1340,7 @@ __device__ int resume(const Med<R>& rock, const Med<R>& air, const Consts& C, Hi
     }
   } else {
     Loc<R> Li = locate(m, x.r0);
-    x.moved = straggled_end(m, C, h.s, Li, x.r0, R(d.energy), x.r1, x.r2, d.weight, d.process, d.element,
+    straggled_end(m, C, h.s, Li, x.r0, R(d.energy), x.r1, x.r2, d.weight, d.process, d.element,
                   true, false, R(0), x.r3, x.a, true, x.flag != 0, g);
   }
   return step_done(h);
