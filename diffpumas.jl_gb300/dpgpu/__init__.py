@@ -398,9 +398,13 @@ def backward_mc_batch(physics, los, *, rock, air, seed=42, straggling=True, scat
 
 from .directional import (CellSegment, DirBatch, DirectionalPath, DirMedia,  # noqa: E402
                           EnergySample,
-                          MaterialConfig, SiteConfig, build_cell_properties_for_mc,
-                          compute_directional_flux_mc, directional_flux_mc_batch,
-                          mc_cell_mixture_and_density, sample_energy_set)
+                          MaterialConfig, SiteConfig, assemble_forward_and_jacobian,
+                          build_cell_properties_for_mc, compute_directional_flux_csda,
+                          compute_directional_flux_mc, csda_flux_batch,
+                          directional_flux_and_grad_csda, directional_flux_mc_batch,
+                          get_csda_correction, get_csda_material_correction,
+                          mc_cell_mixture_and_density, sample_energy_set, set_csda_correction,
+                          set_csda_material_correction)
 
 
 # ----------------------------------------------------------------- tomography

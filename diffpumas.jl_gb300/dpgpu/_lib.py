@@ -77,6 +77,25 @@ class DpDirBatch(C.Structure):
                 ("rock_density", C.c_double), ("detector_elevation", C.c_double)]
 
 
+class DpCsdaConfig(C.Structure):
+    _fields_ = [("rock_material", C.c_int), ("water_material", C.c_int),
+                ("air_material", C.c_int), ("porous_material", C.c_int),
+                ("rock_density", C.c_double), ("water_density", C.c_double),
+                ("porous_density", C.c_double), ("porous_top_thickness", C.c_double),
+                ("detector_elevation", C.c_double), ("primary_altitude", C.c_double),
+                ("correction", C.c_int), ("kappa_strag", C.c_double), ("kappa_hard", C.c_double),
+                ("resid_a", C.c_double), ("resid_b", C.c_double), ("resid_c", C.c_double),
+                ("resid_d", C.c_double), ("material_correction", C.c_int),
+                ("material_linear", C.c_double), ("material_quadratic", C.c_double)]
+
+
+class DpCsdaBatch(C.Structure):
+    _fields_ = [("n_bins", C.c_long), ("cos_theta", C.c_void_p), ("remaining_rock", C.c_void_p),
+                ("surface_exit_z", C.c_void_p), ("valid", C.c_void_p), ("seg_ptr", C.c_void_p),
+                ("seg_cell", C.c_void_p), ("seg_length", C.c_void_p), ("n_energy", C.c_int),
+                ("energy", C.c_void_p), ("charge", C.c_void_p), ("weight", C.c_void_p)]
+
+
 class DpSolveParams(C.Structure):
     _fields_ = [("method", C.c_int), ("n_iter", C.c_int), ("cg_iter", C.c_int),
                 ("precision", C.c_int), ("relaxation", C.c_double), ("lm_damping", C.c_double),
@@ -140,6 +159,10 @@ PROTOTYPES = {
                              _VP, _VP, _I, C.c_uint64, _VP, _VP, _VP, _VP]),
     "dp_mc_los": (_I, [_P, _P, _P, _P, C.POINTER(DpMcConfig), _L, _VP, _I, _VP]),
     "dp_mc_los_dev": (_I, [_P, _P, _P, _P, C.POINTER(DpMcConfig), _L, _VP, _L, _I, _VP]),
+    "dp_dir_csda": (_I, [_P, _P, C.POINTER(DpCsdaConfig), C.POINTER(DpCsdaBatch), _L, _VP, _VP,
+                         _VP, _VP]),
+    "dp_dir_csda_dev": (_I, [_P, _P, C.POINTER(DpCsdaConfig), C.POINTER(DpCsdaBatch), _L, _VP,
+                             _VP, _VP, _VP]),
     "dp_dir_media_create": (_I, [_P, _P, _I, C.POINTER(_P), C.POINTER(_P)]),
     "dp_dir_media_free": (_I, [_P]),
     "dp_dir_mc": (_I, [_P, _P, _P, C.POINTER(DpDirBatch), C.POINTER(DpMcConfig), _VP, _VP, _VP,

@@ -255,3 +255,136 @@ def compute_directional_flux_mc(physics, matcfg, site, path, cell_materials, cel
                                   [list(energy_samples)], seed, straggling=straggling,
                                   energy_threshold_low=energy_threshold_low, precision=precision)
     return float(r["flux"][0]), float(r["sigma"][0])
+
+
+# ---------------------------------------------------- water-fraction CSDA model
+# The CSDA corrections (src/Tomography.jl:136-175): process-wide settings as
+# in the reference, read by every evaluation.
+CsdaCorrection = namedtuple("CsdaCorrection", "enabled kappa_strag kappa_hard resid_a resid_b "
+                            "resid_c resid_d")
+CsdaMaterialCorrection = namedtuple("CsdaMaterialCorrection", "enabled linear quadratic")
+_CORRECTION = CsdaCorrection(False, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0)
+_MATERIAL_CORRECTION = CsdaMaterialCorrection(False, 0.0, 0.0)
+
+
+def set_csda_correction(*, enabled=True, kappa_strag=0.0, kappa_hard=0.0, resid_a=0.0,
+                        resid_b=0.0, resid_c=0.0, resid_d=0.0):
+    """set_csda_correction! (src/Tomography.jl:145-153)."""
+    global _CORRECTION
+    _CORRECTION = CsdaCorrection(bool(enabled), float(kappa_strag), float(kappa_hard),
+                                 float(resid_a), float(resid_b), float(resid_c), float(resid_d))
+    return _CORRECTION
+
+
+def get_csda_correction():
+    return _CORRECTION
+
+
+def set_csda_material_correction(*, enabled=True, linear=0.0, quadratic=0.0):
+    """set_csda_material_correction! (src/Tomography.jl:168-172)."""
+    global _MATERIAL_CORRECTION
+    if not (math.isfinite(linear) and math.isfinite(quadratic)):
+        raise ValueError("nonfinite material coefficients")
+    _MATERIAL_CORRECTION = CsdaMaterialCorrection(bool(enabled), float(linear), float(quadratic))
+    return _MATERIAL_CORRECTION
+
+
+def get_csda_material_correction():
+    return _MATERIAL_CORRECTION
+
+
+def _csda_config(matcfg, site):
+    from ._lib import DpCsdaConfig
+    c, m = _CORRECTION, _MATERIAL_CORRECTION
+    return DpCsdaConfig(matcfg.rock_material - 1, matcfg.water_material - 1,
+                        matcfg.air_material - 1,
+                        matcfg.porous_material - 1 if matcfg.porous_material > 0 else -1,
+                        float(matcfg.rock_density), float(matcfg.water_density),
+                        float(matcfg.porous_density), float(matcfg.porous_top_thickness),
+                        float(site.detector_elevation), float(site.primary_altitude),
+                        int(c.enabled), c.kappa_strag, c.kappa_hard, c.resid_a, c.resid_b,
+                        c.resid_c, c.resid_d, int(m.enabled), m.linear, m.quadratic)
+
+
+def csda_flux_batch(physics, shallow_flags, matcfg, site, paths, water_fractions,
+                    energy_samples, *, jacobian=True):
+    """The water-fraction CSDA flux of every path (compute_directional_flux_csda,
+    src/Tomography.jl:667-727; NaN for invalid paths) in one launch, and with
+    jacobian=True d flux / d w per segment (segment order, CSR offsets
+    seg_ptr; summed over a cell's segments, the cell's Jacobian entry).
+    Returns flux, seg_ptr, seg_cell (0-based), seg_jac."""
+    from ._lib import DpCsdaBatch
+    from . import _ptr
+    n = len(paths)
+    wf = np.ascontiguousarray(water_fractions, np.float64)
+    sh = np.ascontiguousarray(np.asarray(shallow_flags, bool).astype(np.uint8))
+    cos_t = np.array([math.cos(math.radians(p.zenith)) for p in paths])
+    valid = np.array([1 if p.valid else 0 for p in paths], np.int32)
+    seg_ptr = np.zeros(n + 1, np.int64)
+    cells, lens = [], []
+    for d, p in enumerate(paths):
+        seg_ptr[d + 1] = seg_ptr[d] + len(p.segments)
+        cells.extend(int(s.cell_idx) - 1 for s in p.segments)
+        lens.extend(float(s.distance) for s in p.segments)
+    cells = np.array(cells, np.int32)
+    lens = np.array(lens, np.float64)
+    rem = np.array([p.remaining_rock_distance for p in paths], np.float64)
+    ez = np.array([p.surface_exit_z for p in paths], np.float64)
+    E = np.array([s.energy for s in energy_samples], np.float64)
+    q = np.array([s.charge for s in energy_samples], np.float64)
+    w = np.array([s.weight for s in energy_samples], np.float64)
+    B = DpCsdaBatch(n, cos_t.ctypes.data, rem.ctypes.data, ez.ctypes.data, valid.ctypes.data,
+                    seg_ptr.ctypes.data, cells.ctypes.data if len(cells) else None,
+                    lens.ctypes.data if len(lens) else None, len(E), E.ctypes.data,
+                    q.ctypes.data, w.ctypes.data)
+    flux = np.zeros(max(n, 1))
+    jac = np.zeros(max(len(cells), 1))
+    cfg = _csda_config(matcfg, site)
+    ctx = physics.ctx.h
+    check(load().dp_dir_csda(ctx, physics.h, C.byref(cfg), C.byref(B), len(wf), _ptr(sh),
+                             _ptr(wf), _ptr(flux), _ptr(jac) if jacobian else None), ctx)
+    return flux[:n], seg_ptr, cells, jac[:len(cells)]
+
+
+def compute_directional_flux_csda(physics, shallow_flags, matcfg, site, path, water_fractions,
+                                  energy_samples):
+    """Forward CSDA flux for one angular bin (src/Tomography.jl:667-727)."""
+    f, _, _, _ = csda_flux_batch(physics, shallow_flags, matcfg, site, [path], water_fractions,
+                                 energy_samples, jacobian=False)
+    return float(f[0])
+
+
+def directional_flux_and_grad_csda(physics, shallow_flags, matcfg, site, path, water_fractions,
+                                   energy_samples):
+    """(flux, cellids, values): the flux and d flux / d w of the cells the
+    path crosses, 1-based cell ids in order of first crossing
+    (src/Tomography.jl:736-762); (NaN, [], []) for an invalid path."""
+    if not path.valid or math.cos(math.radians(path.zenith)) <= 0.0:
+        return float("nan"), [], np.zeros(0)
+    f, _, cells, jac = csda_flux_batch(physics, shallow_flags, matcfg, site, [path],
+                                       water_fractions, energy_samples)
+    ids, vals = [], []
+    pos = {}
+    for c, v in zip(cells, jac):
+        if c not in pos:
+            pos[c] = len(ids)
+            ids.append(int(c) + 1)
+            vals.append(0.0)
+        vals[pos[c]] += v
+    return float(f[0]), ids, np.array(vals)
+
+
+def assemble_forward_and_jacobian(physics, shallow_flags, matcfg, site, paths, water_fractions,
+                                  energy_samples, *, n_cells, threaded=True):
+    """Forward flux of every bin and the sparse Jacobian J[bin, cell] =
+    d flux / d w (src/Tomography.jl:773-820), one launch for all bins; entries
+    that are zero or not finite are dropped as the reference drops them."""
+    import scipy.sparse as sp
+    flux, seg_ptr, cells, jac = csda_flux_batch(physics, shallow_flags, matcfg, site, paths,
+                                                water_fractions, energy_samples)
+    rows = np.repeat(np.arange(len(paths)), np.diff(seg_ptr))
+    J = sp.coo_matrix((jac, (rows, cells)), shape=(len(paths), n_cells)).tocsc()
+    J.sum_duplicates()
+    J.data[~np.isfinite(J.data)] = 0.0
+    J.eliminate_zeros()
+    return flux, J

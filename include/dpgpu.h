@@ -356,6 +356,52 @@ int dp_dir_mc_dev(dp_ctx* ctx, const dp_physics* phys, dp_dir_media* media,
                   const dp_dir_batch* batch, long total_samples, const dp_mc_config* cfg,
                   dp_los_result* out);
 
+/* ------------------------------------------------ water-fraction CSDA model
+ * compute_directional_flux_csda (src/Tomography.jl:667-727),
+ * directional_flux_and_grad_csda (:736-762) and assemble_forward_and_jacobian
+ * (:773-820): per direction, the CSDA flux of a path through cells of water
+ * mass fraction w, and d flux / d w.  MaterialConfig and SiteConfig
+ * (src/Tomography.jl:179-201) and the CSDA corrections of
+ * set_csda_correction! / set_csda_material_correction! (:136-175). */
+typedef struct {
+  int rock_material, water_material, air_material, porous_material; /* 0-based; porous < 0: none */
+  double rock_density, water_density, porous_density, porous_top_thickness;
+  double detector_elevation, primary_altitude;  /* SiteConfig (m) */
+  int correction;                                /* CsdaCorrection.enabled */
+  double kappa_strag, kappa_hard, resid_a, resid_b, resid_c, resid_d;
+  int material_correction;                       /* CsdaMaterialCorrection.enabled */
+  double material_linear, material_quadratic;
+} dp_csda_config;
+
+/* Directions and the energy samples they share (EnergySample list, at most 256). */
+typedef struct {
+  long n_bins;
+  const double* cos_theta;       /* cosd(zenith) */
+  const double* remaining_rock;  /* remaining_rock_distance (m) */
+  const double* surface_exit_z;  /* surface_exit_z (m above the detector) */
+  const int32_t* valid;          /* NULL: all valid; invalid or cos_theta <= 0: flux NaN */
+  const int64_t* seg_ptr;        /* n_bins + 1 running segment offsets */
+  const int32_t* seg_cell;       /* 0-based cell index per segment */
+  const double* seg_length;      /* m per segment */
+  int n_energy;
+  const double* energy;
+  const double* charge;
+  const double* weight;
+} dp_csda_batch;
+
+/* flux[n_bins]; jac (optional) one value per segment in segment order: the
+ * derivative of the direction's flux with respect to the water fraction of
+ * the segment's cell through that segment (summed over a cell's segments it
+ * is d flux / d w_cell, the entries of the reference's sparse Jacobian).
+ * shallow: one flag per cell (NULL: none shallow).  Host pointers. */
+int dp_dir_csda(dp_ctx* ctx, const dp_physics* phys, const dp_csda_config* cfg,
+                const dp_csda_batch* batch, long n_cells, const uint8_t* shallow,
+                const double* water_fraction, double* flux, double* jac);
+/* The same with every array in device memory (the structs on the host). */
+int dp_dir_csda_dev(dp_ctx* ctx, const dp_physics* phys, const dp_csda_config* cfg,
+                    const dp_csda_batch* batch, long n_cells, const uint8_t* shallow,
+                    const double* water_fraction, double* flux, double* jac);
+
 /* ------------------------------------------------------------------ tomography
  * Voxel-density CSDA forward model (examples/diff_flux_cube.jl:304-557):
  * ray march through a regular grid, per-segment range inversion, decay,

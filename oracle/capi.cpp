@@ -9,6 +9,7 @@
 #endif
 
 #include "mc.hpp"
+#include "wtomo.hpp"
 #include "oracle.hpp"
 
 using namespace orc;
@@ -424,6 +425,69 @@ int orc_dir_segment(void* h, int n_mats, const int* mats, const double* fracs, d
   state[5] = s.uz;
   if (status) *status = s.status | (g.overrun ? (1 << 30) : 0);
   return g.pos;
+}
+
+// Water-fraction CSDA flux of n_bins paths (compute_directional_flux_csda,
+// src/Tomography.jl:667-727) and, when grad is given, d flux / d w of each
+// path's cells (directional_flux_and_grad_csda, :736-762) by one tangent per
+// distinct cell: grad[j] for segment j holds the derivative with respect to
+// its cell at the cell's first segment on the path, 0 at repeats.
+// cfg: rock, water, air, porous material indices; dens: rock, water, porous
+// densities, porous top thickness; site: detector elevation, primary
+// altitude; corr: enabled, kappa_strag, kappa_hard, resid a-d, material
+// enabled, linear, quadratic.
+void orc_dir_csda(void* h, const int* cfg, const double* dens, const double* site,
+                  const double* corr, long n_bins, const double* cos_t, const double* rem,
+                  const double* exit_z, const int* valid, const int64_t* seg_ptr,
+                  const int* seg_cell, const double* seg_len, long n_cells,
+                  const unsigned char* shallow, const double* wf, int n_e, const double* E,
+                  const double* q, const double* ew, double* flux, double* grad, int nthreads) {
+  Physics* p = static_cast<Physics*>(h);
+  WConfig c;
+  c.rock = cfg[0];
+  c.water = cfg[1];
+  c.air = cfg[2];
+  c.porous = cfg[3];
+  c.rho_rock = dens[0];
+  c.rho_water = dens[1];
+  c.rho_porous = dens[2];
+  c.porous_top = dens[3];
+  c.det_elev = site[0];
+  c.primary = site[1];
+  c.corr = corr[0] != 0.0;
+  c.ks = corr[1];
+  c.kh = corr[2];
+  c.ra = corr[3];
+  c.rb = corr[4];
+  c.rc = corr[5];
+  c.rd = corr[6];
+  c.mcorr = corr[7] != 0.0;
+  c.lin = corr[8];
+  c.quad = corr[9];
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+  for (long b = 0; b < n_bins; ++b) {
+    WPath path;
+    path.cos_theta = cos_t[b];
+    path.remaining_rock = rem[b];
+    path.exit_z = exit_z[b];
+    path.valid = valid ? valid[b] != 0 : true;
+    path.cell = seg_cell + seg_ptr[b];
+    path.len = seg_len + seg_ptr[b];
+    path.n_seg = long(seg_ptr[b + 1] - seg_ptr[b]);
+    flux[b] = dir_flux_csda<double>(*p, c, path, shallow, wf, E, q, ew, n_e);
+    if (!grad) continue;
+    std::vector<Dual> wd(wf, wf + n_cells);
+    for (long k = 0; k < path.n_seg; ++k) {
+      double& g = grad[seg_ptr[b] + k];
+      g = 0.0;
+      bool first = true;
+      for (long j = 0; j < k; ++j) first = first && path.cell[j] != path.cell[k];
+      if (!first || !path.valid || !(path.cos_theta > 0.0)) continue;
+      wd[path.cell[k]].d = 1.0;
+      g = dir_flux_csda<Dual>(*p, c, path, shallow, wd.data(), E, q, ew, n_e).d;
+      wd[path.cell[k]].d = 0.0;
+    }
+  }
 }
 
 // MixedKernel columns for tests: returns the node count; cols receives

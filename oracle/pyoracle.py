@@ -96,6 +96,9 @@ def lib():
         L.orc_dir_histories.argtypes = [_P, _I, _IP, _IP, _DP, _I, _D, _I, _D, _L, _DP, _DP, _DP,
                                         _I64P, _IP, _DP, _DP, _I64P, _DP, _DP, _DP, _U64, _U64,
                                         _I, _D, _D, _DP, _IP, _I64P, _DP, _I]
+        _U8P = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+        L.orc_dir_csda.argtypes = [_P, _IP, _DP, _DP, _DP, _L, _DP, _DP, _DP, _IP, _I64P, _IP,
+                                   _DP, _L, _U8P, _DP, _I, _DP, _DP, _DP, _DP, C.c_void_p, _I]
         L.orc_mc_segment_step.restype = _D
         L.orc_mc_segment_step.argtypes = [_D, _D]
         L.orc_dir_segment.restype = _I
@@ -362,6 +365,27 @@ def dir_histories(p, media, rock, rock_density, air, detector_elevation, cos_the
                             int(straggling), threshold_low, energy_limit, contrib, status, steps,
                             Ef, threads or os.cpu_count())
     return contrib, status, steps, Ef
+
+
+def dir_csda(p, cfg, dens, site, corr, cos_t, rem, exit_z, valid, seg_ptr, seg_cell, seg_len,
+             shallow, wf, E, q, ew, grad=False, threads=0):
+    """Water-fraction CSDA flux per path (compute_directional_flux_csda,
+    src/Tomography.jl:667-727) and optionally d flux/d w per segment (the
+    derivative with respect to the segment's cell at its first segment on the
+    path, 0 at repeats).  cfg: 0-based rock, water, air, porous indices; dens:
+    rock, water, porous densities and porous top thickness; site: detector
+    elevation, primary altitude; corr: 10 correction settings."""
+    i32 = lambda a: np.ascontiguousarray(a, np.int32)
+    seg_ptr = np.ascontiguousarray(seg_ptr, np.int64)
+    n = len(cos_t)
+    flux = np.zeros(n)
+    g = np.zeros(max(int(seg_ptr[-1]), 1))
+    lib().orc_dir_csda(p.h, i32(cfg), _arr(dens), _arr(site), _arr(corr), n, _arr(cos_t),
+                       _arr(rem), _arr(exit_z), i32(valid), seg_ptr, i32(seg_cell), _arr(seg_len),
+                       len(wf), np.ascontiguousarray(shallow, np.uint8), _arr(wf), len(E), _arr(E),
+                       _arr(q), _arr(ew), flux, g.ctypes.data if grad else None,
+                       threads or os.cpu_count())
+    return (flux, g[:int(seg_ptr[-1])]) if grad else flux
 
 
 def mc_segment_step(remaining, max_step):
