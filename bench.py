@@ -16,6 +16,9 @@ Workloads (seeded synthetic inputs):
       directions x 1024 histories through a voxel volume of rock and
       rock+water cells, rock to the surface and air above; energies
       1e-3 - 1e9 GeV drawn on the device.  Unit: samples/s.
+  wcsda water-fraction CSDA flux + sparse d flux/d w (the Tomography
+      forward model and Jacobian) over the dir workload's 4096 directions,
+      32 CSDA nodes.  Unit: rays/s.
   c1  backward MC, CSDA mode, StandardRock 2650 kg/m^3, 100 m, 45 deg,
       energies log-uniform 1-100 GeV, +-1 charges, 10^4 histories, with the
       density gradient.  One step = one run_backward_mc estimate.  Unit:
@@ -434,6 +437,51 @@ def setup_dir(dp, torch, dev, precision="mixed", scale=1.0):
     return step_dev, step_e2e, plain_dev, info, phys
 
 
+def setup_wcsda(dp, torch, dev, precision="fp64", scale=1.0):
+    """Water-fraction CSDA forward model with its sparse Jacobian
+    (compute_directional_flux_csda + directional_flux_and_grad_csda for every
+    bin, i.e. assemble_forward_and_jacobian) over the dir workload's 4096
+    directions: 32x32x16 cells at 20 m, water fraction 0 or 0.3 per cell,
+    rock to the surface 600 m up, air to 30 km, 32 CSDA quadrature nodes on
+    [1, 1e6] GeV.  FP64."""
+    phys = dp.create_physics(materials=(dp.STANDARD_ROCK, dp.AIR, dp.WATER))
+    n_dirs = max(16, int(4096 * scale))
+    _, site, paths, _, _, wf = dir_scene(dp, phys, n_dirs)
+    cfg = dp.MaterialConfig(1, 3, 2, -1, 2710.0, 1000.0, 0.0, 0.0)
+    nodes = [dp.EnergySample(*x) for x in zip(*dp.csda_energy_quadrature(32, 1.0, 1e6))]
+    sh = np.zeros(len(wf), bool)
+    batch = dp.CsdaBatch(phys, sh, cfg, site, paths, nodes).to_device()
+    w_t = torch.tensor(wf, dtype=torch.float64, device=dev)
+    flux = torch.zeros(n_dirs, dtype=torch.float64, device=dev)
+    jac = torch.zeros(max(batch.n_seg, 1), dtype=torch.float64, device=dev)
+    one = [dp.CsdaBatch(phys, sh, cfg, site, [p], nodes).to_device() for p in paths[:16]]
+
+    def step_dev():
+        batch.run_dev(w_t, flux, jac)
+
+    def step_e2e():
+        f, _ = batch.run(wf)
+        assert np.isfinite(f).all()
+
+    def plain_dev():
+        for b in one:
+            b.run_dev(w_t, flux, jac)
+
+    info = {"units": n_dirs, "unit": "rays/s", "kernel": "dir_csda_grad",
+            # per bin: 40 B geometry + per segment 4 B cell + 8 B length + 8 B w
+            # read and 8 B Jacobian value written
+            "alg_bytes": n_dirs * 40 + batch.n_seg * 28, "traffic": None,
+            "note": "FP64 pipe bound (the reference's operations with two tangents)",
+            "config": {"workload": "wcsda: water-fraction CSDA flux + d flux/d w per bin, 4096 "
+                                   "directions through 32x32x16 cells @ 20 m (w 0 / 0.3), rock to "
+                                   "600 m, air to 30 km, 32 CSDA nodes [1, 1e6] GeV",
+                       "n_bins": n_dirs, "segments": batch.n_seg, "precision": "fp64"},
+            "h2d": batch.host_bytes() + wf.nbytes, "d2h": 8 * (n_dirs + batch.n_seg),
+            "plain_what": "one launch per direction, first 16 directions", "plain_units": 16,
+            "plain_reps": 1}
+    return step_dev, step_e2e, plain_dev, info, phys
+
+
 def setup_c1(dp, torch, dev):
     phys = dp.create_physics()
     n = 10000
@@ -465,8 +513,8 @@ def run_gpu(args):
     import dpgpu as dp
     dp._default = dp.Context(local)
     setup = {"c2": setup_c2, "c3": setup_c3, "c4": setup_c4, "c5": setup_c5,
-             "c1": setup_c1, "dir": setup_dir}[args.workload]
-    kw = {"scale": args.scale} if args.workload in ("c2", "c4", "c5", "dir") else {}
+             "c1": setup_c1, "dir": setup_dir, "wcsda": setup_wcsda}[args.workload]
+    kw = {"scale": args.scale} if args.workload in ("c2", "c4", "c5", "dir", "wcsda") else {}
     step_dev, step_e2e, plain_dev, info, phys = setup(dp, torch, dev, **kw)
     if args.scale != 1.0:
         info["config"]["scale"] = args.scale
@@ -626,6 +674,8 @@ def cpu_baseline(workload, budget_s=15.0, threads=None):
                           "transport + dual-number CSDA gradient (FP64 oracle, OpenMP)"}
     if workload == "dir":
         return cpu_baseline_dir(O, budget_s, threads)
+    if workload == "wcsda":
+        return cpu_baseline_wcsda(O, budget_s, threads)
     if workload == "c2":
         p = O.default_physics((O.STANDARD_ROCK, O.AIR, O.WATER), coulomb=True)
         rng = np.random.default_rng(0)
@@ -687,13 +737,39 @@ def cpu_baseline_dir(O, budget_s, threads):
                       "OpenMP over histories)"}
 
 
+def cpu_baseline_wcsda(O, budget_s, threads):
+    """The oracle's water-fraction CSDA flux and d flux/d w (one dual-number
+    pass per on-path cell, as the reference's forward-mode segment rules
+    differentiate) over the wcsda directions, OpenMP over bins."""
+    import dpgpu as dp
+    from dpgpu.workloads import directional_config
+    raw, wf = directional_config(4096)
+    p = O.default_physics((O.STANDARD_ROCK, O.AIR, O.WATER))
+    E, q, w = dp.csda_energy_quadrature(32, 1.0, 1e6)
+    n, t0, i = 0, time.perf_counter(), 0
+    while time.perf_counter() - t0 < budget_s:
+        chunk = [raw[(i + k) % len(raw)] for k in range(64)]
+        i += 64
+        seg_ptr = np.concatenate([[0], np.cumsum([len(c[2]) for c in chunk])])
+        O.dir_csda(p, [0, 2, 1, -1], [2710.0, 1000.0, 0.0, 0.0], [963.0, 30000.0], [0] * 10,
+                   [np.cos(np.radians(c[0])) for c in chunk], [c[5] for c in chunk],
+                   [c[6] for c in chunk], [1] * len(chunk), seg_ptr,
+                   [s[0] - 1 for c in chunk for s in c[2]], [s[1] for c in chunk for s in c[2]],
+                   np.zeros(len(wf), np.uint8), wf, E, q, w, grad=True, threads=threads)
+        n += len(chunk)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": "rays/s", "cores": threads, "kind": "port",
+            "sample": f"{n} directions of the wcsda workload (cycled), flux + dual-number "
+                      "d flux/d w (FP64 oracle, OpenMP over bins)"}
+
+
 def run_reference(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     units = {"c2": "samples/s", "c3": "rays/s", "c4": "samples/s", "c5": "iterations/s",
-             "c1": "samples/s", "dir": "samples/s"}[args.workload]
+             "c1": "samples/s", "dir": "samples/s", "wcsda": "rays/s"}[args.workload]
     vals = []
     for _ in range(args.warmup):
         cpu_baseline(args.workload, budget_s=args.cpu_seconds / 4)
@@ -718,7 +794,8 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "c1", "dir"])
+    ap.add_argument("--workload", default="c2",
+                    choices=["c2", "c3", "c4", "c5", "c1", "dir", "wcsda"])
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")

@@ -398,7 +398,8 @@ def backward_mc_batch(physics, los, *, rock, air, seed=42, straggling=True, scat
 
 from .directional import (CellSegment, DirBatch, DirectionalPath, DirMedia,  # noqa: E402
                           EnergySample,
-                          MaterialConfig, SiteConfig, assemble_forward_and_jacobian,
+                          CsdaBatch, MaterialConfig, SiteConfig,
+                          assemble_forward_and_jacobian,
                           build_cell_properties_for_mc, compute_directional_flux_csda,
                           compute_directional_flux_mc, csda_flux_batch,
                           directional_flux_and_grad_csda, directional_flux_mc_batch,

@@ -306,6 +306,77 @@ def _csda_config(matcfg, site):
                         c.resid_c, c.resid_d, int(m.enabled), m.linear, m.quadratic)
 
 
+class CsdaBatch:
+    """Directions and energy samples prepared for dp_dir_csda (the segment
+    arrays of every path, the shared EnergySample list).  run() evaluates a
+    water-fraction field through host arrays; to_device() + run_dev() keep
+    everything resident (torch CUDA tensors)."""
+
+    def __init__(self, physics, shallow_flags, matcfg, site, paths, energy_samples):
+        self.physics, self.n_bins = physics, len(paths)
+        n = self.n_bins
+        seg_ptr = np.zeros(n + 1, np.int64)
+        seg_ptr[1:] = np.cumsum([len(p.segments) for p in paths])
+        self.arrays = {
+            "cos_theta": np.array([math.cos(math.radians(p.zenith)) for p in paths]),
+            "remaining_rock": np.array([p.remaining_rock_distance for p in paths], np.float64),
+            "surface_exit_z": np.array([p.surface_exit_z for p in paths], np.float64),
+            "valid": np.array([1 if p.valid else 0 for p in paths], np.int32),
+            "seg_ptr": seg_ptr,
+            "seg_cell": np.array([s.cell_idx - 1 for p in paths for s in p.segments], np.int32),
+            "seg_length": np.array([s.distance for p in paths for s in p.segments], np.float64),
+            "energy": np.array([x.energy for x in energy_samples], np.float64),
+            "charge": np.array([x.charge for x in energy_samples], np.float64),
+            "weight": np.array([x.weight for x in energy_samples], np.float64),
+            "shallow": np.ascontiguousarray(np.asarray(shallow_flags, bool).astype(np.uint8))}
+        self.n_seg = int(seg_ptr[-1])
+        self.n_energy = len(energy_samples)
+        self.n_cells = len(self.arrays["shallow"])
+        self.config = _csda_config(matcfg, site)
+        self.dev = None
+
+    def _struct(self, ptr):
+        from ._lib import DpCsdaBatch
+        return DpCsdaBatch(self.n_bins, ptr("cos_theta"), ptr("remaining_rock"),
+                           ptr("surface_exit_z"), ptr("valid"), ptr("seg_ptr"), ptr("seg_cell"),
+                           ptr("seg_length"), self.n_energy, ptr("energy"), ptr("charge"),
+                           ptr("weight"))
+
+    def host_bytes(self):
+        return sum(a.nbytes for a in self.arrays.values())
+
+    def run(self, water_fractions, *, jacobian=True):
+        """(flux per bin, d flux / d w per segment or None), host arrays."""
+        from . import _ptr
+        A = self.arrays
+        B = self._struct(lambda k: A[k].ctypes.data if A[k].size else None)
+        wf = np.ascontiguousarray(water_fractions, np.float64)
+        flux = np.zeros(max(self.n_bins, 1))
+        jac = np.zeros(max(self.n_seg, 1))
+        ctx = self.physics.ctx.h
+        check(load().dp_dir_csda(ctx, self.physics.h, C.byref(self.config), C.byref(B),
+                                 len(wf), _ptr(A["shallow"]), _ptr(wf), _ptr(flux),
+                                 _ptr(jac) if jacobian else None), ctx)
+        return flux[:self.n_bins], (jac[:self.n_seg] if jacobian else None)
+
+    def to_device(self):
+        import torch
+        dev = torch.device("cuda", self.physics.ctx.device)
+        self.dev = {k: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+                    for k, a in self.arrays.items()}
+        return self
+
+    def run_dev(self, water_fractions, flux, jac=None):
+        """Enqueues one evaluation on resident arrays: water_fractions, flux
+        (n_bins) and jac (n_seg, optional) are float64 CUDA tensors."""
+        B = self._struct(lambda k: self.dev[k].data_ptr() if self.dev[k].numel() else None)
+        ctx = self.physics.ctx.h
+        check(load().dp_dir_csda_dev(ctx, self.physics.h, C.byref(self.config), C.byref(B),
+                                     self.n_cells, self.dev["shallow"].data_ptr(),
+                                     water_fractions.data_ptr(), flux.data_ptr(),
+                                     jac.data_ptr() if jac is not None else None), ctx)
+
+
 def csda_flux_batch(physics, shallow_flags, matcfg, site, paths, water_fractions,
                     energy_samples, *, jacobian=True):
     """The water-fraction CSDA flux of every path (compute_directional_flux_csda,
@@ -313,37 +384,10 @@ def csda_flux_batch(physics, shallow_flags, matcfg, site, paths, water_fractions
     jacobian=True d flux / d w per segment (segment order, CSR offsets
     seg_ptr; summed over a cell's segments, the cell's Jacobian entry).
     Returns flux, seg_ptr, seg_cell (0-based), seg_jac."""
-    from ._lib import DpCsdaBatch
-    from . import _ptr
-    n = len(paths)
-    wf = np.ascontiguousarray(water_fractions, np.float64)
-    sh = np.ascontiguousarray(np.asarray(shallow_flags, bool).astype(np.uint8))
-    cos_t = np.array([math.cos(math.radians(p.zenith)) for p in paths])
-    valid = np.array([1 if p.valid else 0 for p in paths], np.int32)
-    seg_ptr = np.zeros(n + 1, np.int64)
-    cells, lens = [], []
-    for d, p in enumerate(paths):
-        seg_ptr[d + 1] = seg_ptr[d] + len(p.segments)
-        cells.extend(int(s.cell_idx) - 1 for s in p.segments)
-        lens.extend(float(s.distance) for s in p.segments)
-    cells = np.array(cells, np.int32)
-    lens = np.array(lens, np.float64)
-    rem = np.array([p.remaining_rock_distance for p in paths], np.float64)
-    ez = np.array([p.surface_exit_z for p in paths], np.float64)
-    E = np.array([s.energy for s in energy_samples], np.float64)
-    q = np.array([s.charge for s in energy_samples], np.float64)
-    w = np.array([s.weight for s in energy_samples], np.float64)
-    B = DpCsdaBatch(n, cos_t.ctypes.data, rem.ctypes.data, ez.ctypes.data, valid.ctypes.data,
-                    seg_ptr.ctypes.data, cells.ctypes.data if len(cells) else None,
-                    lens.ctypes.data if len(lens) else None, len(E), E.ctypes.data,
-                    q.ctypes.data, w.ctypes.data)
-    flux = np.zeros(max(n, 1))
-    jac = np.zeros(max(len(cells), 1))
-    cfg = _csda_config(matcfg, site)
-    ctx = physics.ctx.h
-    check(load().dp_dir_csda(ctx, physics.h, C.byref(cfg), C.byref(B), len(wf), _ptr(sh),
-                             _ptr(wf), _ptr(flux), _ptr(jac) if jacobian else None), ctx)
-    return flux[:n], seg_ptr, cells, jac[:len(cells)]
+    b = CsdaBatch(physics, shallow_flags, matcfg, site, paths, energy_samples)
+    flux, jac = b.run(water_fractions, jacobian=jacobian)
+    return flux, b.arrays["seg_ptr"], b.arrays["seg_cell"], (jac if jacobian else
+                                                             np.zeros(b.n_seg))
 
 
 def compute_directional_flux_csda(physics, shallow_flags, matcfg, site, path, water_fractions,
