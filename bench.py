@@ -437,13 +437,14 @@ def setup_dir(dp, torch, dev, precision="mixed", scale=1.0):
     return step_dev, step_e2e, plain_dev, info, phys
 
 
-def setup_wcsda(dp, torch, dev, precision="fp64", scale=1.0):
+def setup_wcsda(dp, torch, dev, precision="mixed", scale=1.0):
     """Water-fraction CSDA forward model with its sparse Jacobian
     (compute_directional_flux_csda + directional_flux_and_grad_csda for every
     bin, i.e. assemble_forward_and_jacobian) over the dir workload's 4096
     directions: 32x32x16 cells at 20 m, water fraction 0 or 0.3 per cell,
     rock to the surface 600 m up, air to 30 km, 32 CSDA quadrature nodes on
-    [1, 1e6] GeV.  FP64."""
+    [1, 1e6] GeV.  Mixed precision (FP32 walk, FP64 adjoint sums and flux);
+    the plain form is the FP64 kernel, one launch per direction."""
     phys = dp.create_physics(materials=(dp.STANDARD_ROCK, dp.AIR, dp.WATER))
     n_dirs = max(16, int(4096 * scale))
     _, site, paths, _, _, wf = dir_scene(dp, phys, n_dirs)
@@ -457,27 +458,28 @@ def setup_wcsda(dp, torch, dev, precision="fp64", scale=1.0):
     one = [dp.CsdaBatch(phys, sh, cfg, site, [p], nodes).to_device() for p in paths[:16]]
 
     def step_dev():
-        batch.run_dev(w_t, flux, jac)
+        batch.run_dev(w_t, flux, jac, precision=precision)
 
     def step_e2e():
-        f, _ = batch.run(wf)
+        f, _ = batch.run(wf, precision=precision)
         assert np.isfinite(f).all()
 
     def plain_dev():
         for b in one:
-            b.run_dev(w_t, flux, jac)
+            b.run_dev(w_t, flux, jac, precision="fp64")
 
-    info = {"units": n_dirs, "unit": "rays/s", "kernel": "dir_csda_grad",
+    info = {"units": n_dirs, "unit": "rays/s",
+            "kernel": "dir_csda32_grad" if precision == "mixed" else "dir_csda_grad",
             # per bin: 40 B geometry + per segment 4 B cell + 8 B length + 8 B w
             # read and 8 B Jacobian value written
             "alg_bytes": n_dirs * 40 + batch.n_seg * 28, "traffic": None,
-            "note": "FP64 pipe bound (the reference's operations with two tangents)",
+            "note": "SM issue / FP64 pipe bound, not HBM (tables in shared memory, paths in L2)",
             "config": {"workload": "wcsda: water-fraction CSDA flux + d flux/d w per bin, 4096 "
                                    "directions through 32x32x16 cells @ 20 m (w 0 / 0.3), rock to "
                                    "600 m, air to 30 km, 32 CSDA nodes [1, 1e6] GeV",
-                       "n_bins": n_dirs, "segments": batch.n_seg, "precision": "fp64"},
+                       "n_bins": n_dirs, "segments": batch.n_seg, "precision": precision},
             "h2d": batch.host_bytes() + wf.nbytes, "d2h": 8 * (n_dirs + batch.n_seg),
-            "plain_what": "one launch per direction, first 16 directions", "plain_units": 16,
+            "plain_what": "FP64, one launch per direction, first 16 directions", "plain_units": 16,
             "plain_reps": 1}
     return step_dev, step_e2e, plain_dev, info, phys
 

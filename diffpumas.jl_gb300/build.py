@@ -22,7 +22,8 @@ UNITS = ["api.cu", "physics_build.cu", "csda_mc.cu", "tomo.cu", "mc.cu", "dir_mc
          "inverse.cu", "wtomo.cu"]
 # per-unit flags: the stochastic transport's FP32 kernel uses the hardware
 # (MUFU) transcendentals; FP64 arithmetic is not affected by these flags
-UNIT_FLAGS = {"mc.cu": ["--use_fast_math"], "dir_mc.cu": ["--use_fast_math"]}
+UNIT_FLAGS = {"mc.cu": ["--use_fast_math"], "dir_mc.cu": ["--use_fast_math"],
+              "wtomo.cu": ["--use_fast_math"]}
 
 
 def nvcc():

@@ -160,9 +160,9 @@ PROTOTYPES = {
     "dp_mc_los": (_I, [_P, _P, _P, _P, C.POINTER(DpMcConfig), _L, _VP, _I, _VP]),
     "dp_mc_los_dev": (_I, [_P, _P, _P, _P, C.POINTER(DpMcConfig), _L, _VP, _L, _I, _VP]),
     "dp_dir_csda": (_I, [_P, _P, C.POINTER(DpCsdaConfig), C.POINTER(DpCsdaBatch), _L, _VP, _VP,
-                         _VP, _VP]),
+                         _VP, _VP, _I]),
     "dp_dir_csda_dev": (_I, [_P, _P, C.POINTER(DpCsdaConfig), C.POINTER(DpCsdaBatch), _L, _VP,
-                             _VP, _VP, _VP]),
+                             _VP, _VP, _VP, _I]),
     "dp_dir_media_create": (_I, [_P, _P, _I, C.POINTER(_P), C.POINTER(_P)]),
     "dp_dir_media_free": (_I, [_P]),
     "dp_dir_mc": (_I, [_P, _P, _P, C.POINTER(DpDirBatch), C.POINTER(DpMcConfig), _VP, _VP, _VP,

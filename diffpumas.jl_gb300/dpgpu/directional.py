@@ -345,8 +345,9 @@ class CsdaBatch:
     def host_bytes(self):
         return sum(a.nbytes for a in self.arrays.values())
 
-    def run(self, water_fractions, *, jacobian=True):
+    def run(self, water_fractions, *, jacobian=True, precision="fp64"):
         """(flux per bin, d flux / d w per segment or None), host arrays."""
+        from . import PRECISION
         from . import _ptr
         A = self.arrays
         B = self._struct(lambda k: A[k].ctypes.data if A[k].size else None)
@@ -356,7 +357,7 @@ class CsdaBatch:
         ctx = self.physics.ctx.h
         check(load().dp_dir_csda(ctx, self.physics.h, C.byref(self.config), C.byref(B),
                                  len(wf), _ptr(A["shallow"]), _ptr(wf), _ptr(flux),
-                                 _ptr(jac) if jacobian else None), ctx)
+                                 _ptr(jac) if jacobian else None, PRECISION[precision]), ctx)
         return flux[:self.n_bins], (jac[:self.n_seg] if jacobian else None)
 
     def to_device(self):
@@ -366,26 +367,28 @@ class CsdaBatch:
                     for k, a in self.arrays.items()}
         return self
 
-    def run_dev(self, water_fractions, flux, jac=None):
+    def run_dev(self, water_fractions, flux, jac=None, precision="fp64"):
         """Enqueues one evaluation on resident arrays: water_fractions, flux
         (n_bins) and jac (n_seg, optional) are float64 CUDA tensors."""
+        from . import PRECISION
         B = self._struct(lambda k: self.dev[k].data_ptr() if self.dev[k].numel() else None)
         ctx = self.physics.ctx.h
         check(load().dp_dir_csda_dev(ctx, self.physics.h, C.byref(self.config), C.byref(B),
                                      self.n_cells, self.dev["shallow"].data_ptr(),
                                      water_fractions.data_ptr(), flux.data_ptr(),
-                                     jac.data_ptr() if jac is not None else None), ctx)
+                                     jac.data_ptr() if jac is not None else None,
+                                     PRECISION[precision]), ctx)
 
 
 def csda_flux_batch(physics, shallow_flags, matcfg, site, paths, water_fractions,
-                    energy_samples, *, jacobian=True):
+                    energy_samples, *, jacobian=True, precision="fp64"):
     """The water-fraction CSDA flux of every path (compute_directional_flux_csda,
     src/Tomography.jl:667-727; NaN for invalid paths) in one launch, and with
     jacobian=True d flux / d w per segment (segment order, CSR offsets
     seg_ptr; summed over a cell's segments, the cell's Jacobian entry).
     Returns flux, seg_ptr, seg_cell (0-based), seg_jac."""
     b = CsdaBatch(physics, shallow_flags, matcfg, site, paths, energy_samples)
-    flux, jac = b.run(water_fractions, jacobian=jacobian)
+    flux, jac = b.run(water_fractions, jacobian=jacobian, precision=precision)
     return flux, b.arrays["seg_ptr"], b.arrays["seg_cell"], (jac if jacobian else
                                                              np.zeros(b.n_seg))
 
@@ -419,13 +422,14 @@ def directional_flux_and_grad_csda(physics, shallow_flags, matcfg, site, path, w
 
 
 def assemble_forward_and_jacobian(physics, shallow_flags, matcfg, site, paths, water_fractions,
-                                  energy_samples, *, n_cells, threaded=True):
+                                  energy_samples, *, n_cells, threaded=True, precision="fp64"):
     """Forward flux of every bin and the sparse Jacobian J[bin, cell] =
     d flux / d w (src/Tomography.jl:773-820), one launch for all bins; entries
     that are zero or not finite are dropped as the reference drops them."""
     import scipy.sparse as sp
     flux, seg_ptr, cells, jac = csda_flux_batch(physics, shallow_flags, matcfg, site, paths,
-                                                water_fractions, energy_samples)
+                                                water_fractions, energy_samples,
+                                                precision=precision)
     rows = np.repeat(np.arange(len(paths)), np.diff(seg_ptr))
     J = sp.coo_matrix((jac, (rows, cells)), shape=(len(paths), n_cells)).tocsc()
     J.sum_duplicates()

@@ -393,14 +393,16 @@ typedef struct {
  * derivative of the direction's flux with respect to the water fraction of
  * the segment's cell through that segment (summed over a cell's segments it
  * is d flux / d w_cell, the entries of the reference's sparse Jacobian).
- * shallow: one flag per cell (NULL: none shallow).  Host pointers. */
+ * shallow: one flag per cell (NULL: none shallow).  precision DP_PREC_FP64:
+ * the reference's FP64 operations; DP_PREC_MIXED: FP32 steps and tangents,
+ * FP64 adjoint prefix sums, flux and reductions.  Host pointers. */
 int dp_dir_csda(dp_ctx* ctx, const dp_physics* phys, const dp_csda_config* cfg,
                 const dp_csda_batch* batch, long n_cells, const uint8_t* shallow,
-                const double* water_fraction, double* flux, double* jac);
+                const double* water_fraction, double* flux, double* jac, int precision);
 /* The same with every array in device memory (the structs on the host). */
 int dp_dir_csda_dev(dp_ctx* ctx, const dp_physics* phys, const dp_csda_config* cfg,
                     const dp_csda_batch* batch, long n_cells, const uint8_t* shallow,
-                    const double* water_fraction, double* flux, double* jac);
+                    const double* water_fraction, double* flux, double* jac, int precision);
 
 /* ------------------------------------------------------------------ tomography
  * Voxel-density CSDA forward model (examples/diff_flux_cube.jl:304-557):

@@ -1,7 +1,8 @@
 """Water-fraction CSDA model on the GPU (compute_directional_flux_csda,
 directional_flux_and_grad_csda, assemble_forward_and_jacobian,
 src/Tomography.jl:444-820) against the oracle, through the C ABI: flux and
-d flux / d w in FP64, with the corrections off and on."""
+d flux / d w in FP64 (and the mixed-precision walk within 1e-4), with the
+corrections off and on."""
 import math
 
 import numpy as np
@@ -177,3 +178,35 @@ def test_assembled_jacobian_and_invalid_paths(dp, phys, scene):
         row = J.getrow(b).toarray().ravel()
         assert set(np.nonzero(row)[0] + 1) <= set(ids)
         np.testing.assert_allclose(row[np.array(ids) - 1], vals, rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("which", ["plain", "correction"])
+def test_mixed_precision_within_1e4(dp, phys, oracle, orc_phys, scene, which):
+    """FP32 walk and tangents (FP64 adjoint sums, flux and reductions): flux
+    within 1e-4 of the FP64 oracle per direction, the Jacobian within 1e-4
+    norm-wise per direction."""
+    wf, paths = scene
+    cfg = dp.MaterialConfig(1, 3, 2, -1, 2650.0, 1000.0, 0.0, 0.0)
+    site = dp.SiteConfig(963.0, 3e4)
+    samples = _samples(dp, 32, 9)
+    corr = [0] * 10
+    try:
+        if which == "correction":
+            dp.set_csda_correction(**CORR[which])
+            c = CORR[which]
+            corr = [1, c["kappa_strag"], c["kappa_hard"], c["resid_a"], c["resid_b"], c["resid_c"],
+                    c["resid_d"], 0, 0.0, 0.0]
+        f, seg_ptr, cells, jac = dp.csda_flux_batch(phys, np.zeros(len(wf), bool), cfg, site, paths,
+                                                    wf, samples, precision="mixed")
+    finally:
+        dp.set_csda_correction(enabled=False)
+    of, og = _oracle(oracle, orc_phys, wf, paths, samples, corr)
+    np.testing.assert_allclose(f, of, rtol=1e-4, atol=0)
+    g = _per_cell_first(seg_ptr, cells, jac)
+    worst = 0.0
+    for b in range(len(paths)):
+        a, z = seg_ptr[b], seg_ptr[b + 1]
+        if z > a:
+            worst = max(worst, np.linalg.norm(g[a:z] - og[a:z]) / np.linalg.norm(og[a:z]))
+    print("mixed-precision Jacobian, worst per-direction relative norm error", worst)
+    assert worst <= 1e-4
