@@ -13,6 +13,7 @@
 // stopping power) are staged once per CTA into shared memory with
 // cp.async.bulk.  Per-history results go to global memory and are reduced in a
 // fixed order (compensated), so estimates are bitwise reproducible.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -437,6 +438,71 @@ __global__ void __launch_bounds__(kRedThreads) reduce_parts_kernel(const KSum* p
   if (threadIdx.x < 3) out[threadIdx.x] = sh[threadIdx.x][0].s + sh[threadIdx.x][0].c;
 }
 
+// compute_flux_csda_direct (src/Geometry.jl:1126-1209): the two-layer CSDA
+// flux in closed form (one range inversion per layer), thread per sample,
+// with d/d rho in tangent mode.  Tables read from global memory (L1/L2).
+__device__ __forceinline__ Dd range_g(const TabView& tv, int m, Dd E) {
+  return interp_logE(tv, tv.col(m, DP_COL_E), tv.col(m, DP_COL_LOGE), tv.col(m, DP_COL_CSDA_R), E,
+                     dlog(E), nullptr);
+}
+__device__ __forceinline__ Dd stop_g(const TabView& tv, int m, Dd E) {
+  return interp_logE(tv, tv.col(m, DP_COL_E), tv.col(m, DP_COL_LOGE), tv.col(m, DP_COL_CSDA_S), E,
+                     dlog(E), nullptr);
+}
+__device__ __forceinline__ Dd energy_g(const TabView& tv, int m, Dd X) {
+  return inverse_range(tv.col(m, DP_COL_CSDA_R), tv.col(m, DP_COL_E), tv.col(m, DP_COL_LOGE), tv.n,
+                       X, nullptr);
+}
+// compute_decay_weight_from_path (src/Geometry.jl:1083-1093)
+__device__ __forceinline__ Dd decay_g(double mass, double ctau, Dd L, Dd Eavg) {
+  Dd g = dd(1.0) + Eavg / mass;
+  Dd b = dsqrt(dmax(dd(1.0) - dd(1.0) / (g * g), dd(1e-12)));
+  return dexp(-L / (b * g * dd(ctau)));
+}
+
+struct DirectParams {
+  TabView tab;
+  int rock, air;
+  double thickness, rho, elevation, H, mass, ctau;
+  long n;
+  const double *E, *q, *w;
+  double *contrib, *dcontrib;
+};
+
+__global__ void __launch_bounds__(128) direct_kernel(DirectParams P) {
+  const TabView& tv = P.tab;
+  const double el = P.elevation * (kPi / 180.0);
+  const double c = cos(kPi / 2 - el);  // cos(zenith) = sin(elevation)
+  const double cs = fmax(fabs(c), 0.01);
+  // compute_air_grammage (src/Geometry.jl:1043-1055)
+  const double Xa =
+      fmax((1.205 * 12e3 / cs) * (exp(-P.thickness / 12e3) - exp(-P.H / 12e3)), 0.0);
+  const double cst = cos_theta_star(c), cs129 = pow(cst, 1.29);
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < P.n; i += long(gridDim.x) * blockDim.x) {
+    const Dd rho = dd(P.rho, 1.0);
+    const Dd E0 = dd(P.E[i]);
+    const Dd Xr = dd(P.thickness / cs) * rho;
+    const Dd E1 = energy_g(tv, P.rock, range_g(tv, P.rock, E0) + Xr);
+    double f = 0.0, df = 0.0;
+    if (E1.v < 1e12 && isfinite(E1.v)) {
+      const Dd wr = stop_g(tv, P.rock, E1) / stop_g(tv, P.rock, E0);
+      const Dd dr = decay_g(P.mass, P.ctau, dd(P.thickness / cs), (E0 + E1) / 2.0);
+      const Dd E2 = energy_g(tv, P.air, range_g(tv, P.air, E1) + dd(Xa));
+      if (E2.v < 1e12 && isfinite(E2.v)) {
+        const Dd wa = stop_g(tv, P.air, E2) / stop_g(tv, P.air, E1);
+        const Dd da = decay_g(P.mass, P.ctau, dd((P.H - P.thickness) / cs), (E1 + E2) / 2.0);
+        double dlogF;
+        const double F = gccly_flux(cst, cs129, E2.v, P.q[i], &dlogF);
+        const Dd wgt = wr * dr * wa * da;
+        f = wgt.v * F;
+        df = wgt.d * F + wgt.v * F * dlogF * E2.d;
+      }
+    }
+    P.contrib[i] = P.w[i] * f;
+    if (P.dcontrib) P.dcontrib[i] = P.w[i] * df;
+  }
+}
+
 static int setup(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params* p, CsdaParams& P) {
   if (!ctx || !ph || !p) return fail(ctx, DP_ERR_ARG, "null argument");
   int rock = p->rock_material, air = p->air_material;
@@ -568,6 +634,50 @@ int dp_csda_flux_samples(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params* 
   DP_CHECK_CUDA(ctx, cudaMemcpyAsync(contrib, dc, nb, cudaMemcpyDeviceToHost, ctx->stream));
   if (dcontrib) DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dcontrib, dd_, nb, cudaMemcpyDeviceToHost, ctx->stream));
   if (steps) DP_CHECK_CUDA(ctx, cudaMemcpyAsync(steps, ds, size_t(n) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  DP_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return DP_OK;
+}
+
+int dp_csda_direct_samples(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params* p, long n,
+                           const double* E, const double* q, const double* w, double* contrib,
+                           double* dcontrib) {
+  CsdaParams S;
+  int rc = setup(ctx, ph, p, S);
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && (!E || !q || !w || !contrib))) return fail(ctx, DP_ERR_ARG, "bad sample arrays");
+  if (n == 0) return DP_OK;
+  DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  size_t nb = size_t(n) * sizeof(double);
+  char* s = static_cast<char*>(scratch(ctx, 5 * nb));
+  if (!s) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
+  double *dE = (double*)s, *dq = dE + n, *dw = dq + n, *dc = dw + n, *dd_ = dc + n;
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dE, E, nb, cudaMemcpyHostToDevice, ctx->stream));
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dq, q, nb, cudaMemcpyHostToDevice, ctx->stream));
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dw, w, nb, cudaMemcpyHostToDevice, ctx->stream));
+  DirectParams P{};
+  P.tab = ph->view;
+  P.rock = S.rock;
+  P.air = S.air;
+  P.thickness = p->rock_thickness;
+  P.rho = p->rock_density;
+  P.elevation = p->elevation;
+  P.H = p->primary_altitude > 0.0 ? p->primary_altitude : 3e4;
+  P.mass = ph->settings.mass;
+  P.ctau = ph->settings.ctau;
+  P.n = n;
+  P.E = dE;
+  P.q = dq;
+  P.w = dw;
+  P.contrib = dc;
+  P.dcontrib = dcontrib ? dd_ : nullptr;
+  long blocks = std::min((n + 127) / 128, 152L * 16);
+  timed_begin(ctx);
+  direct_kernel<<<int(blocks), 128, 0, ctx->stream>>>(P);
+  DP_CHECK_CUDA(ctx, cudaGetLastError());
+  ++ctx->launches;
+  timed_end(ctx, "csda_direct");
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(contrib, dc, nb, cudaMemcpyDeviceToHost, ctx->stream));
+  if (dcontrib) DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dcontrib, dd_, nb, cudaMemcpyDeviceToHost, ctx->stream));
   DP_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return DP_OK;
 }

@@ -278,6 +278,47 @@ def compute_flux_gradient(physics, rock_density, rock_thickness, elevation, ener
     return float(c[0]), float(d[0])
 
 
+def csda_direct_samples(physics, energy, charge, weight, *, rock_thickness, rock_density,
+                        elevation, primary_altitude=PRIMARY_ALTITUDE, rock_material=None,
+                        air_material=None):
+    """compute_flux_csda_direct (src/Geometry.jl:1126-1209) per sample:
+    (w*flux, w*d flux/d rho) arrays.  Materials are 1-based (default
+    StandardRock and Air)."""
+    E, q, w = _f64(energy), _f64(charge), _f64(weight)
+    p = _mc_params(physics, rock_thickness, rock_density, elevation, 1.0, 1.0, len(E), False, 0,
+                   False, False, 100.0, None, primary_altitude)
+    if rock_material is not None:
+        p.rock_material = int(rock_material) - 1
+    if air_material is not None:
+        p.air_material = int(air_material) - 1
+    c, d = np.zeros(len(E)), np.zeros(len(E))
+    check(load().dp_csda_direct_samples(physics.ctx.h, physics.h, C.byref(p), len(E), _ptr(E),
+                                        _ptr(q), _ptr(w), _ptr(c), _ptr(d)), physics.ctx.h)
+    return c, d
+
+
+def compute_flux_csda_direct(physics, rock_material, air_material, rock_density, rock_thickness,
+                             elevation, energy_initial, charge, *,
+                             primary_altitude=PRIMARY_ALTITUDE):
+    """compute_flux_csda_direct (src/Geometry.jl:1126-1209): the flux of one
+    sample (1-based materials)."""
+    c, _ = csda_direct_samples(physics, [energy_initial], [charge], [1.0],
+                               rock_thickness=rock_thickness, rock_density=rock_density,
+                               elevation=elevation, primary_altitude=primary_altitude,
+                               rock_material=rock_material, air_material=air_material)
+    return float(c[0])
+
+
+def compute_flux_gradient_csda(physics, rock_density, rock_thickness, elevation, energy_final,
+                               charge):
+    """compute_flux_gradient_csda (src/Geometry.jl:1253-1276): (flux, d flux/d rho)
+    of the closed-form CSDA flux (StandardRock and Air)."""
+    c, d = csda_direct_samples(physics, [energy_final], [charge], [1.0],
+                               rock_thickness=rock_thickness, rock_density=rock_density,
+                               elevation=elevation)
+    return float(c[0]), float(d[0])
+
+
 # ----------------------------------------------------------------- stochastic MC
 class MaterialMixture:
     """A prepared propagation medium: one material or a runtime mixture with
@@ -406,6 +447,12 @@ from .directional import (CellSegment, DirBatch, DirectionalPath, DirMedia,  # n
                           get_csda_correction, get_csda_material_correction,
                           mc_cell_mixture_and_density, sample_energy_set, set_csda_correction,
                           set_csda_material_correction)
+
+
+from .inverse import (EdgePrior, SmoothnessPrior, apply_laplacian_smoothing,  # noqa: E402
+                      edge_gradient, edge_hessian, gauss_newton_reconstruct,
+                      gradient_descent_reconstruct, laplacian_gradient, make_csda_operator,
+                      mlem_reconstruct, mse, prior_value, rmse, sart_reconstruct)
 
 
 # ----------------------------------------------------------------- tomography

@@ -152,6 +152,7 @@ PROTOTYPES = {
     "dp_csda_flux_samples_dev": (_I, [_P, _P, C.POINTER(DpMcParams), _L, _VP, _VP, _VP, _VP,
                                       _VP, _VP]),
     "dp_mc_samples": (_I, [_P, C.POINTER(DpMcParams), _L, _VP, _VP, _VP]),
+    "dp_csda_direct_samples": (_I, [_P, _P, C.POINTER(DpMcParams), _L, _VP, _VP, _VP, _VP, _VP]),
     "dp_mixture_prepare": (_I, [_P, _P, _I, _VP, _VP, C.POINTER(_P)]),
     "dp_mixture_free": (_I, [_P]),
     "dp_mixture_kernel": (_I, [_P, _I, _VP, _I, C.POINTER(_I), C.POINTER(_D)]),

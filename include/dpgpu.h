@@ -213,6 +213,15 @@ int dp_csda_flux_samples_dev(dp_ctx* ctx, const dp_physics* phys, const dp_mc_pa
                              long n, const double* energy, const double* charge,
                              const double* weight, double* contrib, double* dcontrib,
                              int32_t* steps);
+/* compute_flux_csda_direct (src/Geometry.jl:1126-1209): the two-layer CSDA
+ * flux in closed form (one range inversion per layer, closed-form air
+ * grammage, decay at the mean energy of each layer), as used by
+ * compute_flux_differentiable_csda / compute_flux_gradient_csda
+ * (:1220-1280): contrib[i] = w[i]*flux_i, dcontrib[i] = w[i]*d flux_i/d rho
+ * (optional).  Geometry, materials and primary altitude from p.  Host pointers. */
+int dp_csda_direct_samples(dp_ctx* ctx, const dp_physics* phys, const dp_mc_params* p, long n,
+                           const double* energy, const double* charge, const double* weight,
+                           double* contrib, double* dcontrib);
 /* Philox samples exactly as dp_backward_mc draws them (log-uniform energy,
  * +-1 charge, weight 2*E*log(Emax/Emin)), for parity checks.  Host pointers. */
 int dp_mc_samples(dp_ctx* ctx, const dp_mc_params* p, long n, double* energy,
