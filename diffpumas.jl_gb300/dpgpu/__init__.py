@@ -439,7 +439,8 @@ def backward_mc_batch(physics, los, *, rock, air, seed=42, straggling=True, scat
 
 from .directional import (CellSegment, DirBatch, DirectionalPath, DirMedia,  # noqa: E402
                           EnergySample,
-                          CsdaBatch, MaterialConfig, SiteConfig,
+                          CsdaBatch, MaterialConfig, SiteConfig, VoxelVolume, flat_surface,
+                          precompute_paths, trace_path,
                           assemble_forward_and_jacobian,
                           build_cell_properties_for_mc, compute_directional_flux_csda,
                           compute_directional_flux_mc, csda_flux_batch,

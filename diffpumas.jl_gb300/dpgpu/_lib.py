@@ -96,6 +96,11 @@ class DpCsdaBatch(C.Structure):
                 ("energy", C.c_void_p), ("charge", C.c_void_p), ("weight", C.c_void_p)]
 
 
+class DpVoxelVolume(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("x_edges", C.c_void_p),
+                ("y_edges", C.c_void_p), ("z_edges", C.c_void_p)]
+
+
 class DpSolveParams(C.Structure):
     _fields_ = [("method", C.c_int), ("n_iter", C.c_int), ("cg_iter", C.c_int),
                 ("precision", C.c_int), ("relaxation", C.c_double), ("lm_damping", C.c_double),
@@ -165,6 +170,8 @@ PROTOTYPES = {
     "dp_dir_csda_dev": (_I, [_P, _P, C.POINTER(DpCsdaConfig), C.POINTER(DpCsdaBatch), _L, _VP,
                              _VP, _VP, _VP, _I]),
     "dp_dir_media_create": (_I, [_P, _P, _I, C.POINTER(_P), C.POINTER(_P)]),
+    "dp_voxel_trace": (_I, [_P, C.POINTER(DpVoxelVolume), _L, _VP, _VP, _VP, _VP, _VP, _VP,
+                            C.c_int64, _VP, _VP]),
     "dp_dir_media_free": (_I, [_P]),
     "dp_dir_mc": (_I, [_P, _P, _P, C.POINTER(DpDirBatch), C.POINTER(DpMcConfig), _VP, _VP, _VP,
                        _VP]),

@@ -436,3 +436,76 @@ def assemble_forward_and_jacobian(physics, shallow_flags, matcfg, site, paths, w
     J.data[~np.isfinite(J.data)] = 0.0
     J.eliminate_zeros()
     return flux, J
+
+
+# ------------------------------------------------------------------ voxel paths
+class VoxelVolume:
+    """A voxel volume (examples/lvd_tomography.jl:181-187): increasing cell
+    edges along x, y and z (metres, the detector at the origin), cells x
+    fastest."""
+
+    def __init__(self, x_edges, y_edges, z_edges, shallow_mask=None):
+        self.x_edges, self.y_edges, self.z_edges = (np.ascontiguousarray(e, np.float64)
+                                                    for e in (x_edges, y_edges, z_edges))
+        self.nx, self.ny, self.nz = len(self.x_edges) - 1, len(self.y_edges) - 1, len(self.z_edges) - 1
+        n = self.nx * self.ny * self.nz
+        self.shallow_mask = np.zeros(n, bool) if shallow_mask is None else np.asarray(shallow_mask, bool)
+
+    @property
+    def n_cells(self):
+        return self.nx * self.ny * self.nz
+
+
+def flat_surface(height):
+    """A flat surface `height` metres above the detector, in the role of
+    ray_surface_exit_distance: (slant distance, valid, exit z)."""
+    def surface(zenith, azimuth):
+        c = math.cos(math.radians(zenith))
+        if c <= 0.0:
+            return float("nan"), False, float("nan")
+        return height / c, True, float(height)
+    return surface
+
+
+def precompute_paths(volume, zeniths, azimuths, surface, ctx=None):
+    """DirectionalPath of every (zenith, azimuth) pair, zeniths outer
+    (examples/lvd_tomography.jl:738-779, 835-861): the reference's march
+    through the volume, cut at the surface exit that `surface(zenith,
+    azimuth) -> (slant distance, valid, exit z)` gives (flat_surface(h) for a
+    flat overburden)."""
+    from ._lib import DpVoxelVolume
+    from . import _ptr
+    h = ctx.h if ctx is not None else None  # host work: no device context needed
+    pairs = [(float(t), float(p)) for t in zeniths for p in azimuths]
+    n = len(pairs)
+    zen = np.array([t for t, _ in pairs])
+    az = np.array([p for _, p in pairs])
+    surf = [surface(t, p) for t, p in pairs]
+    dist = np.array([s[0] if s[1] else float("nan") for s in surf])
+    V = DpVoxelVolume(volume.nx, volume.ny, volume.nz, volume.x_edges.ctypes.data,
+                      volume.y_edges.ctypes.data, volume.z_edges.ctypes.data)
+    seg_ptr = np.zeros(n + 1, np.int64)
+    trav, rem = np.zeros(max(n, 1)), np.zeros(max(n, 1))
+    lib = load()
+    check(lib.dp_voxel_trace(h, C.byref(V), n, _ptr(zen), _ptr(az), _ptr(dist), _ptr(seg_ptr),
+                             None, None, 0, None, None), h)
+    m = int(seg_ptr[-1])
+    cells, lens = np.zeros(max(m, 1), np.int32), np.zeros(max(m, 1))
+    check(lib.dp_voxel_trace(h, C.byref(V), n, _ptr(zen), _ptr(az), _ptr(dist), _ptr(seg_ptr),
+                             _ptr(cells), _ptr(lens), m, _ptr(trav), _ptr(rem)), h)
+    out = []
+    for d, (t, p) in enumerate(pairs):
+        if not surf[d][1] or not math.isfinite(dist[d]):
+            out.append(DirectionalPath(t, p, [], float("nan"), float("nan"), float("nan"),
+                                       float("nan"), False))
+            continue
+        segs = [CellSegment(int(c) + 1, float(l)) for c, l in
+                zip(cells[seg_ptr[d]:seg_ptr[d + 1]], lens[seg_ptr[d]:seg_ptr[d + 1]])]
+        out.append(DirectionalPath(t, p, segs, float(trav[d]), float(dist[d]), float(rem[d]),
+                                   float(surf[d][2]), True))
+    return out
+
+
+def trace_path(volume, zenith, azimuth, surface):
+    """trace_path(::VoxelVolume) (examples/lvd_tomography.jl:738-779)."""
+    return precompute_paths(volume, [zenith], [azimuth], surface)[0]

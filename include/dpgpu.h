@@ -365,6 +365,26 @@ int dp_dir_mc_dev(dp_ctx* ctx, const dp_physics* phys, dp_dir_media* media,
                   const dp_dir_batch* batch, long total_samples, const dp_mc_config* cfg,
                   dp_los_result* out);
 
+/* ------------------------------------------------------------ voxel paths
+ * trace_path(::VoxelVolume) / precompute_paths (examples/lvd_tomography.jl:
+ * 583-627, 738-779, 835-861): the straight path from the detector (origin)
+ * along (zenith, azimuth) through a voxel volume with the reference's
+ * POINT_EPS march, cut at the slant distance of the surface exit.  Edges are
+ * increasing (n + 1 per axis), cells x fastest.  Host arrays; a call with
+ * seg_cell = seg_length = NULL only counts (seg_ptr[n_dirs]).  A direction
+ * with surface_distance <= 0 or NaN is invalid (no segments, NaN outputs).
+ * ctx may be NULL (no device work; it only receives the error message). */
+typedef struct {
+  int nx, ny, nz;
+  const double* x_edges;
+  const double* y_edges;
+  const double* z_edges;
+} dp_voxel_volume;
+int dp_voxel_trace(dp_ctx* ctx, const dp_voxel_volume* volume, long n_dirs, const double* zenith,
+                   const double* azimuth, const double* surface_distance, int64_t* seg_ptr,
+                   int32_t* seg_cell, double* seg_length, int64_t seg_cap, double* traveled,
+                   double* remaining_rock);
+
 /* ------------------------------------------------ water-fraction CSDA model
  * compute_directional_flux_csda (src/Tomography.jl:667-727),
  * directional_flux_and_grad_csda (:736-762) and assemble_forward_and_jacobian
