@@ -101,6 +101,141 @@ def test_gauss_newton_recovers_linear_model(dp):
     assert dp.rmse(w, w_true) < 1e-6
 
 
+# ---------------------------------------------------------------- the reference's
+# known answers (test/test_inverse_solver.jl:4-112), graphs 0-based here
+def test_prior_graph_and_curvature(dp):
+    graph = [[1, 1, 0], [], [1]]
+    smooth = dp.SmoothnessPrior(graph, 2.3)
+    assert smooth.neighbors == [[1], [0, 2], [1]]
+    edge = dp.EdgePrior(graph, 2.3, 0.2)
+    assert edge.neighbors == smooth.neighbors
+    w, h = np.array([0.1, 0.4, 0.8]), 1e-6
+    from dpgpu.inverse import _prior_hessian
+    for prior, grad in ((smooth, dp.laplacian_gradient), (edge, dp.edge_gradient)):
+        fd = [(dp.prior_value(prior, w + h * e) - dp.prior_value(prior, w - h * e)) / (2 * h)
+              for e in np.eye(3)]
+        np.testing.assert_allclose(grad(prior, w), fd, rtol=1e-8, atol=1e-9)
+    H = _prior_hessian(smooth, w).toarray()
+    Hfd = np.column_stack([(dp.laplacian_gradient(smooth, w + h * e) -
+                            dp.laplacian_gradient(smooth, w - h * e)) / (2 * h) for e in np.eye(3)])
+    np.testing.assert_allclose(H, Hfd, rtol=1e-8, atol=1e-9)
+    np.testing.assert_allclose(H @ np.ones(3), 0.0, atol=1e-12)
+    assert np.linalg.eigvalsh(H).min() >= -1e-10
+    # Julia's array isapprox is norm-wise: an exact 0 matches a last-bit residue
+    np.testing.assert_allclose(_prior_hessian(edge, w) @ w, dp.edge_gradient(edge, w), atol=1e-12)
+
+
+def _identity(v):
+    return np.array(v, float), sp.identity(len(v), format="csr")
+
+
+def test_gauss_newton_known_answers(dp):
+    # from a perfect data fit the prior still moves the field to the MAP point
+    prior = dp.SmoothnessPrior([[1], [0]], 10.0)
+    fit, hist = dp.gauss_newton_reconstruct(_identity, [1.0, 0.0], w0=[1.0, 0.0], prior=prior,
+                                            n_iter=12, box=(0.0, 1.0))
+    np.testing.assert_allclose(fit, [21 / 41, 20 / 41], atol=1e-6)
+    assert np.linalg.norm(fit - [1.0, 0.0]) > 0.1
+    assert 0.5 * np.linalg.norm(fit - [1.0, 0.0]) ** 2 + dp.prior_value(prior, fit) < \
+        dp.prior_value(prior, [1.0, 0.0])
+    assert hist[0] == 0 and hist[-1] > 0
+    # a fixed neighbour contributes curvature but does not move
+    boundary = lambda v: (np.array([v[0]]), sp.csr_matrix([[1.0, 0.0]]))
+    fixed, _ = dp.gauss_newton_reconstruct(boundary, [0.0], w0=[0.1, 0.8],
+                                           prior=dp.SmoothnessPrior([[1], [0]], 2.0),
+                                           free=[True, False], n_iter=12)
+    assert fixed[1] == 0.8 and fixed[0] == pytest.approx(0.64, abs=1e-6)
+    nonlinear = lambda v: (np.array([math.exp(v[0]) + 0.3 * v[1], 0.4 * v[0] + math.exp(v[1])]),
+                           sp.csr_matrix([[math.exp(v[0]), 0.3], [0.4, math.exp(v[1])]]))
+    fit, _ = dp.gauss_newton_reconstruct(nonlinear, [1.3, 1.6], w0=[0.1, 0.4], weights=[2.0, 5.0],
+                                         prior=dp.SmoothnessPrior([[1], [0]], 0.7),
+                                         free=[True, False], n_iter=30)
+    assert fit[1] == 0.4 and fit[0] == pytest.approx(0.24287925833166624, abs=2e-6)
+    # every coordinate fixed: one model call, the start returned
+    calls = [0]
+
+    def counted(v):
+        calls[0] += 1
+        return _identity(v)
+    allfixed, allhist = dp.gauss_newton_reconstruct(counted, [0.0, 0.0], w0=[0.2, 0.8],
+                                                    free=[False, False], n_iter=12)
+    assert list(allfixed) == [0.2, 0.8] and len(allhist) == 1 and calls[0] == 1
+    with pytest.raises(ValueError):
+        dp.gauss_newton_reconstruct(_identity, np.zeros(2), w0=np.zeros(2), free=[True])
+    # the affine tangent at w0 when not relinearising
+    affine = lambda v: (np.array([2 + 3 * v[0]]), sp.csr_matrix([[3.0]]))
+    frozen, _ = dp.gauss_newton_reconstruct(affine, [3.5], w0=[0.1], relinearize=False,
+                                            n_iter=12)
+    assert frozen[0] == pytest.approx(0.5, abs=1e-7)
+
+
+def test_gradient_descent_known_answers(dp):
+    calls = [0]
+
+    def nonlinear(v):
+        calls[0] += 1
+        return np.array([2 + v[0] + v[0] ** 2]), sp.csr_matrix([[1 + 2 * v[0]]])
+    gd, _ = dp.gradient_descent_reconstruct(nonlinear, [2.8], w0=[0.2], relinearize=False,
+                                            optimizer="gd", n_iter=150, lr=0.1)
+    assert gd[0] == pytest.approx(0.6, abs=1e-7) and calls[0] == 1
+    step_model = lambda v: (np.array(v, float), sp.csr_matrix([[1.0]]))
+    fit, h = dp.gradient_descent_reconstruct(step_model, [1.0], w0=[0.0], optimizer="gd",
+                                             n_iter=1, lr=0.1)
+    assert h[-1] == pytest.approx(np.linalg.norm(fit - [1.0]))
+    flat_calls = [0]
+
+    def flat(v):
+        flat_calls[0] += 1
+        return np.array([0.0]), sp.csr_matrix((1, 5))
+    prior = dp.SmoothnessPrior([[1], [0, 2], [1, 3], [2, 4], [3]], 1.0)
+    start = np.array([0.0, 0.1, 0.6, 0.3, 0.9])
+    smoothed, _ = dp.gradient_descent_reconstruct(flat, [0.0], w0=start, prior=prior,
+                                                  optimizer="pgd", n_iter=50, lr=1.0)
+    assert flat_calls[0] > 3
+    assert dp.prior_value(prior, smoothed) < 1e-6 * dp.prior_value(prior, start)
+    affine = lambda v: (np.array([2 + 3 * v[0]]), sp.csr_matrix([[3.0]]))
+    _, h = dp.gradient_descent_reconstruct(affine, [3.5], w0=[-2.0], optimizer="pgd", n_iter=4,
+                                           lr=1.0)
+    assert abs(h[-1]) < 1e-5
+
+
+def test_gauss_newton_prediction_only_line_search(dp):
+    """test/test_inverse_solver.jl:76-112."""
+    target = np.array([math.exp(8 * 0.65)])
+    counts = {"ref": 0, "fast": 0, "pred": 0}
+    primal = lambda v: np.array([math.exp(8 * v[0])])
+
+    def make(key):
+        def model(v):
+            counts[key] += 1
+            return primal(v), sp.csr_matrix([[8 * math.exp(8 * v[0])]])
+        return model
+
+    def predict(v):
+        counts["pred"] += 1
+        return primal(v)
+    full, fh = dp.gauss_newton_reconstruct(make("ref"), target, w0=[0.01], n_iter=20,
+                                           box=(0.0, 1.0))
+    cheap, ch = dp.gauss_newton_reconstruct(make("fast"), target, w0=[0.01], n_iter=20,
+                                            box=(0.0, 1.0), predict_only=predict)
+    np.testing.assert_allclose(cheap, full, rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(ch, fh, rtol=1e-12, atol=1e-12)
+    assert cheap[0] == pytest.approx(0.65, abs=1e-8)
+    assert counts["fast"] < counts["ref"] and counts["pred"] > 0
+    # an inaccurate prediction may not authorise an objective increase
+    checked, hist = dp.gauss_newton_reconstruct(make("fast"), target, w0=[0.01], n_iter=8,
+                                                box=(0.0, 1.0), predict_only=lambda v: target)
+    assert np.all(np.diff(hist) <= 1e-10)
+    assert np.linalg.norm(primal(checked) - target) < np.linalg.norm(primal([0.01]) - target)
+    zero_calls = [0]
+
+    def zero_model(v):
+        zero_calls[0] += 1
+        return np.array(v, float), sp.csr_matrix([[1.0]])
+    sat, hist = dp.gauss_newton_reconstruct(zero_model, [2.0], w0=[0.9], n_iter=8)
+    assert list(sat) == [0.9] and zero_calls[0] == 1 and len(hist) == 2
+
+
 @pytest.mark.gpu
 def test_gauss_newton_on_the_device_operator(dp):
     """make_csda_operator (src/Tomography_inverse.jl:614-626) on the
