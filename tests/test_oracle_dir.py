@@ -126,3 +126,26 @@ def test_cell_mixture_and_density():
     (m, f), rho = dpgpu.mc_cell_mixture_and_density(0.2, True, cfg)
     assert m == (4, 1, 3) and f == pytest.approx((0.4, 0.4, 0.2))
     assert rho == pytest.approx(1.0 / (0.4 / 1800.0 + 0.4 / 2650.0 + 0.2 / 1000.0), rel=1e-15)
+
+
+def test_shallow_porous_recipe_and_guards():
+    """test/test_shallow_mixture.jl: the shallow porous cell is 1/2 (1 - w)
+    rock, w water, 1/2 (1 - w) porous with harmonic density, down to w = 0
+    (the pure-rock shortcut belongs to the ordinary branch); either guard
+    (no porous material, no porous top thickness) or a deep cell disables it."""
+    import dpgpu
+    cfg = dpgpu.MaterialConfig(1, 2, 3, 3, 2700.0, 1000.0, 1500.0, 50.0)
+    for w in (0.0, 5e-13, 1e-12, 2e-12, 1e-8, 0.3, 1.0):
+        (mats, fr), rho = dpgpu.mc_cell_mixture_and_density(w, True, cfg)
+        share = dict(zip(mats, fr))
+        expected = {1: 0.5 * (1 - w), 2: w, 3: 0.5 * (1 - w)}  # rock, water, porous
+        assert share == pytest.approx(expected, rel=2e-15, abs=0)
+        assert rho == pytest.approx(1 / (0.5 * (1 - w) / 2700 + w / 1000 + 0.5 * (1 - w) / 1500),
+                                    rel=2e-15)
+    for shallow, c in ((False, cfg), (True, cfg._replace(porous_material=0)),
+                       (True, cfg._replace(porous_top_thickness=0.0))):
+        for w in (0.0, 5e-13, 0.3):
+            (mats, fr), rho = dpgpu.mc_cell_mixture_and_density(w, shallow, c)
+            ew = 0.0 if w <= 1e-12 else w
+            assert rho == pytest.approx(1 / ((1 - ew) / 2700 + ew / 1000), rel=2e-15)
+            assert 3 not in mats
