@@ -228,7 +228,7 @@ def setup_c2(dp, torch, dev, precision="mixed", scale=1.0):
 
     kernel = ("mc_init+mc_mixed_lo+mc_mixed_hi+mc_finish+mc_tally" if precision == "mixed"
               else "mc_init+mc_fp64_lo+mc_fp64_hi+mc_finish+mc_tally")
-    info = {"units": n, "unit": "samples/s", "kernel": kernel,
+    info = {"units": n, "unit": "samples/s", "kernel": kernel, "family": "mc",
             # per history: contribution (8 B) and status (4 B) written by the
             # transport kernel and read back by the tally
             "alg_bytes": n * 24,
@@ -301,7 +301,7 @@ def setup_c4(dp, torch, dev, precision="mixed", scale=1.0):
 
     kernel = "mc_init+mc_mixed_lo+mc_mixed_hi+mc_finish+csda_mc32+mc_tally" if precision == "mixed" \
         else "mc_init+mc_fp64_lo+mc_fp64_hi+mc_finish+csda_mc+mc_tally"
-    info = {"units": total, "unit": "samples/s", "kernel": kernel,
+    info = {"units": total, "unit": "samples/s", "kernel": kernel, "family": "mc",
             # per history: contribution and status written and read back,
             # CSDA contribution and derivative written and read back
             "alg_bytes": total * (24 + 32), "traffic": None,
@@ -420,7 +420,7 @@ def setup_dir(dp, torch, dev, precision="mixed", scale=1.0):
             b.run_dev(2028, precision="fp64")
 
     name = "mixed" if precision == "mixed" else "fp64"
-    info = {"units": batch.total, "unit": "samples/s",
+    info = {"units": batch.total, "unit": "samples/s", "family": "dir",
             "kernel": f"dir_init+dir_{name}_lo+dir_{name}_hi+dir_finish+mc_tally",
             # per history: contribution and status written and read back
             "alg_bytes": batch.total * 24, "traffic": None,
@@ -520,6 +520,17 @@ def run_gpu(args):
     step_dev, step_e2e, plain_dev, info, phys = setup(dp, torch, dev, **kw)
     if args.scale != 1.0:
         info["config"]["scale"] = args.scale
+    fam = info.get("family")
+    if fam and info["config"].get("precision") == "mixed":
+        # CTA size of the persistent transport kernels: dp_autotune over the
+        # compiled sizes on this very step (untimed), or the size given
+        if args.mc_threads == "auto" and not args.profile_run:
+            best, ms_each = dp.autotune(phys, fam, "mixed", step_dev)
+            info["config"]["cta_threads"] = best
+            info["config"]["autotune_ms"] = {str(k): round(v, 2) for k, v in ms_each.items()}
+        elif args.mc_threads != "auto":
+            dp.set_mc_threads(phys, fam, "mixed", int(args.mc_threads))
+            info["config"]["cta_threads"] = int(args.mc_threads)
     if args.profile_run:
         # capture mode for the profiler: warm-up steps and one step, nothing else
         for _ in range(args.warmup + 1):
@@ -804,6 +815,10 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain one-launch-per-ray form")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="c2/c4: fraction of the histories / lines of sight (profiling captures)")
+    ap.add_argument("--mc-threads", default="auto",
+                    help="c2/c4/dir: CTA size of the transport kernels (1024, 768, 512) or "
+                         "'auto' (dp_autotune before the warm-up; the default size, 1024, "
+                         "under --profile-run)")
     ap.add_argument("--profile-run", action="store_true",
                     help="only warm-up steps and one step (for ncu captures); prints nothing")
     args = ap.parse_args()

@@ -674,7 +674,6 @@ int dp_csda_direct_samples(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params
   timed_begin(ctx);
   direct_kernel<<<int(blocks), 128, 0, ctx->stream>>>(P);
   DP_CHECK_CUDA(ctx, cudaGetLastError());
-  ++ctx->launches;
   timed_end(ctx, "csda_direct");
   DP_CHECK_CUDA(ctx, cudaMemcpyAsync(contrib, dc, nb, cudaMemcpyDeviceToHost, ctx->stream));
   if (dcontrib) DP_CHECK_CUDA(ctx, cudaMemcpyAsync(dcontrib, dd_, nb, cudaMemcpyDeviceToHost, ctx->stream));

@@ -389,8 +389,8 @@ __host__ __device__ inline uint32_t dir_coop_offset(const DirParams& P) {
   return dir_desc_offset<R>(P) + (uint32_t(P.n_media * sizeof(Med<R>)) + 15u) / 16u * 16u;
 }
 
-template <class R, int PHASE>
-__global__ void __launch_bounds__(KCfg<R>::threads, 1) dir_kernel(const __grid_constant__ DirParams P) {
+template <class R, int PHASE, int T>
+__global__ void __launch_bounds__(T, 1) dir_kernel(const __grid_constant__ DirParams P) {
   extern __shared__ __align__(16) unsigned char smem[];
   const uint32_t tables = uint32_t(P.n_staged) * P.lay.med_bytes;
   if (tables && !stage_blob(smem + 16, P.blob, tables, reinterpret_cast<uint64_t*>(smem))) {
@@ -474,29 +474,28 @@ int dir_device(dp_ctx* ctx, dp_dir_media* M, int precision, dp_dir_media::Dev** 
   return DP_OK;
 }
 
-template <class R, int PHASE>
+template <class R, int PHASE, int T>
 int dir_phase(dp_ctx* ctx, const DirParams& P, size_t smem, long max_blocks) {
-  const int threads = KCfg<R>::threads;
-  DP_CHECK_CUDA(ctx, cudaFuncSetAttribute(dir_kernel<R, PHASE>,
+  const int threads = T;
+  DP_CHECK_CUDA(ctx, cudaFuncSetAttribute(dir_kernel<R, PHASE, T>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   int per_sm = 0, n_sm = 0;
-  DP_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dir_kernel<R, PHASE>,
+  DP_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dir_kernel<R, PHASE, T>,
                                                                    threads, smem));
   DP_CHECK_CUDA(ctx, cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, ctx->device));
   if (per_sm < 1) return fail(ctx, DP_ERR_CUDA, "fixed-path MC kernel does not fit on a multiprocessor");
   long blocks = std::max(1L, std::min(long(per_sm) * n_sm, max_blocks));
   timed_begin(ctx);
-  dir_kernel<R, PHASE><<<int(blocks), threads, smem, ctx->stream>>>(P);
+  dir_kernel<R, PHASE, T><<<int(blocks), threads, smem, ctx->stream>>>(P);
   DP_CHECK_CUDA(ctx, cudaGetLastError());
-  ++ctx->launches;
   timed_end(ctx, sizeof(R) == 4 ? (PHASE ? "dir_mixed_hi" : "dir_mixed_lo")
                                 : (PHASE ? "dir_fp64_hi" : "dir_fp64_lo"));
   return DP_OK;
 }
 
-template <class R>
-int dir_launch(dp_ctx* ctx, DirParams& P) {
-  const int threads = KCfg<R>::threads;
+template <class R, int T>
+int dir_launch_t(dp_ctx* ctx, DirParams& P) {
+  const int threads = T;
   P.coop_stride = KCfg<R>::coop ? ((kItemsPerElement + 4) * P.coop_nel + 3) / 4 * 4 : 0;
   const size_t coop_bytes = size_t(threads / 32) * P.coop_stride * sizeof(float);
   int dev_smem = 0;
@@ -515,17 +514,21 @@ int dir_launch(dp_ctx* ctx, DirParams& P) {
   timed_begin(ctx);
   dir_init_kernel<R><<<int(rec_blocks), 256, 0, ctx->stream>>>(P);
   DP_CHECK_CUDA(ctx, cudaGetLastError());
-  ++ctx->launches;
   timed_end(ctx, "dir_init");
-  int rc = dir_phase<R, 0>(ctx, P, smem, need);
-  if (!rc) rc = dir_phase<R, 1>(ctx, P, smem, need);
+  int rc = dir_phase<R, 0, T>(ctx, P, smem, need);
+  if (!rc) rc = dir_phase<R, 1, T>(ctx, P, smem, need);
   if (rc) return rc;
   timed_begin(ctx);
   dir_finish_kernel<R><<<int(rec_blocks), 256, 0, ctx->stream>>>(P);
   DP_CHECK_CUDA(ctx, cudaGetLastError());
-  ++ctx->launches;
   timed_end(ctx, "dir_finish");
   return DP_OK;
+}
+
+template <class R>
+int dir_launch(dp_ctx* ctx, DirParams& P) {
+  return with_threads<R>(ctx->mc_threads[DP_KERNEL_DIR][sizeof(R) == 4],
+                         [&](auto t) { return dir_launch_t<R, decltype(t)::value>(ctx, P); });
 }
 
 // Enqueues one run over the batch (device arrays) and the per-direction

@@ -513,8 +513,8 @@ struct SlabGeo {
   }
 };
 
-template <class R, int PHASE>
-__global__ void __launch_bounds__(KCfg<R>::threads, 1) mc_kernel(const __grid_constant__ McParams P) {
+template <class R, int PHASE, int T>
+__global__ void __launch_bounds__(T, 1) mc_kernel(const __grid_constant__ McParams P) {
   extern __shared__ __align__(16) unsigned char smem[];
   const unsigned char* base = P.blob;
   const uint32_t tables = P.staged ? 2 * P.lay.med_bytes : 0;
@@ -784,7 +784,7 @@ int group_tally(dp_ctx* ctx, const double* contrib, const int32_t* status, const
       contrib, status, off, coff, n, max_jobs, csda, dcsda, tp);
   los_tally_kernel<<<int((n + warps_per_block - 1) / warps_per_block), 256, 0, ctx->stream>>>(
       tp, off, coff, los, valid, n, csda ? 1 : 0, sigma_n1, out, bits);
-  ctx->launches += 2;
+  ++ctx->launches;  // the second of the pair (timed_begin counts the first)
   DP_CHECK_CUDA(ctx, cudaGetLastError());
   timed_end(ctx, "mc_tally");
   return DP_OK;
@@ -795,31 +795,31 @@ int group_tally(dp_ctx* ctx, const double* contrib, const int32_t* status, const
 
 namespace {
 
-template <class R, int PHASE>
+template <class R, int PHASE, int T>
 int launch_phase(dp_ctx* ctx, McParams& P, size_t smem, long max_blocks) {
-  const int threads = KCfg<R>::threads;
-  DP_CHECK_CUDA(ctx, cudaFuncSetAttribute(mc_kernel<R, PHASE>,
+  const int threads = T;
+  DP_CHECK_CUDA(ctx, cudaFuncSetAttribute(mc_kernel<R, PHASE, T>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   int per_sm = 0, n_sm = 0;
-  DP_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_kernel<R, PHASE>,
+  DP_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_kernel<R, PHASE, T>,
                                                                    threads, smem));
   DP_CHECK_CUDA(ctx, cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, ctx->device));
   if (per_sm < 1) return fail(ctx, DP_ERR_CUDA, "MC kernel does not fit on a multiprocessor");
   long blocks = std::min(long(per_sm) * n_sm, max_blocks);
   if (blocks < 1) blocks = 1;
   timed_begin(ctx);
-  mc_kernel<R, PHASE><<<int(blocks), threads, smem, ctx->stream>>>(P);
+  mc_kernel<R, PHASE, T><<<int(blocks), threads, smem, ctx->stream>>>(P);
   DP_CHECK_CUDA(ctx, cudaGetLastError());
   timed_end(ctx, sizeof(R) == 4 ? (PHASE ? "mc_mixed_hi" : "mc_mixed_lo")
                                 : (PHASE ? "mc_fp64_hi" : "mc_fp64_lo"));
   return DP_OK;
 }
 
-// Both transport phases; P.queue must hold P.n handoff records and
-// P.counter three zeroed words (set here).
-template <class R>
-int launch_mc(dp_ctx* ctx, McParams& P) {
-  const int threads = KCfg<R>::threads;
+// Both transport phases with CTAs of T threads; P.queue must hold P.n
+// handoff records and P.counter three zeroed words (set here).
+template <class R, int T>
+int launch_mc_t(dp_ctx* ctx, McParams& P) {
+  const int threads = T;
   P.coop_nel = std::max(P.info[0].nel, P.info[1].nel);
   P.coop_stride = KCfg<R>::coop ? ((kItemsPerElement + 4) * P.coop_nel + 3) / 4 * 4 : 0;
   size_t coop_bytes = size_t(threads / 32) * P.coop_stride * sizeof(float);
@@ -836,15 +836,21 @@ int launch_mc(dp_ctx* ctx, McParams& P) {
   mc_init_kernel<R><<<int(rec_blocks), 256, 0, ctx->stream>>>(P);
   DP_CHECK_CUDA(ctx, cudaGetLastError());
   timed_end(ctx, "mc_init");
-  int rc = launch_phase<R, 0>(ctx, P, smem, need);
+  int rc = launch_phase<R, 0, T>(ctx, P, smem, need);
   if (rc) return rc;
-  rc = launch_phase<R, 1>(ctx, P, smem, need);
+  rc = launch_phase<R, 1, T>(ctx, P, smem, need);
   if (rc) return rc;
   timed_begin(ctx);
   mc_finish_kernel<R><<<int(rec_blocks), 256, 0, ctx->stream>>>(P);
   DP_CHECK_CUDA(ctx, cudaGetLastError());
   timed_end(ctx, "mc_finish");
   return DP_OK;
+}
+
+template <class R>
+int launch_mc(dp_ctx* ctx, McParams& P) {
+  return with_threads<R>(ctx->mc_threads[DP_KERNEL_MC][sizeof(R) == 4],
+                         [&](auto t) { return launch_mc_t<R, decltype(t)::value>(ctx, P); });
 }
 
 int run(dp_ctx* ctx, McParams& P, int precision) {
@@ -871,7 +877,84 @@ int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_
                   dp_los_result* d_out, double** contrib_out, int** status_or,
                   int compute_gradient);
 
+namespace {
+// compiled CTA sizes of the persistent transport kernels (with_threads)
+constexpr int kThreadsMixed[] = {1024, 768, 512};
+constexpr int kThreadsFp64[] = {256};
+bool shape_args(int family, int precision) {
+  return (family == DP_KERNEL_MC || family == DP_KERNEL_DIR) &&
+         (precision == DP_PREC_FP64 || precision == DP_PREC_MIXED);
+}
+}  // namespace
+
 extern "C" {
+
+int dp_mc_thread_choices(int precision, int* threads, int cap) {
+  if (precision != DP_PREC_FP64 && precision != DP_PREC_MIXED) return DP_ERR_ARG;
+  const int* list = precision == DP_PREC_MIXED ? kThreadsMixed : kThreadsFp64;
+  const int n = precision == DP_PREC_MIXED ? 3 : 1;
+  for (int i = 0; threads && i < std::min(n, cap); ++i) threads[i] = list[i];
+  return n;
+}
+
+int dp_set_mc_threads(dp_ctx* ctx, int family, int precision, int threads) {
+  if (!ctx || !shape_args(family, precision)) return fail(ctx, DP_ERR_ARG, "bad kernel family or precision");
+  int list[8];
+  const int n = dp_mc_thread_choices(precision, list, 8);
+  if (threads != 0 && std::find(list, list + n, threads) == list + n)
+    return fail(ctx, DP_ERR_ARG, "CTA size not compiled for this precision");
+  ctx->mc_threads[family][precision] = threads;
+  return DP_OK;
+}
+
+int dp_get_mc_threads(const dp_ctx* ctx, int family, int precision, int* threads) {
+  if (!ctx || !threads || !shape_args(family, precision)) return DP_ERR_ARG;
+  const int t = ctx->mc_threads[family][precision];
+  *threads = t ? t : (precision == DP_PREC_MIXED ? kThreadsMixed[0] : kThreadsFp64[0]);
+  return DP_OK;
+}
+
+int dp_autotune(dp_ctx* ctx, int family, int precision, int (*run)(void*), void* user,
+                int* best_threads, double* ms, int cap) {
+  if (!ctx || !run || !shape_args(family, precision)) return fail(ctx, DP_ERR_ARG, "bad autotune arguments");
+  int list[8];
+  const int n = dp_mc_thread_choices(precision, list, 8);
+  const int saved = ctx->mc_threads[family][precision];
+  DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+    if (a) cudaEventDestroy(a);
+    return fail(ctx, DP_ERR_CUDA, "event creation failed");
+  }
+  int best = 0, rc = DP_OK;
+  float best_ms = 0.0f;
+  for (int i = 0; i < n && !rc; ++i) {
+    ctx->mc_threads[family][precision] = list[i];
+    rc = run(user);  // untimed: first launch of this size loads its code
+    if (rc) break;
+    if (cudaEventRecord(a, ctx->stream) != cudaSuccess) rc = fail(ctx, DP_ERR_CUDA, "event record failed");
+    if (!rc) rc = run(user);
+    if (!rc && (cudaEventRecord(b, ctx->stream) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess))
+      rc = fail(ctx, DP_ERR_CUDA, "event wait failed");
+    if (rc) break;
+    float t = 0.0f;
+    cudaEventElapsedTime(&t, a, b);
+    if (ms && i < cap) ms[i] = t;
+    if (!best || t < best_ms) {
+      best = list[i];
+      best_ms = t;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc) {
+    ctx->mc_threads[family][precision] = saved;
+    return rc;
+  }
+  ctx->mc_threads[family][precision] = best;
+  if (best_threads) *best_threads = best;
+  return DP_OK;
+}
 
 int dp_mixture_prepare(dp_ctx* ctx, const dp_physics* ph, int n, const int* mats,
                        const double* fracs, dp_mixture** out) {

@@ -16,23 +16,45 @@
 #pragma once
 #include <cooperative_groups.h>
 
+#include <type_traits>
+
 #include "mc_device.cuh"
 
 namespace dp {
 namespace mc {
 
-// Launch shape per precision: the FP32 transport runs 16 warps per SM
-// sharing one staged copy of the tables and evaluates hard-event DCS sums
-// cooperatively per warp; the FP64 transport (one thread per sum) runs 8.
+// Launch shape per precision: one CTA per SM whose warps share one staged
+// copy of the tables.  The FP32 transport evaluates hard-event DCS sums
+// cooperatively per warp; it is compiled for three CTA sizes that trade
+// registers per thread for warps per SM (1024: at most 64 registers, 32
+// warps; 768: at most 80, 24 warps; 512: 116, 16 warps), chosen per context
+// (dp_set_mc_threads, dp_autotune).  The transport is latency bound, so the
+// most warps win: 1024 threads run the two-layer and fixed-path workloads
+// 1.3-1.4x faster than 512, with 164 bytes of spills.  The FP64 transport
+// (one thread per sum, 255 registers) runs 8 warps.
 template <class R> struct KCfg;
 template <> struct KCfg<float> {
-  static constexpr int threads = 512;
+  static constexpr int threads = 1024;  // default CTA size
   static constexpr bool coop = true;
 };
 template <> struct KCfg<double> {
   static constexpr int threads = 256;
   static constexpr bool coop = false;
 };
+
+// Calls f(std::integral_constant<int, T>{}) with T the compiled CTA size
+// matching `threads` (0 or an unknown size: the default).
+template <class R, class F>
+inline int with_threads(int threads, F&& f) {
+  if constexpr (sizeof(R) == 4) {
+    if (threads == 768) return f(std::integral_constant<int, 768>{});
+    if (threads == 512) return f(std::integral_constant<int, 512>{});
+    return f(std::integral_constant<int, 1024>{});
+  } else {
+    (void)threads;
+    return f(std::integral_constant<int, 256>{});
+  }
+}
 
 // Copies `bytes` (16-byte multiple) from global to shared memory with
 // cp.async.bulk completing on one mbarrier; all threads call it.  Returns

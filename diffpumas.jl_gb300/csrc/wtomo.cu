@@ -216,7 +216,6 @@ int run(dp_ctx* ctx, const dp_physics* ph, const dp_csda_config* c, const dp_csd
   timed_begin(ctx);
   kernel<<<int(blocks), wt::kThreads, smem, ctx->stream>>>(P);
   DP_CHECK_CUDA(ctx, cudaGetLastError());
-  ++ctx->launches;
   timed_end(ctx, mixed ? (jac ? "dir_csda32_grad" : "dir_csda32") : (jac ? "dir_csda_grad" : "dir_csda"));
   return DP_OK;
 }

@@ -62,6 +62,71 @@ def default_context():
         return _default
 
 
+# ----------------------------------------------------------------- launch shapes
+KERNEL_MC, KERNEL_DIR = 0, 1  # two-layer transport, fixed-path transport
+_FAMILY = {"mc": KERNEL_MC, "dir": KERNEL_DIR, KERNEL_MC: KERNEL_MC, KERNEL_DIR: KERNEL_DIR}
+_PRECISION = {"fp64": 0, "mixed": 1, 0: 0, 1: 1}
+
+
+def _ctx_of(obj):
+    """The dp_ctx handle of a Context or of an object holding one (.ctx)."""
+    ctx = obj if isinstance(obj, Context) else getattr(obj, "ctx", None)
+    if not isinstance(ctx, Context):
+        raise TypeError("expected a Context or an object with a .ctx Context")
+    return ctx.h
+
+
+def mc_thread_choices(precision="mixed"):
+    """CTA sizes the persistent transport kernels are compiled for (the
+    first is the default)."""
+    buf = (C.c_int * 8)()
+    n = load().dp_mc_thread_choices(_PRECISION[precision], C.cast(buf, C.c_void_p), 8)
+    check(n if n < 0 else 0)
+    return [buf[i] for i in range(n)]
+
+
+def set_mc_threads(ctx, family, precision, threads):
+    """CTA size of the persistent transport kernels of `family` ("mc" or
+    "dir") at `precision` on this context; 0 restores the default."""
+    h = _ctx_of(ctx)
+    check(load().dp_set_mc_threads(h, _FAMILY[family], _PRECISION[precision], int(threads)), h)
+
+
+def get_mc_threads(ctx, family, precision):
+    h = _ctx_of(ctx)
+    t = C.c_int()
+    check(load().dp_get_mc_threads(h, _FAMILY[family], _PRECISION[precision], C.byref(t)), h)
+    return t.value
+
+
+def autotune(ctx, family, precision, run):
+    """dp_autotune: times run() (the caller's workload on this context) once
+    per compiled CTA size of (family, precision) after an untimed run, keeps
+    the fastest on the context and returns (threads, {threads: ms})."""
+    h = _ctx_of(ctx)
+    lib = load()
+    choices = mc_thread_choices(precision)
+    errors = []
+
+    def cb(_user):
+        try:
+            run()
+            return 0
+        except Exception as e:  # reported after dp_autotune returns
+            errors.append(e)
+            return _lib.DP_ERR_STATE
+
+    fn = _lib.AUTOTUNE_RUN(cb)
+    best = C.c_int()
+    ms = (C.c_double * len(choices))()
+    rc = lib.dp_autotune(h, _FAMILY[family], _PRECISION[precision], fn, None, C.byref(best),
+                         C.cast(ms, C.c_void_p), len(choices))
+    if errors:
+        raise errors[0]
+    check(rc, h)
+    return best.value, {t: ms[i] for i, t in enumerate(choices)}
+
+
 def _ptr(a):
     return a.ctypes.data_as(C.c_void_p)
 

@@ -132,6 +132,9 @@ _I = C.c_int
 _L = C.c_long
 _VP = C.c_void_p
 
+# int run(void* user): the workload dp_autotune times
+AUTOTUNE_RUN = C.CFUNCTYPE(C.c_int, C.c_void_p)
+
 # name -> (restype, argtypes); pointers to arrays are passed as c_void_p.
 PROTOTYPES = {
     "dp_version": (_I, []),
@@ -145,6 +148,10 @@ PROTOTYPES = {
     "dp_launch_count": (C.c_longlong, [_P]),
     "dp_set_blocking": (_I, [_P, _I]),
     "dp_sync": (_I, [_P]),
+    "dp_mc_thread_choices": (_I, [_I, _VP, _I]),
+    "dp_set_mc_threads": (_I, [_P, _I, _I, _I]),
+    "dp_get_mc_threads": (_I, [_P, _I, _I, C.POINTER(_I)]),
+    "dp_autotune": (_I, [_P, _I, _I, AUTOTUNE_RUN, _VP, C.POINTER(_I), _VP, _I]),
     "dp_physics_upload": (_I, [_P, C.POINTER(DpSettings), _I, _I, _VP, _VP, C.POINTER(_P)]),
     "dp_physics_create": (_I, [_P, C.POINTER(DpSettings), _I, _VP, _I, _D, _D, C.POINTER(_P)]),
     "dp_physics_free": (_I, [_P]),

@@ -92,6 +92,25 @@ long long dp_launch_count(const dp_ctx* ctx);
 int dp_set_blocking(dp_ctx* ctx, int blocking);
 int dp_sync(dp_ctx* ctx);
 
+/* ------------------------------------------------------------------ launch shapes
+ * CTA size of the persistent transport kernels per kernel family and
+ * precision (DP_PREC_FP64 / DP_PREC_MIXED).  They run one CTA per SM, so the
+ * size trades registers per thread for warps per SM.  threads = 0 selects the
+ * default; dp_mc_thread_choices lists the compiled sizes (first: default). */
+#define DP_KERNEL_MC 0   /* dp_mc_histories, dp_mc_los: two-layer transport */
+#define DP_KERNEL_DIR 1  /* dp_dir_mc: fixed-path transport */
+int dp_mc_thread_choices(int precision, int* threads, int cap);  /* returns the count */
+int dp_set_mc_threads(dp_ctx* ctx, int family, int precision, int threads);
+int dp_get_mc_threads(const dp_ctx* ctx, int family, int precision, int* threads);
+/* Autotuner.  For every compiled CTA size of (family, precision): run(user)
+ * once untimed and once timed (CUDA events on the context stream; run
+ * enqueues the caller's workload on this context and returns a dp status).
+ * Keeps the fastest size on the context and writes it to best_threads;
+ * ms[i] receives the time of choice i (up to cap entries).  A nonzero status
+ * from run ends the search, restores the previous size and is returned. */
+int dp_autotune(dp_ctx* ctx, int family, int precision, int (*run)(void* user), void* user,
+                int* best_threads, double* ms, int cap);
+
 /* ------------------------------------------------------------------ physics tables
  * Column layout of one material table (src/Physics.jl:64-102 MaterialTable).
  * Every column holds n_energies doubles on the material's kinetic-energy grid. */

@@ -27,3 +27,18 @@ def test_library_exports_every_declared_symbol():
     missing = [s for s in declared_symbols() if not hasattr(lib, s)]
     assert not missing, missing
     assert lib.dp_version() == 1
+
+
+def test_launch_shape_choices_and_argument_checks():
+    """The compiled CTA sizes of the persistent transport kernels (no device
+    needed): 1024 (default), 768 and 512 threads for the mixed-precision
+    transport, 256 for FP64; bad arguments are rejected before any device
+    work."""
+    import dpgpu
+    assert dpgpu.mc_thread_choices("mixed") == [1024, 768, 512]
+    assert dpgpu.mc_thread_choices("fp64") == [256]
+    lib = dpgpu.load()
+    assert lib.dp_mc_thread_choices(7, None, 0) == dpgpu._lib.DP_ERR_ARG
+    assert lib.dp_set_mc_threads(None, 0, 1, 512) == dpgpu._lib.DP_ERR_ARG
+    assert lib.dp_autotune(None, 0, 1, dpgpu._lib.AUTOTUNE_RUN(lambda u: 0), None, None, None,
+                           0) == dpgpu._lib.DP_ERR_ARG

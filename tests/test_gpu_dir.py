@@ -217,3 +217,23 @@ def test_single_direction_api(dp, phys, oracle, orc_phys, scene):
     oc, _, _, _ = _oracle_batch(dp, oracle, orc_phys, sub, samples, 41)
     fo, so = _tally(oc, [500])
     assert f > 0 and abs(f - fo[0]) <= max(so[0], 1e-9 * fo[0])
+
+
+def test_cta_sizes_give_identical_histories(dp, phys, scene):
+    """Fixed-path transport at every compiled CTA size: the same
+    contributions, bit for bit (a history's stream does not depend on the
+    thread that runs it; fewer media fit in shared memory at larger sizes)."""
+    n_per = [2000] * 6
+    samples = _samples(n_per, 9)
+    runs = {}
+    try:
+        for t in dp.mc_thread_choices("mixed"):
+            dp.set_mc_threads(phys, "dir", "mixed", t)
+            r = _run(dp, phys, scene, samples, 33, precision="mixed")
+            assert np.all(r["status"] == 0)
+            runs[t] = r
+    finally:
+        dp.set_mc_threads(phys, "dir", "mixed", 0)
+    for t, r in runs.items():
+        np.testing.assert_array_equal(r["contrib"], runs[1024]["contrib"], err_msg=f"{t} threads")
+        np.testing.assert_array_equal(r["flux"], runs[1024]["flux"])

@@ -267,3 +267,62 @@ def test_run_backward_mc_stochastic(dp, phys, oracle, orc_phys):
     assert r.gradient == pytest.approx(cd.mean(), rel=1e-8)
     m = dp.run_backward_mc(phys, precision="mixed", **kw)
     assert abs(m.flux - r.flux) <= 3 * r.sigma
+
+
+# ------------------------------------------------------------------ launch shapes
+def test_cta_sizes_give_identical_histories(dp, phys, media):
+    """A history's random stream is (seed, history id) whichever thread runs
+    it, so every compiled CTA size gives the same contributions, bit for bit."""
+    n, seed = 20000, 5
+    E, q, w, geo = _histories(n, seed)
+    _, air, mix = media
+    runs = {}
+    try:
+        for t in dp.mc_thread_choices("mixed"):
+            dp.set_mc_threads(phys, "mc", "mixed", t)
+            assert dp.get_mc_threads(phys, "mc", "mixed") == t
+            c, st, _, _ = dp.mc_histories(phys, mix, air, E, q, w, seed=seed, precision="mixed",
+                                          **geo)
+            assert np.all(st == 0)
+            runs[t] = c
+    finally:
+        dp.set_mc_threads(phys, "mc", "mixed", 0)
+    assert dp.get_mc_threads(phys, "mc", "mixed") == 1024
+    for t, c in runs.items():
+        np.testing.assert_array_equal(c, runs[1024], err_msg=f"{t} threads")
+
+
+def test_autotune_keeps_the_fastest_size(dp, phys, media):
+    """dp_autotune runs the workload twice per compiled size (untimed, then
+    timed), keeps the fastest on the context; a failing workload restores the
+    previous size and raises."""
+    _, air, mix = media
+    los = dp.make_los([4000], thickness=100.0, density=2650.0, elevation=60.0, energy_min=1.0,
+                      energy_max=1e4, air_height=1000.0)
+    calls = []
+
+    def run():
+        calls.append(1)
+        dp.backward_mc_batch(phys, los, rock=mix, air=air, seed=1, precision="mixed")
+
+    choices = dp.mc_thread_choices("mixed")
+    try:
+        best, ms = dp.autotune(phys, "mc", "mixed", run)
+        assert best in choices and sorted(ms) == sorted(choices)
+        assert all(v > 0 for v in ms.values()) and ms[best] == min(ms.values())
+        assert dp.get_mc_threads(phys, "mc", "mixed") == best
+        assert len(calls) == 2 * len(choices)
+        dp.set_mc_threads(phys, "mc", "mixed", 768)
+
+        def broken():
+            raise RuntimeError("workload failed")
+
+        with pytest.raises(RuntimeError, match="workload failed"):
+            dp.autotune(phys, "mc", "mixed", broken)
+        assert dp.get_mc_threads(phys, "mc", "mixed") == 768
+        with pytest.raises(ValueError):
+            dp.set_mc_threads(phys, "mc", "mixed", 640)
+        with pytest.raises(ValueError):
+            dp.set_mc_threads(phys, "mc", "fp64", 512)
+    finally:
+        dp.set_mc_threads(phys, "mc", "mixed", 0)
