@@ -331,14 +331,14 @@ struct PathGeo {
     h.limit = limit;
     if (C.straggling) {
       if constexpr (PHASE == 0) {
-        if (straggled_step<R, COOP, true>(m, C, s, Li, rho, step, g, false, limit, h.x)) {
+        if (straggled_step<R, COOP, true, true>(m, C, s, Li, rho, step, g, false, limit, h.x)) {
           h.x.kind = CONT_STRAG;
           h.x.medium = h.med;
           return ADV_WAIT;
         }
         return step_end(h, h.x.moved);
       } else {
-        if (mixed_step<R, COOP>(m, C, s, rho, step, g, limit, h.x)) {
+        if (mixed_step<R, COOP, true>(m, C, s, rho, step, g, limit, h.x)) {
           h.x.kind = CONT_MIXED;
           h.x.medium = h.med;
           return ADV_WAIT;
@@ -362,7 +362,7 @@ struct PathGeo {
         mixed_end(h.s, x, Emax, h.limit, false);
       } else {
         ++x.event;
-        if (mixed_run<R, true>(m, P.C, h.s, x, g, h.limit)) {
+        if (mixed_run_in<R, true>(m, P.C, h.s, x, g, h.limit)) {
           x.kind = CONT_MIXED;
           return ADV_WAIT;
         }
@@ -370,9 +370,10 @@ struct PathGeo {
       return step_end(h, mixed_moved(x));
     } else {
       Loc<R> Li = locate(m, x.r0);
-      const R moved = straggled_end(m, P.C, h.s, Li, x.r0, R(d.energy), x.r1, x.r2, d.weight,
-                                    d.process, d.element, true, false, R(0), x.r3, x.a, true,
-                                    x.flag != 0, g);
+      // the fixed-path transport never scatters (x.flag is 0)
+      const R moved = straggled_end_in(m, P.C, h.s, Li, x.r0, R(d.energy), x.r1, x.r2, d.weight,
+                                       d.process, d.element, true, false, R(0), x.r3, x.a, true,
+                                       false, g);
       return step_end(h, moved);
     }
   }

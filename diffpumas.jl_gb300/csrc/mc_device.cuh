@@ -657,9 +657,14 @@ __device__ __forceinline__ bool mixed_event(State<R>& s, Cont<R>& x, const DelOu
   return x.r1 == R(0);
 }
 // Runs the event loop from x.event; returns true when it suspended on a DCS sum.
+// The per-step helpers (mixed_run, fluctuate, straggled_end) come in two
+// forms: *_in, inlined into the caller, and an out-of-line function.  The
+// two-layer transport with scattering calls them out of line (its step body
+// is large and bound by instruction fetch); the fixed-path transport, which
+// never scatters, inlines them (1.1x there).
 template <class R, bool COOP>
-static __device__ __noinline__ bool mixed_run(const Med<R>& m, const Consts& C, State<R>& s, Cont<R>& x, Stream& g,
-                          R energy_limit) {
+__device__ __forceinline__ bool mixed_run_in(const Med<R>& m, const Consts& C, State<R>& s, Cont<R>& x,
+                                             Stream& g, R energy_limit) {
   const int nk = m.nk;
   const R* kE = m.kcol(K_E);
   const R Emax = kE[nk - 1];
@@ -712,8 +717,13 @@ static __device__ __noinline__ bool mixed_run(const Med<R>& m, const Consts& C, 
   mixed_end(s, x, Emax, energy_limit, true);
   return false;
 }
-// Starts a mixed step of `distance` m at `density`; true when it suspended.
 template <class R, bool COOP>
+static __device__ __noinline__ bool mixed_run(const Med<R>& m, const Consts& C, State<R>& s, Cont<R>& x,
+                                              Stream& g, R energy_limit) {
+  return mixed_run_in<R, COOP>(m, C, s, x, g, energy_limit);
+}
+// Starts a mixed step of `distance` m at `density`; true when it suspended.
+template <class R, bool COOP, bool INL = false>
 __device__ bool mixed_step(const Med<R>& m, const Consts& C, State<R>& s, R density, R distance,
                            Stream& g, R energy_limit, Cont<R>& x) {
   const R Emax = m.kcol(K_E)[m.nk - 1];
@@ -732,7 +742,8 @@ __device__ bool mixed_step(const Med<R>& m, const Consts& C, State<R>& s, R dens
   x.r1 = s.w;
   x.r2 = energy_limit > R(0) ? fmin(energy_limit, Emax) : Emax;
   x.event = 0;
-  return mixed_run<R, COOP>(m, C, s, x, g, energy_limit);
+  if constexpr (INL) return mixed_run_in<R, COOP>(m, C, s, x, g, energy_limit);
+  else return mixed_run<R, COOP>(m, C, s, x, g, energy_limit);
 }
 
 // ------------------------------------------------------------ straggling
@@ -751,8 +762,8 @@ __device__ __forceinline__ R truncated_randn(Stream& g) {
 
 // fluctuate_energy_loss, backward (src/Straggling.jl:103-173, :1046-1105).
 template <class R>
-static __device__ __noinline__ R fluctuate(const Med<R>& m, R ki, const Loc<R>& Li, R dX, R Xtot, Stream& g,
-                       R* ratio_out) {
+__device__ __forceinline__ R fluctuate_in(const Med<R>& m, R ki, const Loc<R>& Li, R dX, R Xtot,
+                                        Stream& g, R* ratio_out) {
   R k1 = inv_range(m, MC_MR, Xtot + dX);
   R dk0 = fabs(ki - k1), ratio = R(1);
   if (k1 > R(0) && dk0 > R(0)) {
@@ -784,6 +795,11 @@ static __device__ __noinline__ R fluctuate(const Med<R>& m, R ki, const Loc<R>& 
   if (ratio == R(0)) ratio = R(1);
   *ratio_out = ratio;
   return fmax(k1, R(0));
+}
+template <class R>
+static __device__ __noinline__ R fluctuate(const Med<R>& m, R ki, const Loc<R>& Li, R dX, R Xtot, Stream& g,
+                                           R* ratio_out) {
+  return fluctuate_in<R>(m, ki, Li, dX, Xtot, g, ratio_out);
 }
 
 // sample_ehs_event, backward (src/Straggling.jl:373-434, :1284-1334).
@@ -1019,10 +1035,11 @@ __device__ __forceinline__ double polar_ioni(double m, double ki, double kf) {
 // transport_backward_step_full, mode :straggled (src/Geometry.jl:148-357):
 // straggled_end completes a step from its energy-loss and event decisions.
 template <class R>
-static __device__ __noinline__ R straggled_end(const Med<R>& m, const Consts& C, State<R>& s, const Loc<R>& Li,
-                              R ki, R kf, R ckf, R dX, double dw, int proc, int elem, bool del,
-                              bool ehs, R k_ehs, R density, R step, bool shortened,
-                              bool scattering, Stream& g) {
+__device__ __forceinline__ R straggled_end_in(const Med<R>& m, const Consts& C, State<R>& s,
+                                              const Loc<R>& Li, R ki, R kf, R ckf, R dX, double dw,
+                                              int proc, int elem, bool del, bool ehs, R k_ehs,
+                                              R density, R step, bool shortened, bool scattering,
+                                              Stream& g) {
   const R mass = C.mass_r<R>();
   R astep = dX / density;
   R oz = s.uz;  // the position moves along the incoming direction
@@ -1056,12 +1073,20 @@ static __device__ __noinline__ R straggled_end(const Med<R>& m, const Consts& C,
   s.E = kf;
   return da;
 }
+template <class R>
+static __device__ __noinline__ R straggled_end(const Med<R>& m, const Consts& C, State<R>& s, const Loc<R>& Li,
+                                               R ki, R kf, R ckf, R dX, double dw, int proc, int elem,
+                                               bool del, bool ehs, R k_ehs, R density, R step,
+                                               bool shortened, bool scattering, Stream& g) {
+  return straggled_end_in<R>(m, C, s, Li, ki, kf, ckf, dX, dw, proc, elem, del, ehs, k_ehs, density,
+                             step, shortened, scattering, g);
+}
 
 // The step up to its hard-event decision; true when it suspended on the
 // event's DCS sum (cooperative evaluation), with x holding what straggled_end
 // needs.
 // With MOVED, x.moved receives the path length of a completed step.
-template <class R, bool COOP, bool MOVED = false>
+template <class R, bool COOP, bool MOVED = false, bool INL = false>
 __device__ bool straggled_step(const Med<R>& m, const Consts& C, State<R>& s, const Loc<R>& Li,
                                R density, R step, Stream& g, bool scattering, R energy_limit,
                                Cont<R>& x) {
@@ -1071,7 +1096,8 @@ __device__ bool straggled_step(const Med<R>& m, const Consts& C, State<R>& s, co
   R Xi = at(m, Li, MC_MR);
   R kf = ki, ratio = R(1);
   if (ki > R(0.001)) {
-    kf = fluctuate(m, ki, Li, dX, Xi, g, &ratio);
+    if constexpr (INL) kf = fluctuate_in(m, ki, Li, dX, Xi, g, &ratio);
+    else kf = fluctuate(m, ki, Li, dX, Xi, g, &ratio);
     kf = fmax(kf, ki);
   } else {
     kf = inv_range(m, MC_MR, Xi + dX);
@@ -1145,8 +1171,13 @@ __device__ bool straggled_step(const Med<R>& m, const Consts& C, State<R>& s, co
     dX = X_ehs;
     shortened = true;
   }
-  const R moved = straggled_end(m, C, s, Li, ki, kf, ckf, dX, dw, proc, elem, del, ehs, k_ehs,
-                                density, step, shortened, scattering, g);
+  R moved;
+  if constexpr (INL)
+    moved = straggled_end_in(m, C, s, Li, ki, kf, ckf, dX, dw, proc, elem, del, ehs, k_ehs, density,
+                             step, shortened, scattering, g);
+  else
+    moved = straggled_end(m, C, s, Li, ki, kf, ckf, dX, dw, proc, elem, del, ehs, k_ehs, density,
+                          step, shortened, scattering, g);
   if (MOVED) x.moved = moved;
   return false;
 }
