@@ -484,6 +484,73 @@ def setup_wcsda(dp, torch, dev, precision="mixed", scale=1.0):
     return step_dev, step_e2e, plain_dev, info, phys
 
 
+# objective evaluations of one calibrate_csda_correction with the default
+# grid: 'before', 41 + 4 x 9 grid points, the residual fit and 'after'
+CALIB_EVALS = 80
+
+
+def setup_calib(dp, torch, dev, precision="mixed", scale=1.0):
+    """calibrate_csda_correction over the dir workload's 4096 directions
+    against MC reference fluxes from the device fixed-path MC (1024 histories
+    per direction, final energies 1e-3 - 1e9 GeV; made once, untimed).  One
+    step is one calibration: the kappa_hard grid (41 + 4 x 9 points), the
+    geometric residual fit and the before / after passes, 80 evaluations of
+    the water-fraction CSDA model (32 quadrature nodes on the same energy
+    range) over all bins, one launch each.  The plain form is the reference's
+    loop structure on the device: FP64, one launch per bin and evaluation."""
+    phys = dp.create_physics(materials=(dp.STANDARD_ROCK, dp.AIR, dp.WATER))
+    n_dirs = max(16, int(4096 * scale))
+    cfg, site, paths, mats, dens, wf = dir_scene(dp, phys, n_dirs)
+    mc = dp.DirBatch(phys, cfg, site, paths, mats, dens, None, n_samples=1024,
+                     energy_min=DIR_E[0], energy_max=DIR_E[1]).run(2029, precision="mixed")["flux"]
+    nodes = [dp.EnergySample(*x) for x in zip(*dp.csda_energy_quadrature(32, *DIR_E))]
+    sh = np.zeros(len(wf), bool)
+    bins = list(range(1, n_dirs + 1))
+    model = dp.CsdaBatch(phys, sh, cfg, site, paths, nodes).to_device()
+    result = {}
+
+    def calibrate(m):
+        dp.set_csda_correction(enabled=False)
+        ks, kh, st = dp.calibrate_csda_correction(phys, sh, cfg, site, paths, wf, nodes, mc, bins,
+                                                  precision=precision, model=m)
+        result.update(kappa_hard=kh, rel_before=st["rel_before"], rel_after=st["rel_after"])
+
+    def step_dev():
+        calibrate(model)
+
+    def step_e2e():
+        calibrate(None)  # the bins' batch is built and uploaded inside the call
+
+    one = [dp.CsdaBatch(phys, sh, cfg, site, [p], nodes).to_device() for p in paths[:16]]
+    w_t = torch.tensor(wf, dtype=torch.float64, device=dev)
+    f1 = torch.zeros(1, dtype=torch.float64, device=dev)
+
+    def plain_dev():
+        for _ in range(CALIB_EVALS):
+            for b in one:
+                b.run_dev(w_t, f1, None, precision="fp64")
+
+    info = {"units": 1, "unit": "calibrations/s",
+            "kernel": "dir_csda32" if precision == "mixed" else "dir_csda",
+            # per evaluation: 40 B geometry per bin, per segment 4 B cell,
+            # 8 B length and 8 B w read, 8 B flux per bin written
+            "alg_bytes": CALIB_EVALS * (n_dirs * 48 + model.n_seg * 20), "traffic": None,
+            "note": "host-driven grid search: per evaluation one launch, the water fractions "
+                    "up and the fluxes down",
+            "config": {"workload": "calib: calibrate_csda_correction (kappa_hard grid 41 + 4x9, "
+                                   "geometric residual fit) of the water-fraction CSDA model "
+                                   "against device fixed-path MC fluxes, 4096 directions of the "
+                                   "dir workload, 32 CSDA nodes [1e-3, 1e9] GeV",
+                       "n_bins": n_dirs, "evaluations": CALIB_EVALS, "segments": model.n_seg,
+                       "precision": precision},
+            "h2d": model.host_bytes() + CALIB_EVALS * wf.nbytes,
+            "d2h": CALIB_EVALS * 8 * n_dirs,
+            "plain_what": "FP64, one launch per bin and evaluation, first 16 bins x 80 "
+                          "evaluations", "plain_units": 16 / n_dirs, "plain_reps": 1,
+            "finish": lambda: dict(result)}
+    return step_dev, step_e2e, plain_dev, info, phys
+
+
 def setup_c1(dp, torch, dev):
     phys = dp.create_physics()
     n = 10000
@@ -515,8 +582,10 @@ def run_gpu(args):
     import dpgpu as dp
     dp._default = dp.Context(local)
     setup = {"c2": setup_c2, "c3": setup_c3, "c4": setup_c4, "c5": setup_c5,
-             "c1": setup_c1, "dir": setup_dir, "wcsda": setup_wcsda}[args.workload]
-    kw = {"scale": args.scale} if args.workload in ("c2", "c4", "c5", "dir", "wcsda") else {}
+             "c1": setup_c1, "dir": setup_dir, "wcsda": setup_wcsda,
+             "calib": setup_calib}[args.workload]
+    kw = {"scale": args.scale} if args.workload in ("c2", "c4", "c5", "dir", "wcsda",
+                                                     "calib") else {}
     step_dev, step_e2e, plain_dev, info, phys = setup(dp, torch, dev, **kw)
     if args.scale != 1.0:
         info["config"]["scale"] = args.scale
@@ -689,6 +758,8 @@ def cpu_baseline(workload, budget_s=15.0, threads=None):
         return cpu_baseline_dir(O, budget_s, threads)
     if workload == "wcsda":
         return cpu_baseline_wcsda(O, budget_s, threads)
+    if workload == "calib":
+        return cpu_baseline_calib(O, budget_s, threads)
     if workload == "c2":
         p = O.default_physics((O.STANDARD_ROCK, O.AIR, O.WATER), coulomb=True)
         rng = np.random.default_rng(0)
@@ -776,13 +847,42 @@ def cpu_baseline_wcsda(O, budget_s, threads):
                       "d flux/d w (FP64 oracle, OpenMP over bins)"}
 
 
+def cpu_baseline_calib(O, budget_s, threads):
+    """The oracle's water-fraction CSDA flux (forward only) over the dir
+    directions, OpenMP over bins; one calibration is 80 evaluations of all
+    4096 bins."""
+    import dpgpu as dp
+    from dpgpu.workloads import directional_config
+    raw, wf = directional_config(4096)
+    p = O.default_physics((O.STANDARD_ROCK, O.AIR, O.WATER))
+    E, q, w = dp.csda_energy_quadrature(32, *DIR_E)
+    n, t0, i = 0, time.perf_counter(), 0
+    while time.perf_counter() - t0 < budget_s:
+        chunk = [raw[(i + k) % len(raw)] for k in range(256)]
+        i += 256
+        seg_ptr = np.concatenate([[0], np.cumsum([len(c[2]) for c in chunk])])
+        O.dir_csda(p, [0, 2, 1, -1], [2710.0, 1000.0, 0.0, 0.0], [963.0, 30000.0],
+                   [1, 1.0, 20.0, 0, 0, 0, 0, 0, 0.0, 0.0],
+                   [np.cos(np.radians(c[0])) for c in chunk], [c[5] for c in chunk],
+                   [c[6] for c in chunk], [1] * len(chunk), seg_ptr,
+                   [s[0] - 1 for c in chunk for s in c[2]], [s[1] for c in chunk for s in c[2]],
+                   np.zeros(len(wf), np.uint8), wf, E, q, w, threads=threads)
+        n += len(chunk)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt / (CALIB_EVALS * 4096), "unit": "calibrations/s", "cores": threads,
+            "kind": "port",
+            "sample": f"{n} bin evaluations of the calib workload (cycled; one calibration = "
+                      f"{CALIB_EVALS} x 4096), corrected CSDA flux (FP64 oracle, OpenMP over bins)"}
+
+
 def run_reference(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     units = {"c2": "samples/s", "c3": "rays/s", "c4": "samples/s", "c5": "iterations/s",
-             "c1": "samples/s", "dir": "samples/s", "wcsda": "rays/s"}[args.workload]
+             "c1": "samples/s", "dir": "samples/s", "wcsda": "rays/s",
+             "calib": "calibrations/s"}[args.workload]
     vals = []
     for _ in range(args.warmup):
         cpu_baseline(args.workload, budget_s=args.cpu_seconds / 4)
@@ -808,7 +908,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--workload", default="c2",
-                    choices=["c2", "c3", "c4", "c5", "c1", "dir", "wcsda"])
+                    choices=["c2", "c3", "c4", "c5", "c1", "dir", "wcsda", "calib"])
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")

@@ -519,6 +519,11 @@ from .inverse import (EdgePrior, SmoothnessPrior, apply_laplacian_smoothing,  # 
                       edge_gradient, edge_hessian, gauss_newton_reconstruct,
                       gradient_descent_reconstruct, laplacian_gradient, make_csda_operator,
                       mlem_reconstruct, mse, prior_value, rmse, sart_reconstruct)
+from .calibration import (calibrate_csda_correction,  # noqa: E402
+                          calibrate_csda_material_correction, column_water_fraction,
+                          csda_geom_multiplier, csda_material_multiplier, load_csda_corrections,
+                          path_rock_length, save_csda_corrections)
+from .directional import cell_density  # noqa: E402
 
 
 # ----------------------------------------------------------------- tomography

@@ -25,6 +25,15 @@ def is_shallow_porous(shallow, matcfg):
     return bool(shallow) and matcfg.porous_material > 0 and matcfg.porous_top_thickness > 0.0
 
 
+def cell_density(w, shallow, matcfg):
+    """Density of a cell with water mass fraction w, the CSDA model's form
+    (src/Tomography.jl:295-302): specific volumes add."""
+    if is_shallow_porous(shallow, matcfg):
+        return 1.0 / (0.5 * (1.0 - w) / matcfg.porous_density +
+                      0.5 * (1.0 - w) / matcfg.rock_density + w / matcfg.water_density)
+    return 1.0 / ((1.0 - w) / matcfg.rock_density + w / matcfg.water_density)
+
+
 def mc_cell_mixture_and_density(w, shallow, matcfg):
     """Mixture recipe ((materials, fractions)) and density of a cell with water
     mass fraction w (src/Tomography.jl:826-845): specific volumes add."""
@@ -332,8 +341,14 @@ class CsdaBatch:
         self.n_seg = int(seg_ptr[-1])
         self.n_energy = len(energy_samples)
         self.n_cells = len(self.arrays["shallow"])
-        self.config = _csda_config(matcfg, site)
+        self.matcfg, self.site = matcfg, site
         self.dev = None
+
+    @property
+    def config(self):
+        """dp_csda_config with the corrections in force at the call (the
+        reference reads them at every evaluation)."""
+        return _csda_config(self.matcfg, self.site)
 
     def _struct(self, ptr):
         from ._lib import DpCsdaBatch
@@ -346,16 +361,33 @@ class CsdaBatch:
         return sum(a.nbytes for a in self.arrays.values())
 
     def run(self, water_fractions, *, jacobian=True, precision="fp64"):
-        """(flux per bin, d flux / d w per segment or None), host arrays."""
+        """(flux per bin, d flux / d w per segment or None), host arrays.
+        After to_device() the paths stay resident: only the water fractions
+        go up and the results come back."""
         from . import PRECISION
         from . import _ptr
+        if len(water_fractions) != self.n_cells:
+            raise ValueError("water_fractions and shallow_flags differ in length")
+        if self.dev is not None:
+            import torch
+            dev = self.dev["cos_theta"].device
+            w_t = torch.from_numpy(np.ascontiguousarray(water_fractions, np.float64)).to(dev)
+            torch.cuda.synchronize(dev)
+            f_t = torch.zeros(max(self.n_bins, 1), dtype=torch.float64, device=dev)
+            j_t = torch.zeros(max(self.n_seg, 1), dtype=torch.float64, device=dev) if jacobian \
+                else None
+            self.run_dev(w_t, f_t, j_t, precision=precision)
+            check(load().dp_sync(self.physics.ctx.h), self.physics.ctx.h)
+            return (f_t.cpu().numpy()[:self.n_bins],
+                    j_t.cpu().numpy()[:self.n_seg] if jacobian else None)
         A = self.arrays
         B = self._struct(lambda k: A[k].ctypes.data if A[k].size else None)
         wf = np.ascontiguousarray(water_fractions, np.float64)
         flux = np.zeros(max(self.n_bins, 1))
         jac = np.zeros(max(self.n_seg, 1))
         ctx = self.physics.ctx.h
-        check(load().dp_dir_csda(ctx, self.physics.h, C.byref(self.config), C.byref(B),
+        cfg = self.config
+        check(load().dp_dir_csda(ctx, self.physics.h, C.byref(cfg), C.byref(B),
                                  len(wf), _ptr(A["shallow"]), _ptr(wf), _ptr(flux),
                                  _ptr(jac) if jacobian else None, PRECISION[precision]), ctx)
         return flux[:self.n_bins], (jac[:self.n_seg] if jacobian else None)
@@ -371,9 +403,13 @@ class CsdaBatch:
         """Enqueues one evaluation on resident arrays: water_fractions, flux
         (n_bins) and jac (n_seg, optional) are float64 CUDA tensors."""
         from . import PRECISION
+        if water_fractions.numel() != self.n_cells or flux.numel() < self.n_bins or (
+                jac is not None and jac.numel() < self.n_seg):
+            raise ValueError("device arrays too small for the batch")
         B = self._struct(lambda k: self.dev[k].data_ptr() if self.dev[k].numel() else None)
         ctx = self.physics.ctx.h
-        check(load().dp_dir_csda_dev(ctx, self.physics.h, C.byref(self.config), C.byref(B),
+        cfg = self.config
+        check(load().dp_dir_csda_dev(ctx, self.physics.h, C.byref(cfg), C.byref(B),
                                      self.n_cells, self.dev["shallow"].data_ptr(),
                                      water_fractions.data_ptr(), flux.data_ptr(),
                                      jac.data_ptr() if jac is not None else None,
