@@ -515,6 +515,9 @@ static int setup(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params* p, CsdaP
     if (air < 0) air = ph->n_mat - 1;
   }
   if (rock >= ph->n_mat || air >= ph->n_mat) return fail(ctx, DP_ERR_ARG, "material index out of range");
+  if (p->porous_material >= 0 && p->porous_thickness > 0.0 &&
+      (p->porous_material >= ph->n_mat || !(p->porous_density > 0.0)))
+    return fail(ctx, DP_ERR_ARG, "porous layer: material index out of range or density not positive");
   double tmax = ph->host[(size_t(0) * DP_NCOL + DP_COL_E) * ph->n + ph->n - 1];
   double thr = p->source_energy_max > 0.0 ? p->source_energy_max : std::fmin(1e9, tmax);
   if (!(thr > 0.0 && thr <= tmax))
@@ -695,8 +698,13 @@ int dp_backward_mc(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params* p, dp_
   if (!out || p->n_samples <= 0) return fail(ctx, DP_ERR_ARG, "n_samples must be positive");
   DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
   long n = p->n_samples;
-  // stochastic transport first (its scratch is released before the CSDA pass)
-  const bool stochastic = p->straggling || p->scattering;
+  // stochastic transport first (its scratch is released before the CSDA pass);
+  // a porous layer runs through the stochastic kernels (CSDA steps when
+  // straggling and scattering are off), which model it
+  const bool porous = p->porous_material >= 0 && p->porous_thickness > 0.0;
+  if (porous && p->compute_gradient)
+    return fail(ctx, DP_ERR_ARG, "the CSDA gradient has no porous layer");
+  const bool stochastic = p->straggling || p->scattering || porous;
   dp_los_result st{};
   int st_rc = DP_OK;
   if (stochastic) {

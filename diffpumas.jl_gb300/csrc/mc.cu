@@ -312,27 +312,30 @@ MedInfo make_info(const dp_mixture* m) {
 
 namespace {
 
-// Device blob of the (rock, air) pair in one precision, built once per pair.
+// Device blob of the (rock, air[, porous]) media in one precision, built
+// once per combination.
 int get_blob(dp_ctx* ctx, dp_mixture* rock, const dp_mixture* air, int precision,
-             const unsigned char** dev, Layout* lay) {
+             const unsigned char** dev, Layout* lay, const dp_mixture* porous = nullptr) {
+  const uint64_t puid = porous ? porous->uid : 0;
   for (auto& b : rock->blobs)
-    if (b.partner == air->uid && b.precision == precision) {
+    if (b.partner == air->uid && b.partner2 == puid && b.precision == precision) {
       *dev = b.dev;
       *lay = b.lay;
       return DP_OK;
     }
-  if (rock->n != air->n || rock->nk != air->nk || rock->phys != air->phys)
-    return fail(ctx, DP_ERR_ARG, "rock and air media must come from one physics");
+  if (rock->n != air->n || rock->nk != air->nk || rock->phys != air->phys ||
+      (porous && (porous->n != rock->n || porous->nk != rock->nk || porous->phys != rock->phys)))
+    return fail(ctx, DP_ERR_ARG, "rock, air and porous media must come from one physics");
   size_t es = precision == DP_PREC_MIXED ? sizeof(float) : sizeof(double);
-  const dp_mixture* pair[2] = {rock, air};
-  Layout L = make_layout(pair, 2, es);
-  std::vector<unsigned char> h(size_t(2) * L.med_bytes);
-  pack_medium(rock, L, es, h.data());
-  pack_medium(air, L, es, h.data() + L.med_bytes);
+  const dp_mixture* media[3] = {rock, air, porous};
+  const int nm = porous ? 3 : 2;
+  Layout L = make_layout(media, nm, es);
+  std::vector<unsigned char> h(size_t(nm) * L.med_bytes);
+  for (int k = 0; k < nm; ++k) pack_medium(media[k], L, es, h.data() + size_t(k) * L.med_bytes);
   unsigned char* d = nullptr;
   DP_CHECK_CUDA(ctx, cudaMalloc(&d, h.size()));
   DP_CHECK_CUDA(ctx, cudaMemcpy(d, h.data(), h.size(), cudaMemcpyHostToDevice));
-  rock->blobs.push_back({air->uid, precision, d, L});
+  rock->blobs.push_back({air->uid, puid, precision, d, L});
   *dev = d;
   *lay = L;
   return DP_OK;
@@ -345,9 +348,10 @@ namespace dp {
 namespace mc {
 
 struct McParams {
-  const unsigned char* blob;  // rock medium, then air medium
+  const unsigned char* blob;  // rock medium, air medium, then the porous medium if any
   Layout lay;
-  MedInfo info[2];
+  MedInfo info[3];
+  int porous;                 // the columns have a porous top layer (porous_rec)
   Consts C;
   uint64_t seed;
   int staged;
@@ -369,6 +373,7 @@ struct McParams {
   void* queue;                // Handoff<R> x n: histories crossing the mode switch
   void* start;                // StartRec<R> x n
   void* end;                  // EndRec<R> x n
+  void* porous_rec;           // PorousRec<R> x n when porous
 };
 
 // Start record of history i: energy, charge and weight drawn as
@@ -379,7 +384,7 @@ __global__ void __launch_bounds__(256) mc_init_kernel(const __grid_constant__ Mc
   StartRec<R>* out = static_cast<StartRec<R>*>(P.start);
   for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < P.n;
        i += long(gridDim.x) * blockDim.x) {
-    double E0, q, ws, thick, rho, elev, H;
+    double E0, q, ws, thick, rho, elev, H, p_thick = 0.0, p_rho = 0.0;
     if (P.source == 0) {
       E0 = P.E[i];
       q = P.q[i];
@@ -413,6 +418,16 @@ __global__ void __launch_bounds__(256) mc_init_kernel(const __grid_constant__ Mc
                  : L.elevation;
       H = L.air_height > 0.0 ? thick + L.air_height
                              : (L.primary_altitude > 0.0 ? L.primary_altitude : 3e4);
+      p_thick = L.porous_thickness;
+      p_rho = L.porous_density;
+    }
+    if (P.porous) {
+      // porous_z = rock_thickness - porous_thickness when the layer is
+      // present (src/Geometry.jl:617-618), else the rock top
+      PorousRec<R> pr;
+      pr.pz = alt_make<R>(p_thick > 0.0 ? thick - p_thick : thick);
+      pr.prho = R(p_rho);
+      static_cast<PorousRec<R>*>(P.porous_rec)[i] = pr;
     }
     double theta = (90.0 - elev) * kPi / 180.0;
     StartRec<R> r;
@@ -505,19 +520,58 @@ struct SlabGeo {
   __device__ const Med<R>& medium(int k) const { return k ? air : rock; }
   template <bool COOP, int PHASE>
   __device__ int advance(Hist& h, Stream& g) const {
-    return mc::advance<R, COOP, PHASE>(rock, air, P.C, h, g);
+    return mc::advance<R, COOP, PHASE>(rock, air, nullptr, P.C, h, g);
   }
   template <int PHASE>
   __device__ int resume(Hist& h, Stream& g) const {
-    return mc::resume<R, PHASE>(rock, air, P.C, h, g);
+    return mc::resume<R, PHASE>(rock, air, nullptr, P.C, h, g);
   }
 };
 
-template <class R, int PHASE, int T>
+// The same column with the shallow porous top layer (medium 2).
+template <class R>
+struct SlabGeoP {
+  using Hist = mc::HistP<R>;
+  using Queue = HandoffP<R>;
+  const McParams& P;
+  const Med<R>& rock;
+  const Med<R>& air;
+  const Med<R>& porous;
+  __device__ long n0() const { return P.n; }
+  __device__ void start(long i, Hist& h, Stream& g) const {
+    start_history(P, i, h, g);
+    const PorousRec<R> pr = static_cast<const PorousRec<R>*>(P.porous_rec)[i];
+    h.pz = pr.pz;
+    h.prho = pr.prho;
+  }
+  __device__ long load(const Queue& q, Hist& h, Stream& g) const {
+    const long i = load_handoff(q, P.seed, h, g);
+    h.pz = q.pz;
+    h.prho = q.prho;
+    return i;
+  }
+  __device__ void save(const Hist& h, const Stream& g, long i, Queue* q) const {
+    save_handoff(h, g, i, q);
+    q->pz = h.pz;
+    q->prho = h.prho;
+  }
+  __device__ void end(long i, const Hist& h) const { end_history(P, i, h); }
+  __device__ const Med<R>& medium(int k) const { return k == 1 ? air : (k == 2 ? porous : rock); }
+  template <bool COOP, int PHASE>
+  __device__ int advance(Hist& h, Stream& g) const {
+    return mc::advance<R, COOP, PHASE>(rock, air, &porous, P.C, h, g);
+  }
+  template <int PHASE>
+  __device__ int resume(Hist& h, Stream& g) const {
+    return mc::resume<R, PHASE>(rock, air, &porous, P.C, h, g);
+  }
+};
+
+template <class R, int PHASE, int T, bool POR = false>
 __global__ void __launch_bounds__(T, 1) mc_kernel(const __grid_constant__ McParams P) {
   extern __shared__ __align__(16) unsigned char smem[];
   const unsigned char* base = P.blob;
-  const uint32_t tables = P.staged ? 2 * P.lay.med_bytes : 0;
+  const uint32_t tables = P.staged ? (POR ? 3 : 2) * P.lay.med_bytes : 0;
   if (P.staged) {
     if (!stage_blob(smem + 16, P.blob, tables, reinterpret_cast<uint64_t*>(smem))) {
       if (threadIdx.x == 0) atomicExch(P.err_flag, 1);
@@ -527,10 +581,19 @@ __global__ void __launch_bounds__(T, 1) mc_kernel(const __grid_constant__ McPara
   }
   const Med<R> rock = make_med<R>(base, P.lay, P.info[0]);
   const Med<R> air = make_med<R>(base + P.lay.med_bytes, P.lay, P.info[1]);
-  SlabGeo<R> geo{P, rock, air};
   float* item = reinterpret_cast<float*>(smem + 16 + tables) + size_t(threadIdx.x >> 5) * P.coop_stride;
-  transport_histories<R, PHASE, KCfg<R>::coop>(geo, P.C, P.counter, static_cast<Handoff<R>*>(P.queue),
-                                               item, item + kItemsPerElement * P.coop_nel);
+  if constexpr (POR) {
+    const Med<R> porous = make_med<R>(base + 2 * P.lay.med_bytes, P.lay, P.info[2]);
+    SlabGeoP<R> geo{P, rock, air, porous};
+    transport_histories<R, PHASE, KCfg<R>::coop>(geo, P.C, P.counter,
+                                                 static_cast<HandoffP<R>*>(P.queue), item,
+                                                 item + kItemsPerElement * P.coop_nel);
+  } else {
+    SlabGeo<R> geo{P, rock, air};
+    transport_histories<R, PHASE, KCfg<R>::coop>(geo, P.C, P.counter,
+                                                 static_cast<Handoff<R>*>(P.queue), item,
+                                                 item + kItemsPerElement * P.coop_nel);
+  }
 }
 
 // Per line of sight: compensated sums of the contributions and of their
@@ -687,8 +750,8 @@ __global__ void __launch_bounds__(1024) los_offsets_kernel(const dp_los* los, co
 namespace {
 
 // Per-history device records of a run (hand-off, start, end), sized for FP64.
-constexpr size_t kRecBytes = sizeof(Handoff<double>) + sizeof(StartRec<double>) +
-                             sizeof(EndRec<double>) + 64;
+constexpr size_t kRecBytes = sizeof(HandoffP<double>) + sizeof(StartRec<double>) +
+                             sizeof(EndRec<double>) + sizeof(PorousRec<double>) + 64;
 
 }  // namespace
 
@@ -795,35 +858,37 @@ int group_tally(dp_ctx* ctx, const double* contrib, const int32_t* status, const
 
 namespace {
 
-template <class R, int PHASE, int T>
+template <class R, int PHASE, int T, bool POR>
 int launch_phase(dp_ctx* ctx, McParams& P, size_t smem, long max_blocks) {
   const int threads = T;
-  DP_CHECK_CUDA(ctx, cudaFuncSetAttribute(mc_kernel<R, PHASE, T>,
+  DP_CHECK_CUDA(ctx, cudaFuncSetAttribute(mc_kernel<R, PHASE, T, POR>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   int per_sm = 0, n_sm = 0;
-  DP_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_kernel<R, PHASE, T>,
-                                                                   threads, smem));
+  DP_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                         &per_sm, mc_kernel<R, PHASE, T, POR>, threads, smem));
   DP_CHECK_CUDA(ctx, cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, ctx->device));
   if (per_sm < 1) return fail(ctx, DP_ERR_CUDA, "MC kernel does not fit on a multiprocessor");
   long blocks = std::min(long(per_sm) * n_sm, max_blocks);
   if (blocks < 1) blocks = 1;
   timed_begin(ctx);
-  mc_kernel<R, PHASE, T><<<int(blocks), threads, smem, ctx->stream>>>(P);
+  mc_kernel<R, PHASE, T, POR><<<int(blocks), threads, smem, ctx->stream>>>(P);
   DP_CHECK_CUDA(ctx, cudaGetLastError());
   timed_end(ctx, sizeof(R) == 4 ? (PHASE ? "mc_mixed_hi" : "mc_mixed_lo")
                                 : (PHASE ? "mc_fp64_hi" : "mc_fp64_lo"));
   return DP_OK;
 }
 
-// Both transport phases with CTAs of T threads; P.queue must hold P.n
-// handoff records and P.counter three zeroed words (set here).
-template <class R, int T>
+// Both transport phases with CTAs of T threads (POR: the column has the
+// porous layer, medium 2); P.queue must hold P.n handoff records and
+// P.counter three zeroed words (set here).
+template <class R, int T, bool POR>
 int launch_mc_t(dp_ctx* ctx, McParams& P) {
   const int threads = T;
   P.coop_nel = std::max(P.info[0].nel, P.info[1].nel);
+  if (POR) P.coop_nel = std::max(P.coop_nel, P.info[2].nel);
   P.coop_stride = KCfg<R>::coop ? ((kItemsPerElement + 4) * P.coop_nel + 3) / 4 * 4 : 0;
   size_t coop_bytes = size_t(threads / 32) * P.coop_stride * sizeof(float);
-  size_t tables = size_t(2) * P.lay.med_bytes;
+  size_t tables = size_t(POR ? 3 : 2) * P.lay.med_bytes;
   int dev_smem = 0;
   DP_CHECK_CUDA(ctx, cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
   P.staged = 16 + tables + coop_bytes <= size_t(dev_smem) ? 1 : 0;
@@ -836,9 +901,9 @@ int launch_mc_t(dp_ctx* ctx, McParams& P) {
   mc_init_kernel<R><<<int(rec_blocks), 256, 0, ctx->stream>>>(P);
   DP_CHECK_CUDA(ctx, cudaGetLastError());
   timed_end(ctx, "mc_init");
-  int rc = launch_phase<R, 0, T>(ctx, P, smem, need);
+  int rc = launch_phase<R, 0, T, POR>(ctx, P, smem, need);
   if (rc) return rc;
-  rc = launch_phase<R, 1, T>(ctx, P, smem, need);
+  rc = launch_phase<R, 1, T, POR>(ctx, P, smem, need);
   if (rc) return rc;
   timed_begin(ctx);
   mc_finish_kernel<R><<<int(rec_blocks), 256, 0, ctx->stream>>>(P);
@@ -847,10 +912,12 @@ int launch_mc_t(dp_ctx* ctx, McParams& P) {
   return DP_OK;
 }
 
+// The porous-layer variant is compiled for the default CTA size only.
 template <class R>
 int launch_mc(dp_ctx* ctx, McParams& P) {
+  if (P.porous) return launch_mc_t<R, KCfg<R>::threads, true>(ctx, P);
   return with_threads<R>(ctx->mc_threads[DP_KERNEL_MC][sizeof(R) == 4],
-                         [&](auto t) { return launch_mc_t<R, decltype(t)::value>(ctx, P); });
+                         [&](auto t) { return launch_mc_t<R, decltype(t)::value, false>(ctx, P); });
 }
 
 int run(dp_ctx* ctx, McParams& P, int precision) {
@@ -875,7 +942,7 @@ McParams base_params(dp_ctx* ctx, const unsigned char* blob, const Layout& lay, 
 int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_mixture* air,
                   const dp_mc_config* cfg, long n_los, const dp_los* d_los, long total,
                   dp_los_result* d_out, double** contrib_out, int** status_or,
-                  int compute_gradient);
+                  int compute_gradient, const dp_mixture* porous);
 
 namespace {
 // compiled CTA sizes of the persistent transport kernels (with_threads)
@@ -1075,24 +1142,42 @@ int dp_mc_histories(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock_c,
   return status_code(ctx, bits);
 }
 
-int dp_mc_los_dev(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock_c,
-                  const dp_mixture* air, const dp_mc_config* cfg, long n_los, const dp_los* los,
-                  long total, int compute_gradient, dp_los_result* out) {
+int dp_mc_los_layers_dev(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock_c,
+                         const dp_mixture* porous, const dp_mixture* air,
+                         const dp_mc_config* cfg, long n_los, const dp_los* los, long total,
+                         int compute_gradient, dp_los_result* out) {
   if (!ctx || !ph || !rock_c || !air || !los || !out || n_los <= 0 || total < 0)
     return fail(ctx, DP_ERR_ARG, "bad arguments");
+  if (porous && compute_gradient)
+    return fail(ctx, DP_ERR_ARG, "the CSDA gradient has no porous layer");
   double* contrib = nullptr;
   int* bits = nullptr;
   int rc = dp_mc_run_los(ctx, ph, const_cast<dp_mixture*>(rock_c), air, cfg, n_los, los, total, out,
-                         &contrib, &bits, compute_gradient);
+                         &contrib, &bits, compute_gradient, porous);
   if (rc) return rc;
   if (ctx->blocking) return status_result(ctx, bits);
   return DP_OK;
 }
 
+int dp_mc_los_dev(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock_c,
+                  const dp_mixture* air, const dp_mc_config* cfg, long n_los, const dp_los* los,
+                  long total, int compute_gradient, dp_los_result* out) {
+  return dp_mc_los_layers_dev(ctx, ph, rock_c, nullptr, air, cfg, n_los, los, total,
+                              compute_gradient, out);
+}
+
 int dp_mc_los(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock, const dp_mixture* air,
               const dp_mc_config* cfg, long n_los, const dp_los* los, int compute_gradient,
               dp_los_result* out) {
+  return dp_mc_los_layers(ctx, ph, rock, nullptr, air, cfg, n_los, los, compute_gradient, out);
+}
+
+int dp_mc_los_layers(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock,
+                     const dp_mixture* porous, const dp_mixture* air, const dp_mc_config* cfg,
+                     long n_los, const dp_los* los, int compute_gradient, dp_los_result* out) {
   if (!ctx || !los || !out || n_los <= 0) return fail(ctx, DP_ERR_ARG, "bad arguments");
+  if (porous && compute_gradient)
+    return fail(ctx, DP_ERR_ARG, "the CSDA gradient has no porous layer");
   long total = 0;
   for (long l = 0; l < n_los; ++l) {
     const dp_los& L = los[l];
@@ -1101,6 +1186,8 @@ int dp_mc_los(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock, const d
     // transport_mixed_step needs a positive density (src/MixedTransport.jl:146)
     if (!(L.density > 0.0) || !(L.thickness >= 0.0))
       return fail(ctx, DP_ERR_ARG, "positive density and nonnegative thickness required");
+    if (porous && L.porous_thickness > 0.0 && !(L.porous_density > 0.0))
+      return fail(ctx, DP_ERR_ARG, "a porous layer needs a positive density");
     total += L.n_samples;
   }
   DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -1120,7 +1207,7 @@ int dp_mc_los(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock, const d
   double* contrib = nullptr;
   int* bits = nullptr;
   int rc = dp_mc_run_los(ctx, ph, const_cast<dp_mixture*>(rock), air, cfg, n_los, dl, total, dr,
-                         &contrib, &bits, compute_gradient);
+                         &contrib, &bits, compute_gradient, porous);
   if (rc) return rc;
   DP_CHECK_CUDA(ctx, cudaMemcpyAsync(out, dr, ob, cudaMemcpyDeviceToHost, ctx->stream));
   return status_result(ctx, bits);
@@ -1134,7 +1221,7 @@ int dp_mc_los(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock, const d
 int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_mixture* air,
                   const dp_mc_config* cfg, long n_los, const dp_los* d_los, long total,
                   dp_los_result* d_out, double** contrib_out, int** status_or,
-                  int compute_gradient) {
+                  int compute_gradient, const dp_mixture* porous) {
   Consts C;
   double thr64;
   int rc = check_cfg(ctx, ph, cfg, &C, &thr64);
@@ -1144,7 +1231,7 @@ int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_
   DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
   const unsigned char* blob;
   Layout lay;
-  rc = get_blob(ctx, rock, air, cfg->precision, &blob, &lay);
+  rc = get_blob(ctx, rock, air, cfg->precision, &blob, &lay, porous);
   if (rc) return rc;
   long nt = total > 0 ? total : 1;
   Arena A;
@@ -1158,9 +1245,10 @@ int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_
   int64_t* coff = A.take<int64_t>(n_los + 1);
   TallyPart* tpart = A.take<TallyPart>(tally_jobs(n_los, nt));
   unsigned long long* ctr = A.take<unsigned long long>(3);
-  Handoff<double>* queue = A.take<Handoff<double>>(nt);
+  HandoffP<double>* queue = A.take<HandoffP<double>>(nt);
   StartRec<double>* srec = A.take<StartRec<double>>(nt);
   EndRec<double>* erec = A.take<EndRec<double>>(nt);
+  PorousRec<double>* prec = porous ? A.take<PorousRec<double>>(nt) : nullptr;
   double* cc = compute_gradient ? A.take<double>(nt) : nullptr;
   double* cd = compute_gradient ? A.take<double>(nt) : nullptr;
   int* bits = A.take<int>(1);
@@ -1181,6 +1269,11 @@ int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_
     P.queue = queue;
     P.start = srec;
     P.end = erec;
+    if (porous) {
+      P.porous = 1;
+      P.info[2] = make_info(porous);
+      P.porous_rec = prec;
+    }
     rc = run(ctx, P, cfg->precision);
     if (rc) return rc;
     if (compute_gradient) {
@@ -1202,10 +1295,12 @@ int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_
 namespace dp {
 int mc_backward_stochastic(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params* p, int rock,
                            int air, double threshold, dp_los_result* res) {
-  dp_mixture rm, am;
+  dp_mixture rm, am, pm;
   const double one = 1.0;
+  const bool porous = p->porous_material >= 0 && p->porous_thickness > 0.0;
   int rc = prepare(ctx, ph, 1, &rock, &one, &rm);
   if (!rc) rc = prepare(ctx, ph, 1, &air, &one, &am);
+  if (!rc && porous) rc = prepare(ctx, ph, 1, &p->porous_material, &one, &pm);
   if (rc) return rc;
   dp_mc_config cfg{};
   cfg.straggling = p->straggling;
@@ -1222,6 +1317,10 @@ int mc_backward_stochastic(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params
   L.energy_min = p->energy_min;
   L.energy_max = p->energy_max > p->energy_min ? p->energy_max : p->energy_min;
   L.n_samples = p->n_samples;
+  if (porous) {
+    L.porous_thickness = p->porous_thickness;
+    L.porous_density = p->porous_density;
+  }
   Arena A;
   A.base = static_cast<char*>(scratch(ctx, sizeof(dp_los) + sizeof(dp_los_result) + 1024, 2));
   A.cap = ctx->slot_bytes[2];
@@ -1233,7 +1332,9 @@ int mc_backward_stochastic(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params
     cudaError_t e = cudaMemcpyAsync(dl, &L, sizeof(L), cudaMemcpyHostToDevice, ctx->stream);
     if (e != cudaSuccess) rc = cuda_fail(ctx, e, "cudaMemcpyAsync");
   }
-  if (!rc) rc = dp_mc_run_los(ctx, ph, &rm, &am, &cfg, 1, dl, p->n_samples, dr, nullptr, &bits, 0);
+  if (!rc)
+    rc = dp_mc_run_los(ctx, ph, &rm, &am, &cfg, 1, dl, p->n_samples, dr, nullptr, &bits, 0,
+                       porous ? &pm : nullptr);
   if (!rc) {
     cudaError_t e = cudaMemcpyAsync(res, dr, sizeof(*res), cudaMemcpyDeviceToHost, ctx->stream);
     if (e != cudaSuccess) rc = cuda_fail(ctx, e, "cudaMemcpyAsync");

@@ -13,6 +13,8 @@
 #pragma once
 #include <math_constants.h>
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "dcs.cuh"
 
@@ -1210,6 +1212,14 @@ struct Hist {
   bool need_mode, strag, mixed, scat;
   Cont<R> x;     // suspended step, if x.kind != CONT_NONE
 };
+// A history of the two-layer geometry with the shallow porous layer of
+// TwoLayerGeometry (src/Geometry.jl:47-72): the porous material at density
+// prho for z in [pz, thick); pz = thick when the layer is absent.
+template <class R>
+struct HistP : Hist<R> {
+  Alt<R> pz;
+  R prho;
+};
 
 enum : int { ADV_STEP = 0, ADV_DONE = 1, ADV_WAIT = 2, ADV_HANDOFF = 3 };
 
@@ -1261,12 +1271,43 @@ __device__ __forceinline__ void boundary(F2 z, F2 thick, F2 H, bool in_air, floa
   *dens = !in_air ? rho : 1.205f * expf(-(z.h + z.l) * (1.f / 12e3f));
 }
 
+// The same with the porous top layer (src/Geometry.jl:617-635): the layer's
+// lower face at pz is a boundary in both directions.
+__device__ __forceinline__ void boundary_porous(double z, double thick, double H, double pz,
+                                                bool in_air, bool in_p, double uz, double rho,
+                                                double prho, double* tob, double* dens) {
+  const double eps = kEps64;
+  if (!in_air) {
+    *dens = in_p ? prho : rho;
+    const double next = z < pz ? pz : thick, prev = in_p ? pz : 0.0;
+    *tob = uz > eps ? (next - z) / uz : uz < -eps ? (prev - z) / uz : 1000.0;
+  } else {
+    *dens = 1.205 * exp(-z / 12e3);
+    *tob = uz > eps ? (H - z) / uz : uz < -eps ? (thick - z) / uz : 1000.0;
+  }
+}
+__device__ __forceinline__ void boundary_porous(F2 z, F2 thick, F2 H, F2 pz, bool in_air,
+                                                bool in_p, float uz, float rho, float prho,
+                                                float* tob, float* dens) {
+  const float eps = float(kEps64);
+  float ahead;
+  if (!in_air)
+    ahead = uz > eps ? (in_p ? alt_sub(thick, z) : alt_sub(pz, z))
+                     : (in_p ? alt_sub(pz, z) : -(z.h + z.l));
+  else
+    ahead = uz > eps ? alt_sub(H, z) : alt_sub(thick, z);
+  *tob = (uz > eps || uz < -eps) ? ahead / uz : 1000.f;
+  *dens = !in_air ? (in_p ? prho : rho) : 1.205f * expf(-(z.h + z.l) * (1.f / 12e3f));
+}
+
 // Advances a history by one transport step: ADV_STEP, ADV_DONE when it has
 // ended, ADV_WAIT when the step suspended on a hard-event DCS sum,
-// ADV_HANDOFF when phase 0 reached the mode switch.
-template <class R, bool COOP, int PHASE>
-__device__ __forceinline__ int advance(const Med<R>& rock, const Med<R>& air, const Consts& C,
-                                       Hist<R>& h, Stream& g) {
+// ADV_HANDOFF when phase 0 reached the mode switch.  H is Hist<R>, or
+// HistP<R> for the geometry with the porous layer (medium 2: *porous).
+template <class R, bool COOP, int PHASE, class H>
+__device__ __forceinline__ int advance(const Med<R>& rock, const Med<R>& air, const Med<R>* porous,
+                                       const Consts& C, H& h, Stream& g) {
+  constexpr bool POR = std::is_same<H, HistP<R>>::value;
   const double eps = kEps64;
   State<R>& s = h.s;
   // FP32: thresholds are exactly representable (the host rounds them), eps
@@ -1309,10 +1350,17 @@ __device__ __forceinline__ int advance(const Med<R>& rock, const Med<R>& air, co
     }
     // medium, boundary distance and step (src/Geometry.jl:603-650, :461-476)
     const bool in_air = in_air_at(s.z, h.thick);
-    const Med<R>& m = in_air ? air : rock;
-    const R uz = -s.uz;
+    int med = in_air ? 1 : 0;
     R tob, rd;
-    boundary(s.z, h.thick, h.H, in_air, uz, h.rho, &tob, &rd);
+    const R uz = -s.uz;
+    if constexpr (POR) {
+      const bool in_p = !in_air && in_air_at(s.z, h.pz);  // z >= pz
+      if (in_p) med = 2;
+      boundary_porous(s.z, h.thick, h.H, h.pz, in_air, in_p, uz, h.rho, h.prho, &tob, &rd);
+    } else {
+      boundary(s.z, h.thick, h.H, in_air, uz, h.rho, &tob, &rd);
+    }
+    const Med<R>& m = med == 0 ? rock : (POR && med == 2 ? *porous : air);
     Loc<R> Li = locate(m, s.E);
     R Xi = at(m, Li, MC_CR);
     R lim = R(0.01) * Xi / fmax(rd, R(1e-6));
@@ -1327,7 +1375,7 @@ __device__ __forceinline__ int advance(const Med<R>& rock, const Med<R>& air, co
       if constexpr (PHASE == 0) {
         if (straggled_step<R, COOP>(m, C, s, Li, rd, step, g, h.scat, h.limit, h.x)) {
           h.x.kind = CONT_STRAG;
-          h.x.medium = in_air;
+          h.x.medium = med;
           return ADV_WAIT;
         }
       }
@@ -1335,7 +1383,7 @@ __device__ __forceinline__ int advance(const Med<R>& rock, const Med<R>& air, co
       if constexpr (PHASE == 1) {
         if (mixed_step<R, COOP>(m, C, s, rd, step, g, h.limit, h.x)) {
           h.x.kind = CONT_MIXED;
-          h.x.medium = in_air;
+          h.x.medium = med;
           return ADV_WAIT;
         }
       }
@@ -1351,11 +1399,12 @@ __device__ __forceinline__ int advance(const Med<R>& rock, const Med<R>& air, co
 }
 
 // Resumes a suspended step once h.x.total (and h.x.pick) hold the DCS sum.
-template <class R, int PHASE>
-__device__ int resume(const Med<R>& rock, const Med<R>& air, const Consts& C, Hist<R>& h,
-                      Stream& g) {
+template <class R, int PHASE, class H>
+__device__ int resume(const Med<R>& rock, const Med<R>& air, const Med<R>* porous,
+                      const Consts& C, H& h, Stream& g) {
+  constexpr bool POR = std::is_same<H, HistP<R>>::value;
   Cont<R>& x = h.x;
-  const Med<R>& m = x.medium ? air : rock;
+  const Med<R>& m = x.medium == 0 ? rock : (POR && x.medium == 2 ? *porous : air);
   x.kind = CONT_NONE;
   DelOut d = del_end(x.anc, x.denom, x.total, x.pick);
   if constexpr (PHASE == 1) {
@@ -1387,6 +1436,12 @@ struct Handoff {
   uint32_t block, w0, w1, w2, w3;
   long index;       // history index (output slot)
   uint64_t stream;  // stream id
+};
+// The same with the porous layer of the history's column.
+template <class R>
+struct HandoffP : Handoff<R> {
+  Alt<R> pz;
+  R prho;
 };
 template <class R>
 __device__ __forceinline__ void save_handoff(const Hist<R>& h, const Stream& g, long i,
@@ -1444,6 +1499,12 @@ __device__ __forceinline__ long load_handoff(const Handoff<R>& v, uint64_t seed,
   return v.index;
 }
 
+// Porous layer of a history's column (HistP), written by the init kernel.
+template <class R>
+struct PorousRec {
+  Alt<R> pz;
+  R prho;
+};
 // Start record of a history, written by the init kernel in one converged
 // pass (energy, charge and geometry draws, direction), read by phase 0.
 template <class R>

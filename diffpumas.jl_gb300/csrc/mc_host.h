@@ -26,12 +26,12 @@ struct dp_mixture {
   std::vector<double> el;     // nel x kElStride
   int nel = 0;
   struct Blob {
-    uint64_t partner;
+    uint64_t partner, partner2;  // air medium, porous medium (0: none)
     int precision;
     unsigned char* dev;
     dp::mc::Layout lay;
   };
-  std::vector<Blob> blobs;    // this medium as rock, `partner` as air
+  std::vector<Blob> blobs;    // this medium as rock, `partner` as air, `partner2` as porous
 };
 
 namespace dp {

@@ -268,7 +268,9 @@ MCResult = namedtuple("MCResult", "flux sigma gradient gradient_flux gradient_me
 
 def _mc_params(physics, rock_thickness, rock_density, elevation, energy_min, energy_max,
                n_samples, compute_gradient, seed, straggling, scattering,
-               energy_threshold_low, source_energy_max, primary_altitude, precision="fp64"):
+               energy_threshold_low, source_energy_max, primary_altitude, precision="fp64",
+               porous_material=-1, porous_density=0.0, porous_thickness=0.0):
+    """dp_mc_params; porous_material is 1-based like the reference's (<= 0: none)."""
     rock = physics.materials.get("StandardRock", 0)
     air = physics.materials.get("Air", physics.n_materials - 1)
     return DpMcParams(float(rock_thickness), float(rock_density), float(elevation),
@@ -277,7 +279,27 @@ def _mc_params(physics, rock_thickness, rock_density, elevation, energy_min, ene
                       int(bool(scattering)), int(bool(compute_gradient)),
                       float(energy_threshold_low),
                       float(source_energy_max) if source_energy_max is not None else 0.0,
-                      float(primary_altitude), rock, air, PRECISION[precision])
+                      float(primary_altitude), rock, air, PRECISION[precision],
+                      int(porous_material) - 1 if porous_material > 0 else -1,
+                      float(porous_density), float(porous_thickness))
+
+
+def compute_flux(physics, rock_density, rock_thickness, elevation, energy_min, energy_max, *,
+                 n_samples=1000, seed=42, straggling=True, scattering=True,
+                 energy_threshold_low=100.0, porous_material=-1, porous_density=0.0,
+                 porous_thickness=0.0, primary_altitude=PRIMARY_ALTITUDE, precision="fp64"):
+    """compute_flux (src/Geometry.jl:899-929): (flux, sigma) of the backward MC
+    estimate over the two-layer column, with the optional shallow porous
+    layer (porous_material is a 1-based material index; <= 0 or zero
+    thickness: none)."""
+    p = _mc_params(physics, rock_thickness, rock_density, elevation, energy_min, energy_max,
+                   n_samples, False, seed, straggling, scattering, energy_threshold_low, None,
+                   primary_altitude, precision, porous_material, porous_density,
+                   porous_thickness)
+    out = DpMcResult()
+    check(load().dp_backward_mc(physics.ctx.h, physics.h, C.byref(p), C.byref(out)),
+          physics.ctx.h)
+    return out.flux, out.sigma
 
 
 def run_backward_mc(physics, *, rock_thickness=100.0, rock_density=2650.0, elevation=45.0,
@@ -463,17 +485,21 @@ def mc_histories(physics, rock, air, energy, charge, weight, *, thickness, densi
 
 LOS_FIELDS = ("thickness", "thickness_max", "density", "density_max", "elevation",
               "elevation_max", "primary_altitude", "air_height", "energy_min", "energy_max",
-              "n_samples")
+              "n_samples", "porous_thickness", "porous_density")
 
 
 def make_los(n_samples, *, thickness, density, elevation, energy_min, energy_max=None,
              thickness_max=0.0, density_max=0.0, elevation_max=0.0,
-             primary_altitude=PRIMARY_ALTITUDE, air_height=0.0):
-    """Array of dp_los records (arguments are scalars or arrays of one length)."""
+             primary_altitude=PRIMARY_ALTITUDE, air_height=0.0, porous_thickness=0.0,
+             porous_density=0.0):
+    """Array of dp_los records (arguments are scalars or arrays of one length);
+    porous_thickness / porous_density describe the shallow porous layer that
+    backward_mc_batch(porous=...) adds at the top of each rock column."""
     vals = dict(thickness=thickness, thickness_max=thickness_max, density=density,
                 density_max=density_max, elevation=elevation, elevation_max=elevation_max,
                 primary_altitude=primary_altitude, air_height=air_height, energy_min=energy_min,
-                energy_max=energy_min if energy_max is None else energy_max, n_samples=n_samples)
+                energy_max=energy_min if energy_max is None else energy_max, n_samples=n_samples,
+                porous_thickness=porous_thickness, porous_density=porous_density)
     n = max(len(np.atleast_1d(v)) for v in vals.values())
     arr = (DpLos * n)()
     cols = {k: np.broadcast_to(np.atleast_1d(v), (n,)) for k, v in vals.items()}
@@ -485,18 +511,22 @@ def make_los(n_samples, *, thickness, density, elevation, energy_min, energy_max
 
 def backward_mc_batch(physics, los, *, rock, air, seed=42, straggling=True, scattering=True,
                       energy_threshold_low=100.0, source_energy_max=None, precision="mixed",
-                      compute_gradient=False):
+                      compute_gradient=False, porous=None):
     """Batched stochastic backward MC over lines of sight (one persistent
     launch): per line of sight flux, sigma, n_samples, n_status_nonzero and,
     with compute_gradient, the CSDA surrogate's gradient_flux and gradient
-    (d flux / d density of the line)."""
+    (d flux / d density of the line).  porous: a MaterialMixture for the
+    shallow porous layer of each line (its porous_thickness and
+    porous_density, src/Geometry.jl:617-635); no gradient then."""
     n = len(los)
     out = (DpLosResult * n)()
     cfg = _mc_config(seed, straggling, scattering, energy_threshold_low, source_energy_max,
                      precision)
-    check(load().dp_mc_los(physics.ctx.h, physics.h, rock.h, air.h, C.byref(cfg), n,
-                           C.cast(los, C.c_void_p), int(bool(compute_gradient)),
-                           C.cast(out, C.c_void_p)), physics.ctx.h)
+    check(load().dp_mc_los_layers(physics.ctx.h, physics.h, rock.h,
+                                  porous.h if porous is not None else None, air.h,
+                                  C.byref(cfg), n, C.cast(los, C.c_void_p),
+                                  int(bool(compute_gradient)), C.cast(out, C.c_void_p)),
+          physics.ctx.h)
     keys = ("flux", "sigma", "n_samples", "n_status_nonzero") + \
         (("gradient", "gradient_flux") if compute_gradient else ())
     return {k: np.array([getattr(r, k) for r in out]) for k in keys}
@@ -524,6 +554,9 @@ from .calibration import (calibrate_csda_correction,  # noqa: E402
                           csda_geom_multiplier, csda_material_multiplier, load_csda_corrections,
                           path_rock_length, save_csda_corrections)
 from .directional import cell_density  # noqa: E402
+from .uncertainty import (SystematicSourceResult, TransportUncertaintyResult,  # noqa: E402
+                          TransportVariation, compute_flux_uncertainty,
+                          estimate_transport_uncertainty, relative_uncertainty_percent)
 
 
 # ----------------------------------------------------------------- tomography

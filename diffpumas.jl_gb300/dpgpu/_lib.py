@@ -40,7 +40,9 @@ class DpMcParams(C.Structure):
                 ("straggling", C.c_int), ("scattering", C.c_int),
                 ("compute_gradient", C.c_int), ("energy_threshold_low", C.c_double),
                 ("source_energy_max", C.c_double), ("primary_altitude", C.c_double),
-                ("rock_material", C.c_int), ("air_material", C.c_int), ("precision", C.c_int)]
+                ("rock_material", C.c_int), ("air_material", C.c_int), ("precision", C.c_int),
+                ("porous_material", C.c_int), ("porous_density", C.c_double),
+                ("porous_thickness", C.c_double)]
 
 
 class DpMcResult(C.Structure):
@@ -58,7 +60,8 @@ class DpMcConfig(C.Structure):
 class DpLos(C.Structure):
     _fields_ = [(k, C.c_double) for k in (
         "thickness", "thickness_max", "density", "density_max", "elevation", "elevation_max",
-        "primary_altitude", "air_height", "energy_min", "energy_max")] + [("n_samples", C.c_long)]
+        "primary_altitude", "air_height", "energy_min", "energy_max")] + [("n_samples", C.c_long)] + \
+        [("porous_thickness", C.c_double), ("porous_density", C.c_double)]
 
 
 class DpLosResult(C.Structure):
@@ -172,6 +175,9 @@ PROTOTYPES = {
                              _VP, _VP, _I, C.c_uint64, _VP, _VP, _VP, _VP]),
     "dp_mc_los": (_I, [_P, _P, _P, _P, C.POINTER(DpMcConfig), _L, _VP, _I, _VP]),
     "dp_mc_los_dev": (_I, [_P, _P, _P, _P, C.POINTER(DpMcConfig), _L, _VP, _L, _I, _VP]),
+    "dp_mc_los_layers": (_I, [_P, _P, _P, _P, _P, C.POINTER(DpMcConfig), _L, _VP, _I, _VP]),
+    "dp_mc_los_layers_dev": (_I, [_P, _P, _P, _P, _P, C.POINTER(DpMcConfig), _L, _VP, _L, _I,
+                                  _VP]),
     "dp_dir_csda": (_I, [_P, _P, C.POINTER(DpCsdaConfig), C.POINTER(DpCsdaBatch), _L, _VP, _VP,
                          _VP, _VP, _I]),
     "dp_dir_csda_dev": (_I, [_P, _P, C.POINTER(DpCsdaConfig), C.POINTER(DpCsdaBatch), _L, _VP,

@@ -200,6 +200,15 @@ typedef struct {
   int air_material;          /* -1: "Air" or the last table */
   int precision;             /* stochastic transport: DP_PREC_FP64 (0) or
                                 DP_PREC_MIXED (1); the CSDA path is FP64 */
+  /* Shallow porous layer of TwoLayerGeometry (src/Geometry.jl:47-72,
+   * compute_flux's porous_* keywords, :899): the top porous_thickness m of
+   * the rock column are material porous_material at porous_density.  Active
+   * when porous_material >= 0 and porous_thickness > 0; the column then runs
+   * through the stochastic kernels (CSDA steps when straggling = scattering
+   * = 0), without the CSDA gradient. */
+  int porous_material;       /* -1: none */
+  double porous_density;     /* kg/m^3 */
+  double porous_thickness;   /* m */
 } dp_mc_params;
 
 typedef struct {
@@ -211,7 +220,8 @@ typedef struct {
   long n_status_nonzero;     /* histories that hit a cap (see DP_ST_*) */
 } dp_mc_result;
 
-/* Whole estimator: device sampling, transport, deterministic reduction.
+/* Whole estimator (_compute_flux_estimate, src/Geometry.jl:818-896): device
+ * sampling, transport, deterministic reduction.
  * straggling = scattering = 0: deterministic CSDA transport; otherwise the
  * stochastic dual-mode transport (straggled with scattering below
  * energy_threshold_low, mixed above, src/Geometry.jl:534-672) of the rock
@@ -305,6 +315,9 @@ typedef struct {
   double primary_altitude, air_height;
   double energy_min, energy_max;
   long n_samples;
+  /* the shallow porous layer's thickness and density (src/Geometry.jl:47-72),
+   * used by the *_layers calls with a porous medium; 0: no layer */
+  double porous_thickness, porous_density;
 } dp_los;
 
 typedef struct {
@@ -330,6 +343,17 @@ int dp_mc_los(dp_ctx* ctx, const dp_physics* phys, const dp_mixture* rock, const
 int dp_mc_los_dev(dp_ctx* ctx, const dp_physics* phys, const dp_mixture* rock,
                   const dp_mixture* air, const dp_mc_config* cfg, long n_los, const dp_los* los,
                   long total_samples, int compute_gradient, dp_los_result* out);
+/* The same columns with the shallow porous top layer of TwoLayerGeometry
+ * (src/Geometry.jl:617-635): z in [thickness - porous_thickness, thickness)
+ * is the prepared medium `porous` at each line's porous_density.  NULL
+ * porous: dp_mc_los.  No CSDA gradient (compute_gradient must be 0). */
+int dp_mc_los_layers(dp_ctx* ctx, const dp_physics* phys, const dp_mixture* rock,
+                     const dp_mixture* porous, const dp_mixture* air, const dp_mc_config* cfg,
+                     long n_los, const dp_los* los, int compute_gradient, dp_los_result* out);
+int dp_mc_los_layers_dev(dp_ctx* ctx, const dp_physics* phys, const dp_mixture* rock,
+                         const dp_mixture* porous, const dp_mixture* air,
+                         const dp_mc_config* cfg, long n_los, const dp_los* los,
+                         long total_samples, int compute_gradient, dp_los_result* out);
 
 /* ---------------------------------------------------------- fixed-path MC
  * compute_directional_flux_mc (src/Tomography.jl:979-1041) over many

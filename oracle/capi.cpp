@@ -272,12 +272,15 @@ void orc_tomo_vjp(void* h, int rock, int air, const int* dims, const double* geo
 // the arrays (index i, or index 0 when the stride flag is 0), final energy
 // E[i], charge q[i]; the random stream is (seed, id0 + i).  Outputs the flux
 // contribution w[i]*flux, the status bits, the step count and the final energy.
+// porous >= 0 adds the shallow porous layer of that material with
+// porous_thickness / porous_density (per history when geo_per_history).
 void orc_mc_histories(void* h, int n_rock, const int* rock_mats, const double* rock_fracs, int air,
                       long n, const double* thick, const double* dens, const double* elev,
                       const double* H, int geo_per_history, const double* E, const double* q,
                       const double* w, uint64_t seed, uint64_t id0, int straggling, int scattering,
                       double threshold_low, double source_max, double* contrib, int* status,
-                      long* steps, double* Efinal, int nthreads) {
+                      long* steps, double* Efinal, int nthreads, int porous,
+                      const double* porous_thickness, const double* porous_density) {
   Physics* p = static_cast<Physics*>(h);
   Mixture rm;
   double tot = 0;
@@ -294,6 +297,14 @@ void orc_mc_histories(void* h, int n_rock, const int* rock_mats, const double* r
   md.air = make_medium(*p, am);
   md.krock = prepare_mixed_kernel(*p, rm);
   md.kair = prepare_mixed_kernel(*p, am);
+  if (porous >= 0) {
+    Mixture pm;
+    pm.mats.push_back(porous);
+    pm.fracs.push_back(1.0);
+    md.has_porous = true;
+    md.porous = make_medium(*p, pm);
+    md.kporous = prepare_mixed_kernel(*p, pm);
+  }
   McOptions o;
   o.straggling = straggling != 0;
   o.scattering = scattering != 0;
@@ -303,6 +314,10 @@ void orc_mc_histories(void* h, int n_rock, const int* rock_mats, const double* r
   for (long i = 0; i < n; ++i) {
     long gi = geo_per_history ? i : 0;
     McGeometry geo{thick[gi], dens[gi], elev[gi], H[gi]};
+    if (porous >= 0) {
+      geo.porous_thickness = porous_thickness[gi];
+      geo.porous_density = porous_density[gi];
+    }
     Rng g;
     g.seed = seed;
     g.id = id0 + uint64_t(i);

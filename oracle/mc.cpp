@@ -745,12 +745,19 @@ double stochastic_history(const Physics& p, const McMedia& md, const McGeometry&
       if (s.w <= 0 || !std::isfinite(s.w)) break;
       double uz = -s.uz;
       bool in_air = s.z >= geo.thickness;
-      const Medium& m = in_air ? md.air : md.rock;
-      const MixedKernel& k = in_air ? md.kair : md.krock;
+      // the porous top layer z in [thickness - porous_thickness, thickness)
+      // (src/Geometry.jl:617-635)
+      const bool has_p = md.has_porous && geo.porous_thickness > 0;
+      const double pz = has_p ? geo.thickness - geo.porous_thickness : geo.thickness;
+      const bool in_p = !in_air && has_p && s.z >= pz;
+      const Medium& m = in_air ? md.air : in_p ? md.porous : md.rock;
+      const MixedKernel& k = in_air ? md.kair : in_p ? md.kporous : md.krock;
       double dens, tob;
       if (!in_air) {
-        dens = geo.density;
-        tob = uz > eps ? (geo.thickness - s.z) / uz : uz < -eps ? (0.0 - s.z) / uz : 1000.0;
+        dens = in_p ? geo.porous_density : geo.density;
+        const double next = has_p && s.z < pz ? pz : geo.thickness;
+        const double prev = has_p && s.z >= pz ? pz : 0.0;
+        tob = uz > eps ? (next - s.z) / uz : uz < -eps ? (prev - s.z) / uz : 1000.0;
       } else {
         dens = 1.205 * std::exp(-s.z / 12e3);
         tob = uz > eps ? (H - s.z) / uz : uz < -eps ? (geo.thickness - s.z) / uz : 1000.0;

@@ -74,9 +74,15 @@ void straggled_step(const Physics& p, const Medium& m, const MixedKernel& kern, 
 struct McMedia {
   Medium rock, air;
   MixedKernel krock, kair;
+  // shallow porous layer of TwoLayerGeometry (src/Geometry.jl:47-72): a
+  // single material
+  bool has_porous = false;
+  Medium porous;
+  MixedKernel kporous;
 };
 struct McGeometry {
   double thickness, density, elevation, primary_altitude;
+  double porous_thickness = 0, porous_density = 0;  // the top of the rock column
 };
 struct McOptions {
   bool straggling = true, scattering = true;

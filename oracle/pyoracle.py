@@ -91,7 +91,7 @@ def lib():
         L.orc_mc_histories.argtypes = [_P, _I, _IP, _DP, _I, _L, _DP, _DP, _DP, _DP, _I, _DP, _DP,
                                        _DP, _U64, _U64, _I, _I, _D, _D, _DP, _IP,
                                        np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS"),
-                                       _DP, _I]
+                                       _DP, _I, _I, _DP, _DP]
         _I64P = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
         L.orc_dir_histories.argtypes = [_P, _I, _IP, _IP, _DP, _I, _D, _I, _D, _L, _DP, _DP, _DP,
                                         _I64P, _IP, _DP, _DP, _I64P, _DP, _DP, _DP, _U64, _U64,
@@ -427,17 +427,20 @@ def mixed_kernel(p, mats, fracs=None):
 
 def mc_histories(p, rock, air, thickness, density, elevation, H, E, q, w, seed, id0=0,
                  straggling=True, scattering=True, threshold_low=100.0, source_max=1e9,
-                 rock_fracs=None, threads=0):
+                 rock_fracs=None, threads=0, porous=-1, porous_thickness=0.0,
+                 porous_density=0.0):
     """Stochastic backward histories (the dual-mode loop of src/Geometry.jl:534-757).
 
     rock: a material index or a list of indices (mixture with rock_fracs);
-    geometry arguments are scalars or per-history arrays.  Returns
-    (contribution w*f, status, steps, final energy) per history."""
+    porous >= 0: the shallow porous layer of that material (porous_thickness,
+    porous_density); geometry arguments are scalars or per-history arrays.
+    Returns (contribution w*f, status, steps, final energy) per history."""
     rock = np.atleast_1d(np.asarray(rock, np.int32))
     fr = _arr(rock_fracs if rock_fracs is not None else np.ones(len(rock)))
     E, q, w = _arr(E), _arr(q), _arr(w)
     n = len(E)
-    geo = [_arr(np.atleast_1d(v)) for v in (thickness, density, elevation, H)]
+    geo = [_arr(np.atleast_1d(v)) for v in (thickness, density, elevation, H, porous_thickness,
+                                            porous_density)]
     per = int(any(len(g) > 1 for g in geo))
     if per:
         geo = [_arr(np.broadcast_to(g, (n,))) for g in geo]
@@ -447,5 +450,6 @@ def mc_histories(p, rock, air, thickness, density, elevation, H, E, q, w, seed, 
     threads = threads or os.cpu_count()
     lib().orc_mc_histories(p.h, len(rock), rock, fr, air, n, geo[0], geo[1], geo[2], geo[3], per,
                            E, q, w, seed, id0, int(straggling), int(scattering), threshold_low,
-                           source_max, contrib, status, steps, Ef, threads)
+                           source_max, contrib, status, steps, Ef, threads, int(porous), geo[4],
+                           geo[5])
     return contrib, status, steps, Ef

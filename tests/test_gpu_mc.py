@@ -326,3 +326,94 @@ def test_autotune_keeps_the_fastest_size(dp, phys, media):
             dp.set_mc_threads(phys, "mc", "fp64", 512)
     finally:
         dp.set_mc_threads(phys, "mc", "mixed", 0)
+
+
+# ------------------------------------------------------------------ porous layer
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_porous_layer_batch_matches_oracle(dp, phys, media, oracle, orc_phys, precision):
+    """dp_mc_los_layers: the shallow porous top layer of TwoLayerGeometry
+    (src/Geometry.jl:617-635; here water at 1000 kg/m^3 over the top 25-60 m
+    of rock) against the oracle's histories on the same streams: FP64 per line
+    of sight within 0.5 sigma (to 1e-9 when no history flips), mixed
+    precision within 3 sigma.  A zero-thickness layer is no layer (the
+    porous kernel is compiled apart, so to within its sigma, not bitwise)."""
+    rock, air, _ = media
+    water = dp.MaterialMixture(phys, 3)
+    depth = np.array([60.0, 150.0, 400.0])
+    pt = np.array([25.0, 60.0, 40.0])
+    ns = np.array([400, 800, 600])
+    kw = dict(thickness=depth, density=2650.0, elevation=70.0, energy_min=1.0, energy_max=1e4,
+              air_height=1000.0)
+    los = dp.make_los(ns, porous_thickness=pt, porous_density=1000.0, **kw)
+    out = dp.backward_mc_batch(phys, los, rock=rock, air=air, porous=water, seed=3,
+                               precision=precision, scattering=True)
+    E, q, w = dp.mc_samples(phys, energy_min=1.0, energy_max=1e4, n_samples=int(ns.sum()), seed=3)
+    off = np.concatenate([[0], np.cumsum(ns)])
+    for l in range(3):
+        sl = slice(off[l], off[l + 1])
+        oc, ost, _, _ = oracle.mc_histories(orc_phys, [0], 1, depth[l], 2650.0, 70.0,
+                                            depth[l] + 1000.0, E[sl], q[sl], w[sl], seed=3,
+                                            id0=int(off[l]), porous=2, porous_thickness=pt[l],
+                                            porous_density=1000.0)
+        assert np.all(ost == 0)
+        f = oc.mean()
+        s = math.sqrt(max((oc ** 2).mean() - f * f, 0.0) / ns[l])
+        assert out["n_status_nonzero"][l] == 0
+        bar = max(0.5 * s, 1e-9 * abs(f)) if precision == "fp64" else 3 * s + 1e-3 * abs(f)
+        assert abs(out["flux"][l] - f) <= bar, (l, out["flux"][l], f, s)
+    plain = dp.backward_mc_batch(phys, dp.make_los(ns, **kw), rock=rock, air=air, seed=3,
+                                 precision=precision, scattering=True)
+    zero = dp.backward_mc_batch(phys, dp.make_los(ns, porous_thickness=0.0, porous_density=1000.0,
+                                                  **kw),
+                                rock=rock, air=air, porous=water, seed=3, precision=precision,
+                                scattering=True)
+    assert np.all(np.abs(zero["flux"] - plain["flux"]) <= 0.5 * plain["sigma"] + 1e-12)
+    assert np.all(out["flux"] > plain["flux"])
+    with pytest.raises(ValueError):
+        dp.backward_mc_batch(phys, los, rock=rock, air=air, porous=water, compute_gradient=True)
+
+
+def test_compute_flux_with_porous_layer(dp, phys, oracle, orc_phys):
+    """compute_flux (src/Geometry.jl:899-929) with porous_* keywords: in CSDA
+    mode (straggling = scattering = false) the estimate is deterministic
+    given the samples and equals the oracle's to 1e-10; with straggling and
+    scattering it agrees within 3 sigma."""
+    n = 2000
+    kw = dict(n_samples=n, seed=11, porous_material=3, porous_density=1000.0,
+              porous_thickness=20.0)
+    f, s = dp.compute_flux(phys, 2650.0, 80.0, 55.0, 1.0, 50.0, straggling=False,
+                           scattering=False, **kw)
+    E, q, w = dp.mc_samples(phys, energy_min=1.0, energy_max=50.0, n_samples=n, seed=11)
+    oc, ost, _, _ = oracle.mc_histories(orc_phys, [0], 1, 80.0, 2650.0, 55.0, 3e4, E, q, w,
+                                        seed=11, straggling=False, scattering=False, porous=2,
+                                        porous_thickness=20.0, porous_density=1000.0)
+    assert np.all(ost == 0)
+    assert f == pytest.approx(oc.mean(), rel=1e-10)
+    assert s == pytest.approx(math.sqrt(max((oc ** 2).mean() - oc.mean() ** 2, 0.0) / n),
+                              rel=1e-8)
+    f2, s2 = dp.compute_flux(phys, 2650.0, 80.0, 55.0, 1.0, 50.0, **kw)
+    oc2, _, _, _ = oracle.mc_histories(orc_phys, [0], 1, 80.0, 2650.0, 55.0, 3e4, E, q, w,
+                                       seed=11, porous=2, porous_thickness=20.0,
+                                       porous_density=1000.0)
+    assert abs(f2 - oc2.mean()) <= 3 * s2
+    with pytest.raises(ValueError):
+        dp.compute_flux(phys, 2650.0, 80.0, 55.0, 1.0, 50.0, porous_material=3,
+                        porous_thickness=20.0, porous_density=0.0)
+
+
+def test_flux_uncertainty_budget(dp):
+    """test/runtests.jl:222-245 on the device: compute_flux_uncertainty with
+    create_physics(n_energies=30, K_min=0.05, K_max=1e4); every variation
+    reuses the nominal seed (common random numbers)."""
+    physics = dp.create_physics(n_energies=30, K_min=0.05, K_max=1e4)
+    b = dp.compute_flux_uncertainty(physics, 2650.0, 25.0, 55.0, 1.0, 50.0, n_samples=8,
+                                    seed=11, straggling=True, scattering=True,
+                                    energy_threshold_low=50.0, threshold_factors=(0.5, 2.0))
+    for v in (b.value, b.sigma_mc, b.sigma_syst, b.sigma_total):
+        assert math.isfinite(v)
+    assert b.sigma_mc >= 0.0 and b.sigma_syst >= 0.0
+    assert b.sigma_total >= b.sigma_mc and b.sigma_total >= b.sigma_syst
+    assert len(b.sources["energy_threshold_low"].variant_values) == 2
+    f, s = dp.compute_flux(physics, 2650.0, 25.0, 55.0, 1.0, 50.0, n_samples=8, seed=11,
+                           energy_threshold_low=50.0)
+    assert (b.value, b.sigma_mc) == (f, s)

@@ -174,3 +174,38 @@ def test_history_streams_are_independent_of_threads(oracle, orc_default):
         assert np.array_equal(x, y)
     for x, y in zip(a, c):
         assert np.array_equal(x[5:], y)
+
+
+def test_porous_layer_geometry(oracle, orc_default):
+    """The shallow porous layer of TwoLayerGeometry (src/Geometry.jl:47-72,
+    617-635) in the oracle's dual-mode loop: a layer of zero thickness is no
+    layer (bit for bit); in CSDA mode a layer of the rock itself changes only
+    the step boundaries, and a lighter layer equals a rock column of the same
+    grammage (vertical, same air column above the rock top)."""
+    p = orc_default
+    n = 400
+    rng = np.random.default_rng(3)
+    E = np.exp(rng.uniform(0.0, math.log(1e4), n))
+    q = np.where(rng.random(n) > 0.5, 1.0, -1.0)
+    w = 2 * E * math.log(1e4)
+    base = oracle.mc_histories(p, 0, 1, 100.0, 2650.0, 60.0, 1100.0, E, q, w, seed=4)
+    zero = oracle.mc_histories(p, 0, 1, 100.0, 2650.0, 60.0, 1100.0, E, q, w, seed=4, porous=0,
+                               porous_thickness=0.0, porous_density=1500.0)
+    for x, y in zip(base, zero):
+        assert np.array_equal(x, y)
+    csda = dict(straggling=False, scattering=False)
+    plain = oracle.mc_histories(p, 0, 1, 100.0, 2650.0, 90.0, 1100.0, E, q, w, seed=4, **csda)[0]
+    same = oracle.mc_histories(p, 0, 1, 100.0, 2650.0, 90.0, 1100.0, E, q, w, seed=4, porous=0,
+                               porous_thickness=30.0, porous_density=2650.0, **csda)[0]
+    np.testing.assert_allclose(same, plain, rtol=1e-6, atol=0)
+    light = oracle.mc_histories(p, 0, 1, 100.0, 2650.0, 90.0, 1100.0, E, q, w, seed=4, porous=0,
+                                porous_thickness=30.0, porous_density=1500.0, **csda)[0]
+    t_eq = 70.0 + 30.0 * 1500.0 / 2650.0
+    equiv = oracle.mc_histories(p, 0, 1, t_eq, 2650.0, 90.0, t_eq + 1000.0, E, q, w, seed=4,
+                                **csda)[0]
+    assert (light > 0).sum() > n // 4
+    np.testing.assert_allclose(light, equiv, rtol=2e-4, atol=1e-12 * light.max())
+    assert light.sum() > plain.sum()
+    st = oracle.mc_histories(p, 0, 1, 100.0, 2650.0, 60.0, 1100.0, E, q, w, seed=4, porous=0,
+                             porous_thickness=30.0, porous_density=1500.0)
+    assert np.all(st[1] == 0) and st[0].sum() > base[0].sum()
