@@ -1,5 +1,6 @@
 // api.cu -- context, error handling and physics-table handles of libdpgpu.
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <new>
 
@@ -308,6 +309,152 @@ int dp_physics_create(dp_ctx* ctx, const dp_settings* st, int n_mat, const dp_ma
   return finish_upload(ctx, p, out);
 }
 
+int dp_tables_from_dedx(const dp_settings* st, int n_mat, const dp_material* mats,
+                        const char* const* dedx_paths, int* n_energies, double* cols,
+                        long cap) {
+  if (!st || n_mat <= 0 || !mats || !dedx_paths || !n_energies) return DP_ERR_ARG;
+  std::vector<dp::DedxTable> t(n_mat);
+  std::string err;
+  for (int m = 0; m < n_mat; ++m) {
+    if (!dedx_paths[m] || !dp::load_dedx_table(dedx_paths[m], &t[m], &err)) return DP_ERR_ARG;
+    if (t[m].K != t[0].K) return DP_ERR_ARG;  // one energy grid for every material
+  }
+  const int n = int(t[0].K.size());
+  *n_energies = n;
+  if (!cols) return DP_OK;
+  if (cap < long(n_mat) * DP_NCOL * n) return DP_ERR_ARG;
+  for (int m = 0; m < n_mat; ++m) {
+    dp::HostMaterial h;
+    if (!to_host_material(mats[m], h)) return DP_ERR_ARG;
+    dp::build_dedx_table(h, t[m], *st, cols + size_t(m) * DP_NCOL * n);
+  }
+  return DP_OK;
+}
+
+int dp_physics_create_dedx(dp_ctx* ctx, const dp_settings* st, int n_mat,
+                           const dp_material* mats, const char* const* dedx_paths,
+                           dp_physics** out) {
+  if (!ctx || !st || !mats || !dedx_paths || !out || n_mat <= 0)
+    return fail(ctx, DP_ERR_ARG, "bad arguments");
+  std::vector<dp::DedxTable> t(n_mat);
+  std::string err;
+  for (int m = 0; m < n_mat; ++m) {
+    if (!dedx_paths[m]) return fail(ctx, DP_ERR_ARG, "missing dE/dx file path");
+    if (!dp::load_dedx_table(dedx_paths[m], &t[m], &err)) return fail(ctx, DP_ERR_ARG, err);
+    if (t[m].K != t[0].K)
+      return fail(ctx, DP_ERR_ARG, "the dE/dx files do not share one energy grid");
+  }
+  dp_physics* p = new dp_physics;
+  p->settings = *st;
+  p->n_mat = n_mat;
+  p->n = int(t[0].K.size());
+  p->host.assign(size_t(n_mat) * DP_NCOL * p->n, 0.0);
+  p->recipes.resize(n_mat);
+  for (int m = 0; m < n_mat; ++m) {
+    if (!to_host_material(mats[m], p->recipes[m])) {
+      delete p;
+      return fail(ctx, DP_ERR_ARG, "invalid material recipe");
+    }
+    dp::build_dedx_table(p->recipes[m], t[m], *st, &p->host[size_t(m) * DP_NCOL * p->n]);
+    p->recipes[m].ZoA = t[m].ZoA;
+  }
+  p->has_recipes = true;
+  return finish_upload(ctx, p, out);
+}
+
+// Portable table file (little-endian, the byte order of x86-64 and AArch64):
+//   "DPGPUTAB" | u32 version (1) | u32 n_materials | u32 n_energies |
+//   u32 has_recipes | f64 mass, ctau, cutoff, elastic_ratio |
+//   per material (has_recipes): u32 name length, name bytes, f64 density,
+//   I, ZoA, u32 n_elements, n_elements x f64 (Z, A, I, fraction) |
+//   n_materials x DP_NCOL x n_energies f64 columns (dp_column order).
+}  // extern "C"
+namespace {
+constexpr char kTabMagic[8] = {'D', 'P', 'G', 'P', 'U', 'T', 'A', 'B'};
+struct FileCloser {
+  FILE* f;
+  ~FileCloser() {
+    if (f) std::fclose(f);
+  }
+};
+template <class T>
+bool put(FILE* f, const T& v) {
+  return std::fwrite(&v, sizeof(T), 1, f) == 1;
+}
+template <class T>
+bool get(FILE* f, T* v) {
+  return std::fread(v, sizeof(T), 1, f) == 1;
+}
+}  // namespace
+extern "C" {
+
+int dp_physics_save(const dp_physics* p, const char* path) {
+  if (!p || !path) return DP_ERR_ARG;
+  FileCloser fc{std::fopen(path, "wb")};
+  FILE* f = fc.f;
+  if (!f) return DP_ERR_ARG;
+  bool ok = std::fwrite(kTabMagic, 1, 8, f) == 8 && put(f, uint32_t(1)) &&
+            put(f, uint32_t(p->n_mat)) && put(f, uint32_t(p->n)) &&
+            put(f, uint32_t(p->has_recipes ? 1 : 0)) && put(f, p->settings.mass) &&
+            put(f, p->settings.ctau) && put(f, p->settings.cutoff) &&
+            put(f, p->settings.elastic_ratio);
+  if (ok && p->has_recipes)
+    for (const auto& r : p->recipes) {
+      ok = ok && put(f, uint32_t(r.name.size())) &&
+           std::fwrite(r.name.data(), 1, r.name.size(), f) == r.name.size() &&
+           put(f, r.density) && put(f, r.I) && put(f, r.ZoA) &&
+           put(f, uint32_t(r.elements.size()));
+      for (const auto& e : r.elements)
+        ok = ok && put(f, e.Z) && put(f, e.A) && put(f, e.I) && put(f, e.fraction);
+    }
+  ok = ok && std::fwrite(p->host.data(), sizeof(double), p->host.size(), f) == p->host.size();
+  return ok ? DP_OK : DP_ERR_ARG;
+}
+
+int dp_physics_load(dp_ctx* ctx, const char* path, dp_physics** out) {
+  if (!ctx || !path || !out) return fail(ctx, DP_ERR_ARG, "bad arguments");
+  FileCloser fc{std::fopen(path, "rb")};
+  FILE* f = fc.f;
+  if (!f) return fail(ctx, DP_ERR_ARG, std::string("cannot open ") + path);
+  char magic[8];
+  uint32_t version = 0, n_mat = 0, n = 0, has = 0;
+  dp_settings st{};
+  if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kTabMagic, 8) != 0 ||
+      !get(f, &version) || version != 1 || !get(f, &n_mat) || !get(f, &n) || !get(f, &has) ||
+      !get(f, &st.mass) || !get(f, &st.ctau) || !get(f, &st.cutoff) ||
+      !get(f, &st.elastic_ratio) || n_mat == 0 || n_mat > 4096 || n < 2 || n > (1u << 24))
+    return fail(ctx, DP_ERR_ARG, "not a version-1 physics table file");
+  dp_physics* p = new dp_physics;
+  p->settings = st;
+  p->n_mat = int(n_mat);
+  p->n = int(n);
+  bool ok = true;
+  if (has) {
+    p->recipes.resize(n_mat);
+    for (auto& r : p->recipes) {
+      uint32_t len = 0, ne = 0;
+      ok = ok && get(f, &len) && len < (1u << 16);
+      if (!ok) break;
+      r.name.resize(len);
+      ok = ok && std::fread(&r.name[0], 1, len, f) == len && get(f, &r.density) &&
+           get(f, &r.I) && get(f, &r.ZoA) && get(f, &ne) && ne < 4096;
+      for (uint32_t k = 0; ok && k < ne; ++k) {
+        dp::HostElement e{};
+        ok = get(f, &e.Z) && get(f, &e.A) && get(f, &e.I) && get(f, &e.fraction);
+        r.elements.push_back(e);
+      }
+    }
+    p->has_recipes = ok;
+  }
+  p->host.resize(size_t(n_mat) * DP_NCOL * n);
+  ok = ok && std::fread(p->host.data(), sizeof(double), p->host.size(), f) == p->host.size();
+  if (!ok) {
+    delete p;
+    return fail(ctx, DP_ERR_ARG, "truncated physics table file");
+  }
+  return finish_upload(ctx, p, out);
+}
+
 int dp_physics_free(dp_physics* p) {
   if (!p) return DP_ERR_ARG;
   if (p->dev) {
@@ -330,6 +477,20 @@ int dp_physics_column(const dp_physics* p, int mat, int col, double* out) {
   if (!p || !out || mat < 0 || mat >= p->n_mat || col < 0 || col >= DP_NCOL) return DP_ERR_ARG;
   std::memcpy(out, &p->host[(size_t(mat) * DP_NCOL + col) * p->n], sizeof(double) * p->n);
   return DP_OK;
+}
+
+int dp_physics_settings(const dp_physics* p, dp_settings* out) {
+  if (!p || !out) return DP_ERR_ARG;
+  *out = p->settings;
+  return DP_OK;
+}
+
+int dp_physics_material_name(const dp_physics* p, int m, char* buf, int cap) {
+  if (!p || !p->has_recipes || m < 0 || m >= p->n_mat || !buf) return -1;
+  const std::string& s = p->recipes[m].name;
+  if (int(s.size()) + 1 > cap) return -1;
+  std::memcpy(buf, s.c_str(), s.size() + 1);
+  return int(s.size());
 }
 
 int dp_physics_material_index(const dp_physics* p, const char* name) {

@@ -46,6 +46,17 @@ struct HostMaterial {
 };
 void build_empirical_table(const HostMaterial& m, const dp_settings& st, int n, double Kmin,
                            double Kmax, double* cols);
+// A PUMAS dE/dx table (src/DEDXLoader.jl:26-43) in GeV and kg/m^2.
+struct DedxTable {
+  double ZoA = 0;
+  std::vector<double> K, ion, brems, pair, photo, S, R;
+};
+// load_dedx_file (src/DEDXLoader.jl:49-190); false with *err set on failure.
+bool load_dedx_table(const char* path, DedxTable* t, std::string* err);
+// create_material_table_from_dedx (src/Physics.jl:146-273): DP_NCOL x n
+// columns on the file's grid (n = t.K.size()).
+void build_dedx_table(const HostMaterial& m, const DedxTable& t, const dp_settings& st,
+                      double* cols);
 double host_dcs_moment(int proc, double Z, double A, double I, double mass, double K, double xlo,
                        double xhi, int mode);
 // Brackets one named kernel launch with events when timing is enabled; the

@@ -1,11 +1,16 @@
 // physics_build.cu -- host-side construction of the muon physics tables,
-// the product counterpart of create_physics(MUON) without PUMAS dE/dx files:
-// src/Physics.jl:280-408 (create_material_table_empirical), :534-599
-// (create_physics), src/Materials.jl:360-507 (atomic shells, Fano density
-// effect, electronic stopping) and :939-1007 (DCS energy moments).
+// the product counterpart of create_physics(MUON): src/Physics.jl:280-408
+// (create_material_table_empirical, no PUMAS dE/dx files), :146-273
+// (create_material_table_from_dedx) with src/DEDXLoader.jl:49-190
+// (load_dedx_file), :534-599 (create_physics), src/Materials.jl:360-507
+// (atomic shells, Fano density effect, electronic stopping) and :939-1007
+// (DCS energy moments).
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
+#include <fstream>
+#include <sstream>
 #include <thread>
 #include <vector>
 
@@ -473,6 +478,29 @@ void parallel_for(int n, F f) {
   for (auto& x : th) x.join();
 }
 
+// Coulomb scattering tables (src/Physics.jl:386-397, :234-256 from the
+// CSDA range and m.ZoA) and the per-node kinematic columns (spin factor,
+// magnetic rotation, elastic cutoff angle).
+void coulomb_and_kinematics(const HostMaterial& m, const dp_settings& st, int n, double* cols) {
+  auto C = [&](int c) { return cols + size_t(c) * n; };
+  const double mass = st.mass, cut = st.cutoff;
+  const double *E = C(DP_COL_E), *R = C(DP_COL_CSDA_R);
+  const double aS = m.I * 1e9 / (28.816 * std::sqrt(m.ZoA * m.density * 1e-3));
+  parallel_for(n, [&](int i) {
+    coulomb_node(m, mass, st.elastic_ratio, cut, aS, E[i], R[i], C(DP_COL_LB1) + i,
+                 C(DP_COL_LBE) + i, C(DP_COL_MU0) + i);
+  });
+  for (int i = 0; i < n; ++i) {
+    double K = E[i], g = 1.0 + K / mass, b = std::sqrt(1.0 - 1.0 / (g * g));
+    double p = std::sqrt(K * (K + 2 * mass)), e = K + mass;
+    C(DP_COL_FSPIN)[i] = K * (e + mass) / (e * e);
+    C(DP_COL_MAGROT)[i] = kLarmor / (b * p);
+    double mu0 = C(DP_COL_MU0)[i];
+    C(DP_COL_ECUT)[i] = mu0 < 1e-8 ? 2.0 * std::sqrt(std::max(mu0, 0.0))
+                                   : std::acos(std::max(1.0 - 2.0 * mu0, -1.0));
+  }
+}
+
 }  // namespace
 
 // src/Physics.jl:280-408.  Columns per DP_COL_*, the Coulomb scattering
@@ -527,21 +555,126 @@ void build_empirical_table(const HostMaterial& m, const dp_settings& st, int n, 
     double b = std::sqrt(1.0 - 1.0 / (g * g)), bp = std::sqrt(1.0 - 1.0 / (gp * gp));
     T[i] = T[i - 1] + dK / (((S[i] + S[i - 1]) / 2) * ((b + bp) / 2) * ((g + gp) / 2));
   }
-  // Coulomb scattering tables (src/Physics.jl:386-397)
-  const double aS = m.I * 1e9 / (28.816 * std::sqrt(m.ZoA * m.density * 1e-3));
-  parallel_for(n, [&](int i) {
-    coulomb_node(m, mass, st.elastic_ratio, cut, aS, E[i], R[i], C(DP_COL_LB1) + i,
-                 C(DP_COL_LBE) + i, C(DP_COL_MU0) + i);
-  });
-  for (int i = 0; i < n; ++i) {
-    double K = E[i], g = 1.0 + K / mass, b = std::sqrt(1.0 - 1.0 / (g * g));
-    double p = std::sqrt(K * (K + 2 * mass)), e = K + mass;
-    C(DP_COL_FSPIN)[i] = K * (e + mass) / (e * e);
-    C(DP_COL_MAGROT)[i] = kLarmor / (b * p);
-    double mu0 = C(DP_COL_MU0)[i];
-    C(DP_COL_ECUT)[i] = mu0 < 1e-8 ? 2.0 * std::sqrt(std::max(mu0, 0.0))
-                                   : std::acos(std::max(1.0 - 2.0 * mu0, -1.0));
+  coulomb_and_kinematics(m, st, n, cols);
+}
+
+// load_dedx_file (src/DEDXLoader.jl:49-190): the header up to the units line
+// (<Z/A>), then every line of at least 11 numbers: T [MeV], p, ionisation,
+// bremsstrahlung, pair, photonuclear, radiative, dE/dx [MeV cm^2/g], CSDA
+// range [g/cm^2], delta, beta.  Lines that do not parse are skipped.
+bool load_dedx_table(const char* path, DedxTable* t, std::string* err) {
+  std::ifstream f(path);
+  if (!f) {
+    *err = std::string("DEDX file not found: ") + path;
+    return false;
   }
+  *t = DedxTable{};
+  std::string line;
+  bool data = false;
+  while (std::getline(f, line)) {
+    if (!data) {
+      const size_t z = line.find("<Z/A>");
+      if (z != std::string::npos) {
+        const size_t eq = line.find("= ", z);
+        if (eq != std::string::npos) {
+          const char* s = line.c_str() + eq + 2;
+          char* end = nullptr;
+          const double v = std::strtod(s, &end);
+          if (end != s && (std::isdigit(static_cast<unsigned char>(*s)) || *s == '.')) t->ZoA = v;
+        }
+      }
+      if (line.find("[MeV]") != std::string::npos && line.find("[MeV/c]") != std::string::npos)
+        data = true;
+      continue;
+    }
+    std::istringstream is(line);
+    std::string tok;
+    double v[11];
+    int k = 0;
+    bool ok = true;
+    while (k < 11 && is >> tok) {
+      char* end = nullptr;
+      v[k] = std::strtod(tok.c_str(), &end);
+      if (end == tok.c_str() || *end != '\0') {
+        ok = false;
+        break;
+      }
+      ++k;
+    }
+    if (!ok || k < 11 || line.find_first_not_of(" \t") == std::string::npos) continue;
+    const double conv_dedx = 1e-4, conv_range = 10.0;  // MeV cm^2/g, g/cm^2 -> kg/m^2
+    t->K.push_back(v[0] * 1e-3);
+    t->ion.push_back(v[2] * conv_dedx);
+    t->brems.push_back(v[3] * conv_dedx);
+    t->pair.push_back(v[4] * conv_dedx);
+    t->photo.push_back(v[5] * conv_dedx);
+    t->S.push_back(v[7] * conv_dedx);
+    t->R.push_back(v[8] * conv_range);
+  }
+  if (!data) {
+    *err = std::string("Could not find data section in DEDX file ") + path;
+    return false;
+  }
+  if (t->K.size() < 2) {
+    *err = std::string("no table rows in DEDX file ") + path;
+    return false;
+  }
+  return true;
+}
+
+// src/Physics.jl:146-273.  Energies, CSDA stopping power and range and the
+// four loss components come from the file; the proper time and restricted
+// range are trapezoids; the hard loss, straggling and hard cross section
+// (K >= 1e-3 GeV) are per-element DCS moments; the Coulomb columns use the
+// file's <Z/A>.
+void build_dedx_table(const HostMaterial& m, const DedxTable& t, const dp_settings& st,
+                      double* cols) {
+  const int n = int(t.K.size());
+  auto C = [&](int c) { return cols + size_t(c) * n; };
+  for (int c = 0; c < DP_NCOL; ++c) std::fill(C(c), C(c) + n, 0.0);
+  const double mass = st.mass, cut = st.cutoff;
+  double* E = C(DP_COL_E);
+  for (int i = 0; i < n; ++i) {
+    E[i] = t.K[i];
+    C(DP_COL_LOGE)[i] = std::log(E[i]);
+    C(DP_COL_CSDA_S)[i] = t.S[i];
+    C(DP_COL_CSDA_R)[i] = t.R[i];
+    C(DP_COL_ION)[i] = t.ion[i];
+    C(DP_COL_BREMS)[i] = t.brems[i];
+    C(DP_COL_PAIR)[i] = t.pair[i];
+    C(DP_COL_PHOTO)[i] = t.photo[i];
+  }
+  double *S = C(DP_COL_CSDA_S), *T = C(DP_COL_CSDA_T);
+  T[0] = 0.0;
+  for (int i = 1; i < n; ++i) {
+    double K = E[i], Kp = E[i - 1];
+    double g = 1.0 + K / mass, gp = 1.0 + Kp / mass;
+    double b = std::sqrt(1.0 - 1.0 / (g * g)), bp = std::sqrt(1.0 - 1.0 / (gp * gp));
+    double gm = (g + gp) / 2, bm = (b + bp) / 2, sm = (S[i] + S[i - 1]) / 2;
+    T[i] = T[i - 1] + (K - Kp) / (sm * bm * gm);
+  }
+  parallel_for(n, [&](int i) {
+    double K = E[i], hard = 0, sg = 0, cs = 0;
+    if (K >= 1e-3) {
+      for (const auto& e : m.elements) {
+        const double f = e.fraction;
+        for (int p = 0; p < 4; ++p) hard += f * dcs_moment(p, e.Z, e.A, e.I, mass, K, cut, 1.0, 1);
+        sg += f * dcs_moment(P_IONI, e.Z, e.A, e.I, mass, K, 0.0, cut, 2);
+      }
+      for (const auto& e : m.elements)
+        for (int p = 0; p < 4; ++p)
+          cs += e.fraction * dcs_moment(p, e.Z, e.A, e.I, mass, K, cut, 1.0, 0);
+    }
+    C(DP_COL_MIXED_S)[i] = std::max(S[i] - hard, 1e-20);
+    C(DP_COL_STRAG)[i] = sg;
+    C(DP_COL_XS)[i] = cs;
+  });
+  double *Sm = C(DP_COL_MIXED_S), *Rm = C(DP_COL_MIXED_R);
+  Rm[0] = E[0] / Sm[0];
+  for (int i = 1; i < n; ++i) Rm[i] = Rm[i - 1] + (E[i] - E[i - 1]) / ((Sm[i] + Sm[i - 1]) / 2);
+  HostMaterial mz = m;
+  mz.ZoA = t.ZoA;
+  coulomb_and_kinematics(mz, st, n, cols);
 }
 
 double host_dcs_moment(int proc, double Z, double A, double I, double mass, double K, double xlo,

@@ -227,6 +227,69 @@ def create_physics(particle="MUON", *, n_energies=200, K_min=1e-3, K_max=1e9,
     return Physics(h, ctx, [m.name for m in materials], st)
 
 
+def _dedx_args(dedx_paths, materials):
+    if len(dedx_paths) != len(materials):
+        raise ValueError("one dE/dx file per material")
+    cs = [m.to_c() for m in materials]
+    arr = (DpMaterial * len(cs))(*[c[0] for c in cs])
+    paths = (C.c_char_p * len(dedx_paths))(*[str(p).encode() for p in dedx_paths])
+    return cs, arr, paths
+
+
+def create_physics_dedx(dedx_paths, materials, *, cutoff=DEFAULT_CUTOFF,
+                        elastic_ratio=DEFAULT_ELASTIC_RATIO, ctx=None):
+    """create_physics with PUMAS dE/dx files (src/Physics.jl:146-273,
+    src/DEDXLoader.jl:100-190): one file per material recipe, built on the
+    host by libdpgpu and uploaded."""
+    ctx = ctx or default_context()
+    st = _settings(cutoff=cutoff, elastic_ratio=elastic_ratio)
+    cs, arr, paths = _dedx_args(dedx_paths, materials)
+    h = C.c_void_p()
+    check(load().dp_physics_create_dedx(ctx.h, C.byref(st), len(cs), C.cast(arr, C.c_void_p),
+                                        C.cast(paths, C.c_void_p), C.byref(h)), ctx.h)
+    return Physics(h, ctx, [m.name for m in materials], st)
+
+
+def tables_from_dedx(dedx_paths, materials, *, cutoff=DEFAULT_CUTOFF,
+                     elastic_ratio=DEFAULT_ELASTIC_RATIO):
+    """The dE/dx-file tables on the host only (no device): a list of dicts
+    column name -> array, one per material."""
+    st = _settings(cutoff=cutoff, elastic_ratio=elastic_ratio)
+    cs, arr, paths = _dedx_args(dedx_paths, materials)
+    n = C.c_int()
+    lib = load()
+    check(lib.dp_tables_from_dedx(C.byref(st), len(cs), C.cast(arr, C.c_void_p),
+                                  C.cast(paths, C.c_void_p), C.byref(n), None, 0))
+    cols = np.zeros((len(cs), len(COLUMNS), n.value))
+    check(lib.dp_tables_from_dedx(C.byref(st), len(cs), C.cast(arr, C.c_void_p),
+                                  C.cast(paths, C.c_void_p), C.byref(n), _ptr(cols), cols.size))
+    return [{c: cols[m, k] for k, c in enumerate(COLUMNS)} for m in range(len(cs))]
+
+
+def save_physics(physics, path):
+    """Writes the portable table file (dp_physics_save)."""
+    check(load().dp_physics_save(physics.h, str(path).encode()), physics.ctx.h)
+    return path
+
+
+def load_physics(path, ctx=None):
+    """Reads a portable table file onto the device (dp_physics_load)."""
+    ctx = ctx or default_context()
+    lib = load()
+    h = C.c_void_p()
+    check(lib.dp_physics_load(ctx.h, str(path).encode(), C.byref(h)), ctx.h)
+    st = DpSettings()
+    check(lib.dp_physics_settings(h, C.byref(st)))
+    n_mat = C.c_int()
+    lib.dp_physics_info(h, C.byref(n_mat), None)
+    names = []
+    buf = C.create_string_buffer(1 << 16)
+    for m in range(n_mat.value):
+        k = lib.dp_physics_material_name(h, m, buf, len(buf))
+        names.append(buf.value.decode() if k >= 0 else f"material{m + 1}")
+    return Physics(h, ctx, names, st)
+
+
 def upload_physics(tables, names, materials=None, *, mass=MUON_MASS, ctau=MUON_C_TAU,
                    cutoff=DEFAULT_CUTOFF, elastic_ratio=DEFAULT_ELASTIC_RATIO, ctx=None):
     """Uploads caller-built tables: `tables` is a list (one per material) of

@@ -157,6 +157,12 @@ PROTOTYPES = {
     "dp_autotune": (_I, [_P, _I, _I, AUTOTUNE_RUN, _VP, C.POINTER(_I), _VP, _I]),
     "dp_physics_upload": (_I, [_P, C.POINTER(DpSettings), _I, _I, _VP, _VP, C.POINTER(_P)]),
     "dp_physics_create": (_I, [_P, C.POINTER(DpSettings), _I, _VP, _I, _D, _D, C.POINTER(_P)]),
+    "dp_physics_create_dedx": (_I, [_P, C.POINTER(DpSettings), _I, _VP, _VP, C.POINTER(_P)]),
+    "dp_tables_from_dedx": (_I, [C.POINTER(DpSettings), _I, _VP, _VP, C.POINTER(_I), _VP, _L]),
+    "dp_physics_save": (_I, [_P, C.c_char_p]),
+    "dp_physics_load": (_I, [_P, C.c_char_p, C.POINTER(_P)]),
+    "dp_physics_settings": (_I, [_P, C.POINTER(DpSettings)]),
+    "dp_physics_material_name": (_I, [_P, _I, C.c_char_p, _I]),
     "dp_physics_free": (_I, [_P]),
     "dp_physics_info": (_I, [_P, C.POINTER(_I), C.POINTER(_I)]),
     "dp_physics_column": (_I, [_P, _I, _I, _VP]),

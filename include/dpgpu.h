@@ -179,6 +179,34 @@ int dp_physics_info(const dp_physics* phys, int* n_materials, int* n_energies);
 int dp_physics_column(const dp_physics* phys, int mat, int col, double* out);
 /* Index of the material with this name, or -1 (src/Physics.jl:609 get_material_index). */
 int dp_physics_material_index(const dp_physics* phys, const char* name);
+/* create_physics with PUMAS dE/dx files (src/Physics.jl:146-273
+ * create_material_table_from_dedx, src/DEDXLoader.jl:100-190
+ * load_dedx_file): material m's energy grid, CSDA stopping power and range
+ * and energy-loss components come from dedx_paths[m]; the restricted
+ * stopping power, straggling, hard cross section and Coulomb columns are
+ * integrated from the recipe (with the file's <Z/A>).  All files must share
+ * one energy grid. */
+int dp_physics_create_dedx(dp_ctx* ctx, const dp_settings* settings, int n_materials,
+                           const dp_material* materials, const char* const* dedx_paths,
+                           dp_physics** out);
+/* The same tables on the host only (no device): *n_energies receives the
+ * grid size; with cols (capacity cap doubles) the n_materials x DP_NCOL x
+ * n_energies columns.  Returns DP_ERR_ARG for unreadable files, differing
+ * grids or a small cap. */
+int dp_tables_from_dedx(const dp_settings* settings, int n_materials,
+                        const dp_material* materials, const char* const* dedx_paths,
+                        int* n_energies, double* cols, long cap);
+/* Portable table file, the counterpart of the reference's Julia-only
+ * .pumas serialisation (src/Loader.jl:30-105): settings, recipes and every
+ * column in FP64, little-endian; loading reproduces the tables bit for bit
+ * on x86-64 and AArch64 hosts. */
+int dp_physics_save(const dp_physics* phys, const char* path);
+int dp_physics_load(dp_ctx* ctx, const char* path, dp_physics** out);
+/* The settings of a table set, and material m's name (copied into buf,
+ * NUL-terminated; returns its length, or -1 without recipes or if cap is
+ * too small). */
+int dp_physics_settings(const dp_physics* phys, dp_settings* out);
+int dp_physics_material_name(const dp_physics* phys, int mat, char* buf, int cap);
 
 /* ------------------------------------------------------------------ backward MC
  * run_backward_mc (src/Geometry.jl:1286-1338) on a two-layer rock + air column. */
