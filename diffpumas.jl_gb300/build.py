@@ -19,7 +19,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr", "--extended-lambda"]
 UNITS = ["api.cu", "physics_build.cu", "csda_mc.cu", "tomo.cu", "mc.cu", "dir_mc.cu",
-         "inverse.cu", "wtomo.cu", "voxel_trace.cu"]
+         "inverse.cu", "wtomo.cu", "voxel_trace.cu", "topo_trace.cu"]
 # per-unit flags: the stochastic transport's FP32 kernel uses the hardware
 # (MUFU) transcendentals; FP64 arithmetic is not affected by these flags
 UNIT_FLAGS = {"mc.cu": ["--use_fast_math"], "dir_mc.cu": ["--use_fast_math"],

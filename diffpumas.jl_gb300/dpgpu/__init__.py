@@ -617,6 +617,8 @@ from .calibration import (calibrate_csda_correction,  # noqa: E402
                           csda_geom_multiplier, csda_material_multiplier, load_csda_corrections,
                           path_rock_length, save_csda_corrections)
 from .directional import cell_density  # noqa: E402
+from .topography import (ElevationMap, Terrain, TetraVolume,  # noqa: E402
+                         compute_shallow_mask, ray_triangle_intersect, trace_tetra_paths)
 from .uncertainty import (SystematicSourceResult, TransportUncertaintyResult,  # noqa: E402
                           TransportVariation, compute_flux_uncertainty,
                           estimate_transport_uncertainty, relative_uncertainty_percent)

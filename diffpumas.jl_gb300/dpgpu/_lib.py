@@ -104,6 +104,22 @@ class DpVoxelVolume(C.Structure):
                 ("y_edges", C.c_void_p), ("z_edges", C.c_void_p)]
 
 
+class DpElevationMap(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("x0", C.c_double), ("y0", C.c_double),
+                ("dx", C.c_double), ("dy", C.c_double), ("z", C.c_void_p)]
+
+
+class DpTerrain(C.Structure):
+    _fields_ = [("map", DpElevationMap), ("xy_scale", C.c_double),
+                ("detector_elevation", C.c_double), ("step", C.c_double),
+                ("max_distance", C.c_double)]
+
+
+class DpTetraMesh(C.Structure):
+    _fields_ = [("n_points", C.c_long), ("points", C.c_void_p), ("n_tets", C.c_long),
+                ("tets", C.c_void_p)]
+
+
 class DpSolveParams(C.Structure):
     _fields_ = [("method", C.c_int), ("n_iter", C.c_int), ("cg_iter", C.c_int),
                 ("precision", C.c_int), ("relaxation", C.c_double), ("lm_damping", C.c_double),
@@ -191,6 +207,13 @@ PROTOTYPES = {
     "dp_dir_media_create": (_I, [_P, _P, _I, C.POINTER(_P), C.POINTER(_P)]),
     "dp_voxel_trace": (_I, [_P, C.POINTER(DpVoxelVolume), _L, _VP, _VP, _VP, _VP, _VP, _VP,
                             C.c_int64, _VP, _VP]),
+    "dp_map_elevation": (_I, [C.POINTER(DpElevationMap), _L, _VP, _VP, _VP, _VP]),
+    "dp_map_gradient": (_I, [C.POINTER(DpElevationMap), _L, _VP, _VP, _VP, _VP, _VP]),
+    "dp_surface_exit": (_I, [C.POINTER(DpTerrain), _L, _VP, _VP, _VP, _VP, _VP]),
+    "dp_ray_triangle": (_I, [_VP, _VP, _VP, _VP, _VP, C.POINTER(_D), _VP]),
+    "dp_tetra_neighbors": (_I, [C.POINTER(DpTetraMesh), _VP]),
+    "dp_tetra_trace": (_I, [_P, C.POINTER(DpTetraMesh), _VP, C.POINTER(DpTerrain), _L, _VP, _VP,
+                            _VP, _VP, _VP, C.c_int64, _VP, _VP, _VP, _VP, _VP]),
     "dp_dir_media_free": (_I, [_P]),
     "dp_dir_mc": (_I, [_P, _P, _P, C.POINTER(DpDirBatch), C.POINTER(DpMcConfig), _VP, _VP, _VP,
                        _VP]),

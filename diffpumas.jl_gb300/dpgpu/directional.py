@@ -505,18 +505,39 @@ def flat_surface(height):
 
 def precompute_paths(volume, zeniths, azimuths, surface, ctx=None):
     """DirectionalPath of every (zenith, azimuth) pair, zeniths outer
-    (examples/lvd_tomography.jl:738-779, 835-861): the reference's march
-    through the volume, cut at the surface exit that `surface(zenith,
-    azimuth) -> (slant distance, valid, exit z)` gives (flat_surface(h) for a
-    flat overburden)."""
+    (examples/lvd_tomography.jl:694-779, 835-861): the reference's march
+    through a VoxelVolume, or its walk through a TetraVolume, cut at the
+    surface exit that `surface(zenith, azimuth) -> (slant distance, valid,
+    exit z)` gives: flat_surface(h) for a flat overburden, or a Terrain
+    (elevation map; required by a TetraVolume)."""
     from ._lib import DpVoxelVolume
     from . import _ptr
+    from .topography import Terrain, TetraVolume, trace_tetra_paths
     h = ctx.h if ctx is not None else None  # host work: no device context needed
     pairs = [(float(t), float(p)) for t in zeniths for p in azimuths]
     n = len(pairs)
     zen = np.array([t for t, _ in pairs])
     az = np.array([p for _, p in pairs])
-    surf = [surface(t, p) for t, p in pairs]
+    if isinstance(volume, TetraVolume):
+        if not isinstance(surface, Terrain):
+            raise ValueError("a tetrahedral volume is traced against a Terrain")
+        seg_ptr, cells, lens, trav, dist, rem, ez, ok = trace_tetra_paths(volume, surface, zen, az)
+        out = []
+        for d, (t, p) in enumerate(pairs):
+            if not ok[d]:
+                out.append(DirectionalPath(t, p, [], float("nan"), float("nan"), float("nan"),
+                                           float("nan"), False))
+                continue
+            segs = [CellSegment(int(c), float(l)) for c, l in
+                    zip(cells[seg_ptr[d]:seg_ptr[d + 1]], lens[seg_ptr[d]:seg_ptr[d + 1]])]
+            out.append(DirectionalPath(t, p, segs, float(trav[d]), float(dist[d]), float(rem[d]),
+                                       float(ez[d]), True))
+        return out
+    if isinstance(surface, Terrain):
+        sd, sz, sok = surface.surface_exit(zen, az)
+        surf = [(float(a), bool(o), float(b)) for a, b, o in zip(sd, sz, sok)]
+    else:
+        surf = [surface(t, p) for t, p in pairs]
     dist = np.array([s[0] if s[1] else float("nan") for s in surf])
     V = DpVoxelVolume(volume.nx, volume.ny, volume.nz, volume.x_edges.ctypes.data,
                       volume.y_edges.ctypes.data, volume.z_edges.ctypes.data)

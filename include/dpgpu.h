@@ -456,6 +456,62 @@ int dp_voxel_trace(dp_ctx* ctx, const dp_voxel_volume* volume, long n_dirs, cons
                    int32_t* seg_cell, double* seg_length, int64_t seg_cap, double* traveled,
                    double* remaining_rock);
 
+/* ------------------------------------------------ terrain and tetrahedral meshes
+ * Host geometry (no device work).  An elevation map (Turtle ElevationMap,
+ * src/Turtle.jl:455-481): z[iy * nx + ix] at node x0 + ix dx, y0 + iy dy.
+ * map_elevation (:520-557) bilinear, map_gradient (:559-634); inside[i] = 0
+ * off the map. */
+typedef struct {
+  int nx, ny;
+  double x0, y0, dx, dy;
+  const double* z;
+} dp_elevation_map;
+int dp_map_elevation(const dp_elevation_map* map, long n, const double* x, const double* y,
+                     double* z, int32_t* inside);
+int dp_map_gradient(const dp_elevation_map* map, long n, const double* x, const double* y,
+                    double* gx, double* gy, int32_t* inside);
+/* The terrain above a detector at the origin: the surface height at local
+ * metres (x, y) is map_elevation(map, x xy_scale, y xy_scale) -
+ * detector_elevation (examples/lvd_tomography.jl:214-217; the LVD map is in
+ * km, xy_scale 1e-3).  ray_surface_exit_distance (:219-252) marches in
+ * steps of `step` m up to max_distance (40 m, 25 km there), then bisects 40
+ * times; dp_surface_exit gives per direction the slant distance, the exit
+ * altitude above the detector and ok = 0 for a direction that leaves the
+ * map or points down. */
+typedef struct {
+  dp_elevation_map map;
+  double xy_scale, detector_elevation, step, max_distance;
+} dp_terrain;
+int dp_surface_exit(const dp_terrain* terrain, long n_dirs, const double* zenith,
+                    const double* azimuth, double* distance, double* exit_z, int32_t* ok);
+/* Ray-triangle intersection (src/TriangleIntersect.jl:78-115, Moller-Trumbore):
+ * returns 1 and the distance (and the point, 3 doubles, if given) on a hit, 0
+ * otherwise. */
+int dp_ray_triangle(const double* origin, const double* dir, const double* p1, const double* p2,
+                    const double* p3, double* distance, double* point);
+/* A tetrahedral mesh (TetraVolume, examples/lvd_tomography.jl:172-179):
+ * points[3 i + k], tets[4 t + v] 1-based point indices (TetGen's
+ * connectivity; the mesh is built by the caller).  dp_tetra_neighbors fills
+ * neighbors[4 t + f] with the 1-based tetrahedron across face f of
+ * tetra_face_indices (:415-422), 0 on the boundary (build_tetra_neighbors,
+ * :431-453).  dp_tetra_trace is trace_path(::TetraVolume) (:694-736) for
+ * every direction: the POINT_EPS walk from the tetrahedron containing the
+ * start point through neighbours, cut at the terrain's surface exit; cells
+ * are 1-based tetrahedra; the count / fill protocol of dp_voxel_trace. */
+typedef struct {
+  long n_points;
+  const double* points;
+  long n_tets;
+  const int32_t* tets;
+} dp_tetra_mesh;
+int dp_tetra_neighbors(const dp_tetra_mesh* mesh, int32_t* neighbors);
+int dp_tetra_trace(dp_ctx* ctx, const dp_tetra_mesh* mesh, const int32_t* neighbors,
+                   const dp_terrain* terrain, long n_dirs, const double* zenith,
+                   const double* azimuth, int64_t* seg_ptr, int32_t* seg_cell,
+                   double* seg_length, int64_t seg_cap, double* traveled,
+                   double* surface_distance, double* remaining_rock, double* exit_z,
+                   int32_t* valid);
+
 /* ------------------------------------------------ water-fraction CSDA model
  * compute_directional_flux_csda (src/Tomography.jl:667-727),
  * directional_flux_and_grad_csda (:736-762) and assemble_forward_and_jacobian
