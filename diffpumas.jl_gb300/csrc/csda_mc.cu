@@ -290,7 +290,6 @@ __global__ void __launch_bounds__(128) csda32_kernel(CsdaParams P, const float* 
                  b + F_SLOPE * ld32, b + F_DSDLE * ld32, b + F_DLE * ld32};
   };
 
-  const double eps = kEps64;
   const float mass = float(P.mass), ctau = float(P.ctau);
   for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < P.n;
        i += long(gridDim.x) * blockDim.x) {

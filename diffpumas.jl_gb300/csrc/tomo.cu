@@ -1027,7 +1027,6 @@ static int eval_core(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, cons
   P.nw = nw;
   P.flux = flux;
   const bool adj = (cot && grad) || jac || jraw;
-  long ncell = long(pa->grid.nx) * pa->grid.ny * pa->grid.nz;
   // slot 1: node starts, then the Jacobian values
   size_t need = size_t(P.n_nodes) * sizeof(NodeInit) + size_t(pa->nnz + 1) * 8 + 1024;
   Arena A;
