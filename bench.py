@@ -232,12 +232,14 @@ def setup_c2(dp, torch, dev, precision="mixed", scale=1.0):
             # per history: contribution (8 B) and status (4 B) written by the
             # transport kernel and read back by the tally
             "alg_bytes": n * 24,
-            # DRAM bytes of one step from an ncu capture of all six launches at
-            # 2e5 histories (89.6 MB), scaled by the histories: the start, hand-off
-            # and end records grow in proportion
-            "traffic": int(448 * n) if precision == "mixed" else None,
-            "note": "SM-issue bound, not HBM: ncu smsp__issue_active 18.0% (phase 0) and "
-                    "28.5% (phase 1), DRAM throughput < 0.1%",
+            # DRAM bytes of one step from an ncu capture of all seven launches at
+            # 2e5 histories (918.6 MB: the records and the transport kernels'
+            # local-memory write-back), scaled by the histories, which both
+            # grow in proportion with
+            "traffic": int(4593 * n) if precision == "mixed" else None,
+            "note": "SM-issue bound, not HBM: ncu smsp__issue_active 25.4% (phase 0) and "
+                    "39.9% (phase 1) at 1024-thread CTAs; DRAM traffic (mostly local-memory "
+                    "write-back of the spilled stack) is 0.6% of the bandwidth",
             "config": {"workload": "c2: straggled MC with DEL/EHS + Coulomb scattering, rock mixture "
                                    "rock/water/air 0.70/0.25/0.05 (per-history thickness U[20,500] m, "
                                    "density U[2000,2800], elevation U[30,90] deg) under 1 km air, "
