@@ -11,6 +11,21 @@
 
 namespace dp {
 
+// Threads of the block that reduces one large CSC bucket (cells next to a
+// detector hold thousands of entries).
+constexpr int kBigThreads = 128;
+// Sum over the kBigThreads threads of a block in a fixed order (shuffle tree
+// per warp, then the warp partials in warp order); valid in thread 0.
+__device__ __forceinline__ double big_block_sum(double v, double* sh /* kBigThreads / 32 */) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < kBigThreads / 32; ++w) s += sh[w];
+  return s;
+}
+
 // src/Constants.jl:17-92 (values the path uses)
 constexpr double kMuonMass = 0.10565839;
 constexpr double kMuonCTau = 658.654;

@@ -88,8 +88,11 @@ int csda_los(dp_ctx* ctx, const dp_physics* ph, int rock, int air, double thresh
 // a caller-owned Jacobian buffer and J^T v on the resident paths' buckets.
 int tomo_eval_raw(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, const dp_tomo_params* tp,
                   const double* rho, double* flux, void* jraw, int precision);
+// The bucketed Jacobian values in CSC order (nnz entries of out), for
+// repeated J^T v products with csc = true.
+int tomo_csc_values(dp_ctx* ctx, const dp_paths* pa, const void* jbuf, int precision, void* out);
 int tomo_transpose(dp_ctx* ctx, const dp_paths* pa, const void* jbuf, int precision,
-                   const double* cot, double* grad);
+                   const double* cot, double* grad, bool csc = false);
 // Bump allocator over one scratch slot (256-byte aligned pieces).
 struct Arena {
   char* base = nullptr;

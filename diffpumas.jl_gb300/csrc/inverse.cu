@@ -63,12 +63,17 @@ __global__ void rowabs_kernel(const int64_t* row_ptr, const int32_t* cell, const
 // A ray can cross a cell in several segments: J_ij is the sum of its
 // segments' entries, which sit next to each other in the bucket (ordered by
 // entry index), so runs of one row are merged before squaring.
+// One thread per cell with at most kBigBucket entries; the larger buckets
+// (the cells next to a detector, crossed by thousands of rays) go to
+// colsum_big_kernel.
+constexpr int kBigBucket = 32;  // the bucket split of the J^T v gather (tomo.cu)
 template <class V>
 __global__ void colsum_kernel(const int64_t* cptr, const int32_t* perm, const V* val,
                               const int32_t* prow, const double* wt, long ncell, int mode,
                               double* out) {
   long c = blockIdx.x * long(blockDim.x) + threadIdx.x;
   if (c >= ncell) return;
+  if (cptr[c + 1] - cptr[c] > kBigBucket) return;
   double s = 0.0, run = 0.0;
   int row = -1;
   for (int64_t p = cptr[c], e = cptr[c + 1]; p < e; ++p) {
@@ -78,10 +83,41 @@ __global__ void colsum_kernel(const int64_t* cptr, const int32_t* perm, const V*
       row = r;
       run = 0.0;
     }
-    run += double(val[perm[p]]);
+    run += double(val[perm ? perm[p] : p]);
   }
   if (row >= 0) s += mode == 0 ? fabs(run) : (wt ? wt[row] : 1.0) * run * run;
   out[c] = mode == 0 ? (s > 0.0 ? s : 1.0) : s;
+}
+// A block of kBigThreads per large bucket: the bucket is cut into
+// kBigThreads contiguous chunks and each run of one row belongs to the thread
+// whose chunk it starts in (a thread skips the tail of the run entering its
+// chunk and finishes its last run past the chunk end), so every run is merged
+// before squaring, as above; the threads' sums combine in a fixed order.
+template <class V>
+__global__ void __launch_bounds__(kBigThreads) colsum_big_kernel(
+    const int64_t* cptr, const int32_t* perm, const V* val, const int32_t* prow,
+    const double* wt, const int32_t* big, int mode, double* out) {
+  __shared__ double sh[kBigThreads / 32];
+  const int c = big[blockIdx.x];
+  const int64_t b = cptr[c], e = cptr[c + 1];
+  const int64_t len = (e - b + kBigThreads - 1) / kBigThreads;
+  int64_t p = b + threadIdx.x * len;
+  const int64_t stop = p + len < e ? p + len : e;
+  double s = 0.0;
+  if (p < stop) {
+    if (p > b) {
+      const int prev = prow[p - 1];
+      while (p < stop && prow[p] == prev) ++p;
+    }
+    while (p < stop) {
+      const int r = prow[p];
+      double run = 0.0;
+      for (; p < e && prow[p] == r; ++p) run += double(val[perm ? perm[p] : p]);
+      s += mode == 0 ? fabs(run) : (wt ? wt[r] : 1.0) * run * run;
+    }
+  }
+  s = big_block_sum(s, sh);
+  if (threadIdx.x == 0) out[c] = mode == 0 ? (s > 0.0 ? s : 1.0) : s;
 }
 
 // Fixed-order dot product: block partials, then one block.
@@ -291,16 +327,19 @@ struct Solver {
   const dp_tomo_params* tp;
   int precision;
   long n_rays, ncell;
-  void* jv;      // Jacobian values (FP32 or FP64)
+  void* jv;      // Jacobian values (FP32 or FP64), CSR (segment) order
+  void* jcsc;    // the same values in CSC (bucket) order, for J^T v and column sums
   double* part;  // reduction partials
   double* s;     // device scalars
   int grid(long n) const { return int(std::min<long>((n + kThreads - 1) / kThreads, 152L * 8)); }
 
   int dot(const double* a, const double* b, const double* w, long n, double* out) {
+    timed_begin(ctx);
     dot_part_kernel<<<kRedBlocks, kThreads, 0, ctx->stream>>>(a, b, w, n, part);
     dot_final_kernel<<<1, kThreads, 0, ctx->stream>>>(part, kRedBlocks, out);
-    ctx->launches += 2;
+    ++ctx->launches;  // the second of the pair (timed_begin counts the first)
     DP_CHECK_CUDA(ctx, cudaGetLastError());
+    timed_end(ctx, "gn_dot");
     return DP_OK;
   }
   double host_scalar(const double* d) {
@@ -311,6 +350,7 @@ struct Solver {
   }
   int spmv(const double* x, const double* wt, double* y) {
     int blocks = int((n_rays * 32 + kThreads - 1) / kThreads);
+    timed_begin(ctx);
     if (precision)
       spmv_kernel<float><<<blocks, kThreads, 0, ctx->stream>>>(pa->row_ptr, pa->cell,
                                                                static_cast<const float*>(jv), x,
@@ -319,21 +359,34 @@ struct Solver {
       spmv_kernel<double><<<blocks, kThreads, 0, ctx->stream>>>(pa->row_ptr, pa->cell,
                                                                 static_cast<const double*>(jv), x,
                                                                 n_rays, wt, y);
-    ++ctx->launches;
     DP_CHECK_CUDA(ctx, cudaGetLastError());
+    timed_end(ctx, "gn_spmv");
     return DP_OK;
   }
-  int transpose(const double* u, double* out) { return tomo_transpose(ctx, pa, jv, precision, u, out); }
+  int transpose(const double* u, double* out) {
+    return tomo_transpose(ctx, pa, jcsc, precision, u, out, true);
+  }
   int colsum(const double* wt, int mode, double* out) {
     int blocks = int((ncell + kThreads - 1) / kThreads);
-    if (precision)
-      colsum_kernel<float><<<blocks, kThreads, 0, ctx->stream>>>(
-          pa->cptr, pa->perm, static_cast<const float*>(jv), pa->prow, wt, ncell, mode, out);
-    else
-      colsum_kernel<double><<<blocks, kThreads, 0, ctx->stream>>>(
-          pa->cptr, pa->perm, static_cast<const double*>(jv), pa->prow, wt, ncell, mode, out);
-    ++ctx->launches;
+    timed_begin(ctx);
+    if (precision) {
+      const float* v = static_cast<const float*>(jcsc);
+      colsum_kernel<float><<<blocks, kThreads, 0, ctx->stream>>>(pa->cptr, nullptr, v, pa->prow,
+                                                                 wt, ncell, mode, out);
+      if (pa->n_big > 0)
+        colsum_big_kernel<float><<<pa->n_big, kBigThreads, 0, ctx->stream>>>(
+            pa->cptr, nullptr, v, pa->prow, wt, pa->big, mode, out);
+    } else {
+      const double* v = static_cast<const double*>(jcsc);
+      colsum_kernel<double><<<blocks, kThreads, 0, ctx->stream>>>(pa->cptr, nullptr, v, pa->prow,
+                                                                  wt, ncell, mode, out);
+      if (pa->n_big > 0)
+        colsum_big_kernel<double><<<pa->n_big, kBigThreads, 0, ctx->stream>>>(
+            pa->cptr, nullptr, v, pa->prow, wt, pa->big, mode, out);
+    }
+    if (pa->n_big > 0) ++ctx->launches;
     DP_CHECK_CUDA(ctx, cudaGetLastError());
+    timed_end(ctx, "gn_colsum");
     return DP_OK;
   }
   int rowabs(double* out) {
@@ -350,7 +403,9 @@ struct Solver {
   }
   // forward (and Jacobian when jac) at rho
   int eval(const double* rho, double* flux, bool jac) {
-    return tomo_eval_raw(ctx, ph, pa, tp, rho, flux, jac ? jv : nullptr, precision);
+    const int rc = tomo_eval_raw(ctx, ph, pa, tp, rho, flux, jac ? jv : nullptr, precision);
+    if (rc || !jac) return rc;
+    return tomo_csc_values(ctx, pa, jv, precision, jcsc);
   }
   Dims dims;
   double prior = 0.0;  // smoothness weight
@@ -400,13 +455,15 @@ int dp_tomo_solve_dev(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa,
   S.dims = Dims{pa->grid.nx, pa->grid.ny, pa->grid.nz};
   S.prior = sp->prior_weight > 0.0 ? sp->prior_weight : 0.0;
   const long nr = S.n_rays, nc = S.ncell;
-  // slot 0: Jacobian values, 5 row vectors, 10 cell vectors, partials, scalars
-  size_t need = size_t(pa->nnz + 1) * (S.precision ? 4 : 8) + size_t(nr) * 5 * 8 +
+  // slot 0: Jacobian values (CSR and CSC order), 5 row vectors, 10 cell vectors,
+  // partials, scalars
+  size_t need = 2 * size_t(pa->nnz + 1) * (S.precision ? 4 : 8) + size_t(nr) * 5 * 8 +
                 size_t(nc) * 10 * 8 + kRedBlocks * 8 + 64 + 16 * 256;
   Arena A;
   A.base = static_cast<char*>(scratch(ctx, need, 0));
   A.cap = ctx->slot_bytes[0];
   S.jv = A.take<char>(size_t(pa->nnz + 1) * (S.precision ? 4 : 8));
+  S.jcsc = A.take<char>(size_t(pa->nnz + 1) * (S.precision ? 4 : 8));
   double *flux = A.take<double>(nr), *r = A.take<double>(nr), *u = A.take<double>(nr),
          *rowsum = A.take<double>(nr), *tmp = A.take<double>(nr);
   double *g = A.take<double>(nc), *col = A.take<double>(nc), *x = A.take<double>(nc),

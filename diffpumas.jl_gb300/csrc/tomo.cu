@@ -711,22 +711,21 @@ __global__ void __launch_bounds__(kWarps * 32, 8) eval32_kernel(EvalP P) {
   }
 }
 
-// J^T r over the precomputed CSC permutation: one warp per cell; lane l sums
-// entries l, l+32, ... of the bucket in order, then a fixed shuffle tree --
-// the same arithmetic order on every call.
+// J^T r over the precomputed CSC permutation of a large bucket: one block of
+// kBigThreads per cell; thread t sums entries t, t + kBigThreads, ... in
+// order, then big_block_sum -- the same arithmetic order on every call.
+// perm == nullptr: the values are already in CSC order.
 template <class V>
-__global__ void gather_big_kernel(const int64_t* cptr, const int32_t* perm, const V* val,
-                                  const int32_t* prow, const double* cot, const int32_t* big,
-                                  int n_big, double* grad) {
-  long w = (blockIdx.x * long(blockDim.x) + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (w >= n_big) return;
-  int c = big[w];
+__global__ void __launch_bounds__(kBigThreads) gather_big_kernel(
+    const int64_t* cptr, const int32_t* perm, const V* val, const int32_t* prow,
+    const double* cot, const int32_t* big, int n_big, double* grad) {
+  __shared__ double sh[kBigThreads / 32];
+  const int c = big[blockIdx.x];
   double s = 0.0;
-  for (int64_t p = cptr[c] + lane, e = cptr[c + 1]; p < e; p += 32)
-    s += double(val[perm[p]]) * cot[prow[p]];
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if (lane == 0) grad[c] = s;
+  for (int64_t p = cptr[c] + threadIdx.x, e = cptr[c + 1]; p < e; p += kBigThreads)
+    s += double(val[perm ? perm[p] : p]) * cot[prow[p]];
+  s = big_block_sum(s, sh);
+  if (threadIdx.x == 0) grad[c] = s;
 }
 // Cells with at most kSmallBucket entries: one thread, entries in order.
 template <class V>
@@ -738,8 +737,19 @@ __global__ void gather_small_kernel(const int64_t* cptr, const int32_t* perm, co
   int64_t b = cptr[c], e = cptr[c + 1];
   if (e - b > kSmallBucket) return;  // gather_big_kernel
   double s = 0.0;
-  for (int64_t p = b; p < e; ++p) s += double(val[perm[p]]) * cot[prow[p]];
+  for (int64_t p = b; p < e; ++p) s += double(val[perm ? perm[p] : p]) * cot[prow[p]];
   grad[c] = s;
+}
+// The Jacobian values of the bucketed entries in CSC order (out[p] =
+// val[perm[p]] for p < *n_bucketed), so that repeated J^T v products read
+// them contiguously.
+template <class V>
+__global__ void csc_values_kernel(const int32_t* perm, const V* val, const int64_t* n_bucketed,
+                                  int64_t n, V* out) {
+  const int64_t m = *n_bucketed;
+  for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < m && p < n;
+       p += int64_t(gridDim.x) * blockDim.x)
+    out[p] = val[perm[p]];
 }
 
 // ---------------------------------------------------------------- plain form
@@ -1080,27 +1090,47 @@ static int eval_core(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, cons
   return ctx->blocking ? check(ctx) : DP_OK;
 }
 
-// J^T v over the CSC buckets (deterministic segmented sums, no float atomics).
+int tomo_csc_values(dp_ctx* ctx, const dp_paths* pa, const void* jbuf, int precision,
+                    void* out) {
+  const long ncell = long(pa->grid.nx) * pa->grid.ny * pa->grid.nz;
+  const int blocks = int(std::min<int64_t>((pa->nnz + 255) / 256, 152L * 32));
+  if (blocks < 1) return DP_OK;
+  timed_begin(ctx);
+  if (precision == 0)
+    csc_values_kernel<double><<<blocks, 256, 0, ctx->stream>>>(
+        pa->perm, static_cast<const double*>(jbuf), pa->cptr + ncell, pa->nnz,
+        static_cast<double*>(out));
+  else
+    csc_values_kernel<float><<<blocks, 256, 0, ctx->stream>>>(
+        pa->perm, static_cast<const float*>(jbuf), pa->cptr + ncell, pa->nnz,
+        static_cast<float*>(out));
+  DP_CHECK_CUDA(ctx, cudaGetLastError());
+  timed_end(ctx, "tomo_csc_values");
+  return DP_OK;
+}
+
+// J^T v over the CSC buckets (deterministic segmented sums, no float atomics);
+// csc: jbuf holds the values in CSC order (tomo_csc_values).
 int tomo_transpose(dp_ctx* ctx, const dp_paths* pa, const void* jbuf, int precision,
-                   const double* cot, double* grad) {
+                   const double* cot, double* grad, bool csc) {
   long ncell = long(pa->grid.nx) * pa->grid.ny * pa->grid.nz;
+  const int32_t* perm = csc ? nullptr : pa->perm;
   {
     timed_begin(ctx);
-    const int nbw = int((long(pa->n_big) * 32 + 255) / 256);
     if (precision == 0) {
       const double* v = static_cast<const double*>(jbuf);
       gather_small_kernel<double><<<int((ncell + 255) / 256), 256, 0, ctx->stream>>>(
-          pa->cptr, pa->perm, v, pa->prow, cot, ncell, grad);
+          pa->cptr, perm, v, pa->prow, cot, ncell, grad);
       if (pa->n_big > 0)
-        gather_big_kernel<double><<<nbw, 256, 0, ctx->stream>>>(pa->cptr, pa->perm, v, pa->prow, cot,
-                                                                 pa->big, pa->n_big, grad);
+        gather_big_kernel<double><<<pa->n_big, kBigThreads, 0, ctx->stream>>>(
+            pa->cptr, perm, v, pa->prow, cot, pa->big, pa->n_big, grad);
     } else {
       const float* v = static_cast<const float*>(jbuf);
       gather_small_kernel<float><<<int((ncell + 255) / 256), 256, 0, ctx->stream>>>(
-          pa->cptr, pa->perm, v, pa->prow, cot, ncell, grad);
+          pa->cptr, perm, v, pa->prow, cot, ncell, grad);
       if (pa->n_big > 0)
-        gather_big_kernel<float><<<nbw, 256, 0, ctx->stream>>>(pa->cptr, pa->perm, v, pa->prow, cot,
-                                                                pa->big, pa->n_big, grad);
+        gather_big_kernel<float><<<pa->n_big, kBigThreads, 0, ctx->stream>>>(
+            pa->cptr, perm, v, pa->prow, cot, pa->big, pa->n_big, grad);
     }
     ctx->launches += pa->n_big > 0 ? 1 : 0;
     DP_CHECK_CUDA(ctx, cudaGetLastError());
@@ -1452,7 +1482,7 @@ extern "C" int dp_tomo_eval_noalloc_dev(dp_ctx* ctx, const dp_physics* ph, const
         pa->cptr, pa->perm, jac, pa->prow, cot, ncell, grad);
     ++ctx->launches;
     if (pa->n_big > 0) {
-      gather_big_kernel<float><<<int((long(pa->n_big) * 32 + 255) / 256), 256, 0, ctx->stream>>>(
+      gather_big_kernel<float><<<pa->n_big, kBigThreads, 0, ctx->stream>>>(
           pa->cptr, pa->perm, jac, pa->prow, cot, pa->big, pa->n_big, grad);
       ++ctx->launches;
     }
