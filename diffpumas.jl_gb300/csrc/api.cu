@@ -93,7 +93,9 @@ int dp_init(int device, dp_ctx** out) {
       cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
       cudaMalloc(&c->d_flag, sizeof(int)) != cudaSuccess ||
-      cudaMemset(c->d_flag, 0, sizeof(int)) != cudaSuccess) {
+      cudaMemset(c->d_flag, 0, sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&c->d_work, sizeof(unsigned long long)) != cudaSuccess) {
+    if (c->d_flag) cudaFree(c->d_flag);
     delete c;
     return DP_ERR_CUDA;
   }
@@ -109,6 +111,7 @@ int dp_destroy(dp_ctx* c) {
   for (void* s : c->slot)
     if (s) cudaFree(s);
   if (c->d_flag) cudaFree(c->d_flag);
+  if (c->d_work) cudaFree(c->d_work);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   for (auto& p : c->pending) {

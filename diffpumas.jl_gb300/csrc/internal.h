@@ -30,6 +30,7 @@ struct dp_ctx {
   void* slot[4] = {nullptr, nullptr, nullptr, nullptr};
   size_t slot_bytes[4] = {0, 0, 0, 0};
   int* d_flag = nullptr;  // device error flag (bounded waits that gave up)
+  unsigned long long* d_work = nullptr;  // work counter of dynamically scheduled kernels
   // CTA size of the persistent transport kernels per family (DP_KERNEL_MC,
   // DP_KERNEL_DIR) and precision (DP_PREC_FP64, DP_PREC_MIXED); 0: default.
   int mc_threads[2][2] = {{0, 0}, {0, 0}};

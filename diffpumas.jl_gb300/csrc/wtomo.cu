@@ -65,6 +65,7 @@ struct Params {
   double* flux;
   double* jac;
   int* err_flag;
+  unsigned long long* next_bin;  // bins handed out so far (zeroed before the launch)
 };
 
 // Per-sample results of pass 1.
@@ -199,6 +200,7 @@ int run(dp_ctx* ctx, const dp_physics* ph, const dp_csda_config* c, const dp_csd
   P.flux = flux;
   P.jac = jac;
   P.err_flag = ctx->d_flag;
+  P.next_bin = ctx->d_work;
   if (precision != DP_PREC_FP64 && precision != DP_PREC_MIXED)
     return fail(ctx, DP_ERR_ARG, "precision must be DP_PREC_FP64 or DP_PREC_MIXED");
   const bool mixed = precision == DP_PREC_MIXED;
@@ -213,6 +215,7 @@ int run(dp_ctx* ctx, const dp_physics* ph, const dp_csda_config* c, const dp_csd
   DP_CHECK_CUDA(ctx, cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, ctx->device));
   const long need = (B->n_bins + wt::kThreads / 32 - 1) / (wt::kThreads / 32);
   const long blocks = std::max(1L, std::min(need, long(std::max(per_sm, 1)) * n_sm));
+  DP_CHECK_CUDA(ctx, cudaMemsetAsync(P.next_bin, 0, sizeof(unsigned long long), ctx->stream));
   timed_begin(ctx);
   kernel<<<int(blocks), wt::kThreads, smem, ctx->stream>>>(P);
   DP_CHECK_CUDA(ctx, cudaGetLastError());

@@ -391,9 +391,15 @@ __global__ void __launch_bounds__(kThreads) wtomo_kernel(const __grid_constant__
                  Real(P.rho_porous), Real(P.det_elev)};
 
   const int lane = threadIdx.x & 31;
-  const long warps = long(gridDim.x) * (kThreads / 32);
   const int n_chunks = (P.n_e + 31) / 32;
-  for (long b = long(blockIdx.x) * (kThreads / 32) + (threadIdx.x >> 5); b < P.n_bins; b += warps) {
+  // bins are handed out one at a time as warps finish (path lengths differ
+  // widely; a static stride leaves a partial last round)
+  auto next_bin = [&]() -> long {
+    unsigned long long v = 0;
+    if (lane == 0) v = atomicAdd(P.next_bin, 1ull);
+    return long(__shfl_sync(0xffffffffu, v, 0));
+  };
+  for (long b = next_bin(); b < P.n_bins; b = next_bin()) {
     const int64_t s0 = P.seg_ptr[b], s1 = P.seg_ptr[b + 1];
     const double ct = P.cos_t[b];
     // device-array calls: cells outside the water-fraction vector end the call
