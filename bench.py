@@ -589,6 +589,8 @@ def run_gpu(args):
              "calib": setup_calib}[args.workload]
     kw = {"scale": args.scale} if args.workload in ("c2", "c4", "c5", "dir", "wcsda",
                                                      "calib") else {}
+    if args.workload != "c1":
+        kw["precision"] = args.precision
     step_dev, step_e2e, plain_dev, info, phys = setup(dp, torch, dev, **kw)
     if args.scale != 1.0:
         info["config"]["scale"] = args.scale
@@ -918,6 +920,9 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain one-launch-per-ray form")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="c2/c4: fraction of the histories / lines of sight (profiling captures)")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
+                    help="arithmetic of the timed kernels (c1 is FP64 only); fp64 runs the "
+                         "reference's operations (parity mode)")
     ap.add_argument("--mc-threads", default="auto",
                     help="c2/c4/dir: CTA size of the transport kernels (1024, 768, 512) or "
                          "'auto' (dp_autotune before the warm-up; the default size, 1024, "
