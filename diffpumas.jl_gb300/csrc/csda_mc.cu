@@ -535,19 +535,28 @@ static int setup(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params* p, CsdaP
   return DP_OK;
 }
 
+// One wave of resident blocks whose threads stride over the histories (a
+// grid of several partial waves idles SMs at its end).
 static int launch(dp_ctx* ctx, CsdaParams& P, const dp_physics* ph32 = nullptr) {
-  int threads = 128;
+  const int threads = 128;
+  const size_t smem = ph32 ? size_t(2 * F_NCOL) * ph32->ld32 * sizeof(float)
+                           : size_t(S_NCOL) * P.tab.ld * sizeof(double);
+  int per_sm = 0, n_sm = 0;
+  if (ph32)
+    DP_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, csda32_kernel, threads,
+                                                                     smem));
+  else
+    DP_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, csda_mc_kernel,
+                                                                     threads, smem));
+  DP_CHECK_CUDA(ctx, cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, ctx->device));
   long blocks = (P.n + threads - 1) / threads;
-  if (blocks > 152L * 16) blocks = 152L * 16;
+  blocks = std::min(blocks, long(std::max(per_sm, 1)) * n_sm);
   if (blocks < 1) blocks = 1;
   timed_begin(ctx);
-  if (ph32) {
-    size_t smem = size_t(2 * F_NCOL) * ph32->ld32 * sizeof(float);
+  if (ph32)
     csda32_kernel<<<int(blocks), threads, smem, ctx->stream>>>(P, ph32->dev32, ph32->ld32);
-  } else {
-    size_t smem = size_t(S_NCOL) * P.tab.ld * sizeof(double);
+  else
     csda_mc_kernel<<<int(blocks), threads, smem, ctx->stream>>>(P);
-  }
   DP_CHECK_CUDA(ctx, cudaGetLastError());
   timed_end(ctx, ph32 ? "csda_mc32" : "csda_mc");
   return DP_OK;
