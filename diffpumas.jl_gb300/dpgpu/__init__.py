@@ -622,6 +622,8 @@ from .topography import (ElevationMap, Terrain, TetraVolume,  # noqa: E402
 from .uncertainty import (SystematicSourceResult, TransportUncertaintyResult,  # noqa: E402
                           TransportVariation, compute_flux_uncertainty,
                           estimate_transport_uncertainty, relative_uncertainty_percent)
+from .posterior import (laplace_posterior, null_model_tests, profile_inventory,  # noqa: E402
+                        profiled_log_observation_operator)
 
 
 # ----------------------------------------------------------------- tomography

@@ -283,83 +283,166 @@ def gradient_descent_reconstruct(model, obs, *, w0, n_iter=200, lr=1e-2,
     return w, history
 
 
+def _gn_accept_trial(f_new, f_cur, grad, step, mode):
+    """Acceptance of a trial point (src/Tomography_inverse.jl:441-446):
+    legacy needs a relative decrease of 1e-10; active_set needs a descent
+    direction and the Armijo condition with c = 1e-4."""
+    if not math.isfinite(f_new):
+        return False
+    if mode == "legacy":
+        return f_new < f_cur - 1e-10 * abs(f_cur)
+    directional = float(np.dot(grad, step))
+    return directional < 0 and f_new < f_cur and f_new <= f_cur + 1e-4 * directional
+
+
+def _normal_equations(J, active, W, r, prior, w):
+    Ja = J[:, active]
+    if _issparse(Ja):
+        if W is None:
+            normal, grad = (Ja.T @ Ja).toarray(), Ja.T @ r
+        else:
+            normal, grad = (Ja.T @ Ja.multiply(W[:, None]).tocsr()).toarray(), Ja.T @ (W * r)
+    else:
+        Ja = np.asarray(Ja, np.float64)
+        if W is None:
+            normal, grad = Ja.T @ Ja, Ja.T @ r
+        else:
+            normal, grad = Ja.T @ (W[:, None] * Ja), Ja.T @ (W * r)
+    grad = np.asarray(grad, np.float64).ravel()
+    if prior is not None:
+        grad = grad + _prior_grad(prior, w)[active]
+        normal = normal + _prior_hessian(prior, w)[active][:, active].toarray()
+    return normal, grad
+
+
+def _issparse(x):
+    return _sparse().issparse(x)
+
+
 def gauss_newton_reconstruct(model, obs, *, w0, n_iter=12, box=(0.0, MAX_WATER_FRACTION),
                              prior=None, lm_damping=1e-3, lm_factor=3.0, relinearize=True,
                              weights=None, free=None, predict_only=None, solver_mode="legacy",
-                             rel_objective_tol=0.0, stop=None):
+                             projected_gradient_tol=1e-6, objective_tol=0.0, diagnostics=None,
+                             diagnostic_callback=None, rel_objective_tol=0.0, iterates=None,
+                             update_log=None, stop=None):
     """Box-constrained Levenberg-Marquardt on the regularised normal equations
-    (J^T W J + H_R + mu diag) delta = -(J^T W r + grad R) (:448-603), the
-    reference's legacy acceptance f_new < f - 1e-10 |f|, 6 damping levels x 14
-    halvings.  stop (a one-element list) receives the stop reason."""
-    if solver_mode != "legacy":
-        raise ValueError("only solver_mode='legacy' is provided")
-    w = np.clip(np.array(w0, np.float64), *box)
+    (J^T W J + H_R + mu diag) delta = -(J^T W r + grad R) (src/Tomography_inverse.jl:448-603).
+
+    solver_mode "legacy": 6 damping levels x 14 halvings, accepting a
+    relative decrease of 1e-10.  "active_set": coordinates at a bound whose
+    gradient points outward are frozen, a projected Newton direction that is
+    not descent falls back to the diagonally scaled gradient, acceptance is
+    projected Armijo, a seventh try takes a bounded scaled-gradient step with
+    up to 40 halvings, and the loop stops once the infinity norm of the
+    projected gradient is at most projected_gradient_tol.  predict_only(w)
+    gives the prediction for line-search trials; an accepted trial is checked
+    again with the full model.  diagnostics (a list) and diagnostic_callback
+    receive {iteration, objective, projected_gradient} records, the final
+    state included; iterates receives w0 and every accepted iterate;
+    update_log one record per update; stop (a one-element list) the stop
+    reason: max_updates, projected_gradient, no_step, objective_decrease or
+    no_free_cells."""
+    if solver_mode not in ("legacy", "active_set"):
+        raise ValueError("unknown solver_mode")
+    legacy = solver_mode == "legacy"
+    lo, hi = box
+    w = np.clip(np.array(w0, np.float64), lo, hi)
     obs = np.asarray(obs, np.float64)
     if free is not None and len(free) != len(w):
         raise ValueError("free mask must match w0")
     active = np.arange(len(w)) if free is None else np.nonzero(np.asarray(free, bool))[0]
     W = None if weights is None else np.asarray(weights, np.float64)
 
+    def record(row):
+        if diagnostics is not None:
+            diagnostics.append(row)
+        if diagnostic_callback is not None:
+            diagnostic_callback(row)
+
     def objective(pred, wv):
-        r = pred - obs
+        r = np.asarray(pred, np.float64) - obs
         data = 0.5 * float(r @ r) if W is None else 0.5 * float(np.sum(W * r * r))
         return data + prior_value(prior, wv)
 
     pred, J = model(w)
-    origin, pred0, J0 = w.copy(), np.array(pred), J
+    pred = np.asarray(pred, np.float64)
+    origin, pred0, J0 = w.copy(), pred.copy(), J
     r = pred - obs
     f_cur = objective(pred, w)
     mu = lm_damping
     history = [float(np.linalg.norm(r))]
+    if iterates is not None:
+        iterates.append(w.copy())
     if stop is not None:
         stop[:] = ["max_updates"]
     if len(active) == 0:
         if stop is not None:
             stop[:] = ["no_free_cells"]
         return w, history
-    for _ in range(n_iter):
-        Ja = J[:, active]
-        if W is None:
-            normal = (Ja.T @ Ja).toarray()
-            grad = Ja.T @ r
-        else:
-            WJ = Ja.multiply(W[:, None]).tocsr()
-            normal = (Ja.T @ WJ).toarray()
-            grad = Ja.T @ (W * r)
-        if prior is not None:
-            grad = grad + _prior_grad(prior, w)[active]
-            normal = normal + _prior_hessian(prior, w)[active][:, active].toarray()
+    for update in range(1, n_iter + 1):
+        normal, grad = _normal_equations(J, active, W, r, prior, w)
+        wa = w[active]
+        pg_norm = float(np.max(np.abs(wa - np.clip(wa - grad, lo, hi))))
+        record({"iteration": len(history) - 1, "objective": f_cur, "projected_gradient": pg_norm})
+        if not legacy and pg_norm <= projected_gradient_tol:
+            if stop is not None:
+                stop[:] = ["projected_gradient"]
+            break
+        movable = (np.ones(len(active), bool) if legacy else
+                   ~(((wa <= lo) & (grad > 0)) | ((wa >= hi) & (grad < 0))))
         d = np.diag(normal).copy()
         dmax = d.max() if d.max() > 0 else 1.0
         accepted = False
-        f_before = f_cur
-        for _try in range(6):
+        f_before, mu_before, tries = f_cur, mu, 0
+        for attempt in range(1, (6 if legacy else 7) + 1):
+            tries += 1
             A = normal + np.diag(mu * np.maximum(d, 1e-12 * dmax))
-            try:
-                delta = -np.linalg.solve(A, grad)
-            except np.linalg.LinAlgError:
-                delta = np.zeros(len(active))
+            rescue = not legacy and attempt == 7
+            if rescue:
+                delta = -grad / np.maximum(np.maximum(d, np.max(np.abs(grad))), 1e-30)
+            else:
+                try:
+                    delta = np.zeros(len(active))
+                    m = np.nonzero(movable)[0]
+                    delta[m] = -np.linalg.solve(A[np.ix_(m, m)], grad[m])
+                    if not legacy:
+                        projected = np.clip(wa + delta, lo, hi) - wa
+                        if float(grad @ projected) >= 0:
+                            delta = -grad / np.maximum(d, 1e-12 * dmax)
+                except np.linalg.LinAlgError:
+                    delta = (np.zeros(len(active)) if legacy else
+                             -grad / np.maximum(d, 1e-12 * dmax))
             if not np.all(np.isfinite(delta)):
                 mu = min(mu * lm_factor, 1e12)
                 continue
             alpha = 1.0
-            for _ls in range(14):
+            cached = None
+            for _ls in range(40 if rescue else 14):
                 w_new = w.copy()
-                w_new[active] = np.clip(w[active] + alpha * delta, *box)
+                w_new[active] = np.clip(wa + alpha * delta, lo, hi)
                 if np.array_equal(w_new, w):
                     break
-                if relinearize and predict_only is not None:
-                    pred_new, J_new = predict_only(w_new), None
-                elif relinearize:
-                    pred_new, J_new = model(w_new)
+                if cached is not None and np.array_equal(w_new, cached[0]):
+                    pred_new, J_new = cached[1], cached[2]
+                elif relinearize and predict_only is not None:
+                    pred_new, J_new = np.asarray(predict_only(w_new), np.float64), None
+                    cached = (w_new, pred_new, None)
                 else:
-                    pred_new, J_new = pred0 + J0 @ (w_new - origin), J0
-                f_new = objective(pred_new, w_new)
-                if math.isfinite(f_new) and f_new < f_cur - 1e-10 * abs(f_cur):
-                    if J_new is None:
+                    if relinearize:
                         pred_new, J_new = model(w_new)
+                    else:
+                        pred_new, J_new = pred0 + J0 @ (w_new - origin), J0
+                    pred_new = np.asarray(pred_new, np.float64)
+                    cached = (w_new, pred_new, J_new)
+                f_new = objective(pred_new, w_new)
+                step = w_new[active] - wa
+                if _gn_accept_trial(f_new, f_cur, grad, step, solver_mode):
+                    if relinearize and predict_only is not None and J_new is None:
+                        pred_new, J_new = model(w_new)
+                        pred_new = np.asarray(pred_new, np.float64)
                         f_new = objective(pred_new, w_new)
-                    if math.isfinite(f_new) and f_new < f_cur - 1e-10 * abs(f_cur):
+                        cached = (w_new, pred_new, J_new)
+                    if _gn_accept_trial(f_new, f_cur, grad, step, solver_mode):
                         w, r, J, pred, f_cur = w_new, pred_new - obs, J_new, pred_new, f_new
                         accepted = True
                         break
@@ -369,14 +452,28 @@ def gauss_newton_reconstruct(model, obs, *, w0, n_iter=12, box=(0.0, MAX_WATER_F
                 break
             mu = min(mu * lm_factor, 1e12)
         history.append(float(np.linalg.norm(r)))
+        if update_log is not None:
+            update_log.append({"update": update, "objective_before": f_before,
+                               "objective_after": f_cur, "projected_gradient": pg_norm,
+                               "damping": mu_before, "tries": tries, "accepted": accepted})
         if not accepted:
             if stop is not None:
                 stop[:] = ["no_step"]
             break
+        if iterates is not None:
+            iterates.append(w.copy())
         if rel_objective_tol > 0 and f_before - f_cur < rel_objective_tol * abs(f_before):
             if stop is not None:
                 stop[:] = ["objective_decrease"]
             break
+        if (not legacy and objective_tol > 0 and
+                abs(f_before - f_cur) <= objective_tol * max(1.0, abs(f_before))):
+            break
+    if diagnostics is not None or diagnostic_callback is not None:
+        _, grad = _normal_equations(J, active, W, r, prior, w)
+        wa = w[active]
+        record({"iteration": len(history) - 1, "objective": f_cur,
+                "projected_gradient": float(np.max(np.abs(wa - np.clip(wa - grad, lo, hi))))})
     return w, history
 
 

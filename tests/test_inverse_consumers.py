@@ -263,3 +263,108 @@ def test_gauss_newton_on_the_device_operator(dp):
     assert h[-1] < 0.5 * h[0]
     assert dp.rmse(w, wf, seen) < dp.rmse(w0, wf, seen)
     assert np.array_equal(w[~seen], w0[~seen])
+
+
+# ---------------------------------------------- active-set mode (test/stability_v2.jl)
+def test_reference_gn_acceptance_rule(dp):
+    """test/stability_v2.jl:3-11: projection can turn a descent direction
+    uphill at a shortened step; the active-set rule asks for descent and
+    the Armijo decrease."""
+    from dpgpu.inverse import _gn_accept_trial
+    initial = np.array([0.1, 0.05, 0.9])
+    direction = np.array([10.0, -10.0, -1.0])
+    full = np.clip(initial + direction, 0.0, 1.0) - initial
+    short = np.clip(initial + 0.05 * direction, 0.0, 1.0) - initial
+    assert np.ones(3) @ full < 0 and np.ones(3) @ short > 0
+    assert not _gn_accept_trial(1.00001, 1.0, np.ones(3), short, "active_set")
+    assert not _gn_accept_trial(0.9, 1.0, np.ones(3), short, "active_set")
+    assert _gn_accept_trial(0.9, 1.0, np.ones(3), full, "active_set")
+    assert not _gn_accept_trial(math.nan, 1.0, np.ones(3), full, "legacy")
+    with pytest.raises(ValueError):
+        dp.gauss_newton_reconstruct(lambda w: (w, np.eye(1)), [0.0], w0=[0.1], solver_mode="x")
+
+
+def _robust_example(dp):
+    A = np.array([[1.0, 0.2], [-0.3, 1.0], [0.6, -0.7], [-0.8, -0.1]])
+
+    def model(w):
+        p = np.exp(A @ w)
+        return p, p[:, None] * A
+
+    observed = np.exp(A @ np.array([0.3, 0.6])) * 2.5
+    return dp.profiled_log_observation_operator(model, observed, robust_scale=0.3)
+
+
+@pytest.mark.parametrize("initial", [[0.0, 0.0], [0.7, 0.7], [0.1, 0.8]])
+def test_reference_active_set_recovers_robust_fit(dp, initial):
+    """test/stability_v2.jl:23-29: the robust log-ratio operator from three
+    starting points converges to (0.3, 0.6) with a KKT residual below 1e-8
+    and a non-increasing objective."""
+    robust, _ = _robust_example(dp)
+    diagnostics = []
+    fit, _ = dp.gauss_newton_reconstruct(robust, np.zeros(4), w0=initial, n_iter=100,
+                                         solver_mode="active_set", projected_gradient_tol=1e-9,
+                                         diagnostics=diagnostics)
+    np.testing.assert_allclose(fit, [0.3, 0.6], atol=1e-5)
+    assert diagnostics[-1]["projected_gradient"] < 1e-8
+    assert np.all(np.diff([d["objective"] for d in diagnostics]) <= 1e-12)
+
+
+def test_reference_active_set_coupled_bound(dp):
+    """test/stability_v2.jl:31-38: a coupled normal matrix where clipping
+    the unconstrained Newton step stalls; the active set reaches the bound."""
+    B = np.array([[1.0, 0.9], [0.0, 0.2]])
+    diagnostics, stop = [], [None]
+    fit, _ = dp.gauss_newton_reconstruct(lambda w: (B @ w, B), [-1.0, 0.4], w0=[0.0, 0.5],
+                                         n_iter=100, solver_mode="active_set",
+                                         diagnostics=diagnostics, projected_gradient_tol=1e-9,
+                                         stop=stop)
+    assert fit[0] == pytest.approx(0.0, abs=1e-8)
+    assert diagnostics[-1]["projected_gradient"] < 1e-8
+    assert stop == ["projected_gradient"]
+
+
+def test_reference_cheap_residual_search(dp):
+    """test/stability_v2.jl:41-66: line searches through the prediction
+    callback give the same fit with fewer full-model calls; the bounded
+    projected-gradient rescue recovers a cubic whose derivative vanishes at
+    the start."""
+    calls, cheap = [0], [0]
+
+    def model(w):
+        calls[0] += 1
+        return np.array([math.exp(w[0] ** 3)]), np.array([[3 * w[0] ** 2 * math.exp(w[0] ** 3)]])
+
+    def prediction(w):
+        cheap[0] += 1
+        return np.array([math.exp(w[0] ** 3)])
+
+    op, _, predict = dp.profiled_log_observation_operator(
+        model, [math.exp(0.125)], normalization=1.0, robust_scale=0.3, predict_only=prediction,
+        return_predict_only=True)
+    calls[0] = 0
+    plain, _ = dp.gauss_newton_reconstruct(op, [0.0], w0=[0.01], n_iter=20,
+                                           solver_mode="active_set")
+    plain_calls = calls[0]
+    calls[0] = cheap[0] = 0
+    events, log, its = [], [], []
+    fast, _ = dp.gauss_newton_reconstruct(op, [0.0], w0=[0.01], n_iter=20,
+                                          solver_mode="active_set", predict_only=predict,
+                                          diagnostic_callback=events.append, update_log=log,
+                                          iterates=its)
+    np.testing.assert_allclose(fast, plain, rtol=1e-12, atol=1e-12)
+    assert calls[0] < plain_calls and cheap[0] > 0
+    assert events[-1]["projected_gradient"] <= 1e-6
+    assert len(its) == 1 + sum(e["accepted"] for e in log)
+
+    def cubic(w):
+        return np.array([w[0] ** 3]), np.array([[3 * w[0] ** 2]])
+
+    diagnostics = []
+    rec, _ = dp.gauss_newton_reconstruct(cubic, [0.125], w0=[0.0001], n_iter=100,
+                                         solver_mode="active_set", projected_gradient_tol=1e-12,
+                                         diagnostics=diagnostics,
+                                         predict_only=lambda w: np.array([w[0] ** 3]))
+    np.testing.assert_allclose(rec, [0.5], atol=1e-8)
+    assert diagnostics[-1]["projected_gradient"] < 1e-12
+    assert np.all(np.diff([d["objective"] for d in diagnostics]) <= 0)
