@@ -367,7 +367,7 @@ def setup_c5(dp, torch, dev, precision="mixed", scale=1.0):
         state["rho_host"] = state["rho"].cpu().numpy()
 
     info = {"units": n_iter, "unit": "iterations/s",
-            "kernel": "tomo_adjoint+tomo_forward+tomo_transpose+gn_spmv+gn_colsum+gn_dot",
+            "kernel": "tomo_adjoint+tomo_forward+tomo_transpose+gn_spmv+gn_colsum+gn_dot+gn_cg",
             "alg_bytes": 0, "traffic": None,
             "config": {"workload": "c5: Gauss-Newton inversion, 128x128x64 @ 10 m, 8 x 8192 rays, "
                                    "Poisson counts ~1e3/ray, 50 iterations x 10 CG, start 2650",

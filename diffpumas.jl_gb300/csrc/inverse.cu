@@ -189,32 +189,6 @@ __global__ void cg_init_kernel(const double* g, const double* prec, long n, doub
     p[i] = zi;
   }
 }
-// Ap += mu * diag * p (the Levenberg-Marquardt term)
-__global__ void lm_add_kernel(const double* p, const double* damp, long n, double* Ap) {
-  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
-       i += long(gridDim.x) * blockDim.x)
-    Ap[i] += damp[i] * p[i];
-}
-// x += a p, r -= a Ap, z = r / prec with a = s[0] / s[1]
-__global__ void cg_step_kernel(const double* s, const double* p, const double* Ap,
-                               const double* prec, long n, double* x, double* r, double* z) {
-  const double a = s[1] != 0.0 ? s[0] / s[1] : 0.0;
-  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
-       i += long(gridDim.x) * blockDim.x) {
-    x[i] += a * p[i];
-    double ri = r[i] - a * Ap[i];
-    r[i] = ri;
-    z[i] = ri / prec[i];
-  }
-}
-// p = z + b p with b = s[2] / s[0]; then s[0] = s[2]
-__global__ void cg_dir_kernel(double* s, const double* z, long n, double* p) {
-  const double b = s[0] != 0.0 ? s[2] / s[0] : 0.0;
-  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
-       i += long(gridDim.x) * blockDim.x)
-    p[i] = z[i] + b * p[i];
-}
-__global__ void cg_shift_kernel(double* s) { s[0] = s[2]; }
 // trial = clamp(rho + alpha d, box)
 __global__ void trial_kernel(const double* rho, const double* d, long n, double alpha, double lo,
                              double hi, double* out) {
@@ -263,17 +237,100 @@ __device__ __forceinline__ int degree(Dims d, long c, int* nb) {
   if (k < d.nz - 1) nb[n++] = int(c + sxy);
   return n;
 }
+// sum_{j in N(c)} (x_c - x_j), neighbours in the order of degree(): -x, +x,
+// -y, +y, -z, +z (no neighbour array, so nothing goes to local memory)
+__device__ __forceinline__ double lap_sum(const double* x, Dims d, long c) {
+  const long sxy = long(d.nx) * d.ny;
+  const long k = c / sxy, rem = c - k * sxy;
+  const int j = int(rem / d.nx), i = int(rem - long(j) * d.nx);
+  const double xc = x[c];
+  double s = 0.0;
+  if (i > 0) s += xc - x[c - 1];
+  if (i < d.nx - 1) s += xc - x[c + 1];
+  if (j > 0) s += xc - x[c - d.nx];
+  if (j < d.ny - 1) s += xc - x[c + d.nx];
+  if (k > 0) s += xc - x[c - sxy];
+  if (k < d.nz - 1) s += xc - x[c + sxy];
+  return s;
+}
 // out = (accumulate ? out : 0) + coef * sum_{j in N(c)} (x_c - x_j)
 __global__ void lap_kernel(const double* x, Dims d, double coef, int accumulate, double* out) {
   const long n = long(d.nx) * d.ny * d.nz;
   for (long c = blockIdx.x * long(blockDim.x) + threadIdx.x; c < n;
-       c += long(gridDim.x) * blockDim.x) {
-    int nb[6];
-    const int m = degree(d, c, nb);
-    double s = 0.0;
-    for (int t = 0; t < m; ++t) s += x[c] - x[nb[t]];
-    out[c] = (accumulate ? out[c] : 0.0) + coef * s;
+       c += long(gridDim.x) * blockDim.x)
+    out[c] = (accumulate ? out[c] : 0.0) + coef * lap_sum(x, d, c);
+}
+__device__ __forceinline__ void block_part(double s, double* sh, double* part) {
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int h = kThreads / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) sh[threadIdx.x] += sh[threadIdx.x + h];
+    __syncthreads();
   }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+// CG operator tail in one pass: Ap += damp p (+ coef L p when coef != 0),
+// and the block partials of p . Ap in dot_part_kernel's traversal
+// (kRedBlocks blocks, grid stride), finished by dot_final_kernel.
+__global__ void __launch_bounds__(kThreads) cg_apply_kernel(const double* p, const double* damp,
+                                                            Dims d, double coef, long n,
+                                                            double* Ap, double* part) {
+  __shared__ double sh[kThreads];
+  double s = 0.0;
+  for (long i = blockIdx.x * long(kThreads) + threadIdx.x; i < n; i += long(gridDim.x) * kThreads) {
+    const double pi = p[i];
+    double t = Ap[i] + damp[i] * pi;
+    if (coef != 0.0) t = t + coef * lap_sum(p, d, i);
+    Ap[i] = t;
+    s += pi * t;
+  }
+  block_part(s, sh, part);
+}
+// x += a p, r -= a Ap, z = r / prec with a = s[0] / s[1], and the block
+// partials of r . z (same traversal as above).
+__global__ void __launch_bounds__(kThreads) cg_step_dot_kernel(const double* s, const double* p,
+                                                               const double* Ap,
+                                                               const double* prec, long n,
+                                                               double* x, double* r, double* z,
+                                                               double* part) {
+  __shared__ double sh[kThreads];
+  const double a = s[1] != 0.0 ? s[0] / s[1] : 0.0;
+  double acc = 0.0;
+  for (long i = blockIdx.x * long(kThreads) + threadIdx.x; i < n; i += long(gridDim.x) * kThreads) {
+    x[i] += a * p[i];
+    const double ri = r[i] - a * Ap[i];
+    r[i] = ri;
+    const double zi = ri / prec[i];
+    z[i] = zi;
+    acc += ri * zi;
+  }
+  block_part(acc, sh, part);
+}
+// r . z from the partials: s[2] = it, s[5] = s[2] / s[0] (0 if s[0] is 0,
+// the CG beta), then s[0] = s[2].
+__global__ void __launch_bounds__(kThreads) cg_beta_kernel(const double* part, int nb, double* s) {
+  __shared__ double sh[kThreads];
+  double v = 0.0;
+  for (int b = threadIdx.x; b < nb; b += kThreads) v += part[b];
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int h = kThreads / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) sh[threadIdx.x] += sh[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double rz = sh[0];
+    s[2] = rz;
+    s[5] = s[0] != 0.0 ? rz / s[0] : 0.0;
+    s[0] = rz;
+  }
+}
+// p = z + beta p with beta = s[5]
+__global__ void cg_dir_beta_kernel(const double* s, const double* z, long n, double* p) {
+  const double b = s[5];
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
+       i += long(gridDim.x) * blockDim.x)
+    p[i] = z[i] + b * p[i];
 }
 // block partials of sum over the forward edges of (x_i - x_j)^2
 __global__ void __launch_bounds__(kThreads) prior_part_kernel(const double* x, Dims d,
@@ -340,6 +397,26 @@ struct Solver {
     ++ctx->launches;  // the second of the pair (timed_begin counts the first)
     DP_CHECK_CUDA(ctx, cudaGetLastError());
     timed_end(ctx, "gn_dot");
+    return DP_OK;
+  }
+  // the CG operator tail and step, each with its reduction (timed with the dots)
+  int cg_apply(const double* p, const double* damp, double coef, long n, double* Ap) {
+    timed_begin(ctx);
+    cg_apply_kernel<<<kRedBlocks, kThreads, 0, ctx->stream>>>(p, damp, dims, coef, n, Ap, part);
+    dot_final_kernel<<<1, kThreads, 0, ctx->stream>>>(part, kRedBlocks, s + 1);
+    ++ctx->launches;
+    DP_CHECK_CUDA(ctx, cudaGetLastError());
+    timed_end(ctx, "gn_cg");
+    return DP_OK;
+  }
+  int cg_step(const double* p, const double* Ap, const double* prec, long n, double* x, double* r,
+              double* z) {
+    timed_begin(ctx);
+    cg_step_dot_kernel<<<kRedBlocks, kThreads, 0, ctx->stream>>>(s, p, Ap, prec, n, x, r, z, part);
+    cg_beta_kernel<<<1, kThreads, 0, ctx->stream>>>(part, kRedBlocks, s);
+    ++ctx->launches;
+    DP_CHECK_CUDA(ctx, cudaGetLastError());
+    timed_end(ctx, "gn_cg");
     return DP_OK;
   }
   double host_scalar(const double* d) {
@@ -548,19 +625,11 @@ int dp_tomo_solve_dev(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa,
         for (int k = 0; k < cg_iter && !rc; ++k) {
           if ((rc = S.spmv(p, weight, tmp))) break;  // W J p
           if ((rc = S.transpose(tmp, Ap))) break;    // J^T W J p
-          lm_add_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(p, damp, nc, Ap);
+          // + mu D p (+ 2 w L p), and p . Ap
+          if ((rc = S.cg_apply(p, damp, S.prior > 0.0 ? 2.0 * S.prior : 0.0, nc, Ap))) break;
+          if ((rc = S.cg_step(p, Ap, prec, nc, x, cr, z))) break;  // r . z and beta
+          cg_dir_beta_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(S.s, z, nc, p);
           ++ctx->launches;
-          if (S.prior > 0.0) {  // + 2 w L p
-            lap_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(p, S.dims, 2.0 * S.prior, 1, Ap);
-            ++ctx->launches;
-          }
-          S.dot(p, Ap, nullptr, nc, S.s + 1);
-          cg_step_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(S.s, p, Ap, prec, nc, x, cr, z);
-          ++ctx->launches;
-          S.dot(cr, z, nullptr, nc, S.s + 2);
-          cg_dir_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(S.s, z, nc, p);
-          cg_shift_kernel<<<1, 1, 0, ctx->stream>>>(S.s);
-          ctx->launches += 2;
         }
         if (rc) break;
         // backtracking line search, legacy acceptance (src/Tomography_inverse.jl:443-448)
