@@ -590,6 +590,7 @@ int dp_tomo_solve_dev(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa,
     const int cg_iter = sp->cg_iter > 0 ? sp->cg_iter : 10;
     rc = S.eval(rho, flux, true);
     double f_cur = rc ? 0.0 : S.objective(flux, obs, weight, r, rho);
+    bool speculate = true;
     for (int it = 0; it < sp->n_iter && !rc; ++it) {
       {
         S.dot(r, r, nullptr, nr, S.s + 3);
@@ -614,7 +615,7 @@ int dp_tomo_solve_dev(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa,
       double dmax = 0.0;
       for (double v : hp) dmax = std::max(dmax, v);
       if (!(dmax > 0.0)) dmax = 1.0;
-      bool accepted = false;
+      bool accepted = false, have_jac = false;
       for (int attempt = 0; attempt < 6 && !accepted && !rc; ++attempt) {
         // (J^T W J + mu D) d = -g by Jacobi-preconditioned CG from d = 0
         lm_diag_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(col, nc, 1e-12 * dmax, mu, prec,
@@ -638,23 +639,36 @@ int dp_tomo_solve_dev(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa,
           trial_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(rho, x, nc, alpha, sp->box_lo,
                                                                  sp->box_hi, trial);
           ++ctx->launches;
-          if ((rc = S.eval(trial, tmp, false))) break;
+          // While full steps keep being accepted, the first trial is evaluated
+          // with its Jacobian: on acceptance that is the next iteration's
+          // Jacobian, on rejection the one at rho is rebuilt.
+          const bool spec = speculate && attempt == 0 && ls == 0;
+          if ((rc = S.eval(trial, tmp, spec))) break;
           double f_new = S.objective(tmp, obs, weight, u, trial);
           if (std::isfinite(f_new) && f_new < f_cur - 1e-10 * std::fabs(f_cur)) {
             DP_CHECK_CUDA(ctx, cudaMemcpyAsync(rho, trial, nc * 8, cudaMemcpyDeviceToDevice,
                                                ctx->stream));
             f_cur = f_new;
             accepted = true;
+            have_jac = spec;
             break;
           }
+          if (spec && (rc = S.eval(rho, flux, true))) break;
           alpha *= 0.5;
         }
         if (accepted) mu = std::max(mu / 3.0, 1e-12);
         else mu = std::min(mu * 3.0, 1e12);
       }
       if (rc || !accepted) break;
-      rc = S.eval(rho, flux, true);
-      if (!rc) f_cur = S.objective(flux, obs, weight, r, rho);
+      speculate = have_jac;
+      if (have_jac) {  // flux, residual and Jacobian of the accepted trial are current
+        DP_CHECK_CUDA(ctx, cudaMemcpyAsync(flux, tmp, nr * 8, cudaMemcpyDeviceToDevice,
+                                           ctx->stream));
+        DP_CHECK_CUDA(ctx, cudaMemcpyAsync(r, u, nr * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+      } else {
+        rc = S.eval(rho, flux, true);
+        if (!rc) f_cur = S.objective(flux, obs, weight, r, rho);
+      }
     }
   }
   if (!rc) {
