@@ -176,6 +176,7 @@ def setup_c3(dp, torch, dev, precision="mixed"):
     # ncu capture summarised in profiles/tomo_adjoint_c3_mixed.md
     traffic = 3494400 if precision == "mixed" else None
     info = {"units": n_rays, "unit": "rays/s", "kernel": "tomo_adjoint", "alg_bytes": alg,
+            "dominant": "tomo_adjoint", "dominant_bytes": alg,
             "traffic": traffic,
             "config": {"workload": "c3: tomography forward + adjoint, 64x64x32 @ 10 m, 4x1024 rays, "
                                    "32 energy nodes [1,1e6] GeV, flux + J^T r per step",
@@ -193,6 +194,13 @@ def _device_bytes(torch, dev, obj):
 
 
 C2_MIX = ([1, 3, 2], [0.70, 0.25, 0.05])  # rock, water, air (1-based material indices)
+# Issue figures of the dominant transport kernels, from ncu captures of small
+# cases of the same kernels (the bound that binds them: instruction issue)
+C2_ISSUE = {"issue_active": 0.254, "lanes_per_inst": 8.1,
+            "source": "ncu smsp__issue_active and smsp__thread_inst_executed_per_inst_executed, "
+                      "mc_kernel<float,0,1024> (phase 0) on a 2e5-history c2 case"}
+C4_ISSUE = {"issue_active": 0.263, "lanes_per_inst": 14.2,
+            "source": "ncu, mc_kernel<float,1,1024> (mc_mixed_hi) on a reduced c4 case"}
 
 
 def c2_los(dp, n):
@@ -217,10 +225,14 @@ def setup_c2(dp, torch, dev, precision="mixed", scale=1.0):
     cfgs = {p: dp._mc_config(2026, True, True, 100.0, None, p) for p in ("mixed", "fp64")}
     d_los = _device_bytes(torch, dev, los)
     d_out = torch.zeros(C.sizeof(dp.DpLosResult), dtype=torch.uint8, device=dev)
+    # the plain FP64 form runs a tenth of the histories (its rate per history
+    # does not depend on their number)
+    n_plain = max(1, n // 10)
+    d_los_plain = _device_bytes(torch, dev, c2_los(dp, n_plain))
 
-    def run_dev(p):
-        dp.check(lib.dp_mc_los_dev(ctx, phys.h, mix.h, air.h, C.byref(cfgs[p]), 1, d_los.data_ptr(),
-                                   n, 0, d_out.data_ptr()), ctx)
+    def run_dev(p, nn=n, d=d_los):
+        dp.check(lib.dp_mc_los_dev(ctx, phys.h, mix.h, air.h, C.byref(cfgs[p]), 1, d.data_ptr(),
+                                   nn, 0, d_out.data_ptr()), ctx)
 
     def step_e2e():
         r = dp.backward_mc_batch(phys, los, rock=mix, air=air, seed=2026, precision=precision)
@@ -247,9 +259,16 @@ def setup_c2(dp, torch, dev, precision="mixed", scale=1.0):
                        "n_samples": n, "precision": precision, "tables": "create_physics(MUON), "
                        "rock+air+water, 200 nodes, with Coulomb columns"},
             "h2d": C.sizeof(dp.DpLos), "d2h": C.sizeof(dp.DpLosResult),
-            "plain_what": "FP64 transport (the reference's operations), same launch",
+            # the phase-0 transport kernel (below the mode switch, every history):
+            # 16 B of history parameters in and 16 B of result out per history
+            "dominant": "mc_mixed_lo" if precision == "mixed" else "mc_fp64_lo",
+            "dominant_bytes": n * 32,
+            "issue": C2_ISSUE if precision == "mixed" else None,
+            "plain_what": "FP64 transport (the reference's operations), same launch, "
+                          f"{n_plain} histories", "plain_units": n_plain,
             "plain_reps": 1, "plain_warm": False}
-    return (lambda: run_dev(precision)), step_e2e, (lambda: run_dev("fp64")), info, phys
+    return ((lambda: run_dev(precision)), step_e2e,
+            (lambda: run_dev("fp64", n_plain, d_los_plain)), info, phys)
 
 
 def c4_los(dp, seed=4, n_los=16384):
@@ -289,14 +308,15 @@ def setup_c4(dp, torch, dev, precision="mixed", scale=1.0):
         assert r["n_status_nonzero"].sum() == 0
 
     # plain form: FP64 transport, one launch per line of sight, on the first
-    # 16 lines (their rate stands for the batch)
-    sub = (dp.DpLos * 16)(*[los[i] for i in range(16)])
-    sub_n = sum(los[i].n_samples for i in range(16))
+    # 4 lines (their rate stands for the batch)
+    n_plain = 4
+    sub = (dp.DpLos * n_plain)(*[los[i] for i in range(n_plain)])
+    sub_n = sum(los[i].n_samples for i in range(n_plain))
     d_sub = _device_bytes(torch, dev, sub)
     one = C.sizeof(dp.DpLos)
 
     def plain_dev():
-        for i in range(16):
+        for i in range(n_plain):
             dp.check(lib.dp_mc_los_dev(ctx, phys.h, rock.h, air.h, C.byref(cfgs["fp64"]), 1,
                                        d_sub.data_ptr() + i * one, sub[i].n_samples, 1,
                                        d_out.data_ptr()), ctx)
@@ -314,8 +334,13 @@ def setup_c4(dp, torch, dev, precision="mixed", scale=1.0):
                                    "line of sight",
                        "n_los": n_los, "n_samples": total, "precision": precision},
             "h2d": n_los * C.sizeof(dp.DpLos), "d2h": n_los * C.sizeof(dp.DpLosResult),
+            # the transport kernel above the mode switch (every history here):
+            # 16 B of history parameters in and 16 B of result out per history
+            "dominant": "mc_mixed_hi" if precision == "mixed" else "mc_fp64_hi",
+            "dominant_bytes": total * 32,
+            "issue": C4_ISSUE if precision == "mixed" else None,
             "plain_what": "FP64 transport (+ FP64 CSDA gradient), one launch per line of sight, "
-                          "first 16 lines", "plain_units": sub_n, "plain_reps": 1}
+                          f"first {n_plain} lines", "plain_units": sub_n, "plain_reps": 1}
     return run_dev, step_e2e, plain_dev, info, phys
 
 
@@ -366,9 +391,15 @@ def setup_c5(dp, torch, dev, precision="mixed", scale=1.0):
         step()
         state["rho_host"] = state["rho"].cpu().numpy()
 
+    # algorithmic bytes of one Jacobian evaluation (the dominant kernel, about
+    # one launch per iteration): per ray the row pointers, cos theta and the flux
+    # written (32 B); per segment the cell id, length, density gather and the
+    # FP32 Jacobian value written (24 B)
+    jb = 4 if precision == "mixed" else 8
     info = {"units": n_iter, "unit": "iterations/s",
             "kernel": "tomo_adjoint+tomo_forward+tomo_transpose+gn_spmv+gn_colsum+gn_dot+gn_cg",
-            "alg_bytes": 0, "traffic": None,
+            "alg_bytes": len(rays) * 32 + paths.nnz * (20 + jb), "traffic": None,
+            "dominant": "tomo_adjoint", "dominant_bytes": len(rays) * 32 + paths.nnz * (20 + jb),
             "config": {"workload": "c5: Gauss-Newton inversion, 128x128x64 @ 10 m, 8 x 8192 rays, "
                                    "Poisson counts ~1e3/ray, 50 iterations x 10 CG, start 2650",
                        "rays": len(rays), "segments": paths.nnz, "precision": precision},
@@ -569,6 +600,8 @@ def setup_c1(dp, torch, dev):
         dp.check(lib.dp_backward_mc(phys.ctx.h, phys.h, C.byref(p), C.byref(out)), phys.ctx.h)
 
     info = {"units": n, "unit": "samples/s", "kernel": "csda_mc", "alg_bytes": n * (24 + 16),
+            # per history: (E, q, w) in and the contribution and its derivative out
+            "dominant": "csda_mc", "dominant_bytes": n * (24 + 16),
             "config": {"workload": "c1: backward MC CSDA, StandardRock 100 m @ 45 deg, 2650 kg/m3, "
                                    "E 1-100 GeV, 1e4 histories, with d flux/d rho",
                        "n_samples": n, "precision": "fp64"},
@@ -577,19 +610,23 @@ def setup_c1(dp, torch, dev):
 
 
 # ------------------------------------------------------------------ arms
-def run_gpu(args):
-    import torch
-    world, rank, local = dist_setup()
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    import dpgpu as dp
-    dp._default = dp.Context(local)
-    setup = {"c2": setup_c2, "c3": setup_c3, "c4": setup_c4, "c5": setup_c5,
-             "c1": setup_c1, "dir": setup_dir, "wcsda": setup_wcsda,
-             "calib": setup_calib}[args.workload]
-    kw = {"scale": args.scale} if args.workload in ("c2", "c4", "c5", "dir", "wcsda",
-                                                     "calib") else {}
-    if args.workload != "c1":
+SETUP = {"c2": setup_c2, "c3": setup_c3, "c4": setup_c4, "c5": setup_c5, "c1": setup_c1,
+         "dir": setup_dir, "wcsda": setup_wcsda, "calib": setup_calib}
+UNITS = {"c2": "samples/s", "c3": "rays/s", "c4": "samples/s", "c5": "iterations/s",
+         "c1": "samples/s", "dir": "samples/s", "wcsda": "rays/s", "calib": "calibrations/s"}
+# the other configurations measured with the default (c2) run, each in full:
+# value, e2e, roofline, cpu_baseline, plain form, clocks
+SUB_WORKLOADS = ("c1", "c3", "c4", "c5")
+
+
+def measure(args, workload, dp, torch, dev, world, rank, local, steps, warmup, cpu_budget):
+    """One workload: warm-up, `steps` timed steps (device time, CUDA events on
+    the context stream, L2 flushed between steps), the end-to-end form through
+    the host-pointer C ABI, the plain FP64 form and, on rank 0, the bounded CPU
+    baseline.  Returns the JSON line's fields."""
+    setup = SETUP[workload]
+    kw = {"scale": args.scale} if workload in ("c2", "c4", "c5", "dir", "wcsda", "calib") else {}
+    if workload != "c1":
         kw["precision"] = args.precision
     step_dev, step_e2e, plain_dev, info, phys = setup(dp, torch, dev, **kw)
     if args.scale != 1.0:
@@ -607,16 +644,16 @@ def run_gpu(args):
             info["config"]["cta_threads"] = int(args.mc_threads)
     if args.profile_run:
         # capture mode for the profiler: warm-up steps and one step, nothing else
-        for _ in range(args.warmup + 1):
+        for _ in range(warmup + 1):
             step_dev()
         torch.cuda.synchronize()
-        return
+        return None
     lib = dp.load()
     ctx = phys.ctx.h
     stream = torch.cuda.ExternalStream(lib.dp_get_stream(ctx), device=dev)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step_dev()
     torch.cuda.synchronize()
     barrier(world)
@@ -633,7 +670,7 @@ def run_gpu(args):
         launches0 = lib.dp_launch_count(ctx)
         events = []
         t_wall = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(steps):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             with torch.cuda.stream(stream):
                 flush.zero_()  # L2 flush between timed steps (outside the events)
@@ -649,27 +686,28 @@ def run_gpu(args):
     times = [a.elapsed_time(b) for a, b in events]
     barrier(world)
     launches = lib.dp_launch_count(ctx) - launches0
-    kms = C.c_double(0.0)
-    breakdown = {}
+    kms = 0.0
+    breakdown, nlaunch = {}, {}
     for name in info["kernel"].split("+"):  # summed over the kernels of the timed step
-        k = C.c_double()
-        lib.dp_kernel_time(ctx, name.encode(), C.byref(k))
-        kms.value += k.value
-        breakdown[name] = k.value / args.steps
+        k, cnt = C.c_double(), C.c_longlong()
+        lib.dp_kernel_stats(ctx, name.encode(), C.byref(k), C.byref(cnt))
+        kms += k.value
+        breakdown[name] = k.value / steps
+        nlaunch[name] = cnt.value / steps
     lib.dp_set_timing(ctx, 0)
     ms = max_over_ranks(world, sum(times) / len(times))
     value = world * info["units"] / (ms * 1e-3)
 
     # end to end through the host-pointer C ABI (copies inside the timed region)
-    for _ in range(max(1, args.warmup // 2)):
+    for _ in range(max(1, warmup // 2)):
         step_e2e()
     torch.cuda.synchronize()
     barrier(world)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         step_e2e()
     torch.cuda.synchronize()
-    e2e_ms = max_over_ranks(world, (time.perf_counter() - t0) * 1e3 / args.steps)
+    e2e_ms = max_over_ranks(world, (time.perf_counter() - t0) * 1e3 / steps)
 
     # plain FP64 one-launch-per-ray form (speed-up denominator)
     plain = None
@@ -689,31 +727,65 @@ def run_gpu(args):
                  "what": info.get("plain_what", "plain FP64 one-launch-per-ray, forward only")}
 
     peak, peak_kind = peaks()
-    kernel_ms = kms.value / args.steps
-    achieved = info["alg_bytes"] / (kernel_ms * 1e-3) / 1e9 if kernel_ms > 0 else None
+    # roofline of the dominant kernel: its algorithmic bytes per launch over its
+    # average launch duration (CUDA events on the context stream, timed steps)
+    dom = info.get("dominant") or max(breakdown, key=breakdown.get)
+    dom_ms = breakdown.get(dom, 0.0) / max(1.0, nlaunch.get(dom, 1.0))
+    dom_bytes = info.get("dominant_bytes", info["alg_bytes"])
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9 if dom_ms > 0 else None
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak if achieved else None,
+            "traffic": info.get("traffic"), "kernel": dom, "kernel_ms": dom_ms,
+            "launches_per_step": nlaunch.get(dom),
+            "alg_bytes_per_launch": dom_bytes, "step_kernels_ms": kms / steps,
+            "kernel_ms_each": breakdown, "peak_source": peak_kind}
+    if info.get("issue"):
+        roof["issue"] = info["issue"]
+    if info.get("note"):
+        roof["note"] = info["note"]
     line = {"metric": METRIC, "value": value, "unit": info["unit"], "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "steps": steps, "warmup": warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32+f64" if info["config"].get("precision") == "mixed" else "f64",
             "data": "synthetic (seeded)", "config": dict(info["config"], l2="flushed between steps",
                                                           parallelism=f"replicas x{world}"),
             "e2e": {"value": world * info["units"] / (e2e_ms * 1e-3), "unit": info["unit"],
                     "h2d_bytes_per_step": info["h2d"], "d2h_bytes_per_step": info["d2h"]},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak if achieved else None,
-                         "traffic": info.get("traffic"),
-                         "kernel": info["kernel"], "kernel_ms": kernel_ms,
-                         "kernel_ms_each": breakdown, "peak_source": peak_kind,
-                         **({"note": info["note"]} if info.get("note") else {})},
+            "roofline": roof,
             "gpu_launches": int(launches),
             "plain_gpu": plain,
             "speedup_vs_plain": (value / plain["value"]) if plain else None,
             "clocks": clk.summary(), "wall_s": t_wall}
     if "finish" in info:
         line["result"] = info["finish"]()
+    if "check" in info:
+        line["check"] = info["check"]()
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(workload, budget_s=cpu_budget)
+    return line
+
+
+def run_gpu(args):
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    import dpgpu as dp
+    dp._default = dp.Context(local)
+    line = measure(args, args.workload, dp, torch, dev, world, rank, local, args.steps,
+                   args.warmup, args.cpu_seconds)
+    if line is None:
+        return
+    if args.workload == "c2" and not args.only:
+        # every other configuration of the path, measured the same way with
+        # fewer steps each (their steps are 0.2-630 ms)
+        line["workloads"] = {}
+        for w in SUB_WORKLOADS:
+            sub = measure(args, w, dp, torch, dev, world, rank, local, min(args.steps, 10),
+                          args.warmup, min(args.cpu_seconds, 5.0))
+            line["workloads"][w] = {k: v for k, v in sub.items() if k != "metric"}
+        line["gpu_launches"] += sum(v["gpu_launches"] for v in line["workloads"].values())
     if rank == 0:
-        if not args.no_cpu and args.workload != "c5":
-            line["cpu_baseline"] = cpu_baseline(args.workload, budget_s=args.cpu_seconds)
         print(json.dumps(line))
 
 
@@ -759,6 +831,8 @@ def cpu_baseline(workload, budget_s=15.0, threads=None):
         return {"value": n / dt, "unit": "samples/s", "cores": threads, "kind": "port",
                 "sample": f"{l} lines of sight ({n} histories) of the c4 workload: stochastic "
                           "transport + dual-number CSDA gradient (FP64 oracle, OpenMP)"}
+    if workload == "c5":
+        return cpu_baseline_c5(O, budget_s, threads)
     if workload == "dir":
         return cpu_baseline_dir(O, budget_s, threads)
     if workload == "wcsda":
@@ -792,6 +866,53 @@ def cpu_baseline(workload, budget_s=15.0, threads=None):
     dt = time.perf_counter() - t0
     return {"value": n / dt, "unit": "samples/s", "cores": threads, "kind": "port",
             "sample": f"{n} histories of the c1 workload with the dual-number gradient (FP64 oracle, OpenMP)"}
+
+
+def cpu_baseline_c5(O, budget_s, threads):
+    """One Gauss-Newton iteration of the c5 workload on the host: the oracle's
+    flux and reverse-sweep Jacobian pass over all 65,536 rays (timed on a
+    cycled sample of rays, OpenMP over rays, scaled to the full set) plus the
+    10 conjugate-gradient iterations' products with the sparse Jacobian
+    (scipy.sparse on a matrix of the c5 shape and segment count).  The
+    reference's own solver forms the dense normal matrix, which for
+    1,048,576 cells does not fit in memory, so its loop cannot be timed."""
+    import scipy.sparse as sp
+    from dpgpu.workloads import tomography_config
+    grid, _, rays, nodes = tomography_config(nx=128, ny=128, nz=64, n_detectors=8,
+                                             rays_per_detector=8192)
+    p = O.default_physics((O.STANDARD_ROCK, O.AIR))
+    dims = np.array([grid.nx, grid.ny, grid.nz], np.int32)
+    geom = np.array([*grid.origin, *grid.pitch])
+    rho = np.full(grid.ncell, 2650.0)
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < 0.7 * budget_s:
+        i = (n * 7919) % len(rays)
+        chunk = rays[i:i + 512]
+        O.tomo_vjp(p, 0, 1, dims, geom, rho, 2500.0, chunk, nodes, np.ones(len(chunk)),
+                   threads=threads)
+        n += len(chunk)
+    t_jac = (time.perf_counter() - t0) / n * len(rays)
+    # the products of 10 CG iterations: W J p and J^T (W J p), on a matrix with
+    # the c5 paths' shape and nonzeros (about 99 segments per ray)
+    rng = np.random.default_rng(0)
+    nnz_row = 99
+    cols = rng.integers(0, grid.ncell, len(rays) * nnz_row)
+    J = sp.csr_matrix((rng.uniform(-1, 0, cols.size), cols,
+                       np.arange(0, cols.size + 1, nnz_row)), shape=(len(rays), grid.ncell))
+    Jt = J.T.tocsr()
+    x = rng.uniform(size=grid.ncell)
+    w = rng.uniform(size=len(rays))
+    reps, t1 = 0, time.perf_counter()
+    while reps < 2 or time.perf_counter() - t1 < 0.3 * budget_s:
+        Jt @ (w * (J @ x))
+        reps += 1
+    t_cg = 10 * (time.perf_counter() - t1) / reps
+    return {"value": 1.0 / (t_jac + t_cg), "unit": "iterations/s", "cores": threads,
+            "kind": "port",
+            "sample": f"{n} rays of the c5 workload (cycled) through the oracle's flux + "
+                      f"reverse-sweep J^T r (FP64, OpenMP), scaled to {len(rays)} rays "
+                      f"({t_jac:.2f} s), plus 10 CG iterations of sparse products "
+                      f"(scipy, {t_cg:.2f} s); the reference's dense normal solve does not fit"}
 
 
 def cpu_baseline_dir(O, budget_s, threads):
@@ -880,30 +1001,37 @@ def cpu_baseline_calib(O, budget_s, threads):
                       f"{CALIB_EVALS} x 4096), corrected CSDA flux (FP64 oracle, OpenMP over bins)"}
 
 
+def reference_line(args, workload, steps, warmup, budget):
+    vals = []
+    for _ in range(warmup):
+        cpu_baseline(workload, budget_s=budget / 4)
+    for _ in range(steps):
+        vals.append(cpu_baseline(workload, budget_s=budget)["value"])
+    cb = cpu_baseline(workload, budget_s=min(budget, 1.0))
+    v = statistics.mean(vals)
+    cb["value"] = v
+    unit = UNITS[workload]
+    return {"value": v, "unit": unit, "steps": steps, "warmup": warmup,
+            "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": workload,
+                       "note": "reference is Julia (no toolchain on this box): FP64 oracle port "
+                               "of its code path on all host cores"},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def run_reference(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    units = {"c2": "samples/s", "c3": "rays/s", "c4": "samples/s", "c5": "iterations/s",
-             "c1": "samples/s", "dir": "samples/s", "wcsda": "rays/s",
-             "calib": "calibrations/s"}[args.workload]
-    vals = []
-    for _ in range(args.warmup):
-        cpu_baseline(args.workload, budget_s=args.cpu_seconds / 4)
-    for _ in range(args.steps):
-        vals.append(cpu_baseline(args.workload, budget_s=args.cpu_seconds)["value"])
-    cb = cpu_baseline(args.workload, budget_s=1.0)
-    v = statistics.mean(vals)
-    cb["value"] = v
-    line = {"metric": METRIC, "impl": "reference", "value": v, "unit": units, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": args.workload,
-                       "note": "reference is Julia (no toolchain on this box): FP64 oracle port of "
-                               "its code path on all host cores"},
-            "cpu_baseline": cb,
-            "e2e": {"value": v, "unit": units, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line = {"metric": METRIC, "impl": "reference", "n_gpus": world, "scaling": "weak",
+            "vs_baseline": None}
+    line.update(reference_line(args, args.workload, args.steps, args.warmup, args.cpu_seconds))
+    if args.workload == "c2" and not args.only:
+        line["workloads"] = {w: reference_line(args, w, min(args.steps, 3), 1,
+                                               min(args.cpu_seconds, 3.0))
+                             for w in SUB_WORKLOADS}
     print(json.dumps(line))
 
 
@@ -915,8 +1043,11 @@ def main():
     ap.add_argument("--workload", default="c2",
                     choices=["c2", "c3", "c4", "c5", "c1", "dir", "wcsda", "calib"])
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--cpu-seconds", type=float, default=6.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--only", action="store_true",
+                    help="c2: measure c2 alone (by default the line also holds c1, c3, c4 and "
+                         "c5 under 'workloads')")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain one-launch-per-ray form")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="c2/c4: fraction of the histories / lines of sight (profiling captures)")

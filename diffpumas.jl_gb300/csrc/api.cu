@@ -48,11 +48,12 @@ static void resolve_timing(dp_ctx* ctx) {
     cudaEventElapsedTime(&ms, p.a, p.b);
     bool found = false;
     for (auto& kv : ctx->ktime)
-      if (kv.first == p.name) {
-        kv.second += ms;
+      if (kv.name == p.name) {
+        kv.ms += ms;
+        ++kv.n;
         found = true;
       }
-    if (!found) ctx->ktime.emplace_back(p.name, double(ms));
+    if (!found) ctx->ktime.push_back({p.name, double(ms), 1});
     ctx->spare.push_back(p.a);
     ctx->spare.push_back(p.b);
   }
@@ -142,19 +143,42 @@ int dp_set_timing(dp_ctx* c, int enable) {
 }
 
 int dp_kernel_time(dp_ctx* c, const char* name, double* ms) {
+  return dp_kernel_stats(c, name, ms, nullptr);
+}
+
+int dp_kernel_stats(dp_ctx* c, const char* name, double* ms, long long* launches) {
   if (!c || !name || !ms) return DP_ERR_ARG;
   dp::resolve_timing(c);
   *ms = 0.0;
+  if (launches) *launches = 0;
   for (const auto& kv : c->ktime)
-    if (kv.first == name) *ms = kv.second;
+    if (kv.name == name) {
+      *ms = kv.ms;
+      if (launches) *launches = kv.n;
+    }
   return DP_OK;
 }
 
 long long dp_launch_count(const dp_ctx* c) { return c ? c->launches : -1; }
 
+long long dp_scratch_bytes(const dp_ctx* c) {
+  if (!c) return -1;
+  long long b = 0;
+  for (size_t s : c->slot_bytes) b += (long long)s;
+  return b;
+}
+
 int dp_set_blocking(dp_ctx* c, int blocking) {
   if (!c) return DP_ERR_ARG;
   c->blocking = blocking ? 1 : 0;
+  return DP_OK;
+}
+
+int dp_set_debug_limits(dp_ctx* c, int step_cap, int event_cap, int wait_iters) {
+  if (!c) return DP_ERR_ARG;
+  c->dbg_step_cap = step_cap < 0 ? -1 : step_cap;
+  c->dbg_event_cap = event_cap < 0 ? -1 : event_cap;
+  c->dbg_wait = wait_iters < 0 ? -1 : wait_iters;
   return DP_OK;
 }
 
@@ -167,8 +191,9 @@ int dp_sync(dp_ctx* c) {
   if (flag) {
     cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream);
     cudaStreamSynchronize(c->stream);
-    return dp::fail(c, DP_ERR_STATE, flag == 2 ? "ray segment buffer overflow"
-                                               : "a kernel wait exceeded its limit");
+    return dp::fail(c, DP_ERR_STATE, flag == 2   ? "ray segment buffer overflow"
+                                     : flag == 4 ? "a CSDA history reached the transport step cap"
+                                                 : "a kernel wait exceeded its limit");
   }
   return DP_OK;
 }

@@ -81,6 +81,7 @@ DP_HD Dd operator-(Dd a, Dd b) { return Dd{a.v - b.v, a.d - b.d}; }
 DP_HD Dd operator-(Dd a) { return Dd{-a.v, -a.d}; }
 DP_HD Dd operator*(Dd a, Dd b) { return Dd{a.v * b.v, a.d * b.v + a.v * b.d}; }
 DP_HD Dd operator*(double a, Dd b) { return Dd{a * b.v, a * b.d}; }
+DP_HD Dd operator*(Dd a, double b) { return Dd{a.v * b, a.d * b}; }
 DP_HD Dd operator/(Dd a, Dd b) {
   double q = a.v / b.v;
   return Dd{q, (a.d - q * b.d) / b.v};
@@ -273,19 +274,49 @@ DP_HD void kmerge(KSum& a, const KSum& b) {
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return uint32_t(__cvta_generic_to_shared(p));
 }
-// Copies `ncol` columns of `bytes` bytes each (16-byte multiples, 16-byte
-// aligned) from global to shared memory with cp.async.bulk completing on one
-// mbarrier.  All threads of the block call it.  Returns false if the wait
-// exceeded its iteration limit (the block must then skip its work).
-__device__ __forceinline__ bool stage_columns(double* smem_dst, const double* const* src, int ncol,
-                                              uint32_t bytes, uint64_t* mbar) {
-  uint32_t bar = smem_u32(mbar);
+// Iteration limit of a staging wait (mbarrier try_wait polls).  A context can
+// lower the first wait's limit for failure-path tests (dp_set_debug_limits);
+// the wait for copies still in flight always uses this one.
+constexpr int kStageWait = 1 << 22;
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, int iters) {
+  uint32_t done = 0;
+  for (int it = 0; it < iters && !done; ++it) {
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(0)
+        : "memory");
+  }
+  return done != 0;
+}
+// Ends a staging wait of the whole block: true when every thread saw the
+// copies land.  Otherwise the threads whose wait gave up wait once more
+// (bounded) for the copies in flight, so that no bulk copy still writes this
+// block's shared memory when it leaves, and the result is false.
+__device__ __forceinline__ bool stage_settle(uint32_t bar, bool done) {
+  if (__syncthreads_and(done) != 0) return true;
+  if (!done) mbar_wait(bar, kStageWait);
+  return false;
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar) {
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(1) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   __syncthreads();
+}
+// Copies `ncol` columns of `bytes` bytes each (16-byte multiples, 16-byte
+// aligned) from global to shared memory with cp.async.bulk completing on one
+// mbarrier.  All threads of the block call it.  Returns false if the wait
+// exceeded `wait_iters` polls (the copies have then landed or their own
+// bounded wait gave up too; the block must skip its work).
+__device__ __forceinline__ bool stage_columns(double* smem_dst, const double* const* src, int ncol,
+                                              uint32_t bytes, uint64_t* mbar,
+                                              int wait_iters = kStageWait) {
+  uint32_t bar = smem_u32(mbar);
+  mbar_init(bar);
   if (threadIdx.x == 0) {
     uint32_t total = bytes * uint32_t(ncol);
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(total)
@@ -299,15 +330,7 @@ __device__ __forceinline__ bool stage_columns(double* smem_dst, const double* co
           : "memory");
     }
   }
-  uint32_t done = 0;
-  for (int it = 0; it < (1 << 22) && !done; ++it) {
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(bar), "r"(0)
-        : "memory");
-  }
-  return __syncthreads_and(done != 0) != 0;
+  return stage_settle(bar, mbar_wait(bar, wait_iters));
 }
 #endif
 

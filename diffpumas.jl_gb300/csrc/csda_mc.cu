@@ -54,7 +54,8 @@ struct CsdaParams {
   const double *E, *q, *w;
   double *contrib, *dcontrib, *sample_out;
   int32_t* steps;
-  int* err_flag;
+  int* err_flag;  // 1: a table-staging wait gave up; 4: a history reached step_cap
+  int step_cap, wait_iters;
   // lines of sight: history i belongs to the record l with
   // los_off[l] <= i < los_off[l + 1] and takes its geometry and energy range
   const dp_los* los;
@@ -62,32 +63,74 @@ struct CsdaParams {
   long n_los;
 };
 
-// Shared-memory table slots (all materials share the energy grid).
+// Shared-memory table slots (all materials share the energy grid): the six
+// staged columns, then per-interval columns derived from them once per block
+// (1 / (R[i+1] - R[i]) and S[i+1] - S[i] per material, log-energy widths).
 enum { S_E = 0, S_LOGE, S_RS, S_RR, S_AS, S_AR, S_NCOL };
+enum { D_RINV = 0, D_RDS, D_AINV, D_ADS, D_DLE, D_NCOL };
+constexpr int kCsdaThreads = 64;
 
-__device__ __forceinline__ Dd range_of(const TabView& tv, const double* sE, const double* slE,
-                                       const double* R, Dd E, Dd lE) {
-  return interp_logE(tv, sE, slE, R, E, lE, nullptr);
+// d(a^-1/2) = -1/2 a^-3/2 da
+__device__ __forceinline__ Dd drsqrt(Dd a) {
+  double r = rsqrt(a.v);
+  return Dd{r, -0.5 * r * r * r * a.d};
 }
 
-__global__ void __launch_bounds__(128) csda_mc_kernel(CsdaParams P) {
+// One material's columns as one history walks them.
+struct CsdaMat {
+  const double *R, *S, *rinv, *ds;
+};
+
+// The CSDA history loop of run_backward_mc (src/Geometry.jl:534-672 with
+// transport_backward_step, :424-457, and the step limit, :461-476), in FP64
+// with the density tangent, arranged so that one step costs one exp and one
+// rsqrt:
+//  - the range at the end of a step is carried into the next step (the
+//    reference recomputes it from the energy: R(K(Y)) = Y to rounding);
+//  - the inverse range locates Y's interval and gives log E' = logE[i] +
+//    t dlogE[i] without a log, and S(E') = S[i] + t dS[i] on the same
+//    interval and parameter (the reference interpolates S at log(E'), the
+//    same point to rounding);
+//  - the stopping-power ratios S(E')/S(E) of consecutive steps in one
+//    material telescope to S(end)/S(start) of the material's run, and the
+//    decay factors multiply to exp(-sum dt / c tau);
+//  - beta gamma = sqrt(gamma^2 - 1) with gamma the mean of the step's end
+//    points, so dt = step * rsqrt(gamma^2 - 1).
+// Every branch the reference takes (boundaries, step limits and clamps, the
+// energy ceiling, the acceptance) is the same, and the results agree with
+// the reference's operation-by-operation program to rounding (~1e-13).
+__global__ void __launch_bounds__(kCsdaThreads) csda_mc_kernel(CsdaParams P) {
   extern __shared__ __align__(16) double smem[];
   __shared__ uint64_t mbar;
   const int ld = P.tab.ld, n = P.tab.n;
   const double* src[S_NCOL] = {P.tab.col(0, DP_COL_E),          P.tab.col(0, DP_COL_LOGE),
                                P.tab.col(P.rock, DP_COL_CSDA_S), P.tab.col(P.rock, DP_COL_CSDA_R),
                                P.tab.col(P.air, DP_COL_CSDA_S),  P.tab.col(P.air, DP_COL_CSDA_R)};
-  if (!stage_columns(smem, src, S_NCOL, uint32_t(ld * sizeof(double)), &mbar)) {
+  if (!stage_columns(smem, src, S_NCOL, uint32_t(ld * sizeof(double)), &mbar, P.wait_iters)) {
     if (threadIdx.x == 0) atomicExch(P.err_flag, 1);
     return;
   }
   const double* sE = smem + S_E * ld;
   const double* slE = smem + S_LOGE * ld;
-  const double* rS = smem + S_RS * ld;
-  const double* rR = smem + S_RR * ld;
-  const double* aS = smem + S_AS * ld;
-  const double* aR = smem + S_AR * ld;
+  double* der = smem + S_NCOL * ld;
+  for (int k = threadIdx.x; k < n - 1; k += blockDim.x) {
+    const double* rR = smem + S_RR * ld;
+    const double* rS = smem + S_RS * ld;
+    const double* aR = smem + S_AR * ld;
+    const double* aS = smem + S_AS * ld;
+    der[D_RINV * ld + k] = 1.0 / (rR[k + 1] - rR[k]);
+    der[D_RDS * ld + k] = rS[k + 1] - rS[k];
+    der[D_AINV * ld + k] = 1.0 / (aR[k + 1] - aR[k]);
+    der[D_ADS * ld + k] = aS[k + 1] - aS[k];
+    der[D_DLE * ld + k] = slE[k + 1] - slE[k];
+  }
+  __syncthreads();
+  const CsdaMat rockM{smem + S_RR * ld, smem + S_RS * ld, der + D_RINV * ld, der + D_RDS * ld};
+  const CsdaMat airM{smem + S_AR * ld, smem + S_AS * ld, der + D_AINV * ld, der + D_ADS * ld};
+  const double* dle = der + D_DLE * ld;
   const double eps = kEps64;
+  const double half_inv_m = 0.5 / P.mass;
+  const int32_t cap = P.step_cap;
   for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < P.n;
        i += long(gridDim.x) * blockDim.x) {
     double E0, q, w;
@@ -116,66 +159,85 @@ __global__ void __launch_bounds__(128) csda_mc_kernel(CsdaParams P) {
       q = P.q[i];
       w = P.w[i];
     }
-    Dd E = dd(E0), wt = dd(1.0), z = dd(0.0);
     const Dd rho = dd(G.rho, 1.0);
-    int hint_r = 0, hint_a = 0;
+    const Dd c_rock = dd(0.01, 0.0) / dmax(rho, dd(1e-6));  // 0.01 / rho
+    const double inv_uz = G.uz > eps || G.uz < -eps ? 1.0 / G.uz : 0.0;
+    Dd E = dd(E0), lE = dd(log(E0)), z = dd(0.0), tau = dd(0.0);
+    Dd wS = dd(1.0), Sstart = dd(1.0), Scur = dd(1.0), X = dd(0.0);
+    int mat = -1, k = 0;
     int32_t nsteps = 0;
-    // S(E) at the start of a step equals S(kf) of the previous step in the
-    // same material (same argument, same table): reuse it.
-    int s_mat = -1;
-    Dd s_cache = dd(0.0);
-    // Hard cap on the total step count of one history (the reference loops
-    // until a boundary; a typical history takes 10^2-10^3 steps).
-    const int32_t kMaxSteps = 2000000;
-    for (int outer = 0; outer < 1000 && nsteps < kMaxSteps; ++outer) {
+    while (nsteps < cap) {
       if (!(E.v < P.threshold - eps)) break;
       if (z.v < 0.0 || z.v >= G.H - eps) break;
-      if (wt.v <= 0.0 || !isfinite(wt.v)) break;
-      double limit = E.v < P.low - eps ? fmin(P.low, P.threshold) : P.threshold;
-      for (int inner = 0; inner < 50000 && nsteps < kMaxSteps; ++inner) {
-        if (z.v < 0.0 || z.v >= G.H - eps) break;
-        if (E.v >= limit - eps) break;
-        if (wt.v <= 0.0 || !isfinite(wt.v)) break;
-        const bool in_air = z.v >= G.thickness;
-        const double *S = in_air ? aS : rS, *R = in_air ? aR : rR;
-        int* hint = in_air ? &hint_a : &hint_r;
-        const int mat = in_air ? 1 : 0;
-        Dd dens, tob;
-        if (!in_air) {
-          dens = rho;
-          if (G.uz > eps) tob = (dd(G.thickness) - z) / G.uz;
-          else if (G.uz < -eps) tob = (dd(0.0) - z) / G.uz;
-          else tob = dd(1000.0);
-        } else {
-          dens = 1.205 * dexp(z / -12e3);
-          if (G.uz > eps) tob = (dd(G.H) - z) / G.uz;
-          else if (G.uz < -eps) tob = (dd(G.thickness) - z) / G.uz;
-          else tob = dd(1000.0);
-        }
-        Dd lE = dlog(E);
-        Dd X = range_of(P.tab, sE, slE, R, E, lE);
-        Dd lim = 0.01 * X / dmax(dens, dd(1e-6));
-        if (in_air) lim = dmin(lim, dd(G.air_limit));
-        Dd step = dmin(tob + dd(1e-7), lim);
-        if (step.v < kStepMin) step = dd(kStepMin);
-        else if (step.v > 1000.0) step = dd(1000.0);
-        // transport_backward_step (src/Geometry.jl:424-457)
-        Dd kf = inverse_range(R, sE, slE, n, X + step * dens, hint);
-        Dd gi = dd(1.0) + E / P.mass, gc = dd(1.0) + kf / P.mass, ga = (gi + gc) / 2.0;
-        Dd ba = dsqrt(dmax(dd(1.0) - dd(1.0) / (ga * ga), dd(1e-12)));
-        Dd dt = step / (ba * ga);
-        z = z - step * dd(G.dir_z);
-        Dd Si = (s_mat == mat) ? s_cache : interp_logE(P.tab, sE, slE, S, E, lE, nullptr);
-        Dd Sf = interp_logE(P.tab, sE, slE, S, kf, dlog(kf), nullptr);
-        wt = wt * (Sf / Si) * dexp(dt / -P.ctau);
-        E = kf;
-        s_mat = mat;
-        s_cache = Sf;
-        ++nsteps;
+      const int m = z.v >= G.thickness ? 1 : 0;
+      const CsdaMat M = m ? airM : rockM;
+      if (m != mat) {
+        // entering a material: range and stopping power at E from the
+        // log-energy interpolation (src/Physics.jl:660-687), as the
+        // reference's first step in it does
+        if (mat >= 0) wS = wS * (Scur / Sstart);
+        mat = m;
+        X = interp_logE(P.tab, sE, slE, M.R, E, lE, nullptr);
+        Sstart = interp_logE(P.tab, sE, slE, M.S, E, lE, nullptr);
+        Scur = Sstart;
+        k = E.v <= sE[0] ? 0 : (E.v >= sE[n - 1] ? n - 2
+                                                  : uniform_interval(slE, n, lE.v, P.tab.lE0,
+                                                                     P.tab.inv_dlE));
       }
+      Dd dens, tob, lim;
+      if (m == 0) {
+        dens = rho;
+        if (G.uz > eps) tob = (dd(G.thickness) - z) * inv_uz;
+        else if (G.uz < -eps) tob = (dd(0.0) - z) * inv_uz;
+        else tob = dd(1000.0);
+        lim = X * c_rock;
+      } else {
+        dens = 1.205 * dexp(z / -12e3);
+        if (G.uz > eps) tob = (dd(G.H) - z) * inv_uz;
+        else if (G.uz < -eps) tob = (dd(G.thickness) - z) * inv_uz;
+        else tob = dd(1000.0);
+        lim = dmin(0.01 * X / dmax(dens, dd(1e-6)), dd(G.air_limit));
+      }
+      Dd step = dmin(tob + dd(1e-7), lim);
+      if (step.v < kStepMin) step = dd(kStepMin);
+      else if (step.v > 1000.0) step = dd(1000.0);
+      // inverse range at Y (src/Physics.jl:833-867), clamped at the table ends
+      const Dd Y = X + step * dens;
+      Dd Ef, lEf, Sf;
+      if (Y.v <= M.R[0]) {
+        k = 0;
+        Ef = dd(sE[0]);
+        lEf = dd(slE[0]);
+        Sf = dd(M.S[0]);
+      } else if (Y.v >= M.R[n - 1]) {
+        k = n - 2;
+        Ef = dd(sE[n - 1]);
+        lEf = dd(slE[n - 1]);
+        Sf = dd(M.S[n - 1]);
+      } else {
+        k = walk_up(M.R, n, Y.v, k);
+        const Dd t = (Y - dd(M.R[k])) * M.rinv[k];
+        lEf = dd(slE[k]) + t * dle[k];
+        Ef = dexp(lEf);
+        Sf = dd(M.S[k]) + t * M.ds[k];
+      }
+      // proper time of the step at the mean Lorentz factor
+      const Dd ga = dd(1.0) + (E + Ef) * half_inv_m;
+      const Dd g2 = ga * ga - dd(1.0);
+      const Dd dt = g2.v > 1e-12 * ga.v * ga.v ? step * drsqrt(g2) : step / (1e-6 * ga);
+      tau = tau + dt;
+      z = z - step * dd(G.dir_z);
+      X = Y;
+      E = Ef;
+      lE = lEf;
+      Scur = Sf;
+      ++nsteps;
     }
+    if (mat >= 0) wS = wS * (Scur / Sstart);
+    const Dd wt = wS * dexp(tau / -P.ctau);
     double f = 0.0, df = 0.0;
-    if (z.v >= G.H - 1.0 && E.v < P.threshold && G.cos_final > 0.0) {
+    if (nsteps >= cap) atomicExch(P.err_flag, 4);
+    else if (z.v >= G.H - 1.0 && E.v < P.threshold && G.cos_final > 0.0) {
       double dlogf;
       double F = gccly_flux(G.cs, G.cs129, E.v, q, &dlogf);
       f = wt.v * F;
@@ -279,7 +341,7 @@ __global__ void __launch_bounds__(128) csda32_kernel(CsdaParams P, const float* 
     for (int c = 0; c < F_NCOL; ++c)
       src[m * F_NCOL + c] = reinterpret_cast<const double*>(
           tab32 + (size_t(m == 0 ? P.rock : P.air) * kNC32 + cols[c]) * ld32);
-  if (!stage_columns(smem, src, 2 * F_NCOL, uint32_t(ld32 * sizeof(float)), &mbar)) {
+  if (!stage_columns(smem, src, 2 * F_NCOL, uint32_t(ld32 * sizeof(float)), &mbar, P.wait_iters)) {
     if (threadIdx.x == 0) atomicExch(P.err_flag, 1);
     return;
   }
@@ -328,7 +390,7 @@ __global__ void __launch_bounds__(128) csda32_kernel(CsdaParams P, const float* 
     int32_t nsteps = 0;
     int s_mat = -1;
     Df s_cache{0.f, 0.f};
-    const int32_t kMaxSteps = 2000000;
+    const int32_t kMaxSteps = P.step_cap;
     for (int outer = 0; outer < 1000 && nsteps < kMaxSteps; ++outer) {
       if (!(E.v < thr)) break;
       if (outside()) break;
@@ -384,7 +446,8 @@ __global__ void __launch_bounds__(128) csda32_kernel(CsdaParams P, const float* 
       }
     }
     double f = 0.0, df = 0.0;
-    if (alt_sub(z, Htop) >= -1.f && double(E.v) < P.threshold && G.cos_final > 0.0) {
+    if (nsteps >= kMaxSteps) atomicExch(P.err_flag, 4);
+    else if (alt_sub(z, Htop) >= -1.f && double(E.v) < P.threshold && G.cos_final > 0.0) {
       double dlogf;
       double F = gccly_flux(G.cs, G.cs129, double(E.v), q, &dlogf);
       f = double(wt.v) * F;
@@ -532,15 +595,17 @@ static int setup(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params* p, CsdaP
   P.mass = ph->settings.mass;
   P.ctau = ph->settings.ctau;
   P.err_flag = ctx->d_flag;
+  P.step_cap = step_cap(ctx);
+  P.wait_iters = stage_wait(ctx);
   return DP_OK;
 }
 
 // One wave of resident blocks whose threads stride over the histories (a
 // grid of several partial waves idles SMs at its end).
 static int launch(dp_ctx* ctx, CsdaParams& P, const dp_physics* ph32 = nullptr) {
-  const int threads = 128;
+  const int threads = ph32 ? 128 : kCsdaThreads;
   const size_t smem = ph32 ? size_t(2 * F_NCOL) * ph32->ld32 * sizeof(float)
-                           : size_t(S_NCOL) * P.tab.ld * sizeof(double);
+                           : size_t(S_NCOL + D_NCOL) * P.tab.ld * sizeof(double);
   int per_sm = 0, n_sm = 0;
   if (ph32)
     DP_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, csda32_kernel, threads,
@@ -569,7 +634,8 @@ static int check_flag(dp_ctx* ctx) {
   DP_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (flag) {
     cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream);
-    return fail(ctx, DP_ERR_STATE, "a table-staging wait exceeded its limit");
+    return fail(ctx, DP_ERR_STATE, flag == 4 ? "a CSDA history reached the transport step cap"
+                                             : "a table-staging wait exceeded its limit");
   }
   return DP_OK;
 }
@@ -588,6 +654,8 @@ int csda_los(dp_ctx* ctx, const dp_physics* ph, int rock, int air, double thresh
   P.mass = ph->settings.mass;
   P.ctau = ph->settings.ctau;
   P.err_flag = ctx->d_flag;
+  P.step_cap = step_cap(ctx);
+  P.wait_iters = stage_wait(ctx);
   P.seed = seed;
   P.n = n;
   P.los = los;

@@ -276,7 +276,7 @@ struct PathGeo {
   // the reference's distance difference of its State.
   __device__ int step_end(Hist& h, R moved) const {
     State<R>& s = h.s;
-    if (++h.steps > 2000000) s.status |= ST_STEP_CAP;
+    if (++h.steps > P.C.step_cap) s.status |= ST_STEP_CAP;
     if (s.status & ST_FATAL) return ADV_DONE;
     alt_add(h.dist, moved);
     const R actual = R(alt_since(h.dist, h.d0));
@@ -394,8 +394,11 @@ template <class R, int PHASE, int T>
 __global__ void __launch_bounds__(T, 1) dir_kernel(const __grid_constant__ DirParams P) {
   extern __shared__ __align__(16) unsigned char smem[];
   const uint32_t tables = uint32_t(P.n_staged) * P.lay.med_bytes;
-  if (tables && !stage_blob(smem + 16, P.blob, tables, reinterpret_cast<uint64_t*>(smem))) {
+  if (tables && !stage_blob(smem + 16, P.blob, tables, reinterpret_cast<uint64_t*>(smem),
+                            P.C.wait_iters)) {
     if (threadIdx.x == 0) atomicExch(P.err_flag, 1);
+    PathGeo<R> geo{P, nullptr};
+    drain_histories<R, PHASE>(geo, P.counter, static_cast<DirHandoff<R>*>(P.queue));
     return;
   }
   Med<R>* meds = reinterpret_cast<Med<R>*>(smem + dir_desc_offset<R>(P));

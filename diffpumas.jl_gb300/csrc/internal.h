@@ -24,7 +24,12 @@ struct dp_ctx {
   };
   std::vector<Pending> pending;        // recorded, not yet resolved (no host sync)
   std::vector<cudaEvent_t> spare;      // recycled events
-  std::vector<std::pair<std::string, double>> ktime;
+  struct KTime {
+    std::string name;
+    double ms;
+    long long n;  // timed launches
+  };
+  std::vector<KTime> ktime;
   std::string err;
   // Grow-only device scratch slots, reused across calls on this context.
   void* slot[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -34,9 +39,18 @@ struct dp_ctx {
   // CTA size of the persistent transport kernels per family (DP_KERNEL_MC,
   // DP_KERNEL_DIR) and precision (DP_PREC_FP64, DP_PREC_MIXED); 0: default.
   int mc_threads[2][2] = {{0, 0}, {0, 0}};
+  // Limits lowered for failure-path tests (dp_set_debug_limits); negative:
+  // the default (2,000,000 transport steps, 100,000 hard events per mixed
+  // step, dp::kStageWait polls of a table-staging wait).
+  int dbg_step_cap = -1, dbg_event_cap = -1, dbg_wait = -1;
 };
 
 namespace dp {
+constexpr int kStepCap = 2000000;  // transport steps of one history
+constexpr int kEventCap = 100000;  // hard events of one mixed step (src/MixedTransport.jl:157)
+inline int step_cap(const dp_ctx* c) { return c->dbg_step_cap >= 0 ? c->dbg_step_cap : kStepCap; }
+inline int event_cap(const dp_ctx* c) { return c->dbg_event_cap >= 0 ? c->dbg_event_cap : kEventCap; }
+inline int stage_wait(const dp_ctx* c) { return c->dbg_wait >= 0 ? c->dbg_wait : kStageWait; }
 struct HostElement {
   double Z, A, I, fraction;
 };

@@ -590,7 +590,7 @@ int dp_tomo_solve_dev(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa,
     const int cg_iter = sp->cg_iter > 0 ? sp->cg_iter : 10;
     rc = S.eval(rho, flux, true);
     double f_cur = rc ? 0.0 : S.objective(flux, obs, weight, r, rho);
-    bool speculate = true;
+    bool speculate = sp->no_speculation == 0;
     for (int it = 0; it < sp->n_iter && !rc; ++it) {
       {
         S.dot(r, r, nullptr, nr, S.s + 3);
@@ -615,7 +615,7 @@ int dp_tomo_solve_dev(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa,
       double dmax = 0.0;
       for (double v : hp) dmax = std::max(dmax, v);
       if (!(dmax > 0.0)) dmax = 1.0;
-      bool accepted = false, have_jac = false;
+      bool accepted = false, have_jac = false, first_trial = false;
       for (int attempt = 0; attempt < 6 && !accepted && !rc; ++attempt) {
         // (J^T W J + mu D) d = -g by Jacobi-preconditioned CG from d = 0
         lm_diag_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(col, nc, 1e-12 * dmax, mu, prec,
@@ -651,6 +651,7 @@ int dp_tomo_solve_dev(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa,
             f_cur = f_new;
             accepted = true;
             have_jac = spec;
+            first_trial = attempt == 0 && ls == 0;
             break;
           }
           if (spec && (rc = S.eval(rho, flux, true))) break;
@@ -660,7 +661,9 @@ int dp_tomo_solve_dev(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa,
         else mu = std::min(mu * 3.0, 1e12);
       }
       if (rc || !accepted) break;
-      speculate = have_jac;
+      // speculate again in the next iteration only if this one took its
+      // first trial (a halved or re-damped step predicts more rejections)
+      speculate = sp->no_speculation == 0 && first_trial;
       if (have_jac) {  // flux, residual and Jacobian of the accepted trial are current
         DP_CHECK_CUDA(ctx, cudaMemcpyAsync(flux, tmp, nr * 8, cudaMemcpyDeviceToDevice,
                                            ctx->stream));

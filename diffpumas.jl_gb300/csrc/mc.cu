@@ -573,8 +573,16 @@ __global__ void __launch_bounds__(T, 1) mc_kernel(const __grid_constant__ McPara
   const unsigned char* base = P.blob;
   const uint32_t tables = P.staged ? (POR ? 3 : 2) * P.lay.med_bytes : 0;
   if (P.staged) {
-    if (!stage_blob(smem + 16, P.blob, tables, reinterpret_cast<uint64_t*>(smem))) {
+    if (!stage_blob(smem + 16, P.blob, tables, reinterpret_cast<uint64_t*>(smem), P.C.wait_iters)) {
       if (threadIdx.x == 0) atomicExch(P.err_flag, 1);
+      const Med<R> none{};
+      if constexpr (POR) {
+        SlabGeoP<R> geo{P, none, none, none};
+        drain_histories<R, PHASE>(geo, P.counter, static_cast<HandoffP<R>*>(P.queue));
+      } else {
+        SlabGeo<R> geo{P, none, none};
+        drain_histories<R, PHASE>(geo, P.counter, static_cast<Handoff<R>*>(P.queue));
+      }
       return;
     }
     base = smem + 16;
@@ -786,6 +794,9 @@ int check_cfg(dp_ctx* ctx, const dp_physics* ph, const dp_mc_config* cfg, Consts
   C->mass_f = float(C->mass);
   C->ctau_f = float(C->ctau);
   C->elastic_ratio_f = float(C->elastic_ratio);
+  C->step_cap = step_cap(ctx);
+  C->event_cap = event_cap(ctx);
+  C->wait_iters = stage_wait(ctx);
   C->straggling = cfg->straggling != 0;
   C->scattering = cfg->scattering != 0;
   return DP_OK;
@@ -798,17 +809,31 @@ int read_flag(dp_ctx* ctx) {
   if (flag) {
     cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream);
     return fail(ctx, DP_ERR_STATE,
-                flag == 2 ? "total_samples differs from the sum of n_samples"
-                          : "a table-staging wait exceeded its limit");
+                flag == 2   ? "total_samples differs from the sum of n_samples"
+                : flag == 4 ? "a CSDA history reached the transport step cap"
+                            : "a table-staging wait exceeded its limit");
   }
   return DP_OK;
 }
 
+// The reference's message for the first throw site a history met (the
+// order of the checks follows the order in which the reference would raise).
 int status_code(dp_ctx* ctx, int bits) {
-  if (bits & (DP_ST_DOMAIN_HI | DP_ST_DOMAIN_LO | DP_ST_ZERO_RATE | DP_ST_BAD_WEIGHT))
-    return fail(ctx, DP_ERR_DOMAIN, "a history left the prepared tables or met an invalid hard event");
-  if (bits & (DP_ST_STEP_CAP | DP_ST_EVENT_CAP | DP_ST_TABLE_WAIT))
-    return fail(ctx, DP_ERR_STATE, "a history reached a loop cap");
+  if (bits & DP_ST_DOMAIN_HI)  // src/MixedTransport.jl:45,155,196
+    return fail(ctx, DP_ERR_DOMAIN,
+                "Ancestor energy exceeds mixed tables; regenerate with larger K_max");
+  if (bits & DP_ST_DOMAIN_LO)  // src/MixedTransport.jl:44
+    return fail(ctx, DP_ERR_DOMAIN, "Below prepared mixed kernel domain");
+  if (bits & DP_ST_ZERO_RATE)  // src/MixedTransport.jl:113
+    return fail(ctx, DP_ERR_DOMAIN, "Cannot sample a zero-rate hard event");
+  if (bits & DP_ST_BAD_WEIGHT)  // src/MixedTransport.jl:186
+    return fail(ctx, DP_ERR_DOMAIN, "Invalid adjoint hard-event weight");
+  if (bits & DP_ST_EVENT_CAP)  // src/MixedTransport.jl:193
+    return fail(ctx, DP_ERR_STATE, "Mixed transport exceeded 100000 hard events; segment incomplete");
+  if (bits & DP_ST_STEP_CAP)
+    return fail(ctx, DP_ERR_STATE, "a history reached the transport step cap");
+  if (bits & DP_ST_TABLE_WAIT)
+    return fail(ctx, DP_ERR_STATE, "a table-staging wait exceeded its limit");
   if (bits & DP_ST_NO_PROGRESS)
     return fail(ctx, DP_ERR_STATE, "MC segment made no spatial progress");
   if (bits & DP_ST_BAD_MEDIUM)

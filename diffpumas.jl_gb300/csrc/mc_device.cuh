@@ -132,6 +132,8 @@ struct Consts {
   float thr_low_f, thr_f;  // the same in FP32 (exact for the FP32 transport)
   float mass_f, ctau_f, elastic_ratio_f;
   int straggling, scattering;
+  // loop caps and the table-staging wait limit of the launch
+  int step_cap, event_cap, wait_iters;
   // physics constants in the transport precision
   template <class R> __device__ __forceinline__ R mass_r() const {
     return sizeof(R) == 8 ? R(mass) : R(mass_f);
@@ -671,7 +673,7 @@ __device__ __forceinline__ bool mixed_run_in(const Med<R>& m, const Consts& C, S
   const R* kE = m.kcol(K_E);
   const R Emax = kE[nk - 1];
   const R mass = C.mass_r<R>(), ctau = C.ctau_r<R>(), rdens = x.c;
-  for (; x.event < 100000; ++x.event) {
+  for (; x.event < C.event_cap; ++x.event) {
     R k = x.r0;
     if (x.a <= x.d || k >= x.r2) {
       mixed_end(s, x, Emax, energy_limit, false);
@@ -1231,9 +1233,9 @@ enum : int { ADV_STEP = 0, ADV_DONE = 1, ADV_WAIT = 2, ADV_HANDOFF = 3 };
 
 // Bookkeeping after a completed step.
 template <class R>
-__device__ __forceinline__ int step_done(Hist<R>& h) {
+__device__ __forceinline__ int step_done(Hist<R>& h, const Consts& C) {
   ++h.inner;
-  if (++h.steps > 2000000) h.s.status |= ST_STEP_CAP;
+  if (++h.steps > C.step_cap) h.s.status |= ST_STEP_CAP;
   return (h.s.status & ST_FATAL) != 0 ? ADV_DONE : ADV_STEP;
 }
 
@@ -1390,7 +1392,7 @@ __device__ __forceinline__ int advance(const Med<R>& rock, const Med<R>& air, co
     } else {
       csda_step(m, C, s, Li, rd, step);
     }
-    return step_done(h);
+    return step_done(h, C);
   }
   // The mode checks alternate without a step only if the thresholds were not
   // representable in R (the host rounds them); end the history flagged.
@@ -1423,7 +1425,7 @@ __device__ int resume(const Med<R>& rock, const Med<R>& air, const Med<R>* porou
     straggled_end(m, C, h.s, Li, x.r0, R(d.energy), x.r1, x.r2, d.weight, d.process, d.element,
                   true, false, R(0), x.r3, x.a, true, x.flag != 0, g);
   }
-  return step_done(h);
+  return step_done(h, C);
 }
 
 // A history handed from phase 0 to phase 1: its state, geometry, loop

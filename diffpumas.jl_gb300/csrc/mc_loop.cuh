@@ -58,28 +58,12 @@ inline int with_threads(int threads, F&& f) {
 
 // Copies `bytes` (16-byte multiple) from global to shared memory with
 // cp.async.bulk completing on one mbarrier; all threads call it.  Returns
-// false if the bounded wait gave up; the caller then waits once more
-// (bounded) for the copy in flight before it leaves.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar) {
-  uint32_t done = 0;
-  for (int it = 0; it < (1 << 22) && !done; ++it) {
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(bar), "r"(0)
-        : "memory");
-  }
-  return done != 0;
-}
+// false if the wait exceeded `wait_iters` polls (stage_settle has then waited
+// for the copy in flight).
 static __device__ __noinline__ bool stage_blob(unsigned char* dst, const unsigned char* src, uint32_t bytes,
-                                        uint64_t* mbar) {
+                                        uint64_t* mbar, int wait_iters) {
   uint32_t bar = smem_u32(mbar);
-  if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(1) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  }
-  __syncthreads();
+  mbar_init(bar);
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
                  : "memory");
@@ -93,10 +77,7 @@ static __device__ __noinline__ bool stage_blob(unsigned char* dst, const unsigne
           : "memory");
     }
   }
-  const bool done = mbar_wait(bar);
-  if (__syncthreads_and(done) != 0) return true;
-  if (!done) mbar_wait(bar);
-  return false;
+  return stage_settle(bar, mbar_wait(bar, wait_iters));
 }
 
 // Next history index for the calling thread (warp-aggregated atomic).
@@ -107,6 +88,26 @@ __device__ __forceinline__ long next_history(unsigned long long* counter) {
   if (g.thread_rank() == 0) base = atomicAdd(counter, (unsigned long long)g.size());
   base = g.shfl(base, 0);
   return long(base + g.thread_rank());
+}
+
+// A block whose table staging gave up takes its share of the phase's
+// histories all the same and ends each one flagged DP_ST_TABLE_WAIT (no flux,
+// no table read), so that every history of the launch is accounted for.
+template <class R, int PHASE, class G>
+__device__ __forceinline__ void drain_histories(G& geo, unsigned long long* counter,
+                                                typename G::Queue* queue) {
+  const long n = PHASE == 0 ? geo.n0() : long(*(volatile unsigned long long*)(counter + 2));
+  typename G::Hist h;
+  Stream g;
+  for (;;) {
+    const long j = next_history(counter + PHASE);
+    if (j >= n) break;
+    long i = j;
+    if (PHASE == 0) geo.start(j, h, g);
+    else i = geo.load(queue[j], h, g);
+    h.s.status |= ST_TABLE;
+    geo.end(i, h);
+  }
 }
 
 // Runs histories until none is left for this phase.  counter[PHASE] hands out

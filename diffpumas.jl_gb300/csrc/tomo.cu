@@ -345,6 +345,7 @@ struct EvalP {
   double* jval64;
   float* jval32;
   int* err_flag;
+  int wait_iters;  // polls of the table-staging wait
 };
 
 __device__ __forceinline__ double seg_density(const EvalP& P, int c) {
@@ -386,7 +387,7 @@ __global__ void __launch_bounds__(kWarps * 32) eval64_kernel(EvalP P) {
   const double* src[T_NCOL] = {P.tab.col(0, DP_COL_E),          P.tab.col(0, DP_COL_LOGE),
                                P.tab.col(P.rock, DP_COL_CSDA_S), P.tab.col(P.rock, DP_COL_CSDA_R),
                                P.tab.col(P.air, DP_COL_CSDA_S),  P.tab.col(P.air, DP_COL_CSDA_R)};
-  if (!stage_columns(smem, src, T_NCOL, uint32_t(ld * sizeof(double)), &mbar)) {
+  if (!stage_columns(smem, src, T_NCOL, uint32_t(ld * sizeof(double)), &mbar, P.wait_iters)) {
     if (threadIdx.x == 0) atomicExch(P.err_flag, 1);
     return;
   }
@@ -572,7 +573,7 @@ __global__ void __launch_bounds__(kWarps * 32, 8) eval32_kernel(EvalP P) {
     src[kNC32 + c] = reinterpret_cast<const double*>(base + (size_t(P.air) * kNC32 + c) * ld);
   }
   if (!stage_columns(reinterpret_cast<double*>(fsm), src, 2 * kNC32, uint32_t(ld * sizeof(float)),
-                     &mbar)) {
+                     &mbar, P.wait_iters)) {
     if (threadIdx.x == 0) atomicExch(P.err_flag, 1);
     return;
   }
@@ -1013,6 +1014,7 @@ static int make_eval(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, cons
   P.cell = pa->cell;
   P.len = pa->len;
   P.err_flag = ctx->d_flag;
+  P.wait_iters = stage_wait(ctx);
   return DP_OK;
 }
 
@@ -1417,7 +1419,10 @@ static __device__ __align__(256) float g_noalloc_jacobian[kNoAllocMaxSegments];
 
 // Device address of g_noalloc_jacobian, looked up once per device with that
 // device current (the host-side symbol is only a stand-in, never a device
-// address).
+// address).  The address belongs to the device's primary context, the one
+// the CUDA runtime uses: it stays valid until the process exits unless the
+// caller resets the device (cudaDeviceReset), after which this entry point
+// must not be called again in the process.
 static float* noalloc_scratch(int device, cudaError_t* err) {
   constexpr int kMaxDevices = 64;
   static std::mutex mu;
@@ -1468,10 +1473,12 @@ extern "C" int dp_tomo_eval_noalloc_dev(dp_ctx* ctx, const dp_physics* ph, const
   const long blocks = std::min<long>((pa->n_rays + kWarps - 1) / kWarps, 152L * 16);
   const bool adj = cot != nullptr;
   if (adj) {
-    cudaFuncSetAttribute(eval32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    DP_CHECK_CUDA(ctx, cudaFuncSetAttribute(eval32_kernel<true>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
     eval32_kernel<true><<<int(blocks), kWarps * 32, smem, ctx->stream>>>(P);
   } else {
-    cudaFuncSetAttribute(eval32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    DP_CHECK_CUDA(ctx, cudaFuncSetAttribute(eval32_kernel<false>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
     eval32_kernel<false><<<int(blocks), kWarps * 32, smem, ctx->stream>>>(P);
   }
   ++ctx->launches;

@@ -66,6 +66,7 @@ struct Params {
   double* jac;
   int* err_flag;
   unsigned long long* next_bin;  // bins handed out so far (zeroed before the launch)
+  int wait_iters;                // polls of the table-staging wait
 };
 
 // Per-sample results of pass 1.
@@ -201,6 +202,7 @@ int run(dp_ctx* ctx, const dp_physics* ph, const dp_csda_config* c, const dp_csd
   P.jac = jac;
   P.err_flag = ctx->d_flag;
   P.next_bin = ctx->d_work;
+  P.wait_iters = stage_wait(ctx);
   if (precision != DP_PREC_FP64 && precision != DP_PREC_MIXED)
     return fail(ctx, DP_ERR_ARG, "precision must be DP_PREC_FP64 or DP_PREC_MIXED");
   const bool mixed = precision == DP_PREC_MIXED;

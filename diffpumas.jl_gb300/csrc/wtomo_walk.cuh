@@ -373,7 +373,7 @@ __global__ void __launch_bounds__(kThreads) wtomo_kernel(const __grid_constant__
   extern __shared__ __align__(16) unsigned char smem[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
   double* cols = reinterpret_cast<double*>(smem + 16);
-  if (!stage_columns(cols, P.col, wt::kSlots, P.col_bytes, bar)) {
+  if (!stage_columns(cols, P.col, wt::kSlots, P.col_bytes, bar, P.wait_iters)) {
     if (threadIdx.x == 0) atomicExch(P.err_flag, 1);
     return;
   }

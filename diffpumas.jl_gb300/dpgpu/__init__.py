@@ -14,8 +14,9 @@ from collections import namedtuple
 import numpy as np
 
 from . import _lib
-from ._lib import (COLUMNS, DpElement, DpGrid, DpLos, DpLosResult, DpMaterial, DpMcConfig,
-                   DpMcParams, DpMcResult, DpRay, DpSettings, DpTomoParams, check, load)
+from ._lib import (COLUMNS, DomainError, DpElement, DpError, DpGrid, DpLos, DpLosResult,
+                   DpMaterial, DpMcConfig, DpMcParams, DpMcResult, DpRay, DpSettings,
+                   DpTomoParams, check, load)
 
 PRECISION = {"fp64": 0, "mixed": 1}
 MUON_MASS = 0.10565839
@@ -90,6 +91,17 @@ def set_mc_threads(ctx, family, precision, threads):
     "dir") at `precision` on this context; 0 restores the default."""
     h = _ctx_of(ctx)
     check(load().dp_set_mc_threads(h, _FAMILY[family], _PRECISION[precision], int(threads)), h)
+
+
+def set_debug_limits(ctx, step_cap=None, event_cap=None, wait_iters=None):
+    """dp_set_debug_limits: lowers this context's loop caps (transport steps
+    of a history, hard events of a mixed step) and the poll count of the
+    table-staging waits, for tests of the failure paths.  None restores the
+    default.  A history that reaches a limit ends with its DP_ST_* bit and the
+    call reports DP_ERR_STATE."""
+    h = _ctx_of(ctx)
+    v = lambda x: -1 if x is None else int(x)
+    check(load().dp_set_debug_limits(h, v(step_cap), v(event_cap), v(wait_iters)), h)
 
 
 def get_mc_threads(ctx, family, precision):
@@ -807,7 +819,7 @@ class TomoPaths:
 
     def solve(self, obs, rho0, *, method="gn", n_iter=12, weight=None, cg_iter=10,
               relaxation=0.2, lm_damping=1e-3, box=(500.0, 3500.0), precision="mixed",
-              prior_weight=0.0, smooth_strength=0.1):
+              prior_weight=0.0, smooth_strength=0.1, speculation=True):
         """Inversion loop on the device (src/Tomography_inverse.jl): "sart"
         (sart_reconstruct, Jacobian re-evaluated per iterate) or "gn"
         (gauss_newton_reconstruct with matrix-free CG).  obs, weight and rho0
@@ -818,7 +830,7 @@ class TomoPaths:
         sp = DpSolveParams({"sart": 0, "gn": 1}[method], int(n_iter), int(cg_iter),
                            PRECISION[precision], float(relaxation), float(lm_damping),
                            float(box[0]), float(box[1]), float(prior_weight),
-                           float(smooth_strength))
+                           float(smooth_strength), 0 if speculation else 1)
         hist = np.zeros(n_iter + 1)
         torch.cuda.synchronize(self.dev)
         check(load().dp_tomo_solve_dev(self.physics.ctx.h, self.physics.h, self.h,

@@ -124,7 +124,7 @@ class DpSolveParams(C.Structure):
     _fields_ = [("method", C.c_int), ("n_iter", C.c_int), ("cg_iter", C.c_int),
                 ("precision", C.c_int), ("relaxation", C.c_double), ("lm_damping", C.c_double),
                 ("box_lo", C.c_double), ("box_hi", C.c_double), ("prior_weight", C.c_double),
-                ("smooth_strength", C.c_double)]
+                ("smooth_strength", C.c_double), ("no_speculation", C.c_int)]
 
 
 class DpGrid(C.Structure):
@@ -164,9 +164,12 @@ PROTOTYPES = {
     "dp_get_stream": (_VP, [_P]),
     "dp_set_timing": (_I, [_P, _I]),
     "dp_kernel_time": (_I, [_P, C.c_char_p, C.POINTER(_D)]),
+    "dp_kernel_stats": (_I, [_P, C.c_char_p, C.POINTER(_D), C.POINTER(C.c_longlong)]),
     "dp_launch_count": (C.c_longlong, [_P]),
+    "dp_scratch_bytes": (C.c_longlong, [_P]),
     "dp_set_blocking": (_I, [_P, _I]),
     "dp_sync": (_I, [_P]),
+    "dp_set_debug_limits": (_I, [_P, _I, _I, _I]),
     "dp_mc_thread_choices": (_I, [_I, _VP, _I]),
     "dp_set_mc_threads": (_I, [_P, _I, _I, _I]),
     "dp_get_mc_threads": (_I, [_P, _I, _I, C.POINTER(_I)]),
@@ -263,6 +266,13 @@ class DpError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"libdpgpu error {code}: {msg}")
         self.code = code
+        self.msg = msg
+
+
+class DomainError(DpError):
+    """DP_ERR_DOMAIN: where the reference throws DomainError (an energy outside
+    the prepared tables, src/MixedTransport.jl:44-45,155,196) or errors on an
+    invalid hard-event weight (:186); the message is the reference's."""
 
 
 def check(rc, ctx=None):
@@ -270,5 +280,7 @@ def check(rc, ctx=None):
         msg = load().dp_last_error(ctx).decode() if ctx else ""
         if rc == DP_ERR_ARG:
             raise ValueError(msg or "invalid argument")
+        if rc == DP_ERR_DOMAIN:
+            raise DomainError(rc, msg)
         raise DpError(rc, msg)
     return rc

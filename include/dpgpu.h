@@ -82,8 +82,13 @@ void* dp_get_stream(const dp_ctx* ctx);
  * "tomo_forward", "tomo_adjoint", "tomo_transpose". */
 int dp_set_timing(dp_ctx* ctx, int enable);
 int dp_kernel_time(dp_ctx* ctx, const char* kernel, double* ms_total);
+/* The same with the number of timed launches of that kernel (may be NULL). */
+int dp_kernel_stats(dp_ctx* ctx, const char* kernel, double* ms_total, long long* launches);
 /* Number of kernels this context has launched. */
 long long dp_launch_count(const dp_ctx* ctx);
+/* Bytes of device scratch this context holds (its grow-on-demand slots,
+ * reused across calls and freed by dp_destroy); a diagnostic. */
+long long dp_scratch_bytes(const dp_ctx* ctx);
 /* blocking = 1 (default): device-pointer calls synchronise and report kernel
  * errors before returning.  blocking = 0: they return once enqueued (no host
  * synchronisation, e.g. for CUDA-graph capture or back-to-back solver
@@ -91,6 +96,16 @@ long long dp_launch_count(const dp_ctx* ctx);
  * synchronise. */
 int dp_set_blocking(dp_ctx* ctx, int blocking);
 int dp_sync(dp_ctx* ctx);
+/* Failure-path limits of this context, for tests of the error paths (no
+ * reference counterpart; the reference's loops throw at fixed counts,
+ * src/MixedTransport.jl:157,193).  step_cap: transport steps of one history
+ * (default 2,000,000; DP_ST_STEP_CAP); event_cap: hard events of one mixed
+ * step (default 100,000 as in the reference; DP_ST_EVENT_CAP); wait_iters:
+ * polls of a table-staging wait before the block gives up (default 2^22;
+ * DP_ST_TABLE_WAIT, the copy in flight is still awaited before the block
+ * leaves).  A negative value restores the default.  Every limit ends its loop
+ * with a status the call reports (DP_ERR_STATE); none of them faults. */
+int dp_set_debug_limits(dp_ctx* ctx, int step_cap, int event_cap, int wait_iters);
 
 /* ------------------------------------------------------------------ launch shapes
  * CTA size of the persistent transport kernels per kernel family and
@@ -662,7 +677,9 @@ int dp_tomo_eval(dp_ctx* ctx, const dp_physics* phys, const dp_paths* paths,
  * that first call before any stream capture.  All calls share the array and
  * every value is rewritten before it is read, so nothing needs clearing, but
  * calls that overlap on the GPU (other contexts or streams at the same time)
- * race on it. */
+ * race on it.  The address looked up is the one in the device's primary
+ * context (the CUDA runtime's): after a cudaDeviceReset the process must not
+ * call this entry point again. */
 int dp_tomo_eval_noalloc_dev(dp_ctx* ctx, const dp_physics* phys, const dp_paths* paths,
                              const dp_tomo_params* tp, const double* rho, const double* cot,
                              double* flux, double* grad_rho);
@@ -702,6 +719,11 @@ typedef struct {
                             src/Tomography_inverse.jl:17-79): GN objective term,
                             SART smoothing sweep */
   double smooth_strength; /* SART sweep strength (<= 0: 0.1) */
+  int no_speculation;     /* GN: 0 (default) evaluates the first line-search trial
+                             with its Jacobian while the iterations' first trials
+                             keep being accepted (the accepted trial's Jacobian is
+                             the next iteration's); 1 never does.  The iterates
+                             are the same either way. */
 } dp_solve_params;
 /* obs: n_rays observed fluxes, weight: n_rays data weights (NULL: 1), rho:
  * the start density in, the estimate out (all device pointers; node arrays of

@@ -453,3 +453,55 @@ def mc_histories(p, rock, air, thickness, density, elevation, H, E, q, w, seed, 
                            source_max, contrib, status, steps, Ef, threads, int(porous), geo[4],
                            geo[5])
     return contrib, status, steps, Ef
+
+
+# ----------------------------------------------------------------- Philox draws
+# The counter-based generator (Philox4x32-10, Salmon et al., SC'11) that keys
+# every history's stream by (seed, history id), vectorised over histories.
+# Block 0 holds run_backward_mc's energy and charge draw (src/Pumas.jl:195-207,
+# src/Geometry.jl:863-875: kf = E_min exp(rk u1), w = 2 kf rk, q = +-1 with
+# probability 1/2); blocks 1-2 hold the per-history geometry that a line of
+# sight with ranges draws (thickness and density from block 1, elevation from
+# block 2), uniform on each range.
+_M0, _M1, _W0, _W1, _MASK = 0xD2511F53, 0xCD9E8D57, 0x9E3779B9, 0xBB67AE85, 0xFFFFFFFF
+
+
+def philox(ids, block, seed):
+    ids = np.asarray(ids, np.uint64)
+    c0, c1 = ids & _MASK, ids >> np.uint64(32)
+    c2 = np.full_like(c0, block)
+    c3 = np.zeros_like(c0)
+    k0, k1 = np.uint64(seed & _MASK), np.uint64((seed >> 32) & _MASK)
+    m0, m1, mask = np.uint64(_M0), np.uint64(_M1), np.uint64(_MASK)
+    for _ in range(10):
+        p0, p1 = m0 * c0, m1 * c2
+        c0, c1, c2, c3 = ((p1 >> np.uint64(32)) ^ c1 ^ k0, p1 & mask,
+                          (p0 >> np.uint64(32)) ^ c3 ^ k1, p0 & mask)
+        k0 = (k0 + np.uint64(_W0)) & mask
+        k1 = (k1 + np.uint64(_W1)) & mask
+    return c0, c1, c2, c3
+
+
+def u01(a, b):
+    return ((a >> np.uint64(5)).astype(np.float64) * 67108864.0 +
+            (b >> np.uint64(6)).astype(np.float64)) / 9007199254740992.0
+
+
+def energy_draws(seed, ids, emin, emax):
+    """(E, q, w) of histories `ids` (Philox block 0)."""
+    x, y, z, w = philox(ids, 0, seed)
+    rk = math.log(emax / emin)
+    E = emin * np.exp(rk * u01(x, y))
+    return E, np.where(u01(z, w) > 0.5, 1.0, -1.0), 2.0 * E * rk
+
+
+def los_geometry_draws(seed, ids, thickness, thickness_max, density, density_max, elevation,
+                       elevation_max):
+    """Per-history (thickness, density, elevation) of a line of sight with
+    ranges (Philox blocks 1 and 2)."""
+    x1, y1, z1, w1 = philox(ids, 1, seed)
+    x2, y2, _, _ = philox(ids, 2, seed)
+    t = thickness + (thickness_max - thickness) * u01(x1, y1)
+    r = density + (density_max - density) * u01(z1, w1)
+    e = elevation + (elevation_max - elevation) * u01(x2, y2)
+    return t, r, e

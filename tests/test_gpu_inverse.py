@@ -157,3 +157,20 @@ def test_smoothness_prior_gradient_step(dp, problem):
                                precision="fp64", prior_weight=1e-8)
     assert roughness(smooth.cpu().numpy()) < roughness(free.cpu().numpy())
     assert np.isfinite(hist[-1]) and hist[-1] < hist[0]
+
+
+def test_gn_speculation_gives_the_same_iterates(dp, problem):
+    """The speculative Jacobian (the first line-search trial evaluated with
+    its Jacobian while first trials keep being accepted) changes which
+    evaluations run, not the iterates.  A tiny initial damping makes early
+    full steps overshoot, so the line search rejects trials, rebuilds the
+    Jacobian at the iterate and later resumes speculating; the misfit history
+    and the estimate equal those of a run that never speculates, bit for bit."""
+    paths, T = problem["paths"], problem["T"]
+    rho0 = T(np.full(paths.grid.ncell, 2650.0))
+    runs = [paths.solve(problem["obs"], rho0, method="gn", n_iter=8, lm_damping=1e-9,
+                        precision="mixed", speculation=s) for s in (True, False)]
+    (r_on, h_on), (r_off, h_off) = runs
+    np.testing.assert_array_equal(h_on, h_off)
+    np.testing.assert_array_equal(r_on.cpu().numpy(), r_off.cpu().numpy())
+    assert np.isfinite(h_on[0]) and np.nanmin(h_on[1:]) < h_on[0]

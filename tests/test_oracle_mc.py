@@ -120,29 +120,26 @@ def test_mixed_kernel_preparation(oracle, orc_default):
     assert np.allclose(S[::8], p.column(0, "mixed_S"), rtol=1e-12)
 
 
-FLAT_POINTS = [(0.0, 0.0), (0.0, 60.0), (50.0, 15.0), (100.0, 45.0), (200.0, 0.0),
-               (300.0, 30.0), (400.0, 60.0), (500.0, 75.0), (600.0, 15.0), (800.0, 0.0),
-               (800.0, 45.0), (800.0, 75.0)]
-
-
 def test_flat_column_flux_vs_reference_mc(oracle):
     """docs/revision_evidence/corrected_transport/full102_comparison.csv: the
-    reference's stochastic flux (straggling + scattering, mode switch at
-    100 GeV, primary altitude 1000 m, rock 2650 kg/m^3, final energies
-    log-uniform on [1e-3, 1e9] GeV with weight 2 E log(1e12), charge +-1)
-    against the oracle with 20000 histories per point.  The RNG streams
-    differ, so agreement is statistical: every |z| < 4 and the RMS z-score
-    of the 12 points below 1.6 (the 102-point comparison at 40000 histories
-    gives RMS 0.97 against the reference and 1.02 against PUMAS C)."""
+    reference's stochastic flux at all 102 points (17 rock thicknesses x 6
+    zenith angles; straggling + scattering, mode switch at 100 GeV, primary
+    altitude 1000 m, rock 2650 kg/m^3, final energies log-uniform on
+    [1e-3, 1e9] GeV with weight 2 E log(1e12), charge +-1) against the oracle
+    with 20000 histories per point.  The RNG streams differ, so agreement is
+    statistical: with z the difference over the combined sigma, at most 2 of
+    the 102 points may have |z| > 3 (the expected count of a correct model is
+    0.3) and the RMS z must be at most 1.2 (1 for a correct model)."""
     p = revision_physics(oracle)
     rows = {}
     for line in open(os.path.join(GOLDEN, "full102_comparison.csv")):
         f = line.strip().split(",")
         if f[0][0].isdigit():
             rows[(float(f[0]), float(f[1]))] = (float(f[4]), float(f[5]))
+    assert len(rows) == 102
     n, span = 20000, math.log(1e12)
     zs = []
-    for (t, zen) in FLAT_POINTS:
+    for (t, zen), (jf, js) in sorted(rows.items()):
         seed = int(t * 100 + zen) + 1
         rng = np.random.default_rng(seed)
         E = 1e-3 * np.exp(span * rng.random(n))
@@ -152,11 +149,10 @@ def test_flat_column_flux_vs_reference_mc(oracle):
         assert np.all(st == 0)
         f = c.mean()
         s = math.sqrt(max((c * c).mean() - f * f, 0.0) / n)
-        jf, js = rows[(t, zen)]
-        z = (f - jf) / math.hypot(s, js)
-        assert abs(z) < 4, (t, zen, f, jf)
-        zs.append(z)
-    assert math.sqrt(np.mean(np.square(zs))) < 1.6
+        zs.append((f - jf) / math.hypot(s, js))
+    zs = np.array(zs)
+    assert (np.abs(zs) > 3).sum() <= 2, zs
+    assert math.sqrt(np.mean(zs ** 2)) <= 1.2, math.sqrt(np.mean(zs ** 2))
 
 
 def test_history_streams_are_independent_of_threads(oracle, orc_default):
