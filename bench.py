@@ -32,6 +32,7 @@ independent replicas (weak scaling).
 import argparse
 import ctypes as C
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -172,8 +173,8 @@ def setup_c3(dp, torch, dev, precision="mixed"):
     # and the Jacobian value written (4 B in mixed precision, 8 B in FP64).
     jb = 4 if precision == "mixed" else 8
     alg = n_rays * (16 + 8 + 8) + nseg * (4 + 8 + 8 + jb)
-    # DRAM read+write bytes of one tomo_adjoint launch on this workload, from the
-    # ncu capture summarised in profiles/tomo_adjoint_c3_mixed.md
+    # DRAM read+write bytes of one tomo_adjoint launch on this workload, from an
+    # ncu capture of the kernel on this workload
     traffic = 3494400 if precision == "mixed" else None
     info = {"units": n_rays, "unit": "rays/s", "kernel": "tomo_adjoint", "alg_bytes": alg,
             "dominant": "tomo_adjoint", "dominant_bytes": alg,
@@ -186,6 +187,19 @@ def setup_c3(dp, torch, dev, precision="mixed"):
             "h2d": 8 * (rho_h.size + cot_h.size + 3 * len(nodes[0])),
             "d2h": 8 * (n_rays + grid.ncell)}
     return step_dev, step_e2e, plain_dev, info, phys
+
+
+def bench_checks():
+    """FP64 oracle fluxes of the c2 and c4 workloads on the bench's own streams
+    (written by tests/golden/make_bench_checks.py)."""
+    with open(os.path.join(ROOT, "tests", "golden", "bench_checks.json")) as f:
+        return json.load(f)
+
+
+def los_results(dp, d_out, n):
+    raw = d_out.cpu().numpy().tobytes()
+    k = C.sizeof(dp.DpLosResult)
+    return [dp.DpLosResult.from_buffer_copy(raw[i * k:(i + 1) * k]) for i in range(n)]
 
 
 def _device_bytes(torch, dev, obj):
@@ -238,9 +252,22 @@ def setup_c2(dp, torch, dev, precision="mixed", scale=1.0):
         r = dp.backward_mc_batch(phys, los, rock=mix, air=air, seed=2026, precision=precision)
         assert r["n_status_nonzero"][0] == 0
 
+    def check():
+        # the step's answer against the FP64 oracle on the first 2e5 of the same
+        # streams (statistical: the two estimates share those histories)
+        torch.cuda.synchronize()
+        r = los_results(dp, d_out, 1)[0]
+        ref = bench_checks()["c2"]
+        z = (r.flux - ref["flux"]) / math.hypot(r.sigma, ref["sigma"])
+        assert r.n_status_nonzero == 0 and abs(z) < 3, (r.flux, r.sigma, ref)
+        return {"flux": r.flux, "sigma": r.sigma, "oracle_flux": ref["flux"],
+                "oracle_sigma": ref["sigma"], "oracle_histories": ref["n_histories"], "z": z,
+                "pass": True}
+
     kernel = ("mc_init+mc_mixed_lo+mc_mixed_hi+mc_finish+mc_tally" if precision == "mixed"
               else "mc_init+mc_fp64_lo+mc_fp64_hi+mc_finish+mc_tally")
     info = {"units": n, "unit": "samples/s", "kernel": kernel, "family": "mc",
+            **({"check": check} if scale == 1.0 else {}),
             # per history: contribution (8 B) and status (4 B) written by the
             # transport kernel and read back by the tally
             "alg_bytes": n * 24,
@@ -321,9 +348,25 @@ def setup_c4(dp, torch, dev, precision="mixed", scale=1.0):
                                        d_sub.data_ptr() + i * one, sub[i].n_samples, 1,
                                        d_out.data_ptr()), ctx)
 
+    def check():
+        # 64 seeded lines of sight against the FP64 oracle over the same
+        # histories (every history of each line, the same streams)
+        torch.cuda.synchronize()
+        res = los_results(dp, d_out, n_los)
+        zs = []
+        for ref in bench_checks()["c4"]["lines"]:
+            r = res[ref["line"]]
+            assert r.n_status_nonzero == 0 and r.n_samples == ref["n_histories"]
+            zs.append((r.flux - ref["flux"]) / math.hypot(r.sigma, ref["sigma"]))
+        zmax = float(np.abs(zs).max())
+        assert zmax < 3, zs
+        return {"lines": len(zs), "max_abs_z": zmax,
+                "rms_z": float(np.sqrt(np.mean(np.square(zs)))), "pass": True}
+
     kernel = "mc_init+mc_mixed_lo+mc_mixed_hi+mc_finish+csda_mc32+mc_tally" if precision == "mixed" \
         else "mc_init+mc_fp64_lo+mc_fp64_hi+mc_finish+csda_mc+mc_tally"
     info = {"units": total, "unit": "samples/s", "kernel": kernel, "family": "mc",
+            **({"check": check} if scale == 1.0 else {}),
             # per history: contribution and status written and read back,
             # CSDA contribution and derivative written and read back
             "alg_bytes": total * (24 + 32), "traffic": None,
@@ -585,26 +628,28 @@ def setup_calib(dp, torch, dev, precision="mixed", scale=1.0):
     return step_dev, step_e2e, plain_dev, info, phys
 
 
-def setup_c1(dp, torch, dev):
+def setup_c1(dp, torch, dev, precision="mixed"):
+    """run_backward_mc in CSDA mode with the gradient.  "mixed": the FP32 walk
+    with float-pair range, tangent and altitude, FP64 start offset, final
+    energy and flux (within 1e-6 of the FP64 oracle, tested); "fp64": the
+    reference's FP64 operations."""
     phys = dp.create_physics()
     n = 10000
-    kw = dict(rock_thickness=100.0, rock_density=2650.0, elevation=45.0, energy_min=1.0,
-              energy_max=100.0, n_samples=n, compute_gradient=True, seed=42, straggling=False,
-              scattering=False)
     p = dp._mc_params(phys, 100.0, 2650.0, 45.0, 1.0, 100.0, n, True, 42, False, False, 100.0,
-                      None, 3e4)
+                      None, 3e4, precision)
     out = dp.DpMcResult()
     lib = dp.load()
 
     def step():
         dp.check(lib.dp_backward_mc(phys.ctx.h, phys.h, C.byref(p), C.byref(out)), phys.ctx.h)
 
-    info = {"units": n, "unit": "samples/s", "kernel": "csda_mc", "alg_bytes": n * (24 + 16),
+    kernel = "csda_mc32" if precision == "mixed" else "csda_mc"
+    info = {"units": n, "unit": "samples/s", "kernel": kernel, "alg_bytes": n * (24 + 16),
             # per history: (E, q, w) in and the contribution and its derivative out
-            "dominant": "csda_mc", "dominant_bytes": n * (24 + 16),
+            "dominant": kernel, "dominant_bytes": n * (24 + 16),
             "config": {"workload": "c1: backward MC CSDA, StandardRock 100 m @ 45 deg, 2650 kg/m3, "
                                    "E 1-100 GeV, 1e4 histories, with d flux/d rho",
-                       "n_samples": n, "precision": "fp64"},
+                       "n_samples": n, "precision": precision},
             "h2d": 0, "d2h": 8 * 7}
     return step, step, None, info, phys
 
@@ -626,8 +671,7 @@ def measure(args, workload, dp, torch, dev, world, rank, local, steps, warmup, c
     baseline.  Returns the JSON line's fields."""
     setup = SETUP[workload]
     kw = {"scale": args.scale} if workload in ("c2", "c4", "c5", "dir", "wcsda", "calib") else {}
-    if workload != "c1":
-        kw["precision"] = args.precision
+    kw["precision"] = args.precision
     step_dev, step_e2e, plain_dev, info, phys = setup(dp, torch, dev, **kw)
     if args.scale != 1.0:
         info["config"]["scale"] = args.scale
@@ -636,9 +680,10 @@ def measure(args, workload, dp, torch, dev, world, rank, local, steps, warmup, c
         # CTA size of the persistent transport kernels: dp_autotune over the
         # compiled sizes on this very step (untimed), or the size given
         if args.mc_threads == "auto" and not args.profile_run:
-            best, ms_each = dp.autotune(phys, fam, "mixed", step_dev)
-            info["config"]["cta_threads"] = best
-            info["config"]["autotune_ms"] = {str(k): round(v, 2) for k, v in ms_each.items()}
+            best, tried = dp.autotune_shape(phys, fam, "mixed", step_dev)
+            info["config"]["cta_threads"] = best["threads"]
+            info["config"]["launch_shape"] = best
+            info["config"]["autotune_ms"] = [dict(s, ms=round(v, 2)) for s, v in tried]
         elif args.mc_threads != "auto":
             dp.set_mc_threads(phys, fam, "mixed", int(args.mc_threads))
             info["config"]["cta_threads"] = int(args.mc_threads)
@@ -683,6 +728,9 @@ def measure(args, workload, dp, torch, dev, world, rank, local, steps, warmup, c
         t_wall = time.perf_counter() - t_wall
     dp.check(lib.dp_sync(ctx), ctx)
     lib.dp_set_blocking(ctx, 1)
+    # the last timed step's answer against the oracle (before the other forms
+    # overwrite its outputs)
+    checked = info["check"]() if "check" in info else None
     times = [a.elapsed_time(b) for a, b in events]
     barrier(world)
     launches = lib.dp_launch_count(ctx) - launches0
@@ -758,8 +806,8 @@ def measure(args, workload, dp, torch, dev, world, rank, local, steps, warmup, c
             "clocks": clk.summary(), "wall_s": t_wall}
     if "finish" in info:
         line["result"] = info["finish"]()
-    if "check" in info:
-        line["check"] = info["check"]()
+    if checked is not None:
+        line["check"] = checked
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(workload, budget_s=cpu_budget)
     return line
@@ -784,6 +832,14 @@ def run_gpu(args):
             sub = measure(args, w, dp, torch, dev, world, rank, local, min(args.steps, 10),
                           args.warmup, min(args.cpu_seconds, 5.0))
             line["workloads"][w] = {k: v for k, v in sub.items() if k != "metric"}
+        if args.precision == "mixed":
+            # c1 in the reference's FP64 operations too (its configuration
+            # names FP64; the mixed form is the headline entry)
+            sub = measure(argparse.Namespace(**{**vars(args), "precision": "fp64",
+                                                "no_cpu": True}), "c1", dp, torch, dev, world,
+                          rank, local, min(args.steps, 10), args.warmup, 0.0)
+            line["workloads"]["c1"]["fp64"] = {k: sub[k] for k in
+                                               ("value", "unit", "ms_per_step", "e2e", "dtype")}
         line["gpu_launches"] += sum(v["gpu_launches"] for v in line["workloads"].values())
     if rank == 0:
         print(json.dumps(line))
@@ -1052,8 +1108,8 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0,
                     help="c2/c4: fraction of the histories / lines of sight (profiling captures)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
-                    help="arithmetic of the timed kernels (c1 is FP64 only); fp64 runs the "
-                         "reference's operations (parity mode)")
+                    help="arithmetic of the timed kernels; fp64 runs the reference's "
+                         "operations (parity mode)")
     ap.add_argument("--mc-threads", default="auto",
                     help="c2/c4/dir: CTA size of the transport kernels (1024, 768, 512) or "
                          "'auto' (dp_autotune before the warm-up; the default size, 1024, "

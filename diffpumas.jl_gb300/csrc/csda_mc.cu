@@ -251,9 +251,12 @@ __global__ void __launch_bounds__(kCsdaThreads) csda_mc_kernel(CsdaParams P) {
 
 // ------------------------------------------------------------ mixed precision
 // The same history loop with the transport and its density tangent in FP32
-// (the single-precision derived columns: range, stopping power, energy, log
-// energy and the per-interval slopes) and the position in FP64.  Within the
-// mixed-mode tolerance (1e-4) of the FP64 program.
+// (the single-precision derived columns: range pairs, stopping power,
+// energy, log energy and the per-interval slopes), the range, its tangent
+// and the altitude as float pairs, FP64 only for the start offset, the final
+// energy and the flux.  A history's flux and d flux / d rho stay within ~1e-6
+// of the FP64 program: the FP64 pipe runs at 1/64 of the FP32 rate on this
+// GPU, and a CSDA history is a chain of 10^2-10^3 dependent steps.
 struct Df {
   float v, d;
 };
@@ -276,11 +279,20 @@ __device__ __forceinline__ Df fsqrt(Df a) {
 __device__ __forceinline__ Df fmin2(Df a, Df b) { return b.v < a.v ? b : a; }
 __device__ __forceinline__ Df fmax2(Df a, Df b) { return b.v > a.v ? b : a; }
 
-// Staged FP32 columns per material (rock, air).
-enum { F_R = 0, F_S, F_E, F_LE, F_SLOPE, F_DSDLE, F_DLE, F_NCOL };
+// exp(x) - 1 for an offset inside one log-energy interval: its Taylor series
+// to x^7 (truncation below 2e-9 relative for |x| <= 0.25), expm1f beyond.
+__device__ __forceinline__ float expm1_small(float x) {
+  if (fabsf(x) > 0.25f) return expm1f(x);
+  return x * (1.f + x * (0.5f + x * (1.f / 6.f + x * (1.f / 24.f + x * (1.f / 120.f +
+                                               x * (1.f / 720.f + x * (1.f / 5040.f)))))));
+}
+
+// Staged FP32 columns per material (rock, air); RL is the low part of the
+// range pair.
+enum { F_R = 0, F_RL, F_S, F_E, F_LE, F_SLOPE, F_DSDLE, F_DLE, F_NCOL };
 
 struct Tab32 {
-  const float *R, *S, *E, *LE, *SLOPE, *DSDLE, *DLE;
+  const float *R, *RL, *S, *E, *LE, *SLOPE, *DSDLE, *DLE;
 };
 __device__ __forceinline__ int f_interval(const Tab32& t, int n, float lx, const TabView& tv) {
   int i;
@@ -294,47 +306,24 @@ __device__ __forceinline__ int f_interval(const Tab32& t, int n, float lx, const
   while (i < n - 2 && !(lx < t.LE[i + 1])) ++i;
   return i;
 }
-// y(E) linear in log E, derivative through log E (src/Physics.jl:660-739).
-__device__ __forceinline__ void f_lookup(const Tab32& t, int n, const TabView& tv, Df E, Df* X,
-                                         Df* S) {
-  if (E.v <= t.E[0]) {
-    *X = Df{t.R[0], 0.f};
-    *S = Df{t.S[0], 0.f};
-    return;
-  }
-  if (E.v >= t.E[n - 1]) {
-    *X = Df{t.R[n - 1], 0.f};
-    *S = Df{t.S[n - 1], 0.f};
-    return;
-  }
-  float lx = logf(E.v), dl = E.d / E.v;
-  int i = f_interval(t, n, lx, tv);
-  float tt = (lx - t.LE[i]) / t.DLE[i];
-  *X = Df{t.R[i] + tt * (t.R[i + 1] - t.R[i]), dl / t.SLOPE[i]};
-  *S = Df{t.S[i] + tt * (t.S[i + 1] - t.S[i]), t.DSDLE[i] * dl};
-}
-__device__ __forceinline__ Df f_stopping(const Tab32& t, int n, const TabView& tv, Df E) {
-  Df X, S;
-  f_lookup(t, n, tv, E, &X, &S);
-  return S;
-}
-// Inverse range (src/Physics.jl:833-867), differentiated through t and exp.
-__device__ __forceinline__ Df f_inverse(const Tab32& t, int n, Df X, int* hint) {
-  if (X.v <= t.R[0]) return Df{t.E[0], 0.f};
-  if (X.v >= t.R[n - 1]) return Df{t.E[n - 1], 0.f};
-  int i = *hint < 0 ? 0 : (*hint > n - 2 ? n - 2 : *hint);
-  while (i > 0 && X.v < t.R[i]) --i;
-  while (i < n - 2 && !(X.v < t.R[i + 1])) ++i;
-  *hint = i;
-  float e = expf(t.LE[i] + (X.v - t.R[i]) * t.SLOPE[i]);
-  return Df{e, e * t.SLOPE[i] * X.d};
-}
 
+// The lean step of csda_mc_kernel in FP32: one exponential and one rsqrt per
+// step, telescoped stopping-power ratios, a summed decay exponent.  What
+// keeps a history within ~1e-6 of the FP64 program:
+//  - the range and its density tangent are float pairs (TwoSum), so that
+//    10^2-10^3 increments do not drift;
+//  - the energy at a range is E_k (1 + expm1(dle)) with dle the log-energy
+//    offset inside interval k (|dle| <= one grid step), not exp(log E_k +
+//    dle): a float log E carries an absolute error of ~1e-6;
+//  - the history's starting offset comes from (E0 - E_k) / E_k, and the
+//    energy that enters the flux is formed in FP64 from the FP64 node E_k;
+//  - a material entered mid-walk is located by the interval and offset the
+//    walk already holds (all materials share the energy grid).
 __global__ void __launch_bounds__(128) csda32_kernel(CsdaParams P, const float* tab32, int ld32) {
   extern __shared__ __align__(16) double smem[];
   __shared__ uint64_t mbar;
   const int n = P.tab.n;
-  const int cols[F_NCOL] = {C32_RH, C32_S, C32_E, C32_LE, C32_SLOPE, C32_DSDLE, C32_DLE};
+  const int cols[F_NCOL] = {C32_RH, C32_RL, C32_S, C32_E, C32_LE, C32_SLOPE, C32_DSDLE, C32_DLE};
   // FP32 columns are staged as pairs of doubles: ld32 floats = ld32/2 doubles
   const double* src[2 * F_NCOL];
   for (int m = 0; m < 2; ++m)
@@ -348,10 +337,10 @@ __global__ void __launch_bounds__(128) csda32_kernel(CsdaParams P, const float* 
   const float* sf = reinterpret_cast<const float*>(smem);
   auto tab = [&](int m) {
     const float* b = sf + size_t(m) * F_NCOL * ld32;
-    return Tab32{b + F_R * ld32, b + F_S * ld32, b + F_E * ld32, b + F_LE * ld32,
-                 b + F_SLOPE * ld32, b + F_DSDLE * ld32, b + F_DLE * ld32};
+    return Tab32{b + F_R * ld32,  b + F_RL * ld32,    b + F_S * ld32,     b + F_E * ld32,
+                 b + F_LE * ld32, b + F_SLOPE * ld32, b + F_DSDLE * ld32, b + F_DLE * ld32};
   };
-
+  const double* E64 = P.tab.col(0, DP_COL_E);
   const float mass = float(P.mass), ctau = float(P.ctau);
   for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < P.n;
        i += long(gridDim.x) * blockDim.x) {
@@ -376,80 +365,143 @@ __global__ void __launch_bounds__(128) csda32_kernel(CsdaParams P, const float* 
       q = P.q[i];
       w = P.w[i];
     }
-    Df E{float(E0), 0.f}, wt{1.f, 0.f};
-    // altitude as an FP32 pair with its FP32 tangent; boundaries likewise
-    F2 z{0.f, 0.f};
-    float zd = 0.f;
-    const F2 thick = f2_make(G.thickness), Htop = f2_make(G.H);
     const Df rho{float(G.rho), 1.f};
+    const Df c_rock = Df{0.01f, 0.f} / fmax2(rho, Df{1e-6f, 0.f});
+    const F2 thick = f2_make(G.thickness), Htop = f2_make(G.H);
     const float uz = float(G.uz), dir_z = float(G.dir_z), air_limit = float(G.air_limit);
     const float eps = float(kEps64);
-    const float thr = float(P.threshold), low = float(P.low);
-    auto outside = [&]() { return z.h + z.l < 0.f || alt_sub(z, Htop) >= 0.f; };
-    int hint_r = 0, hint_a = 0;
-    int32_t nsteps = 0;
-    int s_mat = -1;
-    Df s_cache{0.f, 0.f};
-    const int32_t kMaxSteps = P.step_cap;
-    for (int outer = 0; outer < 1000 && nsteps < kMaxSteps; ++outer) {
-      if (!(E.v < thr)) break;
-      if (outside()) break;
-      if (wt.v <= 0.f || !isfinite(wt.v)) break;
-      const float limit = E.v < low ? fminf(low, thr) : thr;
-      for (int inner = 0; inner < 50000 && nsteps < kMaxSteps; ++inner) {
-        if (outside()) break;
-        if (E.v >= limit) break;
-        if (wt.v <= 0.f || !isfinite(wt.v)) break;
-        const bool in_air = alt_sub(z, thick) >= 0.f;
-        const int mat = in_air ? 1 : 0;
-        const Tab32 t = tab(mat);
-        Df dens;
-        float ahead;
-        if (!in_air) {
-          dens = rho;
-          ahead = uz > eps ? alt_sub(thick, z) : -(z.h + z.l);
-        } else {
-          float dv = 1.205f * expf(-(z.h + z.l) * (1.f / 12e3f));
-          dens = Df{dv, -dv / 12e3f * zd};
-          ahead = uz > eps ? alt_sub(Htop, z) : alt_sub(thick, z);
-        }
-        float tob_v, tob_d;
-        if (uz > eps || uz < -eps) {
-          tob_v = ahead / uz;
-          tob_d = -zd / uz;
-        } else {
-          tob_v = 1000.f;
-          tob_d = 0.f;
-        }
-        Df X, Si;
-        f_lookup(t, n, P.tab, E, &X, &Si);
-        if (s_mat == mat) Si = s_cache;
-        Df lim = 0.01f * X / fmax2(dens, Df{1e-6f, 0.f});
-        if (in_air) lim = fmin2(lim, Df{air_limit, 0.f});
-        // step = min(tob + 1e-7, lim) clamped to [STEP_MIN, 1000]
-        Df step = tob_v + 1e-7f <= lim.v ? Df{tob_v + 1e-7f, tob_d} : lim;
-        if (step.v < float(kStepMin)) step = Df{float(kStepMin), 0.f};
-        else if (step.v > 1000.f) step = Df{1000.f, 0.f};
-        Df kf = f_inverse(t, n, X + step * dens, in_air ? &hint_a : &hint_r);
-        Df gi = Df{1.f, 0.f} + E / Df{mass, 0.f}, gc = Df{1.f, 0.f} + kf / Df{mass, 0.f};
-        Df ga = 0.5f * (gi + gc);
-        Df ba = fsqrt(fmax2(Df{1.f, 0.f} - Df{1.f, 0.f} / (ga * ga), Df{1e-12f, 0.f}));
-        Df dt = step / (ba * ga);
-        alt_add(z, -(step.v * dir_z));
-        zd -= step.d * dir_z;
-        Df Sf = f_stopping(t, n, P.tab, kf);
-        wt = wt * (Sf / Si) * fexp(Df{-1.f / ctau, 0.f} * dt);
-        E = kf;
-        s_mat = mat;
-        s_cache = Sf;
-        ++nsteps;
+    const float inv_uz = uz > eps || uz < -eps ? 1.f / uz : 0.f;
+    const float thr = float(P.threshold), half_inv_m = 0.5f / mass;
+    // position on the energy grid: interval k and offset dle (value and
+    // tangent); edge -1 / +1: clamped at the first / last node
+    int k, edge = 0;
+    Df dle{0.f, 0.f};
+    {
+      const Tab32 t0 = tab(0);
+      if (E0 <= E64[0]) {
+        k = 0;
+        edge = -1;
+      } else if (E0 >= E64[n - 1]) {
+        k = n - 2;
+        edge = 1;
+        dle.v = t0.DLE[n - 2];
+      } else {
+        k = f_interval(t0, n, logf(float(E0)), P.tab);
+        while (k > 0 && E0 < E64[k]) --k;
+        while (k < n - 2 && !(E0 < E64[k + 1])) ++k;
+        dle.v = log1pf(float(E0 - E64[k]) / float(E64[k]));
       }
     }
+    Df E{float(E0), 0.f}, tau{0.f, 0.f};
+    Df wS{1.f, 0.f}, Sstart{1.f, 0.f}, Scur{1.f, 0.f};
+    F2 X{0.f, 0.f}, Xd{0.f, 0.f}, z{0.f, 0.f};
+    float zd = 0.f, em1 = 0.f;
+    bool moved = false;
+    int mat = -1;
+    int32_t nsteps = 0;
+    const int32_t cap = P.step_cap;
+    while (nsteps < cap) {
+      if (!(E.v < thr)) break;
+      if (z.h + z.l < 0.f || alt_sub(z, Htop) >= 0.f) break;
+      const int m = alt_sub(z, thick) >= 0.f ? 1 : 0;
+      const Tab32 t = tab(m);
+      if (m != mat) {
+        // range and stopping power at the current energy, linear in log E on
+        // interval k (src/Physics.jl:660-687), clamped at the ends
+        if (mat >= 0) wS = wS * (Scur / Sstart);
+        mat = m;
+        if (edge != 0) {
+          const int j = edge < 0 ? 0 : n - 1;
+          X = F2{t.R[j], t.RL[j]};
+          Xd = F2{0.f, 0.f};
+          Sstart = Df{t.S[j], 0.f};
+        } else {
+          const float tt = dle.v / t.DLE[k];
+          X = F2{t.R[k], t.RL[k]};
+          alt_add(X, tt * ((t.R[k + 1] - t.R[k]) + (t.RL[k + 1] - t.RL[k])));
+          Xd = F2{dle.d / t.SLOPE[k], 0.f};
+          Sstart = Df{t.S[k] + dle.v * t.DSDLE[k], dle.d * t.DSDLE[k]};
+        }
+        Scur = Sstart;
+      }
+      Df dens, lim;
+      float ahead;
+      const Df Xv{X.h + X.l, Xd.h + Xd.l};
+      if (m == 0) {
+        dens = rho;
+        ahead = uz > eps ? alt_sub(thick, z) : -(z.h + z.l);
+        lim = Xv * c_rock;
+      } else {
+        const float dv = 1.205f * expf(-(z.h + z.l) * (1.f / 12e3f));
+        dens = Df{dv, -dv / 12e3f * zd};
+        ahead = uz > eps ? alt_sub(Htop, z) : alt_sub(thick, z);
+        lim = fmin2(0.01f * Xv / fmax2(dens, Df{1e-6f, 0.f}), Df{air_limit, 0.f});
+      }
+      const Df tob = inv_uz != 0.f ? Df{ahead * inv_uz, -zd * inv_uz} : Df{1000.f, 0.f};
+      Df step = tob.v + 1e-7f <= lim.v ? Df{tob.v + 1e-7f, tob.d} : lim;
+      if (step.v < float(kStepMin)) step = Df{float(kStepMin), 0.f};
+      else if (step.v > 1000.f) step = Df{1000.f, 0.f};
+      // Y = X + step * dens (pairs), and the inverse range at Y
+      // (src/Physics.jl:833-867)
+      F2 Y = X, Yd = Xd;
+      alt_add(Y, step.v * dens.v);
+      alt_add(Yd, step.d * dens.v + step.v * dens.d);
+      const float Yv = Y.h + Y.l;
+      Df Ef, Sf;
+      if (Yv <= t.R[0]) {
+        k = 0;
+        edge = -1;
+        dle = Df{0.f, 0.f};
+        Ef = Df{t.E[0], 0.f};
+        Sf = Df{t.S[0], 0.f};
+      } else if (Yv >= t.R[n - 1]) {
+        k = n - 2;
+        edge = 1;
+        dle = Df{t.DLE[n - 2], 0.f};
+        Ef = Df{t.E[n - 1], 0.f};
+        Sf = Df{t.S[n - 1], 0.f};
+      } else {
+        while (k > 0 && Yv < t.R[k]) --k;
+        while (k < n - 2 && !(Yv < t.R[k + 1])) ++k;
+        edge = 0;
+        dle = Df{alt_sub(Y, F2{t.R[k], t.RL[k]}) * t.SLOPE[k], (Yd.h + Yd.l) * t.SLOPE[k]};
+        em1 = expm1_small(dle.v);
+        const float ev = t.E[k] + t.E[k] * em1;
+        Ef = Df{ev, ev * dle.d};
+        Sf = Df{t.S[k] + dle.v * t.DSDLE[k], dle.d * t.DSDLE[k]};
+      }
+      // proper time of the step at the mean Lorentz factor
+      const Df ga = Df{1.f, 0.f} + (E + Ef) * Df{half_inv_m, 0.f};
+      const Df g2 = ga * ga - Df{1.f, 0.f};
+      Df dt;
+      if (g2.v > 1e-12f * ga.v * ga.v) {
+        const float r = rsqrtf(g2.v);
+        dt = step * Df{r, -0.5f * r * r * r * g2.d};
+      } else {
+        dt = step / (Df{1e-6f, 0.f} * ga);
+      }
+      tau = tau + dt;
+      alt_add(z, -(step.v * dir_z));
+      zd -= step.d * dir_z;
+      X = Y;
+      Xd = Yd;
+      E = Ef;
+      Scur = Sf;
+      moved = true;
+      ++nsteps;
+    }
+    if (mat >= 0) wS = wS * (Scur / Sstart);
+    const Df wt = wS * fexp(Df{-1.f / ctau, 0.f} * tau);
+    // the final energy in FP64 from the FP64 node
+    const double Efin = !moved     ? E0
+                        : edge < 0 ? E64[0]
+                        : edge > 0 ? E64[n - 1]
+                                   : E64[k] + E64[k] * double(em1);
     double f = 0.0, df = 0.0;
-    if (nsteps >= kMaxSteps) atomicExch(P.err_flag, 4);
-    else if (alt_sub(z, Htop) >= -1.f && double(E.v) < P.threshold && G.cos_final > 0.0) {
+    if (nsteps >= cap) atomicExch(P.err_flag, 4);
+    else if (alt_sub(z, Htop) >= -1.f && Efin < P.threshold && G.cos_final > 0.0) {
       double dlogf;
-      double F = gccly_flux(G.cs, G.cs129, double(E.v), q, &dlogf);
+      double F = gccly_flux(G.cs, G.cs129, Efin, q, &dlogf);
       f = double(wt.v) * F;
       df = double(wt.d) * F + double(wt.v) * F * dlogf * double(E.d);
     }
@@ -688,7 +740,7 @@ int dp_csda_flux_samples_dev(dp_ctx* ctx, const dp_physics* ph, const dp_mc_para
   P.contrib = contrib;
   P.dcontrib = dcontrib;
   P.steps = steps;
-  rc = launch(ctx, P);
+  rc = launch(ctx, P, p->precision == DP_PREC_MIXED ? ph : nullptr);
   if (rc) return rc;
   return check_flag(ctx);
 }
@@ -810,7 +862,7 @@ int dp_backward_mc(dp_ctx* ctx, const dp_physics* ph, const dp_mc_params* p, dp_
   P.emax = p->energy_max > p->energy_min ? p->energy_max : p->energy_min;
   P.contrib = dc;
   P.dcontrib = dd_;
-  rc = launch(ctx, P);
+  rc = launch(ctx, P, p->precision == DP_PREC_MIXED ? ph : nullptr);
   if (rc) return rc;
   reduce3_kernel<<<nb, kRedThreads, 0, ctx->stream>>>(dc, dd_, n, part);
   reduce_parts_kernel<<<1, kRedThreads, 0, ctx->stream>>>(part, nb, sums);

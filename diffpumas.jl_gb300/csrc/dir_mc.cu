@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(T, 1) dir_kernel(const __grid_constant__ DirPa
                             P.C.wait_iters)) {
     if (threadIdx.x == 0) atomicExch(P.err_flag, 1);
     PathGeo<R> geo{P, nullptr};
-    drain_histories<R, PHASE>(geo, P.counter, static_cast<DirHandoff<R>*>(P.queue));
+    drain_histories<R, PHASE>(geo, P.C, P.counter, static_cast<DirHandoff<R>*>(P.queue));
     return;
   }
   Med<R>* meds = reinterpret_cast<Med<R>*>(smem + dir_desc_offset<R>(P));
@@ -504,12 +504,15 @@ int dir_launch_t(dp_ctx* ctx, DirParams& P) {
   const size_t coop_bytes = size_t(threads / 32) * P.coop_stride * sizeof(float);
   int dev_smem = 0;
   DP_CHECK_CUDA(ctx, cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
-  // stage the leading media that fit
+  // stage the leading media that fit (none when the context reads the
+  // tables through L1/L2)
   P.n_staged = 0;
-  for (int k = P.n_media; k >= 0; --k) {
+  const bool stage = ctx->mc_stage[DP_KERNEL_DIR][sizeof(R) == 4] == 0;
+  for (int k = stage ? P.n_media : 0; k >= 0; --k) {
     P.n_staged = k;
     if (dir_coop_offset<R>(P) + coop_bytes <= size_t(dev_smem)) break;
   }
+  P.C.batch = std::max(1, ctx->mc_batch[DP_KERNEL_DIR][sizeof(R) == 4]);
   const size_t smem = dir_coop_offset<R>(P) + coop_bytes;
   if (smem > size_t(dev_smem)) return fail(ctx, DP_ERR_ARG, "too many media for the fixed-path MC kernel");
   const long need = (P.n + threads - 1) / threads;

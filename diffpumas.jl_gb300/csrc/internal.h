@@ -39,6 +39,10 @@ struct dp_ctx {
   // CTA size of the persistent transport kernels per family (DP_KERNEL_MC,
   // DP_KERNEL_DIR) and precision (DP_PREC_FP64, DP_PREC_MIXED); 0: default.
   int mc_threads[2][2] = {{0, 0}, {0, 0}};
+  // Table staging (0: media in shared memory when they fit, 1: read through
+  // L1/L2) and histories a thread takes per refill (0: 1) of the same kernels.
+  int mc_stage[2][2] = {{0, 0}, {0, 0}};
+  int mc_batch[2][2] = {{0, 0}, {0, 0}};
   // Limits lowered for failure-path tests (dp_set_debug_limits); negative:
   // the default (2,000,000 transport steps, 100,000 hard events per mixed
   // step, dp::kStageWait polls of a table-staging wait).

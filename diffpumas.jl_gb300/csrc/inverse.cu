@@ -377,6 +377,81 @@ __global__ void smooth_kernel(const double* x, Dims d, double strength, double l
   }
 }
 
+// ---- MLEM on the model linearised at an iterate (A = -J >= 0, b = f + A rho - obs)
+__global__ void fill_kernel(double* a, long n, double v) {
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
+       i += long(gridDim.x) * blockDim.x)
+    a[i] = v;
+}
+// a = clamp(max(a, floor), lo, hi)
+__global__ void clamp_kernel(double* a, long n, double floor_, double lo, double hi) {
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
+       i += long(gridDim.x) * blockDim.x)
+    a[i] = fmin(fmax(fmax(a[i], floor_), lo), hi);
+}
+// b0 = max(f + A rho - obs, 0) with A rho = -y (y = J rho)
+__global__ void mlem_rhs_kernel(const double* y, const double* f, const double* obs, long n,
+                                double* b0) {
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
+       i += long(gridDim.x) * blockDim.x)
+    b0[i] = fmax(f[i] - y[i] - obs[i], 0.0);
+}
+// ratio = b / max(A rho, 1e-12), b = b0 (fixed linearisation) or max(f + A rho - obs, 0)
+__global__ void mlem_ratio_kernel(const double* y, const double* f, const double* obs,
+                                  const double* b0, long n, double* ratio) {
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
+       i += long(gridDim.x) * blockDim.x) {
+    const double aw = -y[i];
+    const double b = b0 ? b0[i] : fmax(f[i] + aw - obs[i], 0.0);
+    ratio[i] = b / fmax(aw, 1e-12);
+  }
+}
+// rho <- clamp(rho * A^T ratio / (A^T 1 + max(pg, 0)), box), A^T v = -J^T v; a
+// column sum A^T 1 <= 0 counts as 1 (mlem_reconstruct's sens)
+__global__ void mlem_update_kernel(double* rho, const double* jt_ratio, const double* jt_one,
+                                   const double* pg, long n, double lo, double hi) {
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
+       i += long(gridDim.x) * blockDim.x) {
+    double sens = -jt_one[i];
+    if (sens <= 0.0) sens = 1.0;
+    const double den = sens + (pg ? fmax(pg[i], 0.0) : 0.0);
+    rho[i] = fmin(fmax(rho[i] * (-jt_ratio[i]) / den, lo), hi);
+  }
+}
+// ---- gradient descent
+// p = g / max(d, floor) (PGD's preconditioned direction)
+__global__ void precond_kernel(const double* g, const double* d, long n, double floor_, double* p) {
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
+       i += long(gridDim.x) * blockDim.x)
+    p[i] = g[i] / fmax(d[i], floor_);
+}
+// Adam (beta1 0.9, beta2 0.999, eps 1e-8) with bias corrections c1 = 1 - 0.9^t,
+// c2 = 1 - 0.999^t, then the box
+__global__ void adam_kernel(double* w, const double* g, double* m, double* v, long n, double lr,
+                            double c1, double c2, double lo, double hi) {
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
+       i += long(gridDim.x) * blockDim.x) {
+    const double gi = g[i];
+    const double mi = 0.9 * m[i] + (1.0 - 0.9) * gi;
+    const double vi = 0.999 * v[i] + (1.0 - 0.999) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    w[i] = fmin(fmax(w[i] - lr * (mi / c1) / (sqrt(vi / c2) + 1e-8), lo), hi);
+  }
+}
+// out = a - b
+__global__ void sub_kernel(const double* a, const double* b, long n, double* out) {
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
+       i += long(gridDim.x) * blockDim.x)
+    out[i] = a[i] - b[i];
+}
+// out += a
+__global__ void add_kernel(const double* a, long n, double* out) {
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n;
+       i += long(gridDim.x) * blockDim.x)
+    out[i] += a[i];
+}
+
 struct Solver {
   dp_ctx* ctx;
   const dp_physics* ph;
@@ -516,7 +591,8 @@ int dp_tomo_solve_dev(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa,
                       double* rho, const dp_solve_params* sp, double* history) {
   if (!ctx || !ph || !pa || !tp || !obs || !rho || !sp)
     return fail(ctx, DP_ERR_ARG, "null argument");
-  if (sp->n_iter < 0 || (sp->method != DP_SOLVE_SART && sp->method != DP_SOLVE_GN) ||
+  if (sp->n_iter < 0 || sp->method < DP_SOLVE_SART || sp->method > DP_SOLVE_GD ||
+      sp->optimizer < DP_GD_PGD || sp->optimizer > DP_GD_PLAIN ||
       (sp->precision != DP_PREC_FP64 && sp->precision != DP_PREC_MIXED) ||
       !(sp->box_hi > sp->box_lo))
     return fail(ctx, DP_ERR_ARG, "invalid solver parameters");
@@ -584,6 +660,148 @@ int dp_tomo_solve_dev(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa,
                                            ctx->stream));
         ++ctx->launches;
       }
+    }
+  } else if (sp->method == DP_SOLVE_MLEM) {
+    // mlem_reconstruct (src/Tomography_inverse.jl:153-188) with A = -J, b = f + A rho - obs
+    const bool fixed = sp->fixed_linearization != 0;
+    double *ratio = rowsum, *b0 = u, *jt_one = prec, *back = g, *pg = Ap;
+    clamp_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(rho, nc, 1e-6, -1e300, 1e300);
+    ++ctx->launches;
+    for (int it = 0; it < sp->n_iter && !rc; ++it) {
+      if ((rc = S.eval(rho, flux, it == 0 || !fixed))) break;
+      residual_kernel<<<S.grid(nr), kThreads, 0, ctx->stream>>>(flux, obs, nullptr, nr, -1.0, r,
+                                                                 nullptr);
+      ++ctx->launches;
+      S.dot(r, r, nullptr, nr, S.s + 3);
+      record(it, std::sqrt(S.host_scalar(S.s + 3)));
+      if (it == 0 || !fixed) {
+        fill_kernel<<<S.grid(nr), kThreads, 0, ctx->stream>>>(tmp, nr, 1.0);
+        ++ctx->launches;
+        if ((rc = S.transpose(tmp, jt_one))) break;  // J^T 1
+      }
+      if ((rc = S.spmv(rho, nullptr, r))) break;  // y = J rho
+      if (fixed && it == 0) {
+        mlem_rhs_kernel<<<S.grid(nr), kThreads, 0, ctx->stream>>>(r, flux, obs, nr, b0);
+        ++ctx->launches;
+      }
+      mlem_ratio_kernel<<<S.grid(nr), kThreads, 0, ctx->stream>>>(r, flux, obs,
+                                                                  fixed ? b0 : nullptr, nr, ratio);
+      ++ctx->launches;
+      if ((rc = S.transpose(ratio, back))) break;  // J^T ratio
+      if (S.prior > 0.0) {
+        lap_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(rho, S.dims, 2.0 * S.prior, 0, pg);
+        ++ctx->launches;
+      }
+      mlem_update_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(
+          rho, back, jt_one, S.prior > 0.0 ? pg : nullptr, nc, sp->box_lo, sp->box_hi);
+      ++ctx->launches;
+      DP_CHECK_CUDA(ctx, cudaGetLastError());
+    }
+    // the misfit at the last iterate
+    if (!rc && sp->n_iter > 0 && (rc = S.eval(rho, flux, false)) == DP_OK) {
+      residual_kernel<<<S.grid(nr), kThreads, 0, ctx->stream>>>(flux, obs, nullptr, nr, -1.0, r,
+                                                                 nullptr);
+      ++ctx->launches;
+      S.dot(r, r, nullptr, nr, S.s + 3);
+      record(sp->n_iter, std::sqrt(S.host_scalar(S.s + 3)));
+    }
+  } else if (sp->method == DP_SOLVE_GD) {
+    // gradient_descent_reconstruct (src/Tomography_inverse.jl:324-400)
+    const bool fixed = sp->fixed_linearization != 0;
+    const int opt = sp->optimizer;
+    const double lr = sp->lr > 0.0 ? sp->lr : (opt == DP_GD_PGD ? 1.0 : 1e-2);
+    double *f0 = rowsum, *rho0 = x, *m = cr, *v = z, *dir = p, *lp = Ap, *diag = col;
+    clamp_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(rho, nc, -1e300, sp->box_lo,
+                                                           sp->box_hi);
+    ++ctx->launches;
+    rc = S.eval(rho, flux, true);
+    if (!rc && fixed) {
+      DP_CHECK_CUDA(ctx, cudaMemcpyAsync(f0, flux, nr * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+      DP_CHECK_CUDA(ctx, cudaMemcpyAsync(rho0, rho, nc * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    if (opt == DP_GD_ADAM) {
+      DP_CHECK_CUDA(ctx, cudaMemsetAsync(m, 0, nc * 8, ctx->stream));
+      DP_CHECK_CUDA(ctx, cudaMemsetAsync(v, 0, nc * 8, ctx->stream));
+    }
+    double prev = rc ? 0.0 : S.objective(flux, obs, weight, r, rho);
+    if (!rc) {
+      S.dot(r, r, nullptr, nr, S.s + 3);
+      record(0, std::sqrt(S.host_scalar(S.s + 3)));
+    }
+    double c1 = 1.0, c2 = 1.0;
+    for (int t = 1; t <= sp->n_iter && !rc; ++t) {
+      // g = J^T W (pred - obs) + dR/drho
+      residual_kernel<<<S.grid(nr), kThreads, 0, ctx->stream>>>(flux, obs, weight, nr, 1.0, r, u);
+      ++ctx->launches;
+      if ((rc = S.transpose(u, g))) break;
+      if (S.prior > 0.0) {
+        lap_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(rho, S.dims, 2.0 * S.prior, 1, g);
+        ++ctx->launches;
+      }
+      if (opt == DP_GD_PGD) {
+        // Jacobi (Gauss-Newton + prior) preconditioner and the exact step length
+        // of the local quadratic along p = D^-1 g, capped at lr
+        if ((rc = S.colsum(weight, 1, diag))) break;
+        if (S.prior > 0.0) {
+          add_degree_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(S.dims, 2.0 * S.prior, diag);
+          ++ctx->launches;
+        }
+        max_part_kernel<<<kRedBlocks, kThreads, 0, ctx->stream>>>(diag, nc, S.part);
+        ++ctx->launches;
+        std::vector<double> hp(kRedBlocks);
+        DP_CHECK_CUDA(ctx, cudaMemcpyAsync(hp.data(), S.part, kRedBlocks * 8,
+                                           cudaMemcpyDeviceToHost, ctx->stream));
+        DP_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        double dmax = 0.0;
+        for (double hv : hp) dmax = std::max(dmax, hv);
+        if (!(dmax > 0.0)) dmax = 1.0;
+        precond_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(g, diag, nc, 1e-9 * dmax, dir);
+        ++ctx->launches;
+        if ((rc = S.spmv(dir, nullptr, tmp))) break;  // J p
+        S.dot(tmp, tmp, weight, nr, S.s + 3);         // p^T J^T W J p
+        S.dot(g, dir, nullptr, nc, S.s + 4);          // g . p
+        double denom = S.host_scalar(S.s + 3);
+        const double num = S.host_scalar(S.s + 4);
+        if (S.prior > 0.0) {
+          lap_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(dir, S.dims, 2.0 * S.prior, 0, lp);
+          ++ctx->launches;
+          S.dot(dir, lp, nullptr, nc, S.s + 5);
+          denom += S.host_scalar(S.s + 5);
+        }
+        const double alpha =
+            (denom > 0.0 && std::isfinite(num)) ? std::min(std::max(num / denom, 0.0), lr) : 0.0;
+        trial_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(rho, dir, nc, -alpha, sp->box_lo,
+                                                               sp->box_hi, rho);
+        ++ctx->launches;
+      } else if (opt == DP_GD_ADAM) {
+        c1 *= 0.9;
+        c2 *= 0.999;
+        adam_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(rho, g, m, v, nc, lr, 1.0 - c1,
+                                                              1.0 - c2, sp->box_lo, sp->box_hi);
+        ++ctx->launches;
+      } else {
+        trial_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(rho, g, nc, -lr, sp->box_lo,
+                                                               sp->box_hi, rho);
+        ++ctx->launches;
+      }
+      DP_CHECK_CUDA(ctx, cudaGetLastError());
+      // the model at the new iterate: re-evaluated, or f0 + J0 (rho - rho0)
+      if (!fixed) {
+        if ((rc = S.eval(rho, flux, true))) break;
+      } else {
+        sub_kernel<<<S.grid(nc), kThreads, 0, ctx->stream>>>(rho, rho0, nc, lp);
+        ++ctx->launches;
+        if ((rc = S.spmv(lp, nullptr, flux))) break;
+        add_kernel<<<S.grid(nr), kThreads, 0, ctx->stream>>>(f0, nr, flux);
+        ++ctx->launches;
+      }
+      const double obj = S.objective(flux, obs, weight, r, rho);
+      S.dot(r, r, nullptr, nr, S.s + 3);
+      record(t, std::sqrt(S.host_scalar(S.s + 3)));
+      if (opt == DP_GD_PGD &&
+          std::fabs(obj - prev) <= 1e-5 * std::max(std::fabs(prev), 2.220446049250313e-16))
+        break;
+      prev = obj;
     }
   } else {
     double mu = sp->lm_damping > 0.0 ? sp->lm_damping : 1e-3;

@@ -578,10 +578,10 @@ __global__ void __launch_bounds__(T, 1) mc_kernel(const __grid_constant__ McPara
       const Med<R> none{};
       if constexpr (POR) {
         SlabGeoP<R> geo{P, none, none, none};
-        drain_histories<R, PHASE>(geo, P.counter, static_cast<HandoffP<R>*>(P.queue));
+        drain_histories<R, PHASE>(geo, P.C, P.counter, static_cast<HandoffP<R>*>(P.queue));
       } else {
         SlabGeo<R> geo{P, none, none};
-        drain_histories<R, PHASE>(geo, P.counter, static_cast<Handoff<R>*>(P.queue));
+        drain_histories<R, PHASE>(geo, P.C, P.counter, static_cast<Handoff<R>*>(P.queue));
       }
       return;
     }
@@ -797,6 +797,7 @@ int check_cfg(dp_ctx* ctx, const dp_physics* ph, const dp_mc_config* cfg, Consts
   C->step_cap = step_cap(ctx);
   C->event_cap = event_cap(ctx);
   C->wait_iters = stage_wait(ctx);
+  C->batch = 1;
   C->straggling = cfg->straggling != 0;
   C->scattering = cfg->scattering != 0;
   return DP_OK;
@@ -916,7 +917,11 @@ int launch_mc_t(dp_ctx* ctx, McParams& P) {
   size_t tables = size_t(POR ? 3 : 2) * P.lay.med_bytes;
   int dev_smem = 0;
   DP_CHECK_CUDA(ctx, cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
-  P.staged = 16 + tables + coop_bytes <= size_t(dev_smem) ? 1 : 0;
+  P.staged = 16 + tables + coop_bytes <= size_t(dev_smem) &&
+                     ctx->mc_stage[DP_KERNEL_MC][sizeof(R) == 4] == 0
+                 ? 1
+                 : 0;
+  P.C.batch = std::max(1, ctx->mc_batch[DP_KERNEL_MC][sizeof(R) == 4]);
   size_t smem = 16 + (P.staged ? tables : 0) + coop_bytes;
   if (smem > size_t(dev_smem)) return fail(ctx, DP_ERR_ARG, "media too large for the MC kernel");
   long need = (P.n + threads - 1) / threads;
@@ -1003,6 +1008,91 @@ int dp_get_mc_threads(const dp_ctx* ctx, int family, int precision, int* threads
   if (!ctx || !threads || !shape_args(family, precision)) return DP_ERR_ARG;
   const int t = ctx->mc_threads[family][precision];
   *threads = t ? t : (precision == DP_PREC_MIXED ? kThreadsMixed[0] : kThreadsFp64[0]);
+  return DP_OK;
+}
+
+int dp_set_mc_shape(dp_ctx* ctx, int family, int precision, const dp_mc_shape* shape) {
+  if (!ctx || !shape || !shape_args(family, precision))
+    return fail(ctx, DP_ERR_ARG, "bad kernel family, precision or shape");
+  if (shape->staging != 0 && shape->staging != 1)
+    return fail(ctx, DP_ERR_ARG, "staging is 0 (shared memory) or 1 (L1/L2)");
+  if (shape->batch != 0 && shape->batch != 1 && shape->batch != 2 && shape->batch != 4)
+    return fail(ctx, DP_ERR_ARG, "batch is 1, 2 or 4 histories (0: 1)");
+  const int rc = dp_set_mc_threads(ctx, family, precision, shape->threads);
+  if (rc) return rc;
+  ctx->mc_stage[family][precision] = shape->staging;
+  ctx->mc_batch[family][precision] = shape->batch;
+  return DP_OK;
+}
+
+int dp_get_mc_shape(const dp_ctx* ctx, int family, int precision, dp_mc_shape* shape) {
+  if (!ctx || !shape || !shape_args(family, precision)) return DP_ERR_ARG;
+  dp_get_mc_threads(ctx, family, precision, &shape->threads);
+  shape->staging = ctx->mc_stage[family][precision];
+  shape->batch = std::max(1, ctx->mc_batch[family][precision]);
+  return DP_OK;
+}
+
+int dp_autotune_shape(dp_ctx* ctx, int family, int precision, int (*run)(void*), void* user,
+                      dp_mc_shape* best_out, dp_mc_shape* tried, double* ms, int cap,
+                      int* n_tried) {
+  if (!ctx || !run || !shape_args(family, precision))
+    return fail(ctx, DP_ERR_ARG, "bad autotune arguments");
+  dp_mc_shape saved{}, best{};
+  dp_get_mc_shape(ctx, family, precision, &saved);
+  best = saved;
+  DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+    if (a) cudaEventDestroy(a);
+    return fail(ctx, DP_ERR_CUDA, "event creation failed");
+  }
+  int rc = DP_OK, count = 0;
+  float best_ms = -1.0f;
+  // one candidate: run untimed (its code loads), then timed
+  auto trial = [&](const dp_mc_shape& c) -> int {
+    int r = dp_set_mc_shape(ctx, family, precision, &c);
+    if (!r) r = run(user);
+    if (!r && cudaEventRecord(a, ctx->stream) != cudaSuccess)
+      r = fail(ctx, DP_ERR_CUDA, "event record failed");
+    if (!r) r = run(user);
+    if (!r && (cudaEventRecord(b, ctx->stream) != cudaSuccess ||
+               cudaEventSynchronize(b) != cudaSuccess))
+      r = fail(ctx, DP_ERR_CUDA, "event wait failed");
+    if (r) return r;
+    float t = 0.0f;
+    cudaEventElapsedTime(&t, a, b);
+    if (count < cap) {
+      if (tried) tried[count] = c;
+      if (ms) ms[count] = t;
+    }
+    ++count;
+    if (best_ms < 0.0f || t < best_ms) {
+      best_ms = t;
+      best = c;
+    }
+    return DP_OK;
+  };
+  int list[8];
+  const int nt = dp_mc_thread_choices(precision, list, 8);
+  for (int i = 0; i < nt && !rc; ++i) rc = trial(dp_mc_shape{list[i], best.staging, best.batch});
+  const dp_mc_shape after_threads = best;
+  for (int st = 0; st < 2 && !rc; ++st)
+    if (st != after_threads.staging)
+      rc = trial(dp_mc_shape{after_threads.threads, st, after_threads.batch});
+  const dp_mc_shape after_stage = best;
+  for (int bt : {1, 2, 4})
+    if (!rc && bt != after_stage.batch)
+      rc = trial(dp_mc_shape{after_stage.threads, after_stage.staging, bt});
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (n_tried) *n_tried = count;
+  if (rc) {
+    dp_set_mc_shape(ctx, family, precision, &saved);
+    return rc;
+  }
+  dp_set_mc_shape(ctx, family, precision, &best);
+  if (best_out) *best_out = best;
   return DP_OK;
 }
 

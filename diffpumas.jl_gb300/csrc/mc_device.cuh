@@ -134,6 +134,7 @@ struct Consts {
   int straggling, scattering;
   // loop caps and the table-staging wait limit of the launch
   int step_cap, event_cap, wait_iters;
+  int batch;  // histories a thread takes from the work counter at a time (>= 1)
   // physics constants in the transport precision
   template <class R> __device__ __forceinline__ R mass_r() const {
     return sizeof(R) == 8 ? R(mass) : R(mass_f);

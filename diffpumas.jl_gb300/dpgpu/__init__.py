@@ -104,6 +104,56 @@ def set_debug_limits(ctx, step_cap=None, event_cap=None, wait_iters=None):
     check(load().dp_set_debug_limits(h, v(step_cap), v(event_cap), v(wait_iters)), h)
 
 
+def set_mc_shape(ctx, family, precision, threads=0, staging=0, batch=1):
+    """dp_set_mc_shape: CTA size (0: default), table staging (0: shared
+    memory when the media fit, 1: read through L1/L2) and histories a thread
+    takes per refill (1, 2 or 4) of the persistent transport kernels."""
+    from ._lib import DpMcShape
+    h = _ctx_of(ctx)
+    sh = DpMcShape(int(threads), int(staging), int(batch))
+    check(load().dp_set_mc_shape(h, _FAMILY[family], _PRECISION[precision], C.byref(sh)), h)
+
+
+def get_mc_shape(ctx, family, precision):
+    from ._lib import DpMcShape
+    h = _ctx_of(ctx)
+    sh = DpMcShape()
+    check(load().dp_get_mc_shape(h, _FAMILY[family], _PRECISION[precision], C.byref(sh)), h)
+    return {"threads": sh.threads, "staging": sh.staging, "batch": sh.batch}
+
+
+def autotune_shape(ctx, family, precision, run):
+    """dp_autotune_shape: CTA size, then table staging, then refill batch,
+    each chosen by timing run() (the caller's workload on this context) once
+    untimed and once timed per candidate.  Keeps the best on the context and
+    returns (best shape, [(shape, ms), ...])."""
+    from ._lib import DpMcShape
+    h = _ctx_of(ctx)
+    lib = load()
+    errors = []
+
+    def cb(_user):
+        try:
+            run()
+            return 0
+        except Exception as e:  # reported after dp_autotune_shape returns
+            errors.append(e)
+            return _lib.DP_ERR_STATE
+
+    fn = _lib.AUTOTUNE_RUN(cb)
+    best = DpMcShape()
+    tried = (DpMcShape * 16)()
+    ms = (C.c_double * 16)()
+    n = C.c_int()
+    rc = lib.dp_autotune_shape(h, _FAMILY[family], _PRECISION[precision], fn, None,
+                               C.byref(best), tried, C.cast(ms, C.c_void_p), 16, C.byref(n))
+    if errors:
+        raise errors[0]
+    check(rc, h)
+    as_dict = lambda s: {"threads": s.threads, "staging": s.staging, "batch": s.batch}
+    return as_dict(best), [(as_dict(tried[i]), ms[i]) for i in range(min(n.value, 16))]
+
+
 def get_mc_threads(ctx, family, precision):
     h = _ctx_of(ctx)
     t = C.c_int()
@@ -408,14 +458,17 @@ def mc_samples(physics, *, energy_min=1.0, energy_max=None, n_samples=10000, see
 
 def csda_flux_samples(physics, energy, charge, weight, *, rock_thickness, rock_density,
                       elevation, source_energy_max=None, primary_altitude=PRIMARY_ALTITUDE,
-                      energy_threshold_low=100.0, steps=False):
-    """Per-history w*flux and w*d flux/d rho of the deterministic CSDA surrogate."""
+                      energy_threshold_low=100.0, steps=False, precision="fp64"):
+    """Per-history w*flux and w*d flux/d rho of the deterministic CSDA surrogate
+    ("fp64": the reference's operations; "mixed": the FP32 walk with float-pair
+    range and altitude, final energy and flux in FP64)."""
     E, q, w = _f64(energy), _f64(charge), _f64(weight)
     n = len(E)
     c, d = np.zeros(n), np.zeros(n)
     st = np.zeros(n, np.int32) if steps else None
     p = _mc_params(physics, rock_thickness, rock_density, elevation, 1.0, None, n, True, 0,
-                   False, False, energy_threshold_low, source_energy_max, primary_altitude)
+                   False, False, energy_threshold_low, source_energy_max, primary_altitude,
+                   precision)
     check(load().dp_csda_flux_samples(physics.ctx.h, physics.h, C.byref(p), n, _ptr(E), _ptr(q),
                                       _ptr(w), _ptr(c), _ptr(d),
                                       _ptr(st) if st is not None else None), physics.ctx.h)
@@ -819,18 +872,25 @@ class TomoPaths:
 
     def solve(self, obs, rho0, *, method="gn", n_iter=12, weight=None, cg_iter=10,
               relaxation=0.2, lm_damping=1e-3, box=(500.0, 3500.0), precision="mixed",
-              prior_weight=0.0, smooth_strength=0.1, speculation=True):
+              prior_weight=0.0, smooth_strength=0.1, speculation=True, optimizer="pgd",
+              relinearize=True, lr=None):
         """Inversion loop on the device (src/Tomography_inverse.jl): "sart"
-        (sart_reconstruct, Jacobian re-evaluated per iterate) or "gn"
-        (gauss_newton_reconstruct with matrix-free CG).  obs, weight and rho0
-        are float64 CUDA tensors; returns (rho, misfit history)."""
+        (sart_reconstruct, Jacobian re-evaluated per iterate), "gn"
+        (gauss_newton_reconstruct with matrix-free CG), "mlem" (mlem_reconstruct
+        on the model linearised at the iterate, A = -J) or "gd"
+        (gradient_descent_reconstruct, optimizer "pgd", "adam" or "gd").
+        relinearize=False linearises MLEM and GD once at rho0.  obs, weight and
+        rho0 are float64 CUDA tensors; returns (rho, misfit history; NaN past
+        an early stop)."""
         import torch
         from ._lib import DpSolveParams
         rho = rho0.clone()
-        sp = DpSolveParams({"sart": 0, "gn": 1}[method], int(n_iter), int(cg_iter),
-                           PRECISION[precision], float(relaxation), float(lm_damping),
-                           float(box[0]), float(box[1]), float(prior_weight),
-                           float(smooth_strength), 0 if speculation else 1)
+        sp = DpSolveParams({"sart": 0, "gn": 1, "mlem": 2, "gd": 3}[method], int(n_iter),
+                           int(cg_iter), PRECISION[precision], float(relaxation),
+                           float(lm_damping), float(box[0]), float(box[1]), float(prior_weight),
+                           float(smooth_strength), 0 if speculation else 1,
+                           {"pgd": 0, "adam": 1, "gd": 2}[optimizer], 0 if relinearize else 1,
+                           float(lr) if lr is not None else 0.0)
         hist = np.zeros(n_iter + 1)
         torch.cuda.synchronize(self.dev)
         check(load().dp_tomo_solve_dev(self.physics.ctx.h, self.physics.h, self.h,

@@ -120,11 +120,16 @@ class DpTetraMesh(C.Structure):
                 ("tets", C.c_void_p)]
 
 
+class DpMcShape(C.Structure):
+    _fields_ = [("threads", C.c_int), ("staging", C.c_int), ("batch", C.c_int)]
+
+
 class DpSolveParams(C.Structure):
     _fields_ = [("method", C.c_int), ("n_iter", C.c_int), ("cg_iter", C.c_int),
                 ("precision", C.c_int), ("relaxation", C.c_double), ("lm_damping", C.c_double),
                 ("box_lo", C.c_double), ("box_hi", C.c_double), ("prior_weight", C.c_double),
-                ("smooth_strength", C.c_double), ("no_speculation", C.c_int)]
+                ("smooth_strength", C.c_double), ("no_speculation", C.c_int),
+                ("optimizer", C.c_int), ("fixed_linearization", C.c_int), ("lr", C.c_double)]
 
 
 class DpGrid(C.Structure):
@@ -174,6 +179,10 @@ PROTOTYPES = {
     "dp_set_mc_threads": (_I, [_P, _I, _I, _I]),
     "dp_get_mc_threads": (_I, [_P, _I, _I, C.POINTER(_I)]),
     "dp_autotune": (_I, [_P, _I, _I, AUTOTUNE_RUN, _VP, C.POINTER(_I), _VP, _I]),
+    "dp_set_mc_shape": (_I, [_P, _I, _I, C.POINTER(DpMcShape)]),
+    "dp_get_mc_shape": (_I, [_P, _I, _I, C.POINTER(DpMcShape)]),
+    "dp_autotune_shape": (_I, [_P, _I, _I, AUTOTUNE_RUN, _VP, C.POINTER(DpMcShape),
+                               C.POINTER(DpMcShape), _VP, _I, C.POINTER(_I)]),
     "dp_physics_upload": (_I, [_P, C.POINTER(DpSettings), _I, _I, _VP, _VP, C.POINTER(_P)]),
     "dp_physics_create": (_I, [_P, C.POINTER(DpSettings), _I, _VP, _I, _D, _D, C.POINTER(_P)]),
     "dp_physics_create_dedx": (_I, [_P, C.POINTER(DpSettings), _I, _VP, _VP, C.POINTER(_P)]),

@@ -125,6 +125,23 @@ int dp_get_mc_threads(const dp_ctx* ctx, int family, int precision, int* threads
  * from run ends the search, restores the previous size and is returned. */
 int dp_autotune(dp_ctx* ctx, int family, int precision, int (*run)(void* user), void* user,
                 int* best_threads, double* ms, int cap);
+/* The full launch shape of those kernels: the CTA size, where the media
+ * tables live (staging 0: copied to shared memory once per CTA when they fit,
+ * the default; 1: read through L1/L2) and how many consecutive histories a
+ * thread takes from the work counter at a time (batch 1, 2 or 4; 0: 1).  No
+ * choice changes a result: every history keeps its own stream. */
+typedef struct {
+  int threads, staging, batch;
+} dp_mc_shape;
+int dp_set_mc_shape(dp_ctx* ctx, int family, int precision, const dp_mc_shape* shape);
+int dp_get_mc_shape(const dp_ctx* ctx, int family, int precision, dp_mc_shape* shape);
+/* dp_autotune over the whole shape, one dimension at a time (CTA size, then
+ * staging, then batch, each from the best so far): every candidate runs
+ * run(user) once untimed and once timed.  The best shape stays on the context
+ * and goes to *best; tried[i] / ms[i] list the candidates and their times (up
+ * to cap), *n_tried their count. */
+int dp_autotune_shape(dp_ctx* ctx, int family, int precision, int (*run)(void* user), void* user,
+                      dp_mc_shape* best, dp_mc_shape* tried, double* ms, int cap, int* n_tried);
 
 /* ------------------------------------------------------------------ physics tables
  * Column layout of one material table (src/Physics.jl:64-102 MaterialTable).
@@ -241,8 +258,12 @@ typedef struct {
   double primary_altitude;   /* m (3e4) */
   int rock_material;         /* -1: "StandardRock" or 0 */
   int air_material;          /* -1: "Air" or the last table */
-  int precision;             /* stochastic transport: DP_PREC_FP64 (0) or
-                                DP_PREC_MIXED (1); the CSDA path is FP64 */
+  int precision;             /* DP_PREC_FP64 (0): the reference's FP64
+                                operations; DP_PREC_MIXED (1): FP32 stochastic
+                                transport, and CSDA histories walked in FP32
+                                with float-pair range and altitude, the final
+                                energy and the flux in FP64 (within ~1e-6 of
+                                FP64 per history) */
   /* Shallow porous layer of TwoLayerGeometry (src/Geometry.jl:47-72,
    * compute_flux's porous_* keywords, :899): the top porous_thickness m of
    * the rock column are material porous_material at porous_density.  Active
@@ -275,7 +296,8 @@ int dp_backward_mc(dp_ctx* ctx, const dp_physics* phys, const dp_mc_params* p,
 
 /* Deterministic CSDA flux of explicit histories (compute_flux_differentiable,
  * src/Geometry.jl:958-986, and its Zygote gradient :1007-1028): contrib[i] =
- * w[i]*flux_i and dcontrib[i] = w[i]*d flux_i/d rho.  Host pointers. */
+ * w[i]*flux_i and dcontrib[i] = w[i]*d flux_i/d rho, in p->precision.  Host
+ * pointers. */
 int dp_csda_flux_samples(dp_ctx* ctx, const dp_physics* phys, const dp_mc_params* p,
                          long n, const double* energy, const double* charge,
                          const double* weight, double* contrib, double* dcontrib,
@@ -701,13 +723,35 @@ int dp_tomo_forward_plain_dev(dp_ctx* ctx, const dp_physics* phys, const dp_grid
  *   DP_SOLVE_GN    Gauss-Newton / Levenberg-Marquardt on 0.5 sum_i W_i (f_i - obs_i)^2
  *                  (gauss_newton_reconstruct, :448-603, legacy acceptance), the
  *                  damped normal equations solved matrix-free by preconditioned
- *                  conjugate gradients on the device (no dense J^T W J).
- * No reference entry point takes this exact form: it replaces the solver loops
+ *                  conjugate gradients on the device (no dense J^T W J);
+ *   DP_SOLVE_MLEM  mlem_reconstruct (:153-188) on the model linearised at the
+ *                  iterate: with A = -J (the density lowers the flux, so A >= 0)
+ *                  and b = max(f(rho_k) + A rho_k - obs, 0) (obs = f(rho) is
+ *                  then A rho = b), rho <- clamp(rho * A^T (b / max(A rho, 1e-12))
+ *                  / (A^T 1 + max(dR/drho, 0)), box), zero column sums counting
+ *                  as 1, the start lifted to at least 1e-6.  The multiplicative
+ *                  step solves the linearised problem: it need not lower the
+ *                  flux misfit of the nonlinear model;
+ *   DP_SOLVE_GD    gradient_descent_reconstruct (:324-400) with its optimizers:
+ *                  g = J^T W (f - obs) + dR/drho; PGD scales g by the
+ *                  Gauss-Newton + prior diagonal and takes the exact step of the
+ *                  local quadratic along it, capped at lr, and stops when the
+ *                  objective changes by at most 1e-5 of itself; Adam (0.9,
+ *                  0.999, 1e-8) and plain steps of lr otherwise.
+ * MLEM and GD re-evaluate f and J at every iterate, or with fixed_linearization
+ * use f0 + J0 (rho - rho0) (the reference's relinearize = false; MLEM's fixed
+ * A, b).  history[k] is the flux misfit ||f(rho_k) - obs|| at iterate k.  No
+ * reference entry point takes this exact form: it replaces the solver loops
  * around make_csda_operator (:614-626) for the voxel-density model. */
 #define DP_SOLVE_SART 0
 #define DP_SOLVE_GN 1
+#define DP_SOLVE_MLEM 2
+#define DP_SOLVE_GD 3
+#define DP_GD_PGD 0      /* diagonally preconditioned projected gradient, exact step */
+#define DP_GD_ADAM 1
+#define DP_GD_PLAIN 2    /* w <- clamp(w - lr g, box) */
 typedef struct {
-  int method;            /* DP_SOLVE_SART or DP_SOLVE_GN */
+  int method;            /* DP_SOLVE_SART, DP_SOLVE_GN, DP_SOLVE_MLEM or DP_SOLVE_GD */
   int n_iter;            /* outer iterations */
   int cg_iter;           /* GN: conjugate-gradient iterations per solve (<= 0: 10) */
   int precision;         /* forward model: DP_PREC_FP64 or DP_PREC_MIXED */
@@ -724,6 +768,11 @@ typedef struct {
                              keep being accepted (the accepted trial's Jacobian is
                              the next iteration's); 1 never does.  The iterates
                              are the same either way. */
+  int optimizer;          /* GD: DP_GD_PGD (default), DP_GD_ADAM or DP_GD_PLAIN */
+  int fixed_linearization; /* MLEM, GD: 0 re-evaluates f and J at every iterate
+                              (relinearize = true); 1 linearises once at the start,
+                              f(rho) ~ f0 + J0 (rho - rho0) (relinearize = false) */
+  double lr;              /* GD: step (PGD: step-length cap); <= 0: 1 for PGD, 1e-2 else */
 } dp_solve_params;
 /* obs: n_rays observed fluxes, weight: n_rays data weights (NULL: 1), rho:
  * the start density in, the estimate out (all device pointers; node arrays of

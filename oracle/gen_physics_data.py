@@ -14,7 +14,7 @@ Sources (reference project paths):
   src/Straggling.jl       NUCLEAR_RMS_RADII
   src/Coulomb.jl          SALVAT_PREFACTOR, SALVAT_EXPONENT, NUCLEAR_RADII
 
-Usage: python oracle/gen_physics_data.py /root/reference
+Usage: python oracle/gen_physics_data.py <path of the reference checkout>
 Writes oracle/physics_data.inc and diffpumas.jl_gb300/csrc/physics_data.inc
 (two copies: the oracle never includes product files and vice versa).
 """
@@ -119,4 +119,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {sys.argv[0]} <path of the reference checkout>")
+    main(sys.argv[1])

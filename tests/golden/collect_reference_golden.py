@@ -1,7 +1,7 @@
 """Copies the reference's own golden data for the hot path into tests/golden/.
 
 Run once in a checkout that has the reference project (read-only) available:
-    python tests/golden/collect_reference_golden.py /root/reference
+    python tests/golden/collect_reference_golden.py <path of the reference checkout>
 
 Files (paths inside the reference project):
   test/data/pumas_radiative_moments.csv
@@ -40,4 +40,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {sys.argv[0]} <path of the reference checkout>")
+    main(sys.argv[1])

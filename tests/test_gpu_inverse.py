@@ -174,3 +174,121 @@ def test_gn_speculation_gives_the_same_iterates(dp, problem):
     np.testing.assert_array_equal(h_on, h_off)
     np.testing.assert_array_equal(r_on.cpu().numpy(), r_off.cpu().numpy())
     assert np.isfinite(h_on[0]) and np.nanmin(h_on[1:]) < h_on[0]
+
+
+def _laplacian_dense(nx, ny, nz):
+    n = nx * ny * nz
+    L = np.zeros((n, n))
+    idx = np.arange(n).reshape(nz, ny, nx)
+    for a in range(3):
+        lo, hi = [slice(None)] * 3, [slice(None)] * 3
+        lo[a], hi[a] = slice(0, -1), slice(1, None)
+        for i, j in zip(idx[tuple(lo)].ravel(), idx[tuple(hi)].ravel()):
+            L[i, j] -= 1
+            L[j, i] -= 1
+            L[i, i] += 1
+            L[j, j] += 1
+    return L
+
+
+@pytest.mark.parametrize("relinearize", [True, False])
+def test_mlem_iterations_match_numpy(dp, problem, relinearize):
+    """mlem_reconstruct (src/Tomography_inverse.jl:153-188) on the model
+    linearised at the iterate (A = -J >= 0, b = max(f + A rho - obs, 0)), or
+    once at the start: rho <- clamp(rho * A^T (b / max(A rho, 1e-12)) /
+    (A^T 1 + max(2 lambda L rho, 0)), box), three iterations, FP64, against
+    the same update in numpy on the product's Jacobian."""
+    paths, T = problem["paths"], problem["T"]
+    g = paths.grid
+    n = g.ncell
+    rho0 = np.full(n, 2650.0)
+    obs = problem["obs"].cpu().numpy()
+    prior, box = 1e-6, (500.0, 3500.0)
+    rho_d, hist = paths.solve(problem["obs"], T(rho0), method="mlem", n_iter=3, box=box,
+                              precision="fp64", prior_weight=prior, relinearize=relinearize)
+    L = _laplacian_dense(g.nx, g.ny, g.nz)
+    rho = np.maximum(rho0, 1e-6)
+    f0, J0 = _jacobian(paths, T(rho))
+    b0 = np.maximum(f0 - J0 @ rho - obs, 0.0)
+    for it in range(3):
+        f, J = (f0, J0) if (it == 0 or not relinearize) else _jacobian(paths, T(rho))
+        if it > 0 and not relinearize:
+            f = paths.eval(T(rho), precision="fp64")[0].cpu().numpy()
+        assert hist[it] == pytest.approx(np.linalg.norm(obs - f), rel=1e-10)
+        A = -J
+        Aw = A @ rho
+        b = b0 if not relinearize else np.maximum(f + Aw - obs, 0.0)
+        sens = A.T @ np.ones(len(obs))
+        sens[sens <= 0] = 1.0
+        den = sens + np.maximum(2 * prior * (L @ rho), 0.0)
+        rho = np.clip(rho * (A.T @ (b / np.maximum(Aw, 1e-12))) / den, *box)
+    np.testing.assert_allclose(rho_d.cpu().numpy(), rho, rtol=1e-9, atol=1e-6)
+    f_final = paths.eval(T(rho), precision="fp64")[0].cpu().numpy()
+    assert hist[3] == pytest.approx(np.linalg.norm(obs - f_final), rel=1e-9)
+    # the multiplicative step solves the linearised problem, not the flux
+    # model, so it need not lower the flux misfit; only its bounds hold
+    assert rho_d.min().item() >= box[0] and rho_d.max().item() <= box[1]
+
+
+@pytest.mark.parametrize("optimizer,relinearize", [("pgd", True), ("pgd", False),
+                                                   ("adam", True), ("gd", True)])
+def test_gradient_descent_iterations_match_numpy(dp, problem, optimizer, relinearize):
+    """gradient_descent_reconstruct (src/Tomography_inverse.jl:324-400) on
+    0.5 sum W (f - obs)^2 + lambda sum_edges (rho_i - rho_j)^2: PGD (Jacobi
+    preconditioner of the Gauss-Newton + prior diagonal, exact step capped at
+    lr), Adam and plain steps, relinearised or with the start's linear model;
+    four iterations, FP64, against the same loop in numpy."""
+    paths, T = problem["paths"], problem["T"]
+    g = paths.grid
+    n = g.ncell
+    rho0 = np.full(n, 2650.0)
+    obs = problem["obs"].cpu().numpy()
+    W = 1.0 / np.maximum(obs, 1e-30) ** 2
+    prior, box = 1e-7, (500.0, 3500.0)
+    lr = {"pgd": 1.0, "adam": 5.0, "gd": 1e-3}[optimizer]
+    rho_d, hist = paths.solve(problem["obs"], T(rho0), method="gd", n_iter=4, weight=T(W),
+                              box=box, precision="fp64", prior_weight=prior, optimizer=optimizer,
+                              relinearize=relinearize, lr=lr)
+    L = _laplacian_dense(g.nx, g.ny, g.nz)
+    deg = np.diag(L)
+    w = np.clip(rho0, *box)
+    pred, J = _jacobian(paths, T(w))
+    f0, J0, w0 = pred.copy(), J.copy(), w.copy()
+    obj = lambda pr, x: 0.5 * np.sum(W * (pr - obs) ** 2) + prior * (x @ (L @ x))
+    prev = obj(pred, w)
+    m, v = np.zeros(n), np.zeros(n)
+    ref_hist = [np.linalg.norm(pred - obs)]
+    for t in range(1, 5):
+        gr = J.T @ (W * (pred - obs)) + 2 * prior * (L @ w)
+        if optimizer == "pgd":
+            d = (W[:, None] * J * J).sum(0) + 2 * prior * deg
+            dmax = d.max() if d.max() > 0 else 1.0
+            p = gr / np.maximum(d, 1e-9 * dmax)
+            Jp = J @ p
+            denom = Jp @ (W * Jp) + p @ (2 * prior * (L @ p))
+            num = gr @ p
+            a = min(max(num / denom, 0.0), lr) if denom > 0 and np.isfinite(num) else 0.0
+            w = np.clip(w - a * p, *box)
+        elif optimizer == "adam":
+            m = 0.9 * m + 0.1 * gr
+            v = 0.999 * v + 0.001 * gr * gr
+            w = np.clip(w - lr * (m / (1 - 0.9 ** t)) / (np.sqrt(v / (1 - 0.999 ** t)) + 1e-8),
+                        *box)
+        else:
+            w = np.clip(w - lr * gr, *box)
+        if relinearize:
+            pred, J = _jacobian(paths, T(w))
+        else:
+            pred = f0 + J0 @ (w - w0)
+        ref_hist.append(np.linalg.norm(pred - obs))
+        o = obj(pred, w)
+        if optimizer == "pgd" and abs(o - prev) <= 1e-5 * max(abs(prev), 2.2e-16):
+            break
+        prev = o
+    np.testing.assert_allclose(rho_d.cpu().numpy(), w, rtol=1e-9, atol=1e-6)
+    k = len(ref_hist)
+    np.testing.assert_allclose(hist[:k], ref_hist, rtol=1e-9)
+    assert np.isnan(hist[k:]).all()
+    if optimizer == "pgd" and relinearize:
+        f_final = paths.eval(T(w), precision="fp64")[0].cpu().numpy()
+        assert np.linalg.norm(obs - f_final) < ref_hist[0]

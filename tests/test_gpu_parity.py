@@ -102,6 +102,51 @@ def test_run_backward_mc_csda_estimator(dp, phys, oracle, orc_default):
     assert r2 == r
 
 
+@pytest.mark.parametrize("geo,erange", [
+    ((100.0, 2650.0, 45.0), (1.0, 100.0)),
+    ((3.0, 2650.0, 45.0), (0.01, 1e5)),
+    ((1000.0, 2500.0, 80.0), (1.0, 1e4)),
+    ((20.0, 2000.0, 10.0), (0.1, 1e3)),
+])
+def test_mixed_csda_histories_within_1e6_of_oracle(dp, phys, oracle, orc_default, geo, erange):
+    """The FP32 CSDA walk (range, its density tangent and the altitude as
+    float pairs; the start offset, the final energy and the flux in FP64)
+    against the FP64 oracle on the same histories: every history's flux and
+    d flux / d rho within 2e-6 (the derivative, or 1e-6 of the batch's
+    largest), the sample-average flux and gradient within 1e-6 (the
+    deterministic-CSDA tolerance of the FP64 mode)."""
+    t, rho, el = geo
+    E, q, w = dp.mc_samples(phys, energy_min=erange[0], energy_max=erange[1], n_samples=4096,
+                            seed=11)
+    c, d, steps = dp.csda_flux_samples(phys, E, q, w, steps=True, precision="mixed",
+                                       rock_thickness=t, rock_density=rho, elevation=el)
+    oc, od = oracle.backward_mc_csda(orc_default, 0, 1, t, rho, el, E, q, w)
+    assert (oc > 0).sum() > 100
+    np.testing.assert_allclose(c, oc, rtol=2e-6, atol=1e-12 * oc.max())
+    # a history's derivative sums terms of both signs (energy loss against
+    # decay): where they cancel, its error is measured against the batch's
+    # largest derivative
+    np.testing.assert_allclose(d, od, rtol=2e-6, atol=1e-6 * np.abs(od).max())
+    assert c.sum() == pytest.approx(oc.sum(), rel=1e-6)
+    assert d.sum() == pytest.approx(od.sum(), rel=1e-6)
+
+
+def test_run_backward_mc_csda_mixed(dp, phys, oracle, orc_default):
+    """run_backward_mc in the mixed mode on the C1 configuration (10^4
+    histories, E 1-100 GeV, with the gradient): flux, sigma and the gradient
+    within 1e-6 of the FP64 oracle over the same histories."""
+    n = 10000
+    r = dp.run_backward_mc(phys, energy_min=1.0, energy_max=100.0, n_samples=n,
+                           compute_gradient=True, seed=42, straggling=False, scattering=False,
+                           precision="mixed", **C1)
+    E, q, w = dp.mc_samples(phys, energy_min=1.0, energy_max=100.0, n_samples=n, seed=42)
+    oc, od = oracle.backward_mc_csda(orc_default, 0, 1, 100.0, 2650.0, 45.0, E, q, w)
+    f = oc.sum() / n
+    assert r.flux == pytest.approx(f, rel=1e-6)
+    assert r.gradient == pytest.approx(od.sum() / n, rel=1e-6)
+    assert r.sigma == pytest.approx(np.sqrt(max((oc ** 2).sum() / n - f * f, 0) / n), rel=1e-6)
+
+
 def test_gradient_vs_central_difference(dp, phys):
     """test/test_geometry_ad.jl:39-54: adaptive-loop derivative vs central FD."""
     for energy, thickness in ((10.0, 10.0), (120.0, 3.0), (3.0, 100.0)):
