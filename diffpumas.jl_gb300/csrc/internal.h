@@ -43,6 +43,8 @@ struct dp_ctx {
   // L1/L2) and histories a thread takes per refill (0: 1) of the same kernels.
   int mc_stage[2][2] = {{0, 0}, {0, 0}};
   int mc_batch[2][2] = {{0, 0}, {0, 0}};
+  // Hand-out order of the histories (0: longest first, 1: index order).
+  int mc_order[2][2] = {{0, 0}, {0, 0}};
   // Limits lowered for failure-path tests (dp_set_debug_limits); negative:
   // the default (2,000,000 transport steps, 100,000 hard events per mixed
   // step, dp::kStageWait polls of a table-staging wait).

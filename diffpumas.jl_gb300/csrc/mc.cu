@@ -374,6 +374,42 @@ struct McParams {
   void* start;                // StartRec<R> x n
   void* end;                  // EndRec<R> x n
   void* porous_rec;           // PorousRec<R> x n when porous
+  // longest-first schedule (null: counter order): per history the cost
+  // buckets of its phase-0 and phase-1 work, the hand-out orders (history
+  // indices, queue slots) and 2 x kSchedBuckets words of counting-sort scratch
+  uint16_t *key0, *key1;
+  uint32_t *order0, *order1, *sched;
+};
+
+// Cost buckets of a history for the longest-first schedule.  Phase 0 (below
+// the mode switch): its step count follows log(1 + G / X0), G the rock
+// grammage along the direction and X0 the CSDA range at the start energy
+// (the step limits are a fixed fraction of the range), 64 buckets per unit.
+// Phase 1 (mixed steps from hard event to hard event): it follows the rock
+// grammage left above the switch, log(1 + G1 / 1e4 kg/m^2), 128 buckets per
+// unit.  A history above the switch at the start costs phase 0 nothing.
+template <class R>
+__device__ __forceinline__ void cost_buckets(const Med<R>& rock, const Consts& C, double E0,
+                                             double thick, double rho, double uz, uint16_t* k0,
+                                             uint16_t* k1) {
+  const double G = thick * rho / fmax(fabs(uz), 0.05);
+  const double X0 = double(at(rock, locate(rock, R(E0)), MC_CR));
+  const double Xs = double(at(rock, locate(rock, R(C.thr_low)), MC_CR));
+  const double G1 = fmax(G - fmax(Xs - X0, 0.0), 0.0);
+  const double c0 = E0 < C.thr_low ? log1p(G / fmax(X0, 1e-3)) * 64.0 : 0.0;
+  const double c1 = log1p(G1 * 1e-4) * 128.0;
+  *k0 = uint16_t(fmin(c0, double(kSchedBuckets - 1)));
+  *k1 = uint16_t(fmin(c1, double(kSchedBuckets - 1)));
+}
+struct KeyOf {
+  const uint16_t* key;
+  __device__ int operator()(long s) const { return key[s]; }
+};
+template <class Q>
+struct QueueKeyOf {
+  const Q* queue;
+  const uint16_t* key;
+  __device__ int operator()(long s) const { return key[queue[s].index]; }
 };
 
 // Start record of history i: energy, charge and weight drawn as
@@ -430,6 +466,10 @@ __global__ void __launch_bounds__(256) mc_init_kernel(const __grid_constant__ Mc
       static_cast<PorousRec<R>*>(P.porous_rec)[i] = pr;
     }
     double theta = (90.0 - elev) * kPi / 180.0;
+    if (P.key0) {
+      const Med<R> rock = make_med<R>(P.blob, P.lay, P.info[0]);
+      cost_buckets<R>(rock, P.C, E0, thick, rho, cos(theta), P.key0 + i, P.key1 + i);
+    }
     StartRec<R> r;
     r.thick = alt_make<R>(thick);
     r.H = alt_make<R>(H);
@@ -578,10 +618,12 @@ __global__ void __launch_bounds__(T, 1) mc_kernel(const __grid_constant__ McPara
       const Med<R> none{};
       if constexpr (POR) {
         SlabGeoP<R> geo{P, none, none, none};
-        drain_histories<R, PHASE>(geo, P.C, P.counter, static_cast<HandoffP<R>*>(P.queue));
+        drain_histories<R, PHASE>(geo, P.C, P.counter, static_cast<HandoffP<R>*>(P.queue),
+                                  PHASE == 0 ? P.order0 : P.order1);
       } else {
         SlabGeo<R> geo{P, none, none};
-        drain_histories<R, PHASE>(geo, P.C, P.counter, static_cast<Handoff<R>*>(P.queue));
+        drain_histories<R, PHASE>(geo, P.C, P.counter, static_cast<Handoff<R>*>(P.queue),
+                                  PHASE == 0 ? P.order0 : P.order1);
       }
       return;
     }
@@ -595,12 +637,14 @@ __global__ void __launch_bounds__(T, 1) mc_kernel(const __grid_constant__ McPara
     SlabGeoP<R> geo{P, rock, air, porous};
     transport_histories<R, PHASE, KCfg<R>::coop>(geo, P.C, P.counter,
                                                  static_cast<HandoffP<R>*>(P.queue), item,
-                                                 item + kItemsPerElement * P.coop_nel);
+                                                 item + kItemsPerElement * P.coop_nel,
+                                                 PHASE == 0 ? P.order0 : P.order1);
   } else {
     SlabGeo<R> geo{P, rock, air};
     transport_histories<R, PHASE, KCfg<R>::coop>(geo, P.C, P.counter,
                                                  static_cast<Handoff<R>*>(P.queue), item,
-                                                 item + kItemsPerElement * P.coop_nel);
+                                                 item + kItemsPerElement * P.coop_nel,
+                                                 PHASE == 0 ? P.order0 : P.order1);
   }
 }
 
@@ -760,6 +804,23 @@ namespace {
 // Per-history device records of a run (hand-off, start, end), sized for FP64.
 constexpr size_t kRecBytes = sizeof(HandoffP<double>) + sizeof(StartRec<double>) +
                              sizeof(EndRec<double>) + sizeof(PorousRec<double>) + 64;
+// The longest-first schedule: two cost buckets and two order entries per
+// history, and the counting-sort words (kSchedExtra covers those and the
+// arena's alignment of the five arrays).
+constexpr size_t kSchedBytes = 2 * sizeof(uint16_t) + 2 * sizeof(uint32_t);
+constexpr size_t kSchedExtra = 2 * kSchedBuckets * sizeof(uint32_t) + 5 * 256;
+
+// Takes the schedule's arrays from the arena when the context hands
+// histories out longest first (and the indices fit 32 bits).
+void take_sched(dp_ctx* ctx, int precision, long n, Arena& A, McParams& P) {
+  if (ctx->mc_order[DP_KERNEL_MC][precision] != 0 || n >= (1L << 32)) return;
+  P.key0 = A.take<uint16_t>(n);
+  P.key1 = A.take<uint16_t>(n);
+  P.order0 = A.take<uint32_t>(n);
+  P.order1 = A.take<uint32_t>(n);
+  P.sched = A.take<uint32_t>(2 * kSchedBuckets);
+  if (!P.sched) P.key0 = P.key1 = nullptr, P.order0 = P.order1 = P.sched = nullptr;
+}
 
 }  // namespace
 
@@ -931,8 +992,25 @@ int launch_mc_t(dp_ctx* ctx, McParams& P) {
   mc_init_kernel<R><<<int(rec_blocks), 256, 0, ctx->stream>>>(P);
   DP_CHECK_CUDA(ctx, cudaGetLastError());
   timed_end(ctx, "mc_init");
+  if (P.order0) {
+    timed_begin(ctx);
+    DP_CHECK_CUDA(ctx, sched_order(ctx->stream, P.n, nullptr, KeyOf{P.key0}, P.sched, P.order0,
+                                   &ctx->launches));
+    --ctx->launches;  // timed_begin counted one of the three
+    timed_end(ctx, "mc_order");
+  }
   int rc = launch_phase<R, 0, T, POR>(ctx, P, smem, need);
   if (rc) return rc;
+  if (P.order1) {
+    // the queue that phase 0 filled, ordered by the histories' phase-1 cost
+    using Q = typename std::conditional<POR, HandoffP<R>, Handoff<R>>::type;
+    timed_begin(ctx);
+    DP_CHECK_CUDA(ctx, sched_order(ctx->stream, P.n, P.counter + 2,
+                                   QueueKeyOf<Q>{static_cast<const Q*>(P.queue), P.key1}, P.sched,
+                                   P.order1, &ctx->launches));
+    --ctx->launches;
+    timed_end(ctx, "mc_order");
+  }
   rc = launch_phase<R, 1, T, POR>(ctx, P, smem, need);
   if (rc) return rc;
   timed_begin(ctx);
@@ -1018,10 +1096,13 @@ int dp_set_mc_shape(dp_ctx* ctx, int family, int precision, const dp_mc_shape* s
     return fail(ctx, DP_ERR_ARG, "staging is 0 (shared memory) or 1 (L1/L2)");
   if (shape->batch != 0 && shape->batch != 1 && shape->batch != 2 && shape->batch != 4)
     return fail(ctx, DP_ERR_ARG, "batch is 1, 2 or 4 histories (0: 1)");
+  if (shape->order != 0 && shape->order != 1)
+    return fail(ctx, DP_ERR_ARG, "order is 0 (longest first) or 1 (index order)");
   const int rc = dp_set_mc_threads(ctx, family, precision, shape->threads);
   if (rc) return rc;
   ctx->mc_stage[family][precision] = shape->staging;
   ctx->mc_batch[family][precision] = shape->batch;
+  ctx->mc_order[family][precision] = shape->order;
   return DP_OK;
 }
 
@@ -1030,6 +1111,7 @@ int dp_get_mc_shape(const dp_ctx* ctx, int family, int precision, dp_mc_shape* s
   dp_get_mc_threads(ctx, family, precision, &shape->threads);
   shape->staging = ctx->mc_stage[family][precision];
   shape->batch = std::max(1, ctx->mc_batch[family][precision]);
+  shape->order = ctx->mc_order[family][precision];
   return DP_OK;
 }
 
@@ -1075,15 +1157,20 @@ int dp_autotune_shape(dp_ctx* ctx, int family, int precision, int (*run)(void*),
   };
   int list[8];
   const int nt = dp_mc_thread_choices(precision, list, 8);
-  for (int i = 0; i < nt && !rc; ++i) rc = trial(dp_mc_shape{list[i], best.staging, best.batch});
+  for (int i = 0; i < nt && !rc; ++i)
+    rc = trial(dp_mc_shape{list[i], best.staging, best.batch, best.order});
   const dp_mc_shape after_threads = best;
   for (int st = 0; st < 2 && !rc; ++st)
     if (st != after_threads.staging)
-      rc = trial(dp_mc_shape{after_threads.threads, st, after_threads.batch});
+      rc = trial(dp_mc_shape{after_threads.threads, st, after_threads.batch, after_threads.order});
   const dp_mc_shape after_stage = best;
   for (int bt : {1, 2, 4})
     if (!rc && bt != after_stage.batch)
-      rc = trial(dp_mc_shape{after_stage.threads, after_stage.staging, bt});
+      rc = trial(dp_mc_shape{after_stage.threads, after_stage.staging, bt, after_stage.order});
+  const dp_mc_shape after_batch = best;
+  for (int od = 0; od < 2 && !rc; ++od)
+    if (od != after_batch.order)
+      rc = trial(dp_mc_shape{after_batch.threads, after_batch.staging, after_batch.batch, od});
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   if (n_tried) *n_tried = count;
@@ -1192,7 +1279,8 @@ int dp_mc_histories(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock_c,
   long ng = geo_stride ? n : 1;
   size_t nb = size_t(n) * sizeof(double), gb = size_t(ng) * sizeof(double);
   Arena A;
-  A.base = static_cast<char*>(scratch(ctx, 8 * nb + 4 * gb + size_t(n) * (8 + kRecBytes) + 4096, 0));
+  A.base = static_cast<char*>(scratch(
+      ctx, 8 * nb + 4 * gb + size_t(n) * (8 + kRecBytes + kSchedBytes) + kSchedExtra + 4096, 0));
   A.cap = ctx->slot_bytes[0];
   double* dE = A.take<double>(n);
   double* dq = A.take<double>(n);
@@ -1238,6 +1326,7 @@ int dp_mc_histories(dp_ctx* ctx, const dp_physics* ph, const dp_mixture* rock_c,
   P.queue = queue;
   P.start = srec;
   P.end = erec;
+  take_sched(ctx, cfg->precision, n, A, P);
   rc = run(ctx, P, cfg->precision);
   if (rc) return rc;
   std::vector<int32_t> st_h;
@@ -1351,8 +1440,8 @@ int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_
   long nt = total > 0 ? total : 1;
   Arena A;
   A.base = static_cast<char*>(scratch(
-      ctx, size_t(nt) * (12 + 16 + kRecBytes) + size_t(n_los + 1) * 16 +
-               size_t(n_los + nt / kTallyChunk + 1) * sizeof(TallyPart) + 4096, 0));
+      ctx, size_t(nt) * (12 + 16 + kRecBytes + kSchedBytes) + size_t(n_los + 1) * 16 +
+               size_t(n_los + nt / kTallyChunk + 1) * sizeof(TallyPart) + kSchedExtra + 4096, 0));
   A.cap = ctx->slot_bytes[0];
   double* dc = A.take<double>(nt);
   int32_t* ds = A.take<int32_t>(nt);
@@ -1389,6 +1478,7 @@ int dp_mc_run_los(dp_ctx* ctx, const dp_physics* ph, dp_mixture* rock, const dp_
       P.info[2] = make_info(porous);
       P.porous_rec = prec;
     }
+    take_sched(ctx, cfg->precision, total, A, P);
     rc = run(ctx, P, cfg->precision);
     if (rc) return rc;
     if (compute_gradient) {

@@ -16,6 +16,7 @@
 #pragma once
 #include <cooperative_groups.h>
 
+#include <algorithm>
 #include <type_traits>
 
 #include "mc_device.cuh"
@@ -97,7 +98,8 @@ __device__ __forceinline__ long next_history(unsigned long long* counter, int ba
 template <class R, int PHASE, class G>
 __device__ __forceinline__ void drain_histories(G& geo, const Consts& C,
                                                 unsigned long long* counter,
-                                                typename G::Queue* queue) {
+                                                typename G::Queue* queue,
+                                                const uint32_t* order = nullptr) {
   const long n = PHASE == 0 ? geo.n0() : long(*(volatile unsigned long long*)(counter + 2));
   typename G::Hist h;
   Stream g;
@@ -105,9 +107,10 @@ __device__ __forceinline__ void drain_histories(G& geo, const Consts& C,
     const long j0 = next_history(counter + PHASE, C.batch);
     if (j0 >= n) break;
     for (long j = j0; j < j0 + C.batch && j < n; ++j) {
-      long i = j;
-      if (PHASE == 0) geo.start(j, h, g);
-      else i = geo.load(queue[j], h, g);
+      const long k = order ? long(order[j]) : j;
+      long i = k;
+      if (PHASE == 0) geo.start(k, h, g);
+      else i = geo.load(queue[k], h, g);
       h.s.status |= ST_TABLE;
       geo.end(i, h);
     }
@@ -116,12 +119,15 @@ __device__ __forceinline__ void drain_histories(G& geo, const Consts& C,
 
 // Runs histories until none is left for this phase.  counter[PHASE] hands out
 // history indices, counter[2] counts the hand-off queue.  With COOP, `item`
-// and `comp` are this warp's DCS buffers in shared memory.
+// and `comp` are this warp's DCS buffers in shared memory.  `order` (may be
+// null) maps the j-th hand-out to a history (phase 0) or a queue slot (phase
+// 1): the longest-first schedule.
 template <class R, int PHASE, bool COOP, class G>
 __device__ __forceinline__ void transport_histories(G& geo, const Consts& C,
                                                     unsigned long long* counter,
                                                     typename G::Queue* queue, float* item,
-                                                    float* comp) {
+                                                    float* comp,
+                                                    const uint32_t* order = nullptr) {
   const long n = PHASE == 0 ? geo.n0() : long(*(volatile unsigned long long*)(counter + 2));
   typename G::Hist h;
   Stream g;
@@ -135,11 +141,12 @@ __device__ __forceinline__ void transport_histories(G& geo, const Consts& C,
     if (cur >= 0 && ((cur + 1) & (C.batch - 1)) != 0) j = ++cur;
     else j = cur = next_history(counter + PHASE, C.batch);
     if (j >= n) return false;
+    const long k = order ? long(order[j]) : j;
     if (PHASE == 0) {
-      *idx = j;
-      geo.start(j, h, g);
+      *idx = k;
+      geo.start(k, h, g);
     } else {
-      *idx = geo.load(queue[j], h, g);
+      *idx = geo.load(queue[k], h, g);
     }
     return true;
   };
@@ -201,6 +208,74 @@ __device__ __forceinline__ void transport_histories(G& geo, const Consts& C,
   } else {
     while (live) live = settle(geo.template advance<false, PHASE>(h, g), &i);
   }
+}
+
+// ------------------------------------------------------------ longest first
+// The persistent loop hands histories out in counter order, and a warp runs
+// until its last lane's history ends.  Handing the costly histories out
+// first (a counting sort on a per-history cost bucket, descending) keeps the
+// lanes of a warp on histories of similar length and leaves only short ones
+// for the end of the launch.  A history's result does not depend on when or
+// where it runs, so the order changes no result.
+constexpr int kSchedBuckets = 1024;
+
+// count[b] += number of items whose bucket is b (n items, or *n_dev when
+// n_dev is set); bucket_of(s) gives the bucket of item s.
+template <class F>
+__global__ void __launch_bounds__(256) sched_count_kernel(long n, const unsigned long long* n_dev,
+                                                          F bucket_of, uint32_t* count) {
+  __shared__ uint32_t h[kSchedBuckets];
+  for (int b = threadIdx.x; b < kSchedBuckets; b += blockDim.x) h[b] = 0;
+  __syncthreads();
+  const long m = n_dev ? long(*n_dev) : n;
+  for (long s = blockIdx.x * long(blockDim.x) + threadIdx.x; s < m;
+       s += long(gridDim.x) * blockDim.x)
+    atomicAdd(&h[bucket_of(s)], 1u);
+  __syncthreads();
+  for (int b = threadIdx.x; b < kSchedBuckets; b += blockDim.x)
+    if (h[b]) atomicAdd(&count[b], h[b]);
+}
+// offset[b] = items in buckets above b (descending exclusive scan); one block
+// of kSchedBuckets threads.
+static __global__ void __launch_bounds__(kSchedBuckets) sched_scan_kernel(const uint32_t* count,
+                                                                   uint32_t* offset) {
+  __shared__ uint32_t s[kSchedBuckets];
+  const int t = threadIdx.x;
+  s[t] = count[kSchedBuckets - 1 - t];  // descending bucket order
+  __syncthreads();
+  for (int d = 1; d < kSchedBuckets; d <<= 1) {
+    const uint32_t v = t >= d ? s[t - d] : 0u;
+    __syncthreads();
+    s[t] += v;
+    __syncthreads();
+  }
+  offset[kSchedBuckets - 1 - t] = s[t] - count[kSchedBuckets - 1 - t];
+}
+// order[offset[b]++] = s for every item s of bucket b.
+template <class F>
+__global__ void __launch_bounds__(256) sched_scatter_kernel(long n, const unsigned long long* n_dev,
+                                                            F bucket_of, uint32_t* offset,
+                                                            uint32_t* order) {
+  const long m = n_dev ? long(*n_dev) : n;
+  for (long s = blockIdx.x * long(blockDim.x) + threadIdx.x; s < m;
+       s += long(gridDim.x) * blockDim.x)
+    order[atomicAdd(&offset[bucket_of(s)], 1u)] = uint32_t(s);
+}
+// Longest-first order of n items (or *n_dev items: the count of a queue
+// filled on the device), count and offset 2 x kSchedBuckets words of
+// scratch; three launches on the stream.
+template <class F>
+inline cudaError_t sched_order(cudaStream_t st, long n, const unsigned long long* n_dev,
+                               F bucket_of, uint32_t* count, uint32_t* order, long long* launches) {
+  cudaError_t e = cudaMemsetAsync(count, 0, kSchedBuckets * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  const int blocks = int(std::min<long>((n + 255) / 256, 152L * 4));
+  sched_count_kernel<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(n, n_dev, bucket_of, count);
+  sched_scan_kernel<<<1, kSchedBuckets, 0, st>>>(count, count + kSchedBuckets);
+  sched_scatter_kernel<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(n, n_dev, bucket_of,
+                                                               count + kSchedBuckets, order);
+  *launches += 3;
+  return cudaGetLastError();
 }
 
 }  // namespace mc

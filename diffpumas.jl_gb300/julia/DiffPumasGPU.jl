@@ -113,6 +113,7 @@ struct DpSolveParams
 end
 struct DpMcShape
     threads::Cint; staging::Cint; batch::Cint
+    order::Cint                # 0: longest first, 1: index order
 end
 
 # ---------------------------------------------------------------- errors, context
@@ -423,7 +424,7 @@ const TUNE_WORK = Ref{Any}()
 run_cb(::Ptr{Cvoid})::Cint = (TUNE_WORK[](); Cint(0))
 function autotune!(g::GPUPhysics, family::Integer, precision::Integer, work)
     TUNE_WORK[] = work
-    best = Ref{DpMcShape}(DpMcShape(0, 0, 1))
+    best = Ref{DpMcShape}(DpMcShape(0, 0, 1, 0))
     tried = Vector{DpMcShape}(undef, 16); ms = zeros(16); n = Ref{Cint}(0)
     check(ccall((:dp_autotune_shape, lib), Cint,
                 (Ptr{Cvoid}, Cint, Cint, Ptr{Cvoid}, Ptr{Cvoid}, Ref{DpMcShape}, Ptr{DpMcShape},

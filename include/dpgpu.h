@@ -127,16 +127,18 @@ int dp_autotune(dp_ctx* ctx, int family, int precision, int (*run)(void* user), 
                 int* best_threads, double* ms, int cap);
 /* The full launch shape of those kernels: the CTA size, where the media
  * tables live (staging 0: copied to shared memory once per CTA when they fit,
- * the default; 1: read through L1/L2) and how many consecutive histories a
- * thread takes from the work counter at a time (batch 1, 2 or 4; 0: 1).  No
+ * the default; 1: read through L1/L2), how many consecutive histories a
+ * thread takes from the work counter at a time (batch 1, 2 or 4; 0: 1) and
+ * the order histories are handed out in (order 0: longest first, by a
+ * per-history estimate of its steps, the default; 1: index order).  No
  * choice changes a result: every history keeps its own stream. */
 typedef struct {
-  int threads, staging, batch;
+  int threads, staging, batch, order;
 } dp_mc_shape;
 int dp_set_mc_shape(dp_ctx* ctx, int family, int precision, const dp_mc_shape* shape);
 int dp_get_mc_shape(const dp_ctx* ctx, int family, int precision, dp_mc_shape* shape);
 /* dp_autotune over the whole shape, one dimension at a time (CTA size, then
- * staging, then batch, each from the best so far): every candidate runs
+ * staging, then batch, then order, each from the best so far): every candidate runs
  * run(user) once untimed and once timed.  The best shape stays on the context
  * and goes to *best; tried[i] / ms[i] list the candidates and their times (up
  * to cap), *n_tried their count. */

@@ -293,35 +293,39 @@ def test_cta_sizes_give_identical_histories(dp, phys, media):
 
 
 def test_launch_shapes_give_identical_histories(dp, phys, media):
-    """Table staging (shared memory or L1/L2) and the refill batch (1, 2 or 4
-    histories per take) do not change a result either: every shape gives the
-    same contributions bit for bit, and histories taken in runs of a batch
-    all end (none skipped or run twice)."""
+    """Table staging (shared memory or L1/L2), the refill batch (1, 2 or 4
+    histories per take) and the hand-out order (longest first or by index)
+    do not change a result either: every shape gives the same contributions
+    bit for bit, and histories taken in runs of a batch or out of order all
+    end (none skipped or run twice)."""
     n, seed = 20000, 6
     E, q, w, geo = _histories(n, seed)
     _, air, mix = media
     runs = {}
     try:
-        for shape in [(1024, 0, 1), (1024, 1, 1), (1024, 0, 2), (768, 1, 4), (512, 0, 4)]:
+        for shape in [(1024, 0, 1, 0), (1024, 0, 1, 1), (1024, 1, 1, 0), (1024, 0, 2, 1),
+                      (768, 1, 4, 0), (512, 0, 4, 1)]:
             dp.set_mc_shape(phys, "mc", "mixed", *shape)
             assert dp.get_mc_shape(phys, "mc", "mixed") == dict(zip(("threads", "staging",
-                                                                     "batch"), shape))
+                                                                     "batch", "order"), shape))
             c, st, ns, _ = dp.mc_histories(phys, mix, air, E, q, w, seed=seed,
                                            precision="mixed", **geo)
             assert np.all(st == 0) and np.all(ns > 0)
             runs[shape] = c
         with pytest.raises(ValueError):
             dp.set_mc_shape(phys, "mc", "mixed", 1024, 0, 3)
+        with pytest.raises(ValueError):
+            dp.set_mc_shape(phys, "mc", "mixed", 1024, 0, 1, 2)
     finally:
-        dp.set_mc_shape(phys, "mc", "mixed", 0, 0, 1)
+        dp.set_mc_shape(phys, "mc", "mixed", 0, 0, 1, 0)
     for shape, c in runs.items():
-        np.testing.assert_array_equal(c, runs[(1024, 0, 1)], err_msg=str(shape))
+        np.testing.assert_array_equal(c, runs[(1024, 0, 1, 0)], err_msg=str(shape))
 
 
 def test_autotune_shape_searches_every_dimension(dp, phys, media):
     """dp_autotune_shape: the CTA sizes, then the other staging, then the
-    other two batches, each timed after an untimed run; the fastest shape
-    stays on the context."""
+    other two batches, then the other order, each timed after an untimed
+    run; the fastest shape stays on the context."""
     _, air, mix = media
     los = dp.make_los([4000], thickness=100.0, density=2650.0, elevation=60.0, energy_min=1.0,
                       energy_max=1e4, air_height=1000.0)
@@ -334,15 +338,16 @@ def test_autotune_shape_searches_every_dimension(dp, phys, media):
     try:
         best, tried = dp.autotune_shape(phys, "mc", "mixed", run)
         n_sizes = len(dp.mc_thread_choices("mixed"))
-        assert len(tried) == n_sizes + 1 + 2 and len(calls) == 2 * len(tried)
+        assert len(tried) == n_sizes + 1 + 2 + 1 and len(calls) == 2 * len(tried)
         assert {s["threads"] for s, _ in tried} == set(dp.mc_thread_choices("mixed"))
         assert {s["staging"] for s, _ in tried} == {0, 1}
         assert {s["batch"] for s, _ in tried} == {1, 2, 4}
+        assert {s["order"] for s, _ in tried} == {0, 1}
         assert all(v > 0 for _, v in tried)
         assert dp.get_mc_shape(phys, "mc", "mixed") == best
         assert best in [s for s, _ in tried]
     finally:
-        dp.set_mc_shape(phys, "mc", "mixed", 0, 0, 1)
+        dp.set_mc_shape(phys, "mc", "mixed", 0, 0, 1, 0)
 
 
 def test_autotune_keeps_the_fastest_size(dp, phys, media):
