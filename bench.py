@@ -152,13 +152,19 @@ def setup_c3(dp, torch, dev, precision="mixed"):
     h_grad = np.zeros(grid.ncell)
     rho_h, rays_h, cot_h = (np.ascontiguousarray(a, np.float64).ravel() for a in (rho, rays, cot))
     g = grid.to_c()
+    nE, nq, nw = (np.ascontiguousarray(x, np.float64) for x in nodes)
+    tp = dp.DpTomoParams(paths.params.rock_material, paths.params.air_material,
+                         paths.params.side_cell, paths.params.side_density,
+                         paths.params.primary_altitude, len(nE), nE.ctypes.data, nq.ctypes.data,
+                         nw.ctypes.data, dp.PRECISION[precision])
+    hp = lambda a: a.ctypes.data_as(C.c_void_p)
 
     def step_e2e():
-        # reference-facing call with host buffers: rho and r in, flux and J^T r out
-        # (rays traced once beforehand, as precompute_paths does)
-        f, gr = paths.eval_host(rho_h, cot_h, precision=precision, nodes=nodes)
-        h_flux[:] = f
-        h_grad[:] = gr
+        # reference-facing C ABI call with host buffers (dp_tomo_eval): rho and
+        # r in, flux and J^T r out, copies inside the call (rays traced once
+        # beforehand, as precompute_paths does)
+        dp.check(lib.dp_tomo_eval(phys.ctx.h, phys.h, paths.h, C.byref(tp), hp(rho_h), hp(cot_h),
+                                  hp(h_flux), hp(h_grad), None), phys.ctx.h)
 
     def plain_dev():
         dp.check(lib.dp_tomo_forward_plain_dev(phys.ctx.h, phys.h, C.byref(g),
@@ -183,7 +189,7 @@ def setup_c3(dp, torch, dev, precision="mixed"):
                                    "32 energy nodes [1,1e6] GeV, flux + J^T r per step",
                        "grid": [64, 64, 32], "rays": n_rays, "energy_nodes": 32,
                        "segments": nseg, "precision": precision,
-                       "paths": "traced once (resident); e2e traces on every call"},
+                       "paths": "traced once (resident), as precompute_paths does"},
             "h2d": 8 * (rho_h.size + cot_h.size + 3 * len(nodes[0])),
             "d2h": 8 * (n_rays + grid.ncell)}
     return step_dev, step_e2e, plain_dev, info, phys

@@ -113,6 +113,7 @@ int dp_destroy(dp_ctx* c) {
     if (s) cudaFree(s);
   if (c->d_flag) cudaFree(c->d_flag);
   if (c->d_work) cudaFree(c->d_work);
+  if (c->nodes_dev) cudaFree(c->nodes_dev);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   for (auto& p : c->pending) {

@@ -45,6 +45,11 @@ struct dp_ctx {
   int mc_batch[2][2] = {{0, 0}, {0, 0}};
   // Hand-out order of the histories (0: longest first, 1: index order).
   int mc_order[2][2] = {{0, 0}, {0, 0}};
+  // Energy nodes of the last host-pointer tomography evaluation (energies,
+  // charges, weights) and their device copy: a call with the same nodes
+  // uploads none.
+  std::vector<double> nodes_host;
+  double* nodes_dev = nullptr;
   // Limits lowered for failure-path tests (dp_set_debug_limits); negative:
   // the default (2,000,000 transport steps, 100,000 hard events per mixed
   // step, dp::kStageWait polls of a table-staging wait).

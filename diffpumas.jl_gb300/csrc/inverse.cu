@@ -697,14 +697,6 @@ int dp_tomo_solve_dev(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa,
       ++ctx->launches;
       DP_CHECK_CUDA(ctx, cudaGetLastError());
     }
-    // the misfit at the last iterate
-    if (!rc && sp->n_iter > 0 && (rc = S.eval(rho, flux, false)) == DP_OK) {
-      residual_kernel<<<S.grid(nr), kThreads, 0, ctx->stream>>>(flux, obs, nullptr, nr, -1.0, r,
-                                                                 nullptr);
-      ++ctx->launches;
-      S.dot(r, r, nullptr, nr, S.s + 3);
-      record(sp->n_iter, std::sqrt(S.host_scalar(S.s + 3)));
-    }
   } else if (sp->method == DP_SOLVE_GD) {
     // gradient_descent_reconstruct (src/Tomography_inverse.jl:324-400)
     const bool fixed = sp->fixed_linearization != 0;
@@ -892,8 +884,9 @@ int dp_tomo_solve_dev(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa,
       }
     }
   }
-  if (!rc) {
-    // final misfit ||obs - f(rho)||
+  if (!rc && sp->method != DP_SOLVE_GD) {
+    // final misfit ||obs - f(rho)|| (GD records every iterate itself, on the
+    // model it iterates on)
     rc = S.eval(rho, flux, false);
     if (!rc) {
       residual_kernel<<<S.grid(nr), kThreads, 0, ctx->stream>>>(flux, obs, nullptr, nr, -1.0, r,

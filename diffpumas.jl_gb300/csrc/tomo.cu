@@ -1274,20 +1274,72 @@ int dp_tomo_eval(dp_ctx* ctx, const dp_physics* ph, const dp_paths* pa, const dp
     return fail(ctx, DP_ERR_ARG, "energy nodes required");
   DP_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
   long ncell = long(pa->grid.nx) * pa->grid.ny * pa->grid.nz;
-  Inputs d;
-  int rc = upload_inputs(ctx, tp, ncell, pa->n_rays, nullptr, rho, cot, grad != nullptr, d);
-  if (rc) return rc;
+  // the energy nodes: uploaded once and kept on the context while calls pass
+  // the same ones (three fewer round trips per call)
+  const int nn = tp->n_nodes;
+  bool same = ctx->nodes_dev && ctx->nodes_host.size() == size_t(3 * nn);
+  for (int k = 0; same && k < nn; ++k)
+    same = ctx->nodes_host[k] == tp->node_energy[k] &&
+           ctx->nodes_host[nn + k] == tp->node_charge[k] &&
+           ctx->nodes_host[2 * nn + k] == tp->node_weight[k];
+  if (!same) {
+    if (ctx->nodes_dev && ctx->nodes_host.size() != size_t(3 * nn)) {
+      DP_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      cudaFree(ctx->nodes_dev);
+      ctx->nodes_dev = nullptr;
+    }
+    ctx->nodes_host.clear();
+    if (!ctx->nodes_dev &&
+        cudaMalloc(&ctx->nodes_dev, sizeof(double) * 3 * size_t(nn)) != cudaSuccess) {
+      ctx->nodes_dev = nullptr;
+      return fail(ctx, DP_ERR_ALLOC, "node array allocation failed");
+    }
+    std::vector<double> packed(tp->node_energy, tp->node_energy + nn);
+    packed.insert(packed.end(), tp->node_charge, tp->node_charge + nn);
+    packed.insert(packed.end(), tp->node_weight, tp->node_weight + nn);
+    // a pageable source is staged before the call returns
+    DP_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->nodes_dev, packed.data(), 8 * packed.size(),
+                                       cudaMemcpyHostToDevice, ctx->stream));
+    ctx->nodes_host.swap(packed);
+  }
+  const size_t need = 8 * size_t(2 * ncell + 2 * pa->n_rays) + 8 * 256;
+  Arena A;
+  A.base = static_cast<char*>(scratch(ctx, need, 2));
+  A.cap = ctx->slot_bytes[2];
+  double *d_rho = A.take<double>(ncell), *d_flux = A.take<double>(pa->n_rays);
+  double *d_cot = cot ? A.take<double>(pa->n_rays) : nullptr;
+  double *d_grad = grad ? A.take<double>(ncell) : nullptr;
+  if (!d_flux || (cot && !d_cot) || (grad && !d_grad))
+    return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
+  DP_CHECK_CUDA(ctx, cudaMemcpyAsync(d_rho, rho, 8 * ncell, cudaMemcpyHostToDevice, ctx->stream));
+  if (cot)
+    DP_CHECK_CUDA(ctx, cudaMemcpyAsync(d_cot, cot, 8 * pa->n_rays, cudaMemcpyHostToDevice,
+                                       ctx->stream));
   double* djac = nullptr;
   if (jac) {
     djac = static_cast<double*>(scratch(ctx, size_t(pa->nnz + 1) * 8, 3));
     if (!djac) return fail(ctx, DP_ERR_ALLOC, "scratch allocation failed");
   }
-  rc = eval_core(ctx, ph, pa, tp, d.rho, d.nE, d.nq, d.nw, d.cot, d.flux, d.grad, djac, tp->precision);
+  // one synchronisation at the end: the error flag comes back with the results
+  const int saved = ctx->blocking;
+  ctx->blocking = 0;
+  const double* nd = ctx->nodes_dev;
+  int rc = eval_core(ctx, ph, pa, tp, d_rho, nd, nd + nn, nd + 2 * nn, d_cot, d_flux, d_grad,
+                     djac, tp->precision);
+  ctx->blocking = saved;
   if (rc) return rc;
-  cudaMemcpyAsync(flux, d.flux, 8 * pa->n_rays, cudaMemcpyDeviceToHost, ctx->stream);
-  if (grad) cudaMemcpyAsync(grad, d.grad, 8 * ncell, cudaMemcpyDeviceToHost, ctx->stream);
+  int flag = 0;
+  cudaMemcpyAsync(flux, d_flux, 8 * pa->n_rays, cudaMemcpyDeviceToHost, ctx->stream);
+  if (grad) cudaMemcpyAsync(grad, d_grad, 8 * ncell, cudaMemcpyDeviceToHost, ctx->stream);
   if (jac) cudaMemcpyAsync(jac, djac, 8 * pa->nnz, cudaMemcpyDeviceToHost, ctx->stream);
+  if (saved) cudaMemcpyAsync(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
   DP_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (flag) {
+    cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    return fail(ctx, DP_ERR_STATE,
+                flag == 2 ? "ray segment buffer overflow" : "table-staging wait exceeded its limit");
+  }
   return DP_OK;
 }
 

@@ -130,8 +130,11 @@ int dp_autotune(dp_ctx* ctx, int family, int precision, int (*run)(void* user), 
  * the default; 1: read through L1/L2), how many consecutive histories a
  * thread takes from the work counter at a time (batch 1, 2 or 4; 0: 1) and
  * the order histories are handed out in (order 0: longest first, by a
- * per-history estimate of its steps, the default; 1: index order).  No
- * choice changes a result: every history keeps its own stream. */
+ * per-history estimate of its steps, the default; 1: index order).  Every
+ * history keeps its own stream, so staging, batch and order change no result
+ * (bit for bit).  Each CTA size is a separately compiled kernel whose FP32
+ * multiply-adds the code generator may fuse differently, so results at
+ * another size agree statistically, not bit for bit. */
 typedef struct {
   int threads, staging, batch, order;
 } dp_mc_shape;
@@ -742,7 +745,9 @@ int dp_tomo_forward_plain_dev(dp_ctx* ctx, const dp_physics* phys, const dp_grid
  *                  0.999, 1e-8) and plain steps of lr otherwise.
  * MLEM and GD re-evaluate f and J at every iterate, or with fixed_linearization
  * use f0 + J0 (rho - rho0) (the reference's relinearize = false; MLEM's fixed
- * A, b).  history[k] is the flux misfit ||f(rho_k) - obs|| at iterate k.  No
+ * A, b).  history[k] is the flux misfit ||f(rho_k) - obs|| at iterate k (GD
+ * with fixed_linearization: of the linear model it iterates on; NaN past an
+ * early stop).  No
  * reference entry point takes this exact form: it replaces the solver loops
  * around make_csda_operator (:614-626) for the voxel-density model. */
 #define DP_SOLVE_SART 0
