@@ -331,7 +331,8 @@ struct PathGeo {
     h.limit = limit;
     if (C.straggling) {
       if constexpr (PHASE == 0) {
-        if (straggled_step<R, COOP, true, true>(m, C, s, Li, rho, step, g, false, limit, h.x)) {
+        if (straggled_step<R, COOP, true, true>(m, C, s, Li, R(0), rho, step, g, false, limit,
+                                                h.x)) {
           h.x.kind = CONT_STRAG;
           h.x.medium = h.med;
           return ADV_WAIT;
@@ -371,7 +372,7 @@ struct PathGeo {
     } else {
       Loc<R> Li = locate(m, x.r0);
       // the fixed-path transport never scatters (x.flag is 0)
-      const R moved = straggled_end_in(m, P.C, h.s, Li, x.r0, R(d.energy), x.r1, x.r2, d.weight,
+      const R moved = straggled_end_in(m, P.C, h.s, Li, R(0), x.r0, R(d.energy), x.r1, x.r2, d.weight,
                                        d.process, d.element, true, false, R(0), x.r3, x.a, true,
                                        false, g);
       return step_end(h, moved);
@@ -398,7 +399,7 @@ __global__ void __launch_bounds__(T, 1) dir_kernel(const __grid_constant__ DirPa
                             P.C.wait_iters)) {
     if (threadIdx.x == 0) atomicExch(P.err_flag, 1);
     PathGeo<R> geo{P, nullptr};
-    drain_histories<R, PHASE>(geo, P.C, P.counter, static_cast<DirHandoff<R>*>(P.queue));
+    drain_histories<R, PHASE>(geo, P.counter, static_cast<DirHandoff<R>*>(P.queue));
     return;
   }
   Med<R>* meds = reinterpret_cast<Med<R>*>(smem + dir_desc_offset<R>(P));
@@ -512,7 +513,6 @@ int dir_launch_t(dp_ctx* ctx, DirParams& P) {
     P.n_staged = k;
     if (dir_coop_offset<R>(P) + coop_bytes <= size_t(dev_smem)) break;
   }
-  P.C.batch = std::max(1, ctx->mc_batch[DP_KERNEL_DIR][sizeof(R) == 4]);
   const size_t smem = dir_coop_offset<R>(P) + coop_bytes;
   if (smem > size_t(dev_smem)) return fail(ctx, DP_ERR_ARG, "too many media for the fixed-path MC kernel");
   const long need = (P.n + threads - 1) / threads;

@@ -40,9 +40,8 @@ struct dp_ctx {
   // DP_KERNEL_DIR) and precision (DP_PREC_FP64, DP_PREC_MIXED); 0: default.
   int mc_threads[2][2] = {{0, 0}, {0, 0}};
   // Table staging (0: media in shared memory when they fit, 1: read through
-  // L1/L2) and histories a thread takes per refill (0: 1) of the same kernels.
+  // L1/L2) of the same kernels.
   int mc_stage[2][2] = {{0, 0}, {0, 0}};
-  int mc_batch[2][2] = {{0, 0}, {0, 0}};
   // Hand-out order of the histories (0: longest first, 1: index order).
   int mc_order[2][2] = {{0, 0}, {0, 0}};
   // Energy nodes of the last host-pointer tomography evaluation (energies,

@@ -618,11 +618,11 @@ __global__ void __launch_bounds__(T, 1) mc_kernel(const __grid_constant__ McPara
       const Med<R> none{};
       if constexpr (POR) {
         SlabGeoP<R> geo{P, none, none, none};
-        drain_histories<R, PHASE>(geo, P.C, P.counter, static_cast<HandoffP<R>*>(P.queue),
+        drain_histories<R, PHASE>(geo, P.counter, static_cast<HandoffP<R>*>(P.queue),
                                   PHASE == 0 ? P.order0 : P.order1);
       } else {
         SlabGeo<R> geo{P, none, none};
-        drain_histories<R, PHASE>(geo, P.C, P.counter, static_cast<Handoff<R>*>(P.queue),
+        drain_histories<R, PHASE>(geo, P.counter, static_cast<Handoff<R>*>(P.queue),
                                   PHASE == 0 ? P.order0 : P.order1);
       }
       return;
@@ -858,7 +858,6 @@ int check_cfg(dp_ctx* ctx, const dp_physics* ph, const dp_mc_config* cfg, Consts
   C->step_cap = step_cap(ctx);
   C->event_cap = event_cap(ctx);
   C->wait_iters = stage_wait(ctx);
-  C->batch = 1;
   C->straggling = cfg->straggling != 0;
   C->scattering = cfg->scattering != 0;
   return DP_OK;
@@ -982,7 +981,6 @@ int launch_mc_t(dp_ctx* ctx, McParams& P) {
                      ctx->mc_stage[DP_KERNEL_MC][sizeof(R) == 4] == 0
                  ? 1
                  : 0;
-  P.C.batch = std::max(1, ctx->mc_batch[DP_KERNEL_MC][sizeof(R) == 4]);
   size_t smem = 16 + (P.staged ? tables : 0) + coop_bytes;
   if (smem > size_t(dev_smem)) return fail(ctx, DP_ERR_ARG, "media too large for the MC kernel");
   long need = (P.n + threads - 1) / threads;
@@ -1094,14 +1092,11 @@ int dp_set_mc_shape(dp_ctx* ctx, int family, int precision, const dp_mc_shape* s
     return fail(ctx, DP_ERR_ARG, "bad kernel family, precision or shape");
   if (shape->staging != 0 && shape->staging != 1)
     return fail(ctx, DP_ERR_ARG, "staging is 0 (shared memory) or 1 (L1/L2)");
-  if (shape->batch != 0 && shape->batch != 1 && shape->batch != 2 && shape->batch != 4)
-    return fail(ctx, DP_ERR_ARG, "batch is 1, 2 or 4 histories (0: 1)");
   if (shape->order != 0 && shape->order != 1)
     return fail(ctx, DP_ERR_ARG, "order is 0 (longest first) or 1 (index order)");
   const int rc = dp_set_mc_threads(ctx, family, precision, shape->threads);
   if (rc) return rc;
   ctx->mc_stage[family][precision] = shape->staging;
-  ctx->mc_batch[family][precision] = shape->batch;
   ctx->mc_order[family][precision] = shape->order;
   return DP_OK;
 }
@@ -1110,7 +1105,6 @@ int dp_get_mc_shape(const dp_ctx* ctx, int family, int precision, dp_mc_shape* s
   if (!ctx || !shape || !shape_args(family, precision)) return DP_ERR_ARG;
   dp_get_mc_threads(ctx, family, precision, &shape->threads);
   shape->staging = ctx->mc_stage[family][precision];
-  shape->batch = std::max(1, ctx->mc_batch[family][precision]);
   shape->order = ctx->mc_order[family][precision];
   return DP_OK;
 }
@@ -1157,20 +1151,14 @@ int dp_autotune_shape(dp_ctx* ctx, int family, int precision, int (*run)(void*),
   };
   int list[8];
   const int nt = dp_mc_thread_choices(precision, list, 8);
-  for (int i = 0; i < nt && !rc; ++i)
-    rc = trial(dp_mc_shape{list[i], best.staging, best.batch, best.order});
+  for (int i = 0; i < nt && !rc; ++i) rc = trial(dp_mc_shape{list[i], best.staging, best.order});
   const dp_mc_shape after_threads = best;
   for (int st = 0; st < 2 && !rc; ++st)
     if (st != after_threads.staging)
-      rc = trial(dp_mc_shape{after_threads.threads, st, after_threads.batch, after_threads.order});
+      rc = trial(dp_mc_shape{after_threads.threads, st, after_threads.order});
   const dp_mc_shape after_stage = best;
-  for (int bt : {1, 2, 4})
-    if (!rc && bt != after_stage.batch)
-      rc = trial(dp_mc_shape{after_stage.threads, after_stage.staging, bt, after_stage.order});
-  const dp_mc_shape after_batch = best;
   for (int od = 0; od < 2 && !rc; ++od)
-    if (od != after_batch.order)
-      rc = trial(dp_mc_shape{after_batch.threads, after_batch.staging, after_batch.batch, od});
+    if (od != after_stage.order) rc = trial(dp_mc_shape{after_stage.threads, after_stage.staging, od});
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   if (n_tried) *n_tried = count;

@@ -134,7 +134,6 @@ struct Consts {
   int straggling, scattering;
   // loop caps and the table-staging wait limit of the launch
   int step_cap, event_cap, wait_iters;
-  int batch;  // histories a thread takes from the work counter at a time (>= 1)
   // physics constants in the transport precision
   template <class R> __device__ __forceinline__ R mass_r() const {
     return sizeof(R) == 8 ? R(mass) : R(mass_f);
@@ -914,15 +913,16 @@ static __device__ __noinline__ float scattering_angle_f(const Med<float>& m, flo
   return fminf(fmaxf(mu, 0.f), 1.f);
 }
 
-// sample_soft_scattering (src/Straggling.jl:539-590, :1204-1253).
+// sample_soft_scattering (src/Straggling.jl:539-590, :1204-1253).  lb0 is
+// the transport path at the step's start (the step limit computed it) and
+// L1 the location of k1 (the weight update uses it too).
 template <class R>
-static __device__ __noinline__ R soft_scattering(const Med<R>& m, const Loc<R>& L0, R k1, R step, R density,
-                             Stream& g) {
+static __device__ __noinline__ R soft_scattering(const Med<R>& m, R lb0, const Loc<R>& L1, R k1,
+                                                 R step, R density, Stream& g) {
   if (step <= R(0) || density <= R(0)) return R(0);
-  R lb0 = transport_path(m, L0);
   R inv0 = lb0 > R(0) ? density / lb0 : R(0), inv1;
   if (k1 > R(0)) {
-    R lb1 = transport_path(m, locate(m, k1));
+    R lb1 = transport_path(m, L1);
     inv1 = lb1 > R(0) ? density / lb1 : R(0);
   } else {
     inv1 = inv0;
@@ -1041,13 +1041,15 @@ __device__ __forceinline__ double polar_ioni(double m, double ki, double kf) {
 // straggled_end completes a step from its energy-loss and event decisions.
 template <class R>
 __device__ __forceinline__ R straggled_end_in(const Med<R>& m, const Consts& C, State<R>& s,
-                                              const Loc<R>& Li, R ki, R kf, R ckf, R dX, double dw,
+                                              const Loc<R>& Li, R lb0, R ki, R kf, R ckf, R dX,
+                                              double dw,
                                               int proc, int elem, bool del, bool ehs, R k_ehs,
                                               R density, R step, bool shortened, bool scattering,
                                               Stream& g) {
   const R mass = C.mass_r<R>();
   R astep = dX / density;
   R oz = s.uz;  // the position moves along the incoming direction
+  const Loc<R> Lc = locate(m, ckf);  // soft scattering and the weight update
   if (scattering) {
     if (del && proc > 0) {
       const double* e = m.el + kElStride * elem;
@@ -1062,7 +1064,7 @@ __device__ __forceinline__ R straggled_end_in(const Med<R>& m, const Consts& C, 
       else mu = R(scattering_angle(m, C.mass, double(k_ehs), g));
       if (mu > R(0)) rotate(s, mu, g);
     }
-    R mu = soft_scattering(m, Li, ckf, astep, density, g);
+    R mu = soft_scattering(m, lb0, Lc, ckf, astep, density, g);
     if (mu > R(0)) rotate(s, mu, g);
   }
   R pt = astep * mass / R(2) *
@@ -1072,7 +1074,7 @@ __device__ __forceinline__ R straggled_end_in(const Med<R>& m, const Consts& C, 
   R da = astep;
   if (sizeof(R) == 4) da = shortened ? dX / density : step;
   alt_add(s.z, -(da * oz));
-  R wf = at(m, locate(m, ckf), MC_MS) / at(m, Li, MC_MS);
+  R wf = at(m, Lc, MC_MS) / at(m, Li, MC_MS);
   if (sizeof(R) == 4) s.w = s.w * wf * exp(-pt / C.ctau_r<R>()) * R(dw);
   else s.w = R(double(s.w * wf * exp(-pt / C.ctau_r<R>())) * dw);
   s.E = kf;
@@ -1080,11 +1082,11 @@ __device__ __forceinline__ R straggled_end_in(const Med<R>& m, const Consts& C, 
 }
 template <class R>
 static __device__ __noinline__ R straggled_end(const Med<R>& m, const Consts& C, State<R>& s, const Loc<R>& Li,
-                                               R ki, R kf, R ckf, R dX, double dw, int proc, int elem,
-                                               bool del, bool ehs, R k_ehs, R density, R step,
-                                               bool shortened, bool scattering, Stream& g) {
-  return straggled_end_in<R>(m, C, s, Li, ki, kf, ckf, dX, dw, proc, elem, del, ehs, k_ehs, density,
-                             step, shortened, scattering, g);
+                                               R lb0, R ki, R kf, R ckf, R dX, double dw, int proc,
+                                               int elem, bool del, bool ehs, R k_ehs, R density,
+                                               R step, bool shortened, bool scattering, Stream& g) {
+  return straggled_end_in<R>(m, C, s, Li, lb0, ki, kf, ckf, dX, dw, proc, elem, del, ehs, k_ehs,
+                             density, step, shortened, scattering, g);
 }
 
 // The step up to its hard-event decision; true when it suspended on the
@@ -1093,8 +1095,8 @@ static __device__ __noinline__ R straggled_end(const Med<R>& m, const Consts& C,
 // With MOVED, x.moved receives the path length of a completed step.
 template <class R, bool COOP, bool MOVED = false, bool INL = false>
 __device__ bool straggled_step(const Med<R>& m, const Consts& C, State<R>& s, const Loc<R>& Li,
-                               R density, R step, Stream& g, bool scattering, R energy_limit,
-                               Cont<R>& x) {
+                               R lb0, R density, R step, Stream& g, bool scattering,
+                               R energy_limit, Cont<R>& x) {
   const R mass = C.mass_r<R>(), eratio = C.eratio_r<R>();
   R ki = s.E, dX = step * density;
   bool shortened = false;  // the step ended before its requested length
@@ -1178,10 +1180,10 @@ __device__ bool straggled_step(const Med<R>& m, const Consts& C, State<R>& s, co
   }
   R moved;
   if constexpr (INL)
-    moved = straggled_end_in(m, C, s, Li, ki, kf, ckf, dX, dw, proc, elem, del, ehs, k_ehs, density,
+    moved = straggled_end_in(m, C, s, Li, lb0, ki, kf, ckf, dX, dw, proc, elem, del, ehs, k_ehs, density,
                              step, shortened, scattering, g);
   else
-    moved = straggled_end(m, C, s, Li, ki, kf, ckf, dX, dw, proc, elem, del, ehs, k_ehs, density,
+    moved = straggled_end(m, C, s, Li, lb0, ki, kf, ckf, dX, dw, proc, elem, del, ehs, k_ehs, density,
                           step, shortened, scattering, g);
   if (MOVED) x.moved = moved;
   return false;
@@ -1367,8 +1369,11 @@ __device__ __forceinline__ int advance(const Med<R>& rock, const Med<R>& air, co
     Loc<R> Li = locate(m, s.E);
     R Xi = at(m, Li, MC_CR);
     R lim = R(0.01) * Xi / fmax(rd, R(1e-6));
+    // transport path at the start: the scattering step limit, then the soft
+    // scattering of the step
+    const R lb0 = h.scat ? transport_path(m, Li) : R(0);
     if (h.scat) {
-      R lb1 = transport_path(m, Li);
+      const R lb1 = lb0;
       if (lb1 > R(0) && rd > R(0)) lim = fmin(lim, R(0.01) * lb1 / rd);
     }
     if (in_air) lim = fmin(lim, R(0.05 * 12e3) / fmax(fabs(uz), R(0.05)));
@@ -1376,7 +1381,7 @@ __device__ __forceinline__ int advance(const Med<R>& rock, const Med<R>& air, co
     step = fmin(fmax(step, R(kStepMin)), R(1000));
     if (PHASE == 0 && h.strag) {
       if constexpr (PHASE == 0) {
-        if (straggled_step<R, COOP>(m, C, s, Li, rd, step, g, h.scat, h.limit, h.x)) {
+        if (straggled_step<R, COOP>(m, C, s, Li, lb0, rd, step, g, h.scat, h.limit, h.x)) {
           h.x.kind = CONT_STRAG;
           h.x.medium = med;
           return ADV_WAIT;
@@ -1423,7 +1428,8 @@ __device__ int resume(const Med<R>& rock, const Med<R>& air, const Med<R>* porou
     }
   } else {
     Loc<R> Li = locate(m, x.r0);
-    straggled_end(m, C, h.s, Li, x.r0, R(d.energy), x.r1, x.r2, d.weight, d.process, d.element,
+    const R lb0 = x.flag ? transport_path(m, Li) : R(0);
+    straggled_end(m, C, h.s, Li, lb0, x.r0, R(d.energy), x.r1, x.r2, d.weight, d.process, d.element,
                   true, false, R(0), x.r3, x.a, true, x.flag != 0, g);
   }
   return step_done(h, C);

@@ -81,39 +81,35 @@ static __device__ __noinline__ bool stage_blob(unsigned char* dst, const unsigne
   return stage_settle(bar, mbar_wait(bar, wait_iters));
 }
 
-// First of the next `batch` history indices for the calling thread
-// (warp-aggregated atomic: the active threads take consecutive runs).
-__device__ __forceinline__ long next_history(unsigned long long* counter, int batch = 1) {
+// Next history index for the calling thread (warp-aggregated atomic).
+__device__ __forceinline__ long next_history(unsigned long long* counter) {
   namespace cg = cooperative_groups;
   cg::coalesced_group g = cg::coalesced_threads();
   unsigned long long base = 0;
-  if (g.thread_rank() == 0) base = atomicAdd(counter, (unsigned long long)g.size() * batch);
+  if (g.thread_rank() == 0) base = atomicAdd(counter, (unsigned long long)g.size());
   base = g.shfl(base, 0);
-  return long(base + (unsigned long long)g.thread_rank() * batch);
+  return long(base + g.thread_rank());
 }
 
 // A block whose table staging gave up takes its share of the phase's
 // histories all the same and ends each one flagged DP_ST_TABLE_WAIT (no flux,
 // no table read), so that every history of the launch is accounted for.
 template <class R, int PHASE, class G>
-__device__ __forceinline__ void drain_histories(G& geo, const Consts& C,
-                                                unsigned long long* counter,
+__device__ __forceinline__ void drain_histories(G& geo, unsigned long long* counter,
                                                 typename G::Queue* queue,
                                                 const uint32_t* order = nullptr) {
   const long n = PHASE == 0 ? geo.n0() : long(*(volatile unsigned long long*)(counter + 2));
   typename G::Hist h;
   Stream g;
   for (;;) {
-    const long j0 = next_history(counter + PHASE, C.batch);
-    if (j0 >= n) break;
-    for (long j = j0; j < j0 + C.batch && j < n; ++j) {
-      const long k = order ? long(order[j]) : j;
-      long i = k;
-      if (PHASE == 0) geo.start(k, h, g);
-      else i = geo.load(queue[k], h, g);
-      h.s.status |= ST_TABLE;
-      geo.end(i, h);
-    }
+    const long j = next_history(counter + PHASE);
+    if (j >= n) break;
+    const long k = order ? long(order[j]) : j;
+    long i = k;
+    if (PHASE == 0) geo.start(k, h, g);
+    else i = geo.load(queue[k], h, g);
+    h.s.status |= ST_TABLE;
+    geo.end(i, h);
   }
 }
 
@@ -131,15 +127,8 @@ __device__ __forceinline__ void transport_histories(G& geo, const Consts& C,
   const long n = PHASE == 0 ? geo.n0() : long(*(volatile unsigned long long*)(counter + 2));
   typename G::Hist h;
   Stream g;
-  // a thread takes C.batch (1, 2 or 4) consecutive histories from the
-  // counter at a time; the counter only moves in multiples of it, so a run
-  // starts at a multiple of C.batch (a history's result does not depend on
-  // the thread that runs it)
-  long cur = -1;
   auto take = [&](long* idx) -> bool {
-    long j;
-    if (cur >= 0 && ((cur + 1) & (C.batch - 1)) != 0) j = ++cur;
-    else j = cur = next_history(counter + PHASE, C.batch);
+    const long j = next_history(counter + PHASE);
     if (j >= n) return false;
     const long k = order ? long(order[j]) : j;
     if (PHASE == 0) {

@@ -127,21 +127,21 @@ int dp_autotune(dp_ctx* ctx, int family, int precision, int (*run)(void* user), 
                 int* best_threads, double* ms, int cap);
 /* The full launch shape of those kernels: the CTA size, where the media
  * tables live (staging 0: copied to shared memory once per CTA when they fit,
- * the default; 1: read through L1/L2), how many consecutive histories a
- * thread takes from the work counter at a time (batch 1, 2 or 4; 0: 1) and
- * the order histories are handed out in (order 0: longest first, by a
- * per-history estimate of its steps, the default; 1: index order).  Every
- * history keeps its own stream, so staging, batch and order change no result
- * (bit for bit).  Each CTA size is a separately compiled kernel whose FP32
- * multiply-adds the code generator may fuse differently, so results at
- * another size agree statistically, not bit for bit. */
+ * the default; 1: read through L1/L2) and the order histories are handed out
+ * in (order 0: longest first, by a per-history estimate of its steps, the
+ * default; 1: index order).  A thread refills itself one history at a time
+ * from a warp-aggregated counter.  Every history keeps its own stream, so
+ * staging and order change no result (bit for bit).  Each CTA size is a
+ * separately compiled kernel whose FP32 multiply-adds the code generator may
+ * fuse differently, so results at another size agree statistically, not bit
+ * for bit. */
 typedef struct {
-  int threads, staging, batch, order;
+  int threads, staging, order;
 } dp_mc_shape;
 int dp_set_mc_shape(dp_ctx* ctx, int family, int precision, const dp_mc_shape* shape);
 int dp_get_mc_shape(const dp_ctx* ctx, int family, int precision, dp_mc_shape* shape);
 /* dp_autotune over the whole shape, one dimension at a time (CTA size, then
- * staging, then batch, then order, each from the best so far): every candidate runs
+ * staging, then order, each from the best so far): every candidate runs
  * run(user) once untimed and once timed.  The best shape stays on the context
  * and goes to *best; tried[i] / ms[i] list the candidates and their times (up
  * to cap), *n_tried their count. */
