@@ -51,7 +51,7 @@ struct DirParams {
   double* efinal;             // 2 per history: final energy, weight
   unsigned long long* counter;
   int* err_flag;
-  int coop_nel, coop_stride;
+  int coop_nel, coop_stride, coop_kmax;  // batched DCS buffers: elements, floats per warp, events
   void* queue;
   void* start;
   void* end;
@@ -410,11 +410,11 @@ __global__ void __launch_bounds__(T, 1) dir_kernel(const __grid_constant__ DirPa
   }
   __syncthreads();
   PathGeo<R> geo{P, meds};
-  float* item = reinterpret_cast<float*>(smem + dir_coop_offset<R>(P)) +
+  float* coop = reinterpret_cast<float*>(smem + dir_coop_offset<R>(P)) +
                 size_t(threadIdx.x >> 5) * P.coop_stride;
   transport_histories<R, PHASE, KCfg<R>::coop>(geo, P.C, P.counter,
-                                               static_cast<DirHandoff<R>*>(P.queue), item,
-                                               item + kItemsPerElement * P.coop_nel);
+                                               static_cast<DirHandoff<R>*>(P.queue), coop,
+                                               P.coop_kmax);
 }
 
 // Contribution 2 w_i w flux_gccly(cos zenith, E, q) of every ended history
@@ -501,8 +501,10 @@ int dir_phase(dp_ctx* ctx, const DirParams& P, size_t smem, long max_blocks) {
 template <class R, int T>
 int dir_launch_t(dp_ctx* ctx, DirParams& P) {
   const int threads = T;
-  P.coop_stride = KCfg<R>::coop ? ((kItemsPerElement + 4) * P.coop_nel + 3) / 4 * 4 : 0;
-  const size_t coop_bytes = size_t(threads / 32) * P.coop_stride * sizeof(float);
+  const int warps = threads / 32;
+  P.coop_kmax = 1;
+  P.coop_stride = KCfg<R>::coop ? coop_floats(P.coop_nel, 1) : 0;
+  size_t coop_bytes = size_t(warps) * P.coop_stride * sizeof(float);
   int dev_smem = 0;
   DP_CHECK_CUDA(ctx, cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
   // stage the leading media that fit (none when the context reads the
@@ -512,6 +514,13 @@ int dir_launch_t(dp_ctx* ctx, DirParams& P) {
   for (int k = stage ? P.n_media : 0; k >= 0; --k) {
     P.n_staged = k;
     if (dir_coop_offset<R>(P) + coop_bytes <= size_t(dev_smem)) break;
+  }
+  if (KCfg<R>::coop) {
+    // the shared memory left after the staged media batches DCS sums
+    P.coop_kmax = coop_kmax(size_t(dev_smem) - std::min(size_t(dev_smem), size_t(dir_coop_offset<R>(P))),
+                            warps, P.coop_nel);
+    P.coop_stride = coop_floats(P.coop_nel, P.coop_kmax);
+    coop_bytes = size_t(warps) * P.coop_stride * sizeof(float);
   }
   const size_t smem = dir_coop_offset<R>(P) + coop_bytes;
   if (smem > size_t(dev_smem)) return fail(ctx, DP_ERR_ARG, "too many media for the fixed-path MC kernel");

@@ -369,7 +369,7 @@ struct McParams {
   double* efinal;
   unsigned long long* counter;  // [0] phase-0 histories taken, [1] phase-1, [2] queued
   int* err_flag;
-  int coop_nel, coop_stride;  // cooperative DCS buffers: elements, floats per warp
+  int coop_nel, coop_stride, coop_kmax;  // batched DCS buffers: elements, floats per warp, events
   void* queue;                // Handoff<R> x n: histories crossing the mode switch
   void* start;                // StartRec<R> x n
   void* end;                  // EndRec<R> x n
@@ -631,20 +631,18 @@ __global__ void __launch_bounds__(T, 1) mc_kernel(const __grid_constant__ McPara
   }
   const Med<R> rock = make_med<R>(base, P.lay, P.info[0]);
   const Med<R> air = make_med<R>(base + P.lay.med_bytes, P.lay, P.info[1]);
-  float* item = reinterpret_cast<float*>(smem + 16 + tables) + size_t(threadIdx.x >> 5) * P.coop_stride;
+  float* coop = reinterpret_cast<float*>(smem + 16 + tables) + size_t(threadIdx.x >> 5) * P.coop_stride;
   if constexpr (POR) {
     const Med<R> porous = make_med<R>(base + 2 * P.lay.med_bytes, P.lay, P.info[2]);
     SlabGeoP<R> geo{P, rock, air, porous};
     transport_histories<R, PHASE, KCfg<R>::coop>(geo, P.C, P.counter,
-                                                 static_cast<HandoffP<R>*>(P.queue), item,
-                                                 item + kItemsPerElement * P.coop_nel,
-                                                 PHASE == 0 ? P.order0 : P.order1);
+                                                 static_cast<HandoffP<R>*>(P.queue), coop,
+                                                 P.coop_kmax, PHASE == 0 ? P.order0 : P.order1);
   } else {
     SlabGeo<R> geo{P, rock, air};
     transport_histories<R, PHASE, KCfg<R>::coop>(geo, P.C, P.counter,
-                                                 static_cast<Handoff<R>*>(P.queue), item,
-                                                 item + kItemsPerElement * P.coop_nel,
-                                                 PHASE == 0 ? P.order0 : P.order1);
+                                                 static_cast<Handoff<R>*>(P.queue), coop,
+                                                 P.coop_kmax, PHASE == 0 ? P.order0 : P.order1);
   }
 }
 
@@ -972,8 +970,10 @@ int launch_mc_t(dp_ctx* ctx, McParams& P) {
   const int threads = T;
   P.coop_nel = std::max(P.info[0].nel, P.info[1].nel);
   if (POR) P.coop_nel = std::max(P.coop_nel, P.info[2].nel);
-  P.coop_stride = KCfg<R>::coop ? ((kItemsPerElement + 4) * P.coop_nel + 3) / 4 * 4 : 0;
-  size_t coop_bytes = size_t(threads / 32) * P.coop_stride * sizeof(float);
+  const int warps = threads / 32;
+  P.coop_kmax = 1;
+  P.coop_stride = KCfg<R>::coop ? coop_floats(P.coop_nel, 1) : 0;
+  size_t coop_bytes = size_t(warps) * P.coop_stride * sizeof(float);
   size_t tables = size_t(POR ? 3 : 2) * P.lay.med_bytes;
   int dev_smem = 0;
   DP_CHECK_CUDA(ctx, cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
@@ -981,6 +981,14 @@ int launch_mc_t(dp_ctx* ctx, McParams& P) {
                      ctx->mc_stage[DP_KERNEL_MC][sizeof(R) == 4] == 0
                  ? 1
                  : 0;
+  if (KCfg<R>::coop) {
+    // the shared memory left after the tables batches DCS sums
+    const size_t used = 16 + (P.staged ? tables : 0);
+    P.coop_kmax = coop_kmax(size_t(dev_smem) - std::min(size_t(dev_smem), used), warps,
+                            P.coop_nel);
+    P.coop_stride = coop_floats(P.coop_nel, P.coop_kmax);
+    coop_bytes = size_t(warps) * P.coop_stride * sizeof(float);
+  }
   size_t smem = 16 + (P.staged ? tables : 0) + coop_bytes;
   if (smem > size_t(dev_smem)) return fail(ctx, DP_ERR_ARG, "media too large for the MC kernel");
   long need = (P.n + threads - 1) / threads;

@@ -468,61 +468,98 @@ static __device__ __noinline__ int del_pick(const double* el, int nel, double ma
 // one ionisation term.
 constexpr int kItemsPerElement = 23;
 
-// Warp-cooperative FP32 form of del_total: every lane evaluates a share of the
-// terms (per-mass scale N_A/(A 1e-3) against FP32 underflow), the components
-// are summed in a fixed order into comp[] (kept for the pick) and the total
-// is reduced in a fixed tree; all 32 lanes call it with the same arguments.
-static __device__ __noinline__ double coop_total(const float* elf, int nel, float fm, double anc,
-                                          double q, float* item, float* comp) {
+// Per-warp buffer of the batched DCS sums, for up to kmax events of a medium
+// with nel elements: the items (kItemsPerElement x nel floats per event), the
+// components (4 x nel per event) and the totals (one per event), then, on a
+// 16-byte boundary, the events' ancestor energies and energy transfers
+// (doubles).  coop_floats is its size in floats.
+__host__ __device__ inline int coop_head(int nel, int kmax) {
+  return (kmax * ((kItemsPerElement + 4) * nel + 1) + 3) / 4 * 4;
+}
+__host__ __device__ inline int coop_floats(int nel, int kmax) {
+  return coop_head(nel, kmax) + 4 * kmax;
+}
+
+// Warp-cooperative FP32 form of del_total for k events of one medium at once
+// (their ancestor energies anc[] and transfers q[] in the buffer).  The terms
+// of all k events are spread over the lanes one kind at a time (pair
+// asymmetry points, photonuclear points, then bremsstrahlung and
+// ionisation), so that a pass evaluates one DCS model on up to 32 terms
+// instead of four models on one event's 23.  Per event the components are
+// summed in a fixed order (kept for the pick) and the total is reduced in a
+// fixed tree, so an event's total does not depend on the events served with
+// it.  All 32 lanes call it with the same arguments.
+static __device__ __noinline__ void coop_batch(const float* elf, int nel, float fm, int k,
+                                               float* buf) {
   const int lane = threadIdx.x & 31;
-  const float fk = float(anc), fq = float(q);
-  const int n_items = kItemsPerElement * nel;
-  for (int it = lane; it < n_items; it += 32) {
-    const int e = it / kItemsPerElement, j = it - e * kItemsPerElement;
+  const int ni = kItemsPerElement * nel, nc = 4 * nel;
+  float* item = buf;
+  float* comp = item + k * ni;
+  float* tot = comp + k * nc;
+  const double* anc = reinterpret_cast<const double*>(buf + coop_head(nel, k));
+  const double* q = anc + k;
+  // pair-production asymmetry points (items 1..12 of an element)
+  for (int f = lane; f < k * nel * 12; f += 32) {
+    const int i = f / (nel * 12), r = f - i * nel * 12, e = r / 12, p = r - e * 12;
     const float* x = elf + kElfStride * e;
-    const float Z = x[0], A = x[1], sc = x[4];
-    float v = 0.f;
-    if (j == 0) {
-      v = dcs_brems<float>(Z, A, fm, fk, fq, sc);
-    } else if (j <= 12) {
-      float tmin;
-      if (pair_range<float>(Z, A, fm, fk, fq, &tmin))
-        v = -pair_point<float>(Z, A, fm, fk, fq, tmin, j - 1, sc);
-    } else if (j <= 21) {
-      float lmin, dx;
-      if (photo_range<float>(Z, A, fm, fk, fq, &lmin, &dx))
-        v = photo_point<float>(Z, A, fm, fk, fq, lmin, dx, j - 13, sc);
-    } else {
-      v = dcs_ionisation<float>(Z, x[2], fm, fk, fq, sc);
-    }
-    item[it] = isfinite(v) ? v : 0.f;
+    const float fk = float(anc[i]), fq = float(q[i]);
+    float v = 0.f, tmin;
+    if (pair_range<float>(x[0], x[1], fm, fk, fq, &tmin))
+      v = -pair_point<float>(x[0], x[1], fm, fk, fq, tmin, p, x[4]);
+    item[i * ni + e * kItemsPerElement + 1 + p] = isfinite(v) ? v : 0.f;
+  }
+  // photonuclear points (items 13..21)
+  for (int f = lane; f < k * nel * 9; f += 32) {
+    const int i = f / (nel * 9), r = f - i * nel * 9, e = r / 9, p = r - e * 9;
+    const float* x = elf + kElfStride * e;
+    const float fk = float(anc[i]), fq = float(q[i]);
+    float v = 0.f, lmin, dx;
+    if (photo_range<float>(x[0], x[1], fm, fk, fq, &lmin, &dx))
+      v = photo_point<float>(x[0], x[1], fm, fk, fq, lmin, dx, p, x[4]);
+    item[i * ni + e * kItemsPerElement + 13 + p] = isfinite(v) ? v : 0.f;
+  }
+  // bremsstrahlung (item 0) and ionisation (item 22)
+  for (int f = lane; f < k * nel * 2; f += 32) {
+    const int i = f / (nel * 2), r = f - i * nel * 2, e = r >> 1, t = r & 1;
+    const float* x = elf + kElfStride * e;
+    const float fk = float(anc[i]), fq = float(q[i]);
+    const float v = t == 0 ? dcs_brems<float>(x[0], x[1], fm, fk, fq, x[4])
+                           : dcs_ionisation<float>(x[0], x[2], fm, fk, fq, x[4]);
+    item[i * ni + e * kItemsPerElement + (t ? 22 : 0)] = isfinite(v) ? v : 0.f;
   }
   __syncwarp();
-  float mine = 0.f;
-  for (int c = lane; c < 4 * nel; c += 32) {
-    const int e = c >> 2, p = c & 3, base = e * kItemsPerElement;
+  // components: per element bremsstrahlung, pair, photonuclear, ionisation,
+  // each times the mass fraction and the ancestor energy
+  for (int f = lane; f < k * nc; f += 32) {
+    const int i = f / nc, c = f - i * nc, e = c >> 2, p = c & 3;
+    const float* it = item + i * ni + e * kItemsPerElement;
     float v;
     if (p == 0) {
-      v = item[base];
+      v = it[0];
     } else if (p == 1) {
       v = 0.f;
-      for (int i = 0; i < 12; ++i) v += item[base + 1 + i];
+      for (int j = 0; j < 12; ++j) v += it[1 + j];
       v = fmaxf(v, 0.f);
     } else if (p == 2) {
       v = 0.f;
-      for (int i = 0; i < 9; ++i) v += item[base + 13 + i];
+      for (int j = 0; j < 9; ++j) v += it[13 + j];
       v = fmaxf(v, 0.f);
     } else {
-      v = item[base + 22];
+      v = it[22];
     }
-    v *= elf[kElfStride * e + 3] * fk;  // fraction x ancestor energy
-    comp[c] = v;
-    mine += v;
+    v *= elf[kElfStride * e + 3] * float(anc[i]);
+    comp[i * nc + c] = v;
   }
-  for (int d = 16; d > 0; d >>= 1) mine += __shfl_down_sync(0xffffffffu, mine, d);
-  mine = __shfl_sync(0xffffffffu, mine, 0);
   __syncwarp();
-  return double(mine);
+  // totals: per event, lane c's running sum of components c, c + 32, ...,
+  // then a fixed tree over the lanes
+  for (int i = 0; i < k; ++i) {
+    float mine = 0.f;
+    for (int c = lane; c < nc; c += 32) mine += comp[i * nc + c];
+    for (int d = 16; d > 0; d >>= 1) mine += __shfl_down_sync(0xffffffffu, mine, d);
+    if (lane == 0) tot[i] = mine;
+  }
+  __syncwarp();
 }
 
 struct DelOut {

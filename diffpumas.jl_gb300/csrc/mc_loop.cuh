@@ -57,6 +57,14 @@ inline int with_threads(int threads, F&& f) {
   }
 }
 
+// Events a warp's batched DCS pass serves at once: as many as `avail` bytes of
+// shared memory hold for `warps` warps, between 1 and 32 (a warp's lanes).
+inline int coop_kmax(size_t avail, int warps, int nel) {
+  for (int k = 32; k > 1; --k)
+    if (size_t(warps) * size_t(coop_floats(nel, k)) * sizeof(float) <= avail) return k;
+  return 1;
+}
+
 // Copies `bytes` (16-byte multiple) from global to shared memory with
 // cp.async.bulk completing on one mbarrier; all threads call it.  Returns
 // false if the wait exceeded `wait_iters` polls (stage_settle has then waited
@@ -114,16 +122,15 @@ __device__ __forceinline__ void drain_histories(G& geo, unsigned long long* coun
 }
 
 // Runs histories until none is left for this phase.  counter[PHASE] hands out
-// history indices, counter[2] counts the hand-off queue.  With COOP, `item`
-// and `comp` are this warp's DCS buffers in shared memory.  `order` (may be
-// null) maps the j-th hand-out to a history (phase 0) or a queue slot (phase
-// 1): the longest-first schedule.
+// history indices, counter[2] counts the hand-off queue.  With COOP, `coop`
+// is this warp's buffer of batched DCS sums in shared memory (coop_floats
+// for up to kmax events).  `order` (may be null) maps the j-th hand-out to a
+// history (phase 0) or a queue slot (phase 1): the longest-first schedule.
 template <class R, int PHASE, bool COOP, class G>
 __device__ __forceinline__ void transport_histories(G& geo, const Consts& C,
                                                     unsigned long long* counter,
-                                                    typename G::Queue* queue, float* item,
-                                                    float* comp,
-                                                    const uint32_t* order = nullptr) {
+                                                    typename G::Queue* queue, float* coop,
+                                                    int kmax, const uint32_t* order = nullptr) {
   const long n = PHASE == 0 ? geo.n0() : long(*(volatile unsigned long long*)(counter + 2));
   typename G::Hist h;
   Stream g;
@@ -157,23 +164,36 @@ __device__ __forceinline__ void transport_histories(G& geo, const Consts& C,
   if constexpr (COOP) {
     const int lane = threadIdx.x & 31;
     for (;;) {
-      // serve the hard events the warp's suspended steps wait for, one at a time
-      unsigned want = __ballot_sync(0xffffffffu, live && h.x.kind != CONT_NONE);
+      // serve the hard events the warp's suspended steps wait for: the
+      // waiting lanes of one medium together, up to kmax at a time
+      const bool waits = live && h.x.kind != CONT_NONE;
+      unsigned want = __ballot_sync(0xffffffffu, waits);
       while (want) {
-        const int L = __ffs(want) - 1;
-        want &= want - 1;
-        const int med = __shfl_sync(0xffffffffu, h.x.medium, L);
-        const double anc = __shfl_sync(0xffffffffu, h.x.anc, L);
-        const double q = __shfl_sync(0xffffffffu, h.x.q, L);
+        const int med = __shfl_sync(0xffffffffu, h.x.medium, __ffs(want) - 1);
+        unsigned batch = __ballot_sync(0xffffffffu, ((want >> lane) & 1u) && h.x.medium == med);
+        while (__popc(batch) > kmax) batch &= ~(1u << (31 - __clz(batch)));
+        want &= ~batch;
+        const bool mine = (batch >> lane) & 1u;
+        const int slot = __popc(batch & ((1u << lane) - 1u));
+        const int k = __popc(batch);
         const Med<R>& m = geo.medium(med);
-        const double total = coop_total(m.elf, m.nel, float(C.mass), anc, q, item, comp);
-        if (lane == L) {
+        double* anc = reinterpret_cast<double*>(coop + coop_head(m.nel, k));
+        if (mine) {
+          anc[slot] = h.x.anc;
+          anc[k + slot] = h.x.q;
+        }
+        __syncwarp();
+        coop_batch(m.elf, m.nel, float(C.mass), k, coop);
+        if (mine) {
+          const int ni = kItemsPerElement * m.nel, nc = 4 * m.nel;
+          const float* comp = coop + k * ni + slot * nc;
+          const double total = double(coop[k * ni + k * nc + slot]);
           h.x.total = total;
           h.x.pick = -1;
           if (h.x.details && total > 0.0) {
             // process and element pick in the reference's order (src/MixedTransport.jl:131-140)
             double u = uni_d(g) * total;
-            const int last = 4 * m.nel - 1;
+            const int last = nc - 1;
             int pick = last;
             for (int c = 0; c <= last; ++c) {
               u -= double(comp[c]);
@@ -209,7 +229,8 @@ __device__ __forceinline__ void transport_histories(G& geo, const Consts& C,
 constexpr int kSchedBuckets = 1024;
 
 // count[b] += number of items whose bucket is b (n items, or *n_dev when
-// n_dev is set); bucket_of(s) gives the bucket of item s.
+// n_dev is set); bucket_of(s) gives the bucket of item s.  The lanes of a
+// warp that share a bucket add once (many items often share one bucket).
 template <class F>
 __global__ void __launch_bounds__(256) sched_count_kernel(long n, const unsigned long long* n_dev,
                                                           F bucket_of, uint32_t* count) {
@@ -217,9 +238,15 @@ __global__ void __launch_bounds__(256) sched_count_kernel(long n, const unsigned
   for (int b = threadIdx.x; b < kSchedBuckets; b += blockDim.x) h[b] = 0;
   __syncthreads();
   const long m = n_dev ? long(*n_dev) : n;
-  for (long s = blockIdx.x * long(blockDim.x) + threadIdx.x; s < m;
-       s += long(gridDim.x) * blockDim.x)
-    atomicAdd(&h[bucket_of(s)], 1u);
+  const int lane = threadIdx.x & 31;
+  // warp-uniform loop over 32-item groups
+  for (long s0 = blockIdx.x * long(blockDim.x) + (threadIdx.x & ~31); s0 < m;
+       s0 += long(gridDim.x) * blockDim.x) {
+    const long s = s0 + lane;
+    const int b = s < m ? bucket_of(s) : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, b);
+    if (b >= 0 && lane == __ffs(peers) - 1) atomicAdd(&h[b], uint32_t(__popc(peers)));
+  }
   __syncthreads();
   for (int b = threadIdx.x; b < kSchedBuckets; b += blockDim.x)
     if (h[b]) atomicAdd(&count[b], h[b]);
@@ -240,15 +267,25 @@ static __global__ void __launch_bounds__(kSchedBuckets) sched_scan_kernel(const 
   }
   offset[kSchedBuckets - 1 - t] = s[t] - count[kSchedBuckets - 1 - t];
 }
-// order[offset[b]++] = s for every item s of bucket b.
+// order[offset[b]++] = s for every item s of bucket b (the lanes of a warp
+// that share a bucket take consecutive places with one atomic).
 template <class F>
 __global__ void __launch_bounds__(256) sched_scatter_kernel(long n, const unsigned long long* n_dev,
                                                             F bucket_of, uint32_t* offset,
                                                             uint32_t* order) {
   const long m = n_dev ? long(*n_dev) : n;
-  for (long s = blockIdx.x * long(blockDim.x) + threadIdx.x; s < m;
-       s += long(gridDim.x) * blockDim.x)
-    order[atomicAdd(&offset[bucket_of(s)], 1u)] = uint32_t(s);
+  const int lane = threadIdx.x & 31;
+  for (long s0 = blockIdx.x * long(blockDim.x) + (threadIdx.x & ~31); s0 < m;
+       s0 += long(gridDim.x) * blockDim.x) {
+    const long s = s0 + lane;
+    const int b = s < m ? bucket_of(s) : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, b);
+    const int leader = __ffs(peers) - 1;
+    uint32_t at = 0;
+    if (b >= 0 && lane == leader) at = atomicAdd(&offset[b], uint32_t(__popc(peers)));
+    at = __shfl_sync(0xffffffffu, at, leader);
+    if (b >= 0) order[at + __popc(peers & ((1u << lane) - 1u))] = uint32_t(s);
+  }
 }
 // Longest-first order of n items (or *n_dev items: the count of a queue
 // filled on the device), count and offset 2 x kSchedBuckets words of
