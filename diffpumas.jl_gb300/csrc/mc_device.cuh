@@ -571,8 +571,9 @@ struct DelOut {
 // true when the event needs that sum; *anc and *denom (pdf r sigma (1 - p_cel))
 // then describe it.  Otherwise *out is the result.
 template <class R>
-static __device__ __noinline__ bool del_begin(const Med<R>& m, const Consts& C, double k, Stream& g, int* status,
-                          DelOut* out, double* anc_out, double* denom) {
+static __device__ __noinline__ bool del_begin(const Med<R>& m, const Consts& C, double k, Stream& g,
+                                              int* status, DelOut* out, double* anc_out,
+                                              double* denom) {
   *out = DelOut{k, 1.0, 0, -1};
   double sigma = double(klookup(m, K_E, K_SIG, R(k), status));
   if (!(sigma > 0.0)) {
@@ -700,9 +701,9 @@ __device__ __forceinline__ bool mixed_event(State<R>& s, Cont<R>& x, const DelOu
 // Runs the event loop from x.event; returns true when it suspended on a DCS sum.
 // The per-step helpers (mixed_run, fluctuate, straggled_end) come in two
 // forms: *_in, inlined into the caller, and an out-of-line function.  The
-// two-layer transport with scattering calls them out of line (its step body
-// is large and bound by instruction fetch); the fixed-path transport, which
-// never scatters, inlines them (1.1x there).
+// two-layer transport's straggled steps call them out of line (that step body
+// is large and bound by instruction fetch); its mixed phase (mixed steps only)
+// and the fixed-path transport, which never scatters, inline them.
 template <class R, bool COOP>
 __device__ __forceinline__ bool mixed_run_in(const Med<R>& m, const Consts& C, State<R>& s, Cont<R>& x,
                                              Stream& g, R energy_limit) {
@@ -1426,7 +1427,7 @@ __device__ __forceinline__ int advance(const Med<R>& rock, const Med<R>& air, co
       }
     } else if (PHASE == 1 && h.mixed) {
       if constexpr (PHASE == 1) {
-        if (mixed_step<R, COOP>(m, C, s, rd, step, g, h.limit, h.x)) {
+        if (mixed_step<R, COOP, true>(m, C, s, rd, step, g, h.limit, h.x)) {
           h.x.kind = CONT_MIXED;
           h.x.medium = med;
           return ADV_WAIT;
@@ -1458,7 +1459,7 @@ __device__ int resume(const Med<R>& rock, const Med<R>& air, const Med<R>* porou
       mixed_end(h.s, x, Emax, h.limit, false);
     } else {
       ++x.event;
-      if (mixed_run<R, true>(m, C, h.s, x, g, h.limit)) {
+      if (mixed_run_in<R, true>(m, C, h.s, x, g, h.limit)) {
         x.kind = CONT_MIXED;
         return ADV_WAIT;
       }
