@@ -216,11 +216,17 @@ def _device_bytes(torch, dev, obj):
 C2_MIX = ([1, 3, 2], [0.70, 0.25, 0.05])  # rock, water, air (1-based material indices)
 # Issue figures of the dominant transport kernels, from ncu captures of small
 # cases of the same kernels (the bound that binds them: instruction issue)
-C2_ISSUE = {"issue_active": 0.254, "lanes_per_inst": 8.1,
+# Issue-slot figures of the dominant kernels, from the ncu captures of the
+# same builds (reduced cases of each workload; the launch tails weigh more there)
+C2_ISSUE = {"issue_active": 0.1325, "lanes_per_inst": 16.07,
             "source": "ncu smsp__issue_active and smsp__thread_inst_executed_per_inst_executed, "
-                      "mc_kernel<float,0,1024> (phase 0) on a 2e5-history c2 case"}
+                      "mc_kernel<float,0,1024> (phase 0, longest-first order) on a 2e5-history "
+                      "c2 case"}
 C4_ISSUE = {"issue_active": 0.263, "lanes_per_inst": 14.2,
             "source": "ncu, mc_kernel<float,1,1024> (mc_mixed_hi) on a reduced c4 case"}
+C1_ISSUE = {"issue_active": 0.206, "lanes_per_inst": 15.88,
+            "source": "ncu, csda32_kernel on the c1 workload (one warp per scheduler, bound by "
+                      "the dependent steps of each warp's longest history)"}
 
 
 def c2_los(dp, n):
@@ -277,14 +283,14 @@ def setup_c2(dp, torch, dev, precision="mixed", scale=1.0):
             # per history: contribution (8 B) and status (4 B) written by the
             # transport kernel and read back by the tally
             "alg_bytes": n * 24,
-            # DRAM bytes of one step from an ncu capture of all seven launches at
-            # 2e5 histories (918.6 MB: the records and the transport kernels'
-            # local-memory write-back), scaled by the histories, which both
-            # grow in proportion with
-            "traffic": int(4593 * n) if precision == "mixed" else None,
-            "note": "SM-issue bound, not HBM: ncu smsp__issue_active 25.4% (phase 0) and "
-                    "39.9% (phase 1) at 1024-thread CTAs; DRAM traffic (mostly local-memory "
-                    "write-back of the spilled stack) is 0.6% of the bandwidth",
+            # DRAM bytes (read + write) of one phase-0 launch from an ncu capture
+            # at 2e5 histories (154.2 MB: start records and the spilled stack's
+            # write-back), scaled by the histories, which it grows in proportion with
+            "traffic": int(771 * n) if precision == "mixed" else None,
+            "note": "SM-issue bound, not HBM: ncu smsp__issue_active 13.3% (phase 0, a "
+                    "tail-heavy 2e5-history case) with 16.1 of 32 lanes per instruction; DRAM "
+                    "traffic (mostly local-memory write-back of the spilled stack) is under 1% "
+                    "of the bandwidth",
             "config": {"workload": "c2: straggled MC with DEL/EHS + Coulomb scattering, rock mixture "
                                    "rock/water/air 0.70/0.25/0.05 (per-history thickness U[20,500] m, "
                                    "density U[2000,2800], elevation U[30,90] deg) under 1 km air, "
@@ -375,7 +381,11 @@ def setup_c4(dp, torch, dev, precision="mixed", scale=1.0):
             **({"check": check} if scale == 1.0 else {}),
             # per history: contribution and status written and read back,
             # CSDA contribution and derivative written and read back
-            "alg_bytes": total * (24 + 32), "traffic": None,
+            "alg_bytes": total * (24 + 32),
+            # DRAM bytes of one mc_mixed_hi launch from an ncu capture of a tenth
+            # of the lines of sight (7.27 GB for ~8.9e5 histories, mostly
+            # local-memory write-back), scaled by the histories
+            "traffic": int(8160 * total) if precision == "mixed" else None,
             "note": "SM-issue bound, not HBM: ncu smsp__issue_active 26.3% (mixed transport)",
             "config": {"workload": "c4: 16384 vertical lines of sight, depth log-uniform 50-2000 m, "
                                    "density U[2400,2800], 64-1024 histories each (uneven), mixed "
@@ -506,7 +516,10 @@ def setup_dir(dp, torch, dev, precision="mixed", scale=1.0):
     info = {"units": batch.total, "unit": "samples/s", "family": "dir",
             "kernel": f"dir_init+dir_{name}_lo+dir_{name}_hi+dir_finish+mc_tally",
             # per history: contribution and status written and read back
-            "alg_bytes": batch.total * 24, "traffic": None,
+            "alg_bytes": batch.total * 24,
+            # DRAM bytes of one dir_mixed_hi launch from an ncu capture of a tenth
+            # of the directions (2.42 GB for 418,816 histories), scaled by the histories
+            "traffic": int(5776 * batch.total) if precision == "mixed" else None,
             "note": "SM-issue bound (one thread per history, table lookups in shared memory)",
             "config": {"workload": "dir: fixed-path MC (compute_directional_flux_mc), 4096 "
                                    "directions x 1024 histories, 32x32x16 cells @ 20 m of rock / "
@@ -555,7 +568,10 @@ def setup_wcsda(dp, torch, dev, precision="mixed", scale=1.0):
             "kernel": "dir_csda32_grad" if precision == "mixed" else "dir_csda_grad",
             # per bin: 40 B geometry + per segment 4 B cell + 8 B length + 8 B w
             # read and 8 B Jacobian value written
-            "alg_bytes": n_dirs * 40 + batch.n_seg * 28, "traffic": None,
+            "alg_bytes": n_dirs * 40 + batch.n_seg * 28,
+            # DRAM bytes of one launch from an ncu capture of a tenth of the
+            # directions (0.44 MB for 409: tables and paths stay in L2), scaled
+            "traffic": int(1076 * n_dirs) if precision == "mixed" else None,
             "note": "SM issue / FP64 pipe bound, not HBM (tables in shared memory, paths in L2)",
             "config": {"workload": "wcsda: water-fraction CSDA flux + d flux/d w per bin, 4096 "
                                    "directions through 32x32x16 cells @ 20 m (w 0 / 0.3), rock to "
@@ -653,6 +669,9 @@ def setup_c1(dp, torch, dev, precision="mixed"):
     info = {"units": n, "unit": "samples/s", "kernel": kernel, "alg_bytes": n * (24 + 16),
             # per history: (E, q, w) in and the contribution and its derivative out
             "dominant": kernel, "dominant_bytes": n * (24 + 16),
+            # DRAM bytes of one csda32_kernel launch (ncu, this workload)
+            "traffic": 89856 if precision == "mixed" else None,
+            "issue": C1_ISSUE if precision == "mixed" else None,
             "config": {"workload": "c1: backward MC CSDA, StandardRock 100 m @ 45 deg, 2650 kg/m3, "
                                    "E 1-100 GeV, 1e4 histories, with d flux/d rho",
                        "n_samples": n, "precision": precision},
