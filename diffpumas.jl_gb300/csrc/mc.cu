@@ -607,13 +607,23 @@ struct SlabGeoP {
   }
 };
 
+// Shared-memory header of the transport kernels: the staging mbarrier, then
+// the medium descriptors (rock, air, porous), one copy per CTA: the helpers
+// that take a medium by reference then read it there instead of from a copy
+// in every thread's stack.
+template <class R>
+constexpr size_t mc_smem_head() {
+  return (16 + 3 * sizeof(Med<R>) + 15) / 16 * 16;
+}
+
 template <class R, int PHASE, int T, bool POR = false>
 __global__ void __launch_bounds__(T, 1) mc_kernel(const __grid_constant__ McParams P) {
   extern __shared__ __align__(16) unsigned char smem[];
+  constexpr size_t head = mc_smem_head<R>();
   const unsigned char* base = P.blob;
   const uint32_t tables = P.staged ? (POR ? 3 : 2) * P.lay.med_bytes : 0;
   if (P.staged) {
-    if (!stage_blob(smem + 16, P.blob, tables, reinterpret_cast<uint64_t*>(smem), P.C.wait_iters)) {
+    if (!stage_blob(smem + head, P.blob, tables, reinterpret_cast<uint64_t*>(smem), P.C.wait_iters)) {
       if (threadIdx.x == 0) atomicExch(P.err_flag, 1);
       const Med<R> none{};
       if constexpr (POR) {
@@ -627,13 +637,17 @@ __global__ void __launch_bounds__(T, 1) mc_kernel(const __grid_constant__ McPara
       }
       return;
     }
-    base = smem + 16;
+    base = smem + head;
   }
-  const Med<R> rock = make_med<R>(base, P.lay, P.info[0]);
-  const Med<R> air = make_med<R>(base + P.lay.med_bytes, P.lay, P.info[1]);
-  float* coop = reinterpret_cast<float*>(smem + 16 + tables) + size_t(threadIdx.x >> 5) * P.coop_stride;
+  Med<R>* meds = reinterpret_cast<Med<R>*>(smem + 16);
+  if (threadIdx.x < (POR ? 3 : 2))
+    meds[threadIdx.x] = make_med<R>(base + threadIdx.x * P.lay.med_bytes, P.lay, P.info[threadIdx.x]);
+  __syncthreads();
+  const Med<R>& rock = meds[0];
+  const Med<R>& air = meds[1];
+  float* coop = reinterpret_cast<float*>(smem + head + tables) + size_t(threadIdx.x >> 5) * P.coop_stride;
   if constexpr (POR) {
-    const Med<R> porous = make_med<R>(base + 2 * P.lay.med_bytes, P.lay, P.info[2]);
+    const Med<R>& porous = meds[2];
     SlabGeoP<R> geo{P, rock, air, porous};
     transport_histories<R, PHASE, KCfg<R>::coop>(geo, P.C, P.counter,
                                                  static_cast<HandoffP<R>*>(P.queue), coop,
@@ -977,19 +991,19 @@ int launch_mc_t(dp_ctx* ctx, McParams& P) {
   size_t tables = size_t(POR ? 3 : 2) * P.lay.med_bytes;
   int dev_smem = 0;
   DP_CHECK_CUDA(ctx, cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
-  P.staged = 16 + tables + coop_bytes <= size_t(dev_smem) &&
+  P.staged = mc_smem_head<R>() + tables + coop_bytes <= size_t(dev_smem) &&
                      ctx->mc_stage[DP_KERNEL_MC][sizeof(R) == 4] == 0
                  ? 1
                  : 0;
   if (KCfg<R>::coop) {
     // the shared memory left after the tables batches DCS sums
-    const size_t used = 16 + (P.staged ? tables : 0);
+    const size_t used = mc_smem_head<R>() + (P.staged ? tables : 0);
     P.coop_kmax = coop_kmax(size_t(dev_smem) - std::min(size_t(dev_smem), used), warps,
                             P.coop_nel);
     P.coop_stride = coop_floats(P.coop_nel, P.coop_kmax);
     coop_bytes = size_t(warps) * P.coop_stride * sizeof(float);
   }
-  size_t smem = 16 + (P.staged ? tables : 0) + coop_bytes;
+  size_t smem = mc_smem_head<R>() + (P.staged ? tables : 0) + coop_bytes;
   if (smem > size_t(dev_smem)) return fail(ctx, DP_ERR_ARG, "media too large for the MC kernel");
   long need = (P.n + threads - 1) / threads;
   long rec_blocks = std::min((P.n + 255) / 256, 152L * 32);
