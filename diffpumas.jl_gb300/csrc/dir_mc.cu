@@ -52,6 +52,7 @@ struct DirParams {
   unsigned long long* counter;
   int* err_flag;
   int coop_nel, coop_stride, coop_kmax;  // batched DCS buffers: elements, floats per warp, events
+  int sync;  // bit k: phase k runs its steps in CTA lockstep
   void* queue;
   void* start;
   void* end;
@@ -414,7 +415,7 @@ __global__ void __launch_bounds__(T, 1) dir_kernel(const __grid_constant__ DirPa
                 size_t(threadIdx.x >> 5) * P.coop_stride;
   transport_histories<R, PHASE, KCfg<R>::coop>(geo, P.C, P.counter,
                                                static_cast<DirHandoff<R>*>(P.queue), coop,
-                                               P.coop_kmax);
+                                               P.coop_kmax, nullptr, ((P.sync >> PHASE) & 1) != 0);
 }
 
 // Contribution 2 w_i w flux_gccly(cos zenith, E, q) of every ended history
@@ -503,6 +504,7 @@ int dir_launch_t(dp_ctx* ctx, DirParams& P) {
   const int threads = T;
   const int warps = threads / 32;
   P.coop_kmax = 1;
+  P.sync = ctx->mc_sync[DP_KERNEL_DIR][sizeof(R) == 4];
   P.coop_stride = KCfg<R>::coop ? coop_floats(P.coop_nel, 1) : 0;
   size_t coop_bytes = size_t(warps) * P.coop_stride * sizeof(float);
   int dev_smem = 0;

@@ -370,6 +370,7 @@ struct McParams {
   unsigned long long* counter;  // [0] phase-0 histories taken, [1] phase-1, [2] queued
   int* err_flag;
   int coop_nel, coop_stride, coop_kmax;  // batched DCS buffers: elements, floats per warp, events
+  int sync;  // bit k: phase k runs its steps in CTA lockstep
   void* queue;                // Handoff<R> x n: histories crossing the mode switch
   void* start;                // StartRec<R> x n
   void* end;                  // EndRec<R> x n
@@ -651,12 +652,14 @@ __global__ void __launch_bounds__(T, 1) mc_kernel(const __grid_constant__ McPara
     SlabGeoP<R> geo{P, rock, air, porous};
     transport_histories<R, PHASE, KCfg<R>::coop>(geo, P.C, P.counter,
                                                  static_cast<HandoffP<R>*>(P.queue), coop,
-                                                 P.coop_kmax, PHASE == 0 ? P.order0 : P.order1);
+                                                 P.coop_kmax, PHASE == 0 ? P.order0 : P.order1,
+                                                 ((P.sync >> PHASE) & 1) != 0);
   } else {
     SlabGeo<R> geo{P, rock, air};
     transport_histories<R, PHASE, KCfg<R>::coop>(geo, P.C, P.counter,
                                                  static_cast<Handoff<R>*>(P.queue), coop,
-                                                 P.coop_kmax, PHASE == 0 ? P.order0 : P.order1);
+                                                 P.coop_kmax, PHASE == 0 ? P.order0 : P.order1,
+                                                 ((P.sync >> PHASE) & 1) != 0);
   }
 }
 
@@ -986,6 +989,7 @@ int launch_mc_t(dp_ctx* ctx, McParams& P) {
   if (POR) P.coop_nel = std::max(P.coop_nel, P.info[2].nel);
   const int warps = threads / 32;
   P.coop_kmax = 1;
+  P.sync = ctx->mc_sync[DP_KERNEL_MC][sizeof(R) == 4];
   P.coop_stride = KCfg<R>::coop ? coop_floats(P.coop_nel, 1) : 0;
   size_t coop_bytes = size_t(warps) * P.coop_stride * sizeof(float);
   size_t tables = size_t(POR ? 3 : 2) * P.lay.med_bytes;
@@ -1116,10 +1120,13 @@ int dp_set_mc_shape(dp_ctx* ctx, int family, int precision, const dp_mc_shape* s
     return fail(ctx, DP_ERR_ARG, "staging is 0 (shared memory) or 1 (L1/L2)");
   if (shape->order != 0 && shape->order != 1)
     return fail(ctx, DP_ERR_ARG, "order is 0 (longest first) or 1 (index order)");
+  if (shape->sync < 0 || shape->sync > 3)
+    return fail(ctx, DP_ERR_ARG, "sync is a mask of the lockstep phases (0 to 3)");
   const int rc = dp_set_mc_threads(ctx, family, precision, shape->threads);
   if (rc) return rc;
   ctx->mc_stage[family][precision] = shape->staging;
   ctx->mc_order[family][precision] = shape->order;
+  ctx->mc_sync[family][precision] = shape->sync;
   return DP_OK;
 }
 
@@ -1128,6 +1135,7 @@ int dp_get_mc_shape(const dp_ctx* ctx, int family, int precision, dp_mc_shape* s
   dp_get_mc_threads(ctx, family, precision, &shape->threads);
   shape->staging = ctx->mc_stage[family][precision];
   shape->order = ctx->mc_order[family][precision];
+  shape->sync = ctx->mc_sync[family][precision];
   return DP_OK;
 }
 
@@ -1173,14 +1181,33 @@ int dp_autotune_shape(dp_ctx* ctx, int family, int precision, int (*run)(void*),
   };
   int list[8];
   const int nt = dp_mc_thread_choices(precision, list, 8);
-  for (int i = 0; i < nt && !rc; ++i) rc = trial(dp_mc_shape{list[i], best.staging, best.order});
+  for (int i = 0; i < nt && !rc; ++i) {
+    dp_mc_shape c = best;
+    c.threads = list[i];
+    rc = trial(c);
+  }
   const dp_mc_shape after_threads = best;
   for (int st = 0; st < 2 && !rc; ++st)
-    if (st != after_threads.staging)
-      rc = trial(dp_mc_shape{after_threads.threads, st, after_threads.order});
+    if (st != after_threads.staging) {
+      dp_mc_shape c = after_threads;
+      c.staging = st;
+      rc = trial(c);
+    }
   const dp_mc_shape after_stage = best;
   for (int od = 0; od < 2 && !rc; ++od)
-    if (od != after_stage.order) rc = trial(dp_mc_shape{after_stage.threads, after_stage.staging, od});
+    if (od != after_stage.order) {
+      dp_mc_shape c = after_stage;
+      c.order = od;
+      rc = trial(c);
+    }
+  // the lockstep mask only changes the mixed-precision kernels
+  const dp_mc_shape after_order = best;
+  for (int sy = 0; sy < 4 && !rc && precision == DP_PREC_MIXED; ++sy)
+    if (sy != after_order.sync) {
+      dp_mc_shape c = after_order;
+      c.sync = sy;
+      rc = trial(c);
+    }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   if (n_tried) *n_tried = count;

@@ -126,11 +126,14 @@ __device__ __forceinline__ void drain_histories(G& geo, unsigned long long* coun
 // is this warp's buffer of batched DCS sums in shared memory (coop_floats
 // for up to kmax events).  `order` (may be null) maps the j-th hand-out to a
 // history (phase 0) or a queue slot (phase 1): the longest-first schedule.
+// With `lockstep` (block-uniform) every warp of the CTA runs its loop
+// iterations in step with the others until the CTA has no history left.
 template <class R, int PHASE, bool COOP, class G>
 __device__ __forceinline__ void transport_histories(G& geo, const Consts& C,
                                                     unsigned long long* counter,
                                                     typename G::Queue* queue, float* coop,
-                                                    int kmax, const uint32_t* order = nullptr) {
+                                                    int kmax, const uint32_t* order = nullptr,
+                                                    bool lockstep = false) {
   const long n = PHASE == 0 ? geo.n0() : long(*(volatile unsigned long long*)(counter + 2));
   typename G::Hist h;
   Stream g;
@@ -212,7 +215,9 @@ __device__ __forceinline__ void transport_histories(G& geo, const Consts& C,
                                             : geo.template advance<true, PHASE>(h, g);
         live = settle(r, &i);
       }
-      if (!__any_sync(0xffffffffu, live)) break;
+      // lockstep: the CTA's warps take their steps together (one block
+      // barrier per step), so that they fetch the same code at the same time
+      if (lockstep ? !__syncthreads_or(live) : !__any_sync(0xffffffffu, live)) break;
     }
   } else {
     while (live) live = settle(geo.template advance<false, PHASE>(h, g), &i);

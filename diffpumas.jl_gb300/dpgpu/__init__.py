@@ -104,14 +104,22 @@ def set_debug_limits(ctx, step_cap=None, event_cap=None, wait_iters=None):
     check(load().dp_set_debug_limits(h, v(step_cap), v(event_cap), v(wait_iters)), h)
 
 
-def set_mc_shape(ctx, family, precision, threads=0, staging=0, order=0):
+def set_mc_shape(ctx, family, precision, threads=0, staging=0, order=0, sync=None):
     """dp_set_mc_shape: CTA size (0: default), table staging (0: shared
-    memory when the media fit, 1: read through L1/L2) and hand-out order (0:
-    longest first, 1: index order) of the persistent transport kernels."""
+    memory when the media fit, 1: read through L1/L2), hand-out order (0:
+    longest first, 1: index order) and lockstep mask (bit k: the warps of a
+    CTA take the steps of phase k together; None keeps the context's) of the
+    persistent transport kernels."""
     from ._lib import DpMcShape
     h = _ctx_of(ctx)
-    sh = DpMcShape(int(threads), int(staging), int(order))
+    if sync is None:
+        sync = get_mc_shape(ctx, family, precision)["sync"]
+    sh = DpMcShape(int(threads), int(staging), int(order), int(sync))
     check(load().dp_set_mc_shape(h, _FAMILY[family], _PRECISION[precision], C.byref(sh)), h)
+
+
+def _shape_dict(s):
+    return {"threads": s.threads, "staging": s.staging, "order": s.order, "sync": s.sync}
 
 
 def get_mc_shape(ctx, family, precision):
@@ -119,14 +127,15 @@ def get_mc_shape(ctx, family, precision):
     h = _ctx_of(ctx)
     sh = DpMcShape()
     check(load().dp_get_mc_shape(h, _FAMILY[family], _PRECISION[precision], C.byref(sh)), h)
-    return {"threads": sh.threads, "staging": sh.staging, "order": sh.order}
+    return _shape_dict(sh)
 
 
 def autotune_shape(ctx, family, precision, run):
     """dp_autotune_shape: CTA size, then table staging, then hand-out order,
-    each chosen by timing run() (the caller's workload on this context) once
-    untimed and once timed per candidate.  Keeps the best on the context and
-    returns (best shape, [(shape, ms), ...])."""
+    then (mixed precision) the lockstep mask, each chosen by timing run() (the
+    caller's workload on this context) once untimed and once timed per
+    candidate.  Keeps the best on the context and returns (best shape,
+    [(shape, ms), ...])."""
     from ._lib import DpMcShape
     h = _ctx_of(ctx)
     lib = load()
@@ -150,8 +159,7 @@ def autotune_shape(ctx, family, precision, run):
     if errors:
         raise errors[0]
     check(rc, h)
-    as_dict = lambda s: {"threads": s.threads, "staging": s.staging, "order": s.order}
-    return as_dict(best), [(as_dict(tried[i]), ms[i]) for i in range(min(n.value, 16))]
+    return _shape_dict(best), [(_shape_dict(tried[i]), ms[i]) for i in range(min(n.value, 16))]
 
 
 def get_mc_threads(ctx, family, precision):

@@ -121,7 +121,8 @@ class DpTetraMesh(C.Structure):
 
 
 class DpMcShape(C.Structure):
-    _fields_ = [("threads", C.c_int), ("staging", C.c_int), ("order", C.c_int)]
+    _fields_ = [("threads", C.c_int), ("staging", C.c_int), ("order", C.c_int),
+                ("sync", C.c_int)]
 
 
 class DpSolveParams(C.Structure):

@@ -114,6 +114,7 @@ end
 struct DpMcShape
     threads::Cint; staging::Cint
     order::Cint                # 0: longest first, 1: index order
+    sync::Cint                 # bit k: phase k steps in CTA lockstep
 end
 
 # ---------------------------------------------------------------- errors, context
@@ -424,7 +425,7 @@ const TUNE_WORK = Ref{Any}()
 run_cb(::Ptr{Cvoid})::Cint = (TUNE_WORK[](); Cint(0))
 function autotune!(g::GPUPhysics, family::Integer, precision::Integer, work)
     TUNE_WORK[] = work
-    best = Ref{DpMcShape}(DpMcShape(0, 0, 0))
+    best = Ref{DpMcShape}(DpMcShape(0, 0, 0, 0))
     tried = Vector{DpMcShape}(undef, 16); ms = zeros(16); n = Ref{Cint}(0)
     check(ccall((:dp_autotune_shape, lib), Cint,
                 (Ptr{Cvoid}, Cint, Cint, Ptr{Cvoid}, Ptr{Cvoid}, Ref{DpMcShape}, Ptr{DpMcShape},

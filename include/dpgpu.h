@@ -129,19 +129,24 @@ int dp_autotune(dp_ctx* ctx, int family, int precision, int (*run)(void* user), 
  * tables live (staging 0: copied to shared memory once per CTA when they fit,
  * the default; 1: read through L1/L2) and the order histories are handed out
  * in (order 0: longest first, by a per-history estimate of its steps, the
- * default; 1: index order).  A thread refills itself one history at a time
+ * default; 1: index order).  sync is a mask of the transport phases (bit 0:
+ * below the mode switch, bit 1: above it) whose steps the warps of a CTA take
+ * in lockstep, one block barrier per step, so that they fetch the same code
+ * at the same time; it applies to DP_PREC_MIXED (default: 1 for DP_KERNEL_MC,
+ * 0 for DP_KERNEL_DIR).  A thread refills itself one history at a time
  * from a warp-aggregated counter.  Every history keeps its own stream, so
- * staging and order change no result (bit for bit).  Each CTA size is a
+ * staging, order and sync change no result (bit for bit).  Each CTA size is a
  * separately compiled kernel whose FP32 multiply-adds the code generator may
  * fuse differently, so results at another size agree statistically, not bit
  * for bit. */
 typedef struct {
-  int threads, staging, order;
+  int threads, staging, order, sync;
 } dp_mc_shape;
 int dp_set_mc_shape(dp_ctx* ctx, int family, int precision, const dp_mc_shape* shape);
 int dp_get_mc_shape(const dp_ctx* ctx, int family, int precision, dp_mc_shape* shape);
 /* dp_autotune over the whole shape, one dimension at a time (CTA size, then
- * staging, then order, each from the best so far): every candidate runs
+ * staging, then order, then for DP_PREC_MIXED the sync mask, each from the
+ * best so far): every candidate runs
  * run(user) once untimed and once timed.  The best shape stays on the context
  * and goes to *best; tried[i] / ms[i] list the candidates and their times (up
  * to cap), *n_tried their count. */

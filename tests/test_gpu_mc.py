@@ -301,19 +301,23 @@ def test_cta_sizes_give_equivalent_histories(dp, phys, media):
 
 
 def test_launch_shapes_give_identical_histories(dp, phys, media):
-    """Table staging (shared memory or L1/L2) and the hand-out order (longest
-    first or by index) do not change a result at one CTA size: every shape
-    gives the same contributions bit for bit, and histories taken out of
+    """Table staging (shared memory or L1/L2), the hand-out order (longest
+    first or by index) and the lockstep mask (the CTA's warps stepping
+    together in either phase) do not change a result at one CTA size: every
+    shape gives the same contributions bit for bit, and histories taken out of
     order all end (none skipped or run twice)."""
     n, seed = 20000, 6
     E, q, w, geo = _histories(n, seed)
     _, air, mix = media
+    assert dp.get_mc_shape(phys, "mc", "mixed")["sync"] == 1  # the default
     runs = {}
+    shapes = [(1024, 0, 0, 1), (1024, 0, 1, 1), (1024, 1, 0, 1), (1024, 1, 1, 1),
+              (1024, 0, 0, 0), (1024, 0, 0, 2), (1024, 1, 1, 3)]
     try:
-        for shape in [(1024, 0, 0), (1024, 0, 1), (1024, 1, 0), (1024, 1, 1)]:
+        for shape in shapes:
             dp.set_mc_shape(phys, "mc", "mixed", *shape)
             assert dp.get_mc_shape(phys, "mc", "mixed") == dict(zip(("threads", "staging",
-                                                                     "order"), shape))
+                                                                     "order", "sync"), shape))
             c, st, ns, _ = dp.mc_histories(phys, mix, air, E, q, w, seed=seed,
                                            precision="mixed", **geo)
             assert np.all(st == 0) and np.all(ns > 0)
@@ -322,16 +326,18 @@ def test_launch_shapes_give_identical_histories(dp, phys, media):
             dp.set_mc_shape(phys, "mc", "mixed", 1024, 2, 0)
         with pytest.raises(ValueError):
             dp.set_mc_shape(phys, "mc", "mixed", 1024, 0, 2)
+        with pytest.raises(ValueError):
+            dp.set_mc_shape(phys, "mc", "mixed", 1024, 0, 0, 4)
     finally:
-        dp.set_mc_shape(phys, "mc", "mixed", 0, 0, 0)
+        dp.set_mc_shape(phys, "mc", "mixed", 0, 0, 0, 1)
     for shape, c in runs.items():
-        np.testing.assert_array_equal(c, runs[(1024, 0, 0)], err_msg=str(shape))
+        np.testing.assert_array_equal(c, runs[shapes[0]], err_msg=str(shape))
 
 
 def test_autotune_shape_searches_every_dimension(dp, phys, media):
     """dp_autotune_shape: the CTA sizes, then the other staging, then the
-    other order, each timed after an untimed run; the fastest shape stays on
-    the context."""
+    other order, then the other lockstep masks, each timed after an untimed
+    run; the fastest shape stays on the context."""
     _, air, mix = media
     los = dp.make_los([4000], thickness=100.0, density=2650.0, elevation=60.0, energy_min=1.0,
                       energy_max=1e4, air_height=1000.0)
@@ -344,15 +350,16 @@ def test_autotune_shape_searches_every_dimension(dp, phys, media):
     try:
         best, tried = dp.autotune_shape(phys, "mc", "mixed", run)
         n_sizes = len(dp.mc_thread_choices("mixed"))
-        assert len(tried) == n_sizes + 1 + 1 and len(calls) == 2 * len(tried)
+        assert len(tried) == n_sizes + 1 + 1 + 3 and len(calls) == 2 * len(tried)
         assert {s["threads"] for s, _ in tried} == set(dp.mc_thread_choices("mixed"))
         assert {s["staging"] for s, _ in tried} == {0, 1}
         assert {s["order"] for s, _ in tried} == {0, 1}
+        assert {s["sync"] for s, _ in tried} == {0, 1, 2, 3}
         assert all(v > 0 for _, v in tried)
         assert dp.get_mc_shape(phys, "mc", "mixed") == best
         assert best in [s for s, _ in tried]
     finally:
-        dp.set_mc_shape(phys, "mc", "mixed", 0, 0, 0)
+        dp.set_mc_shape(phys, "mc", "mixed", 0, 0, 0, 1)
 
 
 def test_autotune_keeps_the_fastest_size(dp, phys, media):
