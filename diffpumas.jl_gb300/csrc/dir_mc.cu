@@ -357,7 +357,7 @@ struct PathGeo {
     Cont<R>& x = h.x;
     const Med<R>& m = meds[x.medium];
     x.kind = CONT_NONE;
-    DelOut d = del_end(x.anc, x.denom, x.total, x.pick);
+    const DelOutT<R> d = del_end(x.anc, x.denom, x.total, x.pick);
     if constexpr (PHASE == 1) {
       const R Emax = m.kcol(K_E)[m.nk - 1];
       if (mixed_event(h.s, x, d)) {
@@ -373,7 +373,7 @@ struct PathGeo {
     } else {
       Loc<R> Li = locate(m, x.r0);
       // the fixed-path transport never scatters (x.flag is 0)
-      const R moved = straggled_end_in(m, P.C, h.s, Li, R(0), x.r0, R(d.energy), x.r1, x.r2, d.weight,
+      const R moved = straggled_end_in(m, P.C, h.s, Li, R(0), x.r0, d.energy, x.r1, x.r2, d.weight,
                                        d.process, d.element, true, false, R(0), x.r3, x.a, true,
                                        false, g);
       return step_end(h, moved);

@@ -264,6 +264,7 @@ static void pack(const dp_mixture* m, const Layout& L, unsigned char* out) {
     f[2] = float(x[2]);
     f[3] = float(x[3]);
     f[4] = float(kAvogadro / (x[1] * 0.001));
+    f[5] = float(x[4]);  // nuclear RMS radius (DEL polar angles)
   }
   // index tables of the inverse lookups (origins and widths in R)
   R* prm = reinterpret_cast<R*>(reinterpret_cast<double*>(out) + kMaxEl * kElStride);
@@ -870,6 +871,8 @@ int check_cfg(dp_ctx* ctx, const dp_physics* ph, const dp_mc_config* cfg, Consts
   C->mass_f = float(C->mass);
   C->ctau_f = float(C->ctau);
   C->elastic_ratio_f = float(C->elastic_ratio);
+  C->cutoff_f = float(C->cutoff);
+  C->lcut_f = float(-std::log(C->cutoff));
   C->step_cap = step_cap(ctx);
   C->event_cap = event_cap(ctx);
   C->wait_iters = stage_wait(ctx);

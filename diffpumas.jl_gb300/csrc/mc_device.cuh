@@ -64,8 +64,8 @@ struct Layout {
   int nbp, nbk;        // index bins of the physics and kernel columns
   uint32_t o_elf;      // byte offset of the FP32 element table (kElfStride floats each)
 };
-// FP32 element table for the cooperative DCS sums: Z, A, I, fraction,
-// N_A / (A 1e-3) (per-mass scale).
+// FP32 element table for the cooperative DCS sums and the FP32 polar angles:
+// Z, A, I, fraction, N_A / (A 1e-3) (per-mass scale), nuclear RMS radius (m).
 constexpr int kElfStride = 8;
 
 // Inverse lookups (energy from a range or hazard value) start from an index
@@ -131,6 +131,7 @@ struct Consts {
   double thr_low, thr;  // mode switch and source ceiling (GeV)
   float thr_low_f, thr_f;  // the same in FP32 (exact for the FP32 transport)
   float mass_f, ctau_f, elastic_ratio_f;
+  float cutoff_f, lcut_f;  // cutoff and -log(cutoff) in FP32
   int straggling, scattering;
   // loop caps and the table-staging wait limit of the launch
   int step_cap, event_cap, wait_iters;
@@ -471,8 +472,8 @@ constexpr int kItemsPerElement = 23;
 // Per-warp buffer of the batched DCS sums, for up to kmax events of a medium
 // with nel elements: the items (kItemsPerElement x nel floats per event), the
 // components (4 x nel per event) and the totals (one per event), then, on a
-// 16-byte boundary, the events' ancestor energies and energy transfers
-// (doubles).  coop_floats is its size in floats.
+// 16-byte boundary, the events' ancestor energies and energy transfers.
+// coop_floats is its size in floats.
 __host__ __device__ inline int coop_head(int nel, int kmax) {
   return (kmax * ((kItemsPerElement + 4) * nel + 1) + 3) / 4 * 4;
 }
@@ -496,13 +497,13 @@ static __device__ __noinline__ void coop_batch(const float* elf, int nel, float 
   float* item = buf;
   float* comp = item + k * ni;
   float* tot = comp + k * nc;
-  const double* anc = reinterpret_cast<const double*>(buf + coop_head(nel, k));
-  const double* q = anc + k;
+  const float* anc = buf + coop_head(nel, k);
+  const float* q = anc + k;
   // pair-production asymmetry points (items 1..12 of an element)
   for (int f = lane; f < k * nel * 12; f += 32) {
     const int i = f / (nel * 12), r = f - i * nel * 12, e = r / 12, p = r - e * 12;
     const float* x = elf + kElfStride * e;
-    const float fk = float(anc[i]), fq = float(q[i]);
+    const float fk = anc[i], fq = q[i];
     float v = 0.f, tmin;
     if (pair_range<float>(x[0], x[1], fm, fk, fq, &tmin))
       v = -pair_point<float>(x[0], x[1], fm, fk, fq, tmin, p, x[4]);
@@ -512,7 +513,7 @@ static __device__ __noinline__ void coop_batch(const float* elf, int nel, float 
   for (int f = lane; f < k * nel * 9; f += 32) {
     const int i = f / (nel * 9), r = f - i * nel * 9, e = r / 9, p = r - e * 9;
     const float* x = elf + kElfStride * e;
-    const float fk = float(anc[i]), fq = float(q[i]);
+    const float fk = anc[i], fq = q[i];
     float v = 0.f, lmin, dx;
     if (photo_range<float>(x[0], x[1], fm, fk, fq, &lmin, &dx))
       v = photo_point<float>(x[0], x[1], fm, fk, fq, lmin, dx, p, x[4]);
@@ -522,7 +523,7 @@ static __device__ __noinline__ void coop_batch(const float* elf, int nel, float 
   for (int f = lane; f < k * nel * 2; f += 32) {
     const int i = f / (nel * 2), r = f - i * nel * 2, e = r >> 1, t = r & 1;
     const float* x = elf + kElfStride * e;
-    const float fk = float(anc[i]), fq = float(q[i]);
+    const float fk = anc[i], fq = q[i];
     const float v = t == 0 ? dcs_brems<float>(x[0], x[1], fm, fk, fq, x[4])
                            : dcs_ionisation<float>(x[0], x[2], fm, fk, fq, x[4]);
     item[i * ni + e * kItemsPerElement + (t ? 22 : 0)] = isfinite(v) ? v : 0.f;
@@ -547,7 +548,7 @@ static __device__ __noinline__ void coop_batch(const float* elf, int nel, float 
     } else {
       v = it[22];
     }
-    v *= elf[kElfStride * e + 3] * float(anc[i]);
+    v *= elf[kElfStride * e + 3] * anc[i];
     comp[i * nc + c] = v;
   }
   __syncwarp();
@@ -562,10 +563,12 @@ static __device__ __noinline__ void coop_batch(const float* elf, int nel, float 
   __syncwarp();
 }
 
-struct DelOut {
-  double energy, weight;
+template <class R>
+struct DelOutT {
+  R energy, weight;
   int process, element;  // process 0: null CEL event
 };
+using DelOut = DelOutT<double>;
 
 // reverse_del_event (src/MixedTransport.jl:111-142) up to the DCS sum.  Returns
 // true when the event needs that sum; *anc and *denom (pdf r sigma (1 - p_cel))
@@ -599,10 +602,47 @@ static __device__ __noinline__ bool del_begin(const Med<R>& m, const Consts& C, 
   *denom = pdf * rr * sigma * (1.0 - pcel);
   return true;
 }
+// The same in FP32 for the mixed-precision transport: the same draws and
+// decisions, with -log(cutoff) taken from the launch constants,
+// log(onset / (onset - k)) as log1p(k / (onset - k)), 1 - nu formed without
+// cancellation (for xmax = 1, D - 1 = (1/xmin - 1)(1 - u) with D = 1/nu) and
+// the energy transfer as anc nu.  *q receives the transfer.
+static __device__ __noinline__ bool del_begin32(const Med<float>& m, const Consts& C, float k, Stream& g,
+                                                int* status, DelOutT<float>* out, float* anc_out,
+                                                float* q_out, float* denom) {
+  *out = DelOutT<float>{k, 1.f, 0, -1};
+  const float sigma = klookup(m, K_E, K_SIG, k, status);
+  if (!(sigma > 0.f)) {
+    *status |= ST_ZERO_RATE;
+    return false;
+  }
+  const float onset = m.onset, cut = C.cutoff_f, lc = C.lcut_f;
+  const float pcel = k >= onset ? 0.f : lc / (lc + log1pf(k / (onset - k)));
+  if (pcel > 0.f && uni<float>(g) < pcel) {
+    out->weight = 1.f / pcel;
+    return false;
+  }
+  const float me = float(kElectronMass), M = C.mass_f;
+  const float xmax = k < 0.5f * (M - me) * (M - me) / me
+                         ? fminf(1.f, 2.f * me * (k + 2.f * M) / ((M + me) * (M + me)))
+                         : 1.f;
+  const float xmin = k >= onset * (1.f - cut) ? cut : 1.f - k / onset;
+  if (!(xmax > xmin)) return false;
+  const float ixmin = 1.f / xmin, invnorm = ixmin - 1.f / xmax;
+  const float u = uni<float>(g);
+  const float D = ixmin - u * invnorm, nu = 1.f / D;
+  const float rr = xmax >= 1.f ? invnorm * (1.f - u) / D : 1.f - nu;
+  const float anc = k / rr;
+  *anc_out = anc;
+  *q_out = anc * nu;
+  *denom = rr * sigma * (1.f - pcel) / (invnorm * nu * nu);
+  return true;
+}
 // The rest of reverse_del_event once the DCS sum (and, with details, the
 // picked component) is known.
-__device__ __forceinline__ DelOut del_end(double anc, double denom, double total, int pick) {
-  DelOut r{anc, total / denom, 0, -1};
+template <class R>
+__device__ __forceinline__ DelOutT<R> del_end(R anc, R denom, R total, int pick) {
+  DelOutT<R> r{anc, total / denom, 0, -1};
   if (pick >= 0) {
     r.process = pick % 4 + 1;
     r.element = pick / 4;
@@ -662,9 +702,9 @@ struct Cont {
   R moved;             // path length of a completed straggled step (when asked)
   R r0, r1, r2, r3;
   int event, kind, medium, flag;
-  double anc, q, denom;  // the pending event: ancestor, energy transfer, weight denominator
+  R anc, q, denom;  // the pending event: ancestor, energy transfer, weight denominator
   int details;
-  double total;          // answer: DCS sum and picked component
+  R total;          // answer: DCS sum and picked component
   int pick;
 };
 enum : int { CONT_NONE = 0, CONT_MIXED = 1, CONT_STRAG = 2 };
@@ -692,9 +732,9 @@ __device__ void mixed_end(State<R>& s, const Cont<R>& x, R Emax, R energy_limit,
 }
 // Applies a hard event; true when the history's weight vanished.
 template <class R>
-__device__ __forceinline__ bool mixed_event(State<R>& s, Cont<R>& x, const DelOut& d) {
-  x.r0 = R(d.energy);
-  x.r1 = R(double(x.r1) * d.weight);
+__device__ __forceinline__ bool mixed_event(State<R>& s, Cont<R>& x, const DelOutT<R>& d) {
+  x.r0 = d.energy;
+  x.r1 = x.r1 * d.weight;
   if (!(isfinite(x.r1) && x.r1 >= R(0))) s.status |= ST_BAD_WEIGHT;
   return x.r1 == R(0);
 }
@@ -741,14 +781,13 @@ __device__ __forceinline__ bool mixed_run_in(const Med<R>& m, const Consts& C, S
       mixed_end(s, x, Emax, energy_limit, false);
       return false;
     }
-    DelOut d;
-    if (COOP) {
-      if (del_begin(m, C, double(pre), g, &s.status, &d, &x.anc, &x.denom)) {
-        x.q = x.anc - double(pre);
+    DelOutT<R> d;
+    if constexpr (COOP) {  // FP32
+      if (del_begin32(m, C, pre, g, &s.status, &d, &x.anc, &x.q, &x.denom)) {
         x.details = 0;
         return true;
       }
-    } else {
+    } else {  // FP64
       d = reverse_del(m, C, double(pre), g, false, &s.status);
     }
     if (mixed_event(s, x, d)) {
@@ -1052,6 +1091,38 @@ static __device__ __noinline__ double polar_brems(double m, double ki, double kf
   }
   return 0.0;
 }
+// The same in FP32, with every term scaled by the smallest angle mu0: in
+// units of mu0 the density and the score stay of order one (their FP64 form
+// reaches mu0^-4, beyond the FP32 range for small mu0).  t = mu / mu0 and
+// s = 1 + t; the draws are the same.
+static __device__ __noinline__ float polar_brems32(float m, float ki, float kf, float RN, Stream& g) {
+  const float E = ki + m, nu = ki - kf;
+  if (nu <= 0.f || E <= m) return 0.f;
+  const float y = nu / E, tmp = 0.5f * m * nu / (E * (E - nu)), mu0 = tmp * tmp;
+  const float C1 = 2.f * (1.f - y) + y * y, C2 = 4.f * (1.f - y);
+  const float t2 = m * RN / float(kHbarC), muni = t2 * t2 / 6.f;
+  if (sqrtf(mu0) - mu0 < 0.f) return 0.f;
+  const float qr0 = muni * mu0, den0 = mu0 + qr0;
+  if (den0 <= 0.f || (1.f + qr0) <= 0.f) return 0.f;
+  const float x0 = (1.f + 2.f * qr0) * logf((1.f + qr0) / den0) -
+                   (1.f - mu0) * (1.f + 2.f * muni) / (1.f + muni);
+  if (x0 <= 0.f) return 0.f;
+  for (int it = 0; it < 100; ++it) {
+    const float r0r = uni<float>(g), r1 = uni<float>(g);
+    const float t = r0r / (mu0 + 1.f - r0r), sc = 1.f + t, s2 = sc * sc;
+    const float score = r1 * C1 / s2;
+    float pdf = C1 / s2 - t * C2 / (s2 * s2);
+    if (score > pdf) continue;
+    const float q = muni * s2, r = mu0 * s2, qr = q * r;
+    if (qr > 1e5f) continue;
+    const float den = r + qr;
+    if (den <= 0.f || (1.f + qr) <= 0.f) continue;
+    const float x = (1.f + 2.f * qr) * logf((1.f + qr) / den) - (1.f - r) * (1.f + 2.f * q) / (1.f + q);
+    pdf *= x / x0;
+    if (score <= pdf) return t * mu0;
+  }
+  return 0.f;
+}
 static __device__ __noinline__ double polar_photo(double ml, double ki, double kf, Stream& g) {
   double M = 0.5 * (kProtonMass + kNeutronMass), q = ki - kf, E = ki + ml, ml2 = ml * ml;
   double Q2min = ml2 * (q * q - 0.5 * ml2) / (E * (E - q));
@@ -1080,7 +1151,7 @@ __device__ __forceinline__ double polar_ioni(double m, double ki, double kf) {
 template <class R>
 __device__ __forceinline__ R straggled_end_in(const Med<R>& m, const Consts& C, State<R>& s,
                                               const Loc<R>& Li, R lb0, R ki, R kf, R ckf, R dX,
-                                              double dw,
+                                              R dw,
                                               int proc, int elem, bool del, bool ehs, R k_ehs,
                                               R density, R step, bool shortened, bool scattering,
                                               Stream& g) {
@@ -1090,11 +1161,17 @@ __device__ __forceinline__ R straggled_end_in(const Med<R>& m, const Consts& C, 
   const Loc<R> Lc = locate(m, ckf);  // soft scattering and the weight update
   if (scattering) {
     if (del && proc > 0) {
-      const double* e = m.el + kElStride * elem;
-      double mu = proc == 1 || proc == 2 ? polar_brems(C.mass, double(kf), double(ckf), e[4], g)
-                  : proc == 3            ? polar_photo(C.mass, double(kf), double(ckf), g)
-                                         : polar_ioni(C.mass, double(kf), double(ckf));
-      if (mu > 0.0) rotate(s, R(mu), g);
+      R mu;
+      if (proc == 1 || proc == 2) {
+        if constexpr (sizeof(R) == 8)
+          mu = polar_brems(C.mass, kf, ckf, m.el[kElStride * elem + 4], g);
+        else
+          mu = polar_brems32(C.mass_f, kf, ckf, m.elf[kElfStride * elem + 5], g);
+      } else {
+        mu = R(proc == 3 ? polar_photo(C.mass, double(kf), double(ckf), g)
+                         : polar_ioni(C.mass, double(kf), double(ckf)));
+      }
+      if (mu > R(0)) rotate(s, mu, g);
     }
     if (ehs) {
       R mu;
@@ -1113,14 +1190,14 @@ __device__ __forceinline__ R straggled_end_in(const Med<R>& m, const Consts& C, 
   if (sizeof(R) == 4) da = shortened ? dX / density : step;
   alt_add(s.z, -(da * oz));
   R wf = at(m, Lc, MC_MS) / at(m, Li, MC_MS);
-  if (sizeof(R) == 4) s.w = s.w * wf * exp(-pt / C.ctau_r<R>()) * R(dw);
+  if (sizeof(R) == 4) s.w = s.w * wf * exp(-pt / C.ctau_r<R>()) * dw;
   else s.w = R(double(s.w * wf * exp(-pt / C.ctau_r<R>())) * dw);
   s.E = kf;
   return da;
 }
 template <class R>
 static __device__ __noinline__ R straggled_end(const Med<R>& m, const Consts& C, State<R>& s, const Loc<R>& Li,
-                                               R lb0, R ki, R kf, R ckf, R dX, double dw, int proc,
+                                               R lb0, R ki, R kf, R ckf, R dX, R dw, int proc,
                                                int elem, bool del, bool ehs, R k_ehs, R density,
                                                R step, bool shortened, bool scattering, Stream& g) {
   return straggled_end_in<R>(m, C, s, Li, lb0, ki, kf, ckf, dX, dw, proc, elem, del, ehs, k_ehs,
@@ -1182,14 +1259,13 @@ __device__ bool straggled_step(const Med<R>& m, const Consts& C, State<R>& s, co
     if (X_del <= X_ehs) ehs = false;
     else del = false;
   }
-  double dw = 1.0;
+  R dw = R(1);
   R ckf = kf;
   int proc = 0, elem = -1;
   if (del) {
-    DelOut d;
-    if (COOP) {
-      if (del_begin(m, C, double(k_del), g, &s.status, &d, &x.anc, &x.denom)) {
-        x.q = x.anc - double(k_del);
+    DelOutT<R> d;
+    if constexpr (COOP) {  // FP32
+      if (del_begin32(m, C, k_del, g, &s.status, &d, &x.anc, &x.q, &x.denom)) {
         x.details = 1;
         x.a = step;
         x.r0 = ki;
@@ -1199,11 +1275,11 @@ __device__ bool straggled_step(const Med<R>& m, const Consts& C, State<R>& s, co
         x.flag = scattering;
         return true;
       }
-    } else {
+    } else {  // FP64
       d = reverse_del(m, C, double(k_del), g, true, &s.status);
     }
     ckf = k_del;
-    kf = R(d.energy);
+    kf = d.energy;
     dw = d.weight;
     proc = d.process;
     elem = d.element;
@@ -1452,7 +1528,7 @@ __device__ int resume(const Med<R>& rock, const Med<R>& air, const Med<R>* porou
   Cont<R>& x = h.x;
   const Med<R>& m = x.medium == 0 ? rock : (POR && x.medium == 2 ? *porous : air);
   x.kind = CONT_NONE;
-  DelOut d = del_end(x.anc, x.denom, x.total, x.pick);
+  const DelOutT<R> d = del_end(x.anc, x.denom, x.total, x.pick);
   if constexpr (PHASE == 1) {
     const R Emax = m.kcol(K_E)[m.nk - 1];
     if (mixed_event(h.s, x, d)) {
@@ -1467,7 +1543,7 @@ __device__ int resume(const Med<R>& rock, const Med<R>& air, const Med<R>* porou
   } else {
     Loc<R> Li = locate(m, x.r0);
     const R lb0 = x.flag ? transport_path(m, Li) : R(0);
-    straggled_end(m, C, h.s, Li, lb0, x.r0, R(d.energy), x.r1, x.r2, d.weight, d.process, d.element,
+    straggled_end(m, C, h.s, Li, lb0, x.r0, d.energy, x.r1, x.r2, d.weight, d.process, d.element,
                   true, false, R(0), x.r3, x.a, true, x.flag != 0, g);
   }
   return step_done(h, C);

@@ -180,27 +180,27 @@ __device__ __forceinline__ void transport_histories(G& geo, const Consts& C,
         const int slot = __popc(batch & ((1u << lane) - 1u));
         const int k = __popc(batch);
         const Med<R>& m = geo.medium(med);
-        double* anc = reinterpret_cast<double*>(coop + coop_head(m.nel, k));
+        float* anc = coop + coop_head(m.nel, k);
         if (mine) {
           anc[slot] = h.x.anc;
           anc[k + slot] = h.x.q;
         }
         __syncwarp();
-        coop_batch(m.elf, m.nel, float(C.mass), k, coop);
+        coop_batch(m.elf, m.nel, C.mass_f, k, coop);
         if (mine) {
           const int ni = kItemsPerElement * m.nel, nc = 4 * m.nel;
           const float* comp = coop + k * ni + slot * nc;
-          const double total = double(coop[k * ni + k * nc + slot]);
+          const float total = coop[k * ni + k * nc + slot];
           h.x.total = total;
           h.x.pick = -1;
-          if (h.x.details && total > 0.0) {
+          if (h.x.details && total > 0.f) {
             // process and element pick in the reference's order (src/MixedTransport.jl:131-140)
-            double u = uni_d(g) * total;
+            float u = uni<float>(g) * total;
             const int last = nc - 1;
             int pick = last;
             for (int c = 0; c <= last; ++c) {
-              u -= double(comp[c]);
-              if (u <= 0.0) {
+              u -= comp[c];
+              if (u <= 0.f) {
                 pick = c;
                 break;
               }
