@@ -52,7 +52,8 @@ struct DirParams {
   unsigned long long* counter;
   int* err_flag;
   int coop_nel, coop_stride, coop_kmax;  // batched DCS buffers: elements, floats per warp, events
-  int sync;  // bit k: phase k runs its steps in CTA lockstep
+  int coop_kc;  // events per chunk of the CTA buffer (lockstep phases)
+  int sync;     // bit k: phase k runs its steps in CTA lockstep
   void* queue;
   void* start;
   void* end;
@@ -411,11 +412,11 @@ __global__ void __launch_bounds__(T, 1) dir_kernel(const __grid_constant__ DirPa
   }
   __syncthreads();
   PathGeo<R> geo{P, meds};
-  float* coop = reinterpret_cast<float*>(smem + dir_coop_offset<R>(P)) +
-                size_t(threadIdx.x >> 5) * P.coop_stride;
+  float* coop = reinterpret_cast<float*>(smem + dir_coop_offset<R>(P));
   transport_histories<R, PHASE, KCfg<R>::coop>(geo, P.C, P.counter,
                                                static_cast<DirHandoff<R>*>(P.queue), coop,
-                                               P.coop_kmax, nullptr, ((P.sync >> PHASE) & 1) != 0);
+                                               P.coop_stride, P.coop_kmax, P.coop_kc, P.coop_nel,
+                                               nullptr, ((P.sync >> PHASE) & 1) != 0);
 }
 
 // Contribution 2 w_i w flux_gccly(cos zenith, E, q) of every ended history
@@ -504,6 +505,7 @@ int dir_launch_t(dp_ctx* ctx, DirParams& P) {
   const int threads = T;
   const int warps = threads / 32;
   P.coop_kmax = 1;
+  P.coop_kc = 0;
   P.sync = ctx->mc_sync[DP_KERNEL_DIR][sizeof(R) == 4];
   P.coop_stride = KCfg<R>::coop ? coop_floats(P.coop_nel, 1) : 0;
   size_t coop_bytes = size_t(warps) * P.coop_stride * sizeof(float);
@@ -523,6 +525,7 @@ int dir_launch_t(dp_ctx* ctx, DirParams& P) {
                             warps, P.coop_nel);
     P.coop_stride = coop_floats(P.coop_nel, P.coop_kmax);
     coop_bytes = size_t(warps) * P.coop_stride * sizeof(float);
+    P.coop_kc = cta_kc(warps * P.coop_stride, P.coop_nel, threads);
   }
   const size_t smem = dir_coop_offset<R>(P) + coop_bytes;
   if (smem > size_t(dev_smem)) return fail(ctx, DP_ERR_ARG, "too many media for the fixed-path MC kernel");

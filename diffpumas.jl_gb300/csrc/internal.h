@@ -44,9 +44,10 @@ struct dp_ctx {
   int mc_stage[2][2] = {{0, 0}, {0, 0}};
   // Hand-out order of the histories (0: longest first, 1: index order).
   int mc_order[2][2] = {{0, 0}, {0, 0}};
-  // CTA-lockstep phases (bit k: phase k), mixed precision only: the
-  // two-layer transport below its mode switch by default.
-  int mc_sync[2][2] = {{0, 1}, {0, 0}};
+  // CTA-lockstep phases (bit k: phase k), mixed precision only: both phases
+  // of the two-layer transport and the mixed phase of the fixed-path one by
+  // default.
+  int mc_sync[2][2] = {{0, 3}, {0, 2}};
   // Energy nodes of the last host-pointer tomography evaluation (energies,
   // charges, weights) and their device copy: a call with the same nodes
   // uploads none.

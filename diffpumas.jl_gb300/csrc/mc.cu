@@ -371,7 +371,8 @@ struct McParams {
   unsigned long long* counter;  // [0] phase-0 histories taken, [1] phase-1, [2] queued
   int* err_flag;
   int coop_nel, coop_stride, coop_kmax;  // batched DCS buffers: elements, floats per warp, events
-  int sync;  // bit k: phase k runs its steps in CTA lockstep
+  int coop_kc;  // events per chunk of the CTA buffer (lockstep phases)
+  int sync;     // bit k: phase k runs its steps in CTA lockstep
   void* queue;                // Handoff<R> x n: histories crossing the mode switch
   void* start;                // StartRec<R> x n
   void* end;                  // EndRec<R> x n
@@ -647,19 +648,21 @@ __global__ void __launch_bounds__(T, 1) mc_kernel(const __grid_constant__ McPara
   __syncthreads();
   const Med<R>& rock = meds[0];
   const Med<R>& air = meds[1];
-  float* coop = reinterpret_cast<float*>(smem + head + tables) + size_t(threadIdx.x >> 5) * P.coop_stride;
+  float* coop = reinterpret_cast<float*>(smem + head + tables);
   if constexpr (POR) {
     const Med<R>& porous = meds[2];
     SlabGeoP<R> geo{P, rock, air, porous};
     transport_histories<R, PHASE, KCfg<R>::coop>(geo, P.C, P.counter,
                                                  static_cast<HandoffP<R>*>(P.queue), coop,
-                                                 P.coop_kmax, PHASE == 0 ? P.order0 : P.order1,
+                                                 P.coop_stride, P.coop_kmax, P.coop_kc, P.coop_nel,
+                                                 PHASE == 0 ? P.order0 : P.order1,
                                                  ((P.sync >> PHASE) & 1) != 0);
   } else {
     SlabGeo<R> geo{P, rock, air};
     transport_histories<R, PHASE, KCfg<R>::coop>(geo, P.C, P.counter,
                                                  static_cast<Handoff<R>*>(P.queue), coop,
-                                                 P.coop_kmax, PHASE == 0 ? P.order0 : P.order1,
+                                                 P.coop_stride, P.coop_kmax, P.coop_kc, P.coop_nel,
+                                                 PHASE == 0 ? P.order0 : P.order1,
                                                  ((P.sync >> PHASE) & 1) != 0);
   }
 }
@@ -992,6 +995,7 @@ int launch_mc_t(dp_ctx* ctx, McParams& P) {
   if (POR) P.coop_nel = std::max(P.coop_nel, P.info[2].nel);
   const int warps = threads / 32;
   P.coop_kmax = 1;
+  P.coop_kc = 0;
   P.sync = ctx->mc_sync[DP_KERNEL_MC][sizeof(R) == 4];
   P.coop_stride = KCfg<R>::coop ? coop_floats(P.coop_nel, 1) : 0;
   size_t coop_bytes = size_t(warps) * P.coop_stride * sizeof(float);
@@ -1009,6 +1013,7 @@ int launch_mc_t(dp_ctx* ctx, McParams& P) {
                             P.coop_nel);
     P.coop_stride = coop_floats(P.coop_nel, P.coop_kmax);
     coop_bytes = size_t(warps) * P.coop_stride * sizeof(float);
+    P.coop_kc = cta_kc(warps * P.coop_stride, P.coop_nel, threads);
   }
   size_t smem = mc_smem_head<R>() + (P.staged ? tables : 0) + coop_bytes;
   if (smem > size_t(dev_smem)) return fail(ctx, DP_ERR_ARG, "media too large for the MC kernel");

@@ -481,6 +481,58 @@ __host__ __device__ inline int coop_floats(int nel, int kmax) {
   return coop_head(nel, kmax) + 4 * kmax;
 }
 
+// The items of one event's DCS sum in FP32 (element table row x, mass fm,
+// ancestor energy fk, transfer fq): pair-production asymmetry point p (items
+// 1..12 of an element), photonuclear point p (items 13..21), and
+// bremsstrahlung (t = 0, item 0) or ionisation (t = 1, item 22).  Shared by
+// the warp and the CTA forms of the batched sums, so that both give the same
+// bits.
+__device__ __forceinline__ float coop_pair(const float* x, float fm, float fk, float fq, int p) {
+  float v = 0.f, tmin;
+  if (pair_range<float>(x[0], x[1], fm, fk, fq, &tmin))
+    v = -pair_point<float>(x[0], x[1], fm, fk, fq, tmin, p, x[4]);
+  return isfinite(v) ? v : 0.f;
+}
+__device__ __forceinline__ float coop_photo(const float* x, float fm, float fk, float fq, int p) {
+  float v = 0.f, lmin, dx;
+  if (photo_range<float>(x[0], x[1], fm, fk, fq, &lmin, &dx))
+    v = photo_point<float>(x[0], x[1], fm, fk, fq, lmin, dx, p, x[4]);
+  return isfinite(v) ? v : 0.f;
+}
+__device__ __forceinline__ float coop_bi(const float* x, float fm, float fk, float fq, int t) {
+  const float v = t == 0 ? dcs_brems<float>(x[0], x[1], fm, fk, fq, x[4])
+                         : dcs_ionisation<float>(x[0], x[2], fm, fk, fq, x[4]);
+  return isfinite(v) ? v : 0.f;
+}
+// Component p of an element from its items `it` (bremsstrahlung, pair,
+// photonuclear, ionisation), times the mass fraction and the ancestor energy.
+__device__ __forceinline__ float coop_comp(const float* it, int p, float fraction, float fk) {
+  float v;
+  if (p == 0) {
+    v = it[0];
+  } else if (p == 1) {
+    v = 0.f;
+    for (int j = 0; j < 12; ++j) v += it[1 + j];
+    v = fmaxf(v, 0.f);
+  } else if (p == 2) {
+    v = 0.f;
+    for (int j = 0; j < 9; ++j) v += it[13 + j];
+    v = fmaxf(v, 0.f);
+  } else {
+    v = it[22];
+  }
+  v *= fraction * fk;
+  return v;
+}
+// Total of one event's nc components: lane c's running sum of components
+// c, c + 32, ..., then a fixed tree over the lanes (lane 0 holds it).
+__device__ __forceinline__ float coop_total(const float* comp, int nc, int lane) {
+  float mine = 0.f;
+  for (int c = lane; c < nc; c += 32) mine += comp[c];
+  for (int d = 16; d > 0; d >>= 1) mine += __shfl_down_sync(0xffffffffu, mine, d);
+  return mine;
+}
+
 // Warp-cooperative FP32 form of del_total for k events of one medium at once
 // (their ancestor energies anc[] and transfers q[] in the buffer).  The terms
 // of all k events are spread over the lanes one kind at a time (pair
@@ -499,66 +551,27 @@ static __device__ __noinline__ void coop_batch(const float* elf, int nel, float 
   float* tot = comp + k * nc;
   const float* anc = buf + coop_head(nel, k);
   const float* q = anc + k;
-  // pair-production asymmetry points (items 1..12 of an element)
   for (int f = lane; f < k * nel * 12; f += 32) {
     const int i = f / (nel * 12), r = f - i * nel * 12, e = r / 12, p = r - e * 12;
-    const float* x = elf + kElfStride * e;
-    const float fk = anc[i], fq = q[i];
-    float v = 0.f, tmin;
-    if (pair_range<float>(x[0], x[1], fm, fk, fq, &tmin))
-      v = -pair_point<float>(x[0], x[1], fm, fk, fq, tmin, p, x[4]);
-    item[i * ni + e * kItemsPerElement + 1 + p] = isfinite(v) ? v : 0.f;
+    item[i * ni + e * kItemsPerElement + 1 + p] = coop_pair(elf + kElfStride * e, fm, anc[i], q[i], p);
   }
-  // photonuclear points (items 13..21)
   for (int f = lane; f < k * nel * 9; f += 32) {
     const int i = f / (nel * 9), r = f - i * nel * 9, e = r / 9, p = r - e * 9;
-    const float* x = elf + kElfStride * e;
-    const float fk = anc[i], fq = q[i];
-    float v = 0.f, lmin, dx;
-    if (photo_range<float>(x[0], x[1], fm, fk, fq, &lmin, &dx))
-      v = photo_point<float>(x[0], x[1], fm, fk, fq, lmin, dx, p, x[4]);
-    item[i * ni + e * kItemsPerElement + 13 + p] = isfinite(v) ? v : 0.f;
+    item[i * ni + e * kItemsPerElement + 13 + p] = coop_photo(elf + kElfStride * e, fm, anc[i], q[i], p);
   }
-  // bremsstrahlung (item 0) and ionisation (item 22)
   for (int f = lane; f < k * nel * 2; f += 32) {
     const int i = f / (nel * 2), r = f - i * nel * 2, e = r >> 1, t = r & 1;
-    const float* x = elf + kElfStride * e;
-    const float fk = anc[i], fq = q[i];
-    const float v = t == 0 ? dcs_brems<float>(x[0], x[1], fm, fk, fq, x[4])
-                           : dcs_ionisation<float>(x[0], x[2], fm, fk, fq, x[4]);
-    item[i * ni + e * kItemsPerElement + (t ? 22 : 0)] = isfinite(v) ? v : 0.f;
+    item[i * ni + e * kItemsPerElement + (t ? 22 : 0)] = coop_bi(elf + kElfStride * e, fm, anc[i], q[i], t);
   }
   __syncwarp();
-  // components: per element bremsstrahlung, pair, photonuclear, ionisation,
-  // each times the mass fraction and the ancestor energy
   for (int f = lane; f < k * nc; f += 32) {
     const int i = f / nc, c = f - i * nc, e = c >> 2, p = c & 3;
-    const float* it = item + i * ni + e * kItemsPerElement;
-    float v;
-    if (p == 0) {
-      v = it[0];
-    } else if (p == 1) {
-      v = 0.f;
-      for (int j = 0; j < 12; ++j) v += it[1 + j];
-      v = fmaxf(v, 0.f);
-    } else if (p == 2) {
-      v = 0.f;
-      for (int j = 0; j < 9; ++j) v += it[13 + j];
-      v = fmaxf(v, 0.f);
-    } else {
-      v = it[22];
-    }
-    v *= elf[kElfStride * e + 3] * anc[i];
-    comp[i * nc + c] = v;
+    comp[i * nc + c] = coop_comp(item + i * ni + e * kItemsPerElement, p, elf[kElfStride * e + 3], anc[i]);
   }
   __syncwarp();
-  // totals: per event, lane c's running sum of components c, c + 32, ...,
-  // then a fixed tree over the lanes
   for (int i = 0; i < k; ++i) {
-    float mine = 0.f;
-    for (int c = lane; c < nc; c += 32) mine += comp[i * nc + c];
-    for (int d = 16; d > 0; d >>= 1) mine += __shfl_down_sync(0xffffffffu, mine, d);
-    if (lane == 0) tot[i] = mine;
+    const float t = coop_total(comp + i * nc, nc, lane);
+    if (lane == 0) tot[i] = t;
   }
   __syncwarp();
 }

@@ -121,18 +121,134 @@ __device__ __forceinline__ void drain_histories(G& geo, unsigned long long* coun
   }
 }
 
+// CTA form of the batched DCS sums for the lockstep phases.  The buffer at
+// `base` (cta_floats(nel, kc) floats) holds two event counters, then for kc
+// events: items and components in rows of nel elements (the largest element
+// count of the launch's media), totals, ancestor energies, transfers and
+// media.  Every term, component and total is computed exactly as coop_batch
+// computes it, so an event's sum is the same bit for bit in either form.
+__host__ __device__ inline int cta_floats(int nel, int kc) {
+  return 4 + kc * ((kItemsPerElement + 4) * nel + 4);
+}
+// Events per chunk of a CTA buffer of `floats` floats (at most `threads`).
+inline int cta_kc(int floats, int nel, int threads) {
+  int kc = (floats - 4) / ((kItemsPerElement + 4) * nel + 4);
+  return kc < threads ? (kc > 0 ? kc : 0) : threads;
+}
+template <class G>
+__device__ __forceinline__ void cta_batch(const G& geo, float fm, int k, int nel, float* item,
+                                          float* comp, float* tot, const float* anc,
+                                          const float* q, const int* med) {
+  const int t = threadIdx.x, T = blockDim.x;
+  const int ni = kItemsPerElement * nel, nc = 4 * nel;
+  for (int f = t; f < k * nel * 12; f += T) {
+    const int i = f / (nel * 12), r = f - i * nel * 12, e = r / 12, p = r - e * 12;
+    const auto& m = geo.medium(med[i]);
+    if (e < m.nel)
+      item[i * ni + e * kItemsPerElement + 1 + p] = coop_pair(m.elf + kElfStride * e, fm, anc[i], q[i], p);
+  }
+  for (int f = t; f < k * nel * 9; f += T) {
+    const int i = f / (nel * 9), r = f - i * nel * 9, e = r / 9, p = r - e * 9;
+    const auto& m = geo.medium(med[i]);
+    if (e < m.nel)
+      item[i * ni + e * kItemsPerElement + 13 + p] = coop_photo(m.elf + kElfStride * e, fm, anc[i], q[i], p);
+  }
+  for (int f = t; f < k * nel * 2; f += T) {
+    const int i = f / (nel * 2), r = f - i * nel * 2, e = r >> 1, u = r & 1;
+    const auto& m = geo.medium(med[i]);
+    if (e < m.nel)
+      item[i * ni + e * kItemsPerElement + (u ? 22 : 0)] = coop_bi(m.elf + kElfStride * e, fm, anc[i], q[i], u);
+  }
+  __syncthreads();
+  for (int f = t; f < k * nc; f += T) {
+    const int i = f / nc, c = f - i * nc, e = c >> 2, p = c & 3;
+    const auto& m = geo.medium(med[i]);
+    if (e < m.nel)
+      comp[i * nc + c] = coop_comp(item + i * ni + e * kItemsPerElement, p, m.elf[kElfStride * e + 3], anc[i]);
+  }
+  __syncthreads();
+  const int lane = t & 31;
+  for (int i = t >> 5; i < k; i += T >> 5) {
+    const float v = coop_total(comp + i * nc, 4 * geo.medium(med[i]).nel, lane);
+    if (lane == 0) tot[i] = v;
+  }
+  __syncthreads();
+}
+// Serves every suspended step of the CTA (waits: this thread's step waits on
+// a DCS sum; x its continuation) in chunks of kc events; counter `parity` of
+// the buffer numbers the events (any numbering gives the same results).
+// All threads of the CTA call it.
+template <class G, class R>
+__device__ __forceinline__ void serve_cta(const G& geo, const Consts& C, float* base, int kc, int nel,
+                                          int parity, bool waits, Cont<R>& x, Stream& g) {
+  int* cnt = reinterpret_cast<int*>(base) + parity;
+  const int ni = kItemsPerElement * nel, nc = 4 * nel;
+  float* item = base + 4;
+  float* comp = item + kc * ni;
+  float* tot = comp + kc * nc;
+  float* anc = tot + kc;
+  float* q = anc + kc;
+  int* med = reinterpret_cast<int*>(q + kc);
+  int slot = -1;
+  if (waits) {
+    namespace cg = cooperative_groups;
+    cg::coalesced_group grp = cg::coalesced_threads();
+    int b = 0;
+    if (grp.thread_rank() == 0) b = atomicAdd(cnt, int(grp.size()));
+    slot = grp.shfl(b, 0) + int(grp.thread_rank());
+  }
+  __syncthreads();
+  const int nw = *reinterpret_cast<volatile int*>(cnt);
+  for (int c0 = 0; c0 < nw; c0 += kc) {
+    const int k = nw - c0 < kc ? nw - c0 : kc;
+    const int s = slot - c0;
+    const bool mine = slot >= c0 && s < k;
+    if (mine) {
+      anc[s] = x.anc;
+      q[s] = x.q;
+      med[s] = x.medium;
+    }
+    __syncthreads();
+    cta_batch(geo, C.mass_f, k, nel, item, comp, tot, anc, q, med);
+    if (mine) {
+      const int last = 4 * geo.medium(x.medium).nel - 1;
+      const float* cp = comp + s * nc;
+      const float total = tot[s];
+      x.total = total;
+      x.pick = -1;
+      if (x.details && total > 0.f) {
+        // process and element pick in the reference's order (src/MixedTransport.jl:131-140)
+        float u = uni<float>(g) * total;
+        int pick = last;
+        for (int c = 0; c <= last; ++c) {
+          u -= cp[c];
+          if (u <= 0.f) {
+            pick = c;
+            break;
+          }
+        }
+        x.pick = pick;
+      }
+    }
+    __syncthreads();  // the next chunk reuses the buffer
+  }
+}
+
 // Runs histories until none is left for this phase.  counter[PHASE] hands out
 // history indices, counter[2] counts the hand-off queue.  With COOP, `coop`
-// is this warp's buffer of batched DCS sums in shared memory (coop_floats
-// for up to kmax events).  `order` (may be null) maps the j-th hand-out to a
-// history (phase 0) or a queue slot (phase 1): the longest-first schedule.
-// With `lockstep` (block-uniform) every warp of the CTA runs its loop
-// iterations in step with the others until the CTA has no history left.
+// is the CTA's shared memory for batched DCS sums: per warp `stride` floats
+// (coop_floats for up to kmax events of one medium), or, in lockstep, one
+// CTA buffer (cta_floats(nel, kc)).  `order` (may be null) maps the j-th
+// hand-out to a history (phase 0) or a queue slot (phase 1): the
+// longest-first schedule.  With `lockstep` (block-uniform) every warp of the
+// CTA runs its loop iterations in step with the others until the CTA has no
+// history left, and the CTA serves all its waiting steps together.
 template <class R, int PHASE, bool COOP, class G>
 __device__ __forceinline__ void transport_histories(G& geo, const Consts& C,
                                                     unsigned long long* counter,
                                                     typename G::Queue* queue, float* coop,
-                                                    int kmax, const uint32_t* order = nullptr,
+                                                    int stride, int kmax, int kc, int nel,
+                                                    const uint32_t* order = nullptr,
                                                     bool lockstep = false) {
   const long n = PHASE == 0 ? geo.n0() : long(*(volatile unsigned long long*)(counter + 2));
   typename G::Hist h;
@@ -165,7 +281,25 @@ __device__ __forceinline__ void transport_histories(G& geo, const Consts& C,
   long i = 0;
   bool live = take(&i);
   if constexpr (COOP) {
+    if (lockstep && kc > 0) {
+      int* cnt = reinterpret_cast<int*>(coop);
+      if (threadIdx.x == 0) cnt[0] = cnt[1] = 0;
+      __syncthreads();
+      for (int parity = 0;; parity ^= 1) {
+        // counter parity ^ 1 was last read before the previous iteration's barrier
+        if (threadIdx.x == 0) cnt[parity ^ 1] = 0;
+        serve_cta(geo, C, coop, kc, nel, parity, live && h.x.kind != CONT_NONE, h.x, g);
+        if (live) {
+          const int r = h.x.kind != CONT_NONE ? geo.template resume<PHASE>(h, g)
+                                              : geo.template advance<true, PHASE>(h, g);
+          live = settle(r, &i);
+        }
+        if (!__syncthreads_or(live)) break;
+      }
+      return;
+    }
     const int lane = threadIdx.x & 31;
+    coop += size_t(threadIdx.x >> 5) * stride;
     for (;;) {
       // serve the hard events the warp's suspended steps wait for: the
       // waiting lanes of one medium together, up to kmax at a time
@@ -215,9 +349,7 @@ __device__ __forceinline__ void transport_histories(G& geo, const Consts& C,
                                             : geo.template advance<true, PHASE>(h, g);
         live = settle(r, &i);
       }
-      // lockstep: the CTA's warps take their steps together (one block
-      // barrier per step), so that they fetch the same code at the same time
-      if (lockstep ? !__syncthreads_or(live) : !__any_sync(0xffffffffu, live)) break;
+      if (!__any_sync(0xffffffffu, live)) break;
     }
   } else {
     while (live) live = settle(geo.template advance<false, PHASE>(h, g), &i);

@@ -132,13 +132,16 @@ int dp_autotune(dp_ctx* ctx, int family, int precision, int (*run)(void* user), 
  * default; 1: index order).  sync is a mask of the transport phases (bit 0:
  * below the mode switch, bit 1: above it) whose steps the warps of a CTA take
  * in lockstep, one block barrier per step, so that they fetch the same code
- * at the same time; it applies to DP_PREC_MIXED (default: 1 for DP_KERNEL_MC,
- * 0 for DP_KERNEL_DIR).  A thread refills itself one history at a time
- * from a warp-aggregated counter.  Every history keeps its own stream, so
- * staging, order and sync change no result (bit for bit).  Each CTA size is a
+ * at the same time, and whose hard-event DCS sums the whole CTA evaluates
+ * together; it applies to DP_PREC_MIXED (default: 3 for DP_KERNEL_MC, 2 for
+ * DP_KERNEL_DIR).  A thread refills itself one history at a time from a
+ * warp-aggregated counter.  Every history keeps its own stream, so staging
+ * and order change no result (bit for bit).  The DCS sums of a lockstep phase
+ * are compiled separately from those of a free-running one, and the code
+ * generator may fuse their FP32 multiply-adds differently, so results under
+ * another sync mask agree statistically, not bit for bit.  Each CTA size is a
  * separately compiled kernel whose FP32 multiply-adds the code generator may
- * fuse differently, so results at another size agree statistically, not bit
- * for bit. */
+ * fuse differently, so results at another size agree statistically too. */
 typedef struct {
   int threads, staging, order, sync;
 } dp_mc_shape;

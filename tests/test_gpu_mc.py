@@ -301,18 +301,19 @@ def test_cta_sizes_give_equivalent_histories(dp, phys, media):
 
 
 def test_launch_shapes_give_identical_histories(dp, phys, media):
-    """Table staging (shared memory or L1/L2), the hand-out order (longest
-    first or by index) and the lockstep mask (the CTA's warps stepping
-    together in either phase) do not change a result at one CTA size: every
-    shape gives the same contributions bit for bit, and histories taken out of
-    order all end (none skipped or run twice)."""
+    """Table staging (shared memory or L1/L2) and the hand-out order (longest
+    first or by index) do not change a result at one CTA size and lockstep
+    mask: every shape gives the same contributions bit for bit, and histories
+    taken out of order all end (none skipped or run twice).  The other
+    lockstep masks (free-running phases, whose DCS sums are compiled
+    separately) agree statistically, and almost every history to the bit."""
     n, seed = 20000, 6
     E, q, w, geo = _histories(n, seed)
     _, air, mix = media
-    assert dp.get_mc_shape(phys, "mc", "mixed")["sync"] == 1  # the default
+    assert dp.get_mc_shape(phys, "mc", "mixed")["sync"] == 3  # the default
     runs = {}
-    shapes = [(1024, 0, 0, 1), (1024, 0, 1, 1), (1024, 1, 0, 1), (1024, 1, 1, 1),
-              (1024, 0, 0, 0), (1024, 0, 0, 2), (1024, 1, 1, 3)]
+    shapes = [(1024, 0, 0, 3), (1024, 0, 1, 3), (1024, 1, 0, 3), (1024, 1, 1, 3),
+              (1024, 0, 0, 0), (1024, 0, 0, 1), (1024, 1, 1, 2)]
     try:
         for shape in shapes:
             dp.set_mc_shape(phys, "mc", "mixed", *shape)
@@ -329,9 +330,15 @@ def test_launch_shapes_give_identical_histories(dp, phys, media):
         with pytest.raises(ValueError):
             dp.set_mc_shape(phys, "mc", "mixed", 1024, 0, 0, 4)
     finally:
-        dp.set_mc_shape(phys, "mc", "mixed", 0, 0, 0, 1)
+        dp.set_mc_shape(phys, "mc", "mixed", 0, 0, 0, 3)
+    base = runs[shapes[0]]
     for shape, c in runs.items():
-        np.testing.assert_array_equal(c, runs[shapes[0]], err_msg=str(shape))
+        if shape[3] == 3:
+            np.testing.assert_array_equal(c, base, err_msg=str(shape))
+        else:
+            d = c - base
+            assert abs(d.mean()) <= 3 * d.std() / math.sqrt(n) + 1e-15 * abs(base.mean()), shape
+            assert np.mean(c == base) > 0.9, shape
 
 
 def test_autotune_shape_searches_every_dimension(dp, phys, media):
@@ -359,7 +366,7 @@ def test_autotune_shape_searches_every_dimension(dp, phys, media):
         assert dp.get_mc_shape(phys, "mc", "mixed") == best
         assert best in [s for s, _ in tried]
     finally:
-        dp.set_mc_shape(phys, "mc", "mixed", 0, 0, 0, 1)
+        dp.set_mc_shape(phys, "mc", "mixed", 0, 0, 0, 3)
 
 
 def test_autotune_keeps_the_fastest_size(dp, phys, media):
