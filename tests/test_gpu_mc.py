@@ -306,7 +306,8 @@ def test_launch_shapes_give_identical_histories(dp, phys, media):
     mask: every shape gives the same contributions bit for bit, and histories
     taken out of order all end (none skipped or run twice).  The other
     lockstep masks (free-running phases, whose DCS sums are compiled
-    separately) agree statistically, and almost every history to the bit."""
+    separately and round differently in the last bits) agree statistically,
+    and almost every history to 1e-4."""
     n, seed = 20000, 6
     E, q, w, geo = _histories(n, seed)
     _, air, mix = media
@@ -338,7 +339,7 @@ def test_launch_shapes_give_identical_histories(dp, phys, media):
         else:
             d = c - base
             assert abs(d.mean()) <= 3 * d.std() / math.sqrt(n) + 1e-15 * abs(base.mean()), shape
-            assert np.mean(c == base) > 0.9, shape
+            assert np.mean(np.isclose(c, base, rtol=1e-4, atol=0.0)) > 0.98, shape
 
 
 def test_autotune_shape_searches_every_dimension(dp, phys, media):
