@@ -155,6 +155,7 @@ struct PathGeo {
   const Med<R>* meds;
   __device__ long n0() const { return P.n; }
   __device__ const Med<R>& medium(int k) const { return meds[k]; }
+  __device__ const Med<R>* media() const { return meds; }
 
   __device__ R thr() const { return sizeof(R) == 8 ? R(P.C.thr) : R(P.C.thr_f); }
 

@@ -561,6 +561,9 @@ struct SlabGeo {
   }
   __device__ void end(long i, const Hist& h) const { end_history(P, i, h); }
   __device__ const Med<R>& medium(int k) const { return k ? air : rock; }
+  // the descriptors by medium index: rock and air are consecutive entries of
+  // the CTA's descriptor array in shared memory
+  __device__ const Med<R>* media() const { return &rock; }
   template <bool COOP, int PHASE>
   __device__ int advance(Hist& h, Stream& g) const {
     return mc::advance<R, COOP, PHASE>(rock, air, nullptr, P.C, h, g);
@@ -600,6 +603,8 @@ struct SlabGeoP {
   }
   __device__ void end(long i, const Hist& h) const { end_history(P, i, h); }
   __device__ const Med<R>& medium(int k) const { return k == 1 ? air : (k == 2 ? porous : rock); }
+  // rock, air and porous are consecutive entries of the CTA's descriptor array
+  __device__ const Med<R>* media() const { return &rock; }
   template <bool COOP, int PHASE>
   __device__ int advance(Hist& h, Stream& g) const {
     return mc::advance<R, COOP, PHASE>(rock, air, &porous, P.C, h, g);
