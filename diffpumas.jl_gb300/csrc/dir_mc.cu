@@ -487,6 +487,9 @@ int dir_phase(dp_ctx* ctx, const DirParams& P, size_t smem, long max_blocks) {
   const int threads = T;
   DP_CHECK_CUDA(ctx, cudaFuncSetAttribute(dir_kernel<R, PHASE, T>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  DP_CHECK_CUDA(ctx, cudaFuncSetAttribute(dir_kernel<R, PHASE, T>,
+                                          cudaFuncAttributePreferredSharedMemoryCarveout,
+                                          carveout_percent(ctx->device, smem)));
   int per_sm = 0, n_sm = 0;
   DP_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dir_kernel<R, PHASE, T>,
                                                                    threads, smem));
@@ -521,9 +524,10 @@ int dir_launch_t(dp_ctx* ctx, DirParams& P) {
     if (dir_coop_offset<R>(P) + coop_bytes <= size_t(dev_smem)) break;
   }
   if (KCfg<R>::coop) {
-    // the shared memory left after the staged media batches DCS sums
-    P.coop_kmax = coop_kmax(size_t(dev_smem) - std::min(size_t(dev_smem), size_t(dir_coop_offset<R>(P))),
-                            warps, P.coop_nel);
+    // the shared memory left after the staged media, up to the smallest
+    // carve-out step that holds a one-event-per-warp buffer, batches DCS sums
+    const size_t cap = std::min(size_t(dev_smem), carveout_cap(dir_coop_offset<R>(P) + coop_bytes));
+    P.coop_kmax = coop_kmax(cap - std::min(cap, size_t(dir_coop_offset<R>(P))), warps, P.coop_nel);
     P.coop_stride = coop_floats(P.coop_nel, P.coop_kmax);
     coop_bytes = size_t(warps) * P.coop_stride * sizeof(float);
     P.coop_kc = cta_kc(warps * P.coop_stride, P.coop_nel, threads);

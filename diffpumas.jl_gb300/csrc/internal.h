@@ -40,8 +40,9 @@ struct dp_ctx {
   // DP_KERNEL_DIR) and precision (DP_PREC_FP64, DP_PREC_MIXED); 0: default.
   int mc_threads[2][2] = {{0, 0}, {0, 0}};
   // Table staging (0: media in shared memory when they fit, 1: read through
-  // L1/L2) of the same kernels.
-  int mc_stage[2][2] = {{0, 0}, {0, 0}};
+  // L1/L2) of the same kernels; mixed precision reads them through L1/L2 by
+  // default (its kernels leave the SM's shared memory to the L1 cache).
+  int mc_stage[2][2] = {{0, 1}, {0, 1}};
   // Hand-out order of the histories (0: longest first, 1: index order).
   int mc_order[2][2] = {{0, 0}, {0, 0}};
   // CTA-lockstep phases (bit k: phase k), mixed precision only: both phases

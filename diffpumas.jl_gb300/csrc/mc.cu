@@ -975,6 +975,9 @@ int launch_phase(dp_ctx* ctx, McParams& P, size_t smem, long max_blocks) {
   const int threads = T;
   DP_CHECK_CUDA(ctx, cudaFuncSetAttribute(mc_kernel<R, PHASE, T, POR>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  DP_CHECK_CUDA(ctx, cudaFuncSetAttribute(mc_kernel<R, PHASE, T, POR>,
+                                          cudaFuncAttributePreferredSharedMemoryCarveout,
+                                          carveout_percent(ctx->device, smem)));
   int per_sm = 0, n_sm = 0;
   DP_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                          &per_sm, mc_kernel<R, PHASE, T, POR>, threads, smem));
@@ -1011,17 +1014,23 @@ int launch_mc_t(dp_ctx* ctx, McParams& P) {
                      ctx->mc_stage[DP_KERNEL_MC][sizeof(R) == 4] == 0
                  ? 1
                  : 0;
-  if (KCfg<R>::coop) {
-    // the shared memory left after the tables batches DCS sums
-    const size_t used = mc_smem_head<R>() + (P.staged ? tables : 0);
-    P.coop_kmax = coop_kmax(size_t(dev_smem) - std::min(size_t(dev_smem), used), warps,
-                            P.coop_nel);
-    P.coop_stride = coop_floats(P.coop_nel, P.coop_kmax);
-    coop_bytes = size_t(warps) * P.coop_stride * sizeof(float);
-    P.coop_kc = cta_kc(warps * P.coop_stride, P.coop_nel, threads);
-  }
-  size_t smem = mc_smem_head<R>() + (P.staged ? tables : 0) + coop_bytes;
+  // the shared memory left after the tables (up to `cap` bytes in all)
+  // batches DCS sums
+  auto fit = [&](size_t cap) -> size_t {
+    if (KCfg<R>::coop) {
+      const size_t used = mc_smem_head<R>() + (P.staged ? tables : 0);
+      P.coop_kmax = coop_kmax(cap - std::min(cap, used), warps, P.coop_nel);
+      P.coop_stride = coop_floats(P.coop_nel, P.coop_kmax);
+      coop_bytes = size_t(warps) * P.coop_stride * sizeof(float);
+      P.coop_kc = cta_kc(warps * P.coop_stride, P.coop_nel, threads);
+    }
+    return mc_smem_head<R>() + (P.staged ? tables : 0) + coop_bytes;
+  };
+  size_t smem = fit(0);  // one event per warp: the least the kernel needs
   if (smem > size_t(dev_smem)) return fail(ctx, DP_ERR_ARG, "media too large for the MC kernel");
+  // the DCS buffer fills the smallest carve-out step that holds it, the rest
+  // of the SM's 256 KB is L1 for the spilled stack
+  smem = fit(std::min(size_t(dev_smem), carveout_cap(smem)));
   long need = (P.n + threads - 1) / threads;
   long rec_blocks = std::min((P.n + 255) / 256, 152L * 32);
   DP_CHECK_CUDA(ctx, cudaMemsetAsync(P.counter, 0, 3 * sizeof(unsigned long long), ctx->stream));

@@ -104,16 +104,18 @@ def set_debug_limits(ctx, step_cap=None, event_cap=None, wait_iters=None):
     check(load().dp_set_debug_limits(h, v(step_cap), v(event_cap), v(wait_iters)), h)
 
 
-def set_mc_shape(ctx, family, precision, threads=0, staging=0, order=0, sync=None):
+def set_mc_shape(ctx, family, precision, threads=0, staging=None, order=None, sync=None):
     """dp_set_mc_shape: CTA size (0: default), table staging (0: shared
     memory when the media fit, 1: read through L1/L2), hand-out order (0:
     longest first, 1: index order) and lockstep mask (bit k: the warps of a
-    CTA take the steps of phase k together; None keeps the context's) of the
-    persistent transport kernels."""
+    CTA take the steps of phase k together) of the persistent transport
+    kernels; None keeps the context's value."""
     from ._lib import DpMcShape
     h = _ctx_of(ctx)
-    if sync is None:
-        sync = get_mc_shape(ctx, family, precision)["sync"]
+    cur = get_mc_shape(ctx, family, precision)
+    staging = cur["staging"] if staging is None else staging
+    order = cur["order"] if order is None else order
+    sync = cur["sync"] if sync is None else sync
     sh = DpMcShape(int(threads), int(staging), int(order), int(sync))
     check(load().dp_set_mc_shape(h, _FAMILY[family], _PRECISION[precision], C.byref(sh)), h)
 

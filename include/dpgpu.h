@@ -127,7 +127,9 @@ int dp_autotune(dp_ctx* ctx, int family, int precision, int (*run)(void* user), 
                 int* best_threads, double* ms, int cap);
 /* The full launch shape of those kernels: the CTA size, where the media
  * tables live (staging 0: copied to shared memory once per CTA when they fit,
- * the default; 1: read through L1/L2) and the order histories are handed out
+ * the default in FP64; 1: read through L1/L2, the default in DP_PREC_MIXED,
+ * whose kernels size their shared memory to the smallest carve-out step and
+ * leave the rest of the SM's 256 KB to the L1 cache) and the order histories are handed out
  * in (order 0: longest first, by a per-history estimate of its steps, the
  * default; 1: index order).  sync is a mask of the transport phases (bit 0:
  * below the mode switch, bit 1: above it) whose steps the warps of a CTA take

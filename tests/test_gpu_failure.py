@@ -130,15 +130,20 @@ def test_table_wait_runs_out(dp, phys, media):
     flagged DP_ST_TABLE_WAIT; the call returns DP_ERR_STATE and the context
     works afterwards."""
     E = np.exp(np.random.default_rng(3).uniform(0.0, np.log(1e4), 512))
-    rc0, _, c0, st0, _ = _histories(dp, phys, media, E, precision="mixed", thickness=80.0)
-    assert rc0 == 0 and (st0 == 0).all()
-    with _limited(dp, phys, wait_iters=0):
-        rc, msg, c, st, _ = _histories(dp, phys, media, E, precision="mixed", thickness=80.0)
-    assert rc == DP_ERR_STATE and "table-staging" in msg
-    assert (st == ST_TABLE_WAIT).all() and (c == 0).all()
-    rc1, _, c1, st1, _ = _histories(dp, phys, media, E, precision="mixed", thickness=80.0)
-    assert rc1 == 0 and (st1 == 0).all()
-    np.testing.assert_array_equal(c1, c0)
+    shape = dp.get_mc_shape(phys, "mc", "mixed")
+    dp.set_mc_shape(phys, "mc", "mixed", staging=0)  # tables in shared memory
+    try:
+        rc0, _, c0, st0, _ = _histories(dp, phys, media, E, precision="mixed", thickness=80.0)
+        assert rc0 == 0 and (st0 == 0).all()
+        with _limited(dp, phys, wait_iters=0):
+            rc, msg, c, st, _ = _histories(dp, phys, media, E, precision="mixed", thickness=80.0)
+        assert rc == DP_ERR_STATE and "table-staging" in msg
+        assert (st == ST_TABLE_WAIT).all() and (c == 0).all()
+        rc1, _, c1, st1, _ = _histories(dp, phys, media, E, precision="mixed", thickness=80.0)
+        assert rc1 == 0 and (st1 == 0).all()
+        np.testing.assert_array_equal(c1, c0)
+    finally:
+        dp.set_mc_shape(phys, "mc", "mixed", **shape)
 
 
 def test_below_mixed_kernel_domain(dp, phys, media, oracle, orc_phys):

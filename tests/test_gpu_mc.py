@@ -311,7 +311,8 @@ def test_launch_shapes_give_identical_histories(dp, phys, media):
     n, seed = 20000, 6
     E, q, w, geo = _histories(n, seed)
     _, air, mix = media
-    assert dp.get_mc_shape(phys, "mc", "mixed")["sync"] == 3  # the default
+    assert dp.get_mc_shape(phys, "mc", "mixed") == {"threads": 1024, "staging": 1, "order": 0,
+                                                     "sync": 3}  # the defaults
     runs = {}
     shapes = [(1024, 0, 0, 3), (1024, 0, 1, 3), (1024, 1, 0, 3), (1024, 1, 1, 3),
               (1024, 0, 0, 0), (1024, 0, 0, 1), (1024, 1, 1, 2)]
@@ -331,7 +332,7 @@ def test_launch_shapes_give_identical_histories(dp, phys, media):
         with pytest.raises(ValueError):
             dp.set_mc_shape(phys, "mc", "mixed", 1024, 0, 0, 4)
     finally:
-        dp.set_mc_shape(phys, "mc", "mixed", 0, 0, 0, 3)
+        dp.set_mc_shape(phys, "mc", "mixed", 0, 1, 0, 3)
     base = runs[shapes[0]]
     for shape, c in runs.items():
         if shape[3] == 3:
@@ -367,7 +368,7 @@ def test_autotune_shape_searches_every_dimension(dp, phys, media):
         assert dp.get_mc_shape(phys, "mc", "mixed") == best
         assert best in [s for s, _ in tried]
     finally:
-        dp.set_mc_shape(phys, "mc", "mixed", 0, 0, 0, 3)
+        dp.set_mc_shape(phys, "mc", "mixed", 0, 1, 0, 3)
 
 
 def test_autotune_keeps_the_fastest_size(dp, phys, media):
