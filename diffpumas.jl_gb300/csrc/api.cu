@@ -122,6 +122,7 @@ int dp_destroy(dp_ctx* c) {
   }
   for (cudaEvent_t e : c->spare) cudaEventDestroy(e);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  cudaGetLastError();  // a failed release must not surface at a later launch
   delete c;
   return DP_OK;
 }
@@ -272,6 +273,7 @@ static int finish_upload(dp_ctx* ctx, dp_physics* p, dp_physics** out) {
   p->view.lE0 = lE[0];
   p->view.inv_dlE = 1.0 / d;
   p->ctx = ctx;
+  p->device = ctx->device;
   *out = p;
   return DP_OK;
 }
@@ -487,9 +489,11 @@ int dp_physics_load(dp_ctx* ctx, const char* path, dp_physics** out) {
 int dp_physics_free(dp_physics* p) {
   if (!p) return DP_ERR_ARG;
   if (p->dev) {
-    cudaSetDevice(p->ctx->device);
+    // the device saved at creation: the context may already be destroyed
+    cudaSetDevice(p->device);
     cudaFree(p->dev);
     cudaFree(p->dev32);
+    cudaGetLastError();  // a failed release must not surface at a later launch
   }
   delete p;
   return DP_OK;

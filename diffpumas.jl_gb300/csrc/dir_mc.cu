@@ -659,6 +659,7 @@ int dp_dir_media_free(dp_dir_media* M) {
     cudaFree(D.blob);
     cudaFree(D.info);
   }
+  cudaGetLastError();  // a failed release must not surface at a later launch
   delete M;
   return DP_OK;
 }

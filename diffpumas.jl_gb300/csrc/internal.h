@@ -140,6 +140,7 @@ struct Arena {
 
 struct dp_physics {
   dp_ctx* ctx = nullptr;
+  int device = 0;  // the context's device (the free path must not read a destroyed context)
   dp_settings settings{};
   int n_mat = 0, n = 0, ld = 0;
   std::vector<double> host;           // n_mat x DP_NCOL x n
@@ -158,6 +159,7 @@ struct dp_physics {
 // deterministic J^T r gather.
 struct dp_paths {
   dp_ctx* ctx = nullptr;
+  int device = 0;  // the context's device (the free path must not read a destroyed context)
   dp_grid grid{};
   int side_cell = -1;
   long n_rays = 0;

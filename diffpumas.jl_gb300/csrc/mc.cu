@@ -1300,6 +1300,7 @@ int dp_mixture_prepare(dp_ctx* ctx, const dp_physics* ph, int n, const int* mats
 int dp_mixture_free(dp_mixture* m) {
   if (!m) return DP_OK;
   for (auto& b : m->blobs) cudaFree(b.dev);
+  cudaGetLastError();  // a failed release must not surface at a later launch
   delete m;
   return DP_OK;
 }

@@ -858,6 +858,7 @@ static int build_paths(dp_ctx* ctx, const dp_grid& gr, const dp_ray* d_rays_in, 
   long nbc = (ncell + kScan) / kScan + 1;
   dp_paths* P = new dp_paths;
   P->ctx = ctx;
+  P->device = ctx->device;
   P->grid = gr;
   P->side_cell = side_cell;
   P->n_rays = n_rays;
@@ -1352,8 +1353,9 @@ int dp_tomo_paths_create_dev(dp_ctx* ctx, const dp_grid* gr, long n_rays, const 
 
 int dp_tomo_paths_free(dp_paths* p) {
   if (!p) return DP_ERR_ARG;
-  cudaSetDevice(p->ctx->device);
+  cudaSetDevice(p->device);  // the context may already be destroyed
   free_paths_arrays(p);
+  cudaGetLastError();  // a failed release must not surface at a later launch
   delete p;
   return DP_OK;
 }
@@ -1368,7 +1370,7 @@ int dp_tomo_paths_info(const dp_paths* p, long* n_rays, int64_t* nnz, int* max_s
 
 int dp_tomo_paths_csr(const dp_paths* p, int64_t* row_ptr, int32_t* col, double* len) {
   if (!p) return DP_ERR_ARG;
-  cudaSetDevice(p->ctx->device);
+  cudaSetDevice(p->device);
   if (row_ptr) cudaMemcpy(row_ptr, p->row_ptr, 8 * (p->n_rays + 1), cudaMemcpyDeviceToHost);
   if (col) cudaMemcpy(col, p->cell, 4 * p->nnz, cudaMemcpyDeviceToHost);
   if (len) cudaMemcpy(len, p->len, 8 * p->nnz, cudaMemcpyDeviceToHost);
