@@ -218,12 +218,13 @@ C2_MIX = ([1, 3, 2], [0.70, 0.25, 0.05])  # rock, water, air (1-based material i
 # cases of the same kernels (the bound that binds them: instruction issue)
 # Issue-slot figures of the dominant kernels, from the ncu captures of the
 # same builds (reduced cases of each workload; the launch tails weigh more there)
-C2_ISSUE = {"issue_active": 0.1325, "lanes_per_inst": 16.07,
+C2_ISSUE = {"issue_active": 0.4306, "lanes_per_inst": 18.38,
             "source": "ncu smsp__issue_active and smsp__thread_inst_executed_per_inst_executed, "
-                      "mc_kernel<float,0,1024> (phase 0, longest-first order) on a 2e5-history "
-                      "c2 case"}
-C4_ISSUE = {"issue_active": 0.263, "lanes_per_inst": 14.2,
-            "source": "ncu, mc_kernel<float,1,1024> (mc_mixed_hi) on a reduced c4 case"}
+                      "mc_kernel<float,0,1024> (phase 0, lockstep, tables through L1/L2) on a "
+                      "5e5-history c2 case"}
+C4_ISSUE = {"issue_active": 0.3864, "lanes_per_inst": 21.21,
+            "source": "ncu, mc_kernel<float,1,1024> (mc_mixed_hi, lockstep) on 819 of the c4 lines "
+                      "(443,846 histories)"}
 C1_ISSUE = {"issue_active": 0.206, "lanes_per_inst": 15.88,
             "source": "ncu, csda32_kernel on the c1 workload (one warp per scheduler, bound by "
                       "the dependent steps of each warp's longest history)"}
@@ -284,13 +285,13 @@ def setup_c2(dp, torch, dev, precision="mixed", scale=1.0):
             # transport kernel and read back by the tally
             "alg_bytes": n * 24,
             # DRAM bytes (read + write) of one phase-0 launch from an ncu capture
-            # at 2e5 histories (154.2 MB: start records and the spilled stack's
-            # write-back), scaled by the histories, which it grows in proportion with
-            "traffic": int(771 * n) if precision == "mixed" else None,
-            "note": "SM-issue bound, not HBM: ncu smsp__issue_active 13.3% (phase 0, a "
-                    "tail-heavy 2e5-history case) with 16.1 of 32 lanes per instruction; DRAM "
-                    "traffic (mostly local-memory write-back of the spilled stack) is under 1% "
-                    "of the bandwidth",
+            # at 5e5 histories (1.45 GB, almost all the write-back of the spilled
+            # stacks), scaled by the histories
+            "traffic": int(2899 * n) if precision == "mixed" else None,
+            "note": "SM-issue bound, not HBM: ncu smsp__issue_active 43.1% (phase 0, a "
+                    "5e5-history case) with 18.4 of 32 lanes per instruction; DRAM traffic "
+                    "(mostly local-memory write-back of the spilled stack) is about 1% of the "
+                    "bandwidth",
             "config": {"workload": "c2: straggled MC with DEL/EHS + Coulomb scattering, rock mixture "
                                    "rock/water/air 0.70/0.25/0.05 (per-history thickness U[20,500] m, "
                                    "density U[2000,2800], elevation U[30,90] deg) under 1 km air, "
@@ -382,11 +383,12 @@ def setup_c4(dp, torch, dev, precision="mixed", scale=1.0):
             # per history: contribution and status written and read back,
             # CSDA contribution and derivative written and read back
             "alg_bytes": total * (24 + 32),
-            # DRAM bytes of one mc_mixed_hi launch from an ncu capture of a tenth
-            # of the lines of sight (7.27 GB for ~8.9e5 histories, mostly
+            # DRAM bytes of one mc_mixed_hi launch from an ncu capture of 819 of
+            # the lines of sight (1.71 GB for 443,846 histories, mostly
             # local-memory write-back), scaled by the histories
-            "traffic": int(8160 * total) if precision == "mixed" else None,
-            "note": "SM-issue bound, not HBM: ncu smsp__issue_active 26.3% (mixed transport)",
+            "traffic": int(3860 * total) if precision == "mixed" else None,
+            "note": "SM-issue bound, not HBM: ncu smsp__issue_active 38.6% (mixed transport, "
+                    "lockstep)",
             "config": {"workload": "c4: 16384 vertical lines of sight, depth log-uniform 50-2000 m, "
                                    "density U[2400,2800], 64-1024 histories each (uneven), mixed "
                                    "transport everywhere, E 1 GeV-10 TeV, + CSDA d flux/d rho per "
