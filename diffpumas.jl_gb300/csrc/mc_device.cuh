@@ -485,8 +485,7 @@ __host__ __device__ inline int coop_floats(int nel, int kmax) {
 // ancestor energy fk, transfer fq): pair-production asymmetry point p (items
 // 1..12 of an element), photonuclear point p (items 13..21), and
 // bremsstrahlung (t = 0, item 0) or ionisation (t = 1, item 22).  Shared by
-// the warp and the CTA forms of the batched sums, so that both give the same
-// bits.
+// the warp and the CTA forms of the batched sums.
 __device__ __forceinline__ float coop_pair(const float* x, float fm, float fk, float fq, int p) {
   float v = 0.f, tmin;
   if (pair_range<float>(x[0], x[1], fm, fk, fq, &tmin))

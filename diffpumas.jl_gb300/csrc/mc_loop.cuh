@@ -152,8 +152,11 @@ __device__ __forceinline__ void drain_histories(G& geo, unsigned long long* coun
 // `base` (cta_floats(nel, kc) floats) holds two event counters, then for kc
 // events: items and components in rows of nel elements (the largest element
 // count of the launch's media), totals, ancestor energies, transfers and
-// media.  Every term, component and total is computed exactly as coop_batch
-// computes it, so an event's sum is the same bit for bit in either form.
+// media.  Terms, components and totals come from the helpers coop_batch uses
+// (coop_pair, coop_photo, coop_bi, coop_comp, coop_total), in the same order
+// per event, so an event's sum does not depend on the events served with it.
+// The two forms are compiled apart, and the code generator may fuse their
+// FP32 multiply-adds differently.
 __host__ __device__ inline int cta_floats(int nel, int kc) {
   return 4 + kc * ((kItemsPerElement + 4) * nel + 4);
 }
