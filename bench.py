@@ -383,10 +383,10 @@ def setup_c4(dp, torch, dev, precision="mixed", scale=1.0):
             # per history: contribution and status written and read back,
             # CSDA contribution and derivative written and read back
             "alg_bytes": total * (24 + 32),
-            # DRAM bytes of one mc_mixed_hi launch from an ncu capture of 819 of
-            # the lines of sight (1.71 GB for 443,846 histories, mostly
+            # DRAM bytes of one mc_mixed_hi launch from an ncu capture of a tenth
+            # of the lines of sight (3.50 GB for 882,273 histories, mostly
             # local-memory write-back), scaled by the histories
-            "traffic": int(3860 * total) if precision == "mixed" else None,
+            "traffic": int(3966 * total) if precision == "mixed" else None,
             "note": "SM-issue bound, not HBM: ncu smsp__issue_active 38.6% (mixed transport, "
                     "lockstep)",
             "config": {"workload": "c4: 16384 vertical lines of sight, depth log-uniform 50-2000 m, "
@@ -520,8 +520,8 @@ def setup_dir(dp, torch, dev, precision="mixed", scale=1.0):
             # per history: contribution and status written and read back
             "alg_bytes": batch.total * 24,
             # DRAM bytes of one dir_mixed_hi launch from an ncu capture of a tenth
-            # of the directions (2.42 GB for 418,816 histories), scaled by the histories
-            "traffic": int(5776 * batch.total) if precision == "mixed" else None,
+            # of the directions (3.49 GB for 418,816 histories), scaled by the histories
+            "traffic": int(8327 * batch.total) if precision == "mixed" else None,
             "note": "SM-issue bound (one thread per history, table lookups in shared memory)",
             "config": {"workload": "dir: fixed-path MC (compute_directional_flux_mc), 4096 "
                                    "directions x 1024 histories, 32x32x16 cells @ 20 m of rock / "
