@@ -31,6 +31,43 @@ DP_HD double gl12(int i, bool weight) {
   return weight ? w[i] : x[i];
 }
 
+// The same nodes and weights for the FP32 terms: each entry is the float of
+// the FP64 entry.  On the device they are read from a global table: a
+// runtime index into the FP64 tables and a conversion per term ran on the
+// FP64 pipe, which runs at 1/64 of the FP32 rate here.
+__device__ const float kGl9f[18] = {
+    float(0.015919880246186957), float(0.08198444633668206), float(0.19331428364970477),
+    float(0.33787328829809554), float(0.5), float(0.66212671170190451),
+    float(0.80668571635029518), float(0.91801555366331788), float(0.98408011975381304),
+    float(0.040637194180787317), float(0.090324080347428781), float(0.13030534820146777),
+    float(0.15617353852000146), float(0.16511967750062989), float(0.15617353852000146),
+    float(0.13030534820146777), float(0.090324080347428781), float(0.040637194180787317),
+};
+__device__ const float kGl12f[24] = {
+    float(0.0092196828766403782), float(0.047941371814762601), float(0.11504866290284765),
+    float(0.20634102285669126), float(0.31608425050090994), float(0.43738329574426554),
+    float(0.5626167042557344), float(0.68391574949909006), float(0.79365897714330869),
+    float(0.88495133709715235), float(0.95205862818523745), float(0.99078031712335957),
+    float(0.023587668193255917), float(0.053469662997659088), float(0.080039164271673166),
+    float(0.10158371336153292), float(0.11674626826917739), float(0.12457352290670144),
+    float(0.12457352290670144), float(0.11674626826917739), float(0.10158371336153292),
+    float(0.080039164271673166), float(0.053469662997659088), float(0.023587668193255917),
+};
+template <class T>
+DP_HD T gl9_t(int i, bool weight) {
+#ifdef __CUDA_ARCH__
+  if constexpr (sizeof(T) == 4) return kGl9f[(weight ? 9 : 0) + i];
+#endif
+  return T(gl9(i, weight));
+}
+template <class T>
+DP_HD T gl12_t(int i, bool weight) {
+#ifdef __CUDA_ARCH__
+  if constexpr (sizeof(T) == 4) return kGl12f[(weight ? 12 : 0) + i];
+#endif
+  return T(gl12(i, weight));
+}
+
 // Real dilogarithm for x <= 1 (Bernoulli series in -log(1-x) plus the
 // reflection Li2(x) = pi^2/6 - log x log(1-x) - Li2(1-x)).  The DCS only
 // evaluates it on (0, 1).
@@ -43,6 +80,7 @@ DP_HD T li2_bernoulli(T x) {
                         1.0 / 526901760.0, -4.064761645144225e-11, 8.921691020456453e-13,
                         -1.9939295860721077e-14, 4.5189800296199183e-16, -1.0356517612181247e-17};
   T s = T(0), p = u * u2;
+#pragma unroll  // the coefficients fold to constants of T (no FP64 conversion per term)
   for (int k = 0; k < 10; ++k) {
     s += T(c[k]) * p;
     p *= u2;
@@ -212,8 +250,8 @@ DP_HD bool pair_range(T Z, T A, T mass, T K, T q, T* tmin) {
 }
 template <class T>
 DP_HD T pair_point(T Z, T A, T mass, T K, T q, T tmin, int i, T scale = T(1)) {
-  T r = exp(T(gl12(i, false)) * tmin);
-  return pair_d2(Z, A, mass, K, q, r, scale) * r * T(gl12(i, true)) * tmin;
+  T r = exp(gl12_t<T>(i, false) * tmin);
+  return pair_d2(Z, A, mass, K, q, r, scale) * r * gl12_t<T>(i, true) * tmin;
 }
 template <class T>
 DP_HD T dcs_pair(T Z, T A, T mass, T K, T q, T scale = T(1)) {
@@ -273,9 +311,9 @@ DP_HD bool photo_range(T Z, T A, T m, T K, T q, T* lmin, T* dx) {
 }
 template <class T>
 DP_HD T photo_point(T Z, T A, T m, T K, T q, T lmin, T dx, int i, T scale = T(1)) {
-  T Q2 = exp(lmin + dx * T(gl9(i, false)));
+  T Q2 = exp(lmin + dx * gl9_t<T>(i, false));
   T v = photo_d2(Z, A, m, K, q, Q2, scale);
-  return v > T(0) ? v * (T(gl9(i, true)) * dx * Q2) : T(0);
+  return v > T(0) ? v * (gl9_t<T>(i, true) * dx * Q2) : T(0);
 }
 template <class T>
 DP_HD T dcs_photo(T Z, T A, T m, T K, T q, T scale = T(1)) {
