@@ -218,7 +218,7 @@ C2_MIX = ([1, 3, 2], [0.70, 0.25, 0.05])  # rock, water, air (1-based material i
 # cases of the same kernels (the bound that binds them: instruction issue)
 # Issue-slot figures of the dominant kernels, from the ncu captures of the
 # same builds (reduced cases of each workload; the launch tails weigh more there)
-C2_ISSUE = {"issue_active": 0.4306, "lanes_per_inst": 18.38,
+C2_ISSUE = {"issue_active": 0.4391, "lanes_per_inst": 18.17,
             "source": "ncu smsp__issue_active and smsp__thread_inst_executed_per_inst_executed, "
                       "mc_kernel<float,0,1024> (phase 0, lockstep, tables through L1/L2) on a "
                       "5e5-history c2 case"}
@@ -285,13 +285,12 @@ def setup_c2(dp, torch, dev, precision="mixed", scale=1.0):
             # transport kernel and read back by the tally
             "alg_bytes": n * 24,
             # DRAM bytes (read + write) of one phase-0 launch from an ncu capture
-            # at 5e5 histories (1.45 GB, almost all the write-back of the spilled
-            # stacks), scaled by the histories
-            "traffic": int(2899 * n) if precision == "mixed" else None,
-            "note": "SM-issue bound, not HBM: ncu smsp__issue_active 43.1% (phase 0, a "
-                    "5e5-history case) with 18.4 of 32 lanes per instruction; DRAM traffic "
-                    "(mostly local-memory write-back of the spilled stack) is about 1% of the "
-                    "bandwidth",
+            # at 5e5 histories (303 MB: records and the spilled stacks' write-back),
+            # scaled by the histories
+            "traffic": int(605 * n) if precision == "mixed" else None,
+            "note": "SM-issue bound, not HBM: ncu smsp__issue_active 43.9% (phase 0, a "
+                    "5e5-history case) with 18.2 of 32 lanes per instruction; DRAM traffic "
+                    "is under 0.3% of the bandwidth",
             "config": {"workload": "c2: straggled MC with DEL/EHS + Coulomb scattering, rock mixture "
                                    "rock/water/air 0.70/0.25/0.05 (per-history thickness U[20,500] m, "
                                    "density U[2000,2800], elevation U[30,90] deg) under 1 km air, "
@@ -384,9 +383,9 @@ def setup_c4(dp, torch, dev, precision="mixed", scale=1.0):
             # CSDA contribution and derivative written and read back
             "alg_bytes": total * (24 + 32),
             # DRAM bytes of one mc_mixed_hi launch from an ncu capture of a tenth
-            # of the lines of sight (3.50 GB for 882,273 histories, mostly
-            # local-memory write-back), scaled by the histories
-            "traffic": int(3966 * total) if precision == "mixed" else None,
+            # of the lines of sight (562 MB for 882,273 histories), scaled by the
+            # histories
+            "traffic": int(637 * total) if precision == "mixed" else None,
             "note": "SM-issue bound, not HBM: ncu smsp__issue_active 38.6% (mixed transport, "
                     "lockstep)",
             "config": {"workload": "c4: 16384 vertical lines of sight, depth log-uniform 50-2000 m, "
@@ -520,8 +519,8 @@ def setup_dir(dp, torch, dev, precision="mixed", scale=1.0):
             # per history: contribution and status written and read back
             "alg_bytes": batch.total * 24,
             # DRAM bytes of one dir_mixed_hi launch from an ncu capture of a tenth
-            # of the directions (3.49 GB for 418,816 histories), scaled by the histories
-            "traffic": int(8327 * batch.total) if precision == "mixed" else None,
+            # of the directions (611 MB for 418,816 histories), scaled by the histories
+            "traffic": int(1458 * batch.total) if precision == "mixed" else None,
             "note": "SM-issue bound (one thread per history, table lookups in shared memory)",
             "config": {"workload": "dir: fixed-path MC (compute_directional_flux_mc), 4096 "
                                    "directions x 1024 histories, 32x32x16 cells @ 20 m of rock / "
