@@ -9,32 +9,29 @@
 
 namespace dp {
 
-// Gauss-Legendre nodes/weights on [0, 1] (computed by Newton iteration).
-DP_HD double gl9(int i, bool weight) {
-  const double x[9] = {0.015919880246186957, 0.08198444633668206, 0.19331428364970477,
-                       0.33787328829809554,  0.5,                 0.66212671170190451,
-                       0.80668571635029518,  0.91801555366331788, 0.98408011975381304};
-  const double w[9] = {0.040637194180787317, 0.090324080347428781, 0.13030534820146777,
-                       0.15617353852000146,  0.16511967750062989,  0.15617353852000146,
-                       0.13030534820146777,  0.090324080347428781, 0.040637194180787317};
-  return weight ? w[i] : x[i];
-}
-DP_HD double gl12(int i, bool weight) {
-  const double x[12] = {0.0092196828766403782, 0.047941371814762601, 0.11504866290284765,
-                        0.20634102285669126,   0.31608425050090994,  0.43738329574426554,
-                        0.5626167042557344,    0.68391574949909006,  0.79365897714330869,
-                        0.88495133709715235,   0.95205862818523745,  0.99078031712335957};
-  const double w[12] = {0.023587668193255917, 0.053469662997659088, 0.080039164271673166,
-                        0.10158371336153292,  0.11674626826917739,  0.12457352290670144,
-                        0.12457352290670144,  0.11674626826917739,  0.10158371336153292,
-                        0.080039164271673166, 0.053469662997659088, 0.023587668193255917};
-  return weight ? w[i] : x[i];
-}
-
-// The same nodes and weights for the FP32 terms: each entry is the float of
-// the FP64 entry.  On the device they are read from a global table: a
-// runtime index into the FP64 tables and a conversion per term ran on the
-// FP64 pipe, which runs at 1/64 of the FP32 rate here.
+// Gauss-Legendre nodes/weights on [0, 1] (computed by Newton iteration): 9
+// nodes then 9 weights, 12 nodes then 12 weights.  On the device the terms
+// read them from global tables; a function-local table indexed at run time
+// is built in each thread's local memory at every call.  The FP32 tables hold
+// the float of each FP64 entry.
+#define DP_GL9 \
+    0.015919880246186957, 0.08198444633668206, 0.19331428364970477, \
+    0.33787328829809554, 0.5, 0.66212671170190451, \
+    0.80668571635029518, 0.91801555366331788, 0.98408011975381304, \
+    0.040637194180787317, 0.090324080347428781, 0.13030534820146777, \
+    0.15617353852000146, 0.16511967750062989, 0.15617353852000146, \
+    0.13030534820146777, 0.090324080347428781, 0.040637194180787317
+#define DP_GL12 \
+    0.0092196828766403782, 0.047941371814762601, 0.11504866290284765, \
+    0.20634102285669126, 0.31608425050090994, 0.43738329574426554, \
+    0.5626167042557344, 0.68391574949909006, 0.79365897714330869, \
+    0.88495133709715235, 0.95205862818523745, 0.99078031712335957, \
+    0.023587668193255917, 0.053469662997659088, 0.080039164271673166, \
+    0.10158371336153292, 0.11674626826917739, 0.12457352290670144, \
+    0.12457352290670144, 0.11674626826917739, 0.10158371336153292, \
+    0.080039164271673166, 0.053469662997659088, 0.023587668193255917
+__device__ const double kGl9d[18] = {DP_GL9};
+__device__ const double kGl12d[24] = {DP_GL12};
 __device__ const float kGl9f[18] = {
     float(0.015919880246186957), float(0.08198444633668206), float(0.19331428364970477),
     float(0.33787328829809554), float(0.5), float(0.66212671170190451),
@@ -53,6 +50,24 @@ __device__ const float kGl12f[24] = {
     float(0.12457352290670144), float(0.11674626826917739), float(0.10158371336153292),
     float(0.080039164271673166), float(0.053469662997659088), float(0.023587668193255917),
 };
+DP_HD double gl9(int i, bool weight) {
+#ifdef __CUDA_ARCH__
+  return kGl9d[(weight ? 9 : 0) + i];
+#else
+  static const double t[18] = {DP_GL9};
+  return t[(weight ? 9 : 0) + i];
+#endif
+}
+DP_HD double gl12(int i, bool weight) {
+#ifdef __CUDA_ARCH__
+  return kGl12d[(weight ? 12 : 0) + i];
+#else
+  static const double t[24] = {DP_GL12};
+  return t[(weight ? 12 : 0) + i];
+#endif
+}
+#undef DP_GL9
+#undef DP_GL12
 template <class T>
 DP_HD T gl9_t(int i, bool weight) {
 #ifdef __CUDA_ARCH__
